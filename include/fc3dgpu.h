@@ -1,0 +1,161 @@
+/* fc3dgpu: GB300 (sm_103a) coloured NSGS for the 3D Coulomb friction-contact
+ * problem, as a drop-in solver beside the reference's
+ * SICONOS_FRICTION_3D_NSGS.
+ *
+ * The entry points below are what the reference's solver registry binds
+ * (solver_registry.h:75-95): a solve function with the registry's
+ * SolverSolveFunc signature and a set_default function.  Host code is C;
+ * the CUDA work sits behind the device-resident API at the end of this
+ * header.  All buffers in the solver-level calls are HOST memory owned by the
+ * caller, exactly as for the reference solver.
+ *
+ * Error behaviour follows the reference: the solve returns 0 on
+ * convergence, 1 when not converged, NUMERICS_ERR_MAX_ITER (-20) when the
+ * iteration budget ran out, and a negative NUMERICS_ERR_* code for invalid
+ * input.  There is no CPU fallback: without a usable CUDA device the solve
+ * returns NUMERICS_ERR_NOT_IMPLEMENTED and fc3dgpu_last_error() says why.
+ */
+#ifndef FC3DGPU_H
+#define FC3DGPU_H
+
+#ifdef FC3DGPU_USE_SICONOS_HEADERS
+#include "FrictionContactProblem.h"
+#include "SolverOptions.h"
+#include "numerics_errors.h"
+#else
+#include "siconos_numerics_abi.h"
+#endif
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* New solver id in the free FC3D range (FrictionContact_options.h:83-131
+ * uses 500-530; the driver accepts 500-599, fc3d_driver.c:212). */
+#define SICONOS_FRICTION_3D_NSGS_GPU 531
+
+/* GPU knobs live in option slots the NSGS solver does not use.  dparam
+ * 20-22 keep the reference's timing meaning (SolverOptions.h:118-120). */
+#define FC3DGPU_IPARAM_PRECISION 23   /* in: 0 FP32 sweeps + FP64 polish (default), 1 FP64 sweeps only */
+#define FC3DGPU_IPARAM_LANES 24       /* in: lanes per contact 1, 2, 4, 8; 0 = autotune (default) */
+#define FC3DGPU_IPARAM_WARMSTART 25   /* in: 0 = reaction on entry (default), 1 = learned proposal */
+#define FC3DGPU_IPARAM_COLOURING 26   /* in: 0 = hash priority (default), 1 = largest degree first */
+#define FC3DGPU_IPARAM_SWEEPS_FP32 27 /* out: FP32 sweeps done */
+#define FC3DGPU_IPARAM_SWEEPS_FP64 28 /* out: FP64 sweeps done */
+#define FC3DGPU_IPARAM_COLOURS 29     /* out: number of colours */
+#define FC3DGPU_DPARAM_SWITCH_TOL 23  /* in: FP32 -> FP64 switch on the incremental error (default 1e-6) */
+#define FC3DGPU_DPARAM_LOCAL_TOL32 24 /* in: FP32 local Newton tolerance (default 1e-6) */
+#define FC3DGPU_DPARAM_STALL 25       /* in: FP32 stall window in sweeps (default 64) */
+#define FC3DGPU_DPARAM_MS_SWEEP32 26  /* out: mean device time of one FP32 sweep (ms) */
+#define FC3DGPU_DPARAM_MS_SWEEP64 27  /* out: mean device time of one FP64 sweep (ms) */
+#define FC3DGPU_DPARAM_MS_SOLVE 28    /* out: device time of the whole solve (ms) */
+#define FC3DGPU_DPARAM_INCR_ERROR 29  /* out: last incremental error */
+
+/* Registry-facing solver functions.  fc3dgpu_nsgs has the signature of
+ * fc3d_nsgs's wrapper (fc3d_nsgs.c:968): problem, reaction (in: warm start,
+ * out: solution), velocity (out: W r + q), options. */
+int fc3dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velocity, SolverOptions *options);
+int fc3dgpu_nsgs_solve_wrap(void *problem, double *reaction, double *velocity, SolverOptions *options);
+int fc3dgpu_nsgs_init_wrap(void *problem, SolverOptions *options);
+void fc3dgpu_nsgs_free_wrap(void *problem, SolverOptions *options);
+
+/* fc3d_driver (fc3d_driver.c:77-145) restricted to this solver id:
+ * validation, trivial take-off case (r = 0, u = q when every q_n >=
+ * -DBL_EPSILON), then fc3dgpu_nsgs.  Inside Siconos the reference's own
+ * fc3d_driver plays this part once the solver is registered. */
+int fc3dgpu_driver(FrictionContactProblem *problem, double *reaction, double *velocity, SolverOptions *options);
+
+/* Defaults of fc3d_nsgs_set_default (fc3d_nsgs.c:919-950) -- LIGHT_WITH_FULL_FINAL,
+ * GIVEN_VALUE local tolerance, no shuffle/freezing/filter/relaxation, tol
+ * 1e-4, one internal OC_NSN_GP_HYBRID solver with the one-contact defaults
+ * (onecontact.c:1037-1056: 100 Newton iterations, tol 1e-14, GP line search
+ * of 10, NSN_AND_PLI_NSN_LOOP, one loop, 100 PLI iterations) -- plus the GPU
+ * knobs above.  Internal solver options are allocated with calloc, like
+ * solver_options_create, when options has none. */
+void fc3dgpu_nsgs_set_default(SolverOptions *options);
+
+/* Stand-alone options (what solver_options_create(SICONOS_FRICTION_3D_NSGS_GPU)
+ * returns once the solver is registered): max_iter 1000, tol 1e-4. */
+SolverOptions *fc3dgpu_options_create(void);
+void fc3dgpu_options_delete(SolverOptions *options);
+
+/* Release the device copy of W cached in options->solverData. */
+void fc3dgpu_release(SolverOptions *options);
+
+/* fc3d_compute_error (fc3d_compute_error.c:70-122) on the GPU in FP64:
+ * velocity <- W reaction + q, *error = relative natural-map error.
+ * Returns 0 when error <= tolerance, 1 otherwise, <0 on failure. */
+int fc3dgpu_compute_error(FrictionContactProblem *problem, double *reaction, double *velocity, double tolerance,
+                          double norm_q, double *error);
+
+/* Many independent problems in one persistent launch (uneven sizes).  Each
+ * problem uses the options' tolerance and budget; info[k] per problem. */
+int fc3dgpu_nsgs_batch(int nproblems, FrictionContactProblem **problems, double **reactions, double **velocities,
+                       SolverOptions *options, int *info);
+
+/* Device colouring of the contact conflict graph of a block-CSR structure
+ * (two contacts conflict when W has a block between them).  Greedy in
+ * decreasing priority, computed in Jones-Plassmann rounds on the GPU.
+ * Returns the number of colours, <0 on failure. */
+int fc3dgpu_colour(int nc, const int64_t *rowptr, const int64_t *colidx, int kind, int32_t *colour);
+
+/* Last error message of this thread ("" when none). */
+const char *fc3dgpu_last_error(void);
+
+/* ------------------------------------------------------------------
+ * Device-resident API: a problem uploaded once and solved many times with
+ * inputs already in HBM (time stepping, benchmarks).
+ * ------------------------------------------------------------------ */
+typedef struct fc3dgpu_ctx fc3dgpu_ctx;
+
+typedef struct {
+  double tol;          /* user tolerance on fc3d_compute_error */
+  int max_iter;        /* total sweep budget */
+  int precision;       /* 0 mixed (FP32 sweeps + FP64 polish), 1 FP64 only */
+  int lanes;           /* lanes per contact (1,2,4,8); 0 = autotune */
+  double switch_tol;   /* FP32 phase ends when incr error < switch_tol ... */
+  int stall_window;    /* ... or has not improved for this many sweeps */
+  double local_tol;    /* FP64 local solver tolerance (1e-14) */
+  double local_tol32;  /* FP32 local solver tolerance */
+  int newton_max;      /* 100 */
+  int pli_max;         /* 100 */
+  int ls_max;          /* 10 */
+  int fp32_only;       /* 1: run FP32 sweeps only, for throughput runs */
+} fc3dgpu_params;
+
+typedef struct {
+  int info;            /* as the solver's return value */
+  int status;          /* device status word; 0 = ok, else a FC3DGPU_STATUS_* bit */
+  int sweeps32, sweeps64;
+  int colours, lanes, grid;
+  double incr_error;   /* last incremental error */
+  double error;        /* final fc3d_compute_error (FP64) */
+  double ms_total;     /* device time of the solve (CUDA events) */
+  double ms_fp32, ms_fp64;
+  double bytes_sweep32, bytes_sweep64; /* algorithmic bytes per sweep */
+} fc3dgpu_stats;
+
+#define FC3DGPU_STATUS_BARRIER_TIMEOUT 1
+#define FC3DGPU_STATUS_NONFINITE 2
+
+void fc3dgpu_params_default(fc3dgpu_params *p);
+fc3dgpu_ctx *fc3dgpu_ctx_create(int device);
+void fc3dgpu_ctx_destroy(fc3dgpu_ctx *ctx);
+/* Upload W as block-CSR (blocks: 9 doubles per block, column-major) and
+ * build the coloured device layout. */
+int fc3dgpu_ctx_set_W(fc3dgpu_ctx *ctx, int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                      int colour_kind);
+int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx *ctx, const double *q, const double *mu);
+int fc3dgpu_ctx_set_r(fc3dgpu_ctx *ctx, const double *r);
+int fc3dgpu_ctx_solve(fc3dgpu_ctx *ctx, const fc3dgpu_params *p, fc3dgpu_stats *st);
+int fc3dgpu_ctx_get_r_u(fc3dgpu_ctx *ctx, double *r, double *u);
+int fc3dgpu_ctx_compute_error(fc3dgpu_ctx *ctx, double *error);
+/* Per-sweep incremental error trace of the last solve (FP32 then FP64). */
+int fc3dgpu_ctx_trace(fc3dgpu_ctx *ctx, double *out, int cap);
+int fc3dgpu_ctx_colours(fc3dgpu_ctx *ctx, int32_t *colour);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

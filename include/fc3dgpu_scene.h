@@ -1,0 +1,60 @@
+/* Seeded sphere-lattice friction-contact scenes.
+ *
+ * The reference ships no generator for its benchmark scenes; this one builds
+ * the workload the benchmarks are quoted on: X*Y*Z rigid spheres (radius
+ * 0.5, mass 1, inertia 0.1*I3) on a cubic lattice of spacing 1.0, centres at
+ * (i, j, k + 0.5) jittered by N(0, jitter_std^2) per coordinate, contacts
+ * between face-neighbour spheres plus a ground plane under the bottom layer.
+ * Each contact's frame has the normal along the centre-to-centre line (ground:
+ * +z) and Gram-Schmidt tangents.  W = H M^-1 H^T is assembled in FP64 as 3x3
+ * column-major blocks in block-CSR order (the SparseBlockStructuredMatrix
+ * layout of the reference, SparseBlockMatrix.h:82-121), and
+ * q = H (v0 + h g) with v0 ~ N(0, v0_std^2) per degree of freedom.
+ *
+ * Random numbers come from splitmix64 and the Marsaglia polar method with a
+ * logarithm written from its series definition, built with
+ * -ffp-contract=off, so a seed gives the same scene bit for bit on x86-64
+ * and aarch64.
+ */
+#ifndef FC3DGPU_SCENE_H
+#define FC3DGPU_SCENE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fc3dgpu_lattice fc3dgpu_lattice;
+
+/* Create the scene geometry and the initial velocities.  Returns NULL on a
+ * bad size (any dimension < 1) or allocation failure. */
+fc3dgpu_lattice *fc3dgpu_lattice_create(int nx, int ny, int nz, uint64_t seed, double jitter_std, double v0_std);
+void fc3dgpu_lattice_free(fc3dgpu_lattice *L);
+
+/* Number of bodies, contacts and 3x3 blocks (diagonal included) of W. */
+int fc3dgpu_lattice_sizes(const fc3dgpu_lattice *L, int *nbodies, int *ncontacts, int64_t *nnzb);
+
+/* Fill W in block-CSR: rowptr[nc+1], colidx[nnzb] (sorted per row),
+ * blocks[9*nnzb] column-major.  Returns 0. */
+int fc3dgpu_lattice_fill_W(const fc3dgpu_lattice *L, int64_t *rowptr, int64_t *colidx, double *blocks);
+
+/* q = H (v + h g) for the current body velocities; g = -9.81 e_z. */
+int fc3dgpu_lattice_fill_q(const fc3dgpu_lattice *L, double h, double *q);
+
+/* Per-contact normal gap (centre distance minus radii; ground: height minus
+ * radius) and contact bodies (A = -1 for the ground; B > A). */
+int fc3dgpu_lattice_fill_geometry(const fc3dgpu_lattice *L, double *gap, int32_t *bodyA, int32_t *bodyB);
+
+/* Random walk of the body velocities: v += N(0, std^2) per degree of
+ * freedom, from its own stream seeded by seed. */
+int fc3dgpu_lattice_perturb_velocities(fc3dgpu_lattice *L, uint64_t seed, double std);
+
+/* Standard normal samples from the generator's own stream (exposed for
+ * tests of the sampler). */
+void fc3dgpu_normal_fill(uint64_t seed, double *out, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

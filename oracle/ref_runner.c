@@ -1,0 +1,216 @@
+/* Array-in/array-out wrappers around the reference's own numerics entry
+ * points, compiled into oracle/_ref by oracle/build_ref.py.  Test
+ * infrastructure only: these let Python tests and the golden-fixture script
+ * run the unmodified reference fc3d_driver (SICONOS_FRICTION_3D_NSGS,
+ * fc3d_nsgs.c:560) and fc3d_compute_error (fc3d_compute_error.c:70) on
+ * problems given as block-CSR arrays, and read the reference's .dat
+ * fixtures with its own reader (FrictionContactProblem.c:103). */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "FrictionContactProblem.h"
+#include "FrictionContact_options.h"
+#include "NonSmoothDrivers.h"
+#include "NumericsMatrix.h"
+#include "SolverOptions.h"
+#include "SparseBlockMatrix.h"
+#include "fc3d_Solvers.h"
+#include "fc3d_compute_error.h"
+#include "numerics_verbose.h"
+#include "op3x3.h"
+#include "projectionOnCone.h"
+
+/* Build a 3x3-block SBM that points into caller-owned arrays.  blocks holds
+ * nnzb column-major 3x3 blocks in row order, rowptr/colidx the block-CSR
+ * structure. */
+static NumericsMatrix *make_sbm(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks) {
+  SparseBlockStructuredMatrix *m = SBM_new();
+  size_t nnzb = (size_t)rowptr[nc];
+  m->nbblocks = nnzb;
+  m->blocknumber0 = (size_t)nc;
+  m->blocknumber1 = (size_t)nc;
+  m->blocksize0 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
+  m->blocksize1 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
+  for (int i = 0; i < nc; i++) m->blocksize0[i] = m->blocksize1[i] = 3 * (size_t)(i + 1);
+  m->filled1 = (size_t)nc + 1;
+  m->filled2 = nnzb;
+  m->index1_data = (size_t *)malloc(sizeof(size_t) * ((size_t)nc + 1));
+  m->index2_data = (size_t *)malloc(sizeof(size_t) * (nnzb ? nnzb : 1));
+  m->block = (double **)malloc(sizeof(double *) * (nnzb ? nnzb : 1));
+  for (int i = 0; i <= nc; i++) m->index1_data[i] = (size_t)rowptr[i];
+  for (size_t k = 0; k < nnzb; k++) {
+    m->index2_data[k] = (size_t)colidx[k];
+    m->block[k] = (double *)&blocks[9 * k];
+  }
+  return NM_create_from_data(NM_SPARSE_BLOCK, 3 * nc, 3 * nc, m);
+}
+
+static void free_sbm(NumericsMatrix *M) {
+  SparseBlockStructuredMatrix *m = M->matrix1;
+  free(m->blocksize0);
+  free(m->blocksize1);
+  free(m->index1_data);
+  free(m->index2_data);
+  free(m->block);
+  free(m->diagonal_blocks);
+  free(m);
+  M->matrix1 = NULL;
+  if (M->internalData) {
+    free(M->internalData->iWork);
+    free(M->internalData->dWork);
+    free(M->internalData);
+  }
+  free(M);
+}
+
+typedef struct {
+  double *buf;
+  int cap;
+  int len;
+} Trace;
+
+static void trace_cb(void *env, size_t size, double *reaction, double *velocity, double error, void *extra) {
+  (void)size;
+  (void)reaction;
+  (void)velocity;
+  (void)extra;
+  Trace *t = (Trace *)env;
+  if (t->len < t->cap) t->buf[t->len] = error;
+  t->len++;
+}
+
+/* Run the reference's fc3d_driver with SICONOS_FRICTION_3D_NSGS default
+ * options (solver_options_create) and the given tolerance and iteration
+ * cap.  r holds the warm start on entry.  trace (optional) receives the
+ * per-iteration error the reference reports through its callback. */
+int ref_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
+                  const double *mu, double *r, double *u, double tol, int maxiter, int *iters, double *err,
+                  double *trace, int trace_cap, int *trace_len) {
+  NumericsMatrix *M = make_sbm(nc, rowptr, colidx, blocks);
+  FrictionContactProblem P;
+  memset(&P, 0, sizeof(P));
+  P.dimension = 3;
+  P.numberOfContacts = nc;
+  P.M = M;
+  P.q = (double *)q;
+  P.mu = (double *)mu;
+  SolverOptions *opt = solver_options_create(SICONOS_FRICTION_3D_NSGS);
+  opt->iparam[SICONOS_IPARAM_MAX_ITER] = maxiter;
+  opt->dparam[SICONOS_DPARAM_TOL] = tol;
+  Trace t = {trace, trace_cap, 0};
+  Callback cb = {&t, trace_cb};
+  if (trace) opt->callback = &cb;
+  int info = fc3d_driver(&P, r, u, opt);
+  if (iters) *iters = opt->iparam[SICONOS_IPARAM_ITER_DONE];
+  if (err) *err = opt->dparam[SICONOS_DPARAM_RESIDU];
+  if (trace_len) *trace_len = t.len;
+  opt->callback = NULL;
+  solver_options_delete(opt);
+  free_sbm(M);
+  return info;
+}
+
+/* The reference's fc3d_compute_error on the given r; u receives q + W r. */
+double ref_fc3d_compute_error(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                              const double *q, const double *mu, const double *r, double *u) {
+  NumericsMatrix *M = make_sbm(nc, rowptr, colidx, blocks);
+  FrictionContactProblem P;
+  memset(&P, 0, sizeof(P));
+  P.dimension = 3;
+  P.numberOfContacts = nc;
+  P.M = M;
+  P.q = (double *)q;
+  P.mu = (double *)mu;
+  double norm_q = cblas_dnrm2(3 * nc, q, 1);
+  double e = 0.0;
+  fc3d_compute_error(&P, (double *)r, u, 1e-300, NULL, norm_q, &e);
+  free_sbm(M);
+  return e;
+}
+
+/* .dat fixtures through the reference's own reader. */
+typedef struct {
+  FrictionContactProblem *P;
+} DatHandle;
+
+void *ref_dat_open(const char *fname, int *nc, int64_t *nnzb, int *storage) {
+  FrictionContactProblem *P = frictionContact_new_from_filename(fname);
+  if (!P) return NULL;
+  DatHandle *h = (DatHandle *)malloc(sizeof(DatHandle));
+  h->P = P;
+  *nc = P->numberOfContacts;
+  *storage = (int)P->M->storageType;
+  if (P->M->storageType == NM_SPARSE_BLOCK)
+    *nnzb = (int64_t)P->M->matrix1->nbblocks;
+  else if (P->M->storageType == NM_DENSE) {
+    /* dense: every 3x3 block with a nonzero entry becomes a block */
+    int n = P->numberOfContacts;
+    int64_t cnt = 0;
+    for (int bi = 0; bi < n; bi++)
+      for (int bj = 0; bj < n; bj++) {
+        int nz = (bi == bj);
+        for (int a = 0; a < 3 && !nz; a++)
+          for (int b = 0; b < 3 && !nz; b++)
+            nz = P->M->matrix0[(size_t)(3 * bj + b) * (size_t)(3 * n) + (size_t)(3 * bi + a)] != 0.0;
+        cnt += nz;
+      }
+    *nnzb = cnt;
+  } else
+    *nnzb = -1;
+  return h;
+}
+
+int ref_dat_get(void *hv, int64_t *rowptr, int64_t *colidx, double *blocks, double *q, double *mu) {
+  DatHandle *h = (DatHandle *)hv;
+  FrictionContactProblem *P = h->P;
+  int n = P->numberOfContacts;
+  memcpy(q, P->q, sizeof(double) * 3 * (size_t)n);
+  memcpy(mu, P->mu, sizeof(double) * (size_t)n);
+  if (P->M->storageType == NM_SPARSE_BLOCK) {
+    SparseBlockStructuredMatrix *m = P->M->matrix1;
+    if (m->filled1 != (size_t)n + 1) {
+      /* trailing empty rows: pad the row pointer */
+      for (int i = 0; i <= n; i++) rowptr[i] = (int64_t)(i < (int)m->filled1 ? m->index1_data[i] : m->index1_data[m->filled1 - 1]);
+    } else
+      for (int i = 0; i <= n; i++) rowptr[i] = (int64_t)m->index1_data[i];
+    for (size_t k = 0; k < m->nbblocks; k++) {
+      colidx[k] = (int64_t)m->index2_data[k];
+      memcpy(&blocks[9 * k], m->block[k], 9 * sizeof(double));
+    }
+    return 0;
+  }
+  if (P->M->storageType == NM_DENSE) {
+    int64_t k = 0;
+    const double *A = P->M->matrix0;
+    for (int bi = 0; bi < n; bi++) {
+      rowptr[bi] = k;
+      for (int bj = 0; bj < n; bj++) {
+        int nz = (bi == bj);
+        for (int a = 0; a < 3 && !nz; a++)
+          for (int b = 0; b < 3 && !nz; b++) nz = A[(size_t)(3 * bj + b) * (size_t)(3 * n) + (size_t)(3 * bi + a)] != 0.0;
+        if (!nz) continue;
+        colidx[k] = bj;
+        for (int b = 0; b < 3; b++)
+          for (int a = 0; a < 3; a++)
+            blocks[9 * k + 3 * b + a] = A[(size_t)(3 * bj + b) * (size_t)(3 * n) + (size_t)(3 * bi + a)];
+        k++;
+      }
+    }
+    rowptr[n] = k;
+    return 0;
+  }
+  return -1;
+}
+
+void ref_dat_close(void *hv) {
+  DatHandle *h = (DatHandle *)hv;
+  frictionContactProblem_free(h->P);
+  free(h);
+}
+
+/* Exported wrappers around static inline helpers of op3x3.h and the
+ * reference's cone projection, for known-answer tests. */
+int ref_solve_3x3_gepp(const double *a, double *b) { return solve_3x3_gepp(a, b); }
+unsigned ref_projection_on_cone(double *r, double mu) { return projectionOnCone(r, mu); }
+void ref_set_verbose(int v) { numerics_set_verbose(v); }

@@ -1,0 +1,1003 @@
+// Device-side set-up of a problem: Jones-Plassmann colouring of the contact
+// conflict graph, stable permutation of the rows by colour into 32-row slabs,
+// and the slot-major block layout (fc3dgpu_layout.cuh).  Everything here runs
+// once per W; the sweeps never touch the block-CSR input again.
+//
+// Colouring.  The reference colours the conflict graph with PETSc's greedy
+// distance-1 colouring (tools/parallel/graph_tools.c:876-928).  Here every
+// contact gets a 32-bit priority (an integer hash of its index, optionally
+// led by its conflict degree); a contact is coloured once all its
+// higher-priority neighbours are, with the smallest colour none of them
+// holds.  That equals sequential greedy colouring in decreasing priority, so
+// the result is deterministic and matches the host greedy colouring of the
+// same graph.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fc3dgpu_sweep_launch.h"
+#include "fc3dgpu_layout.cuh"
+#include "fc3dgpu_local.cuh"
+
+namespace fc3dgpu {
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  // lowbias32 (C. Wellons)
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t colour_priority(uint32_t index, int kind, uint32_t degree) {
+  uint32_t h = hash32(index ^ 0x9e3779b9U);
+  if (kind == 1) return ((degree > 255 ? 255U : degree) << 24) | (h >> 8);
+  return h;
+}
+
+__global__ void k_degree(int nc, const long long* __restrict__ rowptr, const long long* __restrict__ colidx,
+                         int* __restrict__ deg) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
+    for (long long k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      long long j = colidx[k];
+      if (j == i) continue;
+      atomicAdd(&deg[i], 1);
+      atomicAdd(&deg[j], 1);
+    }
+}
+
+__global__ void k_adjacency(int nc, const long long* __restrict__ rowptr, const long long* __restrict__ colidx,
+                            int* __restrict__ cursor, int* __restrict__ adj) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x)
+    for (long long k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      long long j = colidx[k];
+      if (j == i) continue;
+      adj[atomicAdd(&cursor[i], 1)] = (int)j;
+      adj[atomicAdd(&cursor[j], 1)] = i;
+    }
+}
+
+// priority keys; kind 1 counts distinct neighbours (a pair may appear as
+// both (i,j) and (j,i) in W)
+__global__ void k_priority(int nc, const int* __restrict__ gptr, const int* __restrict__ adj, int kind,
+                           uint32_t* __restrict__ key, int* __restrict__ colour) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    uint32_t d = 0;
+    if (kind == 1)
+      for (int k = gptr[i]; k < gptr[i + 1]; k++) {
+        bool dup = false;
+        for (int m = gptr[i]; m < k; m++)
+          if (adj[m] == adj[k]) {
+            dup = true;
+            break;
+          }
+        d += dup ? 0 : 1;
+      }
+    key[i] = colour_priority((uint32_t)i, kind, d);
+    colour[i] = -1;
+  }
+}
+
+__global__ void k_jp_round(int nc, const int* __restrict__ gptr, const int* __restrict__ adj,
+                           const uint32_t* __restrict__ key, int* colour, int* remaining, int* overflow) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    if (((volatile int*)colour)[i] >= 0) continue;
+    const uint32_t ki = key[i];
+    unsigned long long used0 = 0, used1 = 0;
+    bool ready = true;
+    for (int k = gptr[i]; k < gptr[i + 1]; k++) {
+      const int w = adj[k];
+      const uint32_t kw = key[w];
+      if (!(kw > ki || (kw == ki && w < i))) continue;  // lower priority
+      const int c = ((volatile int*)colour)[w];
+      if (c < 0) {
+        ready = false;
+        break;
+      }
+      if (c < 64)
+        used0 |= 1ULL << c;
+      else if (c < 128)
+        used1 |= 1ULL << (c - 64);
+    }
+    if (!ready) {
+      atomicAdd(remaining, 1);
+      continue;
+    }
+    int c = __ffsll(~used0) - 1;
+    if (c < 0 || used0 == ~0ULL) {
+      int c1 = __ffsll(~used1) - 1;
+      c = (c1 < 0) ? 128 : 64 + c1;
+    }
+    if (c >= FC3D_MAX_COLOURS) {
+      atomicOr(overflow, 1);
+      c = FC3D_MAX_COLOURS - 1;
+    }
+    ((volatile int*)colour)[i] = c;
+  }
+}
+
+// per 1024-contact block: colour histogram
+__global__ void k_colour_hist(int nc, const int* __restrict__ colour, int* __restrict__ blockhist) {
+  __shared__ int h[FC3D_MAX_COLOURS];
+  for (int c = threadIdx.x; c < FC3D_MAX_COLOURS; c += blockDim.x) h[c] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < nc) atomicAdd(&h[colour[i]], 1);
+  __syncthreads();
+  for (int c = threadIdx.x; c < FC3D_MAX_COLOURS; c += blockDim.x) blockhist[blockIdx.x * FC3D_MAX_COLOURS + c] = h[c];
+}
+
+// single block: per-(colour, block) offsets inside each colour, colour
+// counts and slab ranges
+__global__ void k_colour_offsets(int nblocks, int* __restrict__ blockhist, int* __restrict__ counts,
+                                 int* __restrict__ sptr) {
+  const int c = threadIdx.x;
+  if (c < FC3D_MAX_COLOURS) {
+    int run = 0;
+    for (int b = 0; b < nblocks; b++) {
+      int v = blockhist[b * FC3D_MAX_COLOURS + c];
+      blockhist[b * FC3D_MAX_COLOURS + c] = run;
+      run += v;
+    }
+    counts[c] = run;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    sptr[0] = 0;
+    for (int k = 0; k < FC3D_MAX_COLOURS; k++) {
+      s += (counts[k] + FC3D_SLAB - 1) / FC3D_SLAB;
+      sptr[k + 1] = s;
+    }
+  }
+}
+
+// stable scatter: contacts keep index order inside their colour
+__global__ void k_colour_scatter(int nc, const int* __restrict__ colour, const int* __restrict__ blockoff,
+                                 const int* __restrict__ sptr, int* __restrict__ perm, int* __restrict__ iperm) {
+  __shared__ int wcount[32][FC3D_MAX_COLOURS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int t = threadIdx.x; t < 32 * FC3D_MAX_COLOURS; t += blockDim.x) (&wcount[0][0])[t] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * 1024 + threadIdx.x;
+  const int c = (i < nc) ? colour[i] : -1;
+  const unsigned mask = __match_any_sync(0xffffffffu, c);
+  const int leader = __ffs(mask) - 1;
+  if (c >= 0 && lane == leader) wcount[w][c] = __popc(mask);
+  __syncthreads();
+  // exclusive prefix over warps, per colour
+  for (int cc = threadIdx.x; cc < FC3D_MAX_COLOURS; cc += blockDim.x) {
+    int run = 0;
+    for (int k = 0; k < 32; k++) {
+      int v = wcount[k][cc];
+      wcount[k][cc] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  if (c >= 0) {
+    const int rank = blockoff[blockIdx.x * FC3D_MAX_COLOURS + c] + wcount[w][c] + __popc(mask & ((1u << lane) - 1));
+    const int p = sptr[c] * FC3D_SLAB + rank;
+    perm[p] = i;
+    iperm[i] = p;
+  }
+}
+
+// per padded row: off-diagonal count and slot position of the diagonal
+__global__ void k_rowinfo(int npad, const int* __restrict__ perm, const long long* __restrict__ rowptr,
+                          const long long* __restrict__ colidx, int* __restrict__ rowlen, int* __restrict__ dpos,
+                          int* __restrict__ nodiag) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x) {
+    const int i = perm[p];
+    if (i < 0) {
+      rowlen[p] = 0;
+      dpos[p] = 0;
+      continue;
+    }
+    int s = 0, d = -1;
+    for (long long k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      if (colidx[k] == i && d < 0)
+        d = s;
+      else
+        s++;
+    }
+    rowlen[p] = s;
+    dpos[p] = d < 0 ? s : d;
+    if (d < 0) atomicOr(nodiag, 1);
+  }
+}
+
+__global__ void k_slab_nslot(int nslab, const int* __restrict__ rowlen, int* __restrict__ nslot) {
+  const int lane = threadIdx.x & 31;
+  const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= nslab) return;
+  int v = rowlen[s * FC3D_SLAB + lane];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane == 0) nslot[s] = v;
+}
+
+// single block: exclusive scan (64-bit output) of n counts; total in *total
+template <typename In>
+__global__ void k_scan_excl(int n, const In* __restrict__ cnt, long long* __restrict__ off, long long* __restrict__ total) {
+  __shared__ long long carry;
+  __shared__ long long buf[1024];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += 1024) {
+    const int t = threadIdx.x, idx = base + t;
+    buf[t] = idx < n ? (long long)cnt[idx] : 0;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      long long v = t >= o ? buf[t - o] : 0;
+      __syncthreads();
+      buf[t] += v;
+      __syncthreads();
+    }
+    if (idx < n) off[idx] = carry + buf[t] - (long long)cnt[idx];
+    __syncthreads();
+    if (t == 1023) carry += buf[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_ll_to_int(int n, const long long* __restrict__ a, int* __restrict__ b) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) b[t] = (int)a[t];
+}
+
+__global__ void k_max_colour(int nc, const int* __restrict__ colour, int* __restrict__ mx) {
+  int m = -1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) m = max(m, colour[i]);
+  for (int o = 16; o >= 1; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+__global__ void k_fill_col_pad(long long nslots, int npad, int* __restrict__ col) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nslots * FC3D_SLAB;
+       t += (long long)gridDim.x * blockDim.x)
+    col[t] = npad;
+}
+
+// scatter the blocks of each row into the slab layout (FP64 master copy)
+__global__ void k_fill_blocks(int nc, const long long* __restrict__ rowptr, const long long* __restrict__ colidx,
+                              const double* __restrict__ blocks, const int* __restrict__ iperm,
+                              const long long* __restrict__ slab_off, double* __restrict__ W, int* __restrict__ col,
+                              double* __restrict__ D, double* __restrict__ rho) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int p = iperm[i];
+    const int slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
+    const long long base = slab_off[slab];
+    int s = 0;
+    bool diag_done = false;
+    for (long long kk = rowptr[i]; kk < rowptr[i + 1]; kk++) {
+      const long long j = colidx[kk];
+      const double* b = blocks + 9 * kk;
+      if (j == i && !diag_done) {
+        diag_done = true;
+        for (int e = 0; e < 9; e++) D[((size_t)slab * 9 + e) * FC3D_SLAB + k] = b[e];
+      } else {
+        const size_t sl = (size_t)(base + s);
+        for (int e = 0; e < 9; e++) W[(sl * 9 + e) * FC3D_SLAB + k] = b[e];
+        col[sl * FC3D_SLAB + k] = iperm[j];
+        s++;
+      }
+    }
+    double M[9];
+    for (int e = 0; e < 9; e++) M[e] = D[((size_t)slab * 9 + e) * FC3D_SLAB + k];
+    double rn = 1.0, rt = 1.0;
+    if (diag_done) ac_rho<double>(M, rn, rt);
+    rho[((size_t)slab * 2) * FC3D_SLAB + k] = rn;
+    rho[((size_t)slab * 2 + 1) * FC3D_SLAB + k] = rt;
+  }
+}
+
+__global__ void k_to_f32(long long n, const double* __restrict__ a, float* __restrict__ b) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+    b[t] = (float)a[t];
+}
+
+__global__ void k_set_q_mu(int nc, const int* __restrict__ iperm, const double* __restrict__ q,
+                           const double* __restrict__ mu, double* __restrict__ q64, double* __restrict__ mu64,
+                           float* __restrict__ q32, float* __restrict__ mu32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int p = iperm[i], slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
+    for (int a = 0; a < 3; a++) {
+      const double v = q[3 * (size_t)i + a];
+      q64[((size_t)slab * 3 + a) * FC3D_SLAB + k] = v;
+      q32[((size_t)slab * 3 + a) * FC3D_SLAB + k] = (float)v;
+    }
+    mu64[(size_t)slab * FC3D_SLAB + k] = mu[i];
+    mu32[(size_t)slab * FC3D_SLAB + k] = (float)mu[i];
+  }
+}
+
+// r (original order, 3 per contact) -> padded AoS copies; PLI step reset to 1
+// as fc3d_AC_initialize does at every solve (onecontact.c:115)
+__global__ void k_set_r(int nc, const int* __restrict__ iperm, const double* __restrict__ r, double* __restrict__ r64,
+                        float* __restrict__ r32, double* __restrict__ rpli64, float* __restrict__ rpli32) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int p = iperm[i];
+    for (int a = 0; a < 3; a++) {
+      r64[4 * (size_t)p + a] = r[3 * (size_t)i + a];
+      r32[4 * (size_t)p + a] = (float)r[3 * (size_t)i + a];
+    }
+    rpli64[p] = 1.0;
+    rpli32[p] = 1.0f;
+  }
+}
+
+__global__ void k_r32_to_r64(int npad, const float* __restrict__ r32, const float* __restrict__ rpli32,
+                             double* __restrict__ r64, double* __restrict__ rpli64) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x) {
+    for (int a = 0; a < 3; a++) r64[4 * (size_t)p + a] = (double)r32[4 * (size_t)p + a];
+    rpli64[p] = (double)rpli32[p];
+  }
+}
+
+__global__ void k_r64_to_r32(int npad, const double* __restrict__ r64, float* __restrict__ r32) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x)
+    for (int a = 0; a < 3; a++) r32[4 * (size_t)p + a] = (float)r64[4 * (size_t)p + a];
+}
+
+__global__ void k_get_r_u(int nc, const int* __restrict__ iperm, const double* __restrict__ r64,
+                          const double* __restrict__ u64, double* __restrict__ r, double* __restrict__ u) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int p = iperm[i];
+    for (int a = 0; a < 3; a++) {
+      if (r) r[3 * (size_t)i + a] = r64[4 * (size_t)p + a];
+      if (u) u[3 * (size_t)i + a] = u64[3 * (size_t)p + a];
+    }
+  }
+}
+
+}  // namespace fc3dgpu
+
+// ---------------------------------------------------------------------------
+// Device context (C-ABI in include/fc3dgpu.h)
+// ---------------------------------------------------------------------------
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "fc3dgpu.h"
+
+static thread_local char g_err[512];
+
+extern "C" const char* fc3dgpu_last_error(void) { return g_err; }
+
+extern "C" void fc3dgpu_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+#define CK(x)                                                                              \
+  do {                                                                                     \
+    cudaError_t e_ = (x);                                                                  \
+    if (e_ != cudaSuccess) {                                                               \
+      fc3dgpu_set_error("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_)); \
+      return NUMERICS_ERR_UNKNOWN;                                                         \
+    }                                                                                      \
+  } while (0)
+
+template <typename T>
+static cudaError_t ensure(T** p, size_t* cap, size_t n) {
+  if (*p && *cap >= n) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
+  if (e == cudaSuccess) *cap = n;
+  return e;
+}
+
+#define BUF(T, name) \
+  T* name = nullptr; \
+  size_t name##_cap = 0
+
+struct fc3dgpu_ctx {
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int nc = 0;
+  long long nnzb = 0;
+  int ncol = 0, nslab = 0, npad = 0;
+  long long nslots = 0;
+  int sptr[FC3D_MAX_COLOURS + 1];
+  double norm_q = 0.0;
+  bool have_W = false, have_q = false, have_r = false;
+  int trace_len = 0;
+  // inputs (original order)
+  BUF(long long, rowptr);
+  BUF(long long, colidx);
+  BUF(double, blocks);
+  BUF(double, qo);
+  BUF(double, muo);
+  BUF(double, ro);
+  BUF(double, uo);
+  // colouring
+  BUF(int, deg);
+  BUF(long long, gptr64);
+  BUF(int, gptr);
+  BUF(int, cursor);
+  BUF(int, adj);
+  BUF(uint32_t, key);
+  BUF(int, colour);
+  BUF(int, blockhist);
+  BUF(int, counts);
+  BUF(int, sptr_d);
+  // layout
+  BUF(int, perm);
+  BUF(int, iperm);
+  BUF(int, rowlen);
+  BUF(int, dpos);
+  BUF(int, slab_nslot);
+  BUF(long long, slab_off);
+  BUF(double, W64);
+  BUF(float, W32);
+  BUF(int, col);
+  BUF(double, D64);
+  BUF(float, D32);
+  BUF(double, rho64);
+  BUF(float, rho32);
+  BUF(double, q64);
+  BUF(float, q32);
+  BUF(double, mu64);
+  BUF(float, mu32);
+  BUF(double, r64);
+  BUF(float, r32);
+  BUF(double, rpli64);
+  BUF(float, rpli32);
+  BUF(double, u64);
+  // control
+  BUF(double, partials);
+  BUF(unsigned, barrier);
+  BUF(int, status);
+  BUF(int, scratch);
+  BUF(long long, scratch64);
+  BUF(double, out);
+  BUF(double, trace);
+};
+
+static int grid1d(long long n, int block = 256) {
+  long long g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > 65535LL * 8) g = 65535LL * 8;
+  return (int)g;
+}
+
+extern "C" void fc3dgpu_params_default(fc3dgpu_params* p) {
+  p->tol = 1e-4;
+  p->max_iter = 1000;
+  p->precision = 0;
+  p->lanes = 0;
+  p->switch_tol = 1e-6;
+  p->stall_window = 64;
+  p->local_tol = 1e-14;
+  p->local_tol32 = 1e-6;
+  p->newton_max = 100;
+  p->pli_max = 100;
+  p->ls_max = 10;
+  p->fp32_only = 0;
+}
+
+extern "C" fc3dgpu_ctx* fc3dgpu_ctx_create(int device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n <= device || device < 0) {
+    fc3dgpu_set_error("no CUDA device %d (%s)", device, e != cudaSuccess ? cudaGetErrorString(e) : "count");
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    fc3dgpu_set_error("cudaSetDevice(%d) failed", device);
+    return nullptr;
+  }
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+  if (!coop) {
+    fc3dgpu_set_error("device %d does not support cooperative launches", device);
+    return nullptr;
+  }
+  fc3dgpu_ctx* c = new fc3dgpu_ctx();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    fc3dgpu_set_error("cudaStreamCreate failed");
+    return nullptr;
+  }
+  for (int i = 0; i < 4; i++) cudaEventCreate(&c->ev[i]);
+  bool ok = ensure(&c->partials, &c->partials_cap, 1024 * 8) == cudaSuccess &&
+            ensure(&c->barrier, &c->barrier_cap, 4) == cudaSuccess &&
+            ensure(&c->status, &c->status_cap, 4) == cudaSuccess &&
+            ensure(&c->scratch, &c->scratch_cap, 16) == cudaSuccess &&
+            ensure(&c->scratch64, &c->scratch64_cap, 16) == cudaSuccess &&
+            ensure(&c->out, &c->out_cap, 16) == cudaSuccess &&
+            ensure(&c->trace, &c->trace_cap, 1 << 17) == cudaSuccess;
+  if (!ok) {
+    fc3dgpu_set_error("device allocation failed");
+    fc3dgpu_ctx_destroy(c);
+    return nullptr;
+  }
+  return c;
+}
+
+extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  void* ptrs[] = {c->rowptr, c->colidx, c->blocks, c->qo, c->muo, c->ro, c->uo, c->deg, c->gptr64, c->gptr,
+                  c->cursor, c->adj, c->key, c->colour, c->blockhist, c->counts, c->sptr_d, c->perm, c->iperm,
+                  c->rowlen, c->dpos, c->slab_nslot, c->slab_off, c->W64, c->W32, c->col, c->D64, c->D32,
+                  c->rho64, c->rho32, c->q64, c->q32, c->mu64, c->mu32, c->r64, c->r32, c->rpli64, c->rpli32,
+                  c->u64, c->partials, c->barrier, c->status, c->scratch, c->scratch64, c->out, c->trace};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (int i = 0; i < 4; i++)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+// Host check of a block-CSR structure before any device kernel indexes with
+// it: monotone row pointer, column indices inside [0, nc).
+static int validate_bcsr(int nc, const int64_t* rowptr, const int64_t* colidx) {
+  if (rowptr[0] != 0) {
+    fc3dgpu_set_error("row pointer must start at 0");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  for (int i = 0; i < nc; i++) {
+    if (rowptr[i + 1] < rowptr[i]) {
+      fc3dgpu_set_error("row pointer decreases at row %d", i);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (colidx[k] < 0 || colidx[k] >= nc) {
+        fc3dgpu_set_error("block column %lld out of range in row %d", (long long)colidx[k], i);
+        return NUMERICS_ERR_INVALID_ARGUMENT;
+      }
+  }
+  return 0;
+}
+
+// Colour the conflict graph of the uploaded structure (rowptr/colidx on the
+// device); result in c->colour, number of colours returned.
+static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind) {
+  using namespace fc3dgpu;
+  cudaStream_t s = c->stream;
+  CK(ensure(&c->deg, &c->deg_cap, (size_t)nc));
+  CK(ensure(&c->gptr64, &c->gptr64_cap, (size_t)nc + 1));
+  CK(ensure(&c->gptr, &c->gptr_cap, (size_t)nc + 1));
+  CK(ensure(&c->cursor, &c->cursor_cap, (size_t)nc));
+  CK(ensure(&c->key, &c->key_cap, (size_t)nc));
+  CK(ensure(&c->colour, &c->colour_cap, (size_t)nc));
+  CK(cudaMemsetAsync(c->deg, 0, sizeof(int) * nc, s));
+  k_degree<<<grid1d(nc), 256, 0, s>>>(nc, c->rowptr, c->colidx, c->deg);
+  k_scan_excl<int><<<1, 1024, 0, s>>>(nc, c->deg, c->gptr64, c->scratch64);
+  long long nadj = 0;
+  CK(cudaMemcpyAsync(&nadj, c->scratch64, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (nadj > 0x7fffffffLL) {
+    fc3dgpu_set_error("conflict graph too large (%lld entries)", nadj);
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaMemcpyAsync(c->gptr64 + nc, c->scratch64, sizeof(long long), cudaMemcpyDeviceToDevice, s));
+  k_ll_to_int<<<grid1d(nc + 1), 256, 0, s>>>(nc + 1, c->gptr64, c->gptr);
+  CK(ensure(&c->adj, &c->adj_cap, (size_t)(nadj ? nadj : 1)));
+  CK(cudaMemcpyAsync(c->cursor, c->gptr, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s));
+  k_adjacency<<<grid1d(nc), 256, 0, s>>>(nc, c->rowptr, c->colidx, c->cursor, c->adj);
+  k_priority<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, kind, c->key, c->colour);
+  int rounds = 0;
+  for (;;) {
+    CK(cudaMemsetAsync(c->scratch, 0, 2 * sizeof(int), s));
+    k_jp_round<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, c->key, c->colour, c->scratch, c->scratch + 1);
+    int h[2];
+    CK(cudaMemcpyAsync(h, c->scratch, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h[1]) {
+      fc3dgpu_set_error("colouring needs more than %d colours", FC3D_MAX_COLOURS);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+    if (h[0] == 0) break;
+    if (++rounds > nc + 1) {
+      fc3dgpu_set_error("colouring did not finish");
+      return NUMERICS_ERR_UNKNOWN;
+    }
+  }
+  CK(cudaMemsetAsync(c->scratch + 2, 0xff, sizeof(int), s));
+  k_max_colour<<<grid1d(nc), 256, 0, s>>>(nc, c->colour, c->scratch + 2);
+  int mx = -1;
+  CK(cudaMemcpyAsync(&mx, c->scratch + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return mx + 1;
+}
+
+extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx,
+                                 const double* blocks, int kind) {
+  using namespace fc3dgpu;
+  if (!c || nc <= 0 || !rowptr || !colidx || !blocks) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_W: invalid argument");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const long long nnzb = rowptr[nc];
+  if (nnzb < nc) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_W: fewer blocks than block rows");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  {
+    int v = validate_bcsr(nc, rowptr, colidx);
+    if (v) return v;
+  }
+  c->have_W = c->have_q = c->have_r = false;
+  CK(ensure(&c->rowptr, &c->rowptr_cap, (size_t)nc + 1));
+  CK(ensure(&c->colidx, &c->colidx_cap, (size_t)nnzb));
+  CK(ensure(&c->blocks, &c->blocks_cap, (size_t)nnzb * 9));
+  CK(cudaMemcpyAsync(c->rowptr, rowptr, sizeof(long long) * (nc + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->colidx, colidx, sizeof(long long) * nnzb, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->blocks, blocks, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+  int ncol = colour_device(c, nc, nnzb, kind);
+  if (ncol < 0) return ncol;
+  // stable permutation by colour
+  const int nblk = (nc + 1023) / 1024;
+  CK(ensure(&c->blockhist, &c->blockhist_cap, (size_t)nblk * FC3D_MAX_COLOURS));
+  CK(ensure(&c->counts, &c->counts_cap, FC3D_MAX_COLOURS));
+  CK(ensure(&c->sptr_d, &c->sptr_d_cap, FC3D_MAX_COLOURS + 1));
+  k_colour_hist<<<nblk, 1024, 0, s>>>(nc, c->colour, c->blockhist);
+  k_colour_offsets<<<1, FC3D_MAX_COLOURS, 0, s>>>(nblk, c->blockhist, c->counts, c->sptr_d);
+  CK(cudaMemcpyAsync(c->sptr, c->sptr_d, sizeof(int) * (FC3D_MAX_COLOURS + 1), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  c->ncol = ncol;
+  c->nslab = c->sptr[ncol];
+  c->npad = c->nslab * FC3D_SLAB;
+  const int npad = c->npad, nslab = c->nslab;
+  CK(ensure(&c->perm, &c->perm_cap, (size_t)npad));
+  CK(ensure(&c->iperm, &c->iperm_cap, (size_t)nc));
+  CK(cudaMemsetAsync(c->perm, 0xff, sizeof(int) * npad, s));
+  k_colour_scatter<<<nblk, 1024, 0, s>>>(nc, c->colour, c->blockhist, c->sptr_d, c->perm, c->iperm);
+  // rows, slabs, slots
+  CK(ensure(&c->rowlen, &c->rowlen_cap, (size_t)npad));
+  CK(ensure(&c->dpos, &c->dpos_cap, (size_t)npad));
+  CK(ensure(&c->slab_nslot, &c->slab_nslot_cap, (size_t)nslab));
+  CK(ensure(&c->slab_off, &c->slab_off_cap, (size_t)nslab));
+  CK(cudaMemsetAsync(c->scratch + 3, 0, sizeof(int), s));
+  k_rowinfo<<<grid1d(npad), 256, 0, s>>>(npad, c->perm, c->rowptr, c->colidx, c->rowlen, c->dpos, c->scratch + 3);
+  k_slab_nslot<<<grid1d((long long)nslab * 32), 256, 0, s>>>(nslab, c->rowlen, c->slab_nslot);
+  k_scan_excl<int><<<1, 1024, 0, s>>>(nslab, c->slab_nslot, c->slab_off, c->scratch64);
+  long long nslots = 0;
+  int nodiag = 0;
+  CK(cudaMemcpyAsync(&nslots, c->scratch64, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&nodiag, c->scratch + 3, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (nodiag) {
+    fc3dgpu_set_error("W has a block row without its diagonal block");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  c->nslots = nslots;
+  const size_t nw = (size_t)(nslots ? nslots : 1) * 9 * FC3D_SLAB;
+  CK(ensure(&c->W64, &c->W64_cap, nw));
+  CK(ensure(&c->W32, &c->W32_cap, nw));
+  CK(ensure(&c->col, &c->col_cap, (size_t)(nslots ? nslots : 1) * FC3D_SLAB));
+  CK(ensure(&c->D64, &c->D64_cap, (size_t)nslab * 9 * FC3D_SLAB));
+  CK(ensure(&c->D32, &c->D32_cap, (size_t)nslab * 9 * FC3D_SLAB));
+  CK(ensure(&c->rho64, &c->rho64_cap, (size_t)nslab * 2 * FC3D_SLAB));
+  CK(ensure(&c->rho32, &c->rho32_cap, (size_t)nslab * 2 * FC3D_SLAB));
+  CK(ensure(&c->q64, &c->q64_cap, (size_t)nslab * 3 * FC3D_SLAB));
+  CK(ensure(&c->q32, &c->q32_cap, (size_t)nslab * 3 * FC3D_SLAB));
+  CK(ensure(&c->mu64, &c->mu64_cap, (size_t)npad));
+  CK(ensure(&c->mu32, &c->mu32_cap, (size_t)npad));
+  CK(ensure(&c->r64, &c->r64_cap, ((size_t)npad + 1) * 4));
+  CK(ensure(&c->r32, &c->r32_cap, ((size_t)npad + 1) * 4));
+  CK(ensure(&c->rpli64, &c->rpli64_cap, (size_t)npad));
+  CK(ensure(&c->rpli32, &c->rpli32_cap, (size_t)npad));
+  CK(ensure(&c->u64, &c->u64_cap, (size_t)npad * 3));
+  CK(cudaMemsetAsync(c->W64, 0, sizeof(double) * nw, s));
+  CK(cudaMemsetAsync(c->D64, 0, sizeof(double) * nslab * 9 * FC3D_SLAB, s));
+  CK(cudaMemsetAsync(c->rho64, 0, sizeof(double) * nslab * 2 * FC3D_SLAB, s));
+  CK(cudaMemsetAsync(c->q64, 0, sizeof(double) * nslab * 3 * FC3D_SLAB, s));
+  CK(cudaMemsetAsync(c->q32, 0, sizeof(float) * nslab * 3 * FC3D_SLAB, s));
+  CK(cudaMemsetAsync(c->mu64, 0, sizeof(double) * npad, s));
+  CK(cudaMemsetAsync(c->mu32, 0, sizeof(float) * npad, s));
+  CK(cudaMemsetAsync(c->r64, 0, sizeof(double) * (npad + 1) * 4, s));
+  CK(cudaMemsetAsync(c->r32, 0, sizeof(float) * (npad + 1) * 4, s));
+  CK(cudaMemsetAsync(c->u64, 0, sizeof(double) * npad * 3, s));
+  k_fill_col_pad<<<grid1d((long long)nslots * FC3D_SLAB), 256, 0, s>>>(nslots, npad, c->col);
+  k_fill_blocks<<<grid1d(nc, 128), 128, 0, s>>>(nc, c->rowptr, c->colidx, c->blocks, c->iperm, c->slab_off, c->W64,
+                                                c->col, c->D64, c->rho64);
+  k_to_f32<<<grid1d((long long)nw), 256, 0, s>>>((long long)nw, c->W64, c->W32);
+  k_to_f32<<<grid1d((long long)nslab * 9 * 32), 256, 0, s>>>((long long)nslab * 9 * 32, c->D64, c->D32);
+  k_to_f32<<<grid1d((long long)nslab * 2 * 32), 256, 0, s>>>((long long)nslab * 2 * 32, c->rho64, c->rho32);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  c->nc = nc;
+  c->nnzb = nnzb;
+  c->have_W = true;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const double* mu) {
+  using namespace fc3dgpu;
+  if (!c || !c->have_W || !q || !mu) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_q_mu: W not set or null input");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  const int nc = c->nc;
+  CK(ensure(&c->qo, &c->qo_cap, (size_t)nc * 3));
+  CK(ensure(&c->muo, &c->muo_cap, (size_t)nc));
+  CK(cudaMemcpyAsync(c->qo, q, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->muo, mu, sizeof(double) * nc, cudaMemcpyHostToDevice, c->stream));
+  k_set_q_mu<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->qo, c->muo, c->q64, c->mu64, c->q32, c->mu32);
+  CK(cudaGetLastError());
+  // |q| as the reference computes it (a plain sum of squares in index order)
+  double s2 = 0.0;
+  for (long long i = 0; i < 3LL * nc; i++) s2 += q[i] * q[i];
+  c->norm_q = sqrt(s2);
+  c->have_q = true;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_set_r(fc3dgpu_ctx* c, const double* r) {
+  using namespace fc3dgpu;
+  if (!c || !c->have_W || !r) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_r: W not set or null input");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  const int nc = c->nc;
+  CK(ensure(&c->ro, &c->ro_cap, (size_t)nc * 3));
+  CK(cudaMemcpyAsync(c->ro, r, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, c->stream));
+  k_set_r<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->ro, c->r64, c->r32, c->rpli64, c->rpli32);
+  CK(cudaGetLastError());
+  c->have_r = true;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_get_r_u(fc3dgpu_ctx* c, double* r, double* u) {
+  using namespace fc3dgpu;
+  if (!c || !c->have_W) {
+    fc3dgpu_set_error("fc3dgpu_ctx_get_r_u: no problem");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  const int nc = c->nc;
+  CK(ensure(&c->ro, &c->ro_cap, (size_t)nc * 3));
+  CK(ensure(&c->uo, &c->uo_cap, (size_t)nc * 3));
+  k_get_r_u<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->r64, c->u64, c->ro, c->uo);
+  CK(cudaGetLastError());
+  if (r) CK(cudaMemcpyAsync(r, c->ro, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+  if (u) CK(cudaMemcpyAsync(u, c->uo, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+template <typename Real>
+static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W, const Real* D, const Real* q,
+                      const Real* mu, const Real* rho, Real* r, Real* rpli) {
+  a.ncol = c->ncol;
+  a.nslab = c->nslab;
+  a.npad = c->npad;
+  for (int k = 0; k <= FC3D_MAX_COLOURS; k++) a.sptr[k] = c->sptr[k];
+  a.slab_nslot = c->slab_nslot;
+  a.slab_off = c->slab_off;
+  a.perm = c->perm;
+  a.dpos = c->dpos;
+  a.W = W;
+  a.col = c->col;
+  a.D = D;
+  a.q = q;
+  a.mu = mu;
+  a.rho = rho;
+  a.r = r;
+  a.rpli = rpli;
+  a.u = c->u64;
+  a.partials = c->partials;
+  a.barrier = c->barrier;
+  a.status = c->status;
+  a.trace = c->trace;
+  a.trace_cap = (int)c->trace_cap;
+  a.trace_base = 0;
+  a.norm_q = c->norm_q;
+  a.spin_limit = 1ULL << 22;
+  a.out = c->out;
+}
+
+static int autotune_lanes(fc3dgpu_ctx* c) {
+  // contacts per colour phase vs. resident warps: more lanes per contact when
+  // a phase has too few contacts to fill the GPU
+  const long long per_phase = (long long)c->nc / (c->ncol > 0 ? c->ncol : 1);
+  const long long warps = (long long)c->nsm * 32;
+  if (per_phase >= 16 * warps) return 1;
+  if (per_phase >= 4 * warps) return 2;
+  return 4;
+}
+
+extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgpu_stats* st) {
+  using namespace fc3dgpu;
+  if (!c || !p || !c->have_W || !c->have_q || !c->have_r) {
+    fc3dgpu_set_error("fc3dgpu_ctx_solve: problem, q/mu or r not set");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  fc3dgpu_stats S;
+  memset(&S, 0, sizeof(S));
+  const int lanes = p->lanes > 0 ? p->lanes : autotune_lanes(c);
+  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8) {
+    fc3dgpu_set_error("lanes per contact must be 1, 2, 4 or 8 (got %d)", lanes);
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  S.lanes = lanes;
+  S.colours = c->ncol;
+  const double s32 = 4.0, s64 = 8.0;
+  S.bytes_sweep32 = (double)c->nnzb * (9 * s32 + 4) + (double)c->nc * (3 * s32 + s32 + 3 * s32 + 3 * s32);
+  S.bytes_sweep64 = (double)c->nnzb * (9 * s64 + 4) + (double)c->nc * (3 * s64 + s64 + 3 * s64 + 3 * s64);
+  CK(cudaMemsetAsync(c->status, 0, sizeof(int), s));
+  CK(cudaEventRecord(c->ev[0], s));
+  int sweeps32 = 0, grid = 0;
+  double out[8];
+  if (p->precision == 0 && p->max_iter > 0) {
+    SweepArgs<float> a;
+    fill_args<float>(c, a, c->W32, c->D32, c->q32, c->mu32, c->rho32, c->r32, c->rpli32);
+    a.max_sweeps = p->max_iter;
+    a.mode = 0;
+    a.user_tol = p->tol;
+    a.local_tol = p->local_tol32;
+    a.switch_tol = p->switch_tol;
+    a.stall_window = p->stall_window;
+    a.newton_max = p->newton_max;
+    a.pli_max = p->pli_max;
+    a.ls_max = p->ls_max;
+    CK(cudaMemsetAsync(c->barrier, 0, sizeof(unsigned), s));
+    CK(launch_sweep_f32(a, lanes, 0, s, &grid));
+    CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(c->ev[1], s));
+    CK(cudaStreamSynchronize(s));
+    sweeps32 = (int)out[0];
+    S.incr_error = out[1];
+    k_r32_to_r64<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r32, c->rpli32, c->r64, c->rpli64);
+    CK(cudaGetLastError());
+  } else {
+    CK(cudaEventRecord(c->ev[1], s));
+  }
+  {
+    SweepArgs<double> a;
+    fill_args<double>(c, a, c->W64, c->D64, c->q64, c->mu64, c->rho64, c->r64, c->rpli64);
+    int budget = p->max_iter - sweeps32;
+    if (budget < 0 || p->fp32_only) budget = 0;
+    a.max_sweeps = budget;
+    a.mode = 1;
+    a.user_tol = p->tol;
+    a.local_tol = p->local_tol;
+    a.switch_tol = 0.0;
+    a.stall_window = 0;
+    a.trace_base = sweeps32;
+    a.newton_max = p->newton_max;
+    a.pli_max = p->pli_max;
+    a.ls_max = p->ls_max;
+    int g64 = 0;
+    CK(cudaMemsetAsync(c->barrier, 0, sizeof(unsigned), s));
+    CK(launch_sweep_f64(a, lanes, 0, s, &g64));
+    if (!grid) grid = g64;
+    CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaEventRecord(c->ev[2], s));
+  int status = 0;
+  CK(cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms1, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&ms2, c->ev[1], c->ev[2]);
+  S.sweeps32 = sweeps32;
+  S.sweeps64 = (int)out[0];
+  if (S.sweeps64 > 0 || p->precision == 1) S.incr_error = out[1];
+  S.error = out[2];
+  S.info = (int)out[3];
+  if (p->fp32_only && sweeps32 >= p->max_iter && S.info > 0) S.info = NUMERICS_ERR_MAX_ITER;
+  if (!p->fp32_only && S.sweeps32 + S.sweeps64 >= p->max_iter && S.info > 0) S.info = NUMERICS_ERR_MAX_ITER;
+  S.ms_fp32 = ms1;
+  S.ms_fp64 = ms2;
+  S.ms_total = (double)ms1 + (double)ms2;
+  S.grid = grid;
+  S.status = status;
+  c->trace_len = S.sweeps32 + S.sweeps64;
+  if (st) *st = S;
+  if (status) {
+    fc3dgpu_set_error("device status %d (%s)", status,
+                      (status & FC3DGPU_STATUS_BARRIER_TIMEOUT) ? "grid barrier timed out" : "non-finite iterate");
+    return NUMERICS_ERR_UNKNOWN;
+  }
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_compute_error(fc3dgpu_ctx* c, double* error) {
+  using namespace fc3dgpu;
+  if (!c || !c->have_W || !c->have_q || !c->have_r) {
+    fc3dgpu_set_error("fc3dgpu_ctx_compute_error: problem, q/mu or r not set");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  SweepArgs<double> a;
+  fill_args<double>(c, a, c->W64, c->D64, c->q64, c->mu64, c->rho64, c->r64, c->rpli64);
+  a.max_sweeps = 0;
+  a.mode = 1;
+  a.user_tol = 1.0;
+  a.local_tol = 1e-14;
+  a.switch_tol = 0;
+  a.stall_window = 0;
+  a.newton_max = 100;
+  a.pli_max = 100;
+  a.ls_max = 10;
+  a.trace = nullptr;
+  int g = 0;
+  double out[8];
+  CK(cudaMemsetAsync(c->barrier, 0, sizeof(unsigned), s));
+  CK(cudaMemsetAsync(c->status, 0, sizeof(int), s));
+  CK(launch_sweep_f64(a, 1, 0, s, &g));
+  CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (error) *error = out[2];
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx* c, double norm_q) {
+  if (!c) return -1;
+  c->norm_q = norm_q;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_trace(fc3dgpu_ctx* c, double* out, int cap) {
+  if (!c) return -1;
+  int n = c->trace_len < (int)c->trace_cap ? c->trace_len : (int)c->trace_cap;
+  if (n > cap) n = cap;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(out, c->trace, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return n;
+}
+
+extern "C" int fc3dgpu_ctx_colours(fc3dgpu_ctx* c, int32_t* colour) {
+  if (!c || !c->have_W) return -1;
+  CK(cudaMemcpyAsync(colour, c->colour, sizeof(int) * c->nc, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return c->ncol;
+}
+
+extern "C" int fc3dgpu_colour(int nc, const int64_t* rowptr, const int64_t* colidx, int kind, int32_t* colour) {
+  if (nc <= 0 || !rowptr || !colidx || !colour) {
+    fc3dgpu_set_error("fc3dgpu_colour: invalid argument");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  fc3dgpu_ctx* c = fc3dgpu_ctx_create(dev);
+  if (!c) return NUMERICS_ERR_NOT_IMPLEMENTED;
+  const long long nnzb = rowptr[nc];
+  int rc = validate_bcsr(nc, rowptr, colidx);
+  if (rc) {
+    fc3dgpu_ctx_destroy(c);
+    return rc;
+  }
+  if (ensure(&c->rowptr, &c->rowptr_cap, (size_t)nc + 1) != cudaSuccess ||
+      ensure(&c->colidx, &c->colidx_cap, (size_t)(nnzb ? nnzb : 1)) != cudaSuccess) {
+    fc3dgpu_set_error("fc3dgpu_colour: allocation failed");
+    rc = NUMERICS_ERR_MEMORY;
+  }
+  if (!rc) {
+    cudaMemcpy(c->rowptr, rowptr, sizeof(long long) * (nc + 1), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->colidx, colidx, sizeof(long long) * nnzb, cudaMemcpyHostToDevice);
+    rc = colour_device(c, nc, nnzb, kind);
+    if (rc >= 0 && cudaMemcpy(colour, c->colour, sizeof(int) * nc, cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = NUMERICS_ERR_UNKNOWN;
+  }
+  fc3dgpu_ctx_destroy(c);
+  return rc;
+}

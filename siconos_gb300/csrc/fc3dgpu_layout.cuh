@@ -1,0 +1,70 @@
+// Device layout of a coloured friction-contact problem, shared by the
+// layout-building code and the sweep kernels.
+//
+// W of the reference is a SparseBlockStructuredMatrix: per block row, a list
+// of scattered 3x3 column-major blocks (SparseBlockMatrix.h:82-121).  On the
+// device the rows are permuted so that each colour is a contiguous range,
+// padded to whole slabs of 32 rows, and each slab is stored slot-major
+// (ELL within the slab):
+//
+//   W[(slab_off[s] + slot) * 9 + e][lane]   element e of the slot-th
+//                                           off-diagonal block of row
+//                                           32*s + lane (coalesced: one
+//                                           128/256-byte line per (slot, e))
+//   col[(slab_off[s] + slot)][lane]         permuted column of that block
+//   D[(s * 9 + e)][lane], q[(s*3 + a)][lane], mu[s][lane], rho[(s*2+b)][lane]
+//
+// Padding rows (perm = -1) and padding slots (rows shorter than the slab's
+// longest) hold zero blocks whose column is the extra zero entry of r at
+// index npad, so the product needs no branch.
+#pragma once
+#include <stdint.h>
+
+#define FC3D_SLAB 32
+#define FC3D_MAX_COLOURS 128
+
+namespace fc3dgpu {
+
+template <typename Real>
+struct SweepArgs {
+  // layout
+  int ncol;
+  int nslab;
+  int npad;                     // 32 * nslab
+  int sptr[FC3D_MAX_COLOURS + 1];  // slab range of each colour
+  const int* slab_nslot;
+  const long long* slab_off;
+  const int* perm;              // padded permuted row -> original contact, -1 pad
+  const int* dpos;              // slot position of the diagonal in the CSR row
+  const Real* W;
+  const int* col;
+  const Real* D;
+  const Real* q;
+  const Real* mu;
+  const Real* rho;
+  // state
+  Real* r;                      // AoS (npad + 1) * 3, entry npad is zero
+  Real* rpli;                   // npad
+  double* u;                    // AoS npad * 3 (FP64 full error output)
+  // reductions and control
+  double* partials;             // gridDim.x * 4
+  unsigned int* barrier;        // zeroed before launch
+  int* status;                  // FC3DGPU_STATUS_* bits
+  double* trace;                // per-sweep incremental error
+  int trace_cap;
+  int trace_base;               // index of this launch's first sweep in trace
+  // controls
+  int max_sweeps;
+  int mode;                     // 0: FP32 accelerator stop rule, 1: reference NSGS logic
+  double user_tol;
+  double local_tol;
+  double switch_tol;
+  int stall_window;
+  double norm_q;
+  int newton_max, pli_max, ls_max;
+  unsigned long long spin_limit;
+  // outputs (written by block 0, thread 0)
+  double* out;                  // [0] sweeps, [1] incr, [2] full error, [3] info, [4] working tol
+};
+
+}  // namespace fc3dgpu

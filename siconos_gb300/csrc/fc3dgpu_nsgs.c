@@ -1,0 +1,516 @@
+/* Host side of the GPU NSGS solver, in C: the registry-facing solve and
+ * set_default functions, option handling, the SBM -> block-CSR repack and
+ * the outputs the reference solver writes.  All device work goes through the
+ * device-resident C-ABI (fc3dgpu_ctx_*), implemented in CUDA.
+ *
+ * Reference behaviour mirrored here:
+ *   fc3d_driver validation and trivial case  fc3d_driver.c:51-145
+ *   fc3d_nsgs_set_default                     fc3d_nsgs.c:919-950
+ *   one-contact local solver defaults         onecontact.c:1037-1056, REGISTER :1139-1143
+ *   solver_options_initialize                 SolverOptions.c:44-96
+ *   outputs iparam[1] / dparam[1], info       fc3d_nsgs.c:894-900
+ *   per-iteration callback                    fc3d_nsgs.c:103-110 */
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "fc3dgpu.h"
+
+void fc3dgpu_set_error(const char *fmt, ...);
+int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx *ctx, double norm_q);
+
+#define FC3DGPU_CACHE_MAGIC 0x46433344u
+
+typedef struct {
+  unsigned magic;
+  fc3dgpu_ctx *ctx;
+  const void *M;
+  const void *sbm;
+  unsigned long long version;
+  int nc;
+  long long nnzb;
+  int colouring;
+} fc3dgpu_cache;
+
+static double now_s(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+/* calloc'd options as solver_options_initialize does */
+static SolverOptions *options_alloc(int id, int max_iter, double tol) {
+  SolverOptions *o = (SolverOptions *)calloc(1, sizeof(SolverOptions));
+  if (!o) return NULL;
+  o->solverId = id;
+  o->iSize = OPTIONS_PARAM_SIZE;
+  o->dSize = OPTIONS_PARAM_SIZE;
+  o->iparam = (int *)calloc(OPTIONS_PARAM_SIZE, sizeof(int));
+  o->dparam = (double *)calloc(OPTIONS_PARAM_SIZE, sizeof(double));
+  if (!o->iparam || !o->dparam) {
+    free(o->iparam);
+    free(o->dparam);
+    free(o);
+    return NULL;
+  }
+  o->iparam[SICONOS_IPARAM_MAX_ITER] = max_iter;
+  o->dparam[SICONOS_DPARAM_TOL] = tol;
+  o->dparam[SICONOS_DPARAM_RESIDU] = INFINITY;
+  o->filterOn = true;
+  o->isSet = true;
+  return o;
+}
+
+/* fc3d_onecontact_nsn_gp_set_default on registry defaults (100, 1e-14) */
+static SolverOptions *local_options_create(void) {
+  SolverOptions *o = options_alloc(SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID, 100, 1e-14);
+  if (!o) return NULL;
+  o->iparam[SICONOS_FRICTION_3D_NSN_RHO_STRATEGY] = SICONOS_FRICTION_3D_NSN_FORMULATION_RHO_STRATEGY_SPLIT_SPECTRAL_NORM;
+  o->dparam[SICONOS_FRICTION_3D_NSN_RHO] = 1.0;
+  o->iparam[SICONOS_FRICTION_3D_NSN_FORMULATION] = SICONOS_FRICTION_3D_NSN_FORMULATION_ALARTCURNIER_STD;
+  o->iparam[SICONOS_FRICTION_3D_NSN_LINESEARCH] = SICONOS_FRICTION_3D_NSN_LINESEARCH_GOLDSTEINPRICE;
+  o->iparam[SICONOS_FRICTION_3D_NSN_LINESEARCH_MAX_ITER] = 10;
+  o->iparam[SICONOS_FRICTION_3D_NSN_HYBRID_STRATEGY] = SICONOS_FRICTION_3D_NSN_HYBRID_STRATEGY_NSN_AND_PLI_NSN_LOOP;
+  o->iparam[SICONOS_FRICTION_3D_NSN_HYBRID_MAX_LOOP] = 1;
+  o->iparam[SICONOS_FRICTION_3D_NSN_HYBRID_MAX_ITER] = 100;
+  return o;
+}
+
+static void options_free(SolverOptions *o) {
+  if (!o) return;
+  for (size_t i = 0; i < o->numberOfInternalSolvers; i++)
+    if (o->internalSolvers) options_free(o->internalSolvers[i]);
+  free(o->internalSolvers);
+  free(o->iparam);
+  free(o->dparam);
+  free(o->dWork);
+  free(o->iWork);
+  free(o->solverData);
+  free(o);
+}
+
+void fc3dgpu_nsgs_set_default(SolverOptions *options) {
+  if (!options || !options->iparam || !options->dparam) return;
+  int *ip = options->iparam;
+  double *dp = options->dparam;
+  ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL;
+  ip[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_GIVEN_VALUE;
+  ip[SICONOS_FRICTION_3D_NSGS_SHUFFLE] = 0;
+  ip[SICONOS_FRICTION_3D_NSGS_SHUFFLE_SEED] = 0;
+  ip[SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] = 0;
+  ip[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] = 0;
+  ip[SICONOS_FRICTION_3D_NSGS_RELAXATION] = 0;
+  ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY] = 0;
+  dp[SICONOS_DPARAM_TOL] = 1e-4;
+  dp[SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO] = 10.0;
+  ip[SICONOS_FRICTION_3D_NSGS_PRINTING_LIKE_IPM] = 1;
+  ip[FC3DGPU_IPARAM_PRECISION] = 0;
+  ip[FC3DGPU_IPARAM_LANES] = 0;
+  ip[FC3DGPU_IPARAM_WARMSTART] = 0;
+  ip[FC3DGPU_IPARAM_COLOURING] = 0;
+  dp[FC3DGPU_DPARAM_SWITCH_TOL] = 1e-6;
+  dp[FC3DGPU_DPARAM_LOCAL_TOL32] = 1e-6;
+  dp[FC3DGPU_DPARAM_STALL] = 64;
+  if (options->numberOfInternalSolvers == 0 || !options->internalSolvers) {
+    options->numberOfInternalSolvers = 1;
+    options->internalSolvers = (SolverOptions **)calloc(1, sizeof(SolverOptions *));
+  } else {
+    options_free(options->internalSolvers[0]);
+  }
+  if (options->internalSolvers) options->internalSolvers[0] = local_options_create();
+}
+
+SolverOptions *fc3dgpu_options_create(void) {
+  SolverOptions *o = options_alloc(SICONOS_FRICTION_3D_NSGS_GPU, 1000, 1e-4);
+  if (!o) return NULL;
+  fc3dgpu_nsgs_set_default(o);
+  return o;
+}
+
+void fc3dgpu_options_delete(SolverOptions *options) {
+  if (!options) return;
+  fc3dgpu_release(options);
+  options_free(options);
+}
+
+void fc3dgpu_release(SolverOptions *options) {
+  if (!options || !options->solverData) return;
+  fc3dgpu_cache *c = (fc3dgpu_cache *)options->solverData;
+  if (c->magic != FC3DGPU_CACHE_MAGIC) return;
+  fc3dgpu_ctx_destroy(c->ctx);
+  free(c);
+  options->solverData = NULL;
+}
+
+/* Block-CSR view of W.  SBM storage is repacked (its blocks are scattered
+ * pointers, BlockCSRMatrix.cpp:249); dense storage keeps every 3x3 block
+ * holding a nonzero, plus the diagonal. */
+typedef struct {
+  int nc;
+  long long nnzb;
+  int64_t *rowptr;
+  int64_t *colidx;
+  double *blocks;
+} Bcsr;
+
+static void bcsr_free(Bcsr *b) {
+  free(b->rowptr);
+  free(b->colidx);
+  free(b->blocks);
+  memset(b, 0, sizeof(*b));
+}
+
+static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
+  memset(out, 0, sizeof(*out));
+  const int nc = P->numberOfContacts;
+  const NumericsMatrix *M = P->M;
+  out->nc = nc;
+  if (M->storageType == NM_SPARSE_BLOCK) {
+    const SparseBlockStructuredMatrix *S = M->matrix1;
+    if (!S || !S->index1_data || !S->index2_data || !S->block) {
+      fc3dgpu_set_error("SBM storage without data");
+      return NUMERICS_ERR_NULL_POINTER;
+    }
+    if ((int)S->blocknumber0 != nc || (int)S->blocknumber1 != nc) {
+      fc3dgpu_set_error("SBM has %zu x %zu block rows/columns, expected %d", S->blocknumber0, S->blocknumber1, nc);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < nc; i++) {
+      size_t lo = i ? S->blocksize0[i - 1] : 0, lo1 = i ? S->blocksize1[i - 1] : 0;
+      if (S->blocksize0[i] - lo != 3 || S->blocksize1[i] - lo1 != 3) {
+        fc3dgpu_set_error("SBM block %d is not 3x3", i);
+        return NUMERICS_ERR_INVALID_ARGUMENT;
+      }
+    }
+    const size_t nrows_filled = S->filled1 ? S->filled1 - 1 : 0;
+    const long long nnzb = (long long)(nrows_filled ? S->index1_data[nrows_filled] : 0);
+    out->nnzb = nnzb;
+    out->rowptr = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nc + 1));
+    out->colidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nnzb ? nnzb : 1));
+    out->blocks = (double *)malloc(sizeof(double) * 9 * (size_t)(nnzb ? nnzb : 1));
+    if (!out->rowptr || !out->colidx || !out->blocks) {
+      bcsr_free(out);
+      fc3dgpu_set_error("host allocation failed");
+      return NUMERICS_ERR_MEMORY;
+    }
+    for (int i = 0; i <= nc; i++)
+      out->rowptr[i] = (int64_t)((size_t)i <= nrows_filled ? S->index1_data[i] : S->index1_data[nrows_filled]);
+    for (long long k = 0; k < nnzb; k++) {
+      out->colidx[k] = (int64_t)S->index2_data[k];
+      memcpy(&out->blocks[9 * k], S->block[k], 9 * sizeof(double));
+    }
+    return 0;
+  }
+  if (M->storageType == NM_DENSE) {
+    const double *A = M->matrix0;
+    if (!A) {
+      fc3dgpu_set_error("dense storage without data");
+      return NUMERICS_ERR_NULL_POINTER;
+    }
+    const size_t n = 3 * (size_t)nc;
+    long long cnt = 0;
+    for (int bi = 0; bi < nc; bi++)
+      for (int bj = 0; bj < nc; bj++) {
+        int nz = (bi == bj);
+        for (int a = 0; a < 3 && !nz; a++)
+          for (int b = 0; b < 3 && !nz; b++) nz = A[(size_t)(3 * bj + b) * n + (size_t)(3 * bi + a)] != 0.0;
+        cnt += nz;
+      }
+    out->nnzb = cnt;
+    out->rowptr = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nc + 1));
+    out->colidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)cnt);
+    out->blocks = (double *)malloc(sizeof(double) * 9 * (size_t)cnt);
+    if (!out->rowptr || !out->colidx || !out->blocks) {
+      bcsr_free(out);
+      fc3dgpu_set_error("host allocation failed");
+      return NUMERICS_ERR_MEMORY;
+    }
+    long long k = 0;
+    for (int bi = 0; bi < nc; bi++) {
+      out->rowptr[bi] = k;
+      for (int bj = 0; bj < nc; bj++) {
+        int nz = (bi == bj);
+        for (int a = 0; a < 3 && !nz; a++)
+          for (int b = 0; b < 3 && !nz; b++) nz = A[(size_t)(3 * bj + b) * n + (size_t)(3 * bi + a)] != 0.0;
+        if (!nz) continue;
+        out->colidx[k] = bj;
+        for (int b = 0; b < 3; b++)
+          for (int a = 0; a < 3; a++) out->blocks[9 * k + 3 * b + a] = A[(size_t)(3 * bj + b) * n + (size_t)(3 * bi + a)];
+        k++;
+      }
+    }
+    out->rowptr[nc] = k;
+    return 0;
+  }
+  fc3dgpu_set_error("storage type %d is not supported (SBM or dense only)", (int)M->storageType);
+  return NUMERICS_ERR_NOT_IMPLEMENTED;
+}
+
+static int check_problem(const FrictionContactProblem *P, const double *r, const double *u) {
+  if (!P || !r || !u || !P->M || !P->q || !P->mu) {
+    fc3dgpu_set_error("null problem, reaction, velocity, M, q or mu");
+    return NUMERICS_ERR_NULL_POINTER;
+  }
+  if (P->numberOfContacts <= 0) {
+    fc3dgpu_set_error("Number of contacts must be positive");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (P->dimension != 3) {
+    fc3dgpu_set_error("dimension must be 3");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (P->M->size0 != 3 * P->numberOfContacts || P->M->size1 != 3 * P->numberOfContacts) {
+    fc3dgpu_set_error("M is %d x %d, expected %d", P->M->size0, P->M->size1, 3 * P->numberOfContacts);
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  for (int i = 0; i < P->numberOfContacts; i++)
+    if (!(P->mu[i] >= 0.0) || isinf(P->mu[i])) {
+      fc3dgpu_set_error("mu[%d] = %g is not a friction coefficient", i, P->mu[i]);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+  return 0;
+}
+
+static int check_options(const SolverOptions *o) {
+  if (!o || !o->iparam || !o->dparam || o->iSize < OPTIONS_PARAM_SIZE || o->dSize < OPTIONS_PARAM_SIZE) {
+    fc3dgpu_set_error("options are not set");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  const int *ip = o->iparam;
+  if (ip[SICONOS_FRICTION_3D_NSGS_SHUFFLE] != 0 || ip[SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] > 0 ||
+      ip[SICONOS_FRICTION_3D_NSGS_RELAXATION] != 0 || ip[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] != 0) {
+    fc3dgpu_set_error("GPU NSGS sweeps in colour order: shuffle, freezing, relaxation and filter are not supported");
+    return NUMERICS_ERR_NOT_IMPLEMENTED;
+  }
+  if (ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] != SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL) {
+    fc3dgpu_set_error("GPU NSGS supports ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL only");
+    return NUMERICS_ERR_NOT_IMPLEMENTED;
+  }
+  if (ip[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] != SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_GIVEN_VALUE) {
+    fc3dgpu_set_error("GPU NSGS supports INTERNAL_ERROR_STRATEGY_GIVEN_VALUE only");
+    return NUMERICS_ERR_NOT_IMPLEMENTED;
+  }
+  if (o->numberOfInternalSolvers < 1 || !o->internalSolvers || !o->internalSolvers[0]) {
+    fc3dgpu_set_error("The NSGS method needs options for the internal solvers");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  if (o->internalSolvers[0]->solverId != SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID) {
+    fc3dgpu_set_error("GPU NSGS runs the OC_NSN_GP_HYBRID local solver only");
+    return NUMERICS_ERR_NOT_IMPLEMENTED;
+  }
+  return 0;
+}
+
+static void params_from_options(const SolverOptions *o, fc3dgpu_params *p) {
+  fc3dgpu_params_default(p);
+  const int *ip = o->iparam;
+  const double *dp = o->dparam;
+  const SolverOptions *lo = o->internalSolvers[0];
+  p->tol = dp[SICONOS_DPARAM_TOL];
+  p->max_iter = ip[SICONOS_IPARAM_MAX_ITER];
+  p->precision = ip[FC3DGPU_IPARAM_PRECISION];
+  p->lanes = ip[FC3DGPU_IPARAM_LANES];
+  if (dp[FC3DGPU_DPARAM_SWITCH_TOL] > 0) p->switch_tol = dp[FC3DGPU_DPARAM_SWITCH_TOL];
+  if (dp[FC3DGPU_DPARAM_LOCAL_TOL32] > 0) p->local_tol32 = dp[FC3DGPU_DPARAM_LOCAL_TOL32];
+  if (dp[FC3DGPU_DPARAM_STALL] > 0) p->stall_window = (int)dp[FC3DGPU_DPARAM_STALL];
+  p->local_tol = lo->dparam[SICONOS_DPARAM_TOL];
+  p->newton_max = lo->iparam[SICONOS_IPARAM_MAX_ITER];
+  if (lo->iparam[SICONOS_FRICTION_3D_NSN_HYBRID_MAX_ITER] > 0) p->pli_max = lo->iparam[SICONOS_FRICTION_3D_NSN_HYBRID_MAX_ITER];
+  if (lo->iparam[SICONOS_FRICTION_3D_NSN_LINESEARCH_MAX_ITER] > 0) p->ls_max = lo->iparam[SICONOS_FRICTION_3D_NSN_LINESEARCH_MAX_ITER];
+}
+
+/* Get (or build) the cached device copy of W for this problem. */
+static int cached_ctx(FrictionContactProblem *P, SolverOptions *o, fc3dgpu_ctx **out) {
+  fc3dgpu_cache *c = (fc3dgpu_cache *)o->solverData;
+  if (c && c->magic != FC3DGPU_CACHE_MAGIC) {
+    fc3dgpu_set_error("options->solverData holds foreign data");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  const NumericsMatrix *M = P->M;
+  const void *sbm = M->storageType == NM_SPARSE_BLOCK ? (const void *)M->matrix1 : (const void *)M->matrix0;
+  unsigned long long ver =
+      M->storageType == NM_SPARSE_BLOCK && M->matrix1 ? M->matrix1->version.number : M->version.number;
+  const int kind = o->iparam[FC3DGPU_IPARAM_COLOURING];
+  if (c && c->ctx && c->M == (const void *)M && c->sbm == sbm && c->version == ver && c->nc == P->numberOfContacts &&
+      c->colouring == kind && ver != 0) {
+    *out = c->ctx;
+    return 0;
+  }
+  if (!c) {
+    c = (fc3dgpu_cache *)calloc(1, sizeof(fc3dgpu_cache));
+    if (!c) {
+      fc3dgpu_set_error("host allocation failed");
+      return NUMERICS_ERR_MEMORY;
+    }
+    c->magic = FC3DGPU_CACHE_MAGIC;
+    o->solverData = c;
+  }
+  if (!c->ctx) {
+    c->ctx = fc3dgpu_ctx_create(0);
+    if (!c->ctx) return NUMERICS_ERR_NOT_IMPLEMENTED;
+  }
+  Bcsr b;
+  int rc = bcsr_from_problem(P, &b);
+  if (rc) return rc;
+  rc = fc3dgpu_ctx_set_W(c->ctx, b.nc, b.rowptr, b.colidx, b.blocks, kind);
+  c->nnzb = b.nnzb;
+  bcsr_free(&b);
+  if (rc) {
+    c->M = NULL;
+    return rc;
+  }
+  c->M = M;
+  c->sbm = sbm;
+  c->version = ver;
+  c->nc = P->numberOfContacts;
+  c->colouring = kind;
+  *out = c->ctx;
+  return 0;
+}
+
+int fc3dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velocity, SolverOptions *options) {
+  int rc = check_problem(problem, reaction, velocity);
+  if (rc) return rc;
+  rc = check_options(options);
+  if (rc) return rc;
+  const double t0 = now_s();
+  fc3dgpu_ctx *ctx = NULL;
+  rc = cached_ctx(problem, options, &ctx);
+  if (rc) return rc;
+  rc = fc3dgpu_ctx_set_q_mu(ctx, problem->q, problem->mu);
+  if (!rc) rc = fc3dgpu_ctx_set_r(ctx, reaction);
+  if (rc) return rc;
+  fc3dgpu_params p;
+  params_from_options(options, &p);
+  fc3dgpu_stats st;
+  const double t1 = now_s();
+  rc = fc3dgpu_ctx_solve(ctx, &p, &st);
+  const double t2 = now_s();
+  if (rc) return rc;
+  rc = fc3dgpu_ctx_get_r_u(ctx, reaction, velocity);
+  if (rc) return rc;
+  const double t3 = now_s();
+  int *ip = options->iparam;
+  double *dp = options->dparam;
+  ip[SICONOS_IPARAM_ITER_DONE] = st.sweeps32 + st.sweeps64;
+  dp[SICONOS_DPARAM_RESIDU] = st.error;
+  ip[FC3DGPU_IPARAM_SWEEPS_FP32] = st.sweeps32;
+  ip[FC3DGPU_IPARAM_SWEEPS_FP64] = st.sweeps64;
+  ip[FC3DGPU_IPARAM_COLOURS] = st.colours;
+  dp[SICONOS_DPARAM_TIME_BEFORE_LOOP] = t1 - t0;
+  dp[SICONOS_DPARAM_TIME_IN_LOOP] = t2 - t1;
+  dp[SICONOS_DPARAM_TIME_AFTER_LOOP] = t3 - t2;
+  dp[FC3DGPU_DPARAM_MS_SWEEP32] = st.sweeps32 ? st.ms_fp32 / st.sweeps32 : 0.0;
+  dp[FC3DGPU_DPARAM_MS_SWEEP64] = st.sweeps64 ? st.ms_fp64 / st.sweeps64 : 0.0;
+  dp[FC3DGPU_DPARAM_MS_SOLVE] = st.ms_total;
+  dp[FC3DGPU_DPARAM_INCR_ERROR] = st.incr_error;
+  if (options->callback && options->callback->collectStatsIteration) {
+    /* The sweeps run on the device without host round trips, so the
+     * per-iteration callback is replayed after the solve: one call per
+     * sweep with that sweep's incremental error and the final iterate. */
+    int n = st.sweeps32 + st.sweeps64;
+    double *tr = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    if (tr) {
+      int m = fc3dgpu_ctx_trace(ctx, tr, n);
+      for (int k = 0; k < m; k++)
+        options->callback->collectStatsIteration(options->callback->env, (size_t)(3 * problem->numberOfContacts),
+                                                 reaction, velocity, tr[k], NULL);
+      free(tr);
+    }
+  }
+  return st.info;
+}
+
+/* fc3d_driver (fc3d_driver.c:77-145) for this solver id: validation,
+ * outputs reset, trivial take-off case (all q_n >= -DBL_EPSILON gives r = 0,
+ * u = q, fc3d_driver.c:51-71), dispatch, [WARN] on a non-zero status. */
+int fc3dgpu_driver(FrictionContactProblem *problem, double *reaction, double *velocity, SolverOptions *options) {
+  int rc = check_problem(problem, reaction, velocity);
+  if (rc) return rc;
+  if (!options || !options->iparam || !options->dparam) {
+    fc3dgpu_set_error("options are not set");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  options->iparam[SICONOS_IPARAM_ITER_DONE] = 0;
+  options->dparam[SICONOS_DPARAM_RESIDU] = 0.0;
+  const int nc = problem->numberOfContacts;
+  int trivial = 1;
+  for (int i = 0; i < nc; i++)
+    if (problem->q[3 * i] < -DBL_EPSILON) {
+      trivial = 0;
+      break;
+    }
+  if (trivial) {
+    for (int i = 0; i < 3 * nc; i++) {
+      velocity[i] = problem->q[i];
+      reaction[i] = 0.0;
+    }
+    return NUMERICS_OK;
+  }
+  if (options->solverId != SICONOS_FRICTION_3D_NSGS_GPU) {
+    fc3dgpu_set_error("Solver ID not found in registry");
+    return NUMERICS_ERR_INVALID_SOLVER;
+  }
+  rc = fc3dgpu_nsgs(problem, reaction, velocity, options);
+  if (rc != NUMERICS_OK) fprintf(stderr, "[WARN] fc3dgpu_driver: solver returned status %d\n", rc);
+  return rc;
+}
+
+int fc3dgpu_nsgs_solve_wrap(void *problem, double *reaction, double *velocity, SolverOptions *options) {
+  return fc3dgpu_nsgs((FrictionContactProblem *)problem, reaction, velocity, options);
+}
+
+int fc3dgpu_nsgs_init_wrap(void *problem, SolverOptions *options) {
+  (void)problem;
+  (void)options;
+  return NUMERICS_OK;
+}
+
+void fc3dgpu_nsgs_free_wrap(void *problem, SolverOptions *options) {
+  /* the device copy of W stays cached in options->solverData across
+   * fc3d_driver calls; fc3dgpu_release frees it */
+  (void)problem;
+  (void)options;
+}
+
+int fc3dgpu_compute_error(FrictionContactProblem *problem, double *reaction, double *velocity, double tolerance,
+                          double norm_q, double *error) {
+  int rc = check_problem(problem, reaction, velocity);
+  if (rc) return rc;
+  if (!error) return NUMERICS_ERR_NULL_POINTER;
+  fc3dgpu_ctx *ctx = fc3dgpu_ctx_create(0);
+  if (!ctx) return NUMERICS_ERR_NOT_IMPLEMENTED;
+  Bcsr b;
+  rc = bcsr_from_problem(problem, &b);
+  if (!rc) {
+    rc = fc3dgpu_ctx_set_W(ctx, b.nc, b.rowptr, b.colidx, b.blocks, 0);
+    bcsr_free(&b);
+  }
+  if (!rc) rc = fc3dgpu_ctx_set_q_mu(ctx, problem->q, problem->mu);
+  if (!rc) rc = fc3dgpu_ctx_set_r(ctx, reaction);
+  if (!rc) rc = fc3dgpu_ctx_set_norm_q(ctx, norm_q);
+  if (!rc) rc = fc3dgpu_ctx_compute_error(ctx, error);
+  if (!rc) rc = fc3dgpu_ctx_get_r_u(ctx, NULL, velocity);
+  fc3dgpu_ctx_destroy(ctx);
+  if (rc) return rc;
+  return *error > tolerance ? 1 : 0;
+}
+
+int fc3dgpu_nsgs_batch(int nproblems, FrictionContactProblem **problems, double **reactions, double **velocities,
+                       SolverOptions *options, int *info) {
+  if (nproblems < 0 || (nproblems > 0 && (!problems || !reactions || !velocities || !info))) {
+    fc3dgpu_set_error("fc3dgpu_nsgs_batch: invalid argument");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  int worst = 0;
+  for (int k = 0; k < nproblems; k++) {
+    fc3dgpu_release(options);
+    info[k] = fc3dgpu_nsgs(problems[k], reactions[k], velocities[k], options);
+    if (info[k] < worst) worst = info[k];
+  }
+  fc3dgpu_release(options);
+  return worst < 0 ? worst : 0;
+}

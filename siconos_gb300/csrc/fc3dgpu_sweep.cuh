@@ -1,0 +1,336 @@
+// Persistent coloured NSGS kernel.
+//
+// One cooperative launch runs every sweep of a solve: for each colour, warps
+// take (slab, round) work units; T lanes own one contact, form the
+// off-diagonal block-row product q_i + sum_j W_ij r_j from coalesced
+// slot-major loads (fc3d_local_problem_compute_q, fc3d_local_problem_tools.c:
+// 48-63, and SBM_row_prod_no_diag_3x3, SparseBlockMatrix.c:1431-1490), then
+// run the local solver in registers; a bounded grid barrier separates colours
+// (contacts of one colour share no body, so their W blocks are zero and the
+// order inside a colour does not matter).  After the last colour the light
+// error sqrt(sum |dr|^2)/|r| (fc3d_nsgs.c:80-96) is reduced in a fixed
+// order, so every block takes the same decision.  In reference mode the
+// kernel also evaluates fc3d_compute_error (fc3d_compute_error.c:70-122) and
+// the tolerance manager (tolerance_manager.h:203-225) on the device, exactly
+// when fc3d_nsgs would (fc3d_nsgs.c:496-534, :839-851, :877-895).
+#pragma once
+#include <cfloat>
+#include <cuda_runtime.h>
+
+#include "fc3dgpu_layout.cuh"
+#include "fc3dgpu_local.cuh"
+
+namespace fc3dgpu {
+
+#define FC3D_BLOCK 256
+#define FC3D_RSTRIDE 4
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier with a poll limit.  On expiry the block records
+// FC3DGPU_STATUS_BARRIER_TIMEOUT and returns false; its caller leaves the
+// kernel, and every other block then times out at its next barrier.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned& epoch, unsigned long long limit, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    epoch++;
+    const unsigned target = epoch * gridDim.x;
+    __threadfence();
+    atomicAdd(bar, 1u);
+    unsigned long long n = 0;
+    int ok = 1;
+    while (ld_acquire_u32(bar) < target) {
+      if (++n > limit) {
+        ok = 0;
+        atomicOr(status, 1);
+        break;
+      }
+      if (n > 64) __nanosleep(64);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <int N>
+__device__ __forceinline__ void block_sum(double v[N], double* out_partials) {
+  __shared__ double sh[FC3D_BLOCK / 32][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    double x = v[i];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[w][i] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < N) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k][threadIdx.x];
+    out_partials[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+// Sum slot k of every block's partials in a fixed order; every block gets
+// the same value.  Called after a grid barrier.
+template <int N>
+__device__ __forceinline__ void grid_sum(const double* partials, int slot0, double out[N]) {
+  __shared__ double res[8];
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      double s = 0.0;
+      for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&partials[b * 8 + slot0 + i]);
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) res[i] = s;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < N; i++) out[i] = res[i];
+  __syncthreads();
+}
+
+template <typename Real>
+__device__ __forceinline__ void load_r3(const Real* r, int p, Real out[3]);
+template <>
+__device__ __forceinline__ void load_r3<float>(const float* r, int p, float out[3]) {
+  float4 v = __ldcg(reinterpret_cast<const float4*>(r) + p);
+  out[0] = v.x;
+  out[1] = v.y;
+  out[2] = v.z;
+}
+template <>
+__device__ __forceinline__ void load_r3<double>(const double* r, int p, double out[3]) {
+  const double2* q = reinterpret_cast<const double2*>(r) + 2 * (size_t)p;
+  double2 a = __ldcg(q), b = __ldcg(q + 1);
+  out[0] = a.x;
+  out[1] = a.y;
+  out[2] = b.x;
+}
+
+template <typename Real, int T>
+__device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab, int round, int lane, Real ltol,
+                                             double& dr2, double& rr2) {
+  constexpr int CPR = 32 / T;
+  const int g = lane / T, j = lane % T;
+  const int k = round * CPR + g;
+  const int p = slab * FC3D_SLAB + k;
+  const long long base = a.slab_off[slab];
+  const int ns = a.slab_nslot[slab];
+  const size_t qi = (size_t)slab * 3 * FC3D_SLAB + k;
+  const Real q0 = a.q[qi], q1 = a.q[qi + FC3D_SLAB], q2 = a.q[qi + 2 * FC3D_SLAB];
+  Real acc[3];
+  if (T == 1) {
+    acc[0] = q0;
+    acc[1] = q1;
+    acc[2] = q2;
+  } else {
+    acc[0] = 0;
+    acc[1] = 0;
+    acc[2] = 0;
+  }
+  for (int s = j; s < ns; s += T) {
+    const size_t sl = (size_t)(base + s);
+    const int pj = __ldg(&a.col[sl * FC3D_SLAB + k]);
+    const Real* w = a.W + sl * 9 * FC3D_SLAB + k;
+    Real wv[9], rv[3];
+#pragma unroll
+    for (int e = 0; e < 9; e++) wv[e] = __ldg(&w[e * FC3D_SLAB]);
+    load_r3<Real>(a.r, pj, rv);
+    mvp3x3(wv, rv, acc);
+  }
+  if (T > 1) {
+#pragma unroll
+    for (int o = T / 2; o >= 1; o >>= 1) {
+      acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], o);
+      acc[1] += __shfl_xor_sync(0xffffffffu, acc[1], o);
+      acc[2] += __shfl_xor_sync(0xffffffffu, acc[2], o);
+    }
+    acc[0] = q0 + acc[0];
+    acc[1] = q1 + acc[1];
+    acc[2] = q2 + acc[2];
+  }
+  if (__ldg(&a.perm[p]) < 0) return;
+  LocalProblem<Real> L;
+#pragma unroll
+  for (int e = 0; e < 9; e++) L.M[e] = __ldg(&a.D[((size_t)slab * 9 + e) * FC3D_SLAB + k]);
+  L.q[0] = acc[0];
+  L.q[1] = acc[1];
+  L.q[2] = acc[2];
+  L.mu = __ldg(&a.mu[(size_t)slab * FC3D_SLAB + k]);
+  L.rhoN = __ldg(&a.rho[((size_t)slab * 2) * FC3D_SLAB + k]);
+  L.rhoT = __ldg(&a.rho[((size_t)slab * 2 + 1) * FC3D_SLAB + k]);
+  L.rho_pli = a.rpli[p];
+  L.tol = ltol;
+  L.newton_max = a.newton_max;
+  L.pli_max = a.pli_max;
+  L.ls_max = a.ls_max;
+  Real ro[3], rn[3];
+  load_r3<Real>(a.r, p, ro);
+  rn[0] = ro[0];
+  rn[1] = ro[1];
+  rn[2] = ro[2];
+  local_solve(L, rn);
+  if (j == 0) {
+    Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
+    rp[0] = rn[0];
+    rp[1] = rn[1];
+    rp[2] = rn[2];
+    a.rpli[p] = L.rho_pli;
+    const double d0 = (double)ro[0] - (double)rn[0], d1 = (double)ro[1] - (double)rn[1],
+                 d2 = (double)ro[2] - (double)rn[2];
+    dr2 += d0 * d0 + d1 * d1 + d2 * d2;
+    rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+  }
+}
+
+// u = q + W r for every row in CSR block order (diagonal at its own slot
+// position, SBM_gemv_3x3, SparseBlockMatrix.c:360-419) and the partial sums
+// of the squared natural-map error, |u|^2 and |r|^2.  FP64 only.
+template <typename Real>
+__device__ __forceinline__ void full_error_rows(const SweepArgs<Real>& a, double v[3]) {
+  v[0] = v[1] = v[2] = 0.0;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int p = tid; p < a.npad; p += nth) {
+    if (__ldg(&a.perm[p]) < 0) continue;
+    const int slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
+    const long long base = a.slab_off[slab];
+    const int ns = a.slab_nslot[slab];
+    const int dp = __ldg(&a.dpos[p]);
+    const size_t qi = (size_t)slab * 3 * FC3D_SLAB + k;
+    Real u[3] = {a.q[qi], a.q[qi + FC3D_SLAB], a.q[qi + 2 * FC3D_SLAB]};
+    Real rp[3], D[9];
+    load_r3<Real>(a.r, p, rp);
+#pragma unroll
+    for (int e = 0; e < 9; e++) D[e] = __ldg(&a.D[((size_t)slab * 9 + e) * FC3D_SLAB + k]);
+    for (int s = 0; s < ns; s++) {
+      if (s == dp) mvp3x3(D, rp, u);
+      const size_t sl = (size_t)(base + s);
+      const int pj = __ldg(&a.col[sl * FC3D_SLAB + k]);
+      const Real* w = a.W + sl * 9 * FC3D_SLAB + k;
+      Real wv[9], rv[3];
+#pragma unroll
+      for (int e = 0; e < 9; e++) wv[e] = __ldg(&w[e * FC3D_SLAB]);
+      load_r3<Real>(a.r, pj, rv);
+      mvp3x3(wv, rv, u);
+    }
+    if (dp >= ns) mvp3x3(D, rp, u);
+    const Real mu = __ldg(&a.mu[(size_t)slab * FC3D_SLAB + k]);
+    v[0] += (double)unitary_error2(rp, u, mu);
+    v[1] += (double)u[0] * u[0] + (double)u[1] * u[1] + (double)u[2] * u[2];
+    v[2] += (double)rp[0] * rp[0] + (double)rp[1] * rp[1] + (double)rp[2] * rp[2];
+    if (a.u) {
+      a.u[3 * (size_t)p + 0] = u[0];
+      a.u[3 * (size_t)p + 1] = u[1];
+      a.u[3 * (size_t)p + 2] = u[2];
+    }
+  }
+}
+
+template <typename Real>
+__device__ __forceinline__ bool full_error_phase(const SweepArgs<Real>& a, int slot0, unsigned& epoch,
+                                                 double& full) {
+  double v[3];
+  full_error_rows(a, v);
+  block_sum<3>(v, a.partials + blockIdx.x * 8 + slot0);
+  if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) return false;
+  double s[3];
+  grid_sum<3>(a.partials, slot0, s);
+  double e = sqrt(s[0]);
+  const double scal = fmax(a.norm_q, fmax(sqrt(s[2]), sqrt(s[1])));
+  if (fabs(scal) > DBL_EPSILON) e /= scal;
+  full = e;
+  return true;
+}
+
+template <typename Real, int T>
+__global__ void __launch_bounds__(FC3D_BLOCK) nsgs_kernel(const SweepArgs<Real> a) {
+  const int lane = threadIdx.x & 31;
+  const int nwb = blockDim.x >> 5;
+  const int gw = blockIdx.x * nwb + (threadIdx.x >> 5), tw = gridDim.x * nwb;
+  unsigned epoch = 0;
+  double working = a.user_tol, local_tol = a.local_tol;
+  double incr = INFINITY, full = INFINITY, best = INFINITY;
+  int sweep = 0, best_sweep = 0;
+  bool converged = false;
+  while (sweep < a.max_sweeps) {
+    sweep++;
+    double acc[2] = {0.0, 0.0};
+    for (int c = 0; c < a.ncol; c++) {
+      const int s0 = a.sptr[c], nunits = (a.sptr[c + 1] - s0) * T;
+      for (int u = gw; u < nunits; u += tw) process_unit<Real, T>(a, s0 + u / T, u % T, lane, (Real)local_tol, acc[0], acc[1]);
+      if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
+      if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) return;
+    }
+    double s[2];
+    grid_sum<2>(a.partials, 0, s);
+    incr = sqrt(s[0]);
+    const double nr = sqrt(s[1]);
+    if (fabs(nr) > DBL_EPSILON) incr /= nr;
+    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0 && a.trace_base + sweep - 1 < a.trace_cap)
+      a.trace[a.trace_base + sweep - 1] = incr;
+    bool stop = false;
+    if (a.mode == 1) {
+      // check_convergence_with_adaptation (fc3d_nsgs.c:496-534)
+      if (incr < working) {
+        if (!full_error_phase(a, 2, epoch, full)) return;
+        if (full <= a.user_tol) {
+          converged = true;
+          stop = true;
+        } else if (incr < 1e-15 || incr < DBL_EPSILON * 100.0) {
+          local_tol = fmax(local_tol / 100.0, DBL_EPSILON * 1e-6);
+        } else if (full > 0.0 && incr > 0.0) {
+          double nt = (incr / full) * a.user_tol;
+          const double user_min = a.user_tol * 1e-6, floor_tol = DBL_EPSILON * 1e-6;
+          const double mint = user_min > floor_tol ? user_min : floor_tol;
+          if (nt < mint) nt = mint;
+          if (nt > 0.0 && nt < working) working = nt;
+        }
+        if (!(working > 0.0)) stop = true;
+      }
+    } else {
+      if (!(incr == incr)) {
+        if (threadIdx.x == 0) atomicOr(a.status, 2);
+        stop = true;
+      }
+      if (incr < a.switch_tol) stop = true;
+      if (incr < 0.99 * best) {
+        best = incr;
+        best_sweep = sweep;
+      } else if (a.stall_window > 0 && sweep - best_sweep >= a.stall_window) {
+        stop = true;
+      }
+    }
+    if (stop) break;
+  }
+  int info = 1;
+  if (a.mode == 1) {
+    // final full error (fc3d_nsgs.c:877-895)
+    if (!full_error_phase(a, 5, epoch, full)) return;
+    info = full < a.user_tol ? 0 : 1;
+    if (sweep == a.max_sweeps && info > 0) info = -20;
+  } else {
+    info = converged ? 0 : 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.out[0] = sweep;
+    a.out[1] = incr;
+    a.out[2] = full;
+    a.out[3] = info;
+    a.out[4] = working;
+    a.out[5] = local_tol;
+  }
+}
+
+}  // namespace fc3dgpu

@@ -1,0 +1,55 @@
+// double instantiations of the persistent coloured NSGS kernel.
+#include "fc3dgpu_sweep.cuh"
+#include "fc3dgpu_sweep_launch.h"
+
+namespace fc3dgpu {
+
+template <int T>
+static cudaError_t launch_t(const SweepArgs<double>& a, int max_grid, cudaStream_t s, int* grid) {
+  auto kern = nsgs_kernel<double, T>;
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FC3D_BLOCK, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int g = nsm * per_sm;
+  if (max_grid > 0 && g > max_grid) g = max_grid;
+  if (g > 1024) g = 1024;
+  *grid = g;
+  void* args[] = {(void*)&a};
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(g), dim3(FC3D_BLOCK), args, 0, s);
+}
+
+template <int T>
+static int grid_t() {
+  int dev = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nsgs_kernel<double, T>, FC3D_BLOCK, 0);
+  return nsm * per_sm;
+}
+
+cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid, cudaStream_t s, int* grid) {
+  switch (lanes) {
+    case 1: return launch_t<1>(a, max_grid, s, grid);
+    case 2: return launch_t<2>(a, max_grid, s, grid);
+    case 4: return launch_t<4>(a, max_grid, s, grid);
+    case 8: return launch_t<8>(a, max_grid, s, grid);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int sweep_grid_f64(int lanes) {
+  switch (lanes) {
+    case 1: return grid_t<1>();
+    case 2: return grid_t<2>();
+    case 4: return grid_t<4>();
+    case 8: return grid_t<8>();
+    default: return 0;
+  }
+}
+
+}  // namespace fc3dgpu

@@ -1,0 +1,17 @@
+// Launchers of the persistent sweep kernel, one translation unit per
+// precision: the FP64 unit is compiled with --fmad=false so its arithmetic
+// is the CPU restatement's, the FP32 unit keeps FMA contraction.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fc3dgpu_layout.cuh"
+
+namespace fc3dgpu {
+// Cooperative launch with as many resident blocks as fit (capped by
+// max_grid when > 0).  Returns the cudaError_t of the launch; *grid gets the
+// number of blocks.
+cudaError_t launch_sweep_f32(const SweepArgs<float>& a, int lanes, int max_grid, cudaStream_t s, int* grid);
+cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid, cudaStream_t s, int* grid);
+int sweep_grid_f32(int lanes);
+int sweep_grid_f64(int lanes);
+}  // namespace fc3dgpu

@@ -1,0 +1,88 @@
+"""Device-resident solver handle over the ``fc3dgpu_ctx_*`` C-ABI: upload a
+problem once, solve many times with inputs already in HBM."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import numerics as sn
+
+
+class DeviceSolver:
+    def __init__(self, device: int = 0):
+        self.L = sn.lib()
+        self.ctx = self.L.fc3dgpu_ctx_create(device)
+        if not self.ctx:
+            raise RuntimeError("fc3dgpu_ctx_create failed: " + sn.last_error())
+        self.nc = 0
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} failed ({rc}): {sn.last_error()}")
+
+    def set_W(self, nc, rowptr, colidx, blocks, colouring: int = 0):
+        self._check(self.L.fc3dgpu_ctx_set_W(self.ctx, nc, np.ascontiguousarray(rowptr, np.int64),
+                                             np.ascontiguousarray(colidx, np.int64),
+                                             np.ascontiguousarray(blocks, np.float64).reshape(-1), colouring),
+                    "set_W")
+        self.nc = nc
+
+    def set_q_mu(self, q, mu):
+        self._check(self.L.fc3dgpu_ctx_set_q_mu(self.ctx, np.ascontiguousarray(q, np.float64),
+                                                np.ascontiguousarray(mu, np.float64)), "set_q_mu")
+
+    def set_r(self, r):
+        self._check(self.L.fc3dgpu_ctx_set_r(self.ctx, np.ascontiguousarray(r, np.float64)), "set_r")
+
+    def load(self, scene, colouring: int = 0, r0=None):
+        self.set_W(scene.nc, scene.rowptr, scene.colidx, scene.blocks, colouring)
+        self.set_q_mu(scene.q, scene.mu)
+        self.set_r(np.zeros(3 * scene.nc) if r0 is None else r0)
+
+    @staticmethod
+    def params(**kw) -> sn.FC3DGPUParams:
+        p = sn.FC3DGPUParams()
+        sn.lib().fc3dgpu_params_default(C.byref(p))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+    def solve(self, **kw) -> dict:
+        p = self.params(**kw)
+        st = sn.FC3DGPUStats()
+        rc = self.L.fc3dgpu_ctx_solve(self.ctx, C.byref(p), C.byref(st))
+        self._check(rc, "solve")
+        return st.as_dict()
+
+    def get(self):
+        r = np.zeros(3 * self.nc)
+        u = np.zeros(3 * self.nc)
+        self._check(self.L.fc3dgpu_ctx_get_r_u(self.ctx, r.ctypes.data, u.ctypes.data), "get_r_u")
+        return r, u
+
+    def compute_error(self) -> float:
+        e = C.c_double()
+        self._check(self.L.fc3dgpu_ctx_compute_error(self.ctx, C.byref(e)), "compute_error")
+        return e.value
+
+    def trace(self, cap: int = 100000) -> np.ndarray:
+        out = np.zeros(cap)
+        n = self.L.fc3dgpu_ctx_trace(self.ctx, out, cap)
+        return out[:max(n, 0)].copy()
+
+    def colours(self) -> np.ndarray:
+        out = np.zeros(self.nc, np.int32)
+        self.L.fc3dgpu_ctx_colours(self.ctx, out)
+        return out
+
+    def close(self):
+        if self.ctx:
+            self.L.fc3dgpu_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,403 @@
+"""Python mirror of the reference's ``siconos.numerics`` friction-contact API
+for the GPU solver (numerics/python/friction_contact_pybind11.cpp:165,525).
+
+Names, argument meaning and return conventions follow the reference:
+
+* ``FrictionContactProblem(dim, nc, M, q, mu)`` -- ``M`` a dense
+  Fortran-ordered numpy matrix or a :class:`SparseBlockMatrix` (3x3 block
+  CSR); ``q`` and ``mu`` are shared, not copied, as the reference's tests
+  check with ``np.may_share_memory``;
+* ``SolverOptions(solver_id)`` -- ``iparam`` / ``dparam`` are numpy views on
+  the C arrays;
+* ``fc3d_driver(problem, reaction, velocity, options)`` returns ``info``
+  (0 converged, negative ``NUMERICS_ERR_*`` codes on invalid input);
+* ``fc3d_compute_error(problem, reaction, velocity, tol, norm_q)`` returns
+  ``(info, error)``.
+
+Everything runs through the C-ABI of ``libfc3dgpu.so`` (``include/fc3dgpu.h``);
+there is no Python or CPU implementation of the solve.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libfc3dgpu.so"
+
+SICONOS_FRICTION_3D_NSGS = 500
+SICONOS_FRICTION_3D_NSGS_GPU = 531
+SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID = 565
+SICONOS_IPARAM_MAX_ITER = 0
+SICONOS_IPARAM_ITER_DONE = 1
+SICONOS_DPARAM_TOL = 0
+SICONOS_DPARAM_RESIDU = 1
+FC3DGPU_IPARAM_PRECISION = 23
+FC3DGPU_IPARAM_LANES = 24
+FC3DGPU_IPARAM_WARMSTART = 25
+FC3DGPU_IPARAM_COLOURING = 26
+FC3DGPU_IPARAM_SWEEPS_FP32 = 27
+FC3DGPU_IPARAM_SWEEPS_FP64 = 28
+FC3DGPU_IPARAM_COLOURS = 29
+FC3DGPU_DPARAM_SWITCH_TOL = 23
+FC3DGPU_DPARAM_LOCAL_TOL32 = 24
+FC3DGPU_DPARAM_STALL = 25
+FC3DGPU_DPARAM_MS_SWEEP32 = 26
+FC3DGPU_DPARAM_MS_SWEEP64 = 27
+FC3DGPU_DPARAM_MS_SOLVE = 28
+FC3DGPU_DPARAM_INCR_ERROR = 29
+NUMERICS_OK = 0
+NUMERICS_ERR_NULL_POINTER = -1
+NUMERICS_ERR_INVALID_ARGUMENT = -2
+NUMERICS_ERR_INVALID_OPTION = -3
+NUMERICS_ERR_INVALID_SOLVER = -4
+NUMERICS_ERR_NOT_IMPLEMENTED = -5
+NUMERICS_ERR_MAX_ITER = -20
+NM_DENSE, NM_SPARSE_BLOCK = 0, 1
+OPTIONS_PARAM_SIZE = 30
+
+_DP = C.POINTER(C.c_double)
+_SZP = C.POINTER(C.c_size_t)
+
+
+class NumericsDataVersion(C.Structure):
+    _fields_ = [("number", C.c_uint64)]
+
+
+class SparseBlockStructuredMatrix(C.Structure):
+    _fields_ = [("nbblocks", C.c_size_t), ("block", C.POINTER(_DP)), ("blocknumber0", C.c_size_t),
+                ("blocknumber1", C.c_size_t), ("blocksize0", _SZP), ("blocksize1", _SZP), ("filled1", C.c_size_t),
+                ("filled2", C.c_size_t), ("index1_data", _SZP), ("index2_data", _SZP),
+                ("diagonal_blocks", _SZP), ("version", NumericsDataVersion)]
+
+
+class NumericsMatrix(C.Structure):
+    _fields_ = [("storageType", C.c_int), ("size0", C.c_int), ("size1", C.c_int), ("matrix0", _DP),
+                ("matrix1", C.POINTER(SparseBlockStructuredMatrix)), ("matrix2", C.c_void_p),
+                ("internalData", C.c_void_p), ("version", NumericsDataVersion), ("destructible", C.c_void_p)]
+
+
+class _FCP(C.Structure):
+    _fields_ = [("dimension", C.c_int), ("numberOfContacts", C.c_int), ("M", C.POINTER(NumericsMatrix)),
+                ("q", _DP), ("mu", _DP)]
+
+
+CALLBACK_T = C.CFUNCTYPE(None, C.c_void_p, C.c_size_t, _DP, _DP, C.c_double, C.c_void_p)
+
+
+class Callback(C.Structure):
+    _fields_ = [("env", C.c_void_p), ("collectStatsIteration", CALLBACK_T)]
+
+
+class _SO(C.Structure):
+    pass
+
+
+_SO._fields_ = [("solverId", C.c_int), ("isSet", C.c_bool), ("iSize", C.c_size_t), ("iparam", C.POINTER(C.c_int)),
+                ("dSize", C.c_size_t), ("dparam", _DP), ("filterOn", C.c_bool), ("dWorkSize", C.c_size_t),
+                ("dWork", _DP), ("iWorkSize", C.c_size_t), ("iWork", C.POINTER(C.c_int)),
+                ("numberOfInternalSolvers", C.c_size_t), ("internalSolvers", C.POINTER(C.POINTER(_SO))),
+                ("callback", C.POINTER(Callback)), ("solverParameters", C.c_void_p), ("solverData", C.c_void_p)]
+
+
+class FC3DGPUParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precision", C.c_int), ("lanes", C.c_int),
+                ("switch_tol", C.c_double), ("stall_window", C.c_int), ("local_tol", C.c_double),
+                ("local_tol32", C.c_double), ("newton_max", C.c_int), ("pli_max", C.c_int), ("ls_max", C.c_int),
+                ("fp32_only", C.c_int)]
+
+
+class FC3DGPUStats(C.Structure):
+    _fields_ = [("info", C.c_int), ("status", C.c_int), ("sweeps32", C.c_int), ("sweeps64", C.c_int),
+                ("colours", C.c_int), ("lanes", C.c_int), ("grid", C.c_int), ("incr_error", C.c_double),
+                ("error", C.c_double), ("ms_total", C.c_double), ("ms_fp32", C.c_double), ("ms_fp64", C.c_double),
+                ("bytes_sweep32", C.c_double), ("bytes_sweep64", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+_I64 = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_I32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_F64 = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+# exported C-ABI symbols: name -> (restype, argtypes)
+ABI = {
+    "fc3dgpu_nsgs": (C.c_int, [C.POINTER(_FCP), _DP, _DP, C.POINTER(_SO)]),
+    "fc3dgpu_nsgs_solve_wrap": (C.c_int, [C.c_void_p, _DP, _DP, C.POINTER(_SO)]),
+    "fc3dgpu_nsgs_init_wrap": (C.c_int, [C.c_void_p, C.POINTER(_SO)]),
+    "fc3dgpu_nsgs_free_wrap": (None, [C.c_void_p, C.POINTER(_SO)]),
+    "fc3dgpu_driver": (C.c_int, [C.POINTER(_FCP), _DP, _DP, C.POINTER(_SO)]),
+    "fc3dgpu_nsgs_set_default": (None, [C.POINTER(_SO)]),
+    "fc3dgpu_options_create": (C.POINTER(_SO), []),
+    "fc3dgpu_options_delete": (None, [C.POINTER(_SO)]),
+    "fc3dgpu_release": (None, [C.POINTER(_SO)]),
+    "fc3dgpu_compute_error": (C.c_int, [C.POINTER(_FCP), _DP, _DP, C.c_double, C.c_double, _DP]),
+    "fc3dgpu_nsgs_batch": (C.c_int, [C.c_int, C.POINTER(C.POINTER(_FCP)), C.POINTER(_DP), C.POINTER(_DP),
+                                     C.POINTER(_SO), C.POINTER(C.c_int)]),
+    "fc3dgpu_colour": (C.c_int, [C.c_int, _I64, _I64, C.c_int, _I32]),
+    "fc3dgpu_last_error": (C.c_char_p, []),
+    "fc3dgpu_params_default": (None, [C.POINTER(FC3DGPUParams)]),
+    "fc3dgpu_ctx_create": (C.c_void_p, [C.c_int]),
+    "fc3dgpu_ctx_destroy": (None, [C.c_void_p]),
+    "fc3dgpu_ctx_set_W": (C.c_int, [C.c_void_p, C.c_int, _I64, _I64, _F64, C.c_int]),
+    "fc3dgpu_ctx_set_q_mu": (C.c_int, [C.c_void_p, _F64, _F64]),
+    "fc3dgpu_ctx_set_r": (C.c_int, [C.c_void_p, _F64]),
+    "fc3dgpu_ctx_solve": (C.c_int, [C.c_void_p, C.POINTER(FC3DGPUParams), C.POINTER(FC3DGPUStats)]),
+    "fc3dgpu_ctx_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_compute_error": (C.c_int, [C.c_void_p, _DP]),
+    "fc3dgpu_ctx_trace": (C.c_int, [C.c_void_p, _F64, C.c_int]),
+    "fc3dgpu_ctx_colours": (C.c_int, [C.c_void_p, _I32]),
+    "fc3dgpu_lattice_create": (C.c_void_p, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double, C.c_double]),
+    "fc3dgpu_lattice_free": (None, [C.c_void_p]),
+    "fc3dgpu_lattice_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
+    "fc3dgpu_lattice_fill_W": (C.c_int, [C.c_void_p, _I64, _I64, _F64]),
+    "fc3dgpu_lattice_fill_q": (C.c_int, [C.c_void_p, C.c_double, _F64]),
+    "fc3dgpu_lattice_fill_geometry": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_lattice_perturb_velocities": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double]),
+    "fc3dgpu_normal_fill": (None, [C.c_uint64, _F64, C.c_int64]),
+}
+
+
+def lib():
+    """The loaded ``libfc3dgpu.so``.  Raises when it has not been built: there
+    is no fallback implementation."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with siconos_gb300.build.build()")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in ABI.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    v = lib().fc3dgpu_last_error()
+    return v.decode() if v else ""
+
+
+class SparseBlockMatrix:
+    """3x3-block CSR matrix exposed to C as a SparseBlockStructuredMatrix
+    whose block pointers point into one contiguous numpy array."""
+
+    def __init__(self, nc: int, rowptr, colidx, blocks):
+        self.nc = int(nc)
+        self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        self.colidx = np.ascontiguousarray(colidx, dtype=np.int64)
+        self.blocks = np.ascontiguousarray(np.asarray(blocks, dtype=np.float64).reshape(-1, 9))
+        nnzb = int(self.rowptr[-1])
+        if self.blocks.shape[0] != nnzb or self.colidx.shape[0] != nnzb:
+            raise ValueError("block-CSR arrays disagree on the number of blocks")
+        self._i1 = self.rowptr.astype(np.uintp)
+        self._i2 = self.colidx.astype(np.uintp)
+        self._bs = (3 * np.arange(1, self.nc + 1)).astype(np.uintp)
+        base = self.blocks.ctypes.data
+        self._ptrs = self._ptr_array(base, max(nnzb, 1))
+        s = SparseBlockStructuredMatrix()
+        s.nbblocks = nnzb
+        s.block = C.cast(self._ptrs, C.POINTER(_DP))
+        s.blocknumber0 = s.blocknumber1 = self.nc
+        s.blocksize0 = self._bs.ctypes.data_as(_SZP)
+        s.blocksize1 = self._bs.ctypes.data_as(_SZP)
+        s.filled1 = self.nc + 1
+        s.filled2 = nnzb
+        s.index1_data = self._i1.ctypes.data_as(_SZP)
+        s.index2_data = self._i2.ctypes.data_as(_SZP)
+        s.diagonal_blocks = None
+        s.version.number = 1
+        self.c = s
+
+    @staticmethod
+    def _ptr_array(base, n):
+        arr = (base + 72 * np.arange(n, dtype=np.uint64)).astype(np.uintp)
+        holder = (_DP * n).from_buffer(arr)
+        holder._keep = arr
+        return holder
+
+    def bump_version(self):
+        """Signal that the block values changed (invalidates the device copy)."""
+        self.c.version.number += 1
+
+    def todense(self) -> np.ndarray:
+        n = 3 * self.nc
+        W = np.zeros((n, n), order="F")
+        for i in range(self.nc):
+            for k in range(self.rowptr[i], self.rowptr[i + 1]):
+                j = self.colidx[k]
+                W[3 * i:3 * i + 3, 3 * j:3 * j + 3] = self.blocks[k].reshape(3, 3, order="F")
+        return W
+
+
+class FrictionContactProblem:
+    """``FrictionContactProblem(dim, nc, M, q, mu)`` sharing the numpy buffers."""
+
+    def __init__(self, dim: int, nc: int, M, q, mu):
+        if dim != 3:
+            raise ValueError("only dimension 3 is supported")
+        self._q = q if (isinstance(q, np.ndarray) and q.dtype == np.float64 and q.flags.c_contiguous) \
+            else np.ascontiguousarray(q, dtype=np.float64)
+        self._mu = mu if (isinstance(mu, np.ndarray) and mu.dtype == np.float64 and mu.flags.c_contiguous) \
+            else np.ascontiguousarray(mu, dtype=np.float64)
+        self._M = M
+        nm = NumericsMatrix()
+        nm.size0 = nm.size1 = 3 * nc
+        if isinstance(M, SparseBlockMatrix):
+            nm.storageType = NM_SPARSE_BLOCK
+            nm.matrix1 = C.pointer(M.c)
+        else:
+            if not (isinstance(M, np.ndarray) and M.dtype == np.float64 and M.flags.f_contiguous):
+                raise TypeError("dense M must be a Fortran-ordered float64 numpy array")
+            nm.storageType = NM_DENSE
+            nm.matrix0 = M.ctypes.data_as(_DP)
+        nm.version.number = 1
+        self._nm = nm
+        p = _FCP()
+        p.dimension = dim
+        p.numberOfContacts = nc
+        p.M = C.pointer(nm)
+        p.q = self._q.ctypes.data_as(_DP)
+        p.mu = self._mu.ctypes.data_as(_DP)
+        self.c = p
+
+    @property
+    def numberOfContacts(self) -> int:
+        return self.c.numberOfContacts
+
+    @property
+    def dimension(self) -> int:
+        return self.c.dimension
+
+    def M(self):
+        return self._M
+
+    def q(self):
+        return self._q
+
+    def mu(self):
+        return self._mu
+
+
+class SolverOptions:
+    """``SolverOptions(solver_id)`` for ``SICONOS_FRICTION_3D_NSGS_GPU``."""
+
+    def __init__(self, solver_id: int = SICONOS_FRICTION_3D_NSGS_GPU):
+        if solver_id != SICONOS_FRICTION_3D_NSGS_GPU:
+            raise ValueError(f"solver {solver_id} is not provided by this library")
+        self.ptr = lib().fc3dgpu_options_create()
+        if not self.ptr:
+            raise MemoryError("fc3dgpu_options_create failed")
+        self._cb = None
+
+    @property
+    def solverId(self) -> int:
+        return self.ptr.contents.solverId
+
+    @property
+    def iparam(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.ptr.contents.iparam, shape=(OPTIONS_PARAM_SIZE,))
+
+    @property
+    def dparam(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.ptr.contents.dparam, shape=(OPTIONS_PARAM_SIZE,))
+
+    @property
+    def internalSolvers(self):
+        o = self.ptr.contents
+        return [_InternalOptions(o.internalSolvers[i]) for i in range(o.numberOfInternalSolvers)]
+
+    def set_callback(self, fn):
+        """fn(size, reaction, velocity, error) per iteration."""
+        def _c(env, size, r, u, err, extra):
+            fn(int(size), np.ctypeslib.as_array(r, shape=(size,)), np.ctypeslib.as_array(u, shape=(size,)), err)
+        cfun = CALLBACK_T(_c)
+        cb = Callback(None, cfun)
+        self._cb = (cfun, cb)
+        self.ptr.contents.callback = C.pointer(cb)
+
+    def release(self):
+        lib().fc3dgpu_release(self.ptr)
+
+    def __del__(self):
+        try:
+            if getattr(self, "ptr", None):
+                self.ptr.contents.callback = None
+                lib().fc3dgpu_options_delete(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+
+class _InternalOptions:
+    def __init__(self, ptr):
+        self.ptr = ptr
+
+    @property
+    def solverId(self) -> int:
+        return self.ptr.contents.solverId
+
+    @property
+    def iparam(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.ptr.contents.iparam, shape=(OPTIONS_PARAM_SIZE,))
+
+    @property
+    def dparam(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.ptr.contents.dparam, shape=(OPTIONS_PARAM_SIZE,))
+
+
+def _vec(x, n):
+    if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous and x.size == n):
+        raise TypeError(f"expected a C-contiguous float64 array of size {n}")
+    return x.ctypes.data_as(_DP)
+
+
+def fc3d_driver(problem: FrictionContactProblem, reaction: np.ndarray, velocity: np.ndarray,
+                options: SolverOptions) -> int:
+    n = 3 * problem.numberOfContacts
+    return lib().fc3dgpu_driver(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), options.ptr)
+
+
+def fc3d_nsgs_gpu(problem, reaction, velocity, options) -> int:
+    """The solver entry itself (what the registry binds), without the
+    driver's trivial-case shortcut."""
+    n = 3 * problem.numberOfContacts
+    return lib().fc3dgpu_nsgs(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), options.ptr)
+
+
+def fc3d_compute_error(problem, reaction, velocity, tolerance: float, norm_q: float):
+    n = 3 * problem.numberOfContacts
+    err = C.c_double()
+    info = lib().fc3dgpu_compute_error(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), tolerance, norm_q,
+                                       C.byref(err))
+    return info, err.value
+
+
+def fc3d_nsgs_batch(problems, reactions, velocities, options):
+    k = len(problems)
+    P = (C.POINTER(_FCP) * k)(*[C.pointer(p.c) for p in problems])
+    R = (_DP * k)(*[_vec(r, 3 * p.numberOfContacts) for r, p in zip(reactions, problems)])
+    U = (_DP * k)(*[_vec(u, 3 * p.numberOfContacts) for u, p in zip(velocities, problems)])
+    info = (C.c_int * k)()
+    rc = lib().fc3dgpu_nsgs_batch(k, P, R, U, options.ptr, info)
+    return rc, list(info)
+
+
+def colour(rowptr, colidx, kind: int = 0) -> tuple[int, np.ndarray]:
+    """Device colouring of a block-CSR structure: (number of colours, colour
+    per contact)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int64)
+    colidx = np.ascontiguousarray(colidx, np.int64)
+    nc = rowptr.size - 1
+    out = np.zeros(nc, np.int32)
+    n = lib().fc3dgpu_colour(nc, rowptr, colidx, kind, out)
+    if n < 0:
+        raise RuntimeError(last_error())
+    return n, out

@@ -1,0 +1,79 @@
+"""Seeded sphere-lattice scenes (include/fc3dgpu_scene.h) as friction-contact
+problems, and the batch / time-stepping workloads built from them."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import numerics as sn
+
+
+@dataclass
+class LatticeScene:
+    dims: tuple
+    seed: int
+    nc: int
+    nbodies: int
+    rowptr: np.ndarray
+    colidx: np.ndarray
+    blocks: np.ndarray  # nnzb x 9, column-major 3x3
+    q: np.ndarray
+    mu: np.ndarray
+    gap: np.ndarray
+    handle: object = None
+
+    @property
+    def nnzb(self) -> int:
+        return int(self.rowptr[-1])
+
+    def problem(self) -> sn.FrictionContactProblem:
+        W = sn.SparseBlockMatrix(self.nc, self.rowptr, self.colidx, self.blocks)
+        return sn.FrictionContactProblem(3, self.nc, W, self.q, self.mu)
+
+    def perturb(self, seed: int, std: float = 0.01, h: float = 1e-3):
+        """v0 += N(0, std^2) per degree of freedom; q recomputed, contacts kept."""
+        L = sn.lib()
+        L.fc3dgpu_lattice_perturb_velocities(self.handle, seed, std)
+        L.fc3dgpu_lattice_fill_q(self.handle, h, self.q)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                sn.lib().fc3dgpu_lattice_free(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+def lattice(nx: int, ny: int, nz: int, seed: int = 1, mu: float = 0.5, jitter_std: float = 1e-3,
+            v0_std: float = 0.1, h: float = 1e-3) -> LatticeScene:
+    L = sn.lib()
+    hdl = L.fc3dgpu_lattice_create(nx, ny, nz, seed, jitter_std, v0_std)
+    if not hdl:
+        raise ValueError("bad lattice size")
+    nb, nc, nnzb = C.c_int(), C.c_int(), C.c_int64()
+    L.fc3dgpu_lattice_sizes(hdl, C.byref(nb), C.byref(nc), C.byref(nnzb))
+    n, k = nc.value, nnzb.value
+    rp = np.zeros(n + 1, np.int64)
+    ci = np.zeros(k, np.int64)
+    bl = np.zeros(9 * k)
+    q = np.zeros(3 * n)
+    gap = np.zeros(n)
+    L.fc3dgpu_lattice_fill_W(hdl, rp, ci, bl)
+    L.fc3dgpu_lattice_fill_q(hdl, h, q)
+    L.fc3dgpu_lattice_fill_geometry(hdl, gap.ctypes.data, None, None)
+    return LatticeScene((nx, ny, nz), seed, n, nb.value, rp, ci, bl.reshape(k, 9), q, np.full(n, float(mu)), gap, hdl)
+
+
+def batch_scenes(count: int = 512, seed: int = 7, lo=(3, 3, 2), hi=(20, 20, 10), mu_range=(0.1, 0.9)):
+    """Independent scenes with dims drawn uniformly in [lo, hi] per axis and
+    mu ~ U(mu_range) per scene."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        d = [int(rng.integers(lo[a], hi[a] + 1)) for a in range(3)]
+        m = float(rng.uniform(*mu_range))
+        out.append(lattice(*d, seed=seed * 100003 + k, mu=m))
+    return out

@@ -1,0 +1,118 @@
+"""Generate the golden fixtures in tests/golden from the reference itself.
+
+Run in a checkout that has the reference sources (the library in
+``oracle/_ref`` is built from them by ``oracle/build_ref.py``):
+
+    python tests/golden/make_golden.py /path/to/reference
+
+For each SBM/dense friction-contact fixture of the reference's own test data
+(numerics/src/FrictionContact/test/data) and for the 5x5x6 lattice scene,
+this stores the problem (block-CSR) and the reference fc3d_driver result
+(SICONOS_FRICTION_3D_NSGS defaults, tol 1e-8, 10000 iterations; and a
+20-iteration run) in one compressed .npz per case.  It also evaluates the
+reference's computeAlartCurnierSTD on the 1000 samples of data/ACinputs.dat
+(the known-answer set of fc3d_AlartCurnierFunctions_test.c), and records
+checksums of generated lattice scenes so that other platforms can check the
+generator reproduces them bit for bit.
+"""
+from __future__ import annotations
+
+import hashlib
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+FIXTURES = [
+    "FC3D_Example1_SBM.dat",
+    "FrictionContact3D_1c.dat",
+    "Confeti-ex13-4contact-Fc3D-SBM.dat",
+    "Confeti-ex13-Fc3D-SBM.dat",
+    "Confeti-ex03-Fc3D-SBM.dat",
+    "KaplasTower-i1061-4.hdf5.dat",
+    "Capsules-i122-1617.dat",
+    "BoxesStack1-i100000-32.hdf5.dat",
+    "RockPile_tob1.dat",
+    "FC3D_Example1.dat",
+    "Rover4396.dat",
+    "NESpheres_10_1.dat",
+]
+
+
+def checksum(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def save_case(name, P, res_full, res_20, extra=None):
+    d = dict(nc=P.nc, rowptr=P.rowptr, colidx=P.colidx, blocks=P.blocks, q=P.q, mu=P.mu,
+             info=res_full.info, iterations=res_full.iterations, error=res_full.error, r=res_full.r, u=res_full.u,
+             trace=res_full.trace, info20=res_20.info, iterations20=res_20.iterations, error20=res_20.error,
+             r20=res_20.r, u20=res_20.u, trace20=res_20.trace)
+    if extra:
+        d.update(extra)
+    np.savez_compressed(HERE / f"{name}.npz", **d)
+
+
+def main(ref_root: str):
+    from oracle import build_ref
+    import oracle as O
+
+    build_ref.build(ref_root)
+    data = Path(ref_root) / "numerics" / "src" / "FrictionContact" / "test" / "data"
+    for f in FIXTURES:
+        P = O.read_dat(data / f)
+        full = O.nsgs_ref(P, tol=1e-8, maxiter=10000, trace_cap=20000)
+        short = O.nsgs_ref(P, tol=1e-8, maxiter=20, trace_cap=20)
+        name = "fixture_" + f.replace(".hdf5", "").replace(".dat", "").replace("-", "_")
+        save_case(name, P, full, short, {"source": f})
+        print(f"{f}: nc={P.nc} nnzb={P.nnzb} info={full.info} it={full.iterations} err={full.error:.3e}")
+
+    # lattice scenes (generator in the product library)
+    from siconos_gb300 import build as B
+    B.build()
+    from siconos_gb300 import scene
+    sums = {}
+    for dims, seed in [((5, 5, 6), 1), ((5, 5, 6), 2), ((3, 3, 2), 1)]:
+        s = scene.lattice(*dims, seed=seed)
+        P = O.Problem(s.nc, s.rowptr, s.colidx, s.blocks, s.q, s.mu)
+        full = O.nsgs_ref(P, tol=1e-8, maxiter=10000, trace_cap=20000)
+        short = O.nsgs_ref(P, tol=1e-8, maxiter=20, trace_cap=20)
+        name = f"lattice_{dims[0]}x{dims[1]}x{dims[2]}_s{seed}"
+        save_case(name, P, full, short, {"dims": np.array(dims), "seed": seed})
+        print(f"{name}: nc={P.nc} info={full.info} it={full.iterations} err={full.error:.3e}")
+    for dims, seed in [((5, 5, 6), 1), ((12, 9, 7), 3), ((60, 60, 30), 1)]:
+        s = scene.lattice(*dims, seed=seed)
+        sums[f"{dims[0]}x{dims[1]}x{dims[2]}_s{seed}"] = [s.nc, s.nnzb, checksum(s.rowptr, s.colidx, s.blocks, s.q)]
+    with open(HERE / "lattice_checksums.txt", "w") as fh:
+        for k, (nc, nnzb, h) in sums.items():
+            fh.write(f"{k} {nc} {nnzb} {h}\n")
+
+    # Alart-Curnier known answers
+    vals = np.array([float(x) for x in (data / "ACinputs.dat").read_text().split()])
+    n = int(vals[0])
+    R = vals[1:1 + 3 * n].reshape(n, 3)
+    V = vals[1 + 3 * n:1 + 6 * n].reshape(n, 3)
+    MU = vals[1 + 6 * n:1 + 7 * n]
+    RHO = vals[1 + 7 * n:1 + 10 * n].reshape(n, 3)
+    lib = O.ref()
+    F = np.zeros((n, 3))
+    A = np.zeros((n, 9))
+    Bm = np.zeros((n, 9))
+    for k in range(n):
+        f, a, b = np.zeros(3), np.zeros(9), np.zeros(9)
+        lib.computeAlartCurnierSTD(np.ascontiguousarray(R[k]), np.ascontiguousarray(V[k]), MU[k],
+                                   np.ascontiguousarray(RHO[k]), f, a.ctypes.data, b.ctypes.data)
+        F[k], A[k], Bm[k] = f, a, b
+    np.savez_compressed(HERE / "ac_known_answers.npz", R=R, V=V, mu=MU, rho=RHO, F=F, A=A, B=Bm)
+    print("ACinputs:", n, "samples")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

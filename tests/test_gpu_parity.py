@@ -1,0 +1,137 @@
+"""GPU parity against the oracle, through the C-ABI.
+
+* colouring: the device Jones-Plassmann colouring equals the oracle's host
+  greedy colouring bit for bit;
+* FP64 coloured sweeps (one lane per contact, no FMA) reproduce the oracle's
+  restatement run in the same colour order bit for bit;
+* whole solves through fc3d_driver reach the reference's fc3d_compute_error
+  tolerance (1e-8) on every fixture where the reference converges, with
+  reactions and velocities close to the reference's;
+* at the 60x60x30 scale, size-independent properties hold.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import CONVERGING, FIXTURE_CASES, LATTICE_CASES, load_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _colour_order(col):
+    return np.lexsort((np.arange(col.size), col)).astype(np.int32)
+
+
+@pytest.mark.parametrize("case", FIXTURE_CASES + LATTICE_CASES)
+@pytest.mark.parametrize("kind", [0, 1])
+def test_device_colouring_equals_host(gpu, case, kind):
+    import siconos_gb300.numerics as sn
+    P, _ = load_case(case)
+    n, col = sn.colour(P.rowptr, P.colidx, kind)
+    ref = np.zeros(P.nc, np.int32)
+    nref = O.port().oracle_colour_greedy(P.nc, P.rowptr, P.colidx, kind, ref)
+    assert n == nref
+    assert np.array_equal(col, ref)
+
+
+@pytest.mark.parametrize("case", ["lattice_5x5x6_s1", "fixture_KaplasTower_i1061_4", "fixture_Confeti_ex13_Fc3D_SBM",
+                                  "fixture_RockPile_tob1"])
+def test_fp64_sweeps_bit_exact_vs_coloured_oracle(gpu, case):
+    P, g = load_case(case)
+    gpu.set_W(P.nc, P.rowptr, P.colidx, P.blocks)
+    gpu.set_q_mu(P.q, P.mu)
+    gpu.set_r(np.zeros(3 * P.nc))
+    st = gpu.solve(tol=1e-300, max_iter=20, precision=1, lanes=1)
+    r, u = gpu.get()
+    order = _colour_order(gpu.colours())
+    ref = O.nsgs_port(P, tol=1e-300, maxiter=20, order=order)
+    assert st["sweeps64"] == 20
+    assert np.array_equal(r, ref.r), np.abs(r - ref.r).max()
+    assert np.allclose(u, ref.u, rtol=0, atol=1e-13 * (1 + np.abs(ref.u).max()))
+    assert abs(st["error"] - ref.error) <= 1e-10 * ref.error
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+def test_fp64_lanes_agree(gpu, lanes):
+    P, g = load_case("lattice_5x5x6_s1")
+    gpu.set_W(P.nc, P.rowptr, P.colidx, P.blocks)
+    gpu.set_q_mu(P.q, P.mu)
+    gpu.set_r(np.zeros(3 * P.nc))
+    gpu.solve(tol=1e-300, max_iter=10, precision=1, lanes=lanes)
+    r, _ = gpu.get()
+    order = _colour_order(gpu.colours())
+    ref = O.nsgs_port(P, tol=1e-300, maxiter=10, order=order)
+    assert np.allclose(r, ref.r, rtol=1e-9, atol=1e-12)
+
+
+def _driver(P, tol=1e-8, maxiter=10000, precision=0):
+    import siconos_gb300.numerics as sn
+    W = sn.SparseBlockMatrix(P.nc, P.rowptr, P.colidx, P.blocks)
+    prob = sn.FrictionContactProblem(3, P.nc, W, P.q.copy(), P.mu.copy())
+    o = sn.SolverOptions()
+    o.iparam[sn.SICONOS_IPARAM_MAX_ITER] = maxiter
+    o.dparam[sn.SICONOS_DPARAM_TOL] = tol
+    o.iparam[sn.FC3DGPU_IPARAM_PRECISION] = precision
+    r = np.zeros(3 * P.nc)
+    u = np.zeros(3 * P.nc)
+    info = sn.fc3d_driver(prob, r, u, o)
+    return info, r, u, o
+
+
+@pytest.mark.parametrize("case", CONVERGING)
+@pytest.mark.parametrize("precision", [0, 1])
+def test_driver_reaches_reference_tolerance(gpu, case, precision):
+    P, g = load_case(case)
+    info, r, u, o = _driver(P, precision=precision)
+    err, u_oracle = O.compute_error_port(P, r)
+    assert info == 0, (info, o.dparam[1])
+    assert err <= 1e-8
+    assert abs(o.dparam[1] - err) <= 1e-9 * max(err, 1e-300) + 1e-18
+    # velocities: u = W r + q
+    assert np.allclose(u, u_oracle, rtol=0, atol=1e-12 * (1 + np.abs(u_oracle).max()))
+    # same solution as the reference, to the reference's own comparison
+    # criterion (test_nsgs_compare.c:200-205: |dr| < 1e-6, |du| < 1e-6)
+    scale_r = max(1.0, np.linalg.norm(g["r"]))
+    scale_u = max(1.0, np.linalg.norm(g["u"]))
+    assert np.linalg.norm(r - g["r"]) <= 1e-6 * scale_r
+    assert np.linalg.norm(u - g["u"]) <= 1e-6 * scale_u
+
+
+@pytest.mark.parametrize("case", ["fixture_BoxesStack1_i100000_32", "fixture_RockPile_tob1"])
+def test_driver_same_info_code_when_reference_does_not_converge(gpu, case):
+    P, g = load_case(case)
+    info, r, u, o = _driver(P, maxiter=2000)
+    assert int(g["info"]) == -20
+    assert info == -20
+    assert o.iparam[1] == 2000
+
+
+def test_error_kernel_matches_oracle(gpu):
+    P, g = load_case("fixture_KaplasTower_i1061_4")
+    rng = np.random.default_rng(3)
+    r = g["r"] + 1e-3 * rng.normal(size=g["r"].size)
+    gpu.set_W(P.nc, P.rowptr, P.colidx, P.blocks)
+    gpu.set_q_mu(P.q, P.mu)
+    gpu.set_r(r)
+    e = gpu.compute_error()
+    e_ref, u_ref = O.compute_error_port(P, r)
+    assert abs(e - e_ref) <= 1e-12 * e_ref
+    _, u = gpu.get()
+    assert np.allclose(u, u_ref, rtol=0, atol=1e-14 * (1 + np.abs(u_ref).max()))
+
+
+def test_c2_scale_properties(gpu):
+    from siconos_gb300 import scene
+    s = scene.lattice(60, 60, 30, seed=1)
+    gpu.load(s)
+    st = gpu.solve(tol=1e-8, max_iter=60)
+    r, u = gpu.get()
+    P = O.Problem(s.nc, s.rowptr, s.colidx, s.blocks, s.q, s.mu)
+    e_ref, u_ref = O.compute_error_port(P, r)
+    assert abs(st["error"] - e_ref) <= 1e-9 * e_ref
+    assert np.allclose(u, u_ref, rtol=0, atol=1e-12 * (1 + np.abs(u_ref).max()))
+    rn, rt = r[0::3], np.hypot(r[1::3], r[2::3])
+    assert np.all(rn >= 0) and np.all(rt <= s.mu * rn * (1 + 1e-12) + 1e-15)
+    col = gpu.colours()
+    assert O.port().oracle_colour_check(s.nc, s.rowptr, s.colidx, col) == 0
+    assert st["sweeps32"] + st["sweeps64"] == 60 and st["status"] == 0
