@@ -463,6 +463,8 @@ struct fc3dgpu_ctx {
   BUF(long long, scratch64);
   BUF(double, out);
   BUF(double, trace);
+  BUF(unsigned long long, counters);
+  int counters_on = 0;
 };
 
 static int grid1d(long long n, int block = 256) {
@@ -519,7 +521,8 @@ extern "C" fc3dgpu_ctx* fc3dgpu_ctx_create(int device) {
             ensure(&c->scratch, &c->scratch_cap, 16) == cudaSuccess &&
             ensure(&c->scratch64, &c->scratch64_cap, 16) == cudaSuccess &&
             ensure(&c->out, &c->out_cap, 16) == cudaSuccess &&
-            ensure(&c->trace, &c->trace_cap, 1 << 17) == cudaSuccess;
+            ensure(&c->trace, &c->trace_cap, 1 << 17) == cudaSuccess &&
+            ensure(&c->counters, &c->counters_cap, 8) == cudaSuccess;
   if (!ok) {
     fc3dgpu_set_error("device allocation failed");
     fc3dgpu_ctx_destroy(c);
@@ -535,7 +538,8 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->cursor, c->adj, c->key, c->colour, c->blockhist, c->counts, c->sptr_d, c->perm, c->iperm,
                   c->rowlen, c->dpos, c->slab_nslot, c->slab_off, c->W64, c->W32, c->col, c->D64, c->D32,
                   c->rho64, c->rho32, c->q64, c->q32, c->mu64, c->mu32, c->r64, c->r32, c->rpli64, c->rpli32,
-                  c->u64, c->partials, c->barrier, c->status, c->scratch, c->scratch64, c->out, c->trace};
+                  c->u64, c->partials, c->barrier, c->status, c->scratch, c->scratch64, c->out, c->trace,
+                  c->counters};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; i++)
@@ -805,6 +809,7 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.trace_base = 0;
   a.norm_q = c->norm_q;
   a.spin_limit = 1ULL << 22;
+  a.counters = c->counters_on ? c->counters : nullptr;
   a.out = c->out;
 }
 
@@ -944,6 +949,21 @@ extern "C" int fc3dgpu_ctx_compute_error(fc3dgpu_ctx* c, double* error) {
   CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (error) *error = out[2];
+  return 0;
+}
+
+// Work counters of the local solver, accumulated over the solves after
+// they are switched on: Newton iterations, PLI iterations, line-search
+// evaluations, local solves, largest Newton count of one local solve.
+extern "C" int fc3dgpu_ctx_counters(fc3dgpu_ctx* c, int enable, unsigned long long* out5) {
+  if (!c) return -1;
+  CK(cudaSetDevice(c->device));
+  if (out5) {
+    CK(cudaMemcpyAsync(out5, c->counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  CK(cudaMemsetAsync(c->counters, 0, 8 * sizeof(unsigned long long), c->stream));
+  c->counters_on = enable;
   return 0;
 }
 

@@ -63,6 +63,7 @@ struct SweepArgs {
   double norm_q;
   int newton_max, pli_max, ls_max;
   unsigned long long spin_limit;
+  unsigned long long* counters;  // optional work counters: Newton its, PLI its, line-search evals, solves, max Newton
   // outputs (written by block 0, thread 0)
   double* out;                  // [0] sweeps, [1] incr, [2] full error, [3] info, [4] working tol
 };

@@ -194,6 +194,7 @@ struct LocalProblem {
   Real tol;
   int newton_max, pli_max, ls_max;
   Real residual;  // SOLVER_RESIDUAL of the local options
+  int n_newton, n_pli, n_ls;  // work counters
 };
 
 template <typename Real>
@@ -208,7 +209,7 @@ __device__ __forceinline__ Real local_error(const LocalProblem<Real>& L, const R
 }
 
 template <typename Real>
-__device__ __forceinline__ Real line_search_gp(const LocalProblem<Real>& L, const Real r[3], const Real dR[3],
+__device__ __forceinline__ Real line_search_gp(LocalProblem<Real>& L, const Real r[3], const Real dR[3],
                                                Real F[3], const Real A[9], const Real B[9], Real v[3]) {
   Real alpha = 1, amin = 0, amax = Real(1e20);
   const Real inf = Real(1e20), m1 = Real(0.1), m2 = Real(0.9);
@@ -235,6 +236,7 @@ __device__ __forceinline__ Real line_search_gp(const LocalProblem<Real>& L, cons
 #pragma unroll
   for (int i = 0; i < 3; i++) dqdt0 += F[i] * tmp[i];
   for (int it = 0; it < L.ls_max; it++) {
+    L.n_ls++;
 #pragma unroll
     for (int i = 0; i < 3; i++) tmp[i] = r[i] + alpha * dR[i];
 #pragma unroll
@@ -257,7 +259,7 @@ __device__ __forceinline__ Real line_search_gp(const LocalProblem<Real>& L, cons
 }
 
 template <typename Real>
-__device__ __noinline__ void newton_damped(LocalProblem<Real>& L, Real r[3]) {
+__device__ __forceinline__ void newton_damped(LocalProblem<Real>& L, Real r[3]) {
   const Real E = Eps<Real>::v();
   Real nq = dsqrt(L.q[0] * L.q[0] + L.q[1] * L.q[1] + L.q[2] * L.q[2]);
   Real nrel = 1;
@@ -272,6 +274,7 @@ __device__ __noinline__ void newton_damped(LocalProblem<Real>& L, Real r[3]) {
   L.residual = dsqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]) * nrel;
   if (L.residual < L.tol) return;
   for (int inew = 1; inew < L.newton_max; ++inew) {
+    L.n_newton++;
     ac_std<Real, true>(r, v, L.mu, L.rhoN, L.rhoT, F, A, B);
     // AWB = -(A M + B), as mm3x3 + add3x3 + scal3x3
 #pragma unroll
@@ -306,7 +309,7 @@ __device__ __noinline__ void newton_damped(LocalProblem<Real>& L, Real r[3]) {
 }
 
 template <typename Real>
-__device__ __noinline__ void pli_solve(LocalProblem<Real>& L, Real r[3]) {
+__device__ __forceinline__ void pli_solve(LocalProblem<Real>& L, Real r[3]) {
   const Real* M = L.M;
   const Real mu = L.mu;
   Real rho = L.rho_pli, rho_k = rho;
@@ -316,6 +319,7 @@ __device__ __noinline__ void pli_solve(LocalProblem<Real>& L, Real r[3]) {
   int localiter = 0;
   while ((localerror > L.tol) && (localiter < L.pli_max)) {
     localiter++;
+    L.n_pli++;
     localerror_k = localerror;
     r_k[0] = r[0];
     r_k[1] = r[1];

@@ -20,7 +20,6 @@
 #include "fc3dgpu.h"
 
 void fc3dgpu_set_error(const char *fmt, ...);
-int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx *ctx, double norm_q);
 
 #define FC3DGPU_CACHE_MAGIC 0x46433344u
 

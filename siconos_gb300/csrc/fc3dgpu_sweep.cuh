@@ -140,15 +140,29 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
     acc[1] = 0;
     acc[2] = 0;
   }
-  for (int s = j; s < ns; s += T) {
-    const size_t sl = (size_t)(base + s);
-    const int pj = __ldg(&a.col[sl * FC3D_SLAB + k]);
-    const Real* w = a.W + sl * 9 * FC3D_SLAB + k;
-    Real wv[9], rv[3];
+  // slots in chunks of CH, fully unrolled: the column indices and W
+  // elements of a chunk are requested together, then the dependent r
+  // gathers, so one row costs two memory round trips per chunk instead of
+  // two per slot.  Accumulation stays in slot order.
+  constexpr int CH = sizeof(Real) == 4 ? 8 : 4;
+  for (int s0 = j; s0 < ns; s0 += CH * T) {
+    int pj[CH];
+    Real wv[CH][9];
 #pragma unroll
-    for (int e = 0; e < 9; e++) wv[e] = __ldg(&w[e * FC3D_SLAB]);
-    load_r3<Real>(a.r, pj, rv);
-    mvp3x3(wv, rv, acc);
+    for (int c = 0; c < CH; c++) {
+      const int s = s0 + c * T;
+      const size_t sl = (size_t)(base + (s < ns ? s : 0));
+      pj[c] = s < ns ? __ldg(&a.col[sl * FC3D_SLAB + k]) : a.npad;
+      const Real* w = a.W + sl * 9 * FC3D_SLAB + k;
+#pragma unroll
+      for (int e = 0; e < 9; e++) wv[c][e] = s < ns ? __ldg(&w[e * FC3D_SLAB]) : Real(0);
+    }
+    Real rv[CH][3];
+#pragma unroll
+    for (int c = 0; c < CH; c++) load_r3<Real>(a.r, pj[c], rv[c]);
+#pragma unroll
+    for (int c = 0; c < CH; c++)
+      if (s0 + c * T < ns) mvp3x3(wv[c], rv[c], acc);
   }
   if (T > 1) {
 #pragma unroll
@@ -176,12 +190,22 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   L.newton_max = a.newton_max;
   L.pli_max = a.pli_max;
   L.ls_max = a.ls_max;
+  L.n_newton = 0;
+  L.n_pli = 0;
+  L.n_ls = 0;
   Real ro[3], rn[3];
   load_r3<Real>(a.r, p, ro);
   rn[0] = ro[0];
   rn[1] = ro[1];
   rn[2] = ro[2];
   local_solve(L, rn);
+  if (a.counters && j == 0) {
+    atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
+    atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);
+    atomicAdd(&a.counters[2], (unsigned long long)L.n_ls);
+    atomicAdd(&a.counters[3], 1ULL);
+    atomicMax(&a.counters[4], (unsigned long long)L.n_newton);
+  }
   if (j == 0) {
     Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
     rp[0] = rn[0];

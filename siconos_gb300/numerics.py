@@ -153,6 +153,8 @@ ABI = {
     "fc3dgpu_ctx_compute_error": (C.c_int, [C.c_void_p, _DP]),
     "fc3dgpu_ctx_trace": (C.c_int, [C.c_void_p, _F64, C.c_int]),
     "fc3dgpu_ctx_colours": (C.c_int, [C.c_void_p, _I32]),
+    "fc3dgpu_ctx_counters": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "fc3dgpu_ctx_set_norm_q": (C.c_int, [C.c_void_p, C.c_double]),
     "fc3dgpu_lattice_create": (C.c_void_p, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double, C.c_double]),
     "fc3dgpu_lattice_free": (None, [C.c_void_p]),
     "fc3dgpu_lattice_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
