@@ -154,10 +154,11 @@ int fc3dgpu_ctx_compute_error(fc3dgpu_ctx *ctx, double *error);
 /* Per-sweep incremental error trace of the last solve (FP32 then FP64). */
 int fc3dgpu_ctx_trace(fc3dgpu_ctx *ctx, double *out, int cap);
 int fc3dgpu_ctx_colours(fc3dgpu_ctx *ctx, int32_t *colour);
-/* Local-solver work counters (Newton iterations, PLI iterations, line-search
- * evaluations, local solves, largest Newton count) since the last call;
- * enable != 0 keeps counting in later solves.  out5 may be NULL. */
-int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out5);
+/* Sweep work counters since the last call: Newton iterations, PLI
+ * iterations, line-search evaluations, local solves, largest Newton count of
+ * one solve, summed and largest SM cycles of one warp work unit, number of
+ * units.  enable != 0 keeps counting in later solves.  out8 may be NULL. */
+int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out8);
 /* Norm of q used by the relative error (default: computed from q). */
 int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx *ctx, double norm_q);
 

@@ -515,6 +515,9 @@ extern "C" fc3dgpu_ctx* fc3dgpu_ctx_create(int device) {
     return nullptr;
   }
   for (int i = 0; i < 4; i++) cudaEventCreate(&c->ev[i]);
+  // load every sweep kernel now: with lazy module loading the first launch
+  // of each instance would otherwise pay the load inside a timed solve
+  fc3dgpu::warm_sweep_kernels();
   bool ok = ensure(&c->partials, &c->partials_cap, 1024 * 8) == cudaSuccess &&
             ensure(&c->barrier, &c->barrier_cap, 4) == cudaSuccess &&
             ensure(&c->status, &c->status_cap, 4) == cudaSuccess &&
@@ -955,11 +958,11 @@ extern "C" int fc3dgpu_ctx_compute_error(fc3dgpu_ctx* c, double* error) {
 // Work counters of the local solver, accumulated over the solves after
 // they are switched on: Newton iterations, PLI iterations, line-search
 // evaluations, local solves, largest Newton count of one local solve.
-extern "C" int fc3dgpu_ctx_counters(fc3dgpu_ctx* c, int enable, unsigned long long* out5) {
+extern "C" int fc3dgpu_ctx_counters(fc3dgpu_ctx* c, int enable, unsigned long long* out8) {
   if (!c) return -1;
   CK(cudaSetDevice(c->device));
-  if (out5) {
-    CK(cudaMemcpyAsync(out5, c->counters, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+  if (out8) {
+    CK(cudaMemcpyAsync(out8, c->counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
   CK(cudaMemsetAsync(c->counters, 0, 8 * sizeof(unsigned long long), c->stream));

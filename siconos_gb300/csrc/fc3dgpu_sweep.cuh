@@ -199,12 +199,24 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   rn[1] = ro[1];
   rn[2] = ro[2];
   local_solve(L, rn);
-  if (a.counters && j == 0) {
-    atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
-    atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);
-    atomicAdd(&a.counters[2], (unsigned long long)L.n_ls);
-    atomicAdd(&a.counters[3], 1ULL);
-    atomicMax(&a.counters[4], (unsigned long long)L.n_newton);
+  if (a.counters) {
+    // warp-aggregated: one atomic per counter per warp and unit
+    unsigned long long c0 = j == 0 ? L.n_newton : 0, c1 = j == 0 ? L.n_pli : 0, c2 = j == 0 ? L.n_ls : 0;
+    unsigned long long c4 = j == 0 ? L.n_newton : 0;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+      c0 += __shfl_xor_sync(__activemask(), c0, o);
+      c1 += __shfl_xor_sync(__activemask(), c1, o);
+      c2 += __shfl_xor_sync(__activemask(), c2, o);
+      c4 = max(c4, __shfl_xor_sync(__activemask(), c4, o));
+    }
+    if (lane == (__ffs(__activemask()) - 1)) {
+      atomicAdd(&a.counters[0], c0);
+      atomicAdd(&a.counters[1], c1);
+      atomicAdd(&a.counters[2], c2);
+      atomicAdd(&a.counters[3], (unsigned long long)__popc(__activemask()) / T);
+      atomicMax(&a.counters[4], c4);
+    }
   }
   if (j == 0) {
     Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
@@ -293,7 +305,19 @@ __global__ void __launch_bounds__(FC3D_BLOCK) nsgs_kernel(const SweepArgs<Real> 
     double acc[2] = {0.0, 0.0};
     for (int c = 0; c < a.ncol; c++) {
       const int s0 = a.sptr[c], nunits = (a.sptr[c + 1] - s0) * T;
-      for (int u = gw; u < nunits; u += tw) process_unit<Real, T>(a, s0 + u / T, u % T, lane, (Real)local_tol, acc[0], acc[1]);
+      for (int u = gw; u < nunits; u += tw) {
+        const long long t0 = a.counters ? clock64() : 0;
+        process_unit<Real, T>(a, s0 + u / T, u % T, lane, (Real)local_tol, acc[0], acc[1]);
+        if (a.counters) {
+          __syncwarp();
+          if (lane == 0) {
+            const unsigned long long dt = (unsigned long long)(clock64() - t0);
+            atomicAdd(&a.counters[5], dt);
+            atomicMax(&a.counters[6], dt);
+            atomicAdd(&a.counters[7], 1ULL);
+          }
+        }
+      }
       if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
       if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) return;
     }

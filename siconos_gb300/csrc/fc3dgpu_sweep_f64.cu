@@ -7,15 +7,21 @@ namespace fc3dgpu {
 template <int T>
 static cudaError_t launch_t(const SweepArgs<double>& a, int max_grid, cudaStream_t s, int* grid) {
   auto kern = nsgs_kernel<double, T>;
-  int dev = 0, nsm = 0, per_sm = 0;
+  static int cached_dev = -1, cached_g = 0;
+  int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FC3D_BLOCK, 0);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int g = nsm * per_sm;
+  if (cached_dev != dev) {
+    int nsm = 0, per_sm = 0;
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FC3D_BLOCK, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    cached_g = nsm * per_sm;
+    cached_dev = dev;
+  }
+  int g = cached_g;
   if (max_grid > 0 && g > max_grid) g = max_grid;
   if (g > 1024) g = 1024;
   *grid = g;
@@ -40,6 +46,14 @@ cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid
     case 8: return launch_t<8>(a, max_grid, s, grid);
     default: return cudaErrorInvalidValue;
   }
+}
+
+void warm_sweep_kernels_f64() {
+  cudaFuncAttributes fa;
+  cudaFuncGetAttributes(&fa, nsgs_kernel<double, 1>);
+  cudaFuncGetAttributes(&fa, nsgs_kernel<double, 2>);
+  cudaFuncGetAttributes(&fa, nsgs_kernel<double, 4>);
+  cudaFuncGetAttributes(&fa, nsgs_kernel<double, 8>);
 }
 
 int sweep_grid_f64(int lanes) {

@@ -13,5 +13,6 @@ namespace fc3dgpu {
 cudaError_t launch_sweep_f32(const SweepArgs<float>& a, int lanes, int max_grid, cudaStream_t s, int* grid);
 cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid, cudaStream_t s, int* grid);
 int sweep_grid_f32(int lanes);
+void warm_sweep_kernels();
 int sweep_grid_f64(int lanes);
 }  // namespace fc3dgpu

@@ -72,9 +72,10 @@ class DeviceSolver:
         return out[:max(n, 0)].copy()
 
     def counters(self, enable: bool = True) -> dict:
-        out = np.zeros(5, np.uint64)
+        out = np.zeros(8, np.uint64)
         self._check(self.L.fc3dgpu_ctx_counters(self.ctx, int(enable), out.ctypes.data), "counters")
-        return dict(zip(["newton", "pli", "line_search", "solves", "max_newton"], (int(v) for v in out)))
+        return dict(zip(["newton", "pli", "line_search", "solves", "max_newton", "unit_cycles", "max_unit_cycles",
+                         "units"], (int(v) for v in out)))
 
     def colours(self) -> np.ndarray:
         out = np.zeros(self.nc, np.int32)

