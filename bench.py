@@ -1,0 +1,361 @@
+"""Benchmark of the GPU coloured NSGS on the 60x60x30 sphere lattice.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--sweeps S]
+
+Workload (one "step"): one FC3D solve of the 60x60x30 lattice scene
+(108,000 spheres, 320,400 contacts, 3,453,120 3x3 blocks of W; mu 0.5,
+v0 ~ N(0, 0.1^2), seed 1) from r = 0 with tol 1e-8 and a budget of S sweeps
+(default 100).  Plain NSGS stalls above 1e-8 on this hyperstatic scene
+(the reference does too), so every step runs its whole budget: coloured FP32
+sweeps, then the FP64 fc3d_compute_error of the result.  The metric is
+contact-sweeps/s = contacts x sweeps / seconds.
+
+* ``value``: device-resident inputs (W, q, mu uploaded once; r zeroed on
+  the device), per-step CUDA events on the solver's own stream, L2 flushed
+  (256 MB write) between steps outside the timed events.
+* ``e2e``: the same solve through the reference-facing C-ABI
+  (fc3d_driver -> fc3dgpu_nsgs) with host buffers: each step uploads W, q,
+  mu, r from host memory and copies r, u back (wall clock).
+* ``cpu_baseline``: the CPU restatement of the reference's fc3d_nsgs
+  (bit-exact with it) on a bounded sample of the same scene, one core.
+* ``--impl reference``: the reference's own CPU fc3d_nsgs (oracle/_ref when it
+  was built on this machine, else the bit-exact restatement) on the same
+  scene, a bounded sample of sweeps per step; its NSGS is sequential, so one
+  core.
+
+With torchrun and N>1 each rank solves its own replica (replicas only:
+one scene does not shard); value = all ranks' contact-sweeps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DIMS = (60, 60, 30)
+SEED = 1
+MU = 0.5
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic_per_sweep():
+    """DRAM bytes per FP32 sweep from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "nsgs_kernel_f32_lattice_60x60x30.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_sweep:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(ws, v):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _init_dist(ws, local):
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group("gloo", init_method="env://")
+
+
+def cpu_sample(scene, sweeps: int, use_ref: bool):
+    """Time `sweeps` sweeps of the reference's sequential NSGS on the scene."""
+    import oracle as O
+    P = O.Problem(scene.nc, scene.rowptr, scene.colidx, scene.blocks, scene.q, scene.mu)
+    t = time.perf_counter()
+    if use_ref:
+        res = O.nsgs_ref(P, tol=1e-300, maxiter=sweeps)
+    else:
+        res = O.nsgs_port(P, tol=1e-300, maxiter=sweeps)
+    dt = time.perf_counter() - t
+    return dt, res
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    _init_dist(ws, local)
+    if rank != 0:
+        return 0
+    import oracle as O
+    from siconos_gb300 import build as B
+    B.build()
+    from siconos_gb300 import scene as sc
+    s = sc.lattice(*DIMS, seed=SEED, mu=MU)
+    use_ref = False
+    try:
+        use_ref = O.ref_available() and O.ref() is not None
+    except OSError:
+        use_ref = False
+    kind = "reference" if use_ref else "port"
+    per_step = args.cpu_sweeps
+    for _ in range(args.warmup):
+        cpu_sample(s, per_step, use_ref)
+    times = []
+    for _ in range(args.steps):
+        dt, res = cpu_sample(s, per_step, use_ref)
+        times.append(dt)
+    tot = sum(times)
+    value = s.nc * per_step * args.steps / tot
+    line = {
+        "impl": "reference", "metric": "contact-sweeps/s (FC3D NSGS, 60x60x30 lattice)", "value": value,
+        "unit": "contact-sweeps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{DIMS[0]}x{DIMS[1]}x{DIMS[2]} sphere lattice, {s.nc} contacts, {s.nnzb} blocks, "
+                               f"mu {MU}, seed {SEED}; reference fc3d_nsgs (SICONOS_FRICTION_3D_NSGS defaults), "
+                               f"{per_step} sweeps per step from r=0",
+                   "parallelism": "1 core (the reference's NSGS is sequential)"},
+        "cpu_baseline": {"value": value, "unit": "contact-sweeps/s", "cores": 1, "kind": kind,
+                         "sample": f"{per_step} NSGS sweeps of the {s.nc}-contact scene per step"},
+        "e2e": {"value": value, "unit": "contact-sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "error_after_sample": res.error,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = _dist()
+    _init_dist(ws, local)
+    from siconos_gb300 import build as B
+    B.build()
+    import ctypes as C
+
+    import torch
+    import siconos_gb300.numerics as sn
+    from siconos_gb300 import scene as sc
+    from siconos_gb300.device import DeviceSolver
+
+    dev = local if ws > 1 else 0
+    s = sc.lattice(*DIMS, seed=SEED + rank, mu=MU)
+    S = args.sweeps
+    d = DeviceSolver(dev)
+    d.set_W(s.nc, s.rowptr, s.colidx, s.blocks)
+    d.set_q_mu(s.q, s.mu)
+    stream = torch.cuda.ExternalStream(d.stream(), device=f"cuda:{dev}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    kw = dict(tol=1e-8, max_iter=S, switch_tol=0.0, stall_window=0)
+
+    def step():
+        d.zero_r()
+        return d.solve(**kw)
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize(dev)
+    _barrier(ws)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    launches0 = d.launches()
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize(dev)
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+                ev[k][0].record(stream)
+            stats.append(step())
+            ev[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+    launches = d.launches() - launches0
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    ms_max = _max_over_ranks(ws, ms)
+    sweeps = sum(st["sweeps32"] + st["sweeps64"] for st in stats)
+    total_cs = s.nc * sweeps * ws
+    value = total_cs / (ms_max / 1e3)
+    # roofline of the dominant kernel: the FP32 sweep kernel, one launch per step
+    fp32_ms = [st["ms_fp32"] for st in stats]
+    fp32_sweeps = [st["sweeps32"] for st in stats]
+    bytes_launch = stats[0]["bytes_sweep32"] * (sum(fp32_sweeps) / len(fp32_sweeps))
+    achieved = bytes_launch / (sum(fp32_ms) / len(fp32_ms) / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    tps = _traffic_per_sweep()
+    roof = {"kernel": "nsgs_kernel<float,1> (persistent coloured FP32 sweeps, one launch per step)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": achieved / peak,
+            "traffic": (tps * sum(fp32_sweeps) / len(fp32_sweeps)) if tps else None,
+            "algorithmic_bytes_per_launch": bytes_launch}
+
+    # e2e through the reference-facing C-ABI with host buffers
+    e2e_value, h2d, d2h = None, 0, 0
+    if rank == 0 or ws > 1:
+        W = sn.SparseBlockMatrix(s.nc, s.rowptr, s.colidx, s.blocks)
+        P = sn.FrictionContactProblem(3, s.nc, W, s.q, s.mu)
+        o = sn.SolverOptions()
+        o.iparam[sn.SICONOS_IPARAM_MAX_ITER] = S
+        o.dparam[sn.SICONOS_DPARAM_TOL] = 1e-8
+        o.dparam[sn.FC3DGPU_DPARAM_SWITCH_TOL] = 1e-300
+        o.dparam[sn.FC3DGPU_DPARAM_STALL] = 1e9
+        r = np.zeros(3 * s.nc)
+        u = np.zeros(3 * s.nc)
+
+        def e2e_step():
+            W.bump_version()  # a new W each step: full upload
+            r[:] = 0.0
+            info = sn.fc3d_nsgs_gpu(P, r, u, o)
+            if info < -1 and info != sn.NUMERICS_ERR_MAX_ITER:
+                raise RuntimeError(f"GPU solve failed ({info}): {sn.last_error()}")
+            return int(o.iparam[sn.SICONOS_IPARAM_ITER_DONE])
+
+        for _ in range(max(args.warmup, 1)):
+            e2e_step()
+        _barrier(ws)
+        t = time.perf_counter()
+        sw = 0
+        for _ in range(args.steps):
+            sw += e2e_step()
+        dt = _max_over_ranks(ws, time.perf_counter() - t)
+        e2e_value = s.nc * sw * ws / dt
+        h2d = s.nnzb * 9 * 8 + (s.nc + 1) * 8 + s.nnzb * 8 + s.nc * (24 + 8 + 24)
+        d2h = s.nc * 48
+        o.release()
+
+    cpu = None
+    if rank == 0 and args.cpu_sweeps > 0:
+        dt, _ = cpu_sample(s, args.cpu_sweeps, False)
+        cpu = {"value": s.nc * args.cpu_sweeps / dt, "unit": "contact-sweeps/s", "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_sweeps} sequential NSGS sweeps of the same {s.nc}-contact scene "
+                         f"(CPU restatement, bit-exact with the reference's fc3d_nsgs)"}
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": "contact-sweeps/s (FC3D NSGS, 60x60x30 lattice)", "value": value, "unit": "contact-sweeps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 sweeps, f64 residual",
+            "data": "synthetic",
+            "config": {"workload": f"{DIMS[0]}x{DIMS[1]}x{DIMS[2]} sphere lattice, {s.nc} contacts, {s.nnzb} "
+                                   f"blocks, mu {MU}, seed {SEED}; one fc3d solve per step from r=0, tol 1e-8, "
+                                   f"budget {S} sweeps (coloured FP32 sweeps + FP64 fc3d_compute_error)",
+                       "colours": stats[0]["colours"], "lanes_per_contact": stats[0]["lanes"],
+                       "grid": stats[0]["grid"], "l2": "flushed between steps (256 MB write outside the events)",
+                       "parallelism": "replicas" if ws > 1 else "1 GPU"},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "contact-sweeps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "sweep_ms_fp32": sum(fp32_ms) / max(1, sum(fp32_sweeps)),
+            "final_error": stats[-1]["error"],
+        }
+        print(json.dumps(line), flush=True)
+    d.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sweeps", type=int, default=100)
+    ap.add_argument("--cpu-sweeps", type=int, default=30)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        args.cpu_sweeps = max(1, min(args.cpu_sweeps, 10))
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

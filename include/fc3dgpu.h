@@ -100,6 +100,11 @@ int fc3dgpu_nsgs_batch(int nproblems, FrictionContactProblem **problems, double 
  * Returns the number of colours, <0 on failure. */
 int fc3dgpu_colour(int nc, const int64_t *rowptr, const int64_t *colidx, int kind, int32_t *colour);
 
+/* Device facts: SM count, L2 bytes, whether kernels can read pageable host
+ * memory (and through the host page tables), cooperative launch support,
+ * compute capability (major*10+minor).  Returns 0 or a negative code. */
+int fc3dgpu_device_info(int device, long long *out6);
+
 /* Last error message of this thread ("" when none). */
 const char *fc3dgpu_last_error(void);
 
@@ -159,6 +164,13 @@ int fc3dgpu_ctx_colours(fc3dgpu_ctx *ctx, int32_t *colour);
  * one solve, summed and largest SM cycles of one warp work unit, number of
  * units.  enable != 0 keeps counting in later solves.  out8 may be NULL. */
 int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out8);
+/* r = 0 on the device (PLI steps reset), without a host copy. */
+int fc3dgpu_ctx_zero_r(fc3dgpu_ctx *ctx);
+/* The CUDA stream (cudaStream_t) every kernel of this context runs on, for
+ * callers that time or order work around a solve. */
+void *fc3dgpu_ctx_stream(fc3dgpu_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+unsigned long long fc3dgpu_ctx_launches(fc3dgpu_ctx *ctx);
 /* Norm of q used by the relative error (default: computed from q). */
 int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx *ctx, double norm_q);
 

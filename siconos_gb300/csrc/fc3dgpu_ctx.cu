@@ -465,6 +465,7 @@ struct fc3dgpu_ctx {
   BUF(double, trace);
   BUF(unsigned long long, counters);
   int counters_on = 0;
+  unsigned long long launches = 0;  // kernels this library launched
 };
 
 static int grid1d(long long n, int block = 256) {
@@ -519,7 +520,7 @@ extern "C" fc3dgpu_ctx* fc3dgpu_ctx_create(int device) {
   // of each instance would otherwise pay the load inside a timed solve
   fc3dgpu::warm_sweep_kernels();
   bool ok = ensure(&c->partials, &c->partials_cap, 1024 * 8) == cudaSuccess &&
-            ensure(&c->barrier, &c->barrier_cap, 4) == cudaSuccess &&
+            ensure(&c->barrier, &c->barrier_cap, 1024) == cudaSuccess &&
             ensure(&c->status, &c->status_cap, 4) == cudaSuccess &&
             ensure(&c->scratch, &c->scratch_cap, 16) == cudaSuccess &&
             ensure(&c->scratch64, &c->scratch64_cap, 16) == cudaSuccess &&
@@ -742,6 +743,7 @@ extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const doubl
   CK(cudaMemcpyAsync(c->muo, mu, sizeof(double) * nc, cudaMemcpyHostToDevice, c->stream));
   k_set_q_mu<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->qo, c->muo, c->q64, c->mu64, c->q32, c->mu32);
   CK(cudaGetLastError());
+  c->launches++;
   // |q| as the reference computes it (a plain sum of squares in index order)
   double s2 = 0.0;
   for (long long i = 0; i < 3LL * nc; i++) s2 += q[i] * q[i];
@@ -762,9 +764,65 @@ extern "C" int fc3dgpu_ctx_set_r(fc3dgpu_ctx* c, const double* r) {
   CK(cudaMemcpyAsync(c->ro, r, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, c->stream));
   k_set_r<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->ro, c->r64, c->r32, c->rpli64, c->rpli32);
   CK(cudaGetLastError());
+  c->launches++;
   c->have_r = true;
   return 0;
 }
+
+// Reset the iterate on the device: r = 0 and the PLI steps to 1, as a solve
+// from a zero warm start after fc3dgpu_ctx_set_r(zeros) would have them.
+__global__ void k_zero_r(int npad, double* __restrict__ r64, float* __restrict__ r32, double* __restrict__ rpli64,
+                         float* __restrict__ rpli32) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p <= npad; p += gridDim.x * blockDim.x) {
+    for (int a = 0; a < 4; a++) {
+      r64[4 * (size_t)p + a] = 0.0;
+      r32[4 * (size_t)p + a] = 0.0f;
+    }
+    if (p < npad) {
+      rpli64[p] = 1.0;
+      rpli32[p] = 1.0f;
+    }
+  }
+}
+
+extern "C" int fc3dgpu_ctx_zero_r(fc3dgpu_ctx* c) {
+  if (!c || !c->have_W) {
+    fc3dgpu_set_error("fc3dgpu_ctx_zero_r: no problem");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  k_zero_r<<<grid1d(c->npad + 1), 256, 0, c->stream>>>(c->npad, c->r64, c->r32, c->rpli64, c->rpli32);
+  CK(cudaGetLastError());
+  c->launches++;
+  c->have_r = true;
+  return 0;
+}
+
+// Device facts: [0] SMs, [1] L2 bytes, [2] pageable host memory readable
+// by kernels, [3] ... through the host page tables, [4] cooperative launch,
+// [5] compute capability major*10+minor.  Returns 0 or a negative code.
+extern "C" int fc3dgpu_device_info(int device, long long* out6) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    fc3dgpu_set_error("no CUDA device %d", device);
+    return NUMERICS_ERR_NOT_IMPLEMENTED;
+  }
+  int v[6] = {0, 0, 0, 0, 0, 0}, ma = 0, mi = 0;
+  cudaDeviceGetAttribute(&v[0], cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&v[1], cudaDevAttrL2CacheSize, device);
+  cudaDeviceGetAttribute(&v[2], cudaDevAttrPageableMemoryAccess, device);
+  cudaDeviceGetAttribute(&v[3], cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+  cudaDeviceGetAttribute(&v[4], cudaDevAttrCooperativeLaunch, device);
+  cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, device);
+  cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, device);
+  v[5] = ma * 10 + mi;
+  for (int i = 0; i < 6; i++) out6[i] = v[i];
+  return 0;
+}
+
+extern "C" void* fc3dgpu_ctx_stream(fc3dgpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" unsigned long long fc3dgpu_ctx_launches(fc3dgpu_ctx* c) { return c ? c->launches : 0; }
 
 extern "C" int fc3dgpu_ctx_get_r_u(fc3dgpu_ctx* c, double* r, double* u) {
   using namespace fc3dgpu;
@@ -778,6 +836,7 @@ extern "C" int fc3dgpu_ctx_get_r_u(fc3dgpu_ctx* c, double* r, double* u) {
   CK(ensure(&c->uo, &c->uo_cap, (size_t)nc * 3));
   k_get_r_u<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->r64, c->u64, c->ro, c->uo);
   CK(cudaGetLastError());
+  c->launches++;
   if (r) CK(cudaMemcpyAsync(r, c->ro, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
   if (u) CK(cudaMemcpyAsync(u, c->uo, sizeof(double) * 3 * nc, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -862,8 +921,9 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     a.newton_max = p->newton_max;
     a.pli_max = p->pli_max;
     a.ls_max = p->ls_max;
-    CK(cudaMemsetAsync(c->barrier, 0, sizeof(unsigned), s));
+    CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
     CK(launch_sweep_f32(a, lanes, 0, s, &grid));
+    c->launches++;
     CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(c->ev[1], s));
     CK(cudaStreamSynchronize(s));
@@ -871,6 +931,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     S.incr_error = out[1];
     k_r32_to_r64<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r32, c->rpli32, c->r64, c->rpli64);
     CK(cudaGetLastError());
+    c->launches++;
   } else {
     CK(cudaEventRecord(c->ev[1], s));
   }
@@ -890,8 +951,9 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     a.pli_max = p->pli_max;
     a.ls_max = p->ls_max;
     int g64 = 0;
-    CK(cudaMemsetAsync(c->barrier, 0, sizeof(unsigned), s));
+    CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
     CK(launch_sweep_f64(a, lanes, 0, s, &g64));
+    c->launches++;
     if (!grid) grid = g64;
     CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
   }
@@ -946,7 +1008,7 @@ extern "C" int fc3dgpu_ctx_compute_error(fc3dgpu_ctx* c, double* error) {
   a.trace = nullptr;
   int g = 0;
   double out[8];
-  CK(cudaMemsetAsync(c->barrier, 0, sizeof(unsigned), s));
+  CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
   CK(cudaMemsetAsync(c->status, 0, sizeof(int), s));
   CK(launch_sweep_f64(a, 1, 0, s, &g));
   CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));

@@ -153,12 +153,15 @@ typedef struct {
   int64_t *rowptr;
   int64_t *colidx;
   double *blocks;
+  int borrowed; /* arrays point into the caller's SBM, not owned */
 } Bcsr;
 
 static void bcsr_free(Bcsr *b) {
-  free(b->rowptr);
-  free(b->colidx);
-  free(b->blocks);
+  if (!b->borrowed) {
+    free(b->rowptr);
+    free(b->colidx);
+    free(b->blocks);
+  }
   memset(b, 0, sizeof(*b));
 }
 
@@ -187,6 +190,20 @@ static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
     const size_t nrows_filled = S->filled1 ? S->filled1 - 1 : 0;
     const long long nnzb = (long long)(nrows_filled ? S->index1_data[nrows_filled] : 0);
     out->nnzb = nnzb;
+    /* Zero-copy view when every block row is filled and the blocks sit
+     * back to back in one allocation (size_t and int64_t share a layout on
+     * the LP64 targets this library builds for). */
+    if (sizeof(size_t) == sizeof(int64_t) && nrows_filled == (size_t)nc && nnzb > 0) {
+      int contiguous = 1;
+      for (long long k = 1; k < nnzb && contiguous; k++) contiguous = (S->block[k] == S->block[0] + 9 * k);
+      if (contiguous) {
+        out->rowptr = (int64_t *)S->index1_data;
+        out->colidx = (int64_t *)S->index2_data;
+        out->blocks = S->block[0];
+        out->borrowed = 1;
+        return 0;
+      }
+    }
     out->rowptr = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nc + 1));
     out->colidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nnzb ? nnzb : 1));
     out->blocks = (double *)malloc(sizeof(double) * 9 * (size_t)(nnzb ? nnzb : 1));

@@ -31,29 +31,45 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
-// Grid-wide barrier with a poll limit.  On expiry the block records
-// FC3DGPU_STATUS_BARRIER_TIMEOUT and returns false; its caller leaves the
-// kernel, and every other block then times out at its next barrier.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned& epoch, unsigned long long limit, int* status) {
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier with a poll limit.  Each block publishes its barrier
+// count in its own flag word (a store, no contended atomic), and one warp of
+// every block polls all flags, 32 at a time, until each shows the count.  On
+// expiry the block records FC3DGPU_STATUS_BARRIER_TIMEOUT and returns false;
+// its caller leaves the kernel, and every other block then times out at its
+// next barrier.  The flags must be zero at launch.
+__device__ __forceinline__ bool grid_barrier(unsigned* flags, unsigned& epoch, unsigned long long limit, int* status) {
   __shared__ int s_ok;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    epoch++;
-    const unsigned target = epoch * gridDim.x;
-    __threadfence();
-    atomicAdd(bar, 1u);
+  epoch++;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    if (lane == 0) {
+      __threadfence();
+      st_release_u32(&flags[blockIdx.x], epoch);
+    }
     unsigned long long n = 0;
     int ok = 1;
-    while (ld_acquire_u32(bar) < target) {
+    for (;;) {
+      bool mine = true;
+      for (int b = lane; b < (int)gridDim.x; b += 32)
+        if (ld_acquire_u32(&flags[b]) < epoch) {
+          mine = false;
+          break;
+        }
+      if (__all_sync(0xffffffffu, mine)) break;
       if (++n > limit) {
         ok = 0;
-        atomicOr(status, 1);
+        if (lane == 0) atomicOr(status, 1);
         break;
       }
-      if (n > 64) __nanosleep(64);
+      if (n > 256) __nanosleep(32);
     }
     __threadfence();
-    s_ok = ok;
+    if (lane == 0) s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;

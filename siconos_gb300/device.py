@@ -55,6 +55,15 @@ class DeviceSolver:
         self._check(rc, "solve")
         return st.as_dict()
 
+    def zero_r(self):
+        self._check(self.L.fc3dgpu_ctx_zero_r(self.ctx), "zero_r")
+
+    def stream(self) -> int:
+        return int(self.L.fc3dgpu_ctx_stream(self.ctx) or 0)
+
+    def launches(self) -> int:
+        return int(self.L.fc3dgpu_ctx_launches(self.ctx))
+
     def get(self):
         r = np.zeros(3 * self.nc)
         u = np.zeros(3 * self.nc)

@@ -142,6 +142,7 @@ ABI = {
                                      C.POINTER(_SO), C.POINTER(C.c_int)]),
     "fc3dgpu_colour": (C.c_int, [C.c_int, _I64, _I64, C.c_int, _I32]),
     "fc3dgpu_last_error": (C.c_char_p, []),
+    "fc3dgpu_device_info": (C.c_int, [C.c_int, C.c_void_p]),
     "fc3dgpu_params_default": (None, [C.POINTER(FC3DGPUParams)]),
     "fc3dgpu_ctx_create": (C.c_void_p, [C.c_int]),
     "fc3dgpu_ctx_destroy": (None, [C.c_void_p]),
@@ -155,6 +156,9 @@ ABI = {
     "fc3dgpu_ctx_colours": (C.c_int, [C.c_void_p, _I32]),
     "fc3dgpu_ctx_counters": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "fc3dgpu_ctx_set_norm_q": (C.c_int, [C.c_void_p, C.c_double]),
+    "fc3dgpu_ctx_zero_r": (C.c_int, [C.c_void_p]),
+    "fc3dgpu_ctx_stream": (C.c_void_p, [C.c_void_p]),
+    "fc3dgpu_ctx_launches": (C.c_ulonglong, [C.c_void_p]),
     "fc3dgpu_lattice_create": (C.c_void_p, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double, C.c_double]),
     "fc3dgpu_lattice_free": (None, [C.c_void_p]),
     "fc3dgpu_lattice_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
@@ -180,6 +184,14 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def device_info(device: int = 0) -> dict:
+    out = np.zeros(6, np.int64)
+    if lib().fc3dgpu_device_info(device, out.ctypes.data) != 0:
+        raise RuntimeError(last_error())
+    return dict(zip(["sms", "l2_bytes", "pageable_access", "pageable_uses_host_page_tables", "cooperative",
+                     "cc"], (int(v) for v in out)))
 
 
 def last_error() -> str:
