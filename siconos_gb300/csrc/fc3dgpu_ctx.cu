@@ -876,12 +876,14 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
 }
 
 static int autotune_lanes(fc3dgpu_ctx* c) {
-  // contacts per colour phase vs. resident warps: more lanes per contact when
-  // a phase has too few contacts to fill the GPU
+  // Measured on GB300 (60x60x30 lattice, 10 colours): one lane per contact
+  // is fastest while a colour phase holds at least one 32-contact slab per
+  // resident warp; splitting a contact over more lanes only pays when the
+  // phases are too small to give every warp a slab.
   const long long per_phase = (long long)c->nc / (c->ncol > 0 ? c->ncol : 1);
-  const long long warps = (long long)c->nsm * 32;
-  if (per_phase >= 16 * warps) return 1;
-  if (per_phase >= 4 * warps) return 2;
+  const long long warps = (long long)c->nsm * 16;
+  if (per_phase >= 32 * warps / 4) return 1;
+  if (per_phase >= 32 * warps / 16) return 2;
   return 4;
 }
 
