@@ -31,13 +31,20 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // Grid-wide barrier with a poll limit.  Each block publishes its barrier
 // count in its own flag word (a store, no contended atomic), and one warp of
-// every block polls all flags, 32 at a time, until each shows the count.  On
+// every block polls all flags with relaxed loads issued together (one memory
+// round trip per poll) until each shows the count, then fences (acquire).  On
 // expiry the block records FC3DGPU_STATUS_BARRIER_TIMEOUT and returns false;
 // its caller leaves the kernel, and every other block then times out at its
 // next barrier.  The flags must be zero at launch.
@@ -55,11 +62,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned* flags, unsigned& epoch, u
     int ok = 1;
     for (;;) {
       bool mine = true;
-      for (int b = lane; b < (int)gridDim.x; b += 32)
-        if (ld_acquire_u32(&flags[b]) < epoch) {
-          mine = false;
-          break;
-        }
+#pragma unroll 8
+      for (int b = lane; b < (int)gridDim.x; b += 32) mine &= (ld_relaxed_u32(&flags[b]) >= epoch);
       if (__all_sync(0xffffffffu, mine)) break;
       if (++n > limit) {
         ok = 0;
@@ -247,6 +251,134 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   }
 }
 
+// Work list of one block: the contacts of the current batch whose local
+// problem is not the trivial take-off, packed densely.
+template <typename Real>
+struct WorkList {
+  int p[FC3D_BLOCK];
+  Real q[FC3D_BLOCK][3];
+  Real ro[FC3D_BLOCK][3];
+  int wcount[FC3D_BLOCK / 32];
+};
+
+// One colour with one lane per contact.  A block takes blockDim/32
+// consecutive slabs; every lane forms its contact's local q (same slot
+// order as the reference's row product).  A contact with q_n > -eps is the
+// trivial take-off of the local solver (onecontact.c:234-245): r = 0,
+// finished at once.  The others are packed in warp order (ballot + fixed
+// prefix, so the packing is deterministic) and solved by the first threads of
+// the block, which keeps lanes busy instead of idling beside take-offs.
+template <typename Real>
+__device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a, int s0, int s1, Real ltol,
+                                                       double& dr2, double& rr2, WorkList<Real>& wk) {
+  const int nwb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int sb = s0 + blockIdx.x * nwb; sb < s1; sb += gridDim.x * nwb) {
+    const int slab = sb + w;
+    const int p = slab * FC3D_SLAB + lane;
+    bool work = false;
+    Real acc[3] = {0, 0, 0}, ro[3] = {0, 0, 0};
+    if (slab < s1 && __ldg(&a.perm[p]) >= 0) {
+      const long long base = a.slab_off[slab];
+      const int ns = a.slab_nslot[slab];
+      const size_t qi = (size_t)slab * 3 * FC3D_SLAB + lane;
+      acc[0] = a.q[qi];
+      acc[1] = a.q[qi + FC3D_SLAB];
+      acc[2] = a.q[qi + 2 * FC3D_SLAB];
+      constexpr int CH = sizeof(Real) == 4 ? 8 : 4;
+      for (int t0 = 0; t0 < ns; t0 += CH) {
+        int pj[CH];
+        Real wv[CH][9];
+#pragma unroll
+        for (int c = 0; c < CH; c++) {
+          const int s = t0 + c;
+          const size_t sl = (size_t)(base + (s < ns ? s : 0));
+          pj[c] = s < ns ? __ldg(&a.col[sl * FC3D_SLAB + lane]) : a.npad;
+          const Real* wp = a.W + sl * 9 * FC3D_SLAB + lane;
+#pragma unroll
+          for (int e = 0; e < 9; e++) wv[c][e] = s < ns ? __ldg(&wp[e * FC3D_SLAB]) : Real(0);
+        }
+        Real rv[CH][3];
+#pragma unroll
+        for (int c = 0; c < CH; c++) load_r3<Real>(a.r, pj[c], rv[c]);
+#pragma unroll
+        for (int c = 0; c < CH; c++)
+          if (t0 + c < ns) mvp3x3(wv[c], rv[c], acc);
+      }
+      load_r3<Real>(a.r, p, ro);
+      if (acc[0] > -Eps<Real>::v()) {
+        Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
+        rp[0] = 0;
+        rp[1] = 0;
+        rp[2] = 0;
+        dr2 += (double)ro[0] * ro[0] + (double)ro[1] * ro[1] + (double)ro[2] * ro[2];
+      } else {
+        work = true;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, work);
+    if (lane == 0) wk.wcount[w] = __popc(m);
+    __syncthreads();
+    int off = 0, total = 0;
+    for (int k = 0; k < nwb; k++) {
+      const int v = wk.wcount[k];
+      off += k < w ? v : 0;
+      total += v;
+    }
+    if (work) {
+      const int idx = off + __popc(m & ((1u << lane) - 1));
+      wk.p[idx] = p;
+      wk.q[idx][0] = acc[0];
+      wk.q[idx][1] = acc[1];
+      wk.q[idx][2] = acc[2];
+      wk.ro[idx][0] = ro[0];
+      wk.ro[idx][1] = ro[1];
+      wk.ro[idx][2] = ro[2];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int pp = wk.p[t];
+      const int sl = pp / FC3D_SLAB, k = pp % FC3D_SLAB;
+      LocalProblem<Real> L;
+#pragma unroll
+      for (int e = 0; e < 9; e++) L.M[e] = __ldg(&a.D[((size_t)sl * 9 + e) * FC3D_SLAB + k]);
+      L.q[0] = wk.q[t][0];
+      L.q[1] = wk.q[t][1];
+      L.q[2] = wk.q[t][2];
+      L.mu = __ldg(&a.mu[(size_t)sl * FC3D_SLAB + k]);
+      L.rhoN = __ldg(&a.rho[((size_t)sl * 2) * FC3D_SLAB + k]);
+      L.rhoT = __ldg(&a.rho[((size_t)sl * 2 + 1) * FC3D_SLAB + k]);
+      L.rho_pli = __ldcg(&a.rpli[pp]);
+      L.tol = ltol;
+      L.newton_max = a.newton_max;
+      L.pli_max = a.pli_max;
+      L.ls_max = a.ls_max;
+      L.n_newton = 0;
+      L.n_pli = 0;
+      L.n_ls = 0;
+      Real o[3] = {wk.ro[t][0], wk.ro[t][1], wk.ro[t][2]};
+      Real rn[3] = {o[0], o[1], o[2]};
+      local_solve(L, rn);
+      Real* rp = a.r + (size_t)pp * FC3D_RSTRIDE;
+      rp[0] = rn[0];
+      rp[1] = rn[1];
+      rp[2] = rn[2];
+      a.rpli[pp] = L.rho_pli;
+      const double d0 = (double)o[0] - (double)rn[0], d1 = (double)o[1] - (double)rn[1],
+                   d2 = (double)o[2] - (double)rn[2];
+      dr2 += d0 * d0 + d1 * d1 + d2 * d2;
+      rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+      if (a.counters) {
+        atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
+        atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);
+        atomicAdd(&a.counters[2], (unsigned long long)L.n_ls);
+        atomicAdd(&a.counters[3], 1ULL);
+        atomicMax(&a.counters[4], (unsigned long long)L.n_newton);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // u = q + W r for every row in CSR block order (diagonal at its own slot
 // position, SBM_gemv_3x3, SparseBlockMatrix.c:360-419) and the partial sums
 // of the squared natural-map error, |u|^2 and |r|^2.  FP64 only.
@@ -308,6 +440,7 @@ __device__ __forceinline__ bool full_error_phase(const SweepArgs<Real>& a, int s
 
 template <typename Real, int T>
 __global__ void __launch_bounds__(FC3D_BLOCK) nsgs_kernel(const SweepArgs<Real> a) {
+  __shared__ WorkList<Real> wk;
   const int lane = threadIdx.x & 31;
   const int nwb = blockDim.x >> 5;
   const int gw = blockIdx.x * nwb + (threadIdx.x >> 5), tw = gridDim.x * nwb;
@@ -321,16 +454,20 @@ __global__ void __launch_bounds__(FC3D_BLOCK) nsgs_kernel(const SweepArgs<Real> 
     double acc[2] = {0.0, 0.0};
     for (int c = 0; c < a.ncol; c++) {
       const int s0 = a.sptr[c], nunits = (a.sptr[c + 1] - s0) * T;
-      for (int u = gw; u < nunits; u += tw) {
-        const long long t0 = a.counters ? clock64() : 0;
-        process_unit<Real, T>(a, s0 + u / T, u % T, lane, (Real)local_tol, acc[0], acc[1]);
-        if (a.counters) {
-          __syncwarp();
-          if (lane == 0) {
-            const unsigned long long dt = (unsigned long long)(clock64() - t0);
-            atomicAdd(&a.counters[5], dt);
-            atomicMax(&a.counters[6], dt);
-            atomicAdd(&a.counters[7], 1ULL);
+      if (T == 1) {
+        process_colour_compact<Real>(a, s0, a.sptr[c + 1], (Real)local_tol, acc[0], acc[1], wk);
+      } else {
+        for (int u = gw; u < nunits; u += tw) {
+          const long long t0 = a.counters ? clock64() : 0;
+          process_unit<Real, T>(a, s0 + u / T, u % T, lane, (Real)local_tol, acc[0], acc[1]);
+          if (a.counters) {
+            __syncwarp();
+            if (lane == 0) {
+              const unsigned long long dt = (unsigned long long)(clock64() - t0);
+              atomicAdd(&a.counters[5], dt);
+              atomicMax(&a.counters[6], dt);
+              atomicAdd(&a.counters[7], 1ULL);
+            }
           }
         }
       }
