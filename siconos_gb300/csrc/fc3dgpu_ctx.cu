@@ -466,6 +466,8 @@ struct fc3dgpu_ctx {
   BUF(unsigned long long, counters);
   int counters_on = 0;
   unsigned long long launches = 0;  // kernels this library launched
+  BUF(unsigned long long, timeline);
+  int timeline_sweep = 0;
 };
 
 static int grid1d(long long n, int block = 256) {
@@ -543,7 +545,7 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->rowlen, c->dpos, c->slab_nslot, c->slab_off, c->W64, c->W32, c->col, c->D64, c->D32,
                   c->rho64, c->rho32, c->q64, c->q32, c->mu64, c->mu32, c->r64, c->r32, c->rpli64, c->rpli32,
                   c->u64, c->partials, c->barrier, c->status, c->scratch, c->scratch64, c->out, c->trace,
-                  c->counters};
+                  c->counters, c->timeline};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; i++)
@@ -872,6 +874,8 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.norm_q = c->norm_q;
   a.spin_limit = 1ULL << 22;
   a.counters = c->counters_on ? c->counters : nullptr;
+  a.timeline = c->timeline_sweep > 0 ? c->timeline : nullptr;
+  a.timeline_sweep = c->timeline_sweep;
   a.out = c->out;
 }
 
@@ -1032,6 +1036,25 @@ extern "C" int fc3dgpu_ctx_counters(fc3dgpu_ctx* c, int enable, unsigned long lo
   CK(cudaMemsetAsync(c->counters, 0, 8 * sizeof(unsigned long long), c->stream));
   c->counters_on = enable;
   return 0;
+}
+
+// Phase timeline of one sweep of the next solves: for colour c and block b,
+// out[(c*grid + b)*2 + {0,1}] = globaltimer (ns) at the phase start and at
+// the end of the block's work.  sweep = 0 switches it off.  Returns the
+// number of entries available (ncol * grid * 2) after a solve.
+extern "C" int fc3dgpu_ctx_timeline(fc3dgpu_ctx* c, int sweep, unsigned long long* out, int cap) {
+  if (!c) return -1;
+  CK(cudaSetDevice(c->device));
+  const size_t need = (size_t)FC3D_MAX_COLOURS * 1024 * 2;
+  CK(ensure(&c->timeline, &c->timeline_cap, need));
+  int n = 0;
+  if (out && c->timeline_sweep > 0) {
+    n = cap < (int)need ? cap : (int)need;
+    CK(cudaMemcpyAsync(out, c->timeline, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  c->timeline_sweep = sweep;
+  return n;
 }
 
 extern "C" int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx* c, double norm_q) {

@@ -64,6 +64,8 @@ struct SweepArgs {
   int newton_max, pli_max, ls_max;
   unsigned long long spin_limit;
   unsigned long long* counters;  // optional work counters: Newton its, PLI its, line-search evals, solves, max Newton
+  unsigned long long* timeline;  // optional: globaltimer at each colour phase's start and work end, per block
+  int timeline_sweep;            // the sweep (1-based) the timeline records
   // outputs (written by block 0, thread 0)
   double* out;                  // [0] sweeps, [1] incr, [2] full error, [3] info, [4] working tol
 };

@@ -31,6 +31,12 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   return v;
 }
 
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -439,7 +445,7 @@ __device__ __forceinline__ bool full_error_phase(const SweepArgs<Real>& a, int s
 }
 
 template <typename Real, int T>
-__global__ void __launch_bounds__(FC3D_BLOCK) nsgs_kernel(const SweepArgs<Real> a) {
+__global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Real> a) {
   __shared__ WorkList<Real> wk;
   const int lane = threadIdx.x & 31;
   const int nwb = blockDim.x >> 5;
@@ -454,6 +460,8 @@ __global__ void __launch_bounds__(FC3D_BLOCK) nsgs_kernel(const SweepArgs<Real> 
     double acc[2] = {0.0, 0.0};
     for (int c = 0; c < a.ncol; c++) {
       const int s0 = a.sptr[c], nunits = (a.sptr[c + 1] - s0) * T;
+      const bool tl = a.timeline && sweep == a.timeline_sweep && threadIdx.x == 0;
+      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 2] = globaltimer_ns();
       if (T == 1) {
         process_colour_compact<Real>(a, s0, a.sptr[c + 1], (Real)local_tol, acc[0], acc[1], wk);
       } else {
@@ -472,6 +480,7 @@ __global__ void __launch_bounds__(FC3D_BLOCK) nsgs_kernel(const SweepArgs<Real> 
         }
       }
       if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
+      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 2 + 1] = globaltimer_ns();
       if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) return;
     }
     double s[2];

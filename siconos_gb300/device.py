@@ -55,6 +55,13 @@ class DeviceSolver:
         self._check(rc, "solve")
         return st.as_dict()
 
+    def timeline(self, sweep: int = 0, cap: int = 1 << 20):
+        """Arm the phase timeline for `sweep` of the next solves and return
+        the previous record as an array (colour, block, [start, end])."""
+        out = np.zeros(cap, np.uint64)
+        n = self.L.fc3dgpu_ctx_timeline(self.ctx, sweep, out.ctypes.data, cap)
+        return out[:max(n, 0)]
+
     def zero_r(self):
         self._check(self.L.fc3dgpu_ctx_zero_r(self.ctx), "zero_r")
 
