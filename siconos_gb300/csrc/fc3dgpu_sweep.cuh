@@ -257,88 +257,111 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   }
 }
 
-// Work list of one block: the contacts of the current batch whose local
+#define FC3D_PASS_SLABS 16
+
+// Work list of one block: the contacts of the current pass whose local
 // problem is not the trivial take-off, packed densely.
 template <typename Real>
 struct WorkList {
-  int p[FC3D_BLOCK];
-  Real q[FC3D_BLOCK][3];
-  Real ro[FC3D_BLOCK][3];
-  int wcount[FC3D_BLOCK / 32];
+  int p[FC3D_PASS_SLABS * FC3D_SLAB];
+  Real q[FC3D_PASS_SLABS * FC3D_SLAB][3];
+  Real ro[FC3D_PASS_SLABS * FC3D_SLAB][3];
+  int count[FC3D_PASS_SLABS];
 };
 
-// One colour with one lane per contact.  A block takes blockDim/32
-// consecutive slabs; every lane forms its contact's local q (same slot
-// order as the reference's row product).  A contact with q_n > -eps is the
-// trivial take-off of the local solver (onecontact.c:234-245): r = 0,
-// finished at once.  The others are packed in warp order (ballot + fixed
-// prefix, so the packing is deterministic) and solved by the first threads of
-// the block, which keeps lanes busy instead of idling beside take-offs.
+// One colour with one lane per contact.  The colour's slabs are split into
+// one contiguous range per block (so no block takes a second round while
+// others idle) and a block handles its range in passes of up to
+// FC3D_PASS_SLABS slabs.  Every lane forms its contact's local q in the
+// reference's slot order.  A contact with q_n > -eps is the trivial take-off
+// of the local solver (onecontact.c:234-245): r = 0, finished at once.  The
+// others are packed in slab order (ballot + fixed prefix, so the packing is
+// deterministic) and solved by the first threads of the block: one local
+// solve latency per pass, with lanes busy instead of idling beside
+// take-offs.
 template <typename Real>
 __device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a, int s0, int s1, Real ltol,
                                                        double& dr2, double& rr2, WorkList<Real>& wk) {
-  const int nwb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int sb = s0 + blockIdx.x * nwb; sb < s1; sb += gridDim.x * nwb) {
-    const int slab = sb + w;
-    const int p = slab * FC3D_SLAB + lane;
-    bool work = false;
-    Real acc[3] = {0, 0, 0}, ro[3] = {0, 0, 0};
-    if (slab < s1 && __ldg(&a.perm[p]) >= 0) {
-      const long long base = a.slab_off[slab];
-      const int ns = a.slab_nslot[slab];
-      const size_t qi = (size_t)slab * 3 * FC3D_SLAB + lane;
-      acc[0] = a.q[qi];
-      acc[1] = a.q[qi + FC3D_SLAB];
-      acc[2] = a.q[qi + 2 * FC3D_SLAB];
-      constexpr int CH = sizeof(Real) == 4 ? 8 : 4;
-      for (int t0 = 0; t0 < ns; t0 += CH) {
-        int pj[CH];
-        Real wv[CH][9];
+  constexpr int NWB = FC3D_BLOCK / 32;
+  constexpr int MAXR = (FC3D_PASS_SLABS + NWB - 1) / NWB;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = s1 - s0;
+  const int lo = s0 + (int)((long long)n * blockIdx.x / gridDim.x);
+  const int hi = s0 + (int)((long long)n * (blockIdx.x + 1) / gridDim.x);
+  for (int ps = lo; ps < hi; ps += FC3D_PASS_SLABS) {
+    const int np = min(FC3D_PASS_SLABS, hi - ps);
+    Real acc[MAXR][3], ro[MAXR][3];
+    unsigned msk[MAXR];
 #pragma unroll
-        for (int c = 0; c < CH; c++) {
-          const int s = t0 + c;
-          const size_t sl = (size_t)(base + (s < ns ? s : 0));
-          pj[c] = s < ns ? __ldg(&a.col[sl * FC3D_SLAB + lane]) : a.npad;
-          const Real* wp = a.W + sl * 9 * FC3D_SLAB + lane;
+    for (int j = 0; j < MAXR; j++) {
+      const int i = w + j * NWB;
+      msk[j] = 0;
+      if (i < np) {
+        const int slab = ps + i;
+        const int p = slab * FC3D_SLAB + lane;
+        bool work = false;
+        acc[j][0] = acc[j][1] = acc[j][2] = 0;
+        ro[j][0] = ro[j][1] = ro[j][2] = 0;
+        if (__ldg(&a.perm[p]) >= 0) {
+          const long long base = a.slab_off[slab];
+          const int ns = a.slab_nslot[slab];
+          const size_t qi = (size_t)slab * 3 * FC3D_SLAB + lane;
+          acc[j][0] = a.q[qi];
+          acc[j][1] = a.q[qi + FC3D_SLAB];
+          acc[j][2] = a.q[qi + 2 * FC3D_SLAB];
+          constexpr int CH = sizeof(Real) == 4 ? 8 : 4;
+          for (int t0 = 0; t0 < ns; t0 += CH) {
+            int pj[CH];
+            Real wv[CH][9];
 #pragma unroll
-          for (int e = 0; e < 9; e++) wv[c][e] = s < ns ? __ldg(&wp[e * FC3D_SLAB]) : Real(0);
+            for (int c = 0; c < CH; c++) {
+              const int sidx = t0 + c;
+              const size_t sl = (size_t)(base + (sidx < ns ? sidx : 0));
+              pj[c] = sidx < ns ? __ldg(&a.col[sl * FC3D_SLAB + lane]) : a.npad;
+              const Real* wp = a.W + sl * 9 * FC3D_SLAB + lane;
+#pragma unroll
+              for (int e = 0; e < 9; e++) wv[c][e] = sidx < ns ? __ldg(&wp[e * FC3D_SLAB]) : Real(0);
+            }
+            Real rv[CH][3];
+#pragma unroll
+            for (int c = 0; c < CH; c++) load_r3<Real>(a.r, pj[c], rv[c]);
+#pragma unroll
+            for (int c = 0; c < CH; c++)
+              if (t0 + c < ns) mvp3x3(wv[c], rv[c], acc[j]);
+          }
+          load_r3<Real>(a.r, p, ro[j]);
+          if (acc[j][0] > -Eps<Real>::v()) {
+            Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
+            rp[0] = 0;
+            rp[1] = 0;
+            rp[2] = 0;
+            dr2 += (double)ro[j][0] * ro[j][0] + (double)ro[j][1] * ro[j][1] + (double)ro[j][2] * ro[j][2];
+          } else {
+            work = true;
+          }
         }
-        Real rv[CH][3];
-#pragma unroll
-        for (int c = 0; c < CH; c++) load_r3<Real>(a.r, pj[c], rv[c]);
-#pragma unroll
-        for (int c = 0; c < CH; c++)
-          if (t0 + c < ns) mvp3x3(wv[c], rv[c], acc);
-      }
-      load_r3<Real>(a.r, p, ro);
-      if (acc[0] > -Eps<Real>::v()) {
-        Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
-        rp[0] = 0;
-        rp[1] = 0;
-        rp[2] = 0;
-        dr2 += (double)ro[0] * ro[0] + (double)ro[1] * ro[1] + (double)ro[2] * ro[2];
-      } else {
-        work = true;
+        msk[j] = __ballot_sync(0xffffffffu, work);
+        if (lane == 0) wk.count[i] = __popc(msk[j]);
       }
     }
-    const unsigned m = __ballot_sync(0xffffffffu, work);
-    if (lane == 0) wk.wcount[w] = __popc(m);
     __syncthreads();
-    int off = 0, total = 0;
-    for (int k = 0; k < nwb; k++) {
-      const int v = wk.wcount[k];
-      off += k < w ? v : 0;
-      total += v;
-    }
-    if (work) {
-      const int idx = off + __popc(m & ((1u << lane) - 1));
-      wk.p[idx] = p;
-      wk.q[idx][0] = acc[0];
-      wk.q[idx][1] = acc[1];
-      wk.q[idx][2] = acc[2];
-      wk.ro[idx][0] = ro[0];
-      wk.ro[idx][1] = ro[1];
-      wk.ro[idx][2] = ro[2];
+    int total = 0;
+    for (int k = 0; k < np; k++) total += wk.count[k];
+#pragma unroll
+    for (int j = 0; j < MAXR; j++) {
+      const int i = w + j * NWB;
+      if (i < np && (msk[j] >> lane) & 1u) {
+        int off = 0;
+        for (int k = 0; k < i; k++) off += wk.count[k];
+        const int idx = off + __popc(msk[j] & ((1u << lane) - 1));
+        wk.p[idx] = (ps + i) * FC3D_SLAB + lane;
+        wk.q[idx][0] = acc[j][0];
+        wk.q[idx][1] = acc[j][1];
+        wk.q[idx][2] = acc[j][2];
+        wk.ro[idx][0] = ro[j][0];
+        wk.ro[idx][1] = ro[j][1];
+        wk.ro[idx][2] = ro[j][2];
+      }
     }
     __syncthreads();
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
