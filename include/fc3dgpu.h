@@ -164,9 +164,10 @@ int fc3dgpu_ctx_colours(fc3dgpu_ctx *ctx, int32_t *colour);
  * one solve, summed and largest SM cycles of one warp work unit, number of
  * units.  enable != 0 keeps counting in later solves.  out8 may be NULL. */
 int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out8);
-/* Phase timeline: in the next solves, record for sweep `sweep` (1-based)
- * the globaltimer (ns) at each colour phase's start and at the end of each
- * block's work, out[(colour*grid + block)*2 + {0,1}]; copies the last record
+/* Phase timeline: in the next solves, record for sweep `sweep` (1-based),
+ * per colour and block, out[(colour*grid + block)*4 + {0..3}] = globaltimer
+ * (ns) at the phase start, at the end of the block's work, after its
+ * row-product pass, and its number of local solves; copies the last record
  * into out (cap entries) and returns how many were copied.  sweep 0 stops. */
 int fc3dgpu_ctx_timeline(fc3dgpu_ctx *ctx, int sweep, unsigned long long *out, int cap);
 /* r = 0 on the device (PLI steps reset), without a host copy. */

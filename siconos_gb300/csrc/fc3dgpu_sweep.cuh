@@ -281,7 +281,8 @@ struct WorkList {
 // take-offs.
 template <typename Real>
 __device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a, int s0, int s1, Real ltol,
-                                                       double& dr2, double& rr2, WorkList<Real>& wk) {
+                                                       double& dr2, double& rr2, WorkList<Real>& wk,
+                                                       unsigned long long* tl) {
   constexpr int NWB = FC3D_BLOCK / 32;
   constexpr int MAXR = (FC3D_PASS_SLABS + NWB - 1) / NWB;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -347,6 +348,10 @@ __device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a,
     __syncthreads();
     int total = 0;
     for (int k = 0; k < np; k++) total += wk.count[k];
+    if (tl && threadIdx.x == 0) {
+      tl[0] = globaltimer_ns();
+      tl[1] = (unsigned long long)total;
+    }
 #pragma unroll
     for (int j = 0; j < MAXR; j++) {
       const int i = w + j * NWB;
@@ -484,9 +489,14 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
     for (int c = 0; c < a.ncol; c++) {
       const int s0 = a.sptr[c], nunits = (a.sptr[c + 1] - s0) * T;
       const bool tl = a.timeline && sweep == a.timeline_sweep && threadIdx.x == 0;
-      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 2] = globaltimer_ns();
+      if (tl) {
+        a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4] = globaltimer_ns();
+        a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 2] = 0;
+        a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 3] = 0;
+      }
       if (T == 1) {
-        process_colour_compact<Real>(a, s0, a.sptr[c + 1], (Real)local_tol, acc[0], acc[1], wk);
+        process_colour_compact<Real>(a, s0, a.sptr[c + 1], (Real)local_tol, acc[0], acc[1], wk,
+                                     tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 4 + 2 : nullptr);
       } else {
         for (int u = gw; u < nunits; u += tw) {
           const long long t0 = a.counters ? clock64() : 0;
@@ -503,7 +513,7 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
         }
       }
       if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
-      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 2 + 1] = globaltimer_ns();
+      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 1] = globaltimer_ns();
       if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) return;
     }
     double s[2];
