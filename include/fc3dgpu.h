@@ -170,6 +170,9 @@ int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out8)
  * row-product pass, and its number of local solves; copies the last record
  * into out (cap entries) and returns how many were copied.  sweep 0 stops. */
 int fc3dgpu_ctx_timeline(fc3dgpu_ctx *ctx, int sweep, unsigned long long *out, int cap);
+/* Bulk-copy (TMA) staging of each block's slab range into shared memory
+ * in the FP32 sweeps: 1 on (default), 0 off.  Returns the previous value. */
+int fc3dgpu_ctx_staging(fc3dgpu_ctx *ctx, int on);
 /* r = 0 on the device (PLI steps reset), without a host copy. */
 int fc3dgpu_ctx_zero_r(fc3dgpu_ctx *ctx);
 /* The CUDA stream (cudaStream_t) every kernel of this context runs on, for

@@ -359,6 +359,8 @@ __global__ void k_get_r_u(int nc, const int* __restrict__ iperm, const double* _
 // ---------------------------------------------------------------------------
 #include <math.h>
 #include <stdarg.h>
+
+#include <vector>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -468,6 +470,9 @@ struct fc3dgpu_ctx {
   unsigned long long launches = 0;  // kernels this library launched
   BUF(unsigned long long, timeline);
   int timeline_sweep = 0;
+  std::vector<long long> slab_off_h;
+  std::vector<int> slab_nslot_h;
+  int staging = 1;  // bulk-copy staging of slab ranges for the FP32 sweeps
 };
 
 static int grid1d(long long n, int block = 256) {
@@ -690,6 +695,10 @@ extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, 
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
   c->nslots = nslots;
+  c->slab_off_h.resize(nslab);
+  c->slab_nslot_h.resize(nslab);
+  CK(cudaMemcpyAsync(c->slab_off_h.data(), c->slab_off, sizeof(long long) * nslab, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(c->slab_nslot_h.data(), c->slab_nslot, sizeof(int) * nslab, cudaMemcpyDeviceToHost, s));
   const size_t nw = (size_t)(nslots ? nslots : 1) * 9 * FC3D_SLAB;
   CK(ensure(&c->W64, &c->W64_cap, nw));
   CK(ensure(&c->W32, &c->W32_cap, nw));
@@ -787,6 +796,15 @@ __global__ void k_zero_r(int npad, double* __restrict__ r64, float* __restrict__
   }
 }
 
+// Bulk-copy staging of slab ranges in the FP32 sweeps: on (1, default) or
+// off (0).  Returns the previous setting.
+extern "C" int fc3dgpu_ctx_staging(fc3dgpu_ctx* c, int on) {
+  if (!c) return -1;
+  const int old = c->staging;
+  c->staging = on ? 1 : 0;
+  return old;
+}
+
 extern "C" int fc3dgpu_ctx_zero_r(fc3dgpu_ctx* c) {
   if (!c || !c->have_W) {
     fc3dgpu_set_error("fc3dgpu_ctx_zero_r: no problem");
@@ -876,7 +894,41 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.counters = c->counters_on ? c->counters : nullptr;
   a.timeline = c->timeline_sweep > 0 ? c->timeline : nullptr;
   a.timeline_sweep = c->timeline_sweep;
+  a.stage_w_bytes = a.stage_c_bytes = a.stage_q_bytes = 0;
   a.out = c->out;
+}
+
+// Staging buffer sizes (bytes of W, col, q) for the largest slab range one
+// of `grid` blocks takes in any colour; 0 when staging cannot be used
+// (a range longer than one pass, or more shared memory than a block has).
+template <typename Real>
+static size_t staging_sizes(fc3dgpu_ctx* c, int grid, unsigned* wb, unsigned* cb, unsigned* qb) {
+  *wb = *cb = *qb = 0;
+  if (!c->staging || grid <= 0) return 0;
+  size_t mw = 0, mc = 0, mq = 0;
+  for (int col = 0; col < c->ncol; col++) {
+    const int s0 = c->sptr[col], n = c->sptr[col + 1] - s0;
+    for (int b = 0; b < grid; b++) {
+      const int lo = s0 + (int)((long long)n * b / grid), hi = s0 + (int)((long long)n * (b + 1) / grid);
+      if (hi <= lo) continue;
+      if (hi - lo > 16) return 0;
+      const long long o0 = c->slab_off_h[lo];
+      const long long o1 = hi < c->nslab ? c->slab_off_h[hi] : c->slab_off_h[hi - 1] + c->slab_nslot_h[hi - 1];
+      const size_t slots = (size_t)(o1 - o0);
+      mw = std::max(mw, slots * 9 * FC3D_SLAB * sizeof(Real));
+      mc = std::max(mc, slots * FC3D_SLAB * sizeof(int));
+      mq = std::max(mq, (size_t)(hi - lo) * 3 * FC3D_SLAB * sizeof(Real));
+    }
+  }
+  const size_t tot = mw + mc + mq;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (tot + 32 * 1024 > (size_t)optin) return 0;  // leave room for the static work list
+  *wb = (unsigned)mw;
+  *cb = (unsigned)mc;
+  *qb = (unsigned)mq;
+  return tot;
 }
 
 static int autotune_lanes(fc3dgpu_ctx* c) {
@@ -927,8 +979,13 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     a.newton_max = p->newton_max;
     a.pli_max = p->pli_max;
     a.ls_max = p->ls_max;
+    size_t smem = 0;
+    if (lanes == 1) {
+      const int g1 = sweep_grid_f32(1);
+      smem = staging_sizes<float>(c, g1, &a.stage_w_bytes, &a.stage_c_bytes, &a.stage_q_bytes);
+    }
     CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
-    CK(launch_sweep_f32(a, lanes, 0, s, &grid));
+    CK(launch_sweep_f32(a, lanes, 0, smem, s, &grid));
     c->launches++;
     CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(c->ev[1], s));
@@ -958,7 +1015,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     a.ls_max = p->ls_max;
     int g64 = 0;
     CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
-    CK(launch_sweep_f64(a, lanes, 0, s, &g64));
+    CK(launch_sweep_f64(a, lanes, 0, 0, s, &g64));
     c->launches++;
     if (!grid) grid = g64;
     CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
@@ -1016,7 +1073,7 @@ extern "C" int fc3dgpu_ctx_compute_error(fc3dgpu_ctx* c, double* error) {
   double out[8];
   CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
   CK(cudaMemsetAsync(c->status, 0, sizeof(int), s));
-  CK(launch_sweep_f64(a, 1, 0, s, &g));
+  CK(launch_sweep_f64(a, 1, 0, 0, s, &g));
   CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (error) *error = out[2];

@@ -66,6 +66,10 @@ struct SweepArgs {
   unsigned long long* counters;  // optional work counters: Newton its, PLI its, line-search evals, solves, max Newton
   unsigned long long* timeline;  // optional: globaltimer at each colour phase's start and work end, per block
   int timeline_sweep;            // the sweep (1-based) the timeline records
+  // bulk-copy staging of each block's slab range (one lane per contact only):
+  // W, col and q of the next colour stream into dynamic shared memory while
+  // the block solves the current colour; 0 bytes = off
+  unsigned stage_w_bytes, stage_c_bytes, stage_q_bytes;
   // outputs (written by block 0, thread 0)
   double* out;                  // [0] sweeps, [1] incr, [2] full error, [3] info, [4] working tol
 };

@@ -257,6 +257,49 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   }
 }
 
+// ---- bulk copies (TMA engine, non-tensor) into shared memory -------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// global -> shared bulk copy completing on an mbarrier; 16-byte aligned
+// addresses, size a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// Bounded wait for the staging barrier: on expiry records the timeout bit.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity, unsigned long long limit,
+                                                  int* status) {
+  unsigned long long n = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++n > limit) {
+      atomicOr(status, 1);
+      return false;
+    }
+  }
+  return true;
+}
+
 #define FC3D_PASS_SLABS 16
 
 // Work list of one block: the contacts of the current pass whose local
@@ -268,6 +311,48 @@ struct WorkList {
   Real ro[FC3D_PASS_SLABS * FC3D_SLAB][3];
   int count[FC3D_PASS_SLABS];
 };
+
+template <typename Real>
+__device__ __forceinline__ void solve_item(const SweepArgs<Real>& a, WorkList<Real>& wk, int t, Real ltol, double& dr2,
+                                           double& rr2) {
+  const int pp = wk.p[t];
+  const int sl = pp / FC3D_SLAB, k = pp % FC3D_SLAB;
+  LocalProblem<Real> L;
+#pragma unroll
+  for (int e = 0; e < 9; e++) L.M[e] = __ldg(&a.D[((size_t)sl * 9 + e) * FC3D_SLAB + k]);
+  L.q[0] = wk.q[t][0];
+  L.q[1] = wk.q[t][1];
+  L.q[2] = wk.q[t][2];
+  L.mu = __ldg(&a.mu[(size_t)sl * FC3D_SLAB + k]);
+  L.rhoN = __ldg(&a.rho[((size_t)sl * 2) * FC3D_SLAB + k]);
+  L.rhoT = __ldg(&a.rho[((size_t)sl * 2 + 1) * FC3D_SLAB + k]);
+  L.rho_pli = __ldcg(&a.rpli[pp]);
+  L.tol = ltol;
+  L.newton_max = a.newton_max;
+  L.pli_max = a.pli_max;
+  L.ls_max = a.ls_max;
+  L.n_newton = 0;
+  L.n_pli = 0;
+  L.n_ls = 0;
+  Real o[3] = {wk.ro[t][0], wk.ro[t][1], wk.ro[t][2]};
+  Real rn[3] = {o[0], o[1], o[2]};
+  local_solve(L, rn);
+  Real* rp = a.r + (size_t)pp * FC3D_RSTRIDE;
+  rp[0] = rn[0];
+  rp[1] = rn[1];
+  rp[2] = rn[2];
+  a.rpli[pp] = L.rho_pli;
+  const double d0 = (double)o[0] - (double)rn[0], d1 = (double)o[1] - (double)rn[1], d2 = (double)o[2] - (double)rn[2];
+  dr2 += d0 * d0 + d1 * d1 + d2 * d2;
+  rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+  if (a.counters) {
+    atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
+    atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);
+    atomicAdd(&a.counters[2], (unsigned long long)L.n_ls);
+    atomicAdd(&a.counters[3], 1ULL);
+    atomicMax(&a.counters[4], (unsigned long long)L.n_newton);
+  }
+}
 
 // One colour with one lane per contact.  The colour's slabs are split into
 // one contiguous range per block (so no block takes a second round while
@@ -369,48 +454,161 @@ __device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a,
       }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int pp = wk.p[t];
-      const int sl = pp / FC3D_SLAB, k = pp % FC3D_SLAB;
-      LocalProblem<Real> L;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) solve_item(a, wk, t, ltol, dr2, rr2);
+    __syncthreads();
+  }
+}
+
+// Slab range [lo, hi) of one colour handled by this block.
+__device__ __forceinline__ void block_range(int s0, int s1, int& lo, int& hi) {
+  const int n = s1 - s0;
+  lo = s0 + (int)((long long)n * blockIdx.x / gridDim.x);
+  hi = s0 + (int)((long long)n * (blockIdx.x + 1) / gridDim.x);
+}
+
+// Issue the bulk copies of W, col and q for slabs [lo, hi) into the
+// staging buffers (one thread).  The caller made sure the previous
+// contents were consumed (block barrier + proxy fence).
+template <typename Real>
+__device__ __forceinline__ void stage_issue(const SweepArgs<Real>& a, int lo, int hi, unsigned char* stage,
+                                            unsigned long long* bar) {
+  const long long o0 = a.slab_off[lo], o1 = hi < a.nslab ? a.slab_off[hi] : (long long)-1;
+  long long slots = 0;
+  if (o1 >= 0) {
+    slots = o1 - o0;
+  } else {
+    slots = a.slab_off[hi - 1] + a.slab_nslot[hi - 1] - o0;
+  }
+  const unsigned wb = (unsigned)(slots * 9 * FC3D_SLAB * sizeof(Real));
+  const unsigned cb = (unsigned)(slots * FC3D_SLAB * sizeof(int));
+  const unsigned qb = (unsigned)((hi - lo) * 3 * FC3D_SLAB * sizeof(Real));
+  mbar_arrive_expect_tx(bar, wb + cb + qb);
+  if (wb) bulk_g2s(stage, a.W + (size_t)o0 * 9 * FC3D_SLAB, wb, bar);
+  if (cb) bulk_g2s(stage + a.stage_w_bytes, a.col + (size_t)o0 * FC3D_SLAB, cb, bar);
+  bulk_g2s(stage + a.stage_w_bytes + a.stage_c_bytes, a.q + (size_t)lo * 3 * FC3D_SLAB, qb, bar);
+}
+
+// process_colour_compact with W, col and q read from the staged shared
+// memory copy of the block's range (which must fit one pass), and the next
+// colour's range staged as soon as this one's row products are done.
+template <typename Real>
+__device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, int c, Real ltol, double& dr2,
+                                                      double& rr2, WorkList<Real>& wk, unsigned char* stage,
+                                                      unsigned long long* bar, unsigned& parity, bool& pending,
+                                                      unsigned long long* tl) {
+  constexpr int NWB = FC3D_BLOCK / 32;
+  constexpr int MAXR = (FC3D_PASS_SLABS + NWB - 1) / NWB;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int lo, hi;
+  block_range(a.sptr[c], a.sptr[c + 1], lo, hi);
+  const int np = hi - lo;
+  const int cn = (c + 1 < a.ncol) ? c + 1 : 0;
+  int nlo, nhi;
+  block_range(a.sptr[cn], a.sptr[cn + 1], nlo, nhi);
+  if (np > 0) {
+    if (pending) {
+      if (!mbar_wait_bounded(bar, parity, a.spin_limit, a.status)) return false;
+      parity ^= 1u;
+      pending = false;
+    }
+    const Real* Ws = reinterpret_cast<const Real*>(stage);
+    const int* Cs = reinterpret_cast<const int*>(stage + a.stage_w_bytes);
+    const Real* Qs = reinterpret_cast<const Real*>(stage + a.stage_w_bytes + a.stage_c_bytes);
+    const long long o0 = a.slab_off[lo];
+    Real acc[MAXR][3], ro[MAXR][3];
+    unsigned msk[MAXR];
 #pragma unroll
-      for (int e = 0; e < 9; e++) L.M[e] = __ldg(&a.D[((size_t)sl * 9 + e) * FC3D_SLAB + k]);
-      L.q[0] = wk.q[t][0];
-      L.q[1] = wk.q[t][1];
-      L.q[2] = wk.q[t][2];
-      L.mu = __ldg(&a.mu[(size_t)sl * FC3D_SLAB + k]);
-      L.rhoN = __ldg(&a.rho[((size_t)sl * 2) * FC3D_SLAB + k]);
-      L.rhoT = __ldg(&a.rho[((size_t)sl * 2 + 1) * FC3D_SLAB + k]);
-      L.rho_pli = __ldcg(&a.rpli[pp]);
-      L.tol = ltol;
-      L.newton_max = a.newton_max;
-      L.pli_max = a.pli_max;
-      L.ls_max = a.ls_max;
-      L.n_newton = 0;
-      L.n_pli = 0;
-      L.n_ls = 0;
-      Real o[3] = {wk.ro[t][0], wk.ro[t][1], wk.ro[t][2]};
-      Real rn[3] = {o[0], o[1], o[2]};
-      local_solve(L, rn);
-      Real* rp = a.r + (size_t)pp * FC3D_RSTRIDE;
-      rp[0] = rn[0];
-      rp[1] = rn[1];
-      rp[2] = rn[2];
-      a.rpli[pp] = L.rho_pli;
-      const double d0 = (double)o[0] - (double)rn[0], d1 = (double)o[1] - (double)rn[1],
-                   d2 = (double)o[2] - (double)rn[2];
-      dr2 += d0 * d0 + d1 * d1 + d2 * d2;
-      rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
-      if (a.counters) {
-        atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
-        atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);
-        atomicAdd(&a.counters[2], (unsigned long long)L.n_ls);
-        atomicAdd(&a.counters[3], 1ULL);
-        atomicMax(&a.counters[4], (unsigned long long)L.n_newton);
+    for (int j = 0; j < MAXR; j++) {
+      const int i = w + j * NWB;
+      msk[j] = 0;
+      if (i < np) {
+        const int slab = lo + i;
+        const int p = slab * FC3D_SLAB + lane;
+        bool work = false;
+        acc[j][0] = acc[j][1] = acc[j][2] = 0;
+        ro[j][0] = ro[j][1] = ro[j][2] = 0;
+        if (__ldg(&a.perm[p]) >= 0) {
+          const int rel = (int)(a.slab_off[slab] - o0);
+          const int ns = a.slab_nslot[slab];
+          acc[j][0] = Qs[(i * 3 + 0) * FC3D_SLAB + lane];
+          acc[j][1] = Qs[(i * 3 + 1) * FC3D_SLAB + lane];
+          acc[j][2] = Qs[(i * 3 + 2) * FC3D_SLAB + lane];
+          constexpr int CH = 16;
+          for (int t0 = 0; t0 < ns; t0 += CH) {
+            Real rv[CH][3];
+#pragma unroll
+            for (int k = 0; k < CH; k++) {
+              const int pj = t0 + k < ns ? Cs[(rel + t0 + k) * FC3D_SLAB + lane] : a.npad;
+              load_r3<Real>(a.r, pj, rv[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < CH; k++) {
+              if (t0 + k < ns) {
+                const Real* wp = Ws + (size_t)(rel + t0 + k) * 9 * FC3D_SLAB + lane;
+                Real wv[9];
+#pragma unroll
+                for (int e = 0; e < 9; e++) wv[e] = wp[e * FC3D_SLAB];
+                mvp3x3(wv, rv[k], acc[j]);
+              }
+            }
+          }
+          load_r3<Real>(a.r, p, ro[j]);
+          if (acc[j][0] > -Eps<Real>::v()) {
+            Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
+            rp[0] = 0;
+            rp[1] = 0;
+            rp[2] = 0;
+            dr2 += (double)ro[j][0] * ro[j][0] + (double)ro[j][1] * ro[j][1] + (double)ro[j][2] * ro[j][2];
+          } else {
+            work = true;
+          }
+        }
+        msk[j] = __ballot_sync(0xffffffffu, work);
+        if (lane == 0) wk.count[i] = __popc(msk[j]);
       }
     }
     __syncthreads();
+    // staged data consumed by every warp: stage the next colour's range now,
+    // so it streams in while this colour is solved and the grid waits
+    if (threadIdx.x == 0 && nhi > nlo) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      stage_issue(a, nlo, nhi, stage, bar);
+    }
+    if (nhi > nlo) pending = true;
+    int total = 0;
+    for (int k = 0; k < np; k++) total += wk.count[k];
+    if (tl && threadIdx.x == 0) {
+      tl[0] = globaltimer_ns();
+      tl[1] = (unsigned long long)total;
+    }
+#pragma unroll
+    for (int j = 0; j < MAXR; j++) {
+      const int i = w + j * NWB;
+      if (i < np && (msk[j] >> lane) & 1u) {
+        int off = 0;
+        for (int k = 0; k < i; k++) off += wk.count[k];
+        const int idx = off + __popc(msk[j] & ((1u << lane) - 1));
+        wk.p[idx] = (lo + i) * FC3D_SLAB + lane;
+        wk.q[idx][0] = acc[j][0];
+        wk.q[idx][1] = acc[j][1];
+        wk.q[idx][2] = acc[j][2];
+        wk.ro[idx][0] = ro[j][0];
+        wk.ro[idx][1] = ro[j][1];
+        wk.ro[idx][2] = ro[j][2];
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < total; t += blockDim.x) solve_item(a, wk, t, ltol, dr2, rr2);
+    __syncthreads();
+  } else if (nhi > nlo && !pending) {
+    // nothing to do in this colour; stage the next one (buffer is free)
+    if (threadIdx.x == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      stage_issue(a, nlo, nhi, stage, bar);
+    }
+    pending = true;
   }
+  return true;
 }
 
 // u = q + W r for every row in CSR block order (diagonal at its own slot
@@ -475,6 +673,25 @@ __device__ __forceinline__ bool full_error_phase(const SweepArgs<Real>& a, int s
 template <typename Real, int T>
 __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Real> a) {
   __shared__ WorkList<Real> wk;
+  __shared__ __align__(8) unsigned long long stage_bar;
+  extern __shared__ __align__(128) unsigned char stage[];
+  constexpr bool can_stage = (sizeof(Real) == 4) && T == 1;
+  const bool staged = can_stage && a.stage_w_bytes > 0;
+  unsigned parity = 0;
+  bool pending = false;
+  if (staged) {
+    if (threadIdx.x == 0) {
+      mbar_init(&stage_bar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int lo, hi;
+    block_range(a.sptr[0], a.sptr[1], lo, hi);
+    if (hi > lo) {
+      if (threadIdx.x == 0) stage_issue(a, lo, hi, stage, &stage_bar);
+      pending = true;
+    }
+  }
   const int lane = threadIdx.x & 31;
   const int nwb = blockDim.x >> 5;
   const int gw = blockIdx.x * nwb + (threadIdx.x >> 5), tw = gridDim.x * nwb;
@@ -494,7 +711,12 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
         a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 2] = 0;
         a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 3] = 0;
       }
-      if (T == 1) {
+      if (can_stage && staged) {
+        if (!process_colour_staged<Real>(a, c, (Real)local_tol, acc[0], acc[1], wk, stage, &stage_bar, parity,
+                                         pending,
+                                         tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 4 + 2 : nullptr))
+          return;
+      } else if (T == 1) {
         process_colour_compact<Real>(a, s0, a.sptr[c + 1], (Real)local_tol, acc[0], acc[1], wk,
                                      tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 4 + 2 : nullptr);
       } else {
@@ -514,7 +736,10 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
       }
       if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
       if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 1] = globaltimer_ns();
-      if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) return;
+      if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) {
+        if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+        return;
+      }
     }
     double s[2];
     grid_sum<2>(a.partials, 0, s);
@@ -527,7 +752,10 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
     if (a.mode == 1) {
       // check_convergence_with_adaptation (fc3d_nsgs.c:496-534)
       if (incr < working) {
-        if (!full_error_phase(a, 2, epoch, full)) return;
+        if (!full_error_phase(a, 2, epoch, full)) {
+          if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+          return;
+        }
         if (full <= a.user_tol) {
           converged = true;
           stop = true;
@@ -556,6 +784,11 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
       }
     }
     if (stop) break;
+  }
+  if (pending) {
+    // a staged copy of the colour after the last one is still in flight
+    mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+    pending = false;
   }
   int info = 1;
   if (a.mode == 1) {

@@ -5,28 +5,32 @@
 namespace fc3dgpu {
 
 template <int T>
-static cudaError_t launch_t(const SweepArgs<double>& a, int max_grid, cudaStream_t s, int* grid) {
+static cudaError_t launch_t(const SweepArgs<double>& a, int max_grid, size_t smem, cudaStream_t s, int* grid) {
   auto kern = nsgs_kernel<double, T>;
   static int cached_dev = -1, cached_g = 0;
+  static size_t cached_smem = 0;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (cached_dev != dev) {
+  if (cached_dev != dev || cached_smem != smem) {
     int nsm = 0, per_sm = 0;
+    e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FC3D_BLOCK, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FC3D_BLOCK, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     cached_g = nsm * per_sm;
     cached_dev = dev;
+    cached_smem = smem;
   }
   int g = cached_g;
   if (max_grid > 0 && g > max_grid) g = max_grid;
   if (g > 1024) g = 1024;
   *grid = g;
   void* args[] = {(void*)&a};
-  return cudaLaunchCooperativeKernel((const void*)kern, dim3(g), dim3(FC3D_BLOCK), args, 0, s);
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(g), dim3(FC3D_BLOCK), args, smem, s);
 }
 
 template <int T>
@@ -38,12 +42,13 @@ static int grid_t() {
   return nsm * per_sm;
 }
 
-cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid, cudaStream_t s, int* grid) {
+cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid, size_t smem, cudaStream_t s,
+                             int* grid) {
   switch (lanes) {
-    case 1: return launch_t<1>(a, max_grid, s, grid);
-    case 2: return launch_t<2>(a, max_grid, s, grid);
-    case 4: return launch_t<4>(a, max_grid, s, grid);
-    case 8: return launch_t<8>(a, max_grid, s, grid);
+    case 1: return launch_t<1>(a, max_grid, smem, s, grid);
+    case 2: return launch_t<2>(a, max_grid, 0, s, grid);
+    case 4: return launch_t<4>(a, max_grid, 0, s, grid);
+    case 8: return launch_t<8>(a, max_grid, 0, s, grid);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -10,8 +10,11 @@ namespace fc3dgpu {
 // Cooperative launch with as many resident blocks as fit (capped by
 // max_grid when > 0).  Returns the cudaError_t of the launch; *grid gets the
 // number of blocks.
-cudaError_t launch_sweep_f32(const SweepArgs<float>& a, int lanes, int max_grid, cudaStream_t s, int* grid);
-cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid, cudaStream_t s, int* grid);
+// smem: dynamic shared memory of the launch (staging buffers), 0 when off
+cudaError_t launch_sweep_f32(const SweepArgs<float>& a, int lanes, int max_grid, size_t smem, cudaStream_t s,
+                             int* grid);
+cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid, size_t smem, cudaStream_t s,
+                             int* grid);
 int sweep_grid_f32(int lanes);
 void warm_sweep_kernels();
 int sweep_grid_f64(int lanes);

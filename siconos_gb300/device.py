@@ -62,6 +62,9 @@ class DeviceSolver:
         n = self.L.fc3dgpu_ctx_timeline(self.ctx, sweep, out.ctypes.data, cap)
         return out[:max(n, 0)]
 
+    def staging(self, on: bool) -> bool:
+        return bool(self.L.fc3dgpu_ctx_staging(self.ctx, int(on)))
+
     def zero_r(self):
         self._check(self.L.fc3dgpu_ctx_zero_r(self.ctx), "zero_r")
 

@@ -161,3 +161,22 @@ def test_c2_scale_properties(gpu):
     col = gpu.colours()
     assert O.port().oracle_colour_check(s.nc, s.rowptr, s.colidx, col) == 0
     assert st["sweeps32"] + st["sweeps64"] == 60 and st["status"] == 0
+
+
+def test_fp32_staged_equals_unstaged(gpu):
+    """The bulk-copy staged FP32 sweep computes what the direct-load sweep
+    computes (same slot order; only the data path differs)."""
+    from siconos_gb300 import scene
+    s = scene.lattice(20, 20, 10, seed=4)
+    gpu.load(s)
+    out = []
+    for on in (True, False):
+        gpu.staging(on)
+        gpu.zero_r()
+        st = gpu.solve(tol=1e-8, max_iter=30, lanes=1, fp32_only=1, switch_tol=0.0, stall_window=0)
+        out.append((gpu.get()[0], st))
+    gpu.staging(True)
+    (r1, s1), (r2, s2) = out
+    assert s1["status"] == 0 and s2["status"] == 0
+    assert np.linalg.norm(r1 - r2) <= 1e-5 * np.linalg.norm(r2)
+    assert abs(s1["error"] - s2["error"]) <= 1e-4 * s2["error"]
