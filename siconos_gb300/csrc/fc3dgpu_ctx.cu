@@ -471,6 +471,7 @@ struct fc3dgpu_ctx {
   BUF(unsigned long long, timeline);
   int timeline_sweep = 0;
   std::vector<long long> slab_off_h;
+  int ccount[FC3D_MAX_COLOURS];
   std::vector<int> slab_nslot_h;
   int staging = 1;  // bulk-copy staging of slab ranges for the FP32 sweeps
 };
@@ -667,6 +668,7 @@ extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, 
   k_colour_hist<<<nblk, 1024, 0, s>>>(nc, c->colour, c->blockhist);
   k_colour_offsets<<<1, FC3D_MAX_COLOURS, 0, s>>>(nblk, c->blockhist, c->counts, c->sptr_d);
   CK(cudaMemcpyAsync(c->sptr, c->sptr_d, sizeof(int) * (FC3D_MAX_COLOURS + 1), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(c->ccount, c->counts, sizeof(int) * FC3D_MAX_COLOURS, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   c->ncol = ncol;
   c->nslab = c->sptr[ncol];
@@ -894,7 +896,8 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.counters = c->counters_on ? c->counters : nullptr;
   a.timeline = c->timeline_sweep > 0 ? c->timeline : nullptr;
   a.timeline_sweep = c->timeline_sweep;
-  a.stage_w_bytes = a.stage_c_bytes = a.stage_q_bytes = 0;
+  a.stage_w_bytes = a.stage_c_bytes = a.stage_q_bytes = a.stage_d_bytes = 0;
+  for (int k = 0; k < FC3D_MAX_COLOURS; k++) a.ccount[k] = c->ccount[k];
   a.out = c->out;
 }
 
@@ -902,10 +905,10 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
 // of `grid` blocks takes in any colour; 0 when staging cannot be used
 // (a range longer than one pass, or more shared memory than a block has).
 template <typename Real>
-static size_t staging_sizes(fc3dgpu_ctx* c, int grid, unsigned* wb, unsigned* cb, unsigned* qb) {
-  *wb = *cb = *qb = 0;
+static size_t staging_sizes(fc3dgpu_ctx* c, int grid, unsigned* wb, unsigned* cb, unsigned* qb, unsigned* db) {
+  *wb = *cb = *qb = *db = 0;
   if (!c->staging || grid <= 0) return 0;
-  size_t mw = 0, mc = 0, mq = 0;
+  size_t mw = 0, mc = 0, mq = 0, md = 0;
   for (int col = 0; col < c->ncol; col++) {
     const int s0 = c->sptr[col], n = c->sptr[col + 1] - s0;
     for (int b = 0; b < grid; b++) {
@@ -918,16 +921,22 @@ static size_t staging_sizes(fc3dgpu_ctx* c, int grid, unsigned* wb, unsigned* cb
       mw = std::max(mw, slots * 9 * FC3D_SLAB * sizeof(Real));
       mc = std::max(mc, slots * FC3D_SLAB * sizeof(int));
       mq = std::max(mq, (size_t)(hi - lo) * 3 * FC3D_SLAB * sizeof(Real));
+      md = std::max(md, (size_t)(hi - lo) * 9 * FC3D_SLAB * sizeof(Real));
     }
   }
-  const size_t tot = mw + mc + mq;
+  const size_t buffers = (mw + mc + mq + md / 9 * 12 + 15) & ~(size_t)15;
+  const size_t tot = buffers + sizeof(fc3dgpu::WorkListS<Real>);
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (tot + 32 * 1024 > (size_t)optin) return 0;  // leave room for the static work list
+  // static shared memory of the kernel: the direct-load work list and a few
+  // reduction arrays
+  const size_t static_smem = sizeof(fc3dgpu::WorkList<Real>) + 2048;
+  if (tot + static_smem > (size_t)optin) return 0;
   *wb = (unsigned)mw;
   *cb = (unsigned)mc;
   *qb = (unsigned)mq;
+  *db = (unsigned)md;
   return tot;
 }
 
@@ -982,7 +991,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     size_t smem = 0;
     if (lanes == 1) {
       const int g1 = sweep_grid_f32(1);
-      smem = staging_sizes<float>(c, g1, &a.stage_w_bytes, &a.stage_c_bytes, &a.stage_q_bytes);
+      smem = staging_sizes<float>(c, g1, &a.stage_w_bytes, &a.stage_c_bytes, &a.stage_q_bytes, &a.stage_d_bytes);
     }
     CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
     CK(launch_sweep_f32(a, lanes, 0, smem, s, &grid));

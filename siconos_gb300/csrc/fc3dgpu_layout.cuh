@@ -32,6 +32,7 @@ struct SweepArgs {
   int nslab;
   int npad;                     // 32 * nslab
   int sptr[FC3D_MAX_COLOURS + 1];  // slab range of each colour
+  int ccount[FC3D_MAX_COLOURS];    // contacts of each colour (rows past it in the range are padding)
   const int* slab_nslot;
   const long long* slab_off;
   const int* perm;              // padded permuted row -> original contact, -1 pad
@@ -69,9 +70,32 @@ struct SweepArgs {
   // bulk-copy staging of each block's slab range (one lane per contact only):
   // W, col and q of the next colour stream into dynamic shared memory while
   // the block solves the current colour; 0 bytes = off
-  unsigned stage_w_bytes, stage_c_bytes, stage_q_bytes;
+  unsigned stage_w_bytes, stage_c_bytes, stage_q_bytes, stage_d_bytes;
   // outputs (written by block 0, thread 0)
   double* out;                  // [0] sweeps, [1] incr, [2] full error, [3] info, [4] working tol
+};
+
+#define FC3D_PASS_SLABS 16
+
+// Work list of one block: the contacts of the current pass whose local
+// problem is not the trivial take-off, packed densely.
+template <typename Real>
+struct WorkList {
+  int p[FC3D_PASS_SLABS * FC3D_SLAB];
+  Real q[FC3D_PASS_SLABS * FC3D_SLAB][3];
+  Real ro[FC3D_PASS_SLABS * FC3D_SLAB][3];
+  int count[FC3D_PASS_SLABS];
+};
+
+// Work list of the staged path: also carries each contact's diagonal block,
+// mu and rho, copied from the staging buffer before it is refilled.
+template <typename Real>
+struct WorkListS {
+  int p[FC3D_PASS_SLABS * FC3D_SLAB];
+  Real q[FC3D_PASS_SLABS * FC3D_SLAB][3];
+  Real ro[FC3D_PASS_SLABS * FC3D_SLAB][3];
+  Real m[FC3D_PASS_SLABS * FC3D_SLAB][12];  // 9 of D, mu, rhoN, rhoT
+  int count[FC3D_PASS_SLABS];
 };
 
 }  // namespace fc3dgpu

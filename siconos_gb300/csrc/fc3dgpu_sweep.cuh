@@ -300,18 +300,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
   return true;
 }
 
-#define FC3D_PASS_SLABS 16
-
-// Work list of one block: the contacts of the current pass whose local
-// problem is not the trivial take-off, packed densely.
-template <typename Real>
-struct WorkList {
-  int p[FC3D_PASS_SLABS * FC3D_SLAB];
-  Real q[FC3D_PASS_SLABS * FC3D_SLAB][3];
-  Real ro[FC3D_PASS_SLABS * FC3D_SLAB][3];
-  int count[FC3D_PASS_SLABS];
-};
-
 template <typename Real>
 __device__ __forceinline__ void solve_item(const SweepArgs<Real>& a, WorkList<Real>& wk, int t, Real ltol, double& dr2,
                                            double& rr2) {
@@ -482,18 +470,75 @@ __device__ __forceinline__ void stage_issue(const SweepArgs<Real>& a, int lo, in
   const unsigned wb = (unsigned)(slots * 9 * FC3D_SLAB * sizeof(Real));
   const unsigned cb = (unsigned)(slots * FC3D_SLAB * sizeof(int));
   const unsigned qb = (unsigned)((hi - lo) * 3 * FC3D_SLAB * sizeof(Real));
-  mbar_arrive_expect_tx(bar, wb + cb + qb);
+  const unsigned db = (unsigned)((hi - lo) * 9 * FC3D_SLAB * sizeof(Real));
+  const unsigned mb = (unsigned)((hi - lo) * FC3D_SLAB * sizeof(Real));
+  const unsigned rb = 2 * mb;
+  unsigned char* sq = stage + a.stage_w_bytes + a.stage_c_bytes;
+  unsigned char* sd = sq + a.stage_q_bytes;
+  unsigned char* sm = sd + a.stage_d_bytes;
+  unsigned char* sr = sm + a.stage_d_bytes / 9;
+  mbar_arrive_expect_tx(bar, wb + cb + qb + db + mb + rb);
   if (wb) bulk_g2s(stage, a.W + (size_t)o0 * 9 * FC3D_SLAB, wb, bar);
   if (cb) bulk_g2s(stage + a.stage_w_bytes, a.col + (size_t)o0 * FC3D_SLAB, cb, bar);
-  bulk_g2s(stage + a.stage_w_bytes + a.stage_c_bytes, a.q + (size_t)lo * 3 * FC3D_SLAB, qb, bar);
+  bulk_g2s(sq, a.q + (size_t)lo * 3 * FC3D_SLAB, qb, bar);
+  bulk_g2s(sd, a.D + (size_t)lo * 9 * FC3D_SLAB, db, bar);
+  bulk_g2s(sm, a.mu + (size_t)lo * FC3D_SLAB, mb, bar);
+  bulk_g2s(sr, a.rho + (size_t)lo * 2 * FC3D_SLAB, rb, bar);
 }
 
 // process_colour_compact with W, col and q read from the staged shared
 // memory copy of the block's range (which must fit one pass), and the next
 // colour's range staged as soon as this one's row products are done.
 template <typename Real>
+__device__ __forceinline__ void solve_item_s(const SweepArgs<Real>& a, WorkListS<Real>& wk, int t, Real ltol,
+                                             double& dr2, double& rr2) {
+  const int pp = wk.p[t];
+  LocalProblem<Real> L;
+#pragma unroll
+  for (int e = 0; e < 9; e++) L.M[e] = wk.m[t][e];
+  L.q[0] = wk.q[t][0];
+  L.q[1] = wk.q[t][1];
+  L.q[2] = wk.q[t][2];
+  L.mu = wk.m[t][9];
+  L.rhoN = wk.m[t][10];
+  L.rhoT = wk.m[t][11];
+  L.rho_pli = __ldcg(&a.rpli[pp]);
+  L.tol = ltol;
+  L.newton_max = a.newton_max;
+  L.pli_max = a.pli_max;
+  L.ls_max = a.ls_max;
+  L.n_newton = 0;
+  L.n_pli = 0;
+  L.n_ls = 0;
+  Real o[3] = {wk.ro[t][0], wk.ro[t][1], wk.ro[t][2]};
+  Real rn[3] = {o[0], o[1], o[2]};
+  local_solve(L, rn);
+  Real* rp = a.r + (size_t)pp * FC3D_RSTRIDE;
+  rp[0] = rn[0];
+  rp[1] = rn[1];
+  rp[2] = rn[2];
+  a.rpli[pp] = L.rho_pli;
+  const double d0 = (double)o[0] - (double)rn[0], d1 = (double)o[1] - (double)rn[1], d2 = (double)o[2] - (double)rn[2];
+  dr2 += d0 * d0 + d1 * d1 + d2 * d2;
+  rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+  if (a.counters) {
+    atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
+    atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);
+    atomicAdd(&a.counters[2], (unsigned long long)L.n_ls);
+    atomicAdd(&a.counters[3], 1ULL);
+    atomicMax(&a.counters[4], (unsigned long long)L.n_newton);
+  }
+}
+
+// process_colour_compact with every per-slab input (W, col, q, D, mu, rho)
+// read from the staged shared-memory copy of the block's range (which must
+// fit one pass).  The only global reads left in the row product are the
+// neighbour and own reactions, all issued together.  The next colour's
+// range is staged as soon as this one's inputs have been copied out, so it
+// streams in while this colour is solved and the grid waits.
+template <typename Real>
 __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, int c, Real ltol, double& dr2,
-                                                      double& rr2, WorkList<Real>& wk, unsigned char* stage,
+                                                      double& rr2, WorkListS<Real>& wk, unsigned char* stage,
                                                       unsigned long long* bar, unsigned& parity, bool& pending,
                                                       unsigned long long* tl) {
   constexpr int NWB = FC3D_BLOCK / 32;
@@ -506,6 +551,25 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
   int nlo, nhi;
   block_range(a.sptr[cn], a.sptr[cn + 1], nlo, nhi);
   if (np > 0) {
+    const int first_row = a.sptr[c] * FC3D_SLAB, end_row = first_row + a.ccount[c];
+    // independent global loads first: slab metadata and own reactions
+    long long off[MAXR];
+    int nsl[MAXR];
+    Real ro[MAXR][3];
+#pragma unroll
+    for (int j = 0; j < MAXR; j++) {
+      const int i = w + j * NWB;
+      off[j] = 0;
+      nsl[j] = 0;
+      ro[j][0] = ro[j][1] = ro[j][2] = 0;
+      if (i < np) {
+        const int slab = lo + i;
+        off[j] = a.slab_off[slab];
+        nsl[j] = a.slab_nslot[slab];
+        const int p = slab * FC3D_SLAB + lane;
+        if (p < end_row) load_r3<Real>(a.r, p, ro[j]);
+      }
+    }
     if (pending) {
       if (!mbar_wait_bounded(bar, parity, a.spin_limit, a.status)) return false;
       parity ^= 1u;
@@ -514,8 +578,11 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
     const Real* Ws = reinterpret_cast<const Real*>(stage);
     const int* Cs = reinterpret_cast<const int*>(stage + a.stage_w_bytes);
     const Real* Qs = reinterpret_cast<const Real*>(stage + a.stage_w_bytes + a.stage_c_bytes);
+    const Real* Ds = reinterpret_cast<const Real*>(stage + a.stage_w_bytes + a.stage_c_bytes + a.stage_q_bytes);
+    const Real* Ms = Ds + a.stage_d_bytes / sizeof(Real) / 9 * 9;
+    const Real* Rs = Ms + a.stage_d_bytes / sizeof(Real) / 9;
     const long long o0 = a.slab_off[lo];
-    Real acc[MAXR][3], ro[MAXR][3];
+    Real acc[MAXR][3];
     unsigned msk[MAXR];
 #pragma unroll
     for (int j = 0; j < MAXR; j++) {
@@ -526,10 +593,9 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
         const int p = slab * FC3D_SLAB + lane;
         bool work = false;
         acc[j][0] = acc[j][1] = acc[j][2] = 0;
-        ro[j][0] = ro[j][1] = ro[j][2] = 0;
-        if (__ldg(&a.perm[p]) >= 0) {
-          const int rel = (int)(a.slab_off[slab] - o0);
-          const int ns = a.slab_nslot[slab];
+        if (p < end_row) {
+          const int rel = (int)(off[j] - o0);
+          const int ns = nsl[j];
           acc[j][0] = Qs[(i * 3 + 0) * FC3D_SLAB + lane];
           acc[j][1] = Qs[(i * 3 + 1) * FC3D_SLAB + lane];
           acc[j][2] = Qs[(i * 3 + 2) * FC3D_SLAB + lane];
@@ -552,7 +618,6 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
               }
             }
           }
-          load_r3<Real>(a.r, p, ro[j]);
           if (acc[j][0] > -Eps<Real>::v()) {
             Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
             rp[0] = 0;
@@ -568,26 +633,15 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
       }
     }
     __syncthreads();
-    // staged data consumed by every warp: stage the next colour's range now,
-    // so it streams in while this colour is solved and the grid waits
-    if (threadIdx.x == 0 && nhi > nlo) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      stage_issue(a, nlo, nhi, stage, bar);
-    }
-    if (nhi > nlo) pending = true;
     int total = 0;
     for (int k = 0; k < np; k++) total += wk.count[k];
-    if (tl && threadIdx.x == 0) {
-      tl[0] = globaltimer_ns();
-      tl[1] = (unsigned long long)total;
-    }
 #pragma unroll
     for (int j = 0; j < MAXR; j++) {
       const int i = w + j * NWB;
       if (i < np && (msk[j] >> lane) & 1u) {
-        int off = 0;
-        for (int k = 0; k < i; k++) off += wk.count[k];
-        const int idx = off + __popc(msk[j] & ((1u << lane) - 1));
+        int o = 0;
+        for (int k = 0; k < i; k++) o += wk.count[k];
+        const int idx = o + __popc(msk[j] & ((1u << lane) - 1));
         wk.p[idx] = (lo + i) * FC3D_SLAB + lane;
         wk.q[idx][0] = acc[j][0];
         wk.q[idx][1] = acc[j][1];
@@ -595,10 +649,25 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
         wk.ro[idx][0] = ro[j][0];
         wk.ro[idx][1] = ro[j][1];
         wk.ro[idx][2] = ro[j][2];
+#pragma unroll
+        for (int e = 0; e < 9; e++) wk.m[idx][e] = Ds[(i * 9 + e) * FC3D_SLAB + lane];
+        wk.m[idx][9] = Ms[i * FC3D_SLAB + lane];
+        wk.m[idx][10] = Rs[(i * 2) * FC3D_SLAB + lane];
+        wk.m[idx][11] = Rs[(i * 2 + 1) * FC3D_SLAB + lane];
       }
     }
     __syncthreads();
-    for (int t = threadIdx.x; t < total; t += blockDim.x) solve_item(a, wk, t, ltol, dr2, rr2);
+    // every input of this range copied out: stage the next colour's range
+    if (threadIdx.x == 0 && nhi > nlo) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      stage_issue(a, nlo, nhi, stage, bar);
+    }
+    if (nhi > nlo) pending = true;
+    if (tl && threadIdx.x == 0) {
+      tl[0] = globaltimer_ns();
+      tl[1] = (unsigned long long)total;
+    }
+    for (int t = threadIdx.x; t < total; t += blockDim.x) solve_item_s(a, wk, t, ltol, dr2, rr2);
     __syncthreads();
   } else if (nhi > nlo && !pending) {
     // nothing to do in this colour; stage the next one (buffer is free)
@@ -674,6 +743,7 @@ template <typename Real, int T>
 __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Real> a) {
   __shared__ WorkList<Real> wk;
   __shared__ __align__(8) unsigned long long stage_bar;
+
   extern __shared__ __align__(128) unsigned char stage[];
   constexpr bool can_stage = (sizeof(Real) == 4) && T == 1;
   const bool staged = can_stage && a.stage_w_bytes > 0;
@@ -712,7 +782,11 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
         a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 3] = 0;
       }
       if (can_stage && staged) {
-        if (!process_colour_staged<Real>(a, c, (Real)local_tol, acc[0], acc[1], wk, stage, &stage_bar, parity,
+        // the staged work list lives in dynamic shared memory after the
+        // staging buffers (W, col, q, D, mu, rho)
+        WorkListS<Real>& wks = *reinterpret_cast<WorkListS<Real>*>(
+            stage + ((a.stage_w_bytes + a.stage_c_bytes + a.stage_q_bytes + a.stage_d_bytes / 9 * 12 + 15) & ~15u));
+        if (!process_colour_staged<Real>(a, c, (Real)local_tol, acc[0], acc[1], wks, stage, &stage_bar, parity,
                                          pending,
                                          tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 4 + 2 : nullptr))
           return;
