@@ -575,6 +575,7 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
       parity ^= 1u;
       pending = false;
     }
+    if (tl && threadIdx.x == 0) tl[2] = globaltimer_ns();
     const Real* Ws = reinterpret_cast<const Real*>(stage);
     const int* Cs = reinterpret_cast<const int*>(stage + a.stage_w_bytes);
     const Real* Qs = reinterpret_cast<const Real*>(stage + a.stage_w_bytes + a.stage_c_bytes);
@@ -631,6 +632,7 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
         msk[j] = __ballot_sync(0xffffffffu, work);
         if (lane == 0) wk.count[i] = __popc(msk[j]);
       }
+      if (j == 0 && tl && threadIdx.x == 0) tl[3] = globaltimer_ns();
     }
     __syncthreads();
     int total = 0;
@@ -777,9 +779,9 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
       const int s0 = a.sptr[c], nunits = (a.sptr[c + 1] - s0) * T;
       const bool tl = a.timeline && sweep == a.timeline_sweep && threadIdx.x == 0;
       if (tl) {
-        a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4] = globaltimer_ns();
-        a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 2] = 0;
-        a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 3] = 0;
+        unsigned long long* e = a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6;
+        e[0] = globaltimer_ns();
+        e[2] = e[3] = e[4] = e[5] = 0;
       }
       if (can_stage && staged) {
         // the staged work list lives in dynamic shared memory after the
@@ -788,11 +790,11 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
             stage + ((a.stage_w_bytes + a.stage_c_bytes + a.stage_q_bytes + a.stage_d_bytes / 9 * 12 + 15) & ~15u));
         if (!process_colour_staged<Real>(a, c, (Real)local_tol, acc[0], acc[1], wks, stage, &stage_bar, parity,
                                          pending,
-                                         tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 4 + 2 : nullptr))
+                                         tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6 + 2 : nullptr))
           return;
       } else if (T == 1) {
         process_colour_compact<Real>(a, s0, a.sptr[c + 1], (Real)local_tol, acc[0], acc[1], wk,
-                                     tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 4 + 2 : nullptr);
+                                     tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6 + 2 : nullptr);
       } else {
         for (int u = gw; u < nunits; u += tw) {
           const long long t0 = a.counters ? clock64() : 0;
@@ -809,7 +811,7 @@ __global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Rea
         }
       }
       if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
-      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 4 + 1] = globaltimer_ns();
+      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 6 + 1] = globaltimer_ns();
       if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) {
         if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
         return;
