@@ -22,7 +22,14 @@
 
 namespace fc3dgpu {
 
-#define FC3D_BLOCK 256
+// Threads per block: 10 warps for the FP32 kernel (a block's slab range of
+// up to 10 slabs is covered in one round), 8 for FP64 (its register use
+// leaves room for 256 threads only).  Both give one block per SM.
+template <typename Real>
+struct BlockDim {
+  static constexpr int value = sizeof(Real) == 4 ? 320 : 256;
+};
+#define FC3D_BLOCK_MAX 320
 #define FC3D_RSTRIDE 4
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -87,7 +94,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* flags, unsigned& epoch, u
 
 template <int N>
 __device__ __forceinline__ void block_sum(double v[N], double* out_partials) {
-  __shared__ double sh[FC3D_BLOCK / 32][8];
+  __shared__ double sh[FC3D_BLOCK_MAX / 32][8];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < N; i++) {
@@ -356,7 +363,7 @@ template <typename Real>
 __device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a, int s0, int s1, Real ltol,
                                                        double& dr2, double& rr2, WorkList<Real>& wk,
                                                        unsigned long long* tl) {
-  constexpr int NWB = FC3D_BLOCK / 32;
+  constexpr int NWB = BlockDim<Real>::value / 32;
   constexpr int MAXR = (FC3D_PASS_SLABS + NWB - 1) / NWB;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = s1 - s0;
@@ -541,7 +548,7 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
                                                       double& rr2, WorkListS<Real>& wk, unsigned char* stage,
                                                       unsigned long long* bar, unsigned& parity, bool& pending,
                                                       unsigned long long* tl) {
-  constexpr int NWB = FC3D_BLOCK / 32;
+  constexpr int NWB = BlockDim<Real>::value / 32;
   constexpr int MAXR = (FC3D_PASS_SLABS + NWB - 1) / NWB;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int lo, hi;
@@ -570,6 +577,7 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
         if (p < end_row) load_r3<Real>(a.r, p, ro[j]);
       }
     }
+    const long long o0 = a.slab_off[lo];
     if (pending) {
       if (!mbar_wait_bounded(bar, parity, a.spin_limit, a.status)) return false;
       parity ^= 1u;
@@ -582,7 +590,6 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
     const Real* Ds = reinterpret_cast<const Real*>(stage + a.stage_w_bytes + a.stage_c_bytes + a.stage_q_bytes);
     const Real* Ms = Ds + a.stage_d_bytes / sizeof(Real) / 9 * 9;
     const Real* Rs = Ms + a.stage_d_bytes / sizeof(Real) / 9;
-    const long long o0 = a.slab_off[lo];
     Real acc[MAXR][3];
     unsigned msk[MAXR];
 #pragma unroll
@@ -742,7 +749,7 @@ __device__ __forceinline__ bool full_error_phase(const SweepArgs<Real>& a, int s
 }
 
 template <typename Real, int T>
-__global__ void __launch_bounds__(FC3D_BLOCK, 1) nsgs_kernel(const SweepArgs<Real> a) {
+__global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const SweepArgs<Real> a) {
   __shared__ WorkList<Real> wk;
   __shared__ __align__(8) unsigned long long stage_bar;
 

@@ -18,7 +18,7 @@ static cudaError_t launch_t(const SweepArgs<double>& a, int max_grid, size_t sme
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, FC3D_BLOCK, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<double>::value, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     cached_g = nsm * per_sm;
@@ -30,7 +30,7 @@ static cudaError_t launch_t(const SweepArgs<double>& a, int max_grid, size_t sme
   if (g > 1024) g = 1024;
   *grid = g;
   void* args[] = {(void*)&a};
-  return cudaLaunchCooperativeKernel((const void*)kern, dim3(g), dim3(FC3D_BLOCK), args, smem, s);
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(g), dim3(BlockDim<double>::value), args, smem, s);
 }
 
 template <int T>
@@ -38,7 +38,7 @@ static int grid_t() {
   int dev = 0, nsm = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nsgs_kernel<double, T>, FC3D_BLOCK, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, nsgs_kernel<double, T>, BlockDim<double>::value, 0);
   return nsm * per_sm;
 }
 
