@@ -91,10 +91,11 @@ struct WorkList {
 // mu and rho, copied from the staging buffer before it is refilled.
 template <typename Real>
 struct WorkListS {
+  // component-major, so consecutive work items sit in consecutive banks
   int p[FC3D_PASS_SLABS * FC3D_SLAB];
-  Real q[FC3D_PASS_SLABS * FC3D_SLAB][3];
-  Real ro[FC3D_PASS_SLABS * FC3D_SLAB][3];
-  Real m[FC3D_PASS_SLABS * FC3D_SLAB][12];  // 9 of D, mu, rhoN, rhoT
+  Real q[3][FC3D_PASS_SLABS * FC3D_SLAB];
+  Real ro[3][FC3D_PASS_SLABS * FC3D_SLAB];
+  Real m[12][FC3D_PASS_SLABS * FC3D_SLAB];  // 9 of D, mu, rhoN, rhoT
   int count[FC3D_PASS_SLABS];
 };
 
