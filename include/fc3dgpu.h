@@ -151,6 +151,19 @@ void fc3dgpu_ctx_destroy(fc3dgpu_ctx *ctx);
  * build the coloured device layout. */
 int fc3dgpu_ctx_set_W(fc3dgpu_ctx *ctx, int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
                       int colour_kind);
+/* Many independent problems as one block-diagonal W: the union block-CSR
+ * (problem k owns the contacts after those of problems 0..k-1; no block may
+ * join two problems), the number of problems and each one's contact count.
+ * Each problem is coloured as it would be alone.  q, mu and r are then
+ * passed as the concatenation of the problems' vectors. */
+int fc3dgpu_ctx_set_W_batch(fc3dgpu_ctx *ctx, int nproblems, const int *problem_nc, const int64_t *rowptr,
+                            const int64_t *colidx, const double *blocks, int colour_kind);
+/* Solve every problem of the batch (persistent kernels with a work queue,
+ * recorded once into a CUDA graph and replayed).  Per problem: FP32 and FP64
+ * sweeps, final fc3d_compute_error and info (as fc3dgpu_nsgs returns it);
+ * *ms = device time.  Arrays may be NULL. */
+int fc3dgpu_ctx_solve_batch(fc3dgpu_ctx *ctx, const fc3dgpu_params *p, int *sweeps32, int *sweeps64, double *error,
+                            int *info, double *ms);
 int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx *ctx, const double *q, const double *mu);
 int fc3dgpu_ctx_set_r(fc3dgpu_ctx *ctx, const double *r);
 int fc3dgpu_ctx_solve(fc3dgpu_ctx *ctx, const fc3dgpu_params *p, fc3dgpu_stats *st);

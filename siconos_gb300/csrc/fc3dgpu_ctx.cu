@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "fc3dgpu_batch_args.cuh"
 #include "fc3dgpu_sweep_launch.h"
 #include "fc3dgpu_layout.cuh"
 #include "fc3dgpu_local.cuh"
@@ -61,7 +62,8 @@ __global__ void k_adjacency(int nc, const long long* __restrict__ rowptr, const 
 // priority keys; kind 1 counts distinct neighbours (a pair may appear as
 // both (i,j) and (j,i) in W)
 __global__ void k_priority(int nc, const int* __restrict__ gptr, const int* __restrict__ adj, int kind,
-                           uint32_t* __restrict__ key, int* __restrict__ colour) {
+                           uint32_t* __restrict__ key, int* __restrict__ colour, const int* __restrict__ grp,
+                           const int* __restrict__ group_off) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
     uint32_t d = 0;
     if (kind == 1)
@@ -74,7 +76,10 @@ __global__ void k_priority(int nc, const int* __restrict__ gptr, const int* __re
           }
         d += dup ? 0 : 1;
       }
-    key[i] = colour_priority((uint32_t)i, kind, d);
+    // batched problems: the index inside the problem, so each problem is
+    // coloured exactly as it would be alone
+    const int local = grp ? i - group_off[grp[i]] : i;
+    key[i] = colour_priority((uint32_t)local, kind, d);
     colour[i] = -1;
   }
 }
@@ -313,6 +318,96 @@ __global__ void k_set_q_mu(int nc, const int* __restrict__ iperm, const double* 
   }
 }
 
+// ---- batched problems: per-problem permutation by colour ----------------
+
+__global__ void k_group_ids(int ngroups, const int* __restrict__ group_off, int* __restrict__ grp) {
+  const int g = blockIdx.x;
+  if (g >= ngroups) return;
+  for (int i = group_off[g] + threadIdx.x; i < group_off[g + 1]; i += blockDim.x) grp[i] = g;
+}
+
+// one block per problem: colour counts, colours used, slabs needed
+__global__ void k_scene_counts(const int* __restrict__ group_off, const int* __restrict__ colour,
+                               int* __restrict__ scounts, int* __restrict__ snslab, int* __restrict__ sncol) {
+  __shared__ int h[FC3D_MAX_COLOURS];
+  const int g = blockIdx.x;
+  for (int k = threadIdx.x; k < FC3D_MAX_COLOURS; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  for (int i = group_off[g] + threadIdx.x; i < group_off[g + 1]; i += blockDim.x) atomicAdd(&h[colour[i]], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ns = 0, nc = 0;
+    for (int k = 0; k < FC3D_MAX_COLOURS; k++) {
+      scounts[(size_t)g * FC3D_MAX_COLOURS + k] = h[k];
+      ns += (h[k] + FC3D_SLAB - 1) / FC3D_SLAB;
+      if (h[k]) nc = k + 1;
+    }
+    snslab[g] = ns;
+    sncol[g] = nc;
+  }
+}
+
+// one block per problem: slab table and stable scatter (index order kept
+// inside each colour), chunk by chunk with a running count per colour
+__global__ void k_scene_scatter(const int* __restrict__ group_off, const int* __restrict__ colour,
+                                const int* __restrict__ scounts, const long long* __restrict__ sbase,
+                                int* __restrict__ ssptr, int* __restrict__ perm, int* __restrict__ iperm) {
+  __shared__ int sptr[FC3D_MAX_COLOURS + 1];
+  __shared__ int carry[FC3D_MAX_COLOURS];
+  __shared__ int chunk_tot[FC3D_MAX_COLOURS];
+  __shared__ int wcount[32][FC3D_MAX_COLOURS];
+  const int g = blockIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    int sl = (int)sbase[g];
+    sptr[0] = sl;
+    for (int k = 0; k < FC3D_MAX_COLOURS; k++) {
+      sl += (scounts[(size_t)g * FC3D_MAX_COLOURS + k] + FC3D_SLAB - 1) / FC3D_SLAB;
+      sptr[k + 1] = sl;
+    }
+  }
+  for (int k = threadIdx.x; k < FC3D_MAX_COLOURS; k += blockDim.x) carry[k] = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k <= FC3D_MAX_COLOURS; k += blockDim.x)
+    ssptr[(size_t)g * (FC3D_MAX_COLOURS + 1) + k] = sptr[k];
+  for (int base = group_off[g]; base < group_off[g + 1]; base += blockDim.x) {
+    for (int t = threadIdx.x; t < 32 * FC3D_MAX_COLOURS; t += blockDim.x) (&wcount[0][0])[t] = 0;
+    __syncthreads();
+    const int i = base + threadIdx.x;
+    const int c = i < group_off[g + 1] ? colour[i] : -1;
+    const unsigned mask = __match_any_sync(0xffffffffu, c);
+    if (c >= 0 && lane == __ffs(mask) - 1) wcount[w][c] = __popc(mask);
+    __syncthreads();
+    // exclusive prefix over warps per colour; chunk totals kept aside
+    for (int cc = threadIdx.x; cc < FC3D_MAX_COLOURS; cc += blockDim.x) {
+      int run = 0;
+      for (int k = 0; k < 32; k++) {
+        const int v = wcount[k][cc];
+        wcount[k][cc] = run;
+        run += v;
+      }
+      chunk_tot[cc] = run;
+    }
+    __syncthreads();
+    if (c >= 0) {
+      const int rank = carry[c] + wcount[w][c] + __popc(mask & ((1u << lane) - 1));
+      const int p = sptr[c] * FC3D_SLAB + rank;
+      perm[p] = i;
+      iperm[i] = p;
+    }
+    __syncthreads();
+    for (int cc = threadIdx.x; cc < FC3D_MAX_COLOURS; cc += blockDim.x) carry[cc] += chunk_tot[cc];
+    __syncthreads();
+  }
+}
+
+// per-problem FP64 budget after the FP32 phase
+__global__ void k_batch_budget(int n, const double* __restrict__ out32, int max_iter, int* __restrict__ budget) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+    const int b = max_iter - (int)out32[(size_t)s * 8];
+    budget[s] = b > 0 ? b : 0;
+  }
+}
+
 // r (original order, 3 per contact) -> padded AoS copies; PLI step reset to 1
 // as fc3d_AC_initialize does at every solve (onecontact.c:115)
 __global__ void k_set_r(int nc, const int* __restrict__ iperm, const double* __restrict__ r, double* __restrict__ r64,
@@ -360,6 +455,7 @@ __global__ void k_get_r_u(int nc, const int* __restrict__ iperm, const double* _
 #include <math.h>
 #include <stdarg.h>
 
+#include <algorithm>
 #include <vector>
 #include <stdio.h>
 #include <stdlib.h>
@@ -474,6 +570,25 @@ struct fc3dgpu_ctx {
   int ccount[FC3D_MAX_COLOURS];
   std::vector<int> slab_nslot_h;
   int staging = 1;  // bulk-copy staging of slab ranges for the FP32 sweeps
+  // batched problems (0 = a single problem)
+  int nscenes = 0;
+  std::vector<int> scene_off_h;  // nscenes + 1 contact offsets
+  std::vector<double> scene_normq_h;
+  BUF(int, scene_off);
+  BUF(int, grp);
+  BUF(int, scounts);
+  BUF(int, snslab);
+  BUF(int, sncol);
+  BUF(long long, sbase);
+  BUF(int, ssptr);
+  BUF(int, sorder);
+  BUF(double, snormq);
+  BUF(int, sbudget);
+  BUF(int, squeue);
+  BUF(double, sout32);
+  BUF(double, sout64);
+  cudaGraphExec_t batch_graph = nullptr;
+  fc3dgpu_params batch_graph_params;
 };
 
 static int grid1d(long long n, int block = 256) {
@@ -527,6 +642,8 @@ extern "C" fc3dgpu_ctx* fc3dgpu_ctx_create(int device) {
   // load every sweep kernel now: with lazy module loading the first launch
   // of each instance would otherwise pay the load inside a timed solve
   fc3dgpu::warm_sweep_kernels();
+  fc3dgpu::warm_batch_kernel_f32();
+  fc3dgpu::warm_batch_kernel_f64();
   bool ok = ensure(&c->partials, &c->partials_cap, 1024 * 8) == cudaSuccess &&
             ensure(&c->barrier, &c->barrier_cap, 1024) == cudaSuccess &&
             ensure(&c->status, &c->status_cap, 4) == cudaSuccess &&
@@ -551,7 +668,9 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->rowlen, c->dpos, c->slab_nslot, c->slab_off, c->W64, c->W32, c->col, c->D64, c->D32,
                   c->rho64, c->rho32, c->q64, c->q32, c->mu64, c->mu32, c->r64, c->r32, c->rpli64, c->rpli32,
                   c->u64, c->partials, c->barrier, c->status, c->scratch, c->scratch64, c->out, c->trace,
-                  c->counters, c->timeline};
+                  c->counters, c->timeline, c->scene_off, c->grp, c->scounts, c->snslab, c->sncol, c->sbase,
+                  c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64};
+  if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; i++)
@@ -583,7 +702,8 @@ static int validate_bcsr(int nc, const int64_t* rowptr, const int64_t* colidx) {
 
 // Colour the conflict graph of the uploaded structure (rowptr/colidx on the
 // device); result in c->colour, number of colours returned.
-static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind) {
+static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, const int* grp = nullptr,
+                         const int* group_off = nullptr) {
   using namespace fc3dgpu;
   cudaStream_t s = c->stream;
   CK(ensure(&c->deg, &c->deg_cap, (size_t)nc));
@@ -607,7 +727,7 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind) {
   CK(ensure(&c->adj, &c->adj_cap, (size_t)(nadj ? nadj : 1)));
   CK(cudaMemcpyAsync(c->cursor, c->gptr, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s));
   k_adjacency<<<grid1d(nc), 256, 0, s>>>(nc, c->rowptr, c->colidx, c->cursor, c->adj);
-  k_priority<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, kind, c->key, c->colour);
+  k_priority<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, kind, c->key, c->colour, grp, group_off);
   int rounds = 0;
   for (;;) {
     CK(cudaMemsetAsync(c->scratch, 0, 2 * sizeof(int), s));
@@ -633,8 +753,8 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind) {
   return mx + 1;
 }
 
-extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx,
-                                 const double* blocks, int kind) {
+static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx, const double* blocks,
+                      int kind, int nscenes, const int* scene_nc) {
   using namespace fc3dgpu;
   if (!c || nc <= 0 || !rowptr || !colidx || !blocks) {
     fc3dgpu_set_error("fc3dgpu_ctx_set_W: invalid argument");
@@ -658,26 +778,71 @@ extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, 
   CK(cudaMemcpyAsync(c->rowptr, rowptr, sizeof(long long) * (nc + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->colidx, colidx, sizeof(long long) * nnzb, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->blocks, blocks, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
-  int ncol = colour_device(c, nc, nnzb, kind);
+  c->nscenes = nscenes;
+  const int* d_grp = nullptr;
+  if (nscenes > 0) {
+    c->scene_off_h.assign(nscenes + 1, 0);
+    for (int g = 0; g < nscenes; g++) c->scene_off_h[g + 1] = c->scene_off_h[g] + scene_nc[g];
+    if (c->scene_off_h[nscenes] != nc) {
+      fc3dgpu_set_error("problem sizes add up to %d contacts, W has %d", c->scene_off_h[nscenes], nc);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+    CK(ensure(&c->scene_off, &c->scene_off_cap, (size_t)nscenes + 1));
+    CK(ensure(&c->grp, &c->grp_cap, (size_t)nc));
+    CK(cudaMemcpyAsync(c->scene_off, c->scene_off_h.data(), sizeof(int) * (nscenes + 1), cudaMemcpyHostToDevice, s));
+    k_group_ids<<<nscenes, 256, 0, s>>>(nscenes, c->scene_off, c->grp);
+    d_grp = c->grp;
+  }
+  int ncol = colour_device(c, nc, nnzb, kind, d_grp, nscenes > 0 ? c->scene_off : nullptr);
   if (ncol < 0) return ncol;
-  // stable permutation by colour
   const int nblk = (nc + 1023) / 1024;
-  CK(ensure(&c->blockhist, &c->blockhist_cap, (size_t)nblk * FC3D_MAX_COLOURS));
   CK(ensure(&c->counts, &c->counts_cap, FC3D_MAX_COLOURS));
   CK(ensure(&c->sptr_d, &c->sptr_d_cap, FC3D_MAX_COLOURS + 1));
-  k_colour_hist<<<nblk, 1024, 0, s>>>(nc, c->colour, c->blockhist);
-  k_colour_offsets<<<1, FC3D_MAX_COLOURS, 0, s>>>(nblk, c->blockhist, c->counts, c->sptr_d);
-  CK(cudaMemcpyAsync(c->sptr, c->sptr_d, sizeof(int) * (FC3D_MAX_COLOURS + 1), cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(c->ccount, c->counts, sizeof(int) * FC3D_MAX_COLOURS, cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  c->ncol = ncol;
-  c->nslab = c->sptr[ncol];
+  if (nscenes == 0) {
+    // stable permutation by colour
+    CK(ensure(&c->blockhist, &c->blockhist_cap, (size_t)nblk * FC3D_MAX_COLOURS));
+    k_colour_hist<<<nblk, 1024, 0, s>>>(nc, c->colour, c->blockhist);
+    k_colour_offsets<<<1, FC3D_MAX_COLOURS, 0, s>>>(nblk, c->blockhist, c->counts, c->sptr_d);
+    CK(cudaMemcpyAsync(c->sptr, c->sptr_d, sizeof(int) * (FC3D_MAX_COLOURS + 1), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(c->ccount, c->counts, sizeof(int) * FC3D_MAX_COLOURS, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    c->ncol = ncol;
+    c->nslab = c->sptr[ncol];
+  } else {
+    // per problem, stable permutation by colour; problems one after the other
+    CK(ensure(&c->scounts, &c->scounts_cap, (size_t)nscenes * FC3D_MAX_COLOURS));
+    CK(ensure(&c->snslab, &c->snslab_cap, (size_t)nscenes));
+    CK(ensure(&c->sncol, &c->sncol_cap, (size_t)nscenes));
+    CK(ensure(&c->sbase, &c->sbase_cap, (size_t)nscenes));
+    CK(ensure(&c->ssptr, &c->ssptr_cap, (size_t)nscenes * (FC3D_MAX_COLOURS + 1)));
+    k_scene_counts<<<nscenes, 256, 0, s>>>(c->scene_off, c->colour, c->scounts, c->snslab, c->sncol);
+    k_scan_excl<int><<<1, 1024, 0, s>>>(nscenes, c->snslab, c->sbase, c->scratch64);
+    long long tot = 0;
+    CK(cudaMemcpyAsync(&tot, c->scratch64, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    c->ncol = ncol;
+    c->nslab = (int)tot;
+    for (int k = 0; k <= FC3D_MAX_COLOURS; k++) c->sptr[k] = k ? c->nslab : 0;
+    for (int k = 0; k < FC3D_MAX_COLOURS; k++) c->ccount[k] = 0;
+  }
   c->npad = c->nslab * FC3D_SLAB;
   const int npad = c->npad, nslab = c->nslab;
   CK(ensure(&c->perm, &c->perm_cap, (size_t)npad));
   CK(ensure(&c->iperm, &c->iperm_cap, (size_t)nc));
   CK(cudaMemsetAsync(c->perm, 0xff, sizeof(int) * npad, s));
-  k_colour_scatter<<<nblk, 1024, 0, s>>>(nc, c->colour, c->blockhist, c->sptr_d, c->perm, c->iperm);
+  if (nscenes == 0) {
+    k_colour_scatter<<<nblk, 1024, 0, s>>>(nc, c->colour, c->blockhist, c->sptr_d, c->perm, c->iperm);
+  } else {
+    k_scene_scatter<<<nscenes, 1024, 0, s>>>(c->scene_off, c->colour, c->scounts, c->sbase, c->ssptr, c->perm,
+                                             c->iperm);
+    // problems by decreasing size for the work queue
+    std::vector<int> order(nscenes);
+    for (int g = 0; g < nscenes; g++) order[g] = g;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return scene_nc[x] > scene_nc[y]; });
+    CK(ensure(&c->sorder, &c->sorder_cap, (size_t)nscenes));
+    CK(cudaMemcpyAsync(c->sorder, order.data(), sizeof(int) * nscenes, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+  }
   // rows, slabs, slots
   CK(ensure(&c->rowlen, &c->rowlen_cap, (size_t)npad));
   CK(ensure(&c->dpos, &c->dpos_cap, (size_t)npad));
@@ -742,6 +907,54 @@ extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, 
   return 0;
 }
 
+extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx,
+                                 const double* blocks, int kind) {
+  if (c && c->batch_graph) {
+    cudaGraphExecDestroy(c->batch_graph);
+    c->batch_graph = nullptr;
+  }
+  return set_W_impl(c, nc, rowptr, colidx, blocks, kind, 0, nullptr);
+}
+
+// Many independent problems as one block-diagonal W: the union block-CSR
+// (problem k's rows and columns are contacts scene_off[k] ..), nscenes and
+// each problem's contact count.
+extern "C" int fc3dgpu_ctx_set_W_batch(fc3dgpu_ctx* c, int nscenes, const int* scene_nc, const int64_t* rowptr,
+                                       const int64_t* colidx, const double* blocks, int kind) {
+  if (!c || nscenes <= 0 || !scene_nc) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_W_batch: invalid argument");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  long long nc = 0;
+  for (int k = 0; k < nscenes; k++) {
+    if (scene_nc[k] <= 0) {
+      fc3dgpu_set_error("problem %d has no contact", k);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+    nc += scene_nc[k];
+  }
+  if (nc > 0x7fffffffLL) {
+    fc3dgpu_set_error("too many contacts in the batch");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  // a block of W must not join two problems
+  long long off = 0;
+  for (int k = 0; k < nscenes; k++) {
+    for (long long i = off; i < off + scene_nc[k]; i++)
+      for (int64_t kk = rowptr[i]; kk < rowptr[i + 1]; kk++)
+        if (colidx[kk] < off || colidx[kk] >= off + scene_nc[k]) {
+          fc3dgpu_set_error("W couples problem %d to another problem (row %lld)", k, i);
+          return NUMERICS_ERR_INVALID_ARGUMENT;
+        }
+    off += scene_nc[k];
+  }
+  if (c->batch_graph) {
+    cudaGraphExecDestroy(c->batch_graph);
+    c->batch_graph = nullptr;
+  }
+  return set_W_impl(c, (int)nc, rowptr, colidx, blocks, kind, nscenes, scene_nc);
+}
+
 extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const double* mu) {
   using namespace fc3dgpu;
   if (!c || !c->have_W || !q || !mu) {
@@ -761,6 +974,18 @@ extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const doubl
   double s2 = 0.0;
   for (long long i = 0; i < 3LL * nc; i++) s2 += q[i] * q[i];
   c->norm_q = sqrt(s2);
+  if (c->nscenes > 0) {
+    c->scene_normq_h.assign(c->nscenes, 0.0);
+    for (int g = 0; g < c->nscenes; g++) {
+      double t = 0.0;
+      for (long long i = 3LL * c->scene_off_h[g]; i < 3LL * c->scene_off_h[g + 1]; i++) t += q[i] * q[i];
+      c->scene_normq_h[g] = sqrt(t);
+    }
+    CK(ensure(&c->snormq, &c->snormq_cap, (size_t)c->nscenes));
+    CK(cudaMemcpyAsync(c->snormq, c->scene_normq_h.data(), sizeof(double) * c->nscenes, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
   c->have_q = true;
   return 0;
 }
@@ -1177,4 +1402,132 @@ extern "C" int fc3dgpu_colour(int nc, const int64_t* rowptr, const int64_t* coli
   }
   fc3dgpu_ctx_destroy(c);
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Batched solve: every problem of a fc3dgpu_ctx_set_W_batch layout in one
+// persistent launch per precision, the whole sequence captured once in a
+// CUDA graph and replayed while the parameters stay the same.
+// ---------------------------------------------------------------------------
+static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
+  using namespace fc3dgpu;
+  cudaStream_t s = c->stream;
+  const int ns = c->nscenes;
+  int g = 0;
+  CK(cudaMemsetAsync(c->squeue, 0, 2 * sizeof(int), s));
+  CK(cudaMemsetAsync(c->sout32, 0, sizeof(double) * 8 * ns, s));
+  if (p->precision == 0 && p->max_iter > 0) {
+    BatchArgs<float> b;
+    fill_args<float>(c, b.base, c->W32, c->D32, c->q32, c->mu32, c->rho32, c->r32, c->rpli32);
+    b.base.max_sweeps = p->max_iter;
+    b.base.mode = 0;
+    b.base.user_tol = p->tol;
+    b.base.local_tol = p->local_tol32;
+    b.base.switch_tol = p->switch_tol;
+    b.base.stall_window = p->stall_window;
+    b.base.newton_max = p->newton_max;
+    b.base.pli_max = p->pli_max;
+    b.base.ls_max = p->ls_max;
+    b.base.trace = nullptr;
+    b.base.timeline = nullptr;
+    b.nscenes = ns;
+    b.order = c->sorder;
+    b.scene_ncol = c->sncol;
+    b.scene_sptr = c->ssptr;
+    b.scene_normq = c->snormq;
+    b.scene_budget = nullptr;
+    b.queue = c->squeue;
+    b.scene_out = c->sout32;
+    CK(launch_batch_f32(b, s, &g));
+    k_r32_to_r64<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r32, c->rpli32, c->r64, c->rpli64);
+  }
+  k_batch_budget<<<grid1d(ns), 256, 0, s>>>(ns, c->sout32, p->fp32_only ? 0 : p->max_iter, c->sbudget);
+  {
+    BatchArgs<double> b;
+    fill_args<double>(c, b.base, c->W64, c->D64, c->q64, c->mu64, c->rho64, c->r64, c->rpli64);
+    b.base.max_sweeps = p->max_iter;
+    b.base.mode = 1;
+    b.base.user_tol = p->tol;
+    b.base.local_tol = p->local_tol;
+    b.base.switch_tol = 0.0;
+    b.base.stall_window = 0;
+    b.base.newton_max = p->newton_max;
+    b.base.pli_max = p->pli_max;
+    b.base.ls_max = p->ls_max;
+    b.base.trace = nullptr;
+    b.base.timeline = nullptr;
+    b.nscenes = ns;
+    b.order = c->sorder;
+    b.scene_ncol = c->sncol;
+    b.scene_sptr = c->ssptr;
+    b.scene_normq = c->snormq;
+    b.scene_budget = c->sbudget;
+    b.queue = c->squeue + 1;
+    b.scene_out = c->sout64;
+    CK(launch_batch_f64(b, s, &g));
+  }
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_solve_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p, int* sweeps32, int* sweeps64,
+                                       double* error, int* info, double* ms) {
+  using namespace fc3dgpu;
+  if (!c || !p || c->nscenes <= 0 || !c->have_q || !c->have_r) {
+    fc3dgpu_set_error("fc3dgpu_ctx_solve_batch: no batch layout, q/mu or r");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const int ns = c->nscenes;
+  CK(ensure(&c->sbudget, &c->sbudget_cap, (size_t)ns));
+  CK(ensure(&c->squeue, &c->squeue_cap, 2));
+  CK(ensure(&c->sout32, &c->sout32_cap, (size_t)ns * 8));
+  CK(ensure(&c->sout64, &c->sout64_cap, (size_t)ns * 8));
+  if (c->batch_graph && memcmp(&c->batch_graph_params, p, sizeof(*p)) != 0) {
+    cudaGraphExecDestroy(c->batch_graph);
+    c->batch_graph = nullptr;
+  }
+  if (!c->batch_graph) {
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = record_batch(c, p);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CK(e);
+    e = cudaGraphInstantiate(&c->batch_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(e);
+    c->batch_graph_params = *p;
+  }
+  CK(cudaMemsetAsync(c->status, 0, sizeof(int), s));
+  CK(cudaEventRecord(c->ev[0], s));
+  CK(cudaGraphLaunch(c->batch_graph, s));
+  CK(cudaEventRecord(c->ev[1], s));
+  c->launches += 4;
+  std::vector<double> o32((size_t)ns * 8), o64((size_t)ns * 8);
+  int status = 0;
+  CK(cudaMemcpyAsync(o32.data(), c->sout32, sizeof(double) * 8 * ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(o64.data(), c->sout64, sizeof(double) * 8 * ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&status, c->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float t = 0;
+  cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
+  if (ms) *ms = t;
+  for (int k = 0; k < ns; k++) {
+    const int n32 = (int)o32[(size_t)k * 8], n64 = (int)o64[(size_t)k * 8];
+    int inf = (int)o64[(size_t)k * 8 + 3];
+    if (n32 + n64 >= p->max_iter && inf > 0) inf = NUMERICS_ERR_MAX_ITER;
+    if (sweeps32) sweeps32[k] = n32;
+    if (sweeps64) sweeps64[k] = n64;
+    if (error) error[k] = o64[(size_t)k * 8 + 2];
+    if (info) info[k] = inf;
+  }
+  if (status) {
+    fc3dgpu_set_error("device status %d in the batched solve", status);
+    return NUMERICS_ERR_UNKNOWN;
+  }
+  return 0;
 }

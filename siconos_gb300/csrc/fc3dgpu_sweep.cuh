@@ -349,6 +349,13 @@ __device__ __forceinline__ void solve_item(const SweepArgs<Real>& a, WorkList<Re
   }
 }
 
+// Slab range [lo, hi) of one colour handled by this block.
+__device__ __forceinline__ void block_range(int s0, int s1, int& lo, int& hi) {
+  const int n = s1 - s0;
+  lo = s0 + (int)((long long)n * blockIdx.x / gridDim.x);
+  hi = s0 + (int)((long long)n * (blockIdx.x + 1) / gridDim.x);
+}
+
 // One colour with one lane per contact.  The colour's slabs are split into
 // one contiguous range per block (so no block takes a second round while
 // others idle) and a block handles its range in passes of up to
@@ -360,15 +367,12 @@ __device__ __forceinline__ void solve_item(const SweepArgs<Real>& a, WorkList<Re
 // solve latency per pass, with lanes busy instead of idling beside
 // take-offs.
 template <typename Real>
-__device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a, int s0, int s1, Real ltol,
-                                                       double& dr2, double& rr2, WorkList<Real>& wk,
-                                                       unsigned long long* tl) {
+__device__ __forceinline__ void process_range_compact(const SweepArgs<Real>& a, int lo, int hi, Real ltol,
+                                                      double& dr2, double& rr2, WorkList<Real>& wk,
+                                                      unsigned long long* tl) {
   constexpr int NWB = BlockDim<Real>::value / 32;
   constexpr int MAXR = (FC3D_PASS_SLABS + NWB - 1) / NWB;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n = s1 - s0;
-  const int lo = s0 + (int)((long long)n * blockIdx.x / gridDim.x);
-  const int hi = s0 + (int)((long long)n * (blockIdx.x + 1) / gridDim.x);
   for (int ps = lo; ps < hi; ps += FC3D_PASS_SLABS) {
     const int np = min(FC3D_PASS_SLABS, hi - ps);
     Real acc[MAXR][3], ro[MAXR][3];
@@ -452,13 +456,6 @@ __device__ __forceinline__ void process_colour_compact(const SweepArgs<Real>& a,
     for (int t = threadIdx.x; t < total; t += blockDim.x) solve_item(a, wk, t, ltol, dr2, rr2);
     __syncthreads();
   }
-}
-
-// Slab range [lo, hi) of one colour handled by this block.
-__device__ __forceinline__ void block_range(int s0, int s1, int& lo, int& hi) {
-  const int n = s1 - s0;
-  lo = s0 + (int)((long long)n * blockIdx.x / gridDim.x);
-  hi = s0 + (int)((long long)n * (blockIdx.x + 1) / gridDim.x);
 }
 
 // Issue the bulk copies of W, col and q for slabs [lo, hi) into the
@@ -693,10 +690,15 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
 // position, SBM_gemv_3x3, SparseBlockMatrix.c:360-419) and the partial sums
 // of the squared natural-map error, |u|^2 and |r|^2.  FP64 only.
 template <typename Real>
-__device__ __forceinline__ void full_error_rows(const SweepArgs<Real>& a, double v[3]) {
+__device__ __forceinline__ void full_error_rows(const SweepArgs<Real>& a, double v[3], int p0 = 0, int p1 = -1,
+                                                int tid = -1, int nth = -1) {
   v[0] = v[1] = v[2] = 0.0;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-  for (int p = tid; p < a.npad; p += nth) {
+  if (p1 < 0) p1 = a.npad;
+  if (tid < 0) {
+    tid = blockIdx.x * blockDim.x + threadIdx.x;
+    nth = gridDim.x * blockDim.x;
+  }
+  for (int p = p0 + tid; p < p1; p += nth) {
     if (__ldg(&a.perm[p]) < 0) continue;
     const int slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
     const long long base = a.slab_off[slab];
@@ -800,8 +802,10 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
                                          tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6 + 2 : nullptr))
           return;
       } else if (T == 1) {
-        process_colour_compact<Real>(a, s0, a.sptr[c + 1], (Real)local_tol, acc[0], acc[1], wk,
-                                     tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6 + 2 : nullptr);
+        int lo, hi;
+        block_range(s0, a.sptr[c + 1], lo, hi);
+        process_range_compact<Real>(a, lo, hi, (Real)local_tol, acc[0], acc[1], wk,
+                                    tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6 + 2 : nullptr);
       } else {
         for (int u = gw; u < nunits; u += tw) {
           const long long t0 = a.counters ? clock64() : 0;

@@ -1,4 +1,5 @@
 // float instantiations of the persistent coloured NSGS kernel.
+#include "fc3dgpu_batch.cuh"
 #include "fc3dgpu_sweep.cuh"
 #include "fc3dgpu_sweep_launch.h"
 
@@ -71,6 +72,33 @@ int sweep_grid_f32(int lanes) {
     case 8: return grid_t<8>();
     default: return 0;
   }
+}
+
+cudaError_t launch_batch_f32(const BatchArgs<float>& b, cudaStream_t s, int* grid) {
+  auto kern = nsgs_batch_kernel<float>;
+  static int cached_dev = -1, cached_g = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (cached_dev != dev) {
+    int nsm = 0, per_sm = 0;
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<float>::value, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    cached_g = nsm * per_sm;
+    cached_dev = dev;
+  }
+  int g = cached_g < b.nscenes ? cached_g : b.nscenes;
+  *grid = g;
+  kern<<<g, BlockDim<float>::value, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+void warm_batch_kernel_f32() {
+  cudaFuncAttributes fa;
+  cudaFuncGetAttributes(&fa, nsgs_batch_kernel<float>);
 }
 
 }  // namespace fc3dgpu

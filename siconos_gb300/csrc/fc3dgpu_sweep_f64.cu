@@ -1,4 +1,5 @@
 // double instantiations of the persistent coloured NSGS kernel.
+#include "fc3dgpu_batch.cuh"
 #include "fc3dgpu_sweep.cuh"
 #include "fc3dgpu_sweep_launch.h"
 
@@ -69,6 +70,33 @@ int sweep_grid_f64(int lanes) {
     case 8: return grid_t<8>();
     default: return 0;
   }
+}
+
+cudaError_t launch_batch_f64(const BatchArgs<double>& b, cudaStream_t s, int* grid) {
+  auto kern = nsgs_batch_kernel<double>;
+  static int cached_dev = -1, cached_g = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (cached_dev != dev) {
+    int nsm = 0, per_sm = 0;
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<double>::value, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    cached_g = nsm * per_sm;
+    cached_dev = dev;
+  }
+  int g = cached_g < b.nscenes ? cached_g : b.nscenes;
+  *grid = g;
+  kern<<<g, BlockDim<double>::value, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+void warm_batch_kernel_f64() {
+  cudaFuncAttributes fa;
+  cudaFuncGetAttributes(&fa, nsgs_batch_kernel<double>);
 }
 
 }  // namespace fc3dgpu

@@ -17,5 +17,11 @@ cudaError_t launch_sweep_f64(const SweepArgs<double>& a, int lanes, int max_grid
                              int* grid);
 int sweep_grid_f32(int lanes);
 void warm_sweep_kernels();
+template <typename Real>
+struct BatchArgs;
+cudaError_t launch_batch_f32(const BatchArgs<float>& b, cudaStream_t s, int* grid);
+cudaError_t launch_batch_f64(const BatchArgs<double>& b, cudaStream_t s, int* grid);
+void warm_batch_kernel_f32();
+void warm_batch_kernel_f64();
 int sweep_grid_f64(int lanes);
 }  // namespace fc3dgpu

@@ -65,6 +65,41 @@ class DeviceSolver:
     def staging(self, on: bool) -> bool:
         return bool(self.L.fc3dgpu_ctx_staging(self.ctx, int(on)))
 
+    # ---- batched problems -------------------------------------------------
+    def load_batch(self, scenes, colouring: int = 0):
+        """Upload independent problems (objects with nc, rowptr, colidx,
+        blocks, q, mu) as one batch; r starts at zero."""
+        ncs = np.array([sc.nc for sc in scenes], np.int32)
+        offs = np.concatenate([[0], np.cumsum(ncs)]).astype(np.int64)
+        boffs = np.concatenate([[0], np.cumsum([sc.rowptr[-1] for sc in scenes])]).astype(np.int64)
+        rowptr = np.concatenate([sc.rowptr[:-1] + b for sc, b in zip(scenes, boffs[:-1])] + [[boffs[-1]]])
+        colidx = np.concatenate([sc.colidx + o for sc, o in zip(scenes, offs[:-1])])
+        blocks = np.concatenate([np.asarray(sc.blocks).reshape(-1, 9) for sc in scenes])
+        self._check(self.L.fc3dgpu_ctx_set_W_batch(self.ctx, len(scenes), ncs, np.ascontiguousarray(rowptr, np.int64),
+                                                   np.ascontiguousarray(colidx, np.int64),
+                                                   np.ascontiguousarray(blocks).reshape(-1), colouring), "set_W_batch")
+        self.nc = int(offs[-1])
+        self.batch_offsets = offs
+        self.set_q_mu(np.concatenate([sc.q for sc in scenes]), np.concatenate([sc.mu for sc in scenes]))
+        self.set_r(np.zeros(3 * self.nc))
+
+    def solve_batch(self, **kw) -> dict:
+        n = len(self.batch_offsets) - 1
+        p = self.params(**kw)
+        s32 = np.zeros(n, np.int32)
+        s64 = np.zeros(n, np.int32)
+        err = np.zeros(n)
+        info = np.zeros(n, np.int32)
+        ms = C.c_double()
+        self._check(self.L.fc3dgpu_ctx_solve_batch(self.ctx, C.byref(p), s32.ctypes.data, s64.ctypes.data,
+                                                   err.ctypes.data, info.ctypes.data, C.byref(ms)), "solve_batch")
+        return {"sweeps32": s32, "sweeps64": s64, "error": err, "info": info, "ms": ms.value}
+
+    def get_batch(self):
+        r, u = self.get()
+        o = self.batch_offsets
+        return [r[3 * o[k]:3 * o[k + 1]] for k in range(len(o) - 1)], [u[3 * o[k]:3 * o[k + 1]] for k in range(len(o) - 1)]
+
     def zero_r(self):
         self._check(self.L.fc3dgpu_ctx_zero_r(self.ctx), "zero_r")
 

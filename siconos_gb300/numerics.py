@@ -148,6 +148,9 @@ ABI = {
     "fc3dgpu_ctx_destroy": (None, [C.c_void_p]),
     "fc3dgpu_ctx_set_W": (C.c_int, [C.c_void_p, C.c_int, _I64, _I64, _F64, C.c_int]),
     "fc3dgpu_ctx_set_q_mu": (C.c_int, [C.c_void_p, _F64, _F64]),
+    "fc3dgpu_ctx_set_W_batch": (C.c_int, [C.c_void_p, C.c_int, _I32, _I64, _I64, _F64, C.c_int]),
+    "fc3dgpu_ctx_solve_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]),
     "fc3dgpu_ctx_set_r": (C.c_int, [C.c_void_p, _F64]),
     "fc3dgpu_ctx_solve": (C.c_int, [C.c_void_p, C.POINTER(FC3DGPUParams), C.POINTER(FC3DGPUStats)]),
     "fc3dgpu_ctx_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
