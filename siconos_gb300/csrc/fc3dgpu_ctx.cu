@@ -1488,6 +1488,8 @@ extern "C" int fc3dgpu_ctx_solve_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p, 
     c->batch_graph = nullptr;
   }
   if (!c->batch_graph) {
+    CK(prepare_batch_f32());
+    CK(prepare_batch_f64());
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     int rc = record_batch(c, p);

@@ -72,9 +72,29 @@ int sweep_grid_f64(int lanes) {
   }
 }
 
+static int batch_cached_dev_f64 = -1, batch_cached_g_f64 = 0;
+
+// Occupancy of the batched kernel, queried outside any stream capture.
+cudaError_t prepare_batch_f64() {
+  auto kern = nsgs_batch_kernel<double>;
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (batch_cached_dev_f64 == dev) return cudaSuccess;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<double>::value, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  batch_cached_g_f64 = nsm * per_sm;
+  batch_cached_dev_f64 = dev;
+  return cudaSuccess;
+}
+
 cudaError_t launch_batch_f64(const BatchArgs<double>& b, cudaStream_t s, int* grid) {
   auto kern = nsgs_batch_kernel<double>;
-  static int cached_dev = -1, cached_g = 0;
+  int& cached_dev = batch_cached_dev_f64;
+  int& cached_g = batch_cached_g_f64;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;

@@ -22,6 +22,8 @@ struct BatchArgs;
 cudaError_t launch_batch_f32(const BatchArgs<float>& b, cudaStream_t s, int* grid);
 cudaError_t launch_batch_f64(const BatchArgs<double>& b, cudaStream_t s, int* grid);
 void warm_batch_kernel_f32();
+cudaError_t prepare_batch_f32();
+cudaError_t prepare_batch_f64();
 void warm_batch_kernel_f64();
 int sweep_grid_f64(int lanes);
 }  // namespace fc3dgpu
