@@ -197,6 +197,34 @@ unsigned long long fc3dgpu_ctx_launches(fc3dgpu_ctx *ctx);
 /* Norm of q used by the relative error (default: computed from q). */
 int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx *ctx, double norm_q);
 
+/* ---- Error evaluation without allocation --------------------------------
+ * No counterpart in the reference (whose fc3d_compute_error,
+ * fc3d_compute_error.c:70-122, is host code).  For callers that cannot let a
+ * library allocate device memory: an application whose memory pool owns the
+ * device, where a cudaMalloc or cudaFree would synchronise the device
+ * mid-step or find no memory left.
+ *
+ * Computes velocity = W reaction + q and the relative natural-map error of
+ * fc3d_compute_error on the current device, on `stream` (a cudaStream_t; NULL
+ * is the default stream), asynchronously: *error is written when the stream
+ * reaches the kernel.  Every pointer is memory the device can access: W as
+ * block-CSR (rowptr[nc+1], colidx[nnz], blocks[9 nnz], 3x3 blocks
+ * column-major), q, mu, reaction as in FrictionContactProblem.  velocity may
+ * be NULL.  A row pointer or column index out of range makes *error NaN.
+ *
+ * Scratch is a fixed device array of FC3DGPU_NOALLOC_SCRATCH_BYTES inside the
+ * library; no call allocates or frees memory.  The first call on a device
+ * looks the array up (once per device): make it before any stream capture
+ * starts.  Calls share the array, so two calls in flight at once on the same
+ * device (other streams or host threads) race: order them on one stream.
+ * More than FC3DGPU_NOALLOC_MAX_CONTACTS contacts is rejected with
+ * NUMERICS_ERR_INVALID_ARGUMENT before any device work. */
+#define FC3DGPU_NOALLOC_MAX_CONTACTS 4194304
+#define FC3DGPU_NOALLOC_SCRATCH_BYTES (8 * (3 * (FC3DGPU_NOALLOC_MAX_CONTACTS / 256) + 32))
+int fc3dgpu_compute_error_device(int nc, int64_t nnz, const int64_t *rowptr, const int64_t *colidx,
+                                 const double *blocks, const double *q, const double *mu, const double *reaction,
+                                 double norm_q, double *velocity, double *error, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

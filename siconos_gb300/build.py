@@ -24,6 +24,7 @@ C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c"]
 CU_SOURCES = {
     "fc3dgpu_ctx.cu": ["--fmad=false"],
     "fc3dgpu_sweep_f64.cu": ["--fmad=false"],
+    "fc3dgpu_noalloc.cu": ["--fmad=false"],
     # the FP32 sweeps are the accelerator whose result the FP64 polish
     # finishes: approximate division and square root, denormals flushed
     "fc3dgpu_sweep_f32.cu": ["--use_fast_math"],

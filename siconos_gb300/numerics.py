@@ -159,6 +159,9 @@ ABI = {
     "fc3dgpu_ctx_colours": (C.c_int, [C.c_void_p, _I32]),
     "fc3dgpu_ctx_counters": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "fc3dgpu_ctx_set_norm_q": (C.c_int, [C.c_void_p, C.c_double]),
+    "fc3dgpu_compute_error_device": (C.c_int, [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+                                               C.c_void_p]),
     "fc3dgpu_ctx_zero_r": (C.c_int, [C.c_void_p]),
     "fc3dgpu_ctx_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_timeline": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
