@@ -25,6 +25,8 @@ CU_SOURCES = {
     "fc3dgpu_ctx.cu": ["--fmad=false"],
     "fc3dgpu_sweep_f64.cu": ["--fmad=false"],
     "fc3dgpu_noalloc.cu": ["--fmad=false"],
+    # BF16 tensor-core MLP of the learned warm start
+    "fc3dgpu_mlp.cu": [],
     # the FP32 sweeps are the accelerator whose result the FP64 polish
     # finishes: approximate division and square root, denormals flushed
     "fc3dgpu_sweep_f32.cu": ["--use_fast_math"],

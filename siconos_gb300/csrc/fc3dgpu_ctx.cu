@@ -18,6 +18,7 @@
 #include "fc3dgpu_sweep_launch.h"
 #include "fc3dgpu_layout.cuh"
 #include "fc3dgpu_local.cuh"
+#include "fc3dgpu_mlp.h"
 
 namespace fc3dgpu {
 
@@ -436,6 +437,64 @@ __global__ void k_r64_to_r32(int npad, const double* __restrict__ r64, float* __
     for (int a = 0; a < 3; a++) r32[4 * (size_t)p + a] = (float)r64[4 * (size_t)p + a];
 }
 
+// The 17 warm-start features of every row (padding rows: zeros): the
+// diagonal block (column-major), q, mu, the current reaction, the gap of
+// the row's contact (gapo in the caller's order, or 0).
+__global__ void k_features(int npad, const int* __restrict__ perm, const double* __restrict__ D64,
+                           const double* __restrict__ q64, const double* __restrict__ mu64,
+                           const double* __restrict__ r64, const double* __restrict__ gapo, float* __restrict__ X) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x) {
+    float* x = X + (size_t)p * FC3DGPU_MLP_FEATURES;
+    const int i = perm[p];
+    if (i < 0) {
+      for (int f = 0; f < FC3DGPU_MLP_FEATURES; f++) x[f] = 0.f;
+      continue;
+    }
+    const int slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
+    for (int e = 0; e < 9; e++) x[e] = (float)D64[((size_t)slab * 9 + e) * FC3D_SLAB + k];
+    for (int a = 0; a < 3; a++) x[9 + a] = (float)q64[(size_t)slab * 3 * FC3D_SLAB + a * FC3D_SLAB + k];
+    x[12] = (float)mu64[(size_t)slab * FC3D_SLAB + k];
+    for (int a = 0; a < 3; a++) x[13 + a] = (float)r64[4 * (size_t)p + a];
+    x[16] = gapo ? (float)gapo[i] : 0.f;
+  }
+}
+
+__global__ void k_gather_features(int nc, const int* __restrict__ iperm, const float* __restrict__ Xp,
+                                  float* __restrict__ X) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)nc * FC3DGPU_MLP_FEATURES;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / FC3DGPU_MLP_FEATURES), f = (int)(e % FC3DGPU_MLP_FEATURES);
+    X[e] = Xp[(size_t)iperm[i] * FC3DGPU_MLP_FEATURES + f];
+  }
+}
+
+// Keep the current reaction in rbak and put the proposal, projected on the
+// row's friction cone, in its place.
+__global__ void k_take_proposal(int npad, const int* __restrict__ perm, const float* __restrict__ Y,
+                                const double* __restrict__ mu64, double* __restrict__ r64, float* __restrict__ r32,
+                                double* __restrict__ rbak) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x) {
+    for (int a = 0; a < 3; a++) rbak[4 * (size_t)p + a] = r64[4 * (size_t)p + a];
+    if (perm[p] < 0) continue;
+    double r[3] = {(double)Y[3 * (size_t)p], (double)Y[3 * (size_t)p + 1], (double)Y[3 * (size_t)p + 2]};
+    const int slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
+    project_cone<double>(r, mu64[(size_t)slab * FC3D_SLAB + k]);
+    for (int a = 0; a < 3; a++) {
+      r64[4 * (size_t)p + a] = r[a];
+      r32[4 * (size_t)p + a] = (float)r[a];
+    }
+  }
+}
+
+__global__ void k_restore_r(int npad, const double* __restrict__ rbak, double* __restrict__ r64,
+                            float* __restrict__ r32) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x)
+    for (int a = 0; a < 3; a++) {
+      r64[4 * (size_t)p + a] = rbak[4 * (size_t)p + a];
+      r32[4 * (size_t)p + a] = (float)rbak[4 * (size_t)p + a];
+    }
+}
+
 __global__ void k_get_r_u(int nc, const int* __restrict__ iperm, const double* __restrict__ r64,
                           const double* __restrict__ u64, double* __restrict__ r, double* __restrict__ u) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
@@ -589,6 +648,11 @@ struct fc3dgpu_ctx {
   BUF(double, sout64);
   cudaGraphExec_t batch_graph = nullptr;
   fc3dgpu_params batch_graph_params;
+  // learned warm start
+  BUF(float, feat);
+  BUF(float, prop);
+  BUF(double, rbak);
+  BUF(double, gapo);
 };
 
 static int grid1d(long long n, int block = 256) {
@@ -669,7 +733,8 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->rho64, c->rho32, c->q64, c->q32, c->mu64, c->mu32, c->r64, c->r32, c->rpli64, c->rpli32,
                   c->u64, c->partials, c->barrier, c->status, c->scratch, c->scratch64, c->out, c->trace,
                   c->counters, c->timeline, c->scene_off, c->grp, c->scounts, c->snslab, c->sncol, c->sbase,
-                  c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64};
+                  c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64, c->feat,
+                  c->prop, c->rbak, c->gapo};
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1218,6 +1283,11 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
       const int g1 = sweep_grid_f32(1);
       smem = staging_sizes<float>(c, g1, &a.stage_w_bytes, &a.stage_c_bytes, &a.stage_q_bytes, &a.stage_d_bytes);
     }
+    // the FP32 sweeps start from the context's reaction (the FP64 iterate of
+    // a previous solve, a warm start, or what fc3dgpu_ctx_set_r gave)
+    k_r64_to_r32<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r64, c->r32);
+    CK(cudaGetLastError());
+    c->launches++;
     CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
     CK(launch_sweep_f32(a, lanes, 0, smem, s, &grid));
     c->launches++;
@@ -1530,6 +1600,91 @@ extern "C" int fc3dgpu_ctx_solve_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p, 
   if (status) {
     fc3dgpu_set_error("device status %d in the batched solve", status);
     return NUMERICS_ERR_UNKNOWN;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Learned warm start (include/fc3dgpu_mlp.h)
+// ---------------------------------------------------------------------------
+static int features_impl(fc3dgpu_ctx* c, const double* gap) {
+  using namespace fc3dgpu;
+  cudaStream_t s = c->stream;
+  if (ensure(&c->feat, &c->feat_cap, (size_t)c->npad * FC3DGPU_MLP_FEATURES) != cudaSuccess ||
+      ensure(&c->gapo, &c->gapo_cap, (size_t)(c->nc ? c->nc : 1)) != cudaSuccess) {
+    fc3dgpu_set_error("warm start: allocation failed");
+    return NUMERICS_ERR_MEMORY;
+  }
+  if (gap) CK(cudaMemcpyAsync(c->gapo, gap, sizeof(double) * c->nc, cudaMemcpyHostToDevice, s));
+  k_features<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->perm, c->D64, c->q64, c->mu64, c->r64,
+                                              gap ? c->gapo : nullptr, c->feat);
+  CK(cudaGetLastError());
+  c->launches++;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_features(fc3dgpu_ctx* c, const double* gap, float* X) {
+  using namespace fc3dgpu;
+  if (!c || !X) return NUMERICS_ERR_NULL_POINTER;
+  if (!c->have_W || !c->have_q || !c->have_r) {
+    fc3dgpu_set_error("fc3dgpu_ctx_features: problem, q/mu or r not set");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  if (int rc = features_impl(c, gap)) return rc;
+  float* Xd = nullptr;
+  CK(cudaMalloc(&Xd, sizeof(float) * FC3DGPU_MLP_FEATURES * (size_t)(c->nc ? c->nc : 1)));
+  k_gather_features<<<grid1d((long long)c->nc * FC3DGPU_MLP_FEATURES), 256, 0, c->stream>>>(c->nc, c->iperm,
+                                                                                           c->feat, Xd);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(X, Xd, sizeof(float) * FC3DGPU_MLP_FEATURES * (size_t)c->nc, cudaMemcpyDeviceToHost,
+                        c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(Xd);
+  CK(e);
+  c->launches++;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_warm_start(fc3dgpu_ctx* c, fc3dgpu_mlp* m, const double* gap, double* out3) {
+  using namespace fc3dgpu;
+  if (!c || !m) return NUMERICS_ERR_NULL_POINTER;
+  if (!c->have_W || !c->have_q || !c->have_r) {
+    fc3dgpu_set_error("fc3dgpu_ctx_warm_start: problem, q/mu or r not set");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (c->nscenes > 0) {
+    fc3dgpu_set_error("fc3dgpu_ctx_warm_start: batched contexts are not supported");
+    return NUMERICS_ERR_NOT_IMPLEMENTED;
+  }
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  if (ensure(&c->prop, &c->prop_cap, (size_t)c->npad * 3) != cudaSuccess ||
+      ensure(&c->rbak, &c->rbak_cap, (size_t)c->npad * 4) != cudaSuccess) {
+    fc3dgpu_set_error("warm start: allocation failed");
+    return NUMERICS_ERR_MEMORY;
+  }
+  double e0 = 0.0, e1 = 0.0;
+  if (int rc = fc3dgpu_ctx_compute_error(c, &e0)) return rc;
+  if (int rc = features_impl(c, gap)) return rc;
+  if (int rc = fc3dgpu_mlp_infer_stream(m, (size_t)c->npad, c->feat, c->prop, s)) return rc;
+  c->launches++;
+  k_take_proposal<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->perm, c->prop, c->mu64, c->r64, c->r32, c->rbak);
+  CK(cudaGetLastError());
+  c->launches++;
+  if (int rc = fc3dgpu_ctx_compute_error(c, &e1)) return rc;
+  const bool take = e1 < e0;  // false for a NaN proposal
+  if (!take) {
+    k_restore_r<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->rbak, c->r64, c->r32);
+    CK(cudaGetLastError());
+    c->launches++;
+    CK(cudaStreamSynchronize(s));
+  }
+  if (out3) {
+    out3[0] = e0;
+    out3[1] = e1;
+    out3[2] = take ? 1.0 : 0.0;
   }
   return 0;
 }

@@ -159,6 +159,19 @@ ABI = {
     "fc3dgpu_ctx_colours": (C.c_int, [C.c_void_p, _I32]),
     "fc3dgpu_ctx_counters": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "fc3dgpu_ctx_set_norm_q": (C.c_int, [C.c_void_p, C.c_double]),
+    "fc3dgpu_mlp_nparams": (C.c_int, []),
+    "fc3dgpu_mlp_create": (C.c_void_p, [C.c_int]),
+    "fc3dgpu_mlp_destroy": (None, [C.c_void_p]),
+    "fc3dgpu_mlp_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_mlp_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_mlp_set_data": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_mlp_train_step": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_float, C.c_void_p,
+                                         C.c_void_p, C.c_int]),
+    "fc3dgpu_mlp_train_step_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_float]),
+    "fc3dgpu_mlp_infer": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_int]),
+    "fc3dgpu_mlp_infer_stream": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_warm_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_compute_error_device": (C.c_int, [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
                                                C.c_void_p]),
