@@ -1265,6 +1265,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
   CK(cudaMemsetAsync(c->status, 0, sizeof(int), s));
   CK(cudaEventRecord(c->ev[0], s));
   int sweeps32 = 0, grid = 0;
+  bool converged32 = false;
   double out[8];
   if (p->precision == 0 && p->max_iter > 0) {
     SweepArgs<float> a;
@@ -1296,6 +1297,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     CK(cudaStreamSynchronize(s));
     sweeps32 = (int)out[0];
     S.incr_error = out[1];
+    converged32 = out[3] == 0.0;
     k_r32_to_r64<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r32, c->rpli32, c->r64, c->rpli64);
     CK(cudaGetLastError());
     c->launches++;
@@ -1318,11 +1320,24 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     a.pli_max = p->pli_max;
     a.ls_max = p->ls_max;
     int g64 = 0;
-    CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
-    CK(launch_sweep_f64(a, lanes, 0, 0, s, &g64));
-    c->launches++;
+    if (converged32 && budget > 0) {
+      // the FP32 iterate met the tolerance in FP32 arithmetic: check it in
+      // FP64 before any FP64 sweep
+      a.max_sweeps = 0;
+      CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
+      CK(launch_sweep_f64(a, lanes, 0, 0, s, &g64));
+      c->launches++;
+      CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      a.max_sweeps = out[3] == 0.0 ? 0 : budget;
+    }
+    if (!(converged32 && a.max_sweeps == 0)) {
+      CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
+      CK(launch_sweep_f64(a, lanes, 0, 0, s, &g64));
+      c->launches++;
+      CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+    }
     if (!grid) grid = g64;
-    CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
   }
   CK(cudaEventRecord(c->ev[2], s));
   int status = 0;

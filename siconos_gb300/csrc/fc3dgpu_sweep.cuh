@@ -777,7 +777,7 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
   const int nwb = blockDim.x >> 5;
   const int gw = blockIdx.x * nwb + (threadIdx.x >> 5), tw = gridDim.x * nwb;
   unsigned epoch = 0;
-  double working = a.user_tol, local_tol = a.local_tol;
+  double working = a.mode == 1 ? a.user_tol : fmax(a.user_tol, a.switch_tol), local_tol = a.local_tol;
   double incr = INFINITY, full = INFINITY, best = INFINITY;
   int sweep = 0, best_sweep = 0;
   bool converged = false;
@@ -868,6 +868,25 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
         best_sweep = sweep;
       } else if (a.stall_window > 0 && sweep - best_sweep >= a.stall_window) {
         stop = true;
+      }
+      // the reference's adaptive convergence test on this precision's
+      // iterate, against max(tol, switch_tol): the FP32 sweeps end as soon
+      // as their full error (FP32 arithmetic, FP64 sums) reaches it
+      if (!stop && incr < working) {
+        if (!full_error_phase(a, 2, epoch, full)) {
+          if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+          return;
+        }
+        const double target = fmax(a.user_tol, a.switch_tol);
+        if (full <= target) {
+          converged = true;
+          stop = true;
+        } else if (full > 0.0 && incr > 0.0) {
+          double nt = (incr / full) * target;
+          const double mint = fmax(target * 1e-6, DBL_EPSILON * 1e-6);
+          if (nt < mint) nt = mint;
+          if (nt < working) working = nt;
+        }
       }
     }
     if (stop) break;

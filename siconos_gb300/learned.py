@@ -211,3 +211,63 @@ def device_features(solver, gap=None) -> np.ndarray:
     if rc != 0:
         raise RuntimeError(f"features failed ({rc}): {sn.last_error()}")
     return X
+
+
+def _timed_solve(solver, **kw):
+    t = time.perf_counter()
+    st = solver.solve(**kw)
+    st["wall_ms"] = 1e3 * (time.perf_counter() - t)
+    return st
+
+
+def evaluate(mlp: WarmStartMLP, dims=(60, 60, 30), seed: int = 424242, mu: float = 0.5, tol: float = 1e-8,
+             max_iter: int = 2000, walk_std: float = 0.01, device: int = 0, **solve_kw) -> dict:
+    """Sweeps and time to `tol` (within `max_iter` sweeps) on a held-out
+    lattice, per warm start:
+      step 0 (fresh scene): zero start, learned start (fallback zero);
+      step 1 (after one velocity random-walk step): zero start, previous-step
+      start, learned start (fallback previous step).
+    The learned rows include the warm start's own time (features,
+    inference, two error evaluations)."""
+    from .device import DeviceSolver
+    from .scene import lattice
+    sc = lattice(*dims, seed=seed, mu=mu)
+    d = DeviceSolver(device)
+    kw = dict(tol=tol, max_iter=max_iter, **solve_kw)
+    out = {"scene": {"dims": list(dims), "seed": seed, "contacts": sc.nc, "blocks": sc.nnzb}, "tol": tol,
+           "max_iter": max_iter}
+    try:
+        d.load(sc)
+        d.solve(tol=tol, max_iter=2)  # warm the kernels and the autotuned launch shape
+        res = {}
+        d.zero_r()
+        res["zero"] = _timed_solve(d, **kw)
+        r0, _ = d.get()
+        d.zero_r()
+        t = time.perf_counter()
+        ws = warm_start(d, mlp, sc.gap)
+        t_ws = 1e3 * (time.perf_counter() - t)
+        st = _timed_solve(d, **kw)
+        st.update(ws, warm_start_ms=t_ws)
+        st["wall_ms"] += t_ws
+        res["learned"] = st
+        out["step0"] = res
+        sc.perturb(seed + 1, walk_std)
+        d.set_q_mu(sc.q, sc.mu)
+        res = {}
+        d.zero_r()
+        res["zero"] = _timed_solve(d, **kw)
+        d.set_r(r0)
+        res["previous"] = _timed_solve(d, **kw)
+        d.set_r(r0)
+        t = time.perf_counter()
+        ws = warm_start(d, mlp, sc.gap)
+        t_ws = 1e3 * (time.perf_counter() - t)
+        st = _timed_solve(d, **kw)
+        st.update(ws, warm_start_ms=t_ws)
+        st["wall_ms"] += t_ws
+        res["learned"] = st
+        out["step1"] = res
+    finally:
+        d.close()
+    return out

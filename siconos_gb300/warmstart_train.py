@@ -1,0 +1,130 @@
+"""Train the learned warm start on solutions the GPU solver generates.
+
+    python -m siconos_gb300.warmstart_train --scenes 2000 --out siconos_gb300/data/warmstart_mlp.npz
+
+Training pairs (features -> reaction) come from the lattice generator with
+dims drawn uniformly in [lo, hi]^3 and mu ~ U(0.1, 0.9) per scene.  Each
+scene gives two solves, both run as one batch per chunk of scenes:
+  step 0  from r = 0 (the previous-reaction features are 0),
+  step 1  after a velocity random-walk step (v0 += N(0, 0.01^2) per degree
+          of freedom, contacts kept), warm-started from step 0's reaction
+          (which becomes the previous-reaction features).
+Solves use the FP32 sweeps + FP64 polish to tol 1e-8 within the sweep
+budget.  Up to `per_scene` contacts per scene and step are kept, so large
+scenes do not dominate.  The network is then trained with Adam on the GPU
+(minibatches of 4096, cosine learning-rate decay) and saved with its
+statistics and training record.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+from .device import DeviceSolver
+from .learned import WarmStartMLP, host_features, init_params, make_stats
+from .scene import lattice
+
+
+def generate(n_scenes: int, seed: int = 1000, lo=(5, 5, 5), hi=(30, 30, 30), per_scene: int = 2048,
+             chunk: int = 128, max_iter: int = 300, walk_std: float = 0.01, device: int = 0, log=None):
+    rng = np.random.default_rng(seed)
+    Xs, Ts = [], []
+    summary = {"scenes": 0, "contacts": 0, "solves": 0, "sweeps": 0, "errors_step0": [], "errors_step1": []}
+    d = DeviceSolver(device)
+    kw = dict(tol=1e-8, max_iter=max_iter)
+    try:
+        for c0 in range(0, n_scenes, chunk):
+            k = min(chunk, n_scenes - c0)
+            scenes = []
+            for j in range(k):
+                dims = [int(v) for v in rng.integers(lo, np.asarray(hi) + 1)]
+                scenes.append(lattice(*dims, seed=seed * 1000003 + c0 + j, mu=float(rng.uniform(0.1, 0.9))))
+            d.load_batch(scenes)
+            o1 = d.solve_batch(**kw)
+            r1, _ = d.get_batch()
+            for sc, r in zip(scenes, r1):
+                X = host_features(sc.nc, sc.rowptr, sc.colidx, sc.blocks, sc.q, sc.mu, None, sc.gap)
+                sel = rng.permutation(sc.nc)[:per_scene]
+                Xs.append(X[sel])
+                Ts.append(r.reshape(-1, 3)[sel].astype(np.float32))
+            for j, sc in enumerate(scenes):
+                sc.perturb(seed * 7919 + c0 + j, walk_std)
+            d.set_q_mu(np.concatenate([sc.q for sc in scenes]), np.concatenate([sc.mu for sc in scenes]))
+            d.set_r(np.concatenate(r1))
+            o2 = d.solve_batch(**kw)
+            r2, _ = d.get_batch()
+            for sc, rp, r in zip(scenes, r1, r2):
+                X = host_features(sc.nc, sc.rowptr, sc.colidx, sc.blocks, sc.q, sc.mu, rp, sc.gap)
+                sel = rng.permutation(sc.nc)[:per_scene]
+                Xs.append(X[sel])
+                Ts.append(r.reshape(-1, 3)[sel].astype(np.float32))
+            summary["scenes"] += k
+            summary["contacts"] += int(sum(sc.nc for sc in scenes))
+            summary["solves"] += 2 * k
+            summary["sweeps"] += int((o1["sweeps32"] + o1["sweeps64"] + o2["sweeps32"] + o2["sweeps64"]).sum())
+            summary["errors_step0"] += [float(e) for e in o1["error"]]
+            summary["errors_step1"] += [float(e) for e in o2["error"]]
+            if log:
+                log({"chunk": c0 // chunk, "scenes": summary["scenes"], "samples": int(sum(len(x) for x in Xs)),
+                     "median_error_step0": float(np.median(o1["error"])),
+                     "median_error_step1": float(np.median(o2["error"]))})
+            del scenes
+    finally:
+        d.close()
+    X = np.concatenate(Xs)
+    T = np.concatenate(Ts)
+    for key in ("errors_step0", "errors_step1"):
+        e = np.asarray(summary.pop(key))
+        summary[key.replace("errors", "median_error")] = float(np.median(e))
+        summary[key.replace("errors", "max_error")] = float(e.max())
+    return X, T, summary
+
+
+def train(X, T, epochs: int = 20, batch: int = 4096, lr: float = 2e-3, wd: float = 1e-4, seed: int = 0,
+          device: int = 0, log=None):
+    rng = np.random.default_rng(seed)
+    val = rng.choice(len(X), max(1, len(X) // 50), replace=False)
+    m = WarmStartMLP(device)
+    m.set_params(init_params(seed), make_stats(X, T))
+    m.set_data(X, T)
+    t = time.perf_counter()
+    hist = m.train(epochs, batch=batch, lr=lr, wd=wd, seed=seed, val_idx=val, log=log)
+    return m, hist, time.perf_counter() - t
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--scenes", type=int, default=2000)
+    ap.add_argument("--seed", type=int, default=1000)
+    ap.add_argument("--lo", type=int, default=5)
+    ap.add_argument("--hi", type=int, default=30)
+    ap.add_argument("--per-scene", type=int, default=2048)
+    ap.add_argument("--chunk", type=int, default=128)
+    ap.add_argument("--max-iter", type=int, default=300)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args(argv)
+
+    def log(row):
+        print(json.dumps(row), flush=True)
+
+    t0 = time.perf_counter()
+    X, T, summary = generate(a.scenes, a.seed, (a.lo,) * 3, (a.hi,) * 3, a.per_scene, a.chunk, a.max_iter, log=log)
+    t_gen = time.perf_counter() - t0
+    m, hist, t_train = train(X, T, a.epochs, a.batch, a.lr, log=log)
+    cfg = dict(vars(a), samples=len(X), generate_s=t_gen, train_s=t_train, **summary)
+    log({"config": cfg, "final": hist[-1]})
+    if a.out:
+        m.save(a.out, config=json.dumps(cfg), history=json.dumps(hist))
+    m.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
