@@ -118,7 +118,8 @@ def main(argv=None):
     X, T, summary = generate(a.scenes, a.seed, (a.lo,) * 3, (a.hi,) * 3, a.per_scene, a.chunk, a.max_iter, log=log)
     t_gen = time.perf_counter() - t0
     m, hist, t_train = train(X, T, a.epochs, a.batch, a.lr, log=log)
-    cfg = dict(vars(a), samples=len(X), generate_s=t_gen, train_s=t_train, **summary)
+    cfg = dict({k: v for k, v in vars(a).items() if k != "out"}, samples=len(X), generate_s=t_gen,
+               train_s=t_train, **summary)
     log({"config": cfg, "final": hist[-1]})
     if a.out:
         m.save(a.out, config=json.dumps(cfg), history=json.dumps(hist))
