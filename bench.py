@@ -211,6 +211,90 @@ def run_reference(args):
     return 0
 
 
+def time_to_tolerance(d, s, tols=(1e-3, 1e-8), budget=(3000, 500)):
+    """Sweeps and device time from r = 0 to each tolerance (within its sweep
+    budget): plain FP64 coloured NSGS, FP32 sweeps + FP64 polish, and the
+    same with the learned warm start (zero start as its fallback)."""
+    from siconos_gb300.learned import WarmStartMLP, warm_start
+    out = []
+    m = WarmStartMLP(0)
+    m.load()
+    try:
+        for tol, mx in zip(tols, budget):
+            row = {"tol": tol, "max_sweeps": mx}
+            for name, kw in (("fp64", dict(precision=1)), ("fp32_fp64_polish", dict(precision=0)),
+                             ("learned_fp32_fp64_polish", dict(precision=0))):
+                d.zero_r()
+                t = time.perf_counter()
+                ws = warm_start(d, m, s.gap) if name.startswith("learned") else None
+                st = d.solve(tol=tol, max_iter=mx, **kw)
+                wall = time.perf_counter() - t
+                row[name] = {"reached": st["info"] == 0, "error": st["error"], "sweeps32": st["sweeps32"],
+                             "sweeps64": st["sweeps64"], "device_ms": st["ms_total"], "wall_ms": 1e3 * wall}
+                if ws is not None:
+                    row[name]["proposal_taken"] = ws["taken"]
+            a, b = row["fp64"], row["fp32_fp64_polish"]
+            if a["reached"] and b["reached"]:
+                row["speedup_fp32_polish_vs_fp64"] = a["wall_ms"] / b["wall_ms"]
+            out.append(row)
+    finally:
+        m.close()
+    return out
+
+
+def batched_c3(count=512, seed=7):
+    """512 independent lattices (dims U[3..20]x[3..20]x[2..10], mu U(0.1, 0.9))
+    in one persistent launch per phase: FP32 throughput over a fixed budget,
+    then FP32 sweeps + FP64 polish to 1e-8 within 1000 sweeps."""
+    from siconos_gb300 import scene as sc
+    from siconos_gb300.device import DeviceSolver
+    t = time.perf_counter()
+    scenes = sc.batch_scenes(count=count, seed=seed)
+    gen_s = time.perf_counter() - t
+    nc = sum(x.nc for x in scenes)
+    d = DeviceSolver(0)
+    try:
+        d.load_batch(scenes)
+        d.solve_batch(tol=1e-8, max_iter=4, fp32_only=1, switch_tol=0.0, stall_window=0)
+        d.zero_r()
+        o = d.solve_batch(tol=1e-8, max_iter=200, fp32_only=1, switch_tol=0.0, stall_window=0)
+        thr = float((o["sweeps32"] * np.array([x.nc for x in scenes])).sum()) / (o["ms"] / 1e3)
+        d.zero_r()
+        o2 = d.solve_batch(tol=1e-8, max_iter=1000)
+    finally:
+        d.close()
+    return {"scenes": count, "contacts": nc, "blocks": int(sum(x.nnzb for x in scenes)),
+            "fp32_200_sweeps": {"device_ms": o["ms"], "contact_sweeps_per_s": thr},
+            "to_1e-8_budget_1000": {"device_ms": o2["ms"], "converged": int((o2["info"] == 0).sum()),
+                                    "max_iter_reached": int((o2["info"] == -20).sum()),
+                                    "mean_sweeps32": float(o2["sweeps32"].mean()),
+                                    "mean_sweeps64": float(o2["sweeps64"].mean()),
+                                    "median_error": float(np.median(o2["error"]))},
+            "generate_s": gen_s}
+
+
+def time_stepping_c5(steps=20):
+    """Consecutive solves of the 80x80x40 lattice (761,600 contacts), q on a
+    random walk, learned warm start with the previous step as fallback, tol
+    1e-3 (the first step starts from zero)."""
+    from siconos_gb300.learned import WarmStartMLP
+    from siconos_gb300.timestep import run_sequence, summarise
+    m = WarmStartMLP(0)
+    m.load()
+    try:
+        run = run_sequence(dims=(80, 80, 40), steps=steps, seed=5, tol=1e-3, max_iter=1500, warm="learned", mlp=m)
+    finally:
+        m.close()
+    out = summarise(run)
+    out["contacts"] = run["scene"]["contacts"]
+    out["blocks"] = run["scene"]["blocks"]
+    later = run["steps"][1:]
+    out["later_steps_mean_sweeps"] = float(np.mean([r["sweeps32"] + r["sweeps64"] for r in later]))
+    out["later_steps_mean_solve_ms"] = float(np.mean([r["solve_ms"] for r in later]))
+    out["q_update_ms_mean"] = float(np.mean([r["q_update_ms"] for r in later]))
+    return out
+
+
 def run_ours(args):
     ws, rank, local = _dist()
     _init_dist(ws, local)
@@ -334,6 +418,16 @@ def run_ours(args):
             "sweep_ms_fp32": sum(fp32_ms) / max(1, sum(fp32_sweeps)),
             "final_error": stats[-1]["error"],
         }
+        if ws == 1 and not args.no_extras:
+            sup = {}
+            for key, fn in (("time_to_tolerance_60x60x30", lambda: time_to_tolerance(d, s)),
+                            ("batched_512_scenes", batched_c3),
+                            ("time_stepping_80x80x40", time_stepping_c5)):
+                try:
+                    sup[key] = fn()
+                except Exception as e:  # a failed extra must not lose the headline line
+                    sup[key] = {"failed": f"{type(e).__name__}: {e}"}
+            line["supplementary"] = sup
         print(json.dumps(line), flush=True)
     d.close()
     if ws > 1:
@@ -350,6 +444,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sweeps", type=int, default=100)
     ap.add_argument("--cpu-sweeps", type=int, default=30)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the time-to-tolerance, batched and time-stepping measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         args.cpu_sweeps = max(1, min(args.cpu_sweeps, 10))
