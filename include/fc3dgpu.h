@@ -187,6 +187,11 @@ int fc3dgpu_ctx_timeline(fc3dgpu_ctx *ctx, int sweep, unsigned long long *out, i
 /* Bulk-copy (TMA) staging of each block's slab range into shared memory
  * in the FP32 sweeps: 1 on (default), 0 off.  Returns the previous value. */
 int fc3dgpu_ctx_staging(fc3dgpu_ctx *ctx, int on);
+/* Synchronisation between the colours of a sweep (one lane per contact):
+ * 1 (default) each block waits only for the blocks whose rows share a W block
+ * with its own, 0 a grid-wide barrier after every colour.  Both give the same
+ * iterates.  Returns the previous setting. */
+int fc3dgpu_ctx_sync(fc3dgpu_ctx *ctx, int neighbourhood);
 /* r = 0 on the device (PLI steps reset), without a host copy. */
 int fc3dgpu_ctx_zero_r(fc3dgpu_ctx *ctx);
 /* The CUDA stream (cudaStream_t) every kernel of this context runs on, for

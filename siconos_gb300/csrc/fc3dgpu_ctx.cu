@@ -486,6 +486,55 @@ __global__ void k_take_proposal(int npad, const int* __restrict__ perm, const fl
   }
 }
 
+struct ColourBounds {
+  int sptr[FC3D_MAX_COLOURS + 1];
+};
+
+// Block that processes slab s in a sweep over `grid` blocks: the colour's
+// slabs are split as block_range does, [s0 + n b / grid, s0 + n (b+1) / grid).
+__device__ __forceinline__ int owner_block(int s, const ColourBounds& cb, int ncol, int grid) {
+  int lo = 0, hi = ncol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (cb.sptr[mid] <= s)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int s0 = cb.sptr[lo], n = cb.sptr[lo + 1] - s0, x = s - s0;
+  int b = (int)(((long long)x * grid) / n);
+  if (b >= grid) b = grid - 1;
+  while (b + 1 < grid && (long long)n * (b + 1) / grid <= x) b++;
+  while (b > 0 && (long long)n * b / grid > x) b--;
+  return b;
+}
+
+// mask[b][b' / 32] bit b' % 32 set when a row of block b and a row of block
+// b' share a W block (both directions).
+__global__ void k_block_adjacency(int nslab, int npad, ColourBounds cb, int ncol, int grid, int words,
+                                  const int* __restrict__ perm, const int* __restrict__ slab_nslot,
+                                  const long long* __restrict__ slab_off, const int* __restrict__ col,
+                                  unsigned* __restrict__ mask) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)nslab * FC3D_SLAB;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(t / FC3D_SLAB), k = (int)(t % FC3D_SLAB);
+    if (perm[(size_t)s * FC3D_SLAB + k] < 0) continue;
+    const int b = owner_block(s, cb, ncol, grid);
+    const int ns = slab_nslot[s];
+    const long long base = slab_off[s];
+    for (int slot = 0; slot < ns; slot++) {
+      const int j = col[(size_t)(base + slot) * FC3D_SLAB + k];
+      if (j < 0 || j >= npad) continue;
+      const int bj = owner_block(j / FC3D_SLAB, cb, ncol, grid);
+      if (bj == b) continue;
+      unsigned* m1 = &mask[(size_t)b * words + bj / 32];
+      unsigned* m2 = &mask[(size_t)bj * words + b / 32];
+      if (!(*(volatile unsigned*)m1 & (1u << (bj % 32)))) atomicOr(m1, 1u << (bj % 32));
+      if (!(*(volatile unsigned*)m2 & (1u << (b % 32)))) atomicOr(m2, 1u << (b % 32));
+    }
+  }
+}
+
 __global__ void k_restore_r(int npad, const double* __restrict__ rbak, double* __restrict__ r64,
                             float* __restrict__ r32) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x)
@@ -648,6 +697,15 @@ struct fc3dgpu_ctx {
   BUF(double, sout64);
   cudaGraphExec_t batch_graph = nullptr;
   fc3dgpu_params batch_graph_params;
+  // neighbourhood synchronisation: block neighbour lists per grid size
+  struct Nbr {
+    int grid = 0;
+    int* ptr = nullptr;
+    int* list = nullptr;
+  } nbrc[2];
+  int nbr_next = 0;
+  BUF(unsigned, nbrmask);
+  int nbr_sync = 1;  // neighbourhood synchronisation on (1, default) or grid barriers (0)
   // learned warm start
   BUF(float, feat);
   BUF(float, prop);
@@ -709,7 +767,7 @@ extern "C" fc3dgpu_ctx* fc3dgpu_ctx_create(int device) {
   fc3dgpu::warm_batch_kernel_f32();
   fc3dgpu::warm_batch_kernel_f64();
   bool ok = ensure(&c->partials, &c->partials_cap, 1024 * 8) == cudaSuccess &&
-            ensure(&c->barrier, &c->barrier_cap, 1024) == cudaSuccess &&
+            ensure(&c->barrier, &c->barrier_cap, FC3D_BARRIER_WORDS) == cudaSuccess &&
             ensure(&c->status, &c->status_cap, 4) == cudaSuccess &&
             ensure(&c->scratch, &c->scratch_cap, 16) == cudaSuccess &&
             ensure(&c->scratch64, &c->scratch64_cap, 16) == cudaSuccess &&
@@ -738,6 +796,11 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (auto& n : c->nbrc) {
+    if (n.ptr) cudaFree(n.ptr);
+    if (n.list) cudaFree(n.list);
+  }
+  if (c->nbrmask) cudaFree(c->nbrmask);
   for (int i = 0; i < 4; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -969,6 +1032,7 @@ static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64
   c->nc = nc;
   c->nnzb = nnzb;
   c->have_W = true;
+  for (auto& n : c->nbrc) n.grid = 0;  // the rows' owners changed
   return 0;
 }
 
@@ -1088,6 +1152,16 @@ __global__ void k_zero_r(int npad, double* __restrict__ r64, float* __restrict__
   }
 }
 
+// Synchronisation between the colours of a sweep (one lane per contact):
+// 1 (default) each block waits only for the blocks it shares W blocks with,
+// 0 every block waits for all.  Returns the previous setting.
+extern "C" int fc3dgpu_ctx_sync(fc3dgpu_ctx* c, int neighbourhood) {
+  if (!c) return -1;
+  const int old = c->nbr_sync;
+  c->nbr_sync = neighbourhood ? 1 : 0;
+  return old;
+}
+
 // Bulk-copy staging of slab ranges in the FP32 sweeps: on (1, default) or
 // off (0).  Returns the previous setting.
 extern "C" int fc3dgpu_ctx_staging(fc3dgpu_ctx* c, int on) {
@@ -1189,6 +1263,58 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.stage_w_bytes = a.stage_c_bytes = a.stage_q_bytes = a.stage_d_bytes = 0;
   for (int k = 0; k < FC3D_MAX_COLOURS; k++) a.ccount[k] = c->ccount[k];
   a.out = c->out;
+  a.nbr_ptr = nullptr;
+  a.nbr = nullptr;
+  a.nbr_grid = 0;
+}
+
+// Neighbour lists of every block for a sweep over `grid` blocks (one lane
+// per contact): built once per layout and grid size.
+template <typename Real>
+static int attach_nbr(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, int grid) {
+  using namespace fc3dgpu;
+  if (!c->nbr_sync || grid <= 0 || c->nscenes > 0 || c->ncol < 2) return 0;
+  fc3dgpu_ctx::Nbr* hit = nullptr;
+  for (auto& n : c->nbrc)
+    if (n.grid == grid) hit = &n;
+  if (!hit) {
+    hit = &c->nbrc[c->nbr_next];
+    c->nbr_next ^= 1;
+    hit->grid = 0;
+    const int words = (grid + 31) / 32;
+    cudaStream_t s = c->stream;
+    CK(ensure(&c->nbrmask, &c->nbrmask_cap, (size_t)grid * words));
+    CK(cudaMemsetAsync(c->nbrmask, 0, sizeof(unsigned) * grid * words, s));
+    ColourBounds cb;
+    for (int k = 0; k <= FC3D_MAX_COLOURS; k++) cb.sptr[k] = c->sptr[k];
+    k_block_adjacency<<<grid1d((long long)c->nslab * FC3D_SLAB), 256, 0, s>>>(
+        c->nslab, c->npad, cb, c->ncol, grid, words, c->perm, c->slab_nslot, c->slab_off, c->col, c->nbrmask);
+    CK(cudaGetLastError());
+    c->launches++;
+    std::vector<unsigned> mask((size_t)grid * words);
+    CK(cudaMemcpyAsync(mask.data(), c->nbrmask, sizeof(unsigned) * mask.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<int> ptr(grid + 1, 0), list;
+    for (int b = 0; b < grid; b++) {
+      for (int b2 = 0; b2 < grid; b2++)
+        if (mask[(size_t)b * words + b2 / 32] & (1u << (b2 % 32))) list.push_back(b2);
+      ptr[b + 1] = (int)list.size();
+    }
+    if (hit->ptr) cudaFree(hit->ptr);
+    if (hit->list) cudaFree(hit->list);
+    hit->ptr = hit->list = nullptr;
+    CK(cudaMalloc(&hit->ptr, sizeof(int) * (grid + 1)));
+    CK(cudaMalloc(&hit->list, sizeof(int) * (list.empty() ? 1 : list.size())));
+    CK(cudaMemcpyAsync(hit->ptr, ptr.data(), sizeof(int) * (grid + 1), cudaMemcpyHostToDevice, s));
+    if (!list.empty())
+      CK(cudaMemcpyAsync(hit->list, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    hit->grid = grid;
+  }
+  a.nbr_ptr = hit->ptr;
+  a.nbr = hit->list;
+  a.nbr_grid = grid;
+  return 0;
 }
 
 // Staging buffer sizes (bytes of W, col, q) for the largest slab range one
@@ -1289,7 +1415,9 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     k_r64_to_r32<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r64, c->r32);
     CK(cudaGetLastError());
     c->launches++;
-    CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
+    if (lanes == 1)
+      if (int rc = attach_nbr<float>(c, a, sweep_grid_f32(1))) return rc;
+    CK(cudaMemsetAsync(c->barrier, 0, FC3D_BARRIER_WORDS * sizeof(unsigned), s));
     CK(launch_sweep_f32(a, lanes, 0, smem, s, &grid));
     c->launches++;
     CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
@@ -1320,11 +1448,13 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     a.pli_max = p->pli_max;
     a.ls_max = p->ls_max;
     int g64 = 0;
+    if (lanes == 1)
+      if (int rc = attach_nbr<double>(c, a, sweep_grid_f64(1))) return rc;
     if (converged32 && budget > 0) {
       // the FP32 iterate met the tolerance in FP32 arithmetic: check it in
       // FP64 before any FP64 sweep
       a.max_sweeps = 0;
-      CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
+      CK(cudaMemsetAsync(c->barrier, 0, FC3D_BARRIER_WORDS * sizeof(unsigned), s));
       CK(launch_sweep_f64(a, lanes, 0, 0, s, &g64));
       c->launches++;
       CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
@@ -1332,7 +1462,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
       a.max_sweeps = out[3] == 0.0 ? 0 : budget;
     }
     if (!(converged32 && a.max_sweeps == 0)) {
-      CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
+      CK(cudaMemsetAsync(c->barrier, 0, FC3D_BARRIER_WORDS * sizeof(unsigned), s));
       CK(launch_sweep_f64(a, lanes, 0, 0, s, &g64));
       c->launches++;
       CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
@@ -1390,7 +1520,7 @@ extern "C" int fc3dgpu_ctx_compute_error(fc3dgpu_ctx* c, double* error) {
   a.trace = nullptr;
   int g = 0;
   double out[8];
-  CK(cudaMemsetAsync(c->barrier, 0, 1024 * sizeof(unsigned), s));
+  CK(cudaMemsetAsync(c->barrier, 0, FC3D_BARRIER_WORDS * sizeof(unsigned), s));
   CK(cudaMemsetAsync(c->status, 0, sizeof(int), s));
   CK(launch_sweep_f64(a, 1, 0, 0, s, &g));
   CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));

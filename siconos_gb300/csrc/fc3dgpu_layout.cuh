@@ -71,11 +71,23 @@ struct SweepArgs {
   // W, col and q of the next colour stream into dynamic shared memory while
   // the block solves the current colour; 0 bytes = off
   unsigned stage_w_bytes, stage_c_bytes, stage_q_bytes, stage_d_bytes;
+  // neighbourhood synchronisation between the colours of a sweep (one lane
+  // per contact only): block b waits only for the blocks whose rows share a
+  // W block with its rows, nbr[nbr_ptr[b] .. nbr_ptr[b + 1]), built for a
+  // grid of nbr_grid blocks; null or another grid = a grid-wide barrier
+  const int* nbr_ptr;
+  const int* nbr;
+  int nbr_grid;
   // outputs (written by block 0, thread 0)
   double* out;                  // [0] sweeps, [1] incr, [2] full error, [3] info, [4] working tol
 };
 
 #define FC3D_PASS_SLABS 16
+
+// Barrier flags: one per block, each on its own 128-byte line so that the
+// blocks polling them do not queue on a few L2 lines.
+#define FC3D_FLAG_STRIDE 32
+#define FC3D_BARRIER_WORDS (1024 * FC3D_FLAG_STRIDE)
 
 // Work list of one block: the contacts of the current pass whose local
 // problem is not the trivial take-off, packed densely.

@@ -67,16 +67,14 @@ __device__ __forceinline__ bool grid_barrier(unsigned* flags, unsigned& epoch, u
   epoch++;
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
-    if (lane == 0) {
-      __threadfence();
-      st_release_u32(&flags[blockIdx.x], epoch);
-    }
+    if (lane == 0) st_release_u32(&flags[blockIdx.x * FC3D_FLAG_STRIDE], epoch);
     unsigned long long n = 0;
     int ok = 1;
     for (;;) {
       bool mine = true;
 #pragma unroll 8
-      for (int b = lane; b < (int)gridDim.x; b += 32) mine &= (ld_relaxed_u32(&flags[b]) >= epoch);
+      for (int b = lane; b < (int)gridDim.x; b += 32)
+        mine &= (ld_relaxed_u32(&flags[b * FC3D_FLAG_STRIDE]) >= epoch);
       if (__all_sync(0xffffffffu, mine)) break;
       if (++n > limit) {
         ok = 0;
@@ -85,7 +83,42 @@ __device__ __forceinline__ bool grid_barrier(unsigned* flags, unsigned& epoch, u
       }
       if (n > 256) __nanosleep(32);
     }
-    __threadfence();
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    if (lane == 0) s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Arrive as the grid barrier does (flag = epoch) but wait only for the
+// listed blocks.  Every block passes the same sequence of barriers, so equal
+// epochs mean the same point of the sweep.  A block can then run at most one
+// colour ahead of any neighbour: rows of colour c read their neighbours'
+// reactions after those neighbours finished colour c - 1 and before they
+// start colour c + 1, exactly as in the grid-synchronised sweep.
+__device__ __forceinline__ bool nbr_barrier(unsigned* flags, unsigned& epoch, const int* nbr, int nn,
+                                            unsigned long long limit, int* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  epoch++;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    if (lane == 0) st_release_u32(&flags[blockIdx.x * FC3D_FLAG_STRIDE], epoch);
+    unsigned long long n = 0;
+    int ok = 1;
+    for (;;) {
+      bool mine = true;
+      for (int k = lane; k < nn; k += 32)
+        mine &= (ld_relaxed_u32(&flags[__ldg(&nbr[k]) * FC3D_FLAG_STRIDE]) >= epoch);
+      if (__all_sync(0xffffffffu, mine)) break;
+      if (++n > limit) {
+        ok = 0;
+        if (lane == 0) atomicOr(status, 1);
+        break;
+      }
+      if (n > 256) __nanosleep(32);
+    }
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
     if (lane == 0) s_ok = ok;
   }
   __syncthreads();
@@ -776,6 +809,7 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
   const int lane = threadIdx.x & 31;
   const int nwb = blockDim.x >> 5;
   const int gw = blockIdx.x * nwb + (threadIdx.x >> 5), tw = gridDim.x * nwb;
+  const bool local_sync = T == 1 && a.nbr_ptr != nullptr && a.nbr_grid == (int)gridDim.x;
   unsigned epoch = 0;
   double working = a.mode == 1 ? a.user_tol : fmax(a.user_tol, a.switch_tol), local_tol = a.local_tol;
   double incr = INFINITY, full = INFINITY, best = INFINITY;
@@ -823,7 +857,11 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
       }
       if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
       if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 6 + 1] = globaltimer_ns();
-      if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) {
+      const bool ok = (local_sync && c < a.ncol - 1)
+                          ? nbr_barrier(a.barrier, epoch, a.nbr + a.nbr_ptr[blockIdx.x],
+                                        a.nbr_ptr[blockIdx.x + 1] - a.nbr_ptr[blockIdx.x], a.spin_limit, a.status)
+                          : grid_barrier(a.barrier, epoch, a.spin_limit, a.status);
+      if (!ok) {
         if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
         return;
       }

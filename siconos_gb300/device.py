@@ -62,6 +62,11 @@ class DeviceSolver:
         n = self.L.fc3dgpu_ctx_timeline(self.ctx, sweep, out.ctypes.data, cap)
         return out[:max(n, 0)]
 
+    def sync(self, neighbourhood: bool) -> bool:
+        """Neighbourhood (True) or grid-wide (False) synchronisation between
+        colours; returns the previous setting."""
+        return bool(self.L.fc3dgpu_ctx_sync(self.ctx, int(neighbourhood)))
+
     def staging(self, on: bool) -> bool:
         return bool(self.L.fc3dgpu_ctx_staging(self.ctx, int(on)))
 

@@ -177,6 +177,7 @@ ABI = {
                                                C.c_void_p]),
     "fc3dgpu_ctx_zero_r": (C.c_int, [C.c_void_p]),
     "fc3dgpu_ctx_staging": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_ctx_sync": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_timeline": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "fc3dgpu_ctx_launches": (C.c_ulonglong, [C.c_void_p]),

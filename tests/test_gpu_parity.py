@@ -180,3 +180,28 @@ def test_fp32_staged_equals_unstaged(gpu):
     assert s1["status"] == 0 and s2["status"] == 0
     assert np.linalg.norm(r1 - r2) <= 1e-5 * np.linalg.norm(r2)
     assert abs(s1["error"] - s2["error"]) <= 1e-4 * s2["error"]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_neighbourhood_sync_equals_grid_barriers(gpu, precision):
+    """Waiting only for the blocks that share W blocks gives the iterates of
+    grid-wide barriers bit for bit (FP64 and FP32 sweeps)."""
+    from siconos_gb300 import scene
+    s = scene.lattice(24, 24, 12, seed=6)
+    gpu.load(s)
+    kw = dict(tol=1e-8, max_iter=25, lanes=1, switch_tol=0.0, stall_window=0)
+    if precision == 0:
+        kw["fp32_only"] = 1
+    else:
+        kw["precision"] = 1
+    out = []
+    for on in (True, False):
+        gpu.sync(on)
+        gpu.zero_r()
+        st = gpu.solve(**kw)
+        out.append((gpu.get()[0], st))
+    gpu.sync(True)
+    (r1, s1), (r2, s2) = out
+    assert s1["status"] == 0 and s2["status"] == 0
+    assert (r1 == r2).all()
+    assert s1["error"] == s2["error"]
