@@ -40,8 +40,14 @@ extern "C" {
 #define FC3DGPU_IPARAM_PRECISION 23   /* in: 0 FP32 sweeps + FP64 polish (default), 1 FP64 sweeps only */
 #define FC3DGPU_IPARAM_LANES 24       /* in: lanes per contact 1, 2, 4, 8; 0 = autotune (default) */
 #define FC3DGPU_IPARAM_WARMSTART 25   /* in: 0 = reaction on entry (default), 1 = learned proposal */
-#define FC3DGPU_IPARAM_COLOURING 26   /* in: 0 = hash priority (default), 1 = largest degree first */
+#define FC3DGPU_IPARAM_COLOURING 26   /* in: colouring kind, see FC3DGPU_COLOURING_DEFAULT */
 #define FC3DGPU_IPARAM_SWEEPS_FP32 27 /* out: FP32 sweeps done */
+/* Colouring kind: low byte 0 = hash priority, 1 = largest degree first;
+ * FC3DGPU_COLOUR_PASSES(n) adds n iterated-greedy recolouring passes (the
+ * classes revisited in reverse order), which shrink the small last colours:
+ * on the 60x60x30 lattice 10 colours become 8. */
+#define FC3DGPU_COLOUR_PASSES(n) ((n) << 8)
+#define FC3DGPU_COLOURING_DEFAULT FC3DGPU_COLOUR_PASSES(4)
 #define FC3DGPU_IPARAM_SWEEPS_FP64 28 /* out: FP64 sweeps done */
 #define FC3DGPU_IPARAM_COLOURS 29     /* out: number of colours */
 #define FC3DGPU_DPARAM_SWITCH_TOL 23  /* in: FP32 -> FP64 switch on the incremental error (default 1e-6) */

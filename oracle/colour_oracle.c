@@ -72,25 +72,9 @@ static int cmp_prio(const void *a, const void *b) {
   return (x > y) - (x < y);
 }
 
-/* Colours in colour[nc]; returns the number of colours.  Degree for kind 1
- * counts distinct conflicting contacts. */
-int oracle_colour_greedy(int nc, const int64_t *rowptr, const int64_t *colidx, int kind, int32_t *colour) {
-  int64_t *gp;
-  int32_t *ga;
-  conflict_graph(nc, rowptr, colidx, &gp, &ga);
-  uint32_t *key = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nc ? nc : 1));
-  int32_t *ord = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc ? nc : 1));
-  /* distinct-neighbour degree: W's structure may list (i,j) and (j,i) */
-  int32_t *mark = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc ? nc : 1));
-  for (int i = 0; i < nc; i++) mark[i] = -1;
+static int greedy_in_key_order(int nc, const int64_t *gp, const int32_t *ga, uint32_t *key, int32_t *ord,
+                               int32_t *colour) {
   for (int i = 0; i < nc; i++) {
-    uint32_t d = 0;
-    for (int64_t k = gp[i]; k < gp[i + 1]; k++)
-      if (mark[ga[k]] != i) {
-        mark[ga[k]] = i;
-        d++;
-      }
-    key[i] = oracle_colour_priority((uint32_t)i, kind, d);
     ord[i] = i;
     colour[i] = -1;
   }
@@ -109,6 +93,40 @@ int oracle_colour_greedy(int nc, const int64_t *rowptr, const int64_t *colidx, i
     while (c < 1024 && used[c]) c++;
     colour[i] = c;
     if (c + 1 > ncol) ncol = c + 1;
+  }
+  return ncol;
+}
+
+/* Colours in colour[nc]; returns the number of colours.  Degree for kind 1
+ * counts distinct conflicting contacts.  kind >> 8 = number of iterated
+ * greedy passes (Culberson): recolour greedily with the current classes
+ * visited as blocks in reverse order (highest colour first), the kind-0
+ * hash (top byte dropped) ordering a class's members. */
+int oracle_colour_greedy(int nc, const int64_t *rowptr, const int64_t *colidx, int kind, int32_t *colour) {
+  const int passes = (kind >> 8) & 0xff;
+  kind &= 0xff;
+  int64_t *gp;
+  int32_t *ga;
+  conflict_graph(nc, rowptr, colidx, &gp, &ga);
+  uint32_t *key = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nc ? nc : 1));
+  int32_t *ord = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc ? nc : 1));
+  /* distinct-neighbour degree: W's structure may list (i,j) and (j,i) */
+  int32_t *mark = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc ? nc : 1));
+  for (int i = 0; i < nc; i++) mark[i] = -1;
+  for (int i = 0; i < nc; i++) {
+    uint32_t d = 0;
+    for (int64_t k = gp[i]; k < gp[i + 1]; k++)
+      if (mark[ga[k]] != i) {
+        mark[ga[k]] = i;
+        d++;
+      }
+    key[i] = oracle_colour_priority((uint32_t)i, kind, d);
+  }
+  int ncol = greedy_in_key_order(nc, gp, ga, key, ord, colour);
+  for (int pass = 0; pass < passes; pass++) {
+    for (int i = 0; i < nc; i++)
+      key[i] = ((uint32_t)colour[i] << 24) | (oracle_colour_priority((uint32_t)i, 0, 0) >> 8);
+    ncol = greedy_in_key_order(nc, gp, ga, key, ord, colour);
   }
   free(key);
   free(ord);

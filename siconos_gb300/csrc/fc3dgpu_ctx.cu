@@ -85,6 +85,20 @@ __global__ void k_priority(int nc, const int* __restrict__ gptr, const int* __re
   }
 }
 
+// Iterated greedy (Culberson): recolour with the current colour classes
+// visited as blocks in reverse order (highest colour first; hash inside a
+// class).  Members of a class are independent, so greedy over whole classes
+// never needs more colours than there are classes, and the small last
+// classes tend to dissolve into the others.
+__global__ void k_recolour_key(int nc, const int* __restrict__ grp, const int* __restrict__ group_off,
+                               uint32_t* __restrict__ key, int* __restrict__ colour) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int local = grp ? i - group_off[grp[i]] : i;
+    key[i] = ((uint32_t)colour[i] << 24) | (colour_priority((uint32_t)local, 0, 0) >> 8);
+    colour[i] = -1;
+  }
+}
+
 __global__ void k_jp_round(int nc, const int* __restrict__ gptr, const int* __restrict__ adj,
                            const uint32_t* __restrict__ key, int* colour, int* remaining, int* overflow) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
@@ -855,30 +869,38 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, const
   CK(ensure(&c->adj, &c->adj_cap, (size_t)(nadj ? nadj : 1)));
   CK(cudaMemcpyAsync(c->cursor, c->gptr, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s));
   k_adjacency<<<grid1d(nc), 256, 0, s>>>(nc, c->rowptr, c->colidx, c->cursor, c->adj);
+  const int passes = (kind >> 8) & 0xff;
+  kind &= 0xff;
   k_priority<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, kind, c->key, c->colour, grp, group_off);
-  int rounds = 0;
-  for (;;) {
-    CK(cudaMemsetAsync(c->scratch, 0, 2 * sizeof(int), s));
-    k_jp_round<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, c->key, c->colour, c->scratch, c->scratch + 1);
-    int h[2];
-    CK(cudaMemcpyAsync(h, c->scratch, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  int ncol = 0;
+  for (int pass = 0; pass <= passes; pass++) {
+    if (pass > 0)
+      k_recolour_key<<<grid1d(nc), 256, 0, s>>>(nc, grp, group_off, c->key, c->colour);
+    int rounds = 0;
+    for (;;) {
+      CK(cudaMemsetAsync(c->scratch, 0, 2 * sizeof(int), s));
+      k_jp_round<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, c->key, c->colour, c->scratch, c->scratch + 1);
+      int h[2];
+      CK(cudaMemcpyAsync(h, c->scratch, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (h[1]) {
+        fc3dgpu_set_error("colouring needs more than %d colours", FC3D_MAX_COLOURS);
+        return NUMERICS_ERR_INVALID_ARGUMENT;
+      }
+      if (h[0] == 0) break;
+      if (++rounds > nc + 1) {
+        fc3dgpu_set_error("colouring did not finish");
+        return NUMERICS_ERR_UNKNOWN;
+      }
+    }
+    CK(cudaMemsetAsync(c->scratch + 2, 0xff, sizeof(int), s));
+    k_max_colour<<<grid1d(nc), 256, 0, s>>>(nc, c->colour, c->scratch + 2);
+    int mx = -1;
+    CK(cudaMemcpyAsync(&mx, c->scratch + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    if (h[1]) {
-      fc3dgpu_set_error("colouring needs more than %d colours", FC3D_MAX_COLOURS);
-      return NUMERICS_ERR_INVALID_ARGUMENT;
-    }
-    if (h[0] == 0) break;
-    if (++rounds > nc + 1) {
-      fc3dgpu_set_error("colouring did not finish");
-      return NUMERICS_ERR_UNKNOWN;
-    }
+    ncol = mx + 1;
   }
-  CK(cudaMemsetAsync(c->scratch + 2, 0xff, sizeof(int), s));
-  k_max_colour<<<grid1d(nc), 256, 0, s>>>(nc, c->colour, c->scratch + 2);
-  int mx = -1;
-  CK(cudaMemcpyAsync(&mx, c->scratch + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  return mx + 1;
+  return ncol;
 }
 
 static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx, const double* blocks,

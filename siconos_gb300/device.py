@@ -21,7 +21,7 @@ class DeviceSolver:
         if rc != 0:
             raise RuntimeError(f"{what} failed ({rc}): {sn.last_error()}")
 
-    def set_W(self, nc, rowptr, colidx, blocks, colouring: int = 0):
+    def set_W(self, nc, rowptr, colidx, blocks, colouring: int = sn.FC3DGPU_COLOURING_DEFAULT):
         self._check(self.L.fc3dgpu_ctx_set_W(self.ctx, nc, np.ascontiguousarray(rowptr, np.int64),
                                              np.ascontiguousarray(colidx, np.int64),
                                              np.ascontiguousarray(blocks, np.float64).reshape(-1), colouring),
@@ -35,7 +35,7 @@ class DeviceSolver:
     def set_r(self, r):
         self._check(self.L.fc3dgpu_ctx_set_r(self.ctx, np.ascontiguousarray(r, np.float64)), "set_r")
 
-    def load(self, scene, colouring: int = 0, r0=None):
+    def load(self, scene, colouring: int = sn.FC3DGPU_COLOURING_DEFAULT, r0=None):
         self.set_W(scene.nc, scene.rowptr, scene.colidx, scene.blocks, colouring)
         self.set_q_mu(scene.q, scene.mu)
         self.set_r(np.zeros(3 * scene.nc) if r0 is None else r0)
@@ -71,7 +71,7 @@ class DeviceSolver:
         return bool(self.L.fc3dgpu_ctx_staging(self.ctx, int(on)))
 
     # ---- batched problems -------------------------------------------------
-    def load_batch(self, scenes, colouring: int = 0):
+    def load_batch(self, scenes, colouring: int = sn.FC3DGPU_COLOURING_DEFAULT):
         """Upload independent problems (objects with nc, rowptr, colidx,
         blocks, q, mu) as one batch; r starts at zero."""
         ncs = np.array([sc.nc for sc in scenes], np.int32)

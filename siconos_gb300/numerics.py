@@ -38,6 +38,7 @@ SICONOS_DPARAM_RESIDU = 1
 FC3DGPU_IPARAM_PRECISION = 23
 FC3DGPU_IPARAM_LANES = 24
 FC3DGPU_IPARAM_WARMSTART = 25
+FC3DGPU_COLOURING_DEFAULT = 4 << 8  # hash priority + 4 recolouring passes
 FC3DGPU_IPARAM_COLOURING = 26
 FC3DGPU_IPARAM_SWEEPS_FP32 = 27
 FC3DGPU_IPARAM_SWEEPS_FP64 = 28

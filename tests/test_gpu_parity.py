@@ -23,7 +23,7 @@ def _colour_order(col):
 
 
 @pytest.mark.parametrize("case", FIXTURE_CASES + LATTICE_CASES)
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 4 << 8, 1 | (2 << 8)])
 def test_device_colouring_equals_host(gpu, case, kind):
     import siconos_gb300.numerics as sn
     P, _ = load_case(case)
