@@ -184,11 +184,12 @@ int fc3dgpu_ctx_colours(fc3dgpu_ctx *ctx, int32_t *colour);
  * units.  enable != 0 keeps counting in later solves.  out8 may be NULL. */
 int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out8);
 /* Phase timeline: in the next solves, record for sweep `sweep` (1-based),
- * per colour and block, out[(colour*grid + block)*6 + {0..5}] = globaltimer
+ * per colour and block, out[(colour*grid + block)*8 + {0..5}] = globaltimer
  * (ns) at the phase start, at the end of the block's work, after its
  * row-product pass, its number of local solves, and (staged sweeps) after the
- * staging wait and after the first slab round; copies the last record into
- * out (cap entries) and returns how many were copied.  sweep 0 stops. */
+ * staging wait and after the first slab round (entries 6, 7 spare); copies
+ * the last record into out (cap entries) and returns how many were copied.
+ * sweep 0 stops. */
 int fc3dgpu_ctx_timeline(fc3dgpu_ctx *ctx, int sweep, unsigned long long *out, int cap);
 /* Bulk-copy (TMA) staging of each block's slab range into shared memory
  * in the FP32 sweeps: 1 on (default), 0 off.  Returns the previous value. */

@@ -1567,14 +1567,15 @@ extern "C" int fc3dgpu_ctx_counters(fc3dgpu_ctx* c, int enable, unsigned long lo
 }
 
 // Phase timeline of one sweep of the next solves: for colour c and block b,
-// out[(c*grid + b)*6 + {0..5}] = globaltimer (ns) at the phase start, at the
+// out[(c*grid + b)*8 + {0..5}] = globaltimer (ns) at the phase start, at the
 // end of the block's work, after its row-product pass (0 when it had no
 // slabs), its number of local solves, and (staged sweeps) after the staging
-// wait and after the first slab round.  sweep = 0 switches it off.
+// wait and after the first slab round; entries 6 and 7 are spare (0).
+// sweep = 0 switches it off.
 extern "C" int fc3dgpu_ctx_timeline(fc3dgpu_ctx* c, int sweep, unsigned long long* out, int cap) {
   if (!c) return -1;
   CK(cudaSetDevice(c->device));
-  const size_t need = (size_t)FC3D_MAX_COLOURS * 1024 * 6;
+  const size_t need = (size_t)FC3D_MAX_COLOURS * 1024 * FC3D_TL_STRIDE;
   CK(ensure(&c->timeline, &c->timeline_cap, need));
   int n = 0;
   if (out && c->timeline_sweep > 0) {

@@ -87,6 +87,9 @@ struct SweepArgs {
 // Barrier flags: one per block, each on its own 128-byte line so that the
 // blocks polling them do not queue on a few L2 lines.
 #define FC3D_FLAG_STRIDE 32
+
+// Phase timeline entries per (colour, block)
+#define FC3D_TL_STRIDE 8
 #define FC3D_BARRIER_WORDS (1024 * FC3D_FLAG_STRIDE)
 
 // Work list of one block: the contacts of the current pass whose local

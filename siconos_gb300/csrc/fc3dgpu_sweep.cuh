@@ -494,16 +494,18 @@ __device__ __forceinline__ void process_range_compact(const SweepArgs<Real>& a, 
 // Issue the bulk copies of W, col and q for slabs [lo, hi) into the
 // staging buffers (one thread).  The caller made sure the previous
 // contents were consumed (block barrier + proxy fence).
+// Slot range [o0, o0 + slots) of the slab range [lo, hi).
+template <typename Real>
+__device__ __forceinline__ void range_slots(const SweepArgs<Real>& a, int lo, int hi, long long& o0,
+                                            long long& slots) {
+  o0 = a.slab_off[lo];
+  slots = (hi < a.nslab ? a.slab_off[hi] : a.slab_off[hi - 1] + a.slab_nslot[hi - 1]) - o0;
+}
+
 template <typename Real>
 __device__ __forceinline__ void stage_issue(const SweepArgs<Real>& a, int lo, int hi, unsigned char* stage,
-                                            unsigned long long* bar) {
-  const long long o0 = a.slab_off[lo], o1 = hi < a.nslab ? a.slab_off[hi] : (long long)-1;
-  long long slots = 0;
-  if (o1 >= 0) {
-    slots = o1 - o0;
-  } else {
-    slots = a.slab_off[hi - 1] + a.slab_nslot[hi - 1] - o0;
-  }
+                                            unsigned long long* bar, long long o0 = -1, long long slots = 0) {
+  if (o0 < 0) range_slots(a, lo, hi, o0, slots);
   const unsigned wb = (unsigned)(slots * 9 * FC3D_SLAB * sizeof(Real));
   const unsigned cb = (unsigned)(slots * FC3D_SLAB * sizeof(int));
   const unsigned qb = (unsigned)((hi - lo) * 3 * FC3D_SLAB * sizeof(Real));
@@ -608,6 +610,11 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
       }
     }
     const long long o0 = a.slab_off[lo];
+    // the last thread stages the next colour (it rarely has a local solve,
+    // so the copy's set-up does not delay one); its slot range is read now
+    const bool issuer = threadIdx.x == blockDim.x - 1;
+    long long n_o0 = -1, n_slots = 0;
+    if (issuer && nhi > nlo) range_slots(a, nlo, nhi, n_o0, n_slots);
     if (pending) {
       if (!mbar_wait_bounded(bar, parity, a.spin_limit, a.status)) return false;
       parity ^= 1u;
@@ -697,9 +704,9 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
     }
     __syncthreads();
     // every input of this range copied out: stage the next colour's range
-    if (threadIdx.x == 0 && nhi > nlo) {
+    if (issuer && nhi > nlo) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      stage_issue(a, nlo, nhi, stage, bar);
+      stage_issue(a, nlo, nhi, stage, bar, n_o0, n_slots);
     }
     if (nhi > nlo) pending = true;
     if (tl && threadIdx.x == 0) {
@@ -822,9 +829,9 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
       const int s0 = a.sptr[c], nunits = (a.sptr[c + 1] - s0) * T;
       const bool tl = a.timeline && sweep == a.timeline_sweep && threadIdx.x == 0;
       if (tl) {
-        unsigned long long* e = a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6;
+        unsigned long long* e = a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * FC3D_TL_STRIDE;
         e[0] = globaltimer_ns();
-        e[2] = e[3] = e[4] = e[5] = 0;
+        e[2] = e[3] = e[4] = e[5] = e[6] = e[7] = 0;
       }
       if (can_stage && staged) {
         // the staged work list lives in dynamic shared memory after the
@@ -833,13 +840,13 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
             stage + ((a.stage_w_bytes + a.stage_c_bytes + a.stage_q_bytes + a.stage_d_bytes / 9 * 12 + 15) & ~15u));
         if (!process_colour_staged<Real>(a, c, (Real)local_tol, acc[0], acc[1], wks, stage, &stage_bar, parity,
                                          pending,
-                                         tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6 + 2 : nullptr))
+                                         tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * FC3D_TL_STRIDE + 2 : nullptr))
           return;
       } else if (T == 1) {
         int lo, hi;
         block_range(s0, a.sptr[c + 1], lo, hi);
         process_range_compact<Real>(a, lo, hi, (Real)local_tol, acc[0], acc[1], wk,
-                                    tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * 6 + 2 : nullptr);
+                                    tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * FC3D_TL_STRIDE + 2 : nullptr);
       } else {
         for (int u = gw; u < nunits; u += tw) {
           const long long t0 = a.counters ? clock64() : 0;
@@ -856,7 +863,7 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
         }
       }
       if (c == a.ncol - 1) block_sum<2>(acc, a.partials + blockIdx.x * 8);
-      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * 6 + 1] = globaltimer_ns();
+      if (tl) a.timeline[((size_t)c * gridDim.x + blockIdx.x) * FC3D_TL_STRIDE + 1] = globaltimer_ns();
       const bool ok = (local_sync && c < a.ncol - 1)
                           ? nbr_barrier(a.barrier, epoch, a.nbr + a.nbr_ptr[blockIdx.x],
                                         a.nbr_ptr[blockIdx.x + 1] - a.nbr_ptr[blockIdx.x], a.spin_limit, a.status)
