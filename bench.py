@@ -274,15 +274,17 @@ def batched_c3(count=512, seed=7):
 
 
 def time_stepping_c5(steps=20):
-    """Consecutive solves of the 80x80x40 lattice (761,600 contacts), q on a
-    random walk, learned warm start with the previous step as fallback, tol
-    1e-3 (the first step starts from zero)."""
+    """Consecutive solves of the 80x80x40 lattice (761,600 contacts), W and q
+    assembled on the device, q on a device random walk, learned warm start
+    with the previous step as fallback, tol 1e-3 (the first step starts from
+    zero)."""
     from siconos_gb300.learned import WarmStartMLP
     from siconos_gb300.timestep import run_sequence, summarise
     m = WarmStartMLP(0)
     m.load()
     try:
-        run = run_sequence(dims=(80, 80, 40), steps=steps, seed=5, tol=1e-3, max_iter=1500, warm="learned", mlp=m)
+        run = run_sequence(dims=(80, 80, 40), steps=steps, seed=5, tol=1e-3, max_iter=1500, warm="learned", mlp=m,
+                           assembly="device")
     finally:
         m.close()
     out = summarise(run)

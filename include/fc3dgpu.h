@@ -208,6 +208,39 @@ void *fc3dgpu_ctx_stream(fc3dgpu_ctx *ctx);
 unsigned long long fc3dgpu_ctx_launches(fc3dgpu_ctx *ctx);
 /* Norm of q used by the relative error (default: computed from q). */
 int fc3dgpu_ctx_set_norm_q(fc3dgpu_ctx *ctx, double norm_q);
+/* Problem sizes of the context: contacts, 3x3 blocks of W, colours. */
+int fc3dgpu_ctx_sizes(fc3dgpu_ctx *ctx, int *nc, long long *nnzb, int *ncolours);
+/* W as the context holds it, block-CSR in contact order (sizes from
+ * fc3dgpu_ctx_sizes; any pointer may be NULL). */
+int fc3dgpu_ctx_get_W(fc3dgpu_ctx *ctx, int64_t *rowptr, int64_t *colidx, double *blocks);
+
+/* ---- Assembly of W and q on the device ---------------------------------
+ * What the reference's mechanics layer does on the host before calling
+ * fc3d_driver (the Delassus matrix W = H M^-1 H^T of the one-step problem and
+ * q = H v_free; OSNSMatrix / BlockCSRMatrix fill in Siconos' kernel), here for
+ * rigid bodies with a scalar mass and an isotropic inertia.  Contact k joins
+ * body bodyA[k] (-1: a fixed obstacle) and body bodyB[k]; frame[9k..9k+8]
+ * holds its rows n, t1, t2 and point[3k..3k+2] its point; H of contact k and
+ * body b is s R [I | -[d]x] with d = point - body position, s = +1 for body B
+ * and -1 for body A.  W's block structure (contacts sharing a body, columns
+ * increasing) and its FP64 blocks are built on the device, then coloured and
+ * laid out as fc3dgpu_ctx_set_W does.  Host arrays in, nothing returned to the
+ * host. */
+int fc3dgpu_ctx_set_contacts(fc3dgpu_ctx *ctx, int nbodies, int ncontacts, const int32_t *bodyA, const int32_t *bodyB,
+                             const double *frame, const double *point, const double *body_pos,
+                             const double *body_mass, const double *body_inertia, int colour_kind);
+/* Friction coefficients of the contacts (host array). */
+int fc3dgpu_ctx_set_mu(fc3dgpu_ctx *ctx, const double *mu);
+/* Body velocities (host, 6 per body: linear then angular) and the time step:
+ * q = H (v + h g), g = -9.81 e_z, formed on the device. */
+int fc3dgpu_ctx_set_velocities(fc3dgpu_ctx *ctx, const double *vel, double h);
+/* One random-walk step of the body velocities on the device, v += std N(0, 1)
+ * per degree of freedom (normals from a counter-based hash of seed and index),
+ * then q re-formed: a time step without any host-device traffic but q's norm. */
+int fc3dgpu_ctx_random_walk(fc3dgpu_ctx *ctx, uint64_t seed, double std);
+/* The context's q (contact order, host array of 3 nc) and body velocities. */
+int fc3dgpu_ctx_get_q(fc3dgpu_ctx *ctx, double *q);
+int fc3dgpu_ctx_get_velocities(fc3dgpu_ctx *ctx, double *vel);
 
 /* ---- Error evaluation without allocation --------------------------------
  * No counterpart in the reference (whose fc3d_compute_error,

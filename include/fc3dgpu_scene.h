@@ -46,6 +46,13 @@ int fc3dgpu_lattice_fill_q(const fc3dgpu_lattice *L, double h, double *q);
  * radius) and contact bodies (A = -1 for the ground; B > A). */
 int fc3dgpu_lattice_fill_geometry(const fc3dgpu_lattice *L, double *gap, int32_t *bodyA, int32_t *bodyB);
 
+/* Contact geometry for an assembly of W and q elsewhere: frames (rows n, t1,
+ * t2; 9 per contact), contact points (3 per contact), body centres (3 per
+ * body), masses, isotropic inertias and velocities (6 per body).  Any
+ * pointer may be NULL. */
+int fc3dgpu_lattice_fill_contacts(const fc3dgpu_lattice *L, double *frame, double *point, double *body_pos,
+                                  double *body_mass, double *body_inertia, double *vel);
+
 /* Random walk of the body velocities: v += N(0, std^2) per degree of
  * freedom, from its own stream seeded by seed. */
 int fc3dgpu_lattice_perturb_velocities(fc3dgpu_lattice *L, uint64_t seed, double std);

@@ -332,6 +332,20 @@ int fc3dgpu_lattice_fill_geometry(const fc3dgpu_lattice *L, double *gap, int32_t
   return 0;
 }
 
+int fc3dgpu_lattice_fill_contacts(const fc3dgpu_lattice *L, double *frame, double *point, double *body_pos,
+                                  double *body_mass, double *body_inertia, double *vel) {
+  if (!L) return -1;
+  if (frame) memcpy(frame, L->frame, sizeof(double) * 9 * (size_t)L->nc);
+  if (point) memcpy(point, L->cpt, sizeof(double) * 3 * (size_t)L->nc);
+  if (body_pos) memcpy(body_pos, L->pos, sizeof(double) * 3 * (size_t)L->nb);
+  if (vel) memcpy(vel, L->vel, sizeof(double) * 6 * (size_t)L->nb);
+  for (int b = 0; b < L->nb; b++) {
+    if (body_mass) body_mass[b] = MASS;
+    if (body_inertia) body_inertia[b] = INERTIA;
+  }
+  return 0;
+}
+
 int fc3dgpu_lattice_perturb_velocities(fc3dgpu_lattice *L, uint64_t seed, double std) {
   if (!L) return -1;
   NormalStream ns = {seed * 2 + 0x5151ULL, 0, 0.0};

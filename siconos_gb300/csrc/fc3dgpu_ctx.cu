@@ -720,6 +720,23 @@ struct fc3dgpu_ctx {
   int nbr_next = 0;
   BUF(unsigned, nbrmask);
   int nbr_sync = 1;  // neighbourhood synchronisation on (1, default) or grid barriers (0)
+  // device assembly of W and q from rigid-body contacts
+  int nb = 0;
+  double step_h = 0.0;
+  bool have_contacts = false, have_mu = false, have_vel = false;
+  BUF(int, cbA);
+  BUF(int, cbB);
+  BUF(double, cframe);
+  BUF(double, cpoint);
+  BUF(double, bpos);
+  BUF(double, bmass);
+  BUF(double, binert);
+  BUF(double, bvel);
+  BUF(int, bdeg);
+  BUF(long long, bptr);
+  BUF(int, blist);
+  BUF(int, crowlen);
+  BUF(double, qsum);
   // learned warm start
   BUF(float, feat);
   BUF(float, prop);
@@ -806,7 +823,8 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->u64, c->partials, c->barrier, c->status, c->scratch, c->scratch64, c->out, c->trace,
                   c->counters, c->timeline, c->scene_off, c->grp, c->scounts, c->snslab, c->sncol, c->sbase,
                   c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64, c->feat,
-                  c->prop, c->rbak, c->gapo};
+                  c->prop, c->rbak, c->gapo, c->cbA, c->cbB, c->cframe, c->cpoint, c->bpos, c->bmass,
+                  c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum};
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -903,6 +921,8 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, const
   return ncol;
 }
 
+static int build_layout(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, int nscenes, const int* scene_nc);
+
 static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx, const double* blocks,
                       int kind, int nscenes, const int* scene_nc) {
   using namespace fc3dgpu;
@@ -922,12 +942,22 @@ static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64
     if (v) return v;
   }
   c->have_W = c->have_q = c->have_r = false;
+  c->have_contacts = c->have_vel = c->have_mu = false;  // W no longer comes from contact geometry
   CK(ensure(&c->rowptr, &c->rowptr_cap, (size_t)nc + 1));
   CK(ensure(&c->colidx, &c->colidx_cap, (size_t)nnzb));
   CK(ensure(&c->blocks, &c->blocks_cap, (size_t)nnzb * 9));
   CK(cudaMemcpyAsync(c->rowptr, rowptr, sizeof(long long) * (nc + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->colidx, colidx, sizeof(long long) * nnzb, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->blocks, blocks, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+  return build_layout(c, nc, nnzb, kind, nscenes, scene_nc);
+}
+
+// Colouring, permutation and slab layout of the block-CSR W already in
+// c->rowptr, c->colidx, c->blocks (original contact order).
+static int build_layout(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, int nscenes, const int* scene_nc) {
+  using namespace fc3dgpu;
+  cudaStream_t s = c->stream;
+  c->have_W = c->have_q = c->have_r = false;
   c->nscenes = nscenes;
   const int* d_grp = nullptr;
   if (nscenes > 0) {
@@ -1854,5 +1884,378 @@ extern "C" int fc3dgpu_ctx_warm_start(fc3dgpu_ctx* c, fc3dgpu_mlp* m, const doub
     out3[1] = e1;
     out3[2] = take ? 1.0 : 0.0;
   }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Device assembly of W = H M^-1 H^T and q = H (v + h g) (include/fc3dgpu.h)
+// ---------------------------------------------------------------------------
+namespace fc3dgpu {
+
+__global__ void k_body_degree(int nc, const int* __restrict__ A, const int* __restrict__ B, int* __restrict__ deg) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    if (A[c] >= 0) atomicAdd(&deg[A[c]], 1);
+    atomicAdd(&deg[B[c]], 1);
+  }
+}
+
+__global__ void k_body_fill(int nc, const int* __restrict__ A, const int* __restrict__ B,
+                            const long long* __restrict__ bptr, int* __restrict__ cur, int* __restrict__ blist) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    if (A[c] >= 0) blist[bptr[A[c]] + atomicAdd(&cur[A[c]], 1)] = c;
+    blist[bptr[B[c]] + atomicAdd(&cur[B[c]], 1)] = c;
+  }
+}
+
+// each body's incident contacts in increasing order (lists are short)
+__global__ void k_body_sort(int nb, const long long* __restrict__ bptr, int* __restrict__ blist) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+    const long long p0 = bptr[b], p1 = bptr[b + 1];
+    for (long long i = p0 + 1; i < p1; i++) {
+      const int v = blist[i];
+      long long j = i - 1;
+      while (j >= p0 && blist[j] > v) {
+        blist[j + 1] = blist[j];
+        j--;
+      }
+      blist[j + 1] = v;
+    }
+  }
+}
+
+// Walk the sorted union of the incident lists of the contact's two bodies:
+// the columns of its block row, in increasing order.
+template <typename F>
+__device__ __forceinline__ void row_columns(int c, const int* A, const int* B, const long long* bptr,
+                                            const int* blist, F f) {
+  const int a = A[c], b = B[c];
+  long long i = a >= 0 ? bptr[a] : 0, ie = a >= 0 ? bptr[a + 1] : 0;
+  long long j = bptr[b], je = bptr[b + 1];
+  int last = -1;
+  while (i < ie || j < je) {
+    int v;
+    if (j >= je || (i < ie && blist[i] <= blist[j]))
+      v = blist[i++];
+    else
+      v = blist[j++];
+    if (v != last) {
+      f(v);
+      last = v;
+    }
+  }
+}
+
+__global__ void k_row_len(int nc, const int* __restrict__ A, const int* __restrict__ B,
+                          const long long* __restrict__ bptr, const int* __restrict__ blist, int* __restrict__ len) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    int n = 0;
+    row_columns(c, A, B, bptr, blist, [&](int) { n++; });
+    len[c] = n;
+  }
+}
+
+// Contribution of a body b shared by contacts ci and cj to block W_ij
+// (column-major): s_i s_j R_i (I/m - [d_i]x [d_j]x / I) R_j^T, with d the
+// contact point minus the body centre and s = +1 for body B, -1 for body A;
+// [a]x [b]x = b a^T - (a.b) I.  The operation order is that of the scene
+// generator, so the blocks are bit-identical to its host assembly.
+__device__ __forceinline__ void add_body_block(int ci, int cj, int b, const int* B, const double* frame,
+                                               const double* cpt, const double* bpos, double m, double inert,
+                                               double W[9]) {
+  const double si = (B[ci] == b) ? 1.0 : -1.0, sj = (B[cj] == b) ? 1.0 : -1.0;
+  double di[3], dj[3];
+  for (int a = 0; a < 3; a++) {
+    di[a] = cpt[3 * (size_t)ci + a] - bpos[3 * (size_t)b + a];
+    dj[a] = cpt[3 * (size_t)cj + a] - bpos[3 * (size_t)b + a];
+  }
+  const double ab = di[0] * dj[0] + di[1] * dj[1] + di[2] * dj[2];
+  double K[3][3];
+  for (int r = 0; r < 3; r++)
+    for (int q = 0; q < 3; q++) {
+      const double cxx = dj[r] * di[q] - (r == q ? ab : 0.0);
+      K[r][q] = (r == q ? 1.0 / m : 0.0) - cxx / inert;
+    }
+  const double* Ri = frame + 9 * (size_t)ci;
+  const double* Rj = frame + 9 * (size_t)cj;
+  double KR[3][3];
+  for (int r = 0; r < 3; r++)
+    for (int q = 0; q < 3; q++) KR[r][q] = K[r][0] * Rj[3 * q + 0] + K[r][1] * Rj[3 * q + 1] + K[r][2] * Rj[3 * q + 2];
+  const double sg = si * sj;
+  for (int r = 0; r < 3; r++)
+    for (int q = 0; q < 3; q++) {
+      const double v = Ri[3 * r + 0] * KR[0][q] + Ri[3 * r + 1] * KR[1][q] + Ri[3 * r + 2] * KR[2][q];
+      W[r + 3 * q] += sg * v;
+    }
+}
+
+__global__ void k_row_fill(int nc, const int* __restrict__ A, const int* __restrict__ B,
+                           const long long* __restrict__ bptr, const int* __restrict__ blist,
+                           const long long* __restrict__ rowptr, long long* __restrict__ colidx,
+                           double* __restrict__ blocks, const double* __restrict__ frame,
+                           const double* __restrict__ cpt, const double* __restrict__ bpos,
+                           const double* __restrict__ mass, const double* __restrict__ inert) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    long long k = rowptr[c];
+    const int bodies[2] = {A[c], B[c]};
+    row_columns(c, A, B, bptr, blist, [&](int j) {
+      double W[9];
+      for (int e = 0; e < 9; e++) W[e] = 0.0;
+      for (int t = 0; t < 2; t++) {
+        const int b = bodies[t];
+        if (b < 0) continue;
+        if (A[j] == b || B[j] == b) add_body_block(c, j, b, B, frame, cpt, bpos, mass[b], inert[b], W);
+      }
+      for (int e = 0; e < 9; e++) blocks[9 * k + e] = W[e];
+      colidx[k] = j;
+      k++;
+    });
+  }
+}
+
+// q = H (v + h g), g = -9.81 e_z, in the generator's operation order.
+__global__ void k_assemble_q(int nc, const int* __restrict__ A, const int* __restrict__ B,
+                             const double* __restrict__ frame, const double* __restrict__ cpt,
+                             const double* __restrict__ bpos, const double* __restrict__ vel, double h,
+                             double* __restrict__ q) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    double u[3] = {0.0, 0.0, 0.0};
+    const int bodies[2] = {A[c], B[c]};
+    for (int t = 0; t < 2; t++) {
+      const int b = bodies[t];
+      if (b < 0) continue;
+      const double s = (B[c] == b) ? 1.0 : -1.0;
+      double d[3];
+      for (int a = 0; a < 3; a++) d[a] = cpt[3 * (size_t)c + a] - bpos[3 * (size_t)b + a];
+      const double* v = vel + 6 * (size_t)b;
+      const double vf[3] = {v[0], v[1], v[2] - 9.81 * h};
+      const double w[3] = {v[3], v[4], v[5]};
+      const double wxd[3] = {w[1] * d[2] - w[2] * d[1], w[2] * d[0] - w[0] * d[2], w[0] * d[1] - w[1] * d[0]};
+      for (int a = 0; a < 3; a++) u[a] += s * (vf[a] + wxd[a]);
+    }
+    const double* R = frame + 9 * (size_t)c;
+    for (int r = 0; r < 3; r++) q[3 * (size_t)c + r] = R[3 * r + 0] * u[0] + R[3 * r + 1] * u[1] + R[3 * r + 2] * u[2];
+  }
+}
+
+// v += std N(0, 1) per degree of freedom; normals by the Box-Muller method
+// from two uniforms hashed (splitmix64) from (seed, index).
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ULL;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_random_walk(long long n, unsigned long long seed, double std, double* __restrict__ vel) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long x = splitmix(seed ^ splitmix((unsigned long long)i));
+    const unsigned long long y = splitmix(x);
+    const double u1 = ((double)(x >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double u2 = (double)(y >> 11) * (1.0 / 9007199254740992.0);
+    vel[i] += std * (sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+  }
+}
+
+// sum of squares in fixed order: per-block partials, then one block
+__global__ void k_sumsq_partial(long long n, const double* __restrict__ x, double* __restrict__ part) {
+  __shared__ double sh[256];
+  double t = 0.0;
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += 256LL * gridDim.x) t += x[i] * x[i];
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = 128; o >= 1; o >>= 1) {
+    if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_sumsq_final(int nparts, double* __restrict__ part) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0.0;
+    for (int k = 0; k < nparts; k++) t += part[k];
+    part[nparts] = t;
+  }
+}
+
+}  // namespace fc3dgpu
+
+static int assemble_q(fc3dgpu_ctx* c) {
+  using namespace fc3dgpu;
+  cudaStream_t s = c->stream;
+  const int nc = c->nc;
+  CK(ensure(&c->qo, &c->qo_cap, (size_t)nc * 3));
+  k_assemble_q<<<grid1d(nc), 256, 0, s>>>(nc, c->cbA, c->cbB, c->cframe, c->cpoint, c->bpos, c->bvel, c->step_h,
+                                          c->qo);
+  k_set_q_mu<<<grid1d(nc), 256, 0, s>>>(nc, c->iperm, c->qo, c->muo, c->q64, c->mu64, c->q32, c->mu32);
+  const int parts = 1024;
+  CK(ensure(&c->qsum, &c->qsum_cap, (size_t)parts + 1));
+  k_sumsq_partial<<<parts, 256, 0, s>>>(3LL * nc, c->qo, c->qsum);
+  k_sumsq_final<<<1, 32, 0, s>>>(parts, c->qsum);
+  CK(cudaGetLastError());
+  c->launches += 4;
+  double s2 = 0.0;
+  CK(cudaMemcpyAsync(&s2, c->qsum + parts, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  c->norm_q = sqrt(s2);
+  c->have_q = true;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_set_contacts(fc3dgpu_ctx* c, int nbodies, int ncontacts, const int32_t* bodyA,
+                                        const int32_t* bodyB, const double* frame, const double* point,
+                                        const double* body_pos, const double* body_mass, const double* body_inertia,
+                                        int colour_kind) {
+  using namespace fc3dgpu;
+  if (!c || nbodies <= 0 || ncontacts <= 0 || !bodyA || !bodyB || !frame || !point || !body_pos || !body_mass ||
+      !body_inertia) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_contacts: invalid argument");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (c->nscenes > 0 || c->batch_graph) {
+    if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+    c->batch_graph = nullptr;
+    c->nscenes = 0;
+  }
+  for (int k = 0; k < ncontacts; k++) {
+    if (bodyB[k] < 0 || bodyB[k] >= nbodies || bodyA[k] < -1 || bodyA[k] >= nbodies || bodyA[k] == bodyB[k]) {
+      fc3dgpu_set_error("fc3dgpu_ctx_set_contacts: contact %d joins bodies %d and %d of %d", k, bodyA[k], bodyB[k],
+                        nbodies);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+  }
+  for (int b = 0; b < nbodies; b++)
+    if (!(body_mass[b] > 0.0) || !(body_inertia[b] > 0.0)) {
+      fc3dgpu_set_error("fc3dgpu_ctx_set_contacts: body %d needs a positive mass and inertia", b);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const int nc = ncontacts, nb = nbodies;
+  c->have_contacts = c->have_vel = false;
+  CK(ensure(&c->cbA, &c->cbA_cap, (size_t)nc));
+  CK(ensure(&c->cbB, &c->cbB_cap, (size_t)nc));
+  CK(ensure(&c->cframe, &c->cframe_cap, (size_t)nc * 9));
+  CK(ensure(&c->cpoint, &c->cpoint_cap, (size_t)nc * 3));
+  CK(ensure(&c->bpos, &c->bpos_cap, (size_t)nb * 3));
+  CK(ensure(&c->bmass, &c->bmass_cap, (size_t)nb));
+  CK(ensure(&c->binert, &c->binert_cap, (size_t)nb));
+  CK(ensure(&c->bvel, &c->bvel_cap, (size_t)nb * 6));
+  CK(ensure(&c->bdeg, &c->bdeg_cap, (size_t)nb));
+  CK(ensure(&c->bptr, &c->bptr_cap, (size_t)nb + 1));
+  CK(ensure(&c->blist, &c->blist_cap, (size_t)nc * 2));
+  CK(ensure(&c->crowlen, &c->crowlen_cap, (size_t)nc));
+  CK(ensure(&c->scratch64, &c->scratch64_cap, 4));
+  CK(cudaMemcpyAsync(c->cbA, bodyA, sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->cbB, bodyB, sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->cframe, frame, sizeof(double) * 9 * nc, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->cpoint, point, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->bpos, body_pos, sizeof(double) * 3 * nb, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->bmass, body_mass, sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->binert, body_inertia, sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+  // body -> incident contacts (sorted), then the block rows
+  CK(cudaMemsetAsync(c->bdeg, 0, sizeof(int) * nb, s));
+  k_body_degree<<<grid1d(nc), 256, 0, s>>>(nc, c->cbA, c->cbB, c->bdeg);
+  k_scan_excl<int><<<1, 1024, 0, s>>>(nb, c->bdeg, c->bptr, c->scratch64);
+  CK(cudaMemcpyAsync(c->bptr + nb, c->scratch64, sizeof(long long), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemsetAsync(c->bdeg, 0, sizeof(int) * nb, s));
+  k_body_fill<<<grid1d(nc), 256, 0, s>>>(nc, c->cbA, c->cbB, c->bptr, c->bdeg, c->blist);
+  k_body_sort<<<grid1d(nb), 256, 0, s>>>(nb, c->bptr, c->blist);
+  k_row_len<<<grid1d(nc), 256, 0, s>>>(nc, c->cbA, c->cbB, c->bptr, c->blist, c->crowlen);
+  CK(ensure(&c->rowptr, &c->rowptr_cap, (size_t)nc + 1));
+  k_scan_excl<int><<<1, 1024, 0, s>>>(nc, c->crowlen, c->rowptr, c->scratch64);
+  CK(cudaMemcpyAsync(c->rowptr + nc, c->scratch64, sizeof(long long), cudaMemcpyDeviceToDevice, s));
+  long long nnzb = 0;
+  CK(cudaMemcpyAsync(&nnzb, c->scratch64, sizeof(long long), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  c->launches += 6;
+  CK(ensure(&c->colidx, &c->colidx_cap, (size_t)nnzb));
+  CK(ensure(&c->blocks, &c->blocks_cap, (size_t)nnzb * 9));
+  k_row_fill<<<grid1d(nc), 256, 0, s>>>(nc, c->cbA, c->cbB, c->bptr, c->blist, c->rowptr, c->colidx, c->blocks,
+                                        c->cframe, c->cpoint, c->bpos, c->bmass, c->binert);
+  CK(cudaGetLastError());
+  c->launches++;
+  int rc = build_layout(c, nc, nnzb, colour_kind, 0, nullptr);
+  if (rc) return rc;
+  c->nb = nb;
+  c->have_contacts = true;
+  c->have_mu = false;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_set_mu(fc3dgpu_ctx* c, const double* mu) {
+  if (!c || !mu || !c->have_W) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_mu: W not set or null input");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  CK(ensure(&c->muo, &c->muo_cap, (size_t)c->nc));
+  CK(cudaMemcpyAsync(c->muo, mu, sizeof(double) * c->nc, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_mu = true;
+  if (c->have_contacts && c->have_vel) return assemble_q(c);
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_set_velocities(fc3dgpu_ctx* c, const double* vel, double h) {
+  if (!c || !vel || !c->have_contacts || !c->have_mu) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_velocities: contacts and mu must be set first");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(c->bvel, vel, sizeof(double) * 6 * c->nb, cudaMemcpyHostToDevice, c->stream));
+  c->step_h = h;
+  c->have_vel = true;
+  return assemble_q(c);
+}
+
+extern "C" int fc3dgpu_ctx_random_walk(fc3dgpu_ctx* c, uint64_t seed, double std) {
+  using namespace fc3dgpu;
+  if (!c || !c->have_vel) {
+    fc3dgpu_set_error("fc3dgpu_ctx_random_walk: velocities not set");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  CK(cudaSetDevice(c->device));
+  k_random_walk<<<grid1d(6LL * c->nb), 256, 0, c->stream>>>(6LL * c->nb, (unsigned long long)seed, std, c->bvel);
+  CK(cudaGetLastError());
+  c->launches++;
+  return assemble_q(c);
+}
+
+extern "C" int fc3dgpu_ctx_get_q(fc3dgpu_ctx* c, double* q) {
+  if (!c || !q || !c->have_q) return NUMERICS_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(q, c->qo, sizeof(double) * 3 * c->nc, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_get_velocities(fc3dgpu_ctx* c, double* vel) {
+  if (!c || !vel || !c->have_vel) return NUMERICS_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(vel, c->bvel, sizeof(double) * 6 * c->nb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_sizes(fc3dgpu_ctx* c, int* nc, long long* nnzb, int* ncolours) {
+  if (!c) return NUMERICS_ERR_NULL_POINTER;
+  if (nc) *nc = c->have_W ? c->nc : 0;
+  if (nnzb) *nnzb = c->have_W ? c->nnzb : 0;
+  if (ncolours) *ncolours = c->have_W ? c->ncol : 0;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_get_W(fc3dgpu_ctx* c, int64_t* rowptr, int64_t* colidx, double* blocks) {
+  if (!c || !c->have_W) return NUMERICS_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(c->device));
+  if (rowptr)
+    CK(cudaMemcpyAsync(rowptr, c->rowptr, sizeof(long long) * (c->nc + 1), cudaMemcpyDeviceToHost, c->stream));
+  if (colidx)
+    CK(cudaMemcpyAsync(colidx, c->colidx, sizeof(long long) * c->nnzb, cudaMemcpyDeviceToHost, c->stream));
+  if (blocks)
+    CK(cudaMemcpyAsync(blocks, c->blocks, sizeof(double) * 9 * c->nnzb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   return 0;
 }

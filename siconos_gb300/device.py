@@ -71,6 +71,52 @@ class DeviceSolver:
         return bool(self.L.fc3dgpu_ctx_staging(self.ctx, int(on)))
 
     # ---- batched problems -------------------------------------------------
+    def set_contacts(self, geo: dict, colouring: int = sn.FC3DGPU_COLOURING_DEFAULT):
+        """Assemble W on the device from contact geometry (see
+        LatticeScene.contacts)."""
+        nc, nb = len(geo["bodyA"]), len(geo["body_mass"])
+        arr = {k: np.ascontiguousarray(geo[k], np.int32 if k.startswith("body") and k[4] in "AB" else np.float64)
+               for k in ("bodyA", "bodyB", "frame", "point", "body_pos", "body_mass", "body_inertia")}
+        self._check(self.L.fc3dgpu_ctx_set_contacts(self.ctx, nb, nc, *(arr[k].ctypes.data for k in
+                                                                         ("bodyA", "bodyB", "frame", "point",
+                                                                          "body_pos", "body_mass", "body_inertia")),
+                                                    colouring), "set_contacts")
+        self.nc, self.nb = nc, nb
+
+    def set_mu(self, mu):
+        m = np.ascontiguousarray(mu, np.float64)
+        self._check(self.L.fc3dgpu_ctx_set_mu(self.ctx, m.ctypes.data), "set_mu")
+
+    def set_velocities(self, vel, h: float = 1e-3):
+        v = np.ascontiguousarray(vel, np.float64)
+        self._check(self.L.fc3dgpu_ctx_set_velocities(self.ctx, v.ctypes.data, h), "set_velocities")
+
+    def random_walk(self, seed: int, std: float = 0.01):
+        self._check(self.L.fc3dgpu_ctx_random_walk(self.ctx, seed, std), "random_walk")
+
+    def get_q(self) -> np.ndarray:
+        q = np.zeros(3 * self.nc)
+        self._check(self.L.fc3dgpu_ctx_get_q(self.ctx, q.ctypes.data), "get_q")
+        return q
+
+    def get_velocities(self) -> np.ndarray:
+        v = np.zeros(6 * self.nb)
+        self._check(self.L.fc3dgpu_ctx_get_velocities(self.ctx, v.ctypes.data), "get_velocities")
+        return v
+
+    def sizes(self):
+        nc, nnzb, ncol = C.c_int(), C.c_longlong(), C.c_int()
+        self._check(self.L.fc3dgpu_ctx_sizes(self.ctx, C.byref(nc), C.byref(nnzb), C.byref(ncol)), "sizes")
+        return nc.value, nnzb.value, ncol.value
+
+    def get_W(self):
+        nc, nnzb, _ = self.sizes()
+        rp = np.zeros(nc + 1, np.int64)
+        ci = np.zeros(nnzb, np.int64)
+        bl = np.zeros(9 * nnzb)
+        self._check(self.L.fc3dgpu_ctx_get_W(self.ctx, rp.ctypes.data, ci.ctypes.data, bl.ctypes.data), "get_W")
+        return rp, ci, bl.reshape(nnzb, 9)
+
     def load_batch(self, scenes, colouring: int = sn.FC3DGPU_COLOURING_DEFAULT):
         """Upload independent problems (objects with nc, rowptr, colidx,
         blocks, q, mu) as one batch; r starts at zero."""

@@ -173,6 +173,17 @@ ABI = {
     "fc3dgpu_mlp_infer_stream": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_ctx_warm_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_ctx_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_get_W": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_set_contacts": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "fc3dgpu_ctx_set_mu": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_set_velocities": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double]),
+    "fc3dgpu_ctx_random_walk": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double]),
+    "fc3dgpu_ctx_get_q": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fc3dgpu_ctx_get_velocities": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fc3dgpu_lattice_fill_contacts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p]),
     "fc3dgpu_compute_error_device": (C.c_int, [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
                                                C.c_void_p]),

@@ -32,6 +32,21 @@ class LatticeScene:
         W = sn.SparseBlockMatrix(self.nc, self.rowptr, self.colidx, self.blocks)
         return sn.FrictionContactProblem(3, self.nc, W, self.q, self.mu)
 
+    def contacts(self) -> dict:
+        """Geometry for a device assembly of W and q: contact bodies, frames,
+        points; body centres, masses, inertias, velocities."""
+        L = sn.lib()
+        A = np.zeros(self.nc, np.int32)
+        B = np.zeros(self.nc, np.int32)
+        L.fc3dgpu_lattice_fill_geometry(self.handle, None, A.ctypes.data, B.ctypes.data)
+        out = {"bodyA": A, "bodyB": B, "frame": np.zeros(9 * self.nc), "point": np.zeros(3 * self.nc),
+               "body_pos": np.zeros(3 * self.nbodies), "body_mass": np.zeros(self.nbodies),
+               "body_inertia": np.zeros(self.nbodies), "vel": np.zeros(6 * self.nbodies)}
+        L.fc3dgpu_lattice_fill_contacts(self.handle, *(out[k].ctypes.data for k in
+                                                       ("frame", "point", "body_pos", "body_mass", "body_inertia",
+                                                        "vel")))
+        return out
+
     def perturb(self, seed: int, std: float = 0.01, h: float = 1e-3):
         """v0 += N(0, std^2) per degree of freedom; q recomputed, contacts kept."""
         L = sn.lib()

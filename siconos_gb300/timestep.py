@@ -2,12 +2,16 @@
 lattice with the contacts (and W) kept and q following a random walk
 (v0 += N(0, walk_std^2) per degree of freedom between steps).
 
-W is uploaded and coloured once; every step uploads only the new q and
-starts from the previous step's reaction (`warm="previous"`), from the
-learned proposal with that reaction as its fallback (`warm="learned"`), or
-from zero (`warm="zero"`).  `checker(scene, r)` (optional) is called on every
-`check_every`-th step with the step's reaction and its value is recorded as
-`check_error`, e.g. an independent FP64 fc3d_compute_error.
+W is assembled and coloured once.  With `assembly="host"` the scene
+generator forms each step's q on the host and uploads it; with
+`assembly="device"` W and q are assembled on the GPU from the contact
+geometry and the velocity random walk runs there too, so a step moves no
+array between host and device.  Each step starts from the previous step's
+reaction (`warm="previous"`), from the learned proposal with that reaction as
+its fallback (`warm="learned"`), or from zero (`warm="zero"`).
+`checker(scene, r, q)` (optional) is called on every `check_every`-th step
+with the step's reaction and q, and its value is recorded as `check_error`,
+e.g. an independent FP64 fc3d_compute_error.
 """
 from __future__ import annotations
 
@@ -21,9 +25,11 @@ from .scene import lattice
 
 def run_sequence(dims=(80, 80, 40), steps: int = 200, seed: int = 5, mu: float = 0.5, walk_std: float = 0.01,
                  tol: float = 1e-3, max_iter: int = 1000, warm: str = "learned", mlp=None, check_every: int = 10,
-                 checker=None, device: int = 0, log=None):
+                 checker=None, device: int = 0, log=None, assembly: str = "host", h: float = 1e-3):
     if warm not in ("learned", "previous", "zero"):
         raise ValueError(f"unknown warm start {warm!r}")
+    if assembly not in ("host", "device"):
+        raise ValueError(f"unknown assembly {assembly!r}")
     if warm == "learned" and mlp is None:
         raise ValueError("the learned warm start needs a trained network")
     from .learned import warm_start
@@ -31,14 +37,24 @@ def run_sequence(dims=(80, 80, 40), steps: int = 200, seed: int = 5, mu: float =
     d = DeviceSolver(device)
     recs = []
     try:
-        d.load(sc)
+        if assembly == "device":
+            geo = sc.contacts()
+            d.set_contacts(geo)
+            d.set_mu(sc.mu)
+            d.set_velocities(geo["vel"], h)
+            d.zero_r()
+        else:
+            d.load(sc)
         d.solve(tol=tol, max_iter=2)  # kernels loaded, launch shape tuned
         d.zero_r()
         for k in range(steps):
             t0 = time.perf_counter()
             if k > 0:
-                sc.perturb(seed * 7919 + k, walk_std)
-                d.set_q_mu(sc.q, sc.mu)
+                if assembly == "device":
+                    d.random_walk(seed * 7919 + k, walk_std)
+                else:
+                    sc.perturb(seed * 7919 + k, walk_std)
+                    d.set_q_mu(sc.q, sc.mu)
             t1 = time.perf_counter()
             if warm == "zero":
                 d.zero_r()
@@ -55,7 +71,8 @@ def run_sequence(dims=(80, 80, 40), steps: int = 200, seed: int = 5, mu: float =
                 rec["error_proposal"] = ws["error_proposal"]
             if checker is not None and k % check_every == 0:
                 r, _ = d.get()
-                rec["check_error"] = float(checker(sc, r))
+                q = d.get_q() if assembly == "device" else sc.q
+                rec["check_error"] = float(checker(sc, r, q))
             recs.append(rec)
             if log:
                 log(rec)

@@ -11,8 +11,8 @@ pytestmark = pytest.mark.gpu
 def _checker():
     import oracle as O
 
-    def check(sc, r):
-        P = O.Problem(sc.nc, sc.rowptr, sc.colidx, sc.blocks, sc.q, sc.mu)
+    def check(sc, r, q):
+        P = O.Problem(sc.nc, sc.rowptr, sc.colidx, sc.blocks, q, sc.mu)
         e, _ = O.compute_error_port(P, r)
         return e
     return check
@@ -27,12 +27,12 @@ def _mlp():
     return m
 
 
-@pytest.mark.parametrize("warm", ["previous", "learned"])
-def test_sequence_small(built_lib, warm):
+@pytest.mark.parametrize("warm,assembly", [("previous", "host"), ("learned", "host"), ("previous", "device")])
+def test_sequence_small(built_lib, warm, assembly):
     from siconos_gb300.timestep import run_sequence, summarise
     m = _mlp() if warm == "learned" else None
     run = run_sequence(dims=(10, 10, 6), steps=30, seed=9, tol=1e-4, max_iter=2000, warm=warm, mlp=m,
-                       check_every=5, checker=_checker())
+                       check_every=5, checker=_checker(), assembly=assembly)
     s = summarise(run)
     assert s["converged"] == 30
     assert s["check_rel_diff_max"] <= 1e-10
@@ -48,13 +48,13 @@ def test_previous_step_start_saves_sweeps(built_lib):
 
 
 def test_sequence_80x80x40(built_lib):
-    """The full time-stepping case: 761,600 contacts, 200 steps, learned
-    warm start with the previous step as fallback, tol 1e-3, the oracle's
-    FP64 error on every 10th step."""
+    """The full time-stepping case: 761,600 contacts, 200 steps, W and q
+    assembled on the device, learned warm start with the previous step as
+    fallback, tol 1e-3, the oracle's FP64 error on every 10th step."""
     from siconos_gb300.timestep import run_sequence, summarise
     m = _mlp()
     run = run_sequence(dims=(80, 80, 40), steps=200, seed=5, tol=1e-3, max_iter=1500, warm="learned", mlp=m,
-                       check_every=10, checker=_checker())
+                       check_every=10, checker=_checker(), assembly="device")
     m.close()
     s = summarise(run)
     print(s)
