@@ -162,6 +162,13 @@ int fc3dgpu_ctx_set_W(fc3dgpu_ctx *ctx, int nc, const int64_t *rowptr, const int
  * join two problems), the number of problems and each one's contact count.
  * Each problem is coloured as it would be alone.  q, mu and r are then
  * passed as the concatenation of the problems' vectors. */
+/* fc3dgpu_ctx_set_W for new values of W: when the block structure (rowptr,
+ * colidx) and the colouring kind equal the current ones (compared on the
+ * device), only the blocks are uploaded and refilled into the current
+ * layout; otherwise it is fc3dgpu_ctx_set_W.  Time stepping with fixed
+ * contacts and the driver's cache use it. */
+int fc3dgpu_ctx_update_W(fc3dgpu_ctx *ctx, int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                         int colour_kind);
 int fc3dgpu_ctx_set_W_batch(fc3dgpu_ctx *ctx, int nproblems, const int *problem_nc, const int64_t *rowptr,
                             const int64_t *colidx, const double *blocks, int colour_kind);
 /* Solve every problem of the batch (persistent kernels with a work queue,

@@ -53,10 +53,26 @@ __device__ __forceinline__ void solve_scene(const BatchArgs<Real>& b, int scene,
   const int p0 = sptr[0] * FC3D_SLAB, p1 = sptr[ncol] * FC3D_SLAB;
   const double norm_q = b.scene_normq[scene];
   const int max_sweeps = b.scene_budget ? b.scene_budget[scene] : a.max_sweeps;
-  double working = a.user_tol, local_tol = a.local_tol;
+  double working = a.mode == 1 ? a.user_tol : fmax(a.user_tol, a.switch_tol), local_tol = a.local_tol;
   double incr = INFINITY, full = INFINITY, best = INFINITY;
   int sweep = 0, best_sweep = 0;
   bool converged = false;
+  if (a.mode == 1 && b.scene_out_prev && b.scene_out_prev[(size_t)scene * 8 + 3] == 0.0) {
+    // the FP32 iterate met the tolerance in FP32 arithmetic: FP64 check first
+    full = scene_full_error(a, p0, p1, norm_q);
+    if (full < a.user_tol) {
+      if (threadIdx.x == 0) {
+        double* o = b.scene_out + (size_t)scene * 8;
+        o[0] = 0;
+        o[1] = b.scene_out_prev[(size_t)scene * 8 + 1];
+        o[2] = full;
+        o[3] = 0;
+        o[4] = working;
+        o[5] = local_tol;
+      }
+      return;
+    }
+  }
   while (sweep < max_sweeps) {
     sweep++;
     double acc[3] = {0.0, 0.0, 0.0};
@@ -98,6 +114,21 @@ __device__ __forceinline__ void solve_scene(const BatchArgs<Real>& b, int scene,
         best_sweep = sweep;
       } else if (a.stall_window > 0 && sweep - best_sweep >= a.stall_window) {
         stop = true;
+      }
+      // the reference's adaptive test on this precision's iterate, against
+      // max(tol, switch_tol), as in the single-problem kernel
+      if (!stop && incr < working) {
+        full = scene_full_error(a, p0, p1, norm_q);
+        const double target = fmax(a.user_tol, a.switch_tol);
+        if (full <= target) {
+          converged = true;
+          stop = true;
+        } else if (full > 0.0 && incr > 0.0) {
+          double nt = (incr / full) * target;
+          const double mint = fmax(target * 1e-6, DBL_EPSILON * 1e-6);
+          if (nt < mint) nt = mint;
+          if (nt < working) working = nt;
+        }
       }
     }
     if (stop) break;

@@ -15,6 +15,9 @@ struct BatchArgs {
   const int* scene_budget;   // sweep budget of each problem (nullptr: base.max_sweeps)
   int* queue;                // next problem index, zero at launch
   double* scene_out;         // nscenes x 8: sweeps, incr, full error, info, working tol, local tol
+  // outputs of the previous (FP32) phase, or nullptr: a problem whose FP32
+  // iterate met the tolerance gets its FP64 error checked before any sweep
+  const double* scene_out_prev;
 };
 
 }  // namespace fc3dgpu

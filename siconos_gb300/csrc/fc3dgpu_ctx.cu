@@ -720,6 +720,9 @@ struct fc3dgpu_ctx {
   int nbr_next = 0;
   BUF(unsigned, nbrmask);
   int nbr_sync = 1;  // neighbourhood synchronisation on (1, default) or grid barriers (0)
+  int colour_kind = -1;  // colouring of the current layout
+  BUF(long long, wtmp);  // new structure for a comparison with the current one
+  BUF(int, wdiff);
   // device assembly of W and q from rigid-body contacts
   int nb = 0;
   double step_h = 0.0;
@@ -824,7 +827,7 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->counters, c->timeline, c->scene_off, c->grp, c->scounts, c->snslab, c->sncol, c->sbase,
                   c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64, c->feat,
                   c->prop, c->rbak, c->gapo, c->cbA, c->cbB, c->cframe, c->cpoint, c->bpos, c->bmass,
-                  c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum};
+                  c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum, c->wtmp, c->wdiff};
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1084,6 +1087,7 @@ static int build_layout(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, int ns
   c->nc = nc;
   c->nnzb = nnzb;
   c->have_W = true;
+  c->colour_kind = kind;
   for (auto& n : c->nbrc) n.grid = 0;  // the rows' owners changed
   return 0;
 }
@@ -1706,6 +1710,7 @@ static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
     b.scene_budget = nullptr;
     b.queue = c->squeue;
     b.scene_out = c->sout32;
+    b.scene_out_prev = nullptr;
     CK(launch_batch_f32(b, s, &g));
     k_r32_to_r64<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r32, c->rpli32, c->r64, c->rpli64);
   }
@@ -1732,6 +1737,7 @@ static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
     b.scene_budget = c->sbudget;
     b.queue = c->squeue + 1;
     b.scene_out = c->sout64;
+    b.scene_out_prev = p->precision == 0 ? c->sout32 : nullptr;
     CK(launch_batch_f64(b, s, &g));
   }
   return 0;
@@ -2257,5 +2263,61 @@ extern "C" int fc3dgpu_ctx_get_W(fc3dgpu_ctx* c, int64_t* rowptr, int64_t* colid
   if (blocks)
     CK(cudaMemcpyAsync(blocks, c->blocks, sizeof(double) * 9 * c->nnzb, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// New values of W on an unchanged block structure
+// ---------------------------------------------------------------------------
+namespace fc3dgpu {
+__global__ void k_differs(long long n, const long long* __restrict__ a, const long long* __restrict__ b,
+                          int* __restrict__ diff) {
+  int d = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    d |= a[i] != b[i];
+  if (__syncthreads_or(d) && threadIdx.x == 0) atomicOr(diff, 1);
+}
+}  // namespace fc3dgpu
+
+extern "C" int fc3dgpu_ctx_update_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx,
+                                    const double* blocks, int kind) {
+  using namespace fc3dgpu;
+  if (!c || nc <= 0 || !rowptr || !colidx || !blocks) {
+    fc3dgpu_set_error("fc3dgpu_ctx_update_W: invalid argument");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (!c->have_W || c->nscenes > 0 || c->have_contacts || nc != c->nc || rowptr[nc] != c->nnzb ||
+      kind != c->colour_kind)
+    return fc3dgpu_ctx_set_W(c, nc, rowptr, colidx, blocks, kind);
+  CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const long long nnzb = c->nnzb;
+  // compare the structure with the current one on the device; no kernel
+  // indexes with the new arrays before they are found equal to the
+  // validated ones
+  CK(ensure(&c->wtmp, &c->wtmp_cap, (size_t)(nc + 1) + (size_t)nnzb));
+  CK(ensure(&c->wdiff, &c->wdiff_cap, 1));
+  CK(cudaMemcpyAsync(c->wtmp, rowptr, sizeof(long long) * (nc + 1), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->wtmp + nc + 1, colidx, sizeof(long long) * nnzb, cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(c->wdiff, 0, sizeof(int), s));
+  k_differs<<<grid1d(nc + 1), 256, 0, s>>>(nc + 1, c->wtmp, c->rowptr, c->wdiff);
+  k_differs<<<grid1d(nnzb), 256, 0, s>>>(nnzb, c->wtmp + nc + 1, c->colidx, c->wdiff);
+  int diff = 1;
+  CK(cudaMemcpyAsync(&diff, c->wdiff, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  c->launches += 2;
+  if (diff) return fc3dgpu_ctx_set_W(c, nc, rowptr, colidx, blocks, kind);
+  // same structure: new values into the existing layout
+  CK(cudaMemcpyAsync(c->blocks, blocks, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+  const long long nw = c->nslots * 9 * FC3D_SLAB;
+  k_fill_blocks<<<grid1d(nc, 128), 128, 0, s>>>(nc, c->rowptr, c->colidx, c->blocks, c->iperm, c->slab_off, c->W64,
+                                                c->col, c->D64, c->rho64);
+  k_to_f32<<<grid1d(nw), 256, 0, s>>>(nw, c->W64, c->W32);
+  k_to_f32<<<grid1d((long long)c->nslab * 9 * 32), 256, 0, s>>>((long long)c->nslab * 9 * 32, c->D64, c->D32);
+  k_to_f32<<<grid1d((long long)c->nslab * 2 * 32), 256, 0, s>>>((long long)c->nslab * 2 * 32, c->rho64, c->rho32);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  c->launches += 4;
   return 0;
 }

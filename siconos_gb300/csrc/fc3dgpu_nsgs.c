@@ -371,7 +371,9 @@ static int cached_ctx(FrictionContactProblem *P, SolverOptions *o, fc3dgpu_ctx *
   Bcsr b;
   int rc = bcsr_from_problem(P, &b);
   if (rc) return rc;
-  rc = fc3dgpu_ctx_set_W(c->ctx, b.nc, b.rowptr, b.colidx, b.blocks, kind);
+  /* a W that changed since the cached one is most often new values on the
+   * same structure (time stepping with fixed contacts): keep the layout then */
+  rc = fc3dgpu_ctx_update_W(c->ctx, b.nc, b.rowptr, b.colidx, b.blocks, kind);
   c->nnzb = b.nnzb;
   bcsr_free(&b);
   if (rc) {

@@ -205,3 +205,33 @@ def test_neighbourhood_sync_equals_grid_barriers(gpu, precision):
     assert s1["status"] == 0 and s2["status"] == 0
     assert (r1 == r2).all()
     assert s1["error"] == s2["error"]
+
+
+def test_update_W_values_equals_fresh_upload(gpu):
+    """New values on the same block structure keep the colouring and layout
+    and solve exactly as a fresh upload; a new structure falls back to it."""
+    import siconos_gb300.numerics as sn
+    from siconos_gb300 import scene
+    s = scene.lattice(16, 16, 8, seed=5)
+    gpu.load(s)
+    ncol0 = gpu.sizes()[2]
+    blocks2 = s.blocks * 1.25
+    L = gpu.L
+    rc = L.fc3dgpu_ctx_update_W(gpu.ctx, s.nc, s.rowptr, s.colidx, np.ascontiguousarray(blocks2).reshape(-1),
+                                sn.FC3DGPU_COLOURING_DEFAULT)
+    assert rc == 0, sn.last_error()
+    gpu.set_q_mu(s.q, s.mu)
+    gpu.zero_r()
+    st1 = gpu.solve(tol=1e-300, max_iter=15, precision=1)
+    r1, _ = gpu.get()
+    gpu.set_W(s.nc, s.rowptr, s.colidx, blocks2)
+    gpu.set_q_mu(s.q, s.mu)
+    gpu.zero_r()
+    st2 = gpu.solve(tol=1e-300, max_iter=15, precision=1)
+    r2, _ = gpu.get()
+    assert (r1 == r2).all() and st1["error"] == st2["error"] and gpu.sizes()[2] == ncol0
+    # another structure: a full upload behind the same call
+    t = scene.lattice(9, 8, 5, seed=2)
+    rc = L.fc3dgpu_ctx_update_W(gpu.ctx, t.nc, t.rowptr, t.colidx, np.ascontiguousarray(t.blocks).reshape(-1),
+                                sn.FC3DGPU_COLOURING_DEFAULT)
+    assert rc == 0 and gpu.sizes()[0] == t.nc
