@@ -14,8 +14,10 @@ contact-sweeps/s = contacts x sweeps / seconds.
   the device), per-step CUDA events on the solver's own stream, L2 flushed
   (256 MB write) between steps outside the timed events.
 * ``e2e``: the same solve through the reference-facing C-ABI
-  (fc3d_driver -> fc3dgpu_nsgs) with host buffers: each step uploads W, q,
-  mu, r from host memory and copies r, u back (wall clock).
+  (fc3d_driver -> fc3dgpu_nsgs) with host buffers: each step marks W as
+  changed, so it uploads W (the colouring and layout are kept once the
+  unchanged structure is recognised on the device), q, mu, r from host memory
+  and copies r, u back (wall clock).
 * ``cpu_baseline``: the CPU restatement of the reference's fc3d_nsgs
   (bit-exact with it) on a bounded sample of the same scene, one core.
 * ``--impl reference``: the reference's own CPU fc3d_nsgs (oracle/_ref when it
