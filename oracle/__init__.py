@@ -113,6 +113,8 @@ def ref():
         lib.ref_dat_get.restype = C.c_int
         lib.ref_dat_get.argtypes = [C.c_void_p, _I64, _I64, _F64, _F64, _F64]
         lib.ref_dat_close.argtypes = [C.c_void_p]
+        lib.ref_dat_write.restype = C.c_int
+        lib.ref_dat_write.argtypes = [C.c_char_p, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]
         lib.computeAlartCurnierSTD.restype = None
         lib.computeAlartCurnierSTD.argtypes = [_F64, _F64, C.c_double, _F64, _F64, C.c_void_p, C.c_void_p]
         lib.ref_solve_3x3_gepp.restype = C.c_int
@@ -121,6 +123,20 @@ def ref():
         lib.ref_projection_on_cone.argtypes = [_F64, C.c_double]
         _ref = lib
     return _ref
+
+
+def write_dat_ref(P: Problem, path: str | Path, dense: bool = False) -> None:
+    """Write a problem with the reference's own writer."""
+    lib = ref()
+    if lib is None:
+        raise RuntimeError("oracle/_ref is not built")
+    rc = lib.ref_dat_write(str(path).encode(), P.nc, np.ascontiguousarray(P.rowptr, np.int64),
+                           np.ascontiguousarray(P.colidx, np.int64),
+                           np.ascontiguousarray(P.blocks, np.float64).reshape(-1),
+                           np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64),
+                           1 if dense else 0)
+    if rc != 0:
+        raise IOError(f"reference writer failed on {path} ({rc})")
 
 
 def read_dat(path: str | Path) -> Problem:

@@ -209,6 +209,52 @@ void ref_dat_close(void *hv) {
   free(h);
 }
 
+/* Write a problem with the reference's own writer (frictionContact_printInFilename):
+ * W as a sparse-block matrix, or (dense != 0) as a dense one. */
+int ref_dat_write(const char *fname, int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                  const double *q, const double *mu, int dense) {
+  const int n = 3 * nc;
+  const int64_t nb = rowptr[nc];
+  NumericsMatrix *M = NULL;
+  if (dense) {
+    M = NM_create(NM_DENSE, n, n);
+    memset(M->matrix0, 0, sizeof(double) * (size_t)n * (size_t)n);
+    for (int i = 0; i < nc; i++)
+      for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+        for (int b = 0; b < 3; b++)
+          for (int a = 0; a < 3; a++)
+            M->matrix0[(size_t)(3 * colidx[k] + b) * (size_t)n + (size_t)(3 * i + a)] = blocks[9 * k + 3 * b + a];
+  } else {
+    SparseBlockStructuredMatrix *m = SBM_new();
+    m->nbblocks = (size_t)nb;
+    m->blocknumber0 = m->blocknumber1 = (size_t)nc;
+    m->blocksize0 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
+    m->blocksize1 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
+    for (int i = 0; i < nc; i++) m->blocksize0[i] = m->blocksize1[i] = (size_t)(3 * (i + 1));
+    m->filled1 = (size_t)nc + 1;
+    m->filled2 = (size_t)nb;
+    m->index1_data = (size_t *)malloc(sizeof(size_t) * ((size_t)nc + 1));
+    m->index2_data = (size_t *)malloc(sizeof(size_t) * (size_t)nb);
+    m->block = (double **)malloc(sizeof(double *) * (size_t)nb);
+    for (int i = 0; i <= nc; i++) m->index1_data[i] = (size_t)rowptr[i];
+    for (int64_t k = 0; k < nb; k++) {
+      m->index2_data[k] = (size_t)colidx[k];
+      m->block[k] = (double *)malloc(9 * sizeof(double));
+      memcpy(m->block[k], &blocks[9 * k], 9 * sizeof(double));
+    }
+    M = NM_new();
+    NM_fill(M, NM_SPARSE_BLOCK, n, n, m);
+  }
+  double *qq = (double *)malloc(sizeof(double) * (size_t)n);
+  double *mm = (double *)malloc(sizeof(double) * (size_t)nc);
+  memcpy(qq, q, sizeof(double) * (size_t)n);
+  memcpy(mm, mu, sizeof(double) * (size_t)nc);
+  FrictionContactProblem *P = frictionContactProblem_new_with_data(3, (size_t)nc, M, qq, mm);
+  int rc = frictionContact_printInFilename(P, (char *)fname);
+  frictionContactProblem_free(P);
+  return rc;
+}
+
 /* Exported wrappers around static inline helpers of op3x3.h and the
  * reference's cone projection, for known-answer tests. */
 int ref_solve_3x3_gepp(const double *a, double *b) { return solve_3x3_gepp(a, b); }

@@ -185,6 +185,12 @@ ABI = {
     "fc3dgpu_ctx_get_velocities": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fc3dgpu_lattice_fill_contacts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p, C.c_void_p]),
+    "fc3dgpu_dat_open": (C.c_void_p, [C.c_char_p]),
+    "fc3dgpu_dat_close": (None, [C.c_void_p]),
+    "fc3dgpu_dat_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_dat_get": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_dat_write": (C.c_int, [C.c_char_p, C.c_int, _I64, _I64, _F64, _F64, _F64]),
+    "fc3dgpu_dat_last_error": (C.c_char_p, []),
     "fc3dgpu_compute_error_device": (C.c_int, [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
                                                C.c_void_p]),
@@ -419,6 +425,41 @@ def fc3d_nsgs_gpu(problem, reaction, velocity, options) -> int:
     driver's trivial-case shortcut."""
     n = 3 * problem.numberOfContacts
     return lib().fc3dgpu_nsgs(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), options.ptr)
+
+
+def read_dat(path) -> "FrictionContactProblem":
+    """A FrictionContactProblem from a .dat file of the reference's text format
+    (frictionContact_new_from_filename for .dat files), W in sparse-block
+    storage."""
+    L = lib()
+    h = L.fc3dgpu_dat_open(str(path).encode())
+    if not h:
+        raise ValueError(f"{path}: {L.fc3dgpu_dat_last_error().decode()}")
+    try:
+        nc, nnzb = C.c_int(), C.c_int64()
+        L.fc3dgpu_dat_sizes(h, C.byref(nc), C.byref(nnzb))
+        n, k = nc.value, nnzb.value
+        rp = np.zeros(n + 1, np.int64)
+        ci = np.zeros(k, np.int64)
+        bl = np.zeros((k, 9))
+        q = np.zeros(3 * n)
+        mu = np.zeros(n)
+        L.fc3dgpu_dat_get(h, rp.ctypes.data, ci.ctypes.data, bl.ctypes.data, q.ctypes.data, mu.ctypes.data)
+    finally:
+        L.fc3dgpu_dat_close(h)
+    return FrictionContactProblem(3, n, SparseBlockMatrix(n, rp, ci, bl), q, mu)
+
+
+def write_dat(problem: "FrictionContactProblem", path) -> None:
+    """Write a problem with a sparse-block W in the reference's .dat format
+    (frictionContact_printInFilename)."""
+    M = problem._M
+    if not isinstance(M, SparseBlockMatrix):
+        raise TypeError("write_dat needs W in sparse-block storage")
+    rc = lib().fc3dgpu_dat_write(str(path).encode(), M.nc, M.rowptr, M.colidx, M.blocks.reshape(-1),
+                                 problem._q, problem._mu)
+    if rc != 0:
+        raise OSError(lib().fc3dgpu_dat_last_error().decode())
 
 
 def fc3d_compute_error(problem, reaction, velocity, tolerance: float, norm_q: float):
