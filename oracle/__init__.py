@@ -30,7 +30,8 @@ _F64 = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 @dataclass
 class Problem:
-    """A 3D friction-contact problem in block-CSR form (host arrays)."""
+    """A friction-contact problem (3D unless dim says 2) in block-CSR form
+    (host arrays)."""
 
     nc: int
     rowptr: np.ndarray
@@ -38,6 +39,7 @@ class Problem:
     blocks: np.ndarray
     q: np.ndarray
     mu: np.ndarray
+    dim: int = 3
 
     @property
     def nnzb(self) -> int:
@@ -68,6 +70,12 @@ def port():
         lib.oracle_fc3d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
                                          C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
                                          C.POINTER(C.c_int)]
+        lib.oracle_fc2d_nsgs.restype = C.c_int
+        lib.oracle_fc2d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
+                                         C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
+                                         C.POINTER(C.c_int)]
+        lib.oracle_fc2d_compute_error.restype = C.c_double
+        lib.oracle_fc2d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double]
         lib.oracle_fc3d_compute_error.restype = C.c_double
         lib.oracle_fc3d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double]
         lib.oracle_ac_std.restype = None
@@ -109,12 +117,18 @@ def ref():
         lib.ref_fc3d_compute_error.restype = C.c_double
         lib.ref_fc3d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64]
         lib.ref_dat_open.restype = C.c_void_p
-        lib.ref_dat_open.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int)]
+        lib.ref_dat_open.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int64), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]
         lib.ref_dat_get.restype = C.c_int
         lib.ref_dat_get.argtypes = [C.c_void_p, _I64, _I64, _F64, _F64, _F64]
         lib.ref_dat_close.argtypes = [C.c_void_p]
+        lib.ref_fc2d_nsgs.restype = C.c_int
+        lib.ref_fc2d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
+                                      C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        lib.ref_fc2d_compute_error.restype = C.c_double
+        lib.ref_fc2d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64]
         lib.ref_dat_write.restype = C.c_int
-        lib.ref_dat_write.argtypes = [C.c_char_p, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]
+        lib.ref_dat_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]
         lib.computeAlartCurnierSTD.restype = None
         lib.computeAlartCurnierSTD.argtypes = [_F64, _F64, C.c_double, _F64, _F64, C.c_void_p, C.c_void_p]
         lib.ref_solve_3x3_gepp.restype = C.c_int
@@ -130,7 +144,7 @@ def write_dat_ref(P: Problem, path: str | Path, dense: bool = False) -> None:
     lib = ref()
     if lib is None:
         raise RuntimeError("oracle/_ref is not built")
-    rc = lib.ref_dat_write(str(path).encode(), P.nc, np.ascontiguousarray(P.rowptr, np.int64),
+    rc = lib.ref_dat_write(str(path).encode(), P.dim, P.nc, np.ascontiguousarray(P.rowptr, np.int64),
                            np.ascontiguousarray(P.colidx, np.int64),
                            np.ascontiguousarray(P.blocks, np.float64).reshape(-1),
                            np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64),
@@ -144,21 +158,21 @@ def read_dat(path: str | Path) -> Problem:
     lib = ref()
     if lib is None:
         raise RuntimeError("oracle/_ref is not built")
-    nc, nnzb, st = C.c_int(), C.c_int64(), C.c_int()
-    h = lib.ref_dat_open(str(path).encode(), C.byref(nc), C.byref(nnzb), C.byref(st))
+    nc, nnzb, st, dm = C.c_int(), C.c_int64(), C.c_int(), C.c_int()
+    h = lib.ref_dat_open(str(path).encode(), C.byref(nc), C.byref(nnzb), C.byref(st), C.byref(dm))
     if not h:
         raise IOError(f"cannot read {path}")
-    n, nb = nc.value, nnzb.value
+    n, nb, d = nc.value, nnzb.value, dm.value
     rp = np.zeros(n + 1, np.int64)
     ci = np.zeros(max(nb, 1), np.int64)
-    bl = np.zeros(9 * max(nb, 1))
-    q = np.zeros(3 * n)
+    bl = np.zeros(d * d * max(nb, 1))
+    q = np.zeros(d * n)
     mu = np.zeros(n)
     rc = lib.ref_dat_get(h, rp, ci, bl, q, mu)
     lib.ref_dat_close(h)
     if rc != 0:
         raise IOError(f"unsupported storage in {path}")
-    return Problem(n, rp, ci[:nb].copy(), bl[: 9 * nb].reshape(nb, 9).copy(), q, mu)
+    return Problem(n, rp, ci[:nb].copy(), bl[: d * d * nb].reshape(nb, d * d).copy(), q, mu, d)
 
 
 def _solve(fn, P: Problem, r0, tol, maxiter, order, trace_cap, is_port):
@@ -200,5 +214,61 @@ def compute_error_ref(P: Problem, r) -> tuple[float, np.ndarray]:
     u = np.zeros(3 * P.nc)
     blocks = np.ascontiguousarray(P.blocks, dtype=np.float64).reshape(-1)
     e = ref().ref_fc3d_compute_error(P.nc, P.rowptr, P.colidx, blocks, P.q, P.mu,
+                                     np.ascontiguousarray(r, np.float64), u)
+    return e, u
+
+
+# ---- 2D friction contact (dim = 2, blocks 2x2) --------------------------------
+def fc2d_nsgs_port(P: Problem, r0=None, tol=1e-5, maxiter=10000, order=None, trace_cap=0) -> Result:
+    """The restatement of fc2d_nsgs (oracle/fc2d_oracle.c)."""
+    r = np.zeros(2 * P.nc) if r0 is None else np.ascontiguousarray(r0, dtype=np.float64).copy()
+    u = np.zeros(2 * P.nc)
+    it, err, tl = C.c_int(), C.c_double(), C.c_int()
+    tr = np.zeros(max(trace_cap, 1))
+    order_arr = None if order is None else np.ascontiguousarray(order, np.int32)
+    info = port().oracle_fc2d_nsgs(P.nc, np.ascontiguousarray(P.rowptr, np.int64),
+                                   np.ascontiguousarray(P.colidx, np.int64),
+                                   np.ascontiguousarray(P.blocks, np.float64).reshape(-1),
+                                   np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64),
+                                   r, u, tol, maxiter, None if order_arr is None else order_arr.ctypes.data,
+                                   C.byref(it), C.byref(err), tr.ctypes.data if trace_cap else None, trace_cap,
+                                   C.byref(tl))
+    return Result(info, it.value, err.value, r, u, tr[: min(tl.value, trace_cap)].copy())
+
+
+def fc2d_nsgs_ref(P: Problem, r0=None, tol=1e-5, maxiter=10000) -> Result:
+    """The reference's own fc2d_nsgs through fc2d_driver."""
+    lib = ref()
+    if lib is None:
+        raise RuntimeError("oracle/_ref is not built")
+    r = np.zeros(2 * P.nc) if r0 is None else np.ascontiguousarray(r0, dtype=np.float64).copy()
+    u = np.zeros(2 * P.nc)
+    it, err = C.c_int(), C.c_double()
+    info = lib.ref_fc2d_nsgs(P.nc, np.ascontiguousarray(P.rowptr, np.int64),
+                             np.ascontiguousarray(P.colidx, np.int64),
+                             np.ascontiguousarray(P.blocks, np.float64).reshape(-1),
+                             np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64), r, u,
+                             tol, maxiter, C.byref(it), C.byref(err))
+    return Result(info, it.value, err.value, r, u, np.zeros(0))
+
+
+def fc2d_compute_error_port(P: Problem, r) -> tuple[float, np.ndarray]:
+    u = np.zeros(2 * P.nc)
+    q = np.ascontiguousarray(P.q, np.float64)
+    nq = float(np.sqrt(np.sum(q * q)))
+    e = port().oracle_fc2d_compute_error(P.nc, np.ascontiguousarray(P.rowptr, np.int64),
+                                         np.ascontiguousarray(P.colidx, np.int64),
+                                         np.ascontiguousarray(P.blocks, np.float64).reshape(-1), q,
+                                         np.ascontiguousarray(P.mu, np.float64),
+                                         np.ascontiguousarray(r, np.float64), u, nq)
+    return e, u
+
+
+def fc2d_compute_error_ref(P: Problem, r) -> tuple[float, np.ndarray]:
+    u = np.zeros(2 * P.nc)
+    e = ref().ref_fc2d_compute_error(P.nc, np.ascontiguousarray(P.rowptr, np.int64),
+                                     np.ascontiguousarray(P.colidx, np.int64),
+                                     np.ascontiguousarray(P.blocks, np.float64).reshape(-1),
+                                     np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64),
                                      np.ascontiguousarray(r, np.float64), u)
     return e, u

@@ -15,6 +15,8 @@
 #include "NumericsMatrix.h"
 #include "SolverOptions.h"
 #include "SparseBlockMatrix.h"
+#include "fc2d_Solvers.h"
+#include "fc2d_compute_error.h"
 #include "fc3d_Solvers.h"
 #include "fc3d_compute_error.h"
 #include "numerics_verbose.h"
@@ -24,7 +26,8 @@
 /* Build a 3x3-block SBM that points into caller-owned arrays.  blocks holds
  * nnzb column-major 3x3 blocks in row order, rowptr/colidx the block-CSR
  * structure. */
-static NumericsMatrix *make_sbm(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks) {
+static NumericsMatrix *make_sbm_d(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                                  int d) {
   SparseBlockStructuredMatrix *m = SBM_new();
   size_t nnzb = (size_t)rowptr[nc];
   m->nbblocks = nnzb;
@@ -32,7 +35,7 @@ static NumericsMatrix *make_sbm(int nc, const int64_t *rowptr, const int64_t *co
   m->blocknumber1 = (size_t)nc;
   m->blocksize0 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
   m->blocksize1 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
-  for (int i = 0; i < nc; i++) m->blocksize0[i] = m->blocksize1[i] = 3 * (size_t)(i + 1);
+  for (int i = 0; i < nc; i++) m->blocksize0[i] = m->blocksize1[i] = (size_t)d * (size_t)(i + 1);
   m->filled1 = (size_t)nc + 1;
   m->filled2 = nnzb;
   m->index1_data = (size_t *)malloc(sizeof(size_t) * ((size_t)nc + 1));
@@ -41,9 +44,13 @@ static NumericsMatrix *make_sbm(int nc, const int64_t *rowptr, const int64_t *co
   for (int i = 0; i <= nc; i++) m->index1_data[i] = (size_t)rowptr[i];
   for (size_t k = 0; k < nnzb; k++) {
     m->index2_data[k] = (size_t)colidx[k];
-    m->block[k] = (double *)&blocks[9 * k];
+    m->block[k] = (double *)&blocks[(size_t)(d * d) * k];
   }
-  return NM_create_from_data(NM_SPARSE_BLOCK, 3 * nc, 3 * nc, m);
+  return NM_create_from_data(NM_SPARSE_BLOCK, d * nc, d * nc, m);
+}
+
+static NumericsMatrix *make_sbm(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks) {
+  return make_sbm_d(nc, rowptr, colidx, blocks, 3);
 }
 
 static void free_sbm(NumericsMatrix *M) {
@@ -111,6 +118,48 @@ int ref_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const do
   return info;
 }
 
+/* The reference's 2D NSGS (fc2d_driver with SICONOS_FRICTION_2D_NSGS and its
+ * defaults, tolerance and iteration budget set) on a block-CSR W of 2x2
+ * blocks. */
+int ref_fc2d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
+                  const double *mu, double *r, double *u, double tol, int maxiter, int *iters, double *err) {
+  NumericsMatrix *M = make_sbm_d(nc, rowptr, colidx, blocks, 2);
+  FrictionContactProblem P;
+  memset(&P, 0, sizeof(P));
+  P.dimension = 2;
+  P.numberOfContacts = nc;
+  P.M = M;
+  P.q = (double *)q;
+  P.mu = (double *)mu;
+  SolverOptions *opt = solver_options_create(SICONOS_FRICTION_2D_NSGS);
+  opt->iparam[SICONOS_IPARAM_MAX_ITER] = maxiter;
+  opt->dparam[SICONOS_DPARAM_TOL] = tol;
+  int info = fc2d_driver(&P, r, u, opt);
+  if (iters) *iters = opt->iparam[SICONOS_IPARAM_ITER_DONE];
+  if (err) *err = opt->dparam[SICONOS_DPARAM_RESIDU];
+  solver_options_delete(opt);
+  free_sbm(M);
+  return info;
+}
+
+/* The reference's fc2d_compute_error on the given r; u receives q + W r. */
+double ref_fc2d_compute_error(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                              const double *q, const double *mu, const double *r, double *u) {
+  NumericsMatrix *M = make_sbm_d(nc, rowptr, colidx, blocks, 2);
+  FrictionContactProblem P;
+  memset(&P, 0, sizeof(P));
+  P.dimension = 2;
+  P.numberOfContacts = nc;
+  P.M = M;
+  P.q = (double *)q;
+  P.mu = (double *)mu;
+  double norm_q = cblas_dnrm2(2 * nc, q, 1);
+  double e = 0.0;
+  fc2d_compute_error(&P, (double *)r, u, 1e-300, norm_q, &e);
+  free_sbm(M);
+  return e;
+}
+
 /* The reference's fc3d_compute_error on the given r; u receives q + W r. */
 double ref_fc3d_compute_error(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
                               const double *q, const double *mu, const double *r, double *u) {
@@ -134,25 +183,26 @@ typedef struct {
   FrictionContactProblem *P;
 } DatHandle;
 
-void *ref_dat_open(const char *fname, int *nc, int64_t *nnzb, int *storage) {
+void *ref_dat_open(const char *fname, int *nc, int64_t *nnzb, int *storage, int *dim) {
   FrictionContactProblem *P = frictionContact_new_from_filename(fname);
   if (!P) return NULL;
   DatHandle *h = (DatHandle *)malloc(sizeof(DatHandle));
   h->P = P;
   *nc = P->numberOfContacts;
+  *dim = P->dimension;
   *storage = (int)P->M->storageType;
   if (P->M->storageType == NM_SPARSE_BLOCK)
     *nnzb = (int64_t)P->M->matrix1->nbblocks;
   else if (P->M->storageType == NM_DENSE) {
-    /* dense: every 3x3 block with a nonzero entry becomes a block */
-    int n = P->numberOfContacts;
+    /* dense: every d x d block with a nonzero entry becomes a block */
+    int n = P->numberOfContacts, d = P->dimension;
     int64_t cnt = 0;
     for (int bi = 0; bi < n; bi++)
       for (int bj = 0; bj < n; bj++) {
         int nz = (bi == bj);
-        for (int a = 0; a < 3 && !nz; a++)
-          for (int b = 0; b < 3 && !nz; b++)
-            nz = P->M->matrix0[(size_t)(3 * bj + b) * (size_t)(3 * n) + (size_t)(3 * bi + a)] != 0.0;
+        for (int a = 0; a < d && !nz; a++)
+          for (int b = 0; b < d && !nz; b++)
+            nz = P->M->matrix0[(size_t)(d * bj + b) * (size_t)(d * n) + (size_t)(d * bi + a)] != 0.0;
         cnt += nz;
       }
     *nnzb = cnt;
@@ -164,8 +214,8 @@ void *ref_dat_open(const char *fname, int *nc, int64_t *nnzb, int *storage) {
 int ref_dat_get(void *hv, int64_t *rowptr, int64_t *colidx, double *blocks, double *q, double *mu) {
   DatHandle *h = (DatHandle *)hv;
   FrictionContactProblem *P = h->P;
-  int n = P->numberOfContacts;
-  memcpy(q, P->q, sizeof(double) * 3 * (size_t)n);
+  int n = P->numberOfContacts, d = P->dimension;
+  memcpy(q, P->q, sizeof(double) * (size_t)d * (size_t)n);
   memcpy(mu, P->mu, sizeof(double) * (size_t)n);
   if (P->M->storageType == NM_SPARSE_BLOCK) {
     SparseBlockStructuredMatrix *m = P->M->matrix1;
@@ -176,7 +226,7 @@ int ref_dat_get(void *hv, int64_t *rowptr, int64_t *colidx, double *blocks, doub
       for (int i = 0; i <= n; i++) rowptr[i] = (int64_t)m->index1_data[i];
     for (size_t k = 0; k < m->nbblocks; k++) {
       colidx[k] = (int64_t)m->index2_data[k];
-      memcpy(&blocks[9 * k], m->block[k], 9 * sizeof(double));
+      memcpy(&blocks[(size_t)(d * d) * k], m->block[k], (size_t)(d * d) * sizeof(double));
     }
     return 0;
   }
@@ -187,13 +237,13 @@ int ref_dat_get(void *hv, int64_t *rowptr, int64_t *colidx, double *blocks, doub
       rowptr[bi] = k;
       for (int bj = 0; bj < n; bj++) {
         int nz = (bi == bj);
-        for (int a = 0; a < 3 && !nz; a++)
-          for (int b = 0; b < 3 && !nz; b++) nz = A[(size_t)(3 * bj + b) * (size_t)(3 * n) + (size_t)(3 * bi + a)] != 0.0;
+        for (int a = 0; a < d && !nz; a++)
+          for (int b = 0; b < d && !nz; b++) nz = A[(size_t)(d * bj + b) * (size_t)(d * n) + (size_t)(d * bi + a)] != 0.0;
         if (!nz) continue;
         colidx[k] = bj;
-        for (int b = 0; b < 3; b++)
-          for (int a = 0; a < 3; a++)
-            blocks[9 * k + 3 * b + a] = A[(size_t)(3 * bj + b) * (size_t)(3 * n) + (size_t)(3 * bi + a)];
+        for (int b = 0; b < d; b++)
+          for (int a = 0; a < d; a++)
+            blocks[(int64_t)(d * d) * k + d * b + a] = A[(size_t)(d * bj + b) * (size_t)(d * n) + (size_t)(d * bi + a)];
         k++;
       }
     }
@@ -211,9 +261,9 @@ void ref_dat_close(void *hv) {
 
 /* Write a problem with the reference's own writer (frictionContact_printInFilename):
  * W as a sparse-block matrix, or (dense != 0) as a dense one. */
-int ref_dat_write(const char *fname, int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
-                  const double *q, const double *mu, int dense) {
-  const int n = 3 * nc;
+int ref_dat_write(const char *fname, int dim, int nc, const int64_t *rowptr, const int64_t *colidx,
+                  const double *blocks, const double *q, const double *mu, int dense) {
+  const int d = dim, n = dim * nc;
   const int64_t nb = rowptr[nc];
   NumericsMatrix *M = NULL;
   if (dense) {
@@ -221,16 +271,16 @@ int ref_dat_write(const char *fname, int nc, const int64_t *rowptr, const int64_
     memset(M->matrix0, 0, sizeof(double) * (size_t)n * (size_t)n);
     for (int i = 0; i < nc; i++)
       for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
-        for (int b = 0; b < 3; b++)
-          for (int a = 0; a < 3; a++)
-            M->matrix0[(size_t)(3 * colidx[k] + b) * (size_t)n + (size_t)(3 * i + a)] = blocks[9 * k + 3 * b + a];
+        for (int b = 0; b < d; b++)
+          for (int a = 0; a < d; a++)
+            M->matrix0[(size_t)(d * colidx[k] + b) * (size_t)n + (size_t)(d * i + a)] = blocks[(int64_t)(d * d) * k + d * b + a];
   } else {
     SparseBlockStructuredMatrix *m = SBM_new();
     m->nbblocks = (size_t)nb;
     m->blocknumber0 = m->blocknumber1 = (size_t)nc;
     m->blocksize0 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
     m->blocksize1 = (size_t *)malloc(sizeof(size_t) * (size_t)nc);
-    for (int i = 0; i < nc; i++) m->blocksize0[i] = m->blocksize1[i] = (size_t)(3 * (i + 1));
+    for (int i = 0; i < nc; i++) m->blocksize0[i] = m->blocksize1[i] = (size_t)(d * (i + 1));
     m->filled1 = (size_t)nc + 1;
     m->filled2 = (size_t)nb;
     m->index1_data = (size_t *)malloc(sizeof(size_t) * ((size_t)nc + 1));
@@ -239,8 +289,8 @@ int ref_dat_write(const char *fname, int nc, const int64_t *rowptr, const int64_
     for (int i = 0; i <= nc; i++) m->index1_data[i] = (size_t)rowptr[i];
     for (int64_t k = 0; k < nb; k++) {
       m->index2_data[k] = (size_t)colidx[k];
-      m->block[k] = (double *)malloc(9 * sizeof(double));
-      memcpy(m->block[k], &blocks[9 * k], 9 * sizeof(double));
+      m->block[k] = (double *)malloc((size_t)(d * d) * sizeof(double));
+      memcpy(m->block[k], &blocks[(int64_t)(d * d) * k], (size_t)(d * d) * sizeof(double));
     }
     M = NM_new();
     NM_fill(M, NM_SPARSE_BLOCK, n, n, m);
@@ -249,7 +299,7 @@ int ref_dat_write(const char *fname, int nc, const int64_t *rowptr, const int64_
   double *mm = (double *)malloc(sizeof(double) * (size_t)nc);
   memcpy(qq, q, sizeof(double) * (size_t)n);
   memcpy(mm, mu, sizeof(double) * (size_t)nc);
-  FrictionContactProblem *P = frictionContactProblem_new_with_data(3, (size_t)nc, M, qq, mm);
+  FrictionContactProblem *P = frictionContactProblem_new_with_data(d, (size_t)nc, M, qq, mm);
   int rc = frictionContact_printInFilename(P, (char *)fname);
   frictionContactProblem_free(P);
   return rc;

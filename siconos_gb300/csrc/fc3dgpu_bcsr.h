@@ -1,0 +1,34 @@
+/* Internal helpers shared by the host-side solver entry points (not part of
+ * the C-ABI in include/). */
+#ifndef FC3DGPU_BCSR_H
+#define FC3DGPU_BCSR_H
+
+#include <stdint.h>
+
+#include "fc3dgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* W of a friction-contact problem as block-CSR of d x d column-major blocks */
+typedef struct {
+  int nc;
+  long long nnzb;
+  int64_t *rowptr;
+  int64_t *colidx;
+  double *blocks;
+  int borrowed; /* arrays point into the caller's SBM, not owned */
+} Bcsr;
+
+int fc3dgpu_bcsr_from_problem(const FrictionContactProblem *P, int d, Bcsr *out);
+void fc3dgpu_bcsr_free(Bcsr *b);
+/* SolverOptions with iparam/dparam of the reference's size, max_iter and tol
+ * set, as solver_options_create does. */
+SolverOptions *fc3dgpu_options_alloc(int id, int max_iter, double tol);
+void fc3dgpu_set_error(const char *fmt, ...);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

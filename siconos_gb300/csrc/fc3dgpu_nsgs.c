@@ -18,6 +18,7 @@
 #include <time.h>
 
 #include "fc3dgpu.h"
+#include "fc3dgpu_bcsr.h"
 
 void fc3dgpu_set_error(const char *fmt, ...);
 
@@ -41,7 +42,7 @@ static double now_s(void) {
 }
 
 /* calloc'd options as solver_options_initialize does */
-static SolverOptions *options_alloc(int id, int max_iter, double tol) {
+SolverOptions *fc3dgpu_options_alloc(int id, int max_iter, double tol) {
   SolverOptions *o = (SolverOptions *)calloc(1, sizeof(SolverOptions));
   if (!o) return NULL;
   o->solverId = id;
@@ -65,7 +66,7 @@ static SolverOptions *options_alloc(int id, int max_iter, double tol) {
 
 /* fc3d_onecontact_nsn_gp_set_default on registry defaults (100, 1e-14) */
 static SolverOptions *local_options_create(void) {
-  SolverOptions *o = options_alloc(SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID, 100, 1e-14);
+  SolverOptions *o = fc3dgpu_options_alloc(SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID, 100, 1e-14);
   if (!o) return NULL;
   o->iparam[SICONOS_FRICTION_3D_NSN_RHO_STRATEGY] = SICONOS_FRICTION_3D_NSN_FORMULATION_RHO_STRATEGY_SPLIT_SPECTRAL_NORM;
   o->dparam[SICONOS_FRICTION_3D_NSN_RHO] = 1.0;
@@ -123,7 +124,7 @@ void fc3dgpu_nsgs_set_default(SolverOptions *options) {
 }
 
 SolverOptions *fc3dgpu_options_create(void) {
-  SolverOptions *o = options_alloc(SICONOS_FRICTION_3D_NSGS_GPU, 1000, 1e-4);
+  SolverOptions *o = fc3dgpu_options_alloc(SICONOS_FRICTION_3D_NSGS_GPU, 1000, 1e-4);
   if (!o) return NULL;
   fc3dgpu_nsgs_set_default(o);
   return o;
@@ -144,19 +145,10 @@ void fc3dgpu_release(SolverOptions *options) {
   options->solverData = NULL;
 }
 
-/* Block-CSR view of W.  SBM storage is repacked (its blocks are scattered
- * pointers, BlockCSRMatrix.cpp:249); dense storage keeps every 3x3 block
- * holding a nonzero, plus the diagonal. */
-typedef struct {
-  int nc;
-  long long nnzb;
-  int64_t *rowptr;
-  int64_t *colidx;
-  double *blocks;
-  int borrowed; /* arrays point into the caller's SBM, not owned */
-} Bcsr;
-
-static void bcsr_free(Bcsr *b) {
+/* Block-CSR view of W (fc3dgpu_bcsr.h): SBM storage is repacked (its blocks
+ * are scattered pointers, BlockCSRMatrix.cpp:249); dense storage keeps every
+ * d x d block holding a nonzero, plus the diagonal. */
+void fc3dgpu_bcsr_free(Bcsr *b) {
   if (!b->borrowed) {
     free(b->rowptr);
     free(b->colidx);
@@ -165,10 +157,11 @@ static void bcsr_free(Bcsr *b) {
   memset(b, 0, sizeof(*b));
 }
 
-static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
+int fc3dgpu_bcsr_from_problem(const FrictionContactProblem *P, int d, Bcsr *out) {
   memset(out, 0, sizeof(*out));
   const int nc = P->numberOfContacts;
   const NumericsMatrix *M = P->M;
+  const size_t dd = (size_t)d * (size_t)d;
   out->nc = nc;
   if (M->storageType == NM_SPARSE_BLOCK) {
     const SparseBlockStructuredMatrix *S = M->matrix1;
@@ -182,8 +175,8 @@ static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
     }
     for (int i = 0; i < nc; i++) {
       size_t lo = i ? S->blocksize0[i - 1] : 0, lo1 = i ? S->blocksize1[i - 1] : 0;
-      if (S->blocksize0[i] - lo != 3 || S->blocksize1[i] - lo1 != 3) {
-        fc3dgpu_set_error("SBM block %d is not 3x3", i);
+      if (S->blocksize0[i] - lo != (size_t)d || S->blocksize1[i] - lo1 != (size_t)d) {
+        fc3dgpu_set_error("SBM block %d is not %dx%d", i, d, d);
         return NUMERICS_ERR_INVALID_ARGUMENT;
       }
     }
@@ -195,7 +188,7 @@ static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
      * the LP64 targets this library builds for). */
     if (sizeof(size_t) == sizeof(int64_t) && nrows_filled == (size_t)nc && nnzb > 0) {
       int contiguous = 1;
-      for (long long k = 1; k < nnzb && contiguous; k++) contiguous = (S->block[k] == S->block[0] + 9 * k);
+      for (long long k = 1; k < nnzb && contiguous; k++) contiguous = (S->block[k] == S->block[0] + dd * k);
       if (contiguous) {
         out->rowptr = (int64_t *)S->index1_data;
         out->colidx = (int64_t *)S->index2_data;
@@ -206,9 +199,9 @@ static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
     }
     out->rowptr = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nc + 1));
     out->colidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nnzb ? nnzb : 1));
-    out->blocks = (double *)malloc(sizeof(double) * 9 * (size_t)(nnzb ? nnzb : 1));
+    out->blocks = (double *)malloc(sizeof(double) * dd * (size_t)(nnzb ? nnzb : 1));
     if (!out->rowptr || !out->colidx || !out->blocks) {
-      bcsr_free(out);
+      fc3dgpu_bcsr_free(out);
       fc3dgpu_set_error("host allocation failed");
       return NUMERICS_ERR_MEMORY;
     }
@@ -216,7 +209,7 @@ static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
       out->rowptr[i] = (int64_t)((size_t)i <= nrows_filled ? S->index1_data[i] : S->index1_data[nrows_filled]);
     for (long long k = 0; k < nnzb; k++) {
       out->colidx[k] = (int64_t)S->index2_data[k];
-      memcpy(&out->blocks[9 * k], S->block[k], 9 * sizeof(double));
+      memcpy(&out->blocks[dd * k], S->block[k], dd * sizeof(double));
     }
     return 0;
   }
@@ -226,21 +219,21 @@ static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
       fc3dgpu_set_error("dense storage without data");
       return NUMERICS_ERR_NULL_POINTER;
     }
-    const size_t n = 3 * (size_t)nc;
+    const size_t n = (size_t)d * (size_t)nc;
     long long cnt = 0;
     for (int bi = 0; bi < nc; bi++)
       for (int bj = 0; bj < nc; bj++) {
         int nz = (bi == bj);
-        for (int a = 0; a < 3 && !nz; a++)
-          for (int b = 0; b < 3 && !nz; b++) nz = A[(size_t)(3 * bj + b) * n + (size_t)(3 * bi + a)] != 0.0;
+        for (int a = 0; a < d && !nz; a++)
+          for (int b = 0; b < d && !nz; b++) nz = A[(size_t)(d * bj + b) * n + (size_t)(d * bi + a)] != 0.0;
         cnt += nz;
       }
     out->nnzb = cnt;
     out->rowptr = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nc + 1));
     out->colidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)cnt);
-    out->blocks = (double *)malloc(sizeof(double) * 9 * (size_t)cnt);
+    out->blocks = (double *)malloc(sizeof(double) * dd * (size_t)cnt);
     if (!out->rowptr || !out->colidx || !out->blocks) {
-      bcsr_free(out);
+      fc3dgpu_bcsr_free(out);
       fc3dgpu_set_error("host allocation failed");
       return NUMERICS_ERR_MEMORY;
     }
@@ -249,12 +242,13 @@ static int bcsr_from_problem(const FrictionContactProblem *P, Bcsr *out) {
       out->rowptr[bi] = k;
       for (int bj = 0; bj < nc; bj++) {
         int nz = (bi == bj);
-        for (int a = 0; a < 3 && !nz; a++)
-          for (int b = 0; b < 3 && !nz; b++) nz = A[(size_t)(3 * bj + b) * n + (size_t)(3 * bi + a)] != 0.0;
+        for (int a = 0; a < d && !nz; a++)
+          for (int b = 0; b < d && !nz; b++) nz = A[(size_t)(d * bj + b) * n + (size_t)(d * bi + a)] != 0.0;
         if (!nz) continue;
         out->colidx[k] = bj;
-        for (int b = 0; b < 3; b++)
-          for (int a = 0; a < 3; a++) out->blocks[9 * k + 3 * b + a] = A[(size_t)(3 * bj + b) * n + (size_t)(3 * bi + a)];
+        for (int b = 0; b < d; b++)
+          for (int a = 0; a < d; a++)
+            out->blocks[dd * k + (size_t)(d * b + a)] = A[(size_t)(d * bj + b) * n + (size_t)(d * bi + a)];
         k++;
       }
     }
@@ -369,13 +363,13 @@ static int cached_ctx(FrictionContactProblem *P, SolverOptions *o, fc3dgpu_ctx *
     if (!c->ctx) return NUMERICS_ERR_NOT_IMPLEMENTED;
   }
   Bcsr b;
-  int rc = bcsr_from_problem(P, &b);
+  int rc = fc3dgpu_bcsr_from_problem(P, 3, &b);
   if (rc) return rc;
   /* a W that changed since the cached one is most often new values on the
    * same structure (time stepping with fixed contacts): keep the layout then */
   rc = fc3dgpu_ctx_update_W(c->ctx, b.nc, b.rowptr, b.colidx, b.blocks, kind);
   c->nnzb = b.nnzb;
-  bcsr_free(&b);
+  fc3dgpu_bcsr_free(&b);
   if (rc) {
     c->M = NULL;
     return rc;
@@ -502,10 +496,10 @@ int fc3dgpu_compute_error(FrictionContactProblem *problem, double *reaction, dou
   fc3dgpu_ctx *ctx = fc3dgpu_ctx_create(0);
   if (!ctx) return NUMERICS_ERR_NOT_IMPLEMENTED;
   Bcsr b;
-  rc = bcsr_from_problem(problem, &b);
+  rc = fc3dgpu_bcsr_from_problem(problem, 3, &b);
   if (!rc) {
     rc = fc3dgpu_ctx_set_W(ctx, b.nc, b.rowptr, b.colidx, b.blocks, 0);
-    bcsr_free(&b);
+    fc3dgpu_bcsr_free(&b);
   }
   if (!rc) rc = fc3dgpu_ctx_set_q_mu(ctx, problem->q, problem->mu);
   if (!rc) rc = fc3dgpu_ctx_set_r(ctx, reaction);

@@ -187,9 +187,9 @@ ABI = {
                                                 C.c_void_p, C.c_void_p]),
     "fc3dgpu_dat_open": (C.c_void_p, [C.c_char_p]),
     "fc3dgpu_dat_close": (None, [C.c_void_p]),
-    "fc3dgpu_dat_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_dat_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_dat_get": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
-    "fc3dgpu_dat_write": (C.c_int, [C.c_char_p, C.c_int, _I64, _I64, _F64, _F64, _F64]),
+    "fc3dgpu_dat_write": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64]),
     "fc3dgpu_dat_last_error": (C.c_char_p, []),
     "fc3dgpu_compute_error_device": (C.c_int, [C.c_int, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
@@ -244,19 +244,22 @@ class SparseBlockMatrix:
     """3x3-block CSR matrix exposed to C as a SparseBlockStructuredMatrix
     whose block pointers point into one contiguous numpy array."""
 
-    def __init__(self, nc: int, rowptr, colidx, blocks):
+    def __init__(self, nc: int, rowptr, colidx, blocks, block_size: int = 3):
         self.nc = int(nc)
+        self.bs = int(block_size)
+        if self.bs not in (2, 3):
+            raise ValueError("blocks are 2x2 or 3x3")
         self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
         self.colidx = np.ascontiguousarray(colidx, dtype=np.int64)
-        self.blocks = np.ascontiguousarray(np.asarray(blocks, dtype=np.float64).reshape(-1, 9))
+        self.blocks = np.ascontiguousarray(np.asarray(blocks, dtype=np.float64).reshape(-1, self.bs * self.bs))
         nnzb = int(self.rowptr[-1])
         if self.blocks.shape[0] != nnzb or self.colidx.shape[0] != nnzb:
             raise ValueError("block-CSR arrays disagree on the number of blocks")
         self._i1 = self.rowptr.astype(np.uintp)
         self._i2 = self.colidx.astype(np.uintp)
-        self._bs = (3 * np.arange(1, self.nc + 1)).astype(np.uintp)
+        self._bs = (self.bs * np.arange(1, self.nc + 1)).astype(np.uintp)
         base = self.blocks.ctypes.data
-        self._ptrs = self._ptr_array(base, max(nnzb, 1))
+        self._ptrs = self._ptr_array(base, max(nnzb, 1), 8 * self.bs * self.bs)
         s = SparseBlockStructuredMatrix()
         s.nbblocks = nnzb
         s.block = C.cast(self._ptrs, C.POINTER(_DP))
@@ -272,8 +275,8 @@ class SparseBlockMatrix:
         self.c = s
 
     @staticmethod
-    def _ptr_array(base, n):
-        arr = (base + 72 * np.arange(n, dtype=np.uint64)).astype(np.uintp)
+    def _ptr_array(base, n, stride=72):
+        arr = (base + stride * np.arange(n, dtype=np.uint64)).astype(np.uintp)
         holder = (_DP * n).from_buffer(arr)
         holder._keep = arr
         return holder
@@ -283,12 +286,13 @@ class SparseBlockMatrix:
         self.c.version.number += 1
 
     def todense(self) -> np.ndarray:
-        n = 3 * self.nc
+        b = self.bs
+        n = b * self.nc
         W = np.zeros((n, n), order="F")
         for i in range(self.nc):
             for k in range(self.rowptr[i], self.rowptr[i + 1]):
                 j = self.colidx[k]
-                W[3 * i:3 * i + 3, 3 * j:3 * j + 3] = self.blocks[k].reshape(3, 3, order="F")
+                W[b * i:b * i + b, b * j:b * j + b] = self.blocks[k].reshape(b, b, order="F")
         return W
 
 
@@ -296,15 +300,17 @@ class FrictionContactProblem:
     """``FrictionContactProblem(dim, nc, M, q, mu)`` sharing the numpy buffers."""
 
     def __init__(self, dim: int, nc: int, M, q, mu):
-        if dim != 3:
-            raise ValueError("only dimension 3 is supported")
+        if dim not in (2, 3):
+            raise ValueError("dimension 2 or 3")
+        if isinstance(M, SparseBlockMatrix) and M.bs != dim:
+            raise ValueError("block size differs from the dimension")
         self._q = q if (isinstance(q, np.ndarray) and q.dtype == np.float64 and q.flags.c_contiguous) \
             else np.ascontiguousarray(q, dtype=np.float64)
         self._mu = mu if (isinstance(mu, np.ndarray) and mu.dtype == np.float64 and mu.flags.c_contiguous) \
             else np.ascontiguousarray(mu, dtype=np.float64)
         self._M = M
         nm = NumericsMatrix()
-        nm.size0 = nm.size1 = 3 * nc
+        nm.size0 = nm.size1 = dim * nc
         if isinstance(M, SparseBlockMatrix):
             nm.storageType = NM_SPARSE_BLOCK
             nm.matrix1 = C.pointer(M.c)
@@ -436,18 +442,18 @@ def read_dat(path) -> "FrictionContactProblem":
     if not h:
         raise ValueError(f"{path}: {L.fc3dgpu_dat_last_error().decode()}")
     try:
-        nc, nnzb = C.c_int(), C.c_int64()
-        L.fc3dgpu_dat_sizes(h, C.byref(nc), C.byref(nnzb))
-        n, k = nc.value, nnzb.value
+        dim, nc, nnzb = C.c_int(), C.c_int(), C.c_int64()
+        L.fc3dgpu_dat_sizes(h, C.byref(dim), C.byref(nc), C.byref(nnzb))
+        d, n, k = dim.value, nc.value, nnzb.value
         rp = np.zeros(n + 1, np.int64)
         ci = np.zeros(k, np.int64)
-        bl = np.zeros((k, 9))
-        q = np.zeros(3 * n)
+        bl = np.zeros((k, d * d))
+        q = np.zeros(d * n)
         mu = np.zeros(n)
         L.fc3dgpu_dat_get(h, rp.ctypes.data, ci.ctypes.data, bl.ctypes.data, q.ctypes.data, mu.ctypes.data)
     finally:
         L.fc3dgpu_dat_close(h)
-    return FrictionContactProblem(3, n, SparseBlockMatrix(n, rp, ci, bl), q, mu)
+    return FrictionContactProblem(d, n, SparseBlockMatrix(n, rp, ci, bl, block_size=d), q, mu)
 
 
 def write_dat(problem: "FrictionContactProblem", path) -> None:
@@ -456,7 +462,7 @@ def write_dat(problem: "FrictionContactProblem", path) -> None:
     M = problem._M
     if not isinstance(M, SparseBlockMatrix):
         raise TypeError("write_dat needs W in sparse-block storage")
-    rc = lib().fc3dgpu_dat_write(str(path).encode(), M.nc, M.rowptr, M.colidx, M.blocks.reshape(-1),
+    rc = lib().fc3dgpu_dat_write(str(path).encode(), M.bs, M.nc, M.rowptr, M.colidx, M.blocks.reshape(-1),
                                  problem._q, problem._mu)
     if rc != 0:
         raise OSError(lib().fc3dgpu_dat_last_error().decode())

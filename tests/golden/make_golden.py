@@ -3,7 +3,7 @@
 Run in a checkout that has the reference sources (the library in
 ``oracle/_ref`` is built from them by ``oracle/build_ref.py``):
 
-    python tests/golden/make_golden.py /path/to/reference
+    python tests/golden/make_golden.py /path/to/reference [--only=fc2d]
 
 For each SBM/dense friction-contact fixture of the reference's own test data
 (numerics/src/FrictionContact/test/data) and for the 5x5x6 lattice scene,
@@ -60,12 +60,63 @@ def save_case(name, P, res_full, res_20, extra=None):
     np.savez_compressed(HERE / f"{name}.npz", **d)
 
 
-def main(ref_root: str):
+FC2D_FIXTURES = [
+    # the reference's fc2d test collection (data_collection_fc2d_1.c)
+    "FrictionContactProblem00374.dat",
+    "FrictionContactProblem00394.dat",
+    "FC2D_SliderCrankLagrangian00000.dat",
+    "FC2D_SliderCrankLagrangian00001.dat",
+    "FrictionContactProblem00727.dat",
+    "FrictionContactProblem00031.dat",
+    "FrictionContactProblem00071.dat",
+    "FrictionContactProblem00237.dat",
+    # CSparse storage: the reference built here cannot read it (its CSparse
+    # sources are not compiled), so these hold the restatement's results
+    "fc2d_granularflowonwall_00667_00000.dat",
+    "fc2d_granularflowonwall_02020_00213.dat",
+    "fc2d_granularflowonwall_07002_00801.dat",
+]
+
+
+def make_fc2d(data: Path):
+    """2D problems with the reference's fc2d_nsgs results (tol 1e-5, 10000
+    iterations, the reference's own fc2d test settings) and a 20-iteration
+    run; problems the reference cannot read here get the restatement's."""
+    import oracle as O
+    import siconos_gb300.numerics as sn
+    for f in FC2D_FIXTURES:
+        storage = (data / f).read_text()[:64].split()[2]
+        if storage != "2":
+            P = O.read_dat(data / f)
+            run, kind = O.fc2d_nsgs_ref, "reference"
+        else:
+            p = sn.read_dat(data / f)
+            M = p._M
+            P = O.Problem(M.nc, M.rowptr, M.colidx, M.blocks, p._q, p._mu, 2)
+            run, kind = O.fc2d_nsgs_port, "oracle"
+        assert P.dim == 2
+        full = run(P, tol=1e-5, maxiter=10000)
+        short = run(P, tol=1e-5, maxiter=20)
+        name = "fc2d_" + f.replace(".dat", "").replace("-", "_")
+        d = dict(nc=P.nc, rowptr=P.rowptr, colidx=P.colidx, blocks=P.blocks, q=P.q, mu=P.mu, dim=2,
+                 info=full.info, iterations=full.iterations, error=full.error, r=full.r, u=full.u,
+                 info20=short.info, iterations20=short.iterations, error20=short.error, r20=short.r, u20=short.u,
+                 source=f, results=kind)
+        np.savez_compressed(HERE / f"{name}.npz", **d)
+        print(f"{f}: nc={P.nc} nnzb={P.nnzb} {kind} info={full.info} it={full.iterations} err={full.error:.3e}")
+
+
+def main(ref_root: str, only: str | None = None):
     from oracle import build_ref
     import oracle as O
 
     build_ref.build(ref_root)
     data = Path(ref_root) / "numerics" / "src" / "FrictionContact" / "test" / "data"
+    if only == "fc2d":
+        from siconos_gb300 import build as B
+        B.build()
+        make_fc2d(data)
+        return
     for f in FIXTURES:
         P = O.read_dat(data / f)
         full = O.nsgs_ref(P, tol=1e-8, maxiter=10000, trace_cap=20000)
@@ -115,4 +166,6 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    only = next((a[7:] for a in sys.argv[1:] if a.startswith("--only=")), None)
+    main(args[0] if args else "/root/reference", only)

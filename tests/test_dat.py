@@ -19,7 +19,7 @@ def _ours(path):
 def _same(a, P):
     rp, ci, bl, q, mu = a
     assert (rp == P.rowptr).all() and (ci == P.colidx).all()
-    assert (bl == np.asarray(P.blocks).reshape(-1, 9)).all()
+    assert (bl.reshape(-1) == np.asarray(P.blocks).reshape(-1)).all()
     assert (q == P.q).all() and (mu == P.mu).all()
 
 
@@ -75,10 +75,10 @@ def test_we_read_the_reference_file(built_lib, tmp_path, case, dense):
 def test_bad_files_rejected(built_lib, tmp_path):
     import siconos_gb300.numerics as sn
     f = tmp_path / "bad.dat"
-    f.write_text("2\n5\n")
+    f.write_text("4\n5\n")
     with pytest.raises(ValueError, match="dimension"):
         sn.read_dat(f)
-    f.write_text("3\n2\n2\n6\n6\n")
+    f.write_text("3\n2\n5\n6\n6\n")
     with pytest.raises(ValueError, match="storage type"):
         sn.read_dat(f)
     with pytest.raises(ValueError, match="cannot open"):
