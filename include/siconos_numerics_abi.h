@@ -98,12 +98,14 @@ typedef struct SolverOptions {
 } SolverOptions;
 
 /* solver ids (FrictionContact_options.h:83, :152) */
+#define SICONOS_FRICTION_2D_NSGS 400
 #define SICONOS_FRICTION_3D_NSGS 500
 #define SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID 565
 
 /* generic indices (SolverOptions.h:94-121) */
 #define SICONOS_IPARAM_MAX_ITER 0
 #define SICONOS_IPARAM_ITER_DONE 1
+#define SICONOS_IPARAM_NSGS_SHUFFLE 5
 #define SICONOS_DPARAM_TOL 0
 #define SICONOS_DPARAM_RESIDU 1
 #define SICONOS_DPARAM_TIME_BEFORE_LOOP 20

@@ -112,7 +112,7 @@ int oracle_fc2d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const
   for (int i = 0; i < nc; i++) {
     diag[i] = -1;
     for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
-      if (colidx[k] == i) diag[i] = k;
+      if (colidx[k] == i && diag[i] < 0) diag[i] = k;
     if (diag[i] < 0) {
       free(diag);
       free(det);

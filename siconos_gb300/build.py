@@ -20,11 +20,13 @@ OUT = PKG / "_lib"
 LIB = OUT / "libfc3dgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c"]
+C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c"]
 CU_SOURCES = {
     "fc3dgpu_ctx.cu": ["--fmad=false"],
     "fc3dgpu_sweep_f64.cu": ["--fmad=false"],
     "fc3dgpu_noalloc.cu": ["--fmad=false"],
+    # host code computes determinants and norms the kernel reuses
+    "fc2dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # BF16 tensor-core MLP of the learned warm start
     "fc3dgpu_mlp.cu": [],
     # the FP32 sweeps are the accelerator whose result the FP64 polish
@@ -79,8 +81,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             logs.append(out)
     if jobs or force or not LIB.exists():
         tmp = OUT / (LIB.name + ".tmp")
-        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs], "-lcuda"] if False else
-             [nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs]])
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs]])
         os.replace(tmp, LIB)
     if verbose:
         for l in logs:

@@ -28,12 +28,20 @@ import numpy as np
 _PKG = Path(__file__).resolve().parent
 LIB_PATH = _PKG / "_lib" / "libfc3dgpu.so"
 
+SICONOS_FRICTION_2D_NSGS = 400
+SICONOS_FRICTION_2D_NSGS_GPU = 412
 SICONOS_FRICTION_3D_NSGS = 500
 SICONOS_FRICTION_3D_NSGS_GPU = 531
 SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID = 565
 SICONOS_IPARAM_MAX_ITER = 0
 SICONOS_IPARAM_ITER_DONE = 1
+SICONOS_IPARAM_NSGS_SHUFFLE = 5
 SICONOS_DPARAM_TOL = 0
+SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION = 7
+SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT = 15
+SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL = 0
+SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT = 1
+SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL = 2
 SICONOS_DPARAM_RESIDU = 1
 FC3DGPU_IPARAM_PRECISION = 23
 FC3DGPU_IPARAM_LANES = 24
@@ -208,6 +216,27 @@ ABI = {
     "fc3dgpu_lattice_fill_geometry": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_lattice_perturb_velocities": (C.c_int, [C.c_void_p, C.c_uint64, C.c_double]),
     "fc3dgpu_normal_fill": (None, [C.c_uint64, _F64, C.c_int64]),
+    "fc2dgpu_nsgs": (C.c_int, [C.POINTER(_FCP), _DP, _DP, C.POINTER(_SO)]),
+    "fc2dgpu_nsgs_solve_wrap": (C.c_int, [C.c_void_p, _DP, _DP, C.POINTER(_SO)]),
+    "fc2dgpu_nsgs_init_wrap": (C.c_int, [C.c_void_p, C.POINTER(_SO)]),
+    "fc2dgpu_nsgs_free_wrap": (None, [C.c_void_p, C.POINTER(_SO)]),
+    "fc2dgpu_nsgs_set_default": (None, [C.POINTER(_SO)]),
+    "fc2dgpu_options_create": (C.POINTER(_SO), []),
+    "fc2dgpu_options_delete": (None, [C.POINTER(_SO)]),
+    "fc2dgpu_release": (None, [C.POINTER(_SO)]),
+    "fc2dgpu_driver": (C.c_int, [C.POINTER(_FCP), _DP, _DP, C.POINTER(_SO)]),
+    "fc2dgpu_compute_error": (C.c_int, [C.POINTER(_FCP), _DP, _DP, C.c_double, C.c_double, _DP]),
+    "fc2dgpu_ctx_create": (C.c_void_p, [C.c_int]),
+    "fc2dgpu_ctx_destroy": (None, [C.c_void_p]),
+    "fc2dgpu_ctx_set_problem": (C.c_int, [C.c_void_p, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]),
+    "fc2dgpu_ctx_set_q_mu": (C.c_int, [C.c_void_p, _F64, _F64]),
+    "fc2dgpu_ctx_set_r": (C.c_int, [C.c_void_p, _F64]),
+    "fc2dgpu_ctx_solve": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int), _DP,
+                                    C.POINTER(C.c_int), _DP]),
+    "fc2dgpu_ctx_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc2dgpu_ctx_compute_error": (C.c_int, [C.c_void_p, C.c_double, _DP]),
+    "fc2dgpu_ctx_colours": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fc2dgpu_ctx_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
 }
 
 
@@ -348,14 +377,18 @@ class FrictionContactProblem:
 
 
 class SolverOptions:
-    """``SolverOptions(solver_id)`` for ``SICONOS_FRICTION_3D_NSGS_GPU``."""
+    """``SolverOptions(solver_id)`` for ``SICONOS_FRICTION_3D_NSGS_GPU`` or
+    ``SICONOS_FRICTION_2D_NSGS_GPU``."""
+
+    _KINDS = {SICONOS_FRICTION_3D_NSGS_GPU: "fc3dgpu", SICONOS_FRICTION_2D_NSGS_GPU: "fc2dgpu"}
 
     def __init__(self, solver_id: int = SICONOS_FRICTION_3D_NSGS_GPU):
-        if solver_id != SICONOS_FRICTION_3D_NSGS_GPU:
+        if solver_id not in self._KINDS:
             raise ValueError(f"solver {solver_id} is not provided by this library")
-        self.ptr = lib().fc3dgpu_options_create()
+        self._kind = self._KINDS[solver_id]
+        self.ptr = getattr(lib(), self._kind + "_options_create")()
         if not self.ptr:
-            raise MemoryError("fc3dgpu_options_create failed")
+            raise MemoryError(self._kind + "_options_create failed")
         self._cb = None
 
     @property
@@ -385,13 +418,13 @@ class SolverOptions:
         self.ptr.contents.callback = C.pointer(cb)
 
     def release(self):
-        lib().fc3dgpu_release(self.ptr)
+        getattr(lib(), self._kind + "_release")(self.ptr)
 
     def __del__(self):
         try:
             if getattr(self, "ptr", None):
                 self.ptr.contents.callback = None
-                lib().fc3dgpu_options_delete(self.ptr)
+                getattr(lib(), self._kind + "_options_delete")(self.ptr)
                 self.ptr = None
         except Exception:
             pass
@@ -484,6 +517,101 @@ def fc3d_nsgs_batch(problems, reactions, velocities, options):
     info = (C.c_int * k)()
     rc = lib().fc3dgpu_nsgs_batch(k, P, R, U, options.ptr, info)
     return rc, list(info)
+
+
+def fc2d_driver(problem: FrictionContactProblem, reaction: np.ndarray, velocity: np.ndarray,
+                options: SolverOptions) -> int:
+    """fc2d_driver for ``SICONOS_FRICTION_2D_NSGS_GPU``: returns ``info``."""
+    n = 2 * problem.numberOfContacts
+    return lib().fc2dgpu_driver(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), options.ptr)
+
+
+def fc2d_nsgs_gpu(problem, reaction, velocity, options) -> int:
+    """The 2D solver entry itself (what the registry binds), options as given."""
+    n = 2 * problem.numberOfContacts
+    return lib().fc2dgpu_nsgs(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), options.ptr)
+
+
+def fc2d_compute_error(problem, reaction, velocity, tolerance: float, norm_q: float):
+    n = 2 * problem.numberOfContacts
+    err = C.c_double()
+    info = lib().fc2dgpu_compute_error(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), tolerance, norm_q,
+                                       C.byref(err))
+    return info, err.value
+
+
+class Fc2dContext:
+    """Device-resident 2D problem (``fc2dgpu_ctx_*``): upload once, solve many
+    times from any reaction."""
+
+    def __init__(self, nc, rowptr, colidx, blocks, q, mu, colouring: int = 0, device: int = 0):
+        L = lib()
+        self.ctx = L.fc2dgpu_ctx_create(device)
+        if not self.ctx:
+            raise RuntimeError(last_error())
+        self.nc = int(nc)
+        rc = L.fc2dgpu_ctx_set_problem(self.ctx, self.nc, np.ascontiguousarray(rowptr, np.int64),
+                                       np.ascontiguousarray(colidx, np.int64),
+                                       np.ascontiguousarray(blocks, np.float64).reshape(-1),
+                                       np.ascontiguousarray(q, np.float64), np.ascontiguousarray(mu, np.float64),
+                                       colouring)
+        if rc != 0:
+            L.fc2dgpu_ctx_destroy(self.ctx)
+            self.ctx = None
+            raise ValueError(last_error())
+
+    def set_r(self, r):
+        _check(lib().fc2dgpu_ctx_set_r(self.ctx, np.ascontiguousarray(r, np.float64)))
+
+    def set_q_mu(self, q, mu):
+        _check(lib().fc2dgpu_ctx_set_q_mu(self.ctx, np.ascontiguousarray(q, np.float64),
+                                          np.ascontiguousarray(mu, np.float64)))
+
+    def solve(self, tol: float, max_iter: int,
+              error_evaluation: int = SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL) -> dict:
+        it, info = C.c_int(), C.c_int()
+        err, ms = C.c_double(), C.c_double()
+        _check(lib().fc2dgpu_ctx_solve(self.ctx, tol, max_iter, error_evaluation, C.byref(it), C.byref(err),
+                                       C.byref(info), C.byref(ms)))
+        return dict(iterations=it.value, error=err.value, info=info.value, ms=ms.value)
+
+    def get_r_u(self):
+        r, u = np.zeros(2 * self.nc), np.zeros(2 * self.nc)
+        _check(lib().fc2dgpu_ctx_get_r_u(self.ctx, r.ctypes.data, u.ctypes.data))
+        return r, u
+
+    def compute_error(self, norm_q: float) -> float:
+        e = C.c_double()
+        _check(lib().fc2dgpu_ctx_compute_error(self.ctx, norm_q, C.byref(e)))
+        return e.value
+
+    def colours(self):
+        out = np.zeros(self.nc, np.int32)
+        n = lib().fc2dgpu_ctx_colours(self.ctx, out.ctypes.data)
+        if n < 0:
+            raise RuntimeError(last_error())
+        return n, out
+
+    def trace(self, cap: int) -> np.ndarray:
+        out = np.zeros(max(cap, 1))
+        n = lib().fc2dgpu_ctx_trace(self.ctx, out.ctypes.data, cap)
+        return out[:max(n, 0)].copy()
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            lib().fc2dgpu_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError(f"status {rc}: {last_error()}")
 
 
 def colour(rowptr, colidx, kind: int = 0) -> tuple[int, np.ndarray]:

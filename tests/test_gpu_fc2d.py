@@ -1,0 +1,196 @@
+"""GPU 2D NSGS (SICONOS_FRICTION_2D_NSGS_GPU) against the oracle.
+
+The GPU sweep visits contacts in colour order; the oracle run with that
+visiting order is the same sequential Gauss-Seidel, so reactions and
+velocities agree bit for bit (FP64, no contraction, the reference's operation
+order).  Errors are sums over contacts whose order differs (a block reduction
+on the device, index order in the oracle): relative 1e-12.  Through the
+driver, which keeps the reference's defaults, every fixture the reference
+solves is solved to its tolerance."""
+import numpy as np
+import pytest
+
+from test_fc2d_oracle import FC2D_CASES, load_fc2d
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def sn(built_lib):
+    import siconos_gb300.numerics as sn
+    try:
+        c = sn.Fc2dContext(1, [0, 1], [0], [1.0, 0.0, 0.0, 1.0], [-1.0, 0.0], [0.5])
+    except (RuntimeError, ValueError) as e:
+        pytest.fail(f"no usable CUDA device for a -m gpu run: {e}")
+    c.close()
+    return sn
+
+
+def _ctx(sn, P, colouring=0):
+    return sn.Fc2dContext(P.nc, P.rowptr, P.colidx, P.blocks, P.q, P.mu, colouring)
+
+
+def _order(colour):
+    return np.argsort(colour, kind="stable").astype(np.int32)
+
+
+@pytest.mark.parametrize("case", FC2D_CASES)
+def test_fixed_sweeps_bit_exact(sn, case):
+    import oracle as O
+    P, _ = load_fc2d(case)
+    ctx = _ctx(sn, P)
+    ncol, colour = ctx.colours()
+    assert ncol >= 1
+    # colour classes are independent sets of the conflict graph
+    rows = np.repeat(np.arange(P.nc), np.diff(P.rowptr))
+    off = rows != P.colidx
+    assert not np.any(colour[rows[off]] == colour[P.colidx[off]])
+    n = 15
+    res = ctx.solve(0.0, n)
+    r, u = ctx.get_r_u()
+    ref = O.fc2d_nsgs_port(P, tol=0.0, maxiter=n, order=_order(colour), trace_cap=n)
+    assert res["iterations"] == ref.iterations == n
+    assert res["info"] == ref.info == 1
+    np.testing.assert_array_equal(r, ref.r)
+    np.testing.assert_array_equal(u, ref.u)
+    assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
+    np.testing.assert_allclose(ctx.trace(n), ref.trace, rtol=RTOL, atol=0)
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", FC2D_CASES)
+def test_converged_solve_matches_oracle(sn, case):
+    import oracle as O
+    P, g = load_fc2d(case)
+    ctx = _ctx(sn, P)
+    _, colour = ctx.colours()
+    res = ctx.solve(1e-5, 10000)
+    r, u = ctx.get_r_u()
+    ref = O.fc2d_nsgs_port(P, tol=1e-5, maxiter=10000, order=_order(colour))
+    assert (res["info"], res["iterations"]) == (ref.info, ref.iterations)
+    np.testing.assert_array_equal(r, ref.r)
+    np.testing.assert_array_equal(u, ref.u)
+    assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
+    # the colour order solves what the reference's natural order solves
+    assert res["info"] == int(g["info"])
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", FC2D_CASES)
+def test_driver_solves_fixture(sn, case):
+    """Through fc2d_driver with its defaults at the reference tests' settings
+    (tol 1e-5, 10000 iterations), from zero."""
+    import oracle as O
+    P, g = load_fc2d(case)
+    W = sn.SparseBlockMatrix(P.nc, P.rowptr, P.colidx, P.blocks, block_size=2)
+    prob = sn.FrictionContactProblem(2, P.nc, W, P.q.copy(), P.mu.copy())
+    o = sn.SolverOptions(sn.SICONOS_FRICTION_2D_NSGS_GPU)
+    o.iparam[sn.SICONOS_IPARAM_MAX_ITER] = 10000
+    o.dparam[sn.SICONOS_DPARAM_TOL] = 1e-5
+    r, u = np.zeros(2 * P.nc), np.zeros(2 * P.nc)
+    info = sn.fc2d_driver(prob, r, u, o)
+    assert info == int(g["info"]) == 0
+    assert o.dparam[sn.SICONOS_DPARAM_RESIDU] < 1e-5
+    e, u_chk = O.fc2d_compute_error_port(P, r)
+    assert e == pytest.approx(o.dparam[sn.SICONOS_DPARAM_RESIDU], rel=RTOL, abs=0)
+    np.testing.assert_array_equal(u, u_chk)
+    # a second call on the same options reuses the device W and starts from r
+    it1 = int(o.iparam[sn.SICONOS_IPARAM_ITER_DONE])
+    assert sn.fc2d_driver(prob, r, u, o) == 0
+    assert int(o.iparam[sn.SICONOS_IPARAM_ITER_DONE]) <= it1
+
+
+def test_compute_error_matches_oracle(sn):
+    import oracle as O
+    P, g = load_fc2d("fc2d_FrictionContactProblem00237")
+    W = sn.SparseBlockMatrix(P.nc, P.rowptr, P.colidx, P.blocks, block_size=2)
+    prob = sn.FrictionContactProblem(2, P.nc, W, P.q, P.mu)
+    r = g["r20"].copy()
+    u = np.zeros_like(r)
+    nq = float(np.sqrt(np.sum(P.q * P.q)))
+    info, e = sn.fc2d_compute_error(prob, r, u, 1e-5, nq)
+    e_ref, u_ref = O.fc2d_compute_error_port(P, r)
+    np.testing.assert_array_equal(u, u_ref)
+    assert e == pytest.approx(e_ref, rel=RTOL, abs=0)
+    assert info == (1 if e > 1e-5 else 0)
+
+
+def test_error_evaluation_modes(sn):
+    """LIGHT stops at the first sweep whose light error is below tol and
+    reports it; FULL and ADAPTIVE evaluate nothing in fc2d_nsgs (all sweeps,
+    error INFINITY, info 1); through the driver the defaults come back."""
+    import oracle as O
+    P, _ = load_fc2d("fc2d_FC2D_SliderCrankLagrangian00001")
+    ctx = _ctx(sn, P)
+    _, colour = ctx.colours()
+    ref = O.fc2d_nsgs_port(P, tol=0.0, maxiter=400, order=_order(colour), trace_cap=400)
+    tol = 1e-6
+    first = int(np.argmax(ref.trace < tol)) + 1
+    assert ref.trace[first - 1] < tol
+    ctx.set_r(np.zeros(2 * P.nc))
+    res = ctx.solve(tol, 400, sn.SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT)
+    assert res["iterations"] == first
+    assert res["error"] == pytest.approx(ref.trace[first - 1], rel=RTOL, abs=0)
+    assert res["info"] == 0
+    for mode in (sn.SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL, 3):
+        ctx.set_r(np.zeros(2 * P.nc))
+        res = ctx.solve(tol, 37, mode)
+        assert res["iterations"] == 37 and res["info"] == 1 and np.isinf(res["error"])
+    ctx.close()
+
+
+def test_singular_diagonal_and_bad_structure(sn):
+    rowptr = np.array([0, 1, 2], np.int64)
+    colidx = np.array([0, 1], np.int64)
+    blocks = np.array([[1.0, 0.0, 0.0, 1.0], [1.0, 1.0, 1.0, 1.0]])
+    ctx = sn.Fc2dContext(2, rowptr, colidx, blocks, [-1.0, 0.1, -1.0, 0.2], [0.3, 0.3])
+    res = ctx.solve(1e-5, 100)
+    assert res["info"] == 1 and res["iterations"] == 0 and np.isinf(res["error"])
+    ctx.close()
+    with pytest.raises(ValueError, match="diagonal"):
+        sn.Fc2dContext(2, rowptr, np.array([1, 0], np.int64), blocks, [-1.0, 0.1, -1.0, 0.2], [0.3, 0.3])
+    with pytest.raises(ValueError, match="out of range"):
+        sn.Fc2dContext(2, rowptr, np.array([0, 5], np.int64), blocks, [-1.0, 0.1, -1.0, 0.2], [0.3, 0.3])
+
+
+def test_dense_storage_problem(sn):
+    """W given as a dense column-major matrix (NM_DENSE): the blocks holding a
+    nonzero are kept, the solve equals the sparse-block one."""
+    import oracle as O
+    P, _ = load_fc2d("fc2d_FrictionContactProblem00071")
+    W = sn.SparseBlockMatrix(P.nc, P.rowptr, P.colidx, P.blocks, block_size=2)
+    dense = W.todense()
+    res = {}
+    for kind, M in (("sbm", W), ("dense", dense)):
+        prob = sn.FrictionContactProblem(2, P.nc, M, P.q.copy(), P.mu.copy())
+        o = sn.SolverOptions(sn.SICONOS_FRICTION_2D_NSGS_GPU)
+        o.dparam[sn.SICONOS_DPARAM_TOL] = 1e-5
+        o.iparam[sn.SICONOS_IPARAM_MAX_ITER] = 10000
+        r, u = np.zeros(2 * P.nc), np.zeros(2 * P.nc)
+        info = sn.fc2d_driver(prob, r, u, o)
+        res[kind] = (info, int(o.iparam[sn.SICONOS_IPARAM_ITER_DONE]), r)
+    assert res["sbm"][0] == res["dense"][0] == 0
+    e, _ = O.fc2d_compute_error_port(P, res["dense"][2])
+    assert e < 1e-5
+
+
+def test_q_change_reuses_layout(sn):
+    """New q and mu on the same W: the context's answer equals a fresh
+    context's."""
+    P, _ = load_fc2d("fc2d_FrictionContactProblem00727")
+    ctx = _ctx(sn, P)
+    q2 = P.q * 1.5
+    mu2 = P.mu * 0.5
+    ctx.set_q_mu(q2, mu2)
+    a = ctx.solve(1e-5, 10000)
+    ra, _ = ctx.get_r_u()
+    import oracle as O
+    P2 = O.Problem(P.nc, P.rowptr, P.colidx, P.blocks, q2, mu2, 2)
+    fresh = _ctx(sn, P2)
+    b = fresh.solve(1e-5, 10000)
+    rb, _ = fresh.get_r_u()
+    assert a["iterations"] == b["iterations"]
+    np.testing.assert_array_equal(ra, rb)
+    ctx.close()
+    fresh.close()
