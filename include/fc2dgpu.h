@@ -8,11 +8,10 @@
  * light error, LIGHT_WITH_FULL_FINAL with fc2d_compute_error, info 0 / 1 as
  * the reference returns it.  Contacts are visited in colour order (contacts
  * of one colour share no W block), so the FP64 iterates are those of the
- * reference's sequential sweep run in that order, bit for bit.  One thread
- * block runs all sweeps of a problem with block barriers between colours and
- * the convergence logic on the device (no host round trip per sweep); the
- * problems this solver targets (up to tens of thousands of contacts) fit one
- * SM's caches.
+ * reference's sequential sweep run in that order, bit for bit.  One
+ * thread-block cluster (up to 16 SMs) runs all sweeps of a problem in one
+ * launch, with the hardware cluster barrier between colours and the
+ * convergence logic on the device: no host round trip per sweep.
  *
  * Buffers of the solver-level calls are HOST memory owned by the caller. */
 #ifndef FC2DGPU_H
@@ -87,6 +86,12 @@ int fc2dgpu_ctx_get_r_u(fc2dgpu_ctx *ctx, double *r, double *u);
 int fc2dgpu_ctx_compute_error(fc2dgpu_ctx *ctx, double norm_q, double *error);
 /* Colour of each contact and the number of colours (return value). */
 int fc2dgpu_ctx_colours(fc2dgpu_ctx *ctx, int32_t *colour);
+/* Launch shape of the sweep kernel: a thread-block cluster of
+ * cluster_blocks blocks (1..16) of `threads` threads (32..512, a multiple
+ * of 32); 0 picks it from the largest colour (the default).  The iterates do
+ * not depend on it; the reduction order of the errors does. */
+int fc2dgpu_ctx_set_launch(fc2dgpu_ctx *ctx, int cluster_blocks, int threads);
+int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx *ctx, int *cluster_blocks, int *threads);
 /* Per-sweep light error of the last solve (cap entries); returns how many. */
 int fc2dgpu_ctx_trace(fc2dgpu_ctx *ctx, double *out, int cap);
 

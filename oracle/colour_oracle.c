@@ -51,7 +51,7 @@ static void conflict_graph(int nc, const int64_t *rowptr, const int64_t *colidx,
     }
   for (int i = 0; i < nc; i++) cnt[i + 1] += cnt[i];
   int32_t *adj = (int32_t *)malloc(sizeof(int32_t) * (size_t)(cnt[nc] ? cnt[nc] : 1));
-  int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nc ? nc : 1));
+  int64_t *fill = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nc > 0 ? nc : 1));
   memcpy(fill, cnt, sizeof(int64_t) * (size_t)nc);
   for (int i = 0; i < nc; i++)
     for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
@@ -108,10 +108,10 @@ int oracle_colour_greedy(int nc, const int64_t *rowptr, const int64_t *colidx, i
   int64_t *gp;
   int32_t *ga;
   conflict_graph(nc, rowptr, colidx, &gp, &ga);
-  uint32_t *key = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nc ? nc : 1));
-  int32_t *ord = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc ? nc : 1));
+  uint32_t *key = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nc > 0 ? nc : 1));
+  int32_t *ord = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc > 0 ? nc : 1));
   /* distinct-neighbour degree: W's structure may list (i,j) and (j,i) */
-  int32_t *mark = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc ? nc : 1));
+  int32_t *mark = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nc > 0 ? nc : 1));
   for (int i = 0; i < nc; i++) mark[i] = -1;
   for (int i = 0; i < nc; i++) {
     uint32_t d = 0;

@@ -27,6 +27,8 @@ CU_SOURCES = {
     "fc3dgpu_noalloc.cu": ["--fmad=false"],
     # host code computes determinants and norms the kernel reuses
     "fc2dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    # the reference's per-colour design, kept for measurement beside fc2dgpu.cu
+    "fc2dgpu_percolour.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # BF16 tensor-core MLP of the learned warm start
     "fc3dgpu_mlp.cu": [],
     # the FP32 sweeps are the accelerator whose result the FP64 polish
@@ -81,7 +83,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             logs.append(out)
     if jobs or force or not LIB.exists():
         tmp = OUT / (LIB.name + ".tmp")
-        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs]])
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs], "-lcusparse"])
         os.replace(tmp, LIB)
     if verbose:
         for l in logs:

@@ -3,10 +3,9 @@
 // Layout: contacts permuted by colour (stable in contact order); per permuted
 // row its blocks in the caller's order (diagonal included, at dpos), each a
 // 2x2 column-major block, with the permuted column index; q, mu, r, u in
-// permuted order.  One thread block per problem: within a colour each
-// thread takes contacts p = lo + tid, lo + tid + blockDim, ...; a block
-// barrier separates colours.  FP64 without FMA contraction, in the
-// reference's operation order.
+// permuted order.  One thread-block cluster per problem (see k_fc2d_nsgs).
+// FP64 without FMA contraction, in the reference's operation order.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -23,7 +22,10 @@ extern "C" void fc3dgpu_set_error(const char* fmt, ...);
 
 namespace fc2dgpu {
 
-constexpr int NT = 512;
+namespace cg = cooperative_groups;
+
+constexpr int NT_MAX = 512;  // threads per block at most
+constexpr int CS_MAX = 16;   // blocks per cluster at most (non-portable size)
 constexpr int MAXC = 128;
 constexpr int TRACE_CAP = 1 << 16;
 
@@ -46,55 +48,93 @@ struct Args {
   double* out;  // [0] sweeps, [1] final error, [2] info, [3] last light error
 };
 
-__device__ __forceinline__ void mvp2x2(const double* a, const double* v, double* y) {
-  y[0] += a[0] * v[0];
-  y[1] += a[1] * v[0];
-  y[0] += a[2] * v[1];
-  y[1] += a[3] * v[1];
+// Reactions change during a solve and other blocks of the cluster write
+// them: they bypass L1 (ld.global.cg) so every read sees the cluster's
+// latest values after a cluster barrier.  W and the per-contact constants
+// are read-only and stay in the L1 of the block that owns the contact.
+__device__ __forceinline__ double2 ld_r(const double* r, int j) {
+  return __ldcg(reinterpret_cast<const double2*>(r) + j);
+}
+__device__ __forceinline__ void st_r(double* r, int j, double x0, double x1) {
+  __stcg(reinterpret_cast<double2*>(r) + j, make_double2(x0, x1));
 }
 
-// Fixed-order block sum of n values per thread (xor-shuffle tree in each
-// warp, then the warps in order): the same for a given block shape.
+__device__ __forceinline__ void mvp2x2(const double* a, const double2 v, double* y) {
+  const double2 a01 = __ldg(reinterpret_cast<const double2*>(a));
+  const double2 a23 = __ldg(reinterpret_cast<const double2*>(a) + 1);
+  y[0] += a01.x * v.x;
+  y[1] += a01.y * v.x;
+  y[0] += a23.x * v.y;
+  y[1] += a23.y * v.y;
+}
+
+// Cluster-wide sum of N values per thread, in a fixed order (xor-shuffle tree
+// in each warp, the warps in order, then the blocks in rank order), so every
+// block of the cluster gets the same bits.  `part` is a two-slot ring in
+// shared memory: a block writes slot k & 1 only after the barrier of call
+// k - 1, which every block passes after reading call k - 2's slot.
+struct Reduce {
+  double part[2][4];
+  double warp[NT_MAX / 32][4];
+  double bcast[4];
+  int calls;
+};
+
 template <int N>
-__device__ __forceinline__ void block_sum(double v[N]) {
-  __shared__ double sh[NT / 32][N];
+__device__ __forceinline__ void cluster_sum(double v[N], Reduce& R, cg::cluster_group& cl) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < N; i++) {
     double x = v[i];
     for (int o = 16; o >= 1; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sh[w][i] = x;
+    if (lane == 0) R.warp[w][i] = x;
+  }
+  __syncthreads();
+  const int slot = R.calls & 1;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < N; i++) {
+      double s = 0.0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += R.warp[k][i];
+      R.part[slot][i] = s;
+    }
+  }
+  cl.sync();
+  if (threadIdx.x == 0) {
+    const int cs = (int)cl.num_blocks();
+    for (int i = 0; i < N; i++) {
+      double s = 0.0;
+      for (int k = 0; k < cs; k++) s += cl.map_shared_rank(&R.part[slot][0], k)[i];
+      R.bcast[i] = s;
+    }
+    R.calls++;
   }
   __syncthreads();
 #pragma unroll
-  for (int i = 0; i < N; i++) {
-    double s = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k][i];
-    v[i] = s;
-  }
+  for (int i = 0; i < N; i++) v[i] = R.bcast[i];
   __syncthreads();
 }
 
 // fc2d_compute_error (fc2d_compute_error.c:40-140): u = q + W r block by
 // block (per block w_i = 1.0 w_i + 1.0 (a_i0 r0 + a_i1 r1), the reference's
 // 2x2 gemv), natural-map error, relative to max(|r|, |u|, |q|).
-__device__ double full_error(const Args& a) {
+__device__ double full_error(const Args& a, Reduce& R, cg::cluster_group& cl) {
   double v[3] = {0.0, 0.0, 0.0};
-  for (int p = threadIdx.x; p < a.nc; p += blockDim.x) {
+  const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
+  for (int p = g0; p < a.nc; p += G) {
     double w[2] = {a.q[2 * p], a.q[2 * p + 1]};
     for (int s = a.rp[p]; s < a.rp[p + 1]; s++) {
       const double* blk = a.W + 4 * (size_t)s;
-      const double* x = a.r + 2 * (size_t)a.col[s];
+      const double2 x = ld_r(a.r, a.col[s]);
       for (int i = 0; i < 2; i++) {
         double t = 0.0;
-        t += blk[i] * x[0];
-        t += blk[2 + i] * x[1];
+        t += blk[i] * x.x;
+        t += blk[2 + i] * x.y;
         w[i] = 1.0 * w[i] + 1.0 * t;
       }
     }
-    a.u[2 * p] = w[0];
-    a.u[2 * p + 1] = w[1];
-    const double r0 = a.r[2 * p], r1 = a.r[2 * p + 1], mu = a.mu[p];
+    st_r(a.u, p, w[0], w[1]);
+    const double2 rr = ld_r(a.r, p);
+    const double r0 = rr.x, r1 = rr.y, mu = a.mu[p];
     double t0 = r0 - w[0] - mu * fabs(w[1]);
     double t1 = r1 - w[1];
     const double normT = fabs(t1);
@@ -111,7 +151,7 @@ __device__ double full_error(const Args& a) {
     v[1] += r0 * r0 + r1 * r1;
     v[2] += w[0] * w[0] + w[1] * w[1];
   }
-  block_sum<3>(v);
+  cluster_sum<3>(v, R, cl);
   double e = sqrt(v[0]);
   const double scal = fmax(sqrt(v[1]), fmax(sqrt(v[2]), a.norm_q));
   if (fabs(scal) > DBL_EPSILON) e /= scal;
@@ -140,43 +180,57 @@ __device__ __forceinline__ void local_solve(const double* W, double D, const dou
   }
 }
 
-__global__ void __launch_bounds__(NT, 1) k_fc2d_nsgs(const Args a) {
+// All sweeps of one problem in one launch of one thread-block cluster.  A
+// colour's contacts are spread over the cluster's threads (contact lo + g,
+// lo + g + G, ... for global thread g of G: a contact always lands on the
+// same block, so its W row stays in that SM's L1); the hardware cluster
+// barrier (release / acquire) separates colours, and the convergence logic
+// runs on the device with the same bits in every block.
+__global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
+  __shared__ Reduce R;
+  cg::cluster_group cl = cg::this_cluster();
+  if (threadIdx.x == 0) R.calls = 0;
+  __syncthreads();
+  const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
+  const bool lead = cl.block_rank() == 0 && threadIdx.x == 0;
   double tolerance = a.tol, err = INFINITY;
   int iter = 0, not_conv = 1;
   while (iter < a.max_iter && not_conv) {
     ++iter;
     double v[2] = {0.0, 0.0};
     for (int c = 0; c < a.ncol; c++) {
-      for (int p = a.cptr[c] + threadIdx.x; p < a.cptr[c + 1]; p += blockDim.x) {
-        const double old0 = a.r[2 * p], old1 = a.r[2 * p + 1];
+      for (int p = a.cptr[c] + g0; p < a.cptr[c + 1]; p += G) {
+        const double2 old = ld_r(a.r, p);
         double ql[2] = {a.q[2 * p], a.q[2 * p + 1]};
         const int s0 = a.rp[p], s1 = a.rp[p + 1], sd = s0 + a.dpos[p];
         // every block on the diagonal is left out (SBM_row_prod_no_diag_2x2)
         for (int s = s0; s < s1; s++) {
           const int j = a.col[s];
-          if (j != p) mvp2x2(a.W + 4 * (size_t)s, a.r + 2 * (size_t)j, ql);
+          if (j != p) mvp2x2(a.W + 4 * (size_t)s, ld_r(a.r, j), ql);
         }
-        double P[2] = {old0, old1};
+        double P[2] = {old.x, old.y};
         local_solve(a.W + 4 * (size_t)sd, a.det[p], ql, a.mu[p], P);
-        const double x0 = old0 - P[0], x1 = old1 - P[1];
+        const double x0 = old.x - P[0], x1 = old.y - P[1];
         v[0] += x0 * x0 + x1 * x1;
-        a.r[2 * p] = P[0];
-        a.r[2 * p + 1] = P[1];
+        st_r(a.r, p, P[0], P[1]);
       }
-      __syncthreads();
+      cl.sync();
     }
-    for (int p = threadIdx.x; p < a.nc; p += blockDim.x) v[1] += a.r[2 * p] * a.r[2 * p] + a.r[2 * p + 1] * a.r[2 * p + 1];
-    block_sum<2>(v);
+    for (int p = g0; p < a.nc; p += G) {
+      const double2 x = ld_r(a.r, p);
+      v[1] += x.x * x.x + x.y * x.y;
+    }
+    cluster_sum<2>(v, R, cl);
     err = sqrt(v[0]);
     const double nr = sqrt(v[1]);
     if (fabs(nr) > DBL_EPSILON) err /= nr;
-    if (a.trace && threadIdx.x == 0 && iter <= TRACE_CAP) a.trace[iter - 1] = err;
+    if (a.trace && lead && iter <= TRACE_CAP) a.trace[iter - 1] = err;
     if (a.mode == 1) {
       not_conv = !(err < tolerance);  // determine_convergence (fc2d_nsgs.c:147-162)
     } else if (a.mode == 0 && err < tolerance) {
       // determine_convergence_with_full_final (fc2d_nsgs.c:187-228)
       not_conv = 0;
-      const double full = full_error(a);
+      const double full = full_error(a, R, cl);
       if (full > a.tol) {
         tolerance = err / full * a.tol;
         not_conv = 1;
@@ -185,23 +239,29 @@ __global__ void __launch_bounds__(NT, 1) k_fc2d_nsgs(const Args a) {
   }
   const double light = err;
   if (a.mode == 0) {
-    err = full_error(a);
+    err = full_error(a, R, cl);
     not_conv = !(err < a.tol);
   } else if (a.mode == 2) {
     err = INFINITY;  // no branch of the sweep loop evaluates an error (fc2d_nsgs.c:438-448)
     not_conv = 1;
   }
-  if (threadIdx.x == 0) {
+  if (lead) {
     a.out[0] = iter;
     a.out[1] = err;
     a.out[2] = not_conv;
     a.out[3] = light;
   }
+  cl.sync();  // no block leaves while another may still read its shared memory
 }
 
-__global__ void __launch_bounds__(NT, 1) k_fc2d_error(const Args a) {
-  const double e = full_error(a);
-  if (threadIdx.x == 0) a.out[1] = e;
+__global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_error(const Args a) {
+  __shared__ Reduce R;
+  cg::cluster_group cl = cg::this_cluster();
+  if (threadIdx.x == 0) R.calls = 0;
+  __syncthreads();
+  const double e = full_error(a, R, cl);
+  if (cl.block_rank() == 0 && threadIdx.x == 0) a.out[1] = e;
+  cl.sync();
 }
 
 }  // namespace fc2dgpu
@@ -213,6 +273,9 @@ using namespace fc2dgpu;
 
 struct fc2dgpu_ctx {
   int device = 0;
+  int cs_req = 0, nt_req = 0;  // launch shape asked for (0 = automatic)
+  int cs = 1, nt = 128;        // launch shape of the current problem
+  int max_colour = 0;          // contacts in the largest colour
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   int nc = 0, ncol = 0;
@@ -233,6 +296,8 @@ struct fc2dgpu_ctx {
       return NUMERICS_ERR_UNKNOWN;                                                        \
     }                                                                                     \
   } while (0)
+
+static void choose_shape(fc2dgpu_ctx* c);
 
 static void free_problem(fc2dgpu_ctx* c) {
   void* ptrs[] = {c->cptr, c->rp, c->col, c->dpos, c->W, c->det, c->q, c->mu, c->r, c->u};
@@ -387,6 +452,9 @@ extern "C" int fc2dgpu_ctx_set_problem(fc2dgpu_ctx* c, int nc, const int64_t* ro
   c->nc = nc;
   c->ncol = ncol;
   c->singular = singular;
+  c->max_colour = 0;
+  for (int k = 0; k < ncol; k++) c->max_colour = std::max(c->max_colour, cptr[k + 1] - cptr[k]);
+  choose_shape(c);
   return 0;
 }
 
@@ -429,6 +497,97 @@ extern "C" int fc2dgpu_ctx_set_r(fc2dgpu_ctx* c, const double* r) {
   return 0;
 }
 
+// Launch shape: a cluster of up to CS_MAX blocks.  The sweep is bound by
+// the FP64 pipes (about two FP64 operations per clock per SM on this part),
+// so a colour with more contacts is spread over more SMs; blocks of up to
+// NT_MAX threads keep each thread on one or two contacts per colour.
+static cudaLaunchConfig_t config(fc2dgpu_ctx* c, int cs, int nt, cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3(cs, 1, 1);
+  cfg.blockDim = dim3(nt, 1, 1);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->stream;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+// Whether a cluster of cs blocks of nt threads of the sweep kernel (the
+// larger of the two kernels) can be resident on this device.
+static bool cluster_fits(fc2dgpu_ctx* c, int cs, int nt) {
+  if (cs > 8 && cudaFuncSetAttribute(k_fc2d_nsgs, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = config(c, cs, nt, attr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n > 0;
+}
+
+static void choose_shape(fc2dgpu_ctx* c) {
+  int cs = c->cs_req, nt = c->nt_req;
+  if (cs <= 0) {
+    const int want = (c->max_colour + 63) / 64;  // about 64 contacts per SM and colour
+    cs = 1;
+    while (cs < want && cs < CS_MAX) cs *= 2;
+  }
+  cs = std::min(std::max(cs, 1), CS_MAX);
+  if (nt <= 0) nt = std::min(NT_MAX, std::max(32, ((c->max_colour + cs - 1) / cs + 31) / 32 * 32));
+  nt = std::min(std::max(nt / 32 * 32, 32), NT_MAX);
+  if (c->cs_req <= 0)
+    while (cs > 1 && !cluster_fits(c, cs, nt)) cs /= 2;
+  c->cs = cs;
+  c->nt = nt;
+}
+
+template <typename K>
+static cudaError_t launch(fc2dgpu_ctx* c, K kernel, const Args& a) {
+  if (c->cs > 8) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = config(c, c->cs, c->nt, attr);
+  return cudaLaunchKernelEx(&cfg, kernel, a);
+}
+
+extern "C" int fc2dgpu_ctx_set_launch(fc2dgpu_ctx* c, int cluster_blocks, int threads) {
+  if (!c || cluster_blocks < 0 || cluster_blocks > CS_MAX || threads < 0 || threads > NT_MAX ||
+      (threads && threads % 32)) {
+    fc3dgpu_set_error("fc2dgpu_ctx_set_launch: cluster of 0..%d blocks, 0 or 32..%d threads (multiple of 32)",
+                      CS_MAX, NT_MAX);
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (cluster_blocks > 0) {
+    if (cudaSetDevice(c->device) != cudaSuccess || !cluster_fits(c, cluster_blocks, threads ? threads : NT_MAX)) {
+      fc3dgpu_set_error("fc2dgpu_ctx_set_launch: a cluster of %d blocks of %d threads does not fit this device",
+                        cluster_blocks, threads ? threads : NT_MAX);
+      return NUMERICS_ERR_INVALID_ARGUMENT;
+    }
+  }
+  c->cs_req = cluster_blocks;
+  c->nt_req = threads;
+  choose_shape(c);
+  return 0;
+}
+
+extern "C" int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx* c, int* cluster_blocks, int* threads) {
+  if (!c) return NUMERICS_ERR_INVALID_ARGUMENT;
+  if (cluster_blocks) *cluster_blocks = c->cs;
+  if (threads) *threads = c->nt;
+  return 0;
+}
+
 static Args args_of(const fc2dgpu_ctx* c) {
   Args a;
   memset(&a, 0, sizeof(a));
@@ -458,8 +617,7 @@ extern "C" int fc2dgpu_ctx_compute_error(fc2dgpu_ctx* c, double norm_q, double* 
   K2(cudaSetDevice(c->device));
   Args a = args_of(c);
   a.norm_q = norm_q;
-  k_fc2d_error<<<1, NT, 0, c->stream>>>(a);
-  K2(cudaGetLastError());
+  K2(launch(c, k_fc2d_error, a));
   K2(cudaMemcpyAsync(error, c->out + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   K2(cudaStreamSynchronize(c->stream));
   return 0;
@@ -492,8 +650,7 @@ extern "C" int fc2dgpu_ctx_solve(fc2dgpu_ctx* c, double tol, int max_iter, int e
            : error_evaluation == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT                ? 1
                                                                                                : 2;
   K2(cudaEventRecord(c->ev[0], c->stream));
-  k_fc2d_nsgs<<<1, NT, 0, c->stream>>>(a);
-  K2(cudaGetLastError());
+  K2(launch(c, k_fc2d_nsgs, a));
   K2(cudaEventRecord(c->ev[1], c->stream));
   double out[4];
   K2(cudaMemcpyAsync(out, c->out, sizeof(out), cudaMemcpyDeviceToHost, c->stream));

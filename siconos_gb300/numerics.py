@@ -237,6 +237,13 @@ ABI = {
     "fc2dgpu_ctx_compute_error": (C.c_int, [C.c_void_p, C.c_double, _DP]),
     "fc2dgpu_ctx_colours": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fc2dgpu_ctx_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "fc2dgpu_ctx_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "fc2dgpu_ctx_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "fc2dgpu_percolour_create": (C.c_void_p, [C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]),
+    "fc2dgpu_percolour_destroy": (None, [C.c_void_p]),
+    "fc2dgpu_percolour_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int), _DP,
+                                          C.POINTER(C.c_int), _DP]),
+    "fc2dgpu_percolour_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -592,6 +599,16 @@ class Fc2dContext:
             raise RuntimeError(last_error())
         return n, out
 
+    def set_launch(self, cluster_blocks: int = 0, threads: int = 0):
+        """Sweep launch shape (0 = automatic); returns the shape in use."""
+        _check(lib().fc2dgpu_ctx_set_launch(self.ctx, cluster_blocks, threads))
+        return self.launch_shape()
+
+    def launch_shape(self):
+        cs, nt = C.c_int(), C.c_int()
+        _check(lib().fc2dgpu_ctx_launch_shape(self.ctx, C.byref(cs), C.byref(nt)))
+        return cs.value, nt.value
+
     def trace(self, cap: int) -> np.ndarray:
         out = np.zeros(max(cap, 1))
         n = lib().fc2dgpu_ctx_trace(self.ctx, out.ctypes.data, cap)
@@ -601,6 +618,46 @@ class Fc2dContext:
         if getattr(self, "ctx", None):
             lib().fc2dgpu_ctx_destroy(self.ctx)
             self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Fc2dPerColour:
+    """The reference's per-colour GPU design for fc2d (cuSPARSE SpMV + local
+    solve per colour, a CUDA graph per sweep, host convergence test), for
+    measurement beside :class:`Fc2dContext` (``include/fc2dgpu_percolour.h``)."""
+
+    def __init__(self, nc, rowptr, colidx, blocks, q, mu, colouring: int = 0, device: int = 0):
+        self.nc = int(nc)
+        self.h = lib().fc2dgpu_percolour_create(device, self.nc, np.ascontiguousarray(rowptr, np.int64),
+                                                np.ascontiguousarray(colidx, np.int64),
+                                                np.ascontiguousarray(blocks, np.float64).reshape(-1),
+                                                np.ascontiguousarray(q, np.float64),
+                                                np.ascontiguousarray(mu, np.float64), colouring)
+        if not self.h:
+            raise RuntimeError(last_error())
+
+    def solve(self, tol: float, max_iter: int, r0=None) -> dict:
+        it, info = C.c_int(), C.c_int()
+        err, ms = C.c_double(), C.c_double()
+        r0p = None if r0 is None else np.ascontiguousarray(r0, np.float64)
+        _check(lib().fc2dgpu_percolour_solve(self.h, None if r0p is None else r0p.ctypes.data, tol, max_iter,
+                                             C.byref(it), C.byref(err), C.byref(info), C.byref(ms)))
+        return dict(iterations=it.value, error=err.value, info=info.value, ms=ms.value)
+
+    def get_r_u(self):
+        r, u = np.zeros(2 * self.nc), np.zeros(2 * self.nc)
+        _check(lib().fc2dgpu_percolour_get_r_u(self.h, r.ctypes.data, u.ctypes.data))
+        return r, u
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fc2dgpu_percolour_destroy(self.h)
+            self.h = None
 
     def __del__(self):
         try:

@@ -101,6 +101,30 @@ def test_driver_solves_fixture(sn, case):
     assert int(o.iparam[sn.SICONOS_IPARAM_ITER_DONE]) <= it1
 
 
+@pytest.mark.parametrize("shape", [(1, 32), (1, 512), (2, 64), (8, 128), (16, 32), (16, 512)])
+def test_launch_shape_does_not_change_iterates(sn, shape):
+    """Any cluster size and block size gives the same reaction bits; the
+    errors differ only by the order of their sums."""
+    import oracle as O
+    P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_02020_00213")
+    ctx = _ctx(sn, P)
+    _, colour = ctx.colours()
+    assert ctx.set_launch(*shape) == shape
+    res = ctx.solve(0.0, 25)
+    r, u = ctx.get_r_u()
+    ref = O.fc2d_nsgs_port(P, tol=0.0, maxiter=25, order=_order(colour))
+    np.testing.assert_array_equal(r, ref.r)
+    np.testing.assert_array_equal(u, ref.u)
+    assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
+    e = ctx.compute_error(float(np.sqrt(np.sum(P.q * P.q))))
+    assert e == pytest.approx(ref.error, rel=RTOL, abs=0)
+    with pytest.raises(RuntimeError):
+        ctx.set_launch(17, 0)
+    with pytest.raises(RuntimeError):
+        ctx.set_launch(1, 100)
+    ctx.close()
+
+
 def test_compute_error_matches_oracle(sn):
     import oracle as O
     P, g = load_fc2d("fc2d_FrictionContactProblem00237")
@@ -194,3 +218,28 @@ def test_q_change_reuses_layout(sn):
     np.testing.assert_array_equal(ra, rb)
     ctx.close()
     fresh.close()
+
+
+@pytest.mark.parametrize("case", ["fc2d_FC2D_SliderCrankLagrangian00000", "fc2d_fc2d_granularflowonwall_02020_00213"])
+def test_per_colour_design_solves_fixture(sn, case):
+    """The reference's per-colour GPU design (the comparator of the bench)
+    reaches the tolerance; its error is fc2d_compute_error of its reaction and
+    its iterates track the oracle's colour-ordered sweep to rounding."""
+    import oracle as O
+    P, g = load_fc2d(case)
+    pc = sn.Fc2dPerColour(P.nc, P.rowptr, P.colidx, P.blocks, P.q, P.mu)
+    res = pc.solve(1e-5, 10000)
+    r, u = pc.get_r_u()
+    assert res["info"] == 0 and res["error"] < 1e-5
+    e, u_ref = O.fc2d_compute_error_port(P, r)
+    assert e == pytest.approx(res["error"], rel=1e-14, abs=0)
+    np.testing.assert_array_equal(u, u_ref)
+    ctx = _ctx(sn, P)
+    _, colour = ctx.colours()
+    ctx.close()
+    short = pc.solve(0.0, 5)
+    r5, _ = pc.get_r_u()
+    ref = O.fc2d_nsgs_port(P, tol=0.0, maxiter=5, order=_order(colour))
+    assert short["iterations"] == 5
+    np.testing.assert_allclose(r5, ref.r, rtol=0, atol=1e-9 * max(1.0, np.abs(ref.r).max()))
+    pc.close()
