@@ -109,7 +109,12 @@ def test_launch_shape_does_not_change_iterates(sn, shape):
     P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_02020_00213")
     ctx = _ctx(sn, P)
     _, colour = ctx.colours()
-    assert ctx.set_launch(*shape) == shape
+    try:
+        got = ctx.set_launch(*shape)
+    except RuntimeError as e:
+        assert "does not fit" in str(e)
+        pytest.skip(f"cluster shape {shape} cannot be resident on this device")
+    assert got == shape
     res = ctx.solve(0.0, 25)
     r, u = ctx.get_r_u()
     ref = O.fc2d_nsgs_port(P, tol=0.0, maxiter=25, order=_order(colour))
