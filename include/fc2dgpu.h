@@ -88,10 +88,12 @@ int fc2dgpu_ctx_compute_error(fc2dgpu_ctx *ctx, double norm_q, double *error);
 int fc2dgpu_ctx_colours(fc2dgpu_ctx *ctx, int32_t *colour);
 /* Launch shape of the sweep kernel: a thread-block cluster of
  * cluster_blocks blocks (1..16) of `threads` threads (32..512, a multiple
- * of 32); 0 picks it from the largest colour (the default).  The iterates do
- * not depend on it; the reduction order of the errors does. */
-int fc2dgpu_ctx_set_launch(fc2dgpu_ctx *ctx, int cluster_blocks, int threads);
-int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx *ctx, int *cluster_blocks, int *threads);
+ * of 32), the reactions kept in HBM (reactions = 1) or replicated in every
+ * block's shared memory (2, up to 13,312 contacts); 0 picks each from the
+ * problem (the default).  The iterates do not depend on the shape; the
+ * reduction order of the errors does. */
+int fc2dgpu_ctx_set_launch(fc2dgpu_ctx *ctx, int cluster_blocks, int threads, int reactions);
+int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx *ctx, int *cluster_blocks, int *threads, int *reactions);
 /* Per-sweep light error of the last solve (cap entries); returns how many. */
 int fc2dgpu_ctx_trace(fc2dgpu_ctx *ctx, double *out, int cap);
 

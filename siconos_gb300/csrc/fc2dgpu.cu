@@ -28,6 +28,7 @@ constexpr int NT_MAX = 512;  // threads per block at most
 constexpr int CS_MAX = 16;   // blocks per cluster at most (non-portable size)
 constexpr int MAXC = 128;
 constexpr int TRACE_CAP = 1 << 16;
+constexpr size_t REP_MAX_BYTES = 208 * 1024;  // shared-memory copy of the reactions at most
 
 struct Args {
   int nc, ncol;
@@ -48,16 +49,31 @@ struct Args {
   double* out;  // [0] sweeps, [1] final error, [2] info, [3] last light error
 };
 
-// Reactions change during a solve and other blocks of the cluster write
-// them: they bypass L1 (ld.global.cg) so every read sees the cluster's
-// latest values after a cluster barrier.  W and the per-contact constants
-// are read-only and stay in the L1 of the block that owns the contact.
-__device__ __forceinline__ double2 ld_r(const double* r, int j) {
-  return __ldcg(reinterpret_cast<const double2*>(r) + j);
-}
-__device__ __forceinline__ void st_r(double* r, int j, double x0, double x1) {
-  __stcg(reinterpret_cast<double2*>(r) + j, make_double2(x0, x1));
-}
+// Where the sweep keeps the reactions.  Global: in HBM, read past L1
+// (ld.global.cg) so every block sees the cluster's latest values after a
+// cluster barrier.  Replicated: a full copy in the shared memory of every
+// block of the cluster; the owner of a contact writes its new reaction into
+// all copies (distributed shared memory stores), so every read in the sweep
+// is a local shared-memory load.  W and the per-contact constants are
+// read-only and stay in the L1 of the block that owns the contact.
+template <bool REP>
+struct Reactions {
+  double2* rs;  // this block's copy (REP)
+  double* r;    // global array
+  __device__ __forceinline__ double2 get(int j) const {
+    if (REP) return rs[j];
+    return __ldcg(reinterpret_cast<const double2*>(r) + j);
+  }
+  __device__ __forceinline__ void put(int j, double x0, double x1, cg::cluster_group& cl) const {
+    const double2 v = make_double2(x0, x1);
+    if (REP) {
+      const int cs = (int)cl.num_blocks();
+      for (int k = 0; k < cs; k++) cl.map_shared_rank(rs, k)[j] = v;
+    } else {
+      __stcg(reinterpret_cast<double2*>(r) + j, v);
+    }
+  }
+};
 
 __device__ __forceinline__ void mvp2x2(const double* a, const double2 v, double* y) {
   const double2 a01 = __ldg(reinterpret_cast<const double2*>(a));
@@ -70,9 +86,10 @@ __device__ __forceinline__ void mvp2x2(const double* a, const double2 v, double*
 
 // Cluster-wide sum of N values per thread, in a fixed order (xor-shuffle tree
 // in each warp, the warps in order, then the blocks in rank order), so every
-// block of the cluster gets the same bits.  `part` is a two-slot ring in
-// shared memory: a block writes slot k & 1 only after the barrier of call
-// k - 1, which every block passes after reading call k - 2's slot.
+// block of the cluster gets the same bits.  The cluster barrier inside also
+// orders every reaction update made before the call.  `part` is a two-slot
+// ring: a block writes slot k & 1 only after the barrier of call k - 1, which
+// every block passes after reading call k - 2's slot.
 struct Reduce {
   double part[2][4];
   double warp[NT_MAX / 32][4];
@@ -99,14 +116,20 @@ __device__ __forceinline__ void cluster_sum(double v[N], Reduce& R, cg::cluster_
     }
   }
   cl.sync();
-  if (threadIdx.x == 0) {
+  if (w == 0) {
+    // lane k fetches block k's partials (the remote loads overlap), lane 0
+    // adds them in rank order
     const int cs = (int)cl.num_blocks();
+    double mine[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) mine[i] = lane < cs ? cl.map_shared_rank(&R.part[slot][0], lane)[i] : 0.0;
+#pragma unroll
     for (int i = 0; i < N; i++) {
       double s = 0.0;
-      for (int k = 0; k < cs; k++) s += cl.map_shared_rank(&R.part[slot][0], k)[i];
-      R.bcast[i] = s;
+      for (int k = 0; k < cs; k++) s += __shfl_sync(0xffffffffu, mine[i], k);
+      if (lane == 0) R.bcast[i] = s;
     }
-    R.calls++;
+    if (lane == 0) R.calls++;
   }
   __syncthreads();
 #pragma unroll
@@ -117,14 +140,15 @@ __device__ __forceinline__ void cluster_sum(double v[N], Reduce& R, cg::cluster_
 // fc2d_compute_error (fc2d_compute_error.c:40-140): u = q + W r block by
 // block (per block w_i = 1.0 w_i + 1.0 (a_i0 r0 + a_i1 r1), the reference's
 // 2x2 gemv), natural-map error, relative to max(|r|, |u|, |q|).
-__device__ double full_error(const Args& a, Reduce& R, cg::cluster_group& cl) {
+template <bool REP>
+__device__ double full_error(const Args& a, const Reactions<REP>& rx, Reduce& R, cg::cluster_group& cl) {
   double v[3] = {0.0, 0.0, 0.0};
   const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
   for (int p = g0; p < a.nc; p += G) {
     double w[2] = {a.q[2 * p], a.q[2 * p + 1]};
     for (int s = a.rp[p]; s < a.rp[p + 1]; s++) {
       const double* blk = a.W + 4 * (size_t)s;
-      const double2 x = ld_r(a.r, a.col[s]);
+      const double2 x = rx.get(a.col[s]);
       for (int i = 0; i < 2; i++) {
         double t = 0.0;
         t += blk[i] * x.x;
@@ -132,8 +156,8 @@ __device__ double full_error(const Args& a, Reduce& R, cg::cluster_group& cl) {
         w[i] = 1.0 * w[i] + 1.0 * t;
       }
     }
-    st_r(a.u, p, w[0], w[1]);
-    const double2 rr = ld_r(a.r, p);
+    __stcg(reinterpret_cast<double2*>(a.u) + p, make_double2(w[0], w[1]));
+    const double2 rr = rx.get(p);
     const double r0 = rr.x, r1 = rr.y, mu = a.mu[p];
     double t0 = r0 - w[0] - mu * fabs(w[1]);
     double t1 = r1 - w[1];
@@ -180,17 +204,46 @@ __device__ __forceinline__ void local_solve(const double* W, double D, const dou
   }
 }
 
+// Copy the reactions into this block's replica; the cluster barrier keeps
+// other blocks from writing into it before the copy is done.
+template <bool REP>
+__device__ __forceinline__ Reactions<REP> open_reactions(const Args& a, double2* smem, cg::cluster_group& cl) {
+  Reactions<REP> rx{smem, a.r};
+  if (REP) {
+    for (int j = threadIdx.x; j < a.nc; j += blockDim.x) smem[j] = __ldcg(reinterpret_cast<const double2*>(a.r) + j);
+    cl.sync();
+  }
+  return rx;
+}
+
+// Write the replica back to HBM (each block its own contacts), then hold
+// every block until no other may still read its shared memory.
+template <bool REP>
+__device__ __forceinline__ void close_reactions(const Args& a, const Reactions<REP>& rx, cg::cluster_group& cl) {
+  if (REP) {
+    const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
+    for (int p = g0; p < a.nc; p += G) __stcg(reinterpret_cast<double2*>(a.r) + p, rx.rs[p]);
+  }
+  cl.sync();
+}
+
 // All sweeps of one problem in one launch of one thread-block cluster.  A
 // colour's contacts are spread over the cluster's threads (contact lo + g,
 // lo + g + G, ... for global thread g of G: a contact always lands on the
 // same block, so its W row stays in that SM's L1); the hardware cluster
-// barrier (release / acquire) separates colours, and the convergence logic
-// runs on the device with the same bits in every block.
+// barrier (release / acquire) separates colours, the barrier of the error
+// reduction closing the last one, and the convergence logic runs on the
+// device with the same bits in every block.  The light error's |r|^2 is
+// summed over the new reactions as they are made (each contact is updated
+// once per sweep, so it is |r|^2 after the sweep).
+template <bool REP>
 __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
+  extern __shared__ double2 rsm[];
   __shared__ Reduce R;
   cg::cluster_group cl = cg::this_cluster();
   if (threadIdx.x == 0) R.calls = 0;
   __syncthreads();
+  const Reactions<REP> rx = open_reactions<REP>(a, rsm, cl);
   const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
   const bool lead = cl.block_rank() == 0 && threadIdx.x == 0;
   double tolerance = a.tol, err = INFINITY;
@@ -200,25 +253,22 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
     double v[2] = {0.0, 0.0};
     for (int c = 0; c < a.ncol; c++) {
       for (int p = a.cptr[c] + g0; p < a.cptr[c + 1]; p += G) {
-        const double2 old = ld_r(a.r, p);
+        const double2 old = rx.get(p);
         double ql[2] = {a.q[2 * p], a.q[2 * p + 1]};
         const int s0 = a.rp[p], s1 = a.rp[p + 1], sd = s0 + a.dpos[p];
         // every block on the diagonal is left out (SBM_row_prod_no_diag_2x2)
         for (int s = s0; s < s1; s++) {
           const int j = a.col[s];
-          if (j != p) mvp2x2(a.W + 4 * (size_t)s, ld_r(a.r, j), ql);
+          if (j != p) mvp2x2(a.W + 4 * (size_t)s, rx.get(j), ql);
         }
         double P[2] = {old.x, old.y};
         local_solve(a.W + 4 * (size_t)sd, a.det[p], ql, a.mu[p], P);
         const double x0 = old.x - P[0], x1 = old.y - P[1];
         v[0] += x0 * x0 + x1 * x1;
-        st_r(a.r, p, P[0], P[1]);
+        v[1] += P[0] * P[0] + P[1] * P[1];
+        rx.put(p, P[0], P[1], cl);
       }
-      cl.sync();
-    }
-    for (int p = g0; p < a.nc; p += G) {
-      const double2 x = ld_r(a.r, p);
-      v[1] += x.x * x.x + x.y * x.y;
+      if (c + 1 < a.ncol) cl.sync();
     }
     cluster_sum<2>(v, R, cl);
     err = sqrt(v[0]);
@@ -230,7 +280,7 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
     } else if (a.mode == 0 && err < tolerance) {
       // determine_convergence_with_full_final (fc2d_nsgs.c:187-228)
       not_conv = 0;
-      const double full = full_error(a, R, cl);
+      const double full = full_error<REP>(a, rx, R, cl);
       if (full > a.tol) {
         tolerance = err / full * a.tol;
         not_conv = 1;
@@ -239,7 +289,7 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
   }
   const double light = err;
   if (a.mode == 0) {
-    err = full_error(a, R, cl);
+    err = full_error<REP>(a, rx, R, cl);
     not_conv = !(err < a.tol);
   } else if (a.mode == 2) {
     err = INFINITY;  // no branch of the sweep loop evaluates an error (fc2d_nsgs.c:438-448)
@@ -251,17 +301,20 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
     a.out[2] = not_conv;
     a.out[3] = light;
   }
-  cl.sync();  // no block leaves while another may still read its shared memory
+  close_reactions<REP>(a, rx, cl);
 }
 
+template <bool REP>
 __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_error(const Args a) {
+  extern __shared__ double2 rsm[];
   __shared__ Reduce R;
   cg::cluster_group cl = cg::this_cluster();
   if (threadIdx.x == 0) R.calls = 0;
   __syncthreads();
-  const double e = full_error(a, R, cl);
+  const Reactions<REP> rx = open_reactions<REP>(a, rsm, cl);
+  const double e = full_error<REP>(a, rx, R, cl);
   if (cl.block_rank() == 0 && threadIdx.x == 0) a.out[1] = e;
-  cl.sync();
+  close_reactions<REP>(a, rx, cl);
 }
 
 }  // namespace fc2dgpu
@@ -274,7 +327,9 @@ using namespace fc2dgpu;
 struct fc2dgpu_ctx {
   int device = 0;
   int cs_req = 0, nt_req = 0;  // launch shape asked for (0 = automatic)
+  int rep_req = 0;             // reactions: 0 automatic, 1 in HBM, 2 replicated in shared memory
   int cs = 1, nt = 128;        // launch shape of the current problem
+  bool rep = false;
   int max_colour = 0;          // contacts in the largest colour
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -498,15 +553,18 @@ extern "C" int fc2dgpu_ctx_set_r(fc2dgpu_ctx* c, const double* r) {
 }
 
 // Launch shape: a cluster of up to CS_MAX blocks.  The sweep is bound by
-// the FP64 pipes (about two FP64 operations per clock per SM on this part),
-// so a colour with more contacts is spread over more SMs; blocks of up to
-// NT_MAX threads keep each thread on one or two contacts per colour.
-static cudaLaunchConfig_t config(fc2dgpu_ctx* c, int cs, int nt, cudaLaunchAttribute* attr) {
+// the latency of each colour's dependent chain (loads, FP64 divisions,
+// barrier) and by the FP64 pipes (about two FP64 operations per clock per SM
+// on this part), so a colour with more contacts is spread over more SMs;
+// blocks of up to NT_MAX threads keep each thread on one or two contacts per
+// colour.  The reactions are replicated in every block's shared memory when
+// 16 bytes per contact fit (up to about 13,000 contacts), else kept in HBM.
+static cudaLaunchConfig_t config(fc2dgpu_ctx* c, int cs, int nt, size_t smem, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3(cs, 1, 1);
   cfg.blockDim = dim3(nt, 1, 1);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = c->stream;
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = cs;
@@ -517,17 +575,30 @@ static cudaLaunchConfig_t config(fc2dgpu_ctx* c, int cs, int nt, cudaLaunchAttri
   return cfg;
 }
 
+static size_t rep_bytes(const fc2dgpu_ctx* c) { return sizeof(double2) * (size_t)c->nc; }
+
+// Kernel attributes a launch of this shape needs (cluster size above the
+// portable 8, dynamic shared memory above 48 KiB).
+template <typename K>
+static cudaError_t prepare(K kernel, int cs, size_t smem) {
+  cudaError_t e = cudaSuccess;
+  if (cs > 8) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess && smem > 0) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return e;
+}
+
 // Whether a cluster of cs blocks of nt threads of the sweep kernel (the
 // larger of the two kernels) can be resident on this device.
-static bool cluster_fits(fc2dgpu_ctx* c, int cs, int nt) {
-  if (cs > 8 && cudaFuncSetAttribute(k_fc2d_nsgs, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
+static bool cluster_fits(fc2dgpu_ctx* c, int cs, int nt, bool rep) {
+  const size_t smem = rep ? rep_bytes(c) : 0;
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = config(c, cs, nt, attr);
+  cudaLaunchConfig_t cfg = config(c, cs, nt, smem, attr);
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs, &cfg) != cudaSuccess) {
+  cudaError_t e = rep ? prepare(k_fc2d_nsgs<true>, cs, smem) : prepare(k_fc2d_nsgs<false>, cs, smem);
+  if (e == cudaSuccess)
+    e = rep ? cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<true>, &cfg)
+            : cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<false>, &cfg);
+  if (e != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
@@ -544,32 +615,39 @@ static void choose_shape(fc2dgpu_ctx* c) {
   cs = std::min(std::max(cs, 1), CS_MAX);
   if (nt <= 0) nt = std::min(NT_MAX, std::max(32, ((c->max_colour + cs - 1) / cs + 31) / 32 * 32));
   nt = std::min(std::max(nt / 32 * 32, 32), NT_MAX);
+  bool rep = c->rep_req == 2 || (c->rep_req == 0 && rep_bytes(c) <= REP_MAX_BYTES);
+  if (rep && c->rep_req == 0 && !cluster_fits(c, cs, nt, true)) rep = false;
   if (c->cs_req <= 0)
-    while (cs > 1 && !cluster_fits(c, cs, nt)) cs /= 2;
+    while (cs > 1 && !cluster_fits(c, cs, nt, rep)) cs /= 2;
   c->cs = cs;
   c->nt = nt;
+  c->rep = rep;
 }
 
 template <typename K>
 static cudaError_t launch(fc2dgpu_ctx* c, K kernel, const Args& a) {
-  if (c->cs > 8) {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-  }
+  const size_t smem = c->rep ? rep_bytes(c) : 0;
+  cudaError_t e = prepare(kernel, c->cs, smem);
+  if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = config(c, c->cs, c->nt, attr);
+  cudaLaunchConfig_t cfg = config(c, c->cs, c->nt, smem, attr);
   return cudaLaunchKernelEx(&cfg, kernel, a);
 }
 
-extern "C" int fc2dgpu_ctx_set_launch(fc2dgpu_ctx* c, int cluster_blocks, int threads) {
+extern "C" int fc2dgpu_ctx_set_launch(fc2dgpu_ctx* c, int cluster_blocks, int threads, int reactions) {
   if (!c || cluster_blocks < 0 || cluster_blocks > CS_MAX || threads < 0 || threads > NT_MAX ||
-      (threads && threads % 32)) {
-    fc3dgpu_set_error("fc2dgpu_ctx_set_launch: cluster of 0..%d blocks, 0 or 32..%d threads (multiple of 32)",
-                      CS_MAX, NT_MAX);
+      (threads && threads % 32) || reactions < 0 || reactions > 2) {
+    fc3dgpu_set_error("fc2dgpu_ctx_set_launch: cluster of 0..%d blocks, 0 or 32..%d threads (multiple of 32), "
+                      "reactions 0, 1 or 2", CS_MAX, NT_MAX);
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (reactions == 2 && (c->nc == 0 || rep_bytes(c) > REP_MAX_BYTES)) {
+    fc3dgpu_set_error("fc2dgpu_ctx_set_launch: %d contacts do not fit a shared-memory copy", c->nc);
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
   if (cluster_blocks > 0) {
-    if (cudaSetDevice(c->device) != cudaSuccess || !cluster_fits(c, cluster_blocks, threads ? threads : NT_MAX)) {
+    const bool rep = reactions == 2 || (reactions == 0 && c->nc > 0 && rep_bytes(c) <= REP_MAX_BYTES);
+    if (cudaSetDevice(c->device) != cudaSuccess || !cluster_fits(c, cluster_blocks, threads ? threads : NT_MAX, rep)) {
       fc3dgpu_set_error("fc2dgpu_ctx_set_launch: a cluster of %d blocks of %d threads does not fit this device",
                         cluster_blocks, threads ? threads : NT_MAX);
       return NUMERICS_ERR_INVALID_ARGUMENT;
@@ -577,14 +655,16 @@ extern "C" int fc2dgpu_ctx_set_launch(fc2dgpu_ctx* c, int cluster_blocks, int th
   }
   c->cs_req = cluster_blocks;
   c->nt_req = threads;
-  choose_shape(c);
+  c->rep_req = reactions;
+  if (c->nc > 0) choose_shape(c);
   return 0;
 }
 
-extern "C" int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx* c, int* cluster_blocks, int* threads) {
+extern "C" int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx* c, int* cluster_blocks, int* threads, int* reactions) {
   if (!c) return NUMERICS_ERR_INVALID_ARGUMENT;
   if (cluster_blocks) *cluster_blocks = c->cs;
   if (threads) *threads = c->nt;
+  if (reactions) *reactions = c->rep ? 2 : 1;
   return 0;
 }
 
@@ -617,7 +697,7 @@ extern "C" int fc2dgpu_ctx_compute_error(fc2dgpu_ctx* c, double norm_q, double* 
   K2(cudaSetDevice(c->device));
   Args a = args_of(c);
   a.norm_q = norm_q;
-  K2(launch(c, k_fc2d_error, a));
+  K2(c->rep ? launch(c, k_fc2d_error<true>, a) : launch(c, k_fc2d_error<false>, a));
   K2(cudaMemcpyAsync(error, c->out + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   K2(cudaStreamSynchronize(c->stream));
   return 0;
@@ -650,7 +730,7 @@ extern "C" int fc2dgpu_ctx_solve(fc2dgpu_ctx* c, double tol, int max_iter, int e
            : error_evaluation == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT                ? 1
                                                                                                : 2;
   K2(cudaEventRecord(c->ev[0], c->stream));
-  K2(launch(c, k_fc2d_nsgs, a));
+  K2(c->rep ? launch(c, k_fc2d_nsgs<true>, a) : launch(c, k_fc2d_nsgs<false>, a));
   K2(cudaEventRecord(c->ev[1], c->stream));
   double out[4];
   K2(cudaMemcpyAsync(out, c->out, sizeof(out), cudaMemcpyDeviceToHost, c->stream));

@@ -237,8 +237,9 @@ ABI = {
     "fc2dgpu_ctx_compute_error": (C.c_int, [C.c_void_p, C.c_double, _DP]),
     "fc2dgpu_ctx_colours": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fc2dgpu_ctx_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
-    "fc2dgpu_ctx_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
-    "fc2dgpu_ctx_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "fc2dgpu_ctx_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "fc2dgpu_ctx_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int)]),
     "fc2dgpu_percolour_create": (C.c_void_p, [C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]),
     "fc2dgpu_percolour_destroy": (None, [C.c_void_p]),
     "fc2dgpu_percolour_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int), _DP,
@@ -599,15 +600,16 @@ class Fc2dContext:
             raise RuntimeError(last_error())
         return n, out
 
-    def set_launch(self, cluster_blocks: int = 0, threads: int = 0):
-        """Sweep launch shape (0 = automatic); returns the shape in use."""
-        _check(lib().fc2dgpu_ctx_set_launch(self.ctx, cluster_blocks, threads))
+    def set_launch(self, cluster_blocks: int = 0, threads: int = 0, reactions: int = 0):
+        """Sweep launch shape (0 = automatic; reactions 1 in HBM, 2 replicated
+        in shared memory); returns the shape in use."""
+        _check(lib().fc2dgpu_ctx_set_launch(self.ctx, cluster_blocks, threads, reactions))
         return self.launch_shape()
 
     def launch_shape(self):
-        cs, nt = C.c_int(), C.c_int()
-        _check(lib().fc2dgpu_ctx_launch_shape(self.ctx, C.byref(cs), C.byref(nt)))
-        return cs.value, nt.value
+        cs, nt, rx = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().fc2dgpu_ctx_launch_shape(self.ctx, C.byref(cs), C.byref(nt), C.byref(rx)))
+        return cs.value, nt.value, rx.value
 
     def trace(self, cap: int) -> np.ndarray:
         out = np.zeros(max(cap, 1))

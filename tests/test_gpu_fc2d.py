@@ -101,10 +101,11 @@ def test_driver_solves_fixture(sn, case):
     assert int(o.iparam[sn.SICONOS_IPARAM_ITER_DONE]) <= it1
 
 
-@pytest.mark.parametrize("shape", [(1, 32), (1, 512), (2, 64), (8, 128), (16, 32), (16, 512)])
+@pytest.mark.parametrize("shape", [(1, 32, 1), (1, 512, 2), (2, 64, 1), (8, 128, 2), (16, 32, 1), (16, 32, 2),
+                                   (16, 512, 1), (16, 128, 2)])
 def test_launch_shape_does_not_change_iterates(sn, shape):
-    """Any cluster size and block size gives the same reaction bits; the
-    errors differ only by the order of their sums."""
+    """Any cluster size, block size and place of the reactions gives the same
+    reaction bits; the errors differ only by the order of their sums."""
     import oracle as O
     P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_02020_00213")
     ctx = _ctx(sn, P)
@@ -123,10 +124,17 @@ def test_launch_shape_does_not_change_iterates(sn, shape):
     assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
     e = ctx.compute_error(float(np.sqrt(np.sum(P.q * P.q))))
     assert e == pytest.approx(ref.error, rel=RTOL, abs=0)
+    # a second solve continues from the reactions the first one left
+    ctx.solve(0.0, 3)
+    r2, _ = ctx.get_r_u()
+    ref2 = O.fc2d_nsgs_port(P, r0=ref.r, tol=0.0, maxiter=3, order=_order(colour))
+    np.testing.assert_array_equal(r2, ref2.r)
     with pytest.raises(RuntimeError):
         ctx.set_launch(17, 0)
     with pytest.raises(RuntimeError):
         ctx.set_launch(1, 100)
+    with pytest.raises(RuntimeError):
+        ctx.set_launch(1, 32, 3)
     ctx.close()
 
 
