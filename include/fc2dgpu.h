@@ -35,9 +35,13 @@ int fc2dgpu_nsgs_solve_wrap(void *problem, double *reaction, double *velocity, S
 int fc2dgpu_nsgs_init_wrap(void *problem, SolverOptions *options);
 void fc2dgpu_nsgs_free_wrap(void *problem, SolverOptions *options);
 /* fc2d_nsgs_set_default (fc2d_nsgs.c:787-792): no shuffle,
- * LIGHT_WITH_FULL_FINAL.  iparam[FC3DGPU_IPARAM_COLOURING] picks the
- * colouring (0 = FC3DGPU_COLOURING_DEFAULT); iparam[FC3DGPU_IPARAM_COLOURS]
- * and dparam[FC3DGPU_DPARAM_MS_SOLVE] report the colours and device time. */
+ * LIGHT_WITH_FULL_FINAL.  GPU knobs as for the 3D solver:
+ * iparam[FC3DGPU_IPARAM_PRECISION] 0 = FP32 sweeps + FP64 polish (default),
+ * 1 = FP64 sweeps only; dparam[FC3DGPU_DPARAM_SWITCH_TOL] and
+ * dparam[FC3DGPU_DPARAM_STALL] the switch (see fc2dgpu_ctx_set_precision);
+ * iparam[FC3DGPU_IPARAM_COLOURING] the colouring (0 = default).  Outputs:
+ * iparam[FC3DGPU_IPARAM_SWEEPS_FP32 / _FP64], iparam[FC3DGPU_IPARAM_COLOURS],
+ * dparam[FC3DGPU_DPARAM_MS_SOLVE]. */
 void fc2dgpu_nsgs_set_default(SolverOptions *options);
 /* Options as solver_options_create(SICONOS_FRICTION_2D_NSGS_GPU) gives them
  * once registered: max_iter 1000, tol 1e-4. */
@@ -77,6 +81,16 @@ int fc2dgpu_ctx_set_r(fc2dgpu_ctx *ctx, const double *r);
  * time.  Any output pointer may be NULL. */
 int fc2dgpu_ctx_solve(fc2dgpu_ctx *ctx, double tol, int max_iter, int error_evaluation, int *iters, double *error,
                       int *info, double *ms);
+/* Precision of the sweeps.  1 (a new context's default): FP64 sweeps only,
+ * the reference's iterates bit for bit.  0: FP32 sweeps until the FP32
+ * light error is below switch_tol (0 = max(tol / 10, 1e-6)) or has not
+ * reached a new low for stall_window sweeps (0 = 64), then the reference's
+ * FP64 loop from that iterate on the remaining budget; FP64 is slow on this
+ * GPU (about 64-cycle latency per operation, 550 for a division), FP32 an
+ * order of magnitude faster.  Both phases run back to back on the device. */
+int fc2dgpu_ctx_set_precision(fc2dgpu_ctx *ctx, int precision, double switch_tol, int stall_window);
+/* FP32 and FP64 sweeps of the last solve. */
+int fc2dgpu_ctx_last_sweeps(fc2dgpu_ctx *ctx, int *sweeps32, int *sweeps64);
 /* Reaction and velocity in contact order; the velocity is the one the last
  * fc2d_compute_error produced (LIGHT_WITH_FULL_FINAL only).  Either may be
  * NULL. */

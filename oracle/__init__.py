@@ -74,6 +74,8 @@ def port():
         lib.oracle_fc2d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
                                          C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
                                          C.POINTER(C.c_int)]
+        lib.oracle_fc2d_sweeps_f32.restype = C.c_int
+        lib.oracle_fc2d_sweeps_f32.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, C.c_int, C.c_void_p]
         lib.oracle_fc2d_compute_error.restype = C.c_double
         lib.oracle_fc2d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double]
         lib.oracle_fc3d_compute_error.restype = C.c_double
@@ -250,6 +252,22 @@ def fc2d_nsgs_ref(P: Problem, r0=None, tol=1e-5, maxiter=10000) -> Result:
                              np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64), r, u,
                              tol, maxiter, C.byref(it), C.byref(err))
     return Result(info, it.value, err.value, r, u, np.zeros(0))
+
+
+def fc2d_sweeps_f32_port(P: Problem, r0, nsweeps: int, order=None) -> np.ndarray:
+    """`nsweeps` single-precision sweeps from r0 (the FP32 phase of the GPU
+    solver's mixed mode, oracle/fc2d_oracle.c); the reaction widened to
+    double."""
+    r = np.ascontiguousarray(r0, dtype=np.float64).copy()
+    order_arr = None if order is None else np.ascontiguousarray(order, np.int32)
+    rc = port().oracle_fc2d_sweeps_f32(P.nc, np.ascontiguousarray(P.rowptr, np.int64),
+                                       np.ascontiguousarray(P.colidx, np.int64),
+                                       np.ascontiguousarray(P.blocks, np.float64).reshape(-1),
+                                       np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64),
+                                       r, nsweeps, None if order_arr is None else order_arr.ctypes.data)
+    if rc != 0:
+        raise ValueError("a contact has no diagonal block")
+    return r
 
 
 def fc2d_compute_error_port(P: Problem, r) -> tuple[float, np.ndarray]:

@@ -169,3 +169,86 @@ int oracle_fc2d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const
   free(det);
   return not_conv;
 }
+
+/* The FP32 phase of the GPU solver's mixed-precision mode, for checking it:
+ * `nsweeps` sweeps of the same algorithm in single precision, visiting
+ * contacts in `order`.  W, q, mu and the reaction are rounded to float, the
+ * diagonal determinants computed in float from the rounded blocks, every
+ * operation in float in the same order as the FP64 sweep (no contraction),
+ * and the reaction returned widened to double. */
+static void mvp2x2_f(const float *a, const float *v, float *r) {
+  r[0] += a[0] * v[0];
+  r[1] += a[1] * v[0];
+  r[0] += a[2] * v[1];
+  r[1] += a[3] * v[1];
+}
+
+static void local_solve_f(const float *W, float D, const float *q, float mu, float *P) {
+  const float Wnn = W[0], Wtn = W[1], Wnt = W[2], Wtt = W[3];
+  if (q[0] > 0) {
+    P[0] = 0;
+    P[1] = 0;
+  } else {
+    P[0] = -(Wtt * q[0] - Wnt * q[1]) / D;
+    P[1] = -(-Wtn * q[0] + Wnn * q[1]) / D;
+    float muPn = mu * P[0];
+    if (fabsf(P[1]) > muPn) {
+      if (P[1] + muPn < 0) {
+        P[0] = -q[0] / (Wnn - mu * Wnt);
+        P[1] = -mu * P[0];
+      } else {
+        P[0] = -q[0] / (Wnn + mu * Wnt);
+        P[1] = mu * P[0];
+      }
+    }
+  }
+}
+
+int oracle_fc2d_sweeps_f32(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                           const double *q, const double *mu, double *r, int nsweeps, const int32_t *order) {
+  const int64_t nnzb = rowptr[nc];
+  float *W = (float *)malloc(sizeof(float) * 4 * (size_t)(nnzb ? nnzb : 1));
+  float *qf = (float *)malloc(sizeof(float) * 2 * (size_t)nc);
+  float *mf = (float *)malloc(sizeof(float) * (size_t)nc);
+  float *rf = (float *)malloc(sizeof(float) * 2 * (size_t)nc);
+  float *det = (float *)malloc(sizeof(float) * (size_t)nc);
+  int64_t *diag = (int64_t *)malloc(sizeof(int64_t) * (size_t)nc);
+  int rc = 0;
+  for (int64_t k = 0; k < 4 * nnzb; k++) W[k] = (float)blocks[k];
+  for (int64_t k = 0; k < 2LL * nc; k++) {
+    qf[k] = (float)q[k];
+    rf[k] = (float)r[k];
+  }
+  for (int i = 0; i < nc; i++) {
+    mf[i] = (float)mu[i];
+    diag[i] = -1;
+    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      if (colidx[k] == i && diag[i] < 0) diag[i] = k;
+    if (diag[i] < 0) {
+      rc = -1;
+      goto done;
+    }
+    const float *b = &W[4 * diag[i]];
+    det[i] = b[0] * b[3] - b[1] * b[2];
+  }
+  for (int s = 0; s < nsweeps; s++)
+    for (int t = 0; t < nc; t++) {
+      const int c = order ? order[t] : t;
+      float loc[2] = {rf[2 * c], rf[2 * c + 1]};
+      float ql[2] = {qf[2 * c], qf[2 * c + 1]};
+      for (int64_t k = rowptr[c]; k < rowptr[c + 1]; k++)
+        if (colidx[k] != c) mvp2x2_f(&W[4 * k], &rf[2 * colidx[k]], ql);
+      local_solve_f(&W[4 * diag[c]], det[c], ql, mf[c], loc);
+      rf[2 * c] = loc[0];
+      rf[2 * c + 1] = loc[1];
+    }
+  for (int64_t k = 0; k < 2LL * nc; k++) r[k] = (double)rf[k];
+done:
+  free(W);
+  free(qf);
+  free(mf);
+  free(rf);
+  free(det);
+  free(diag);
+  return rc;
+}

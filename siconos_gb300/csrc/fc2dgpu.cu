@@ -30,54 +30,78 @@ constexpr int MAXC = 128;
 constexpr int TRACE_CAP = 1 << 16;
 constexpr size_t REP_MAX_BYTES = 208 * 1024;  // shared-memory copy of the reactions at most
 
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<double> {
+  using type = double2;
+};
+template <>
+struct Vec2<float> {
+  using type = float2;
+};
+
+// Sweep modes: the reference's error evaluations (fc2d_nsgs.c:438-448,
+// :496-500) in FP64, and the FP32 phase of the mixed-precision solve.
+enum Mode { FULL_FINAL = 0, LIGHT = 1, NO_EVAL = 2, FP32_PHASE = 3 };
+
+template <typename T>
 struct Args {
   int nc, ncol;
-  const int* cptr;    // ncol + 1 permuted-row bounds of the colours
-  const int* rp;      // nc + 1 slot pointer per permuted row
-  const int* col;     // permuted column of each slot
-  const int* dpos;    // offset in the row of its first diagonal block
-  const double* W;    // 4 per slot
-  const double* det;  // determinant of each row's diagonal block
-  const double* q;
-  const double* mu;
-  double* r;
+  const int* cptr;  // ncol + 1 permuted-row bounds of the colours
+  const int* rp;    // nc + 1 slot pointer per permuted row
+  const int* col;   // permuted column of each slot
+  const int* dpos;  // offset in the row of its first diagonal block
+  const T* W;       // 4 per slot
+  const T* det;     // determinant of each row's diagonal block
+  const T* q;
+  const T* mu;
+  double* r;        // the reactions (FP64, permuted order)
+  T* rw;            // the sweep's copy in HBM when it is not replicated
   double* u;
   double norm_q, tol;
   int max_iter;
-  int mode;  // 0 light with full final, 1 light, 2 no evaluation
+  int mode;
+  double switch_tol;      // FP32 phase: stop below this light error
+  int stall;              // FP32 phase: stop after this many sweeps without a new lowest error
+  const double* before;   // out[] of the phase run before this one (or null)
   double* trace;
   double* out;  // [0] sweeps, [1] final error, [2] info, [3] last light error
 };
 
-// Where the sweep keeps the reactions.  Global: in HBM, read past L1
-// (ld.global.cg) so every block sees the cluster's latest values after a
-// cluster barrier.  Replicated: a full copy in the shared memory of every
-// block of the cluster; the owner of a contact writes its new reaction into
-// all copies (distributed shared memory stores), so every read in the sweep
-// is a local shared-memory load.  W and the per-contact constants are
-// read-only and stay in the L1 of the block that owns the contact.
-template <bool REP>
+// Where the sweep keeps the reactions.  HBM: read past L1 (ld.global.cg)
+// so every block sees the cluster's latest values after a cluster barrier.
+// Replicated: a full copy in the shared memory of every block of the
+// cluster; the owner of a contact writes its new reaction into all copies
+// (distributed shared memory stores), so every read in the sweep is a local
+// shared-memory load.  W and the per-contact constants are read-only and
+// stay in the L1 of the block that owns the contact.
+template <typename T, bool REP>
 struct Reactions {
-  double2* rs;  // this block's copy (REP)
-  double* r;    // global array
-  __device__ __forceinline__ double2 get(int j) const {
+  using V = typename Vec2<T>::type;
+  V* rs;  // this block's copy (REP)
+  T* rw;  // HBM copy
+  __device__ __forceinline__ V get(int j) const {
     if (REP) return rs[j];
-    return __ldcg(reinterpret_cast<const double2*>(r) + j);
+    return __ldcg(reinterpret_cast<const V*>(rw) + j);
   }
-  __device__ __forceinline__ void put(int j, double x0, double x1, cg::cluster_group& cl) const {
-    const double2 v = make_double2(x0, x1);
+  __device__ __forceinline__ void put(int j, T x0, T x1, cg::cluster_group& cl) const {
+    V v;
+    v.x = x0;
+    v.y = x1;
     if (REP) {
       const int cs = (int)cl.num_blocks();
       for (int k = 0; k < cs; k++) cl.map_shared_rank(rs, k)[j] = v;
     } else {
-      __stcg(reinterpret_cast<double2*>(r) + j, v);
+      __stcg(reinterpret_cast<V*>(rw) + j, v);
     }
   }
 };
 
-__device__ __forceinline__ void mvp2x2(const double* a, const double2 v, double* y) {
-  const double2 a01 = __ldg(reinterpret_cast<const double2*>(a));
-  const double2 a23 = __ldg(reinterpret_cast<const double2*>(a) + 1);
+template <typename T, typename V>
+__device__ __forceinline__ void mvp2x2(const T* a, const V v, T* y) {
+  const V a01 = __ldg(reinterpret_cast<const V*>(a));
+  const V a23 = __ldg(reinterpret_cast<const V*>(a) + 1);
   y[0] += a01.x * v.x;
   y[1] += a01.y * v.x;
   y[0] += a23.x * v.y;
@@ -90,19 +114,20 @@ __device__ __forceinline__ void mvp2x2(const double* a, const double2 v, double*
 // orders every reaction update made before the call.  `part` is a two-slot
 // ring: a block writes slot k & 1 only after the barrier of call k - 1, which
 // every block passes after reading call k - 2's slot.
+template <typename T>
 struct Reduce {
-  double part[2][4];
-  double warp[NT_MAX / 32][4];
-  double bcast[4];
+  T part[2][4];
+  T warp[NT_MAX / 32][4];
+  T bcast[4];
   int calls;
 };
 
-template <int N>
-__device__ __forceinline__ void cluster_sum(double v[N], Reduce& R, cg::cluster_group& cl) {
+template <int N, typename T>
+__device__ __forceinline__ void cluster_sum(T v[N], Reduce<T>& R, cg::cluster_group& cl) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < N; i++) {
-    double x = v[i];
+    T x = v[i];
     for (int o = 16; o >= 1; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     if (lane == 0) R.warp[w][i] = x;
   }
@@ -110,7 +135,7 @@ __device__ __forceinline__ void cluster_sum(double v[N], Reduce& R, cg::cluster_
   const int slot = R.calls & 1;
   if (threadIdx.x == 0) {
     for (int i = 0; i < N; i++) {
-      double s = 0.0;
+      T s = 0;
       for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += R.warp[k][i];
       R.part[slot][i] = s;
     }
@@ -120,12 +145,12 @@ __device__ __forceinline__ void cluster_sum(double v[N], Reduce& R, cg::cluster_
     // lane k fetches block k's partials (the remote loads overlap), lane 0
     // adds them in rank order
     const int cs = (int)cl.num_blocks();
-    double mine[N];
+    T mine[N];
 #pragma unroll
-    for (int i = 0; i < N; i++) mine[i] = lane < cs ? cl.map_shared_rank(&R.part[slot][0], lane)[i] : 0.0;
+    for (int i = 0; i < N; i++) mine[i] = lane < cs ? cl.map_shared_rank(&R.part[slot][0], lane)[i] : T(0);
 #pragma unroll
     for (int i = 0; i < N; i++) {
-      double s = 0.0;
+      T s = 0;
       for (int k = 0; k < cs; k++) s += __shfl_sync(0xffffffffu, mine[i], k);
       if (lane == 0) R.bcast[i] = s;
     }
@@ -139,9 +164,10 @@ __device__ __forceinline__ void cluster_sum(double v[N], Reduce& R, cg::cluster_
 
 // fc2d_compute_error (fc2d_compute_error.c:40-140): u = q + W r block by
 // block (per block w_i = 1.0 w_i + 1.0 (a_i0 r0 + a_i1 r1), the reference's
-// 2x2 gemv), natural-map error, relative to max(|r|, |u|, |q|).
+// 2x2 gemv), natural-map error, relative to max(|r|, |u|, |q|).  FP64 only.
 template <bool REP>
-__device__ double full_error(const Args& a, const Reactions<REP>& rx, Reduce& R, cg::cluster_group& cl) {
+__device__ double full_error(const Args<double>& a, const Reactions<double, REP>& rx, Reduce<double>& R,
+                             cg::cluster_group& cl) {
   double v[3] = {0.0, 0.0, 0.0};
   const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
   for (int p = g0; p < a.nc; p += G) {
@@ -182,16 +208,17 @@ __device__ double full_error(const Args& a, const Reactions<REP>& rx, Reduce& R,
   return e;
 }
 
-// fc2d_nsgs_local_solve (fc2d_nsgs.c:212-252)
-__device__ __forceinline__ void local_solve(const double* W, double D, const double* q, double mu, double* P) {
-  const double Wnn = W[0], Wtn = W[1], Wnt = W[2], Wtt = W[3];
+// fc2d_nsgs_local_solve (fc2d_nsgs.c:212-252), in the working precision
+template <typename T>
+__device__ __forceinline__ void local_solve(const T* W, T D, const T* q, T mu, T* P) {
+  const T Wnn = W[0], Wtn = W[1], Wnt = W[2], Wtt = W[3];
   if (q[0] > 0) {
     P[0] = 0;
     P[1] = 0;
   } else {
     P[0] = -(Wtt * q[0] - Wnt * q[1]) / D;
     P[1] = -(-Wtn * q[0] + Wnn * q[1]) / D;
-    const double muPn = mu * P[0];
+    const T muPn = mu * P[0];
     if (fabs(P[1]) > muPn) {
       if (P[1] + muPn < 0) {
         P[0] = -q[0] / (Wnn - mu * Wnt);
@@ -204,66 +231,96 @@ __device__ __forceinline__ void local_solve(const double* W, double D, const dou
   }
 }
 
-// Copy the reactions into this block's replica; the cluster barrier keeps
-// other blocks from writing into it before the copy is done.
-template <bool REP>
-__device__ __forceinline__ Reactions<REP> open_reactions(const Args& a, double2* smem, cg::cluster_group& cl) {
-  Reactions<REP> rx{smem, a.r};
+// Bring the FP64 reactions into the sweep's copy (replica or FP32 copy in
+// HBM); the cluster barrier keeps other blocks from writing into a copy
+// before it is filled.
+template <typename T, bool REP>
+__device__ __forceinline__ Reactions<T, REP> open_reactions(const Args<T>& a, typename Vec2<T>::type* smem,
+                                                            cg::cluster_group& cl) {
+  using V = typename Vec2<T>::type;
+  Reactions<T, REP> rx{smem, a.rw};
+  const double2* r = reinterpret_cast<const double2*>(a.r);
   if (REP) {
-    for (int j = threadIdx.x; j < a.nc; j += blockDim.x) smem[j] = __ldcg(reinterpret_cast<const double2*>(a.r) + j);
+    for (int j = threadIdx.x; j < a.nc; j += blockDim.x) {
+      const double2 x = __ldcg(r + j);
+      V v;
+      v.x = (T)x.x;
+      v.y = (T)x.y;
+      smem[j] = v;
+    }
+    cl.sync();
+  } else if (sizeof(T) != sizeof(double)) {
+    const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
+    for (int j = g0; j < a.nc; j += G) {
+      const double2 x = __ldcg(r + j);
+      V v;
+      v.x = (T)x.x;
+      v.y = (T)x.y;
+      __stcg(reinterpret_cast<V*>(a.rw) + j, v);
+    }
     cl.sync();
   }
   return rx;
 }
 
-// Write the replica back to HBM (each block its own contacts), then hold
-// every block until no other may still read its shared memory.
-template <bool REP>
-__device__ __forceinline__ void close_reactions(const Args& a, const Reactions<REP>& rx, cg::cluster_group& cl) {
-  if (REP) {
+// Write the sweep's copy back to the FP64 reactions (each block its own
+// contacts), then hold every block until no other may still read its
+// shared memory.
+template <typename T, bool REP>
+__device__ __forceinline__ void close_reactions(const Args<T>& a, const Reactions<T, REP>& rx, cg::cluster_group& cl) {
+  if (REP || sizeof(T) != sizeof(double)) {
     const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
-    for (int p = g0; p < a.nc; p += G) __stcg(reinterpret_cast<double2*>(a.r) + p, rx.rs[p]);
+    for (int p = g0; p < a.nc; p += G) {
+      const typename Vec2<T>::type x = rx.get(p);
+      __stcg(reinterpret_cast<double2*>(a.r) + p, make_double2((double)x.x, (double)x.y));
+    }
   }
   cl.sync();
 }
 
-// All sweeps of one problem in one launch of one thread-block cluster.  A
-// colour's contacts are spread over the cluster's threads (contact lo + g,
-// lo + g + G, ... for global thread g of G: a contact always lands on the
-// same block, so its W row stays in that SM's L1); the hardware cluster
-// barrier (release / acquire) separates colours, the barrier of the error
-// reduction closing the last one, and the convergence logic runs on the
-// device with the same bits in every block.  The light error's |r|^2 is
-// summed over the new reactions as they are made (each contact is updated
-// once per sweep, so it is |r|^2 after the sweep).
-template <bool REP>
-__global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
-  extern __shared__ double2 rsm[];
-  __shared__ Reduce R;
+// All sweeps of one problem (or of one precision phase of it) in one launch
+// of one thread-block cluster.  A colour's contacts are spread over the
+// cluster's threads (contact lo + g, lo + g + G, ... for global thread g of
+// G: a contact always lands on the same block, so its W row stays in that
+// SM's L1); the hardware cluster barrier (release / acquire) separates
+// colours, the barrier of the error reduction closing the last one, and the
+// convergence logic runs on the device with the same bits in every block.
+// The light error's |r|^2 is summed over the new reactions as they are made
+// (each contact is updated once per sweep, so it is |r|^2 after the sweep).
+// A phase that follows another starts its sweep count, budget and trace
+// where the previous one stopped (read from the device, no host round trip).
+template <typename T, bool REP>
+__global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
+  using V = typename Vec2<T>::type;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  V* rsm = reinterpret_cast<V*>(dsm);
+  __shared__ Reduce<T> R;
   cg::cluster_group cl = cg::this_cluster();
   if (threadIdx.x == 0) R.calls = 0;
   __syncthreads();
-  const Reactions<REP> rx = open_reactions<REP>(a, rsm, cl);
+  const Reactions<T, REP> rx = open_reactions<T, REP>(a, rsm, cl);
   const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
   const bool lead = cl.block_rank() == 0 && threadIdx.x == 0;
-  double tolerance = a.tol, err = INFINITY;
-  int iter = 0, not_conv = 1;
-  while (iter < a.max_iter && not_conv) {
+  const int done = a.before ? (int)a.before[0] : 0;
+  const int budget = a.max_iter - done;
+  T tolerance = (T)a.tol, err = (T)INFINITY, best = (T)INFINITY;
+  int iter = 0, not_conv = 1, since_best = 0;
+  while (iter < budget && not_conv) {
     ++iter;
-    double v[2] = {0.0, 0.0};
+    T v[2] = {0, 0};
     for (int c = 0; c < a.ncol; c++) {
       for (int p = a.cptr[c] + g0; p < a.cptr[c + 1]; p += G) {
-        const double2 old = rx.get(p);
-        double ql[2] = {a.q[2 * p], a.q[2 * p + 1]};
+        const V old = rx.get(p);
+        T ql[2] = {a.q[2 * p], a.q[2 * p + 1]};
         const int s0 = a.rp[p], s1 = a.rp[p + 1], sd = s0 + a.dpos[p];
         // every block on the diagonal is left out (SBM_row_prod_no_diag_2x2)
         for (int s = s0; s < s1; s++) {
           const int j = a.col[s];
           if (j != p) mvp2x2(a.W + 4 * (size_t)s, rx.get(j), ql);
         }
-        double P[2] = {old.x, old.y};
-        local_solve(a.W + 4 * (size_t)sd, a.det[p], ql, a.mu[p], P);
-        const double x0 = old.x - P[0], x1 = old.y - P[1];
+        T P[2] = {old.x, old.y};
+        local_solve<T>(a.W + 4 * (size_t)sd, a.det[p], ql, a.mu[p], P);
+        const T x0 = old.x - P[0], x1 = old.y - P[1];
         v[0] += x0 * x0 + x1 * x1;
         v[1] += P[0] * P[0] + P[1] * P[1];
         rx.put(p, P[0], P[1], cl);
@@ -272,49 +329,61 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args a) {
     }
     cluster_sum<2>(v, R, cl);
     err = sqrt(v[0]);
-    const double nr = sqrt(v[1]);
-    if (fabs(nr) > DBL_EPSILON) err /= nr;
-    if (a.trace && lead && iter <= TRACE_CAP) a.trace[iter - 1] = err;
-    if (a.mode == 1) {
+    const T nr = sqrt(v[1]);
+    if (fabs(nr) > (T)DBL_EPSILON) err /= nr;
+    if (a.trace && lead && done + iter <= TRACE_CAP) a.trace[done + iter - 1] = (double)err;
+    if (a.mode == FP32_PHASE) {
+      if (err < best) {
+        best = err;
+        since_best = 0;
+      } else {
+        since_best++;
+      }
+      not_conv = !(err < (T)a.switch_tol) && since_best < a.stall;
+    } else if (a.mode == LIGHT) {
       not_conv = !(err < tolerance);  // determine_convergence (fc2d_nsgs.c:147-162)
-    } else if (a.mode == 0 && err < tolerance) {
+    } else if (a.mode == FULL_FINAL && err < tolerance) {
       // determine_convergence_with_full_final (fc2d_nsgs.c:187-228)
       not_conv = 0;
-      const double full = full_error<REP>(a, rx, R, cl);
-      if (full > a.tol) {
-        tolerance = err / full * a.tol;
-        not_conv = 1;
+      if constexpr (sizeof(T) == sizeof(double)) {
+        const double full = full_error<REP>(a, rx, R, cl);
+        if (full > a.tol) {
+          tolerance = err / full * a.tol;
+          not_conv = 1;
+        }
       }
     }
   }
-  const double light = err;
-  if (a.mode == 0) {
-    err = full_error<REP>(a, rx, R, cl);
-    not_conv = !(err < a.tol);
-  } else if (a.mode == 2) {
-    err = INFINITY;  // no branch of the sweep loop evaluates an error (fc2d_nsgs.c:438-448)
-    not_conv = 1;
+  double final_err = (double)err;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (a.mode == FULL_FINAL) {
+      final_err = full_error<REP>(a, rx, R, cl);
+      not_conv = !(final_err < a.tol);
+    } else if (a.mode == NO_EVAL) {
+      final_err = INFINITY;  // no branch of the sweep loop evaluates an error (fc2d_nsgs.c:438-448)
+      not_conv = 1;
+    }
   }
   if (lead) {
-    a.out[0] = iter;
-    a.out[1] = err;
+    a.out[0] = done + iter;
+    a.out[1] = final_err;
     a.out[2] = not_conv;
-    a.out[3] = light;
+    a.out[3] = (double)err;
   }
-  close_reactions<REP>(a, rx, cl);
+  close_reactions<T, REP>(a, rx, cl);
 }
 
 template <bool REP>
-__global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_error(const Args a) {
-  extern __shared__ double2 rsm[];
-  __shared__ Reduce R;
+__global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_error(const Args<double> a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ Reduce<double> R;
   cg::cluster_group cl = cg::this_cluster();
   if (threadIdx.x == 0) R.calls = 0;
   __syncthreads();
-  const Reactions<REP> rx = open_reactions<REP>(a, rsm, cl);
+  const Reactions<double, REP> rx = open_reactions<double, REP>(a, reinterpret_cast<double2*>(dsm), cl);
   const double e = full_error<REP>(a, rx, R, cl);
   if (cl.block_rank() == 0 && threadIdx.x == 0) a.out[1] = e;
-  close_reactions<REP>(a, rx, cl);
+  close_reactions<double, REP>(a, rx, cl);
 }
 
 }  // namespace fc2dgpu
@@ -340,6 +409,12 @@ struct fc2dgpu_ctx {
   int *cptr = nullptr, *rp = nullptr, *col = nullptr, *dpos = nullptr;
   double *W = nullptr, *det = nullptr, *q = nullptr, *mu = nullptr, *r = nullptr, *u = nullptr, *trace = nullptr,
          *out = nullptr;
+  // FP32 copies for the first phase of a mixed-precision solve
+  float *W32 = nullptr, *det32 = nullptr, *q32 = nullptr, *mu32 = nullptr, *r32 = nullptr;
+  int precision = 1;          // 0 FP32 sweeps + FP64 polish, 1 FP64 sweeps only
+  double switch_tol = 0.0;    // FP32 phase stops below this light error (0: max(tol / 10, 1e-6))
+  int stall = 64;             // ... or after this many sweeps without a new lowest error
+  int sweeps32 = 0, sweeps64 = 0;
   int trace_len = 0;
 };
 
@@ -355,11 +430,13 @@ struct fc2dgpu_ctx {
 static void choose_shape(fc2dgpu_ctx* c);
 
 static void free_problem(fc2dgpu_ctx* c) {
-  void* ptrs[] = {c->cptr, c->rp, c->col, c->dpos, c->W, c->det, c->q, c->mu, c->r, c->u};
+  void* ptrs[] = {c->cptr, c->rp, c->col, c->dpos, c->W, c->det, c->q, c->mu, c->r, c->u,
+                  c->W32, c->det32, c->q32, c->mu32, c->r32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   c->cptr = c->rp = c->col = c->dpos = nullptr;
   c->W = c->det = c->q = c->mu = c->r = c->u = nullptr;
+  c->W32 = c->det32 = c->q32 = c->mu32 = c->r32 = nullptr;
   c->nc = 0;
 }
 
@@ -499,6 +576,20 @@ extern "C" int fc2dgpu_ctx_set_problem(fc2dgpu_ctx* c, int nc, const int64_t* ro
   if (e == cudaSuccess) e = upload(&c->mu, mup);
   if (e == cudaSuccess) e = upload(&c->r, zero);
   if (e == cudaSuccess) e = upload(&c->u, zero);
+  // FP32 copies; the determinants of the rounded blocks, in FP32
+  {
+    std::vector<float> W32(W.begin(), W.end()), det32(nc), q32(qp.begin(), qp.end()), mu32(mup.begin(), mup.end());
+    for (int p = 0; p < nc; p++) {
+      const float* b = &W32[4 * ((size_t)rp[p] + dpos[p])];
+      det32[p] = b[0] * b[3] - b[1] * b[2];
+    }
+    std::vector<float> zero32(2 * (size_t)nc, 0.0f);
+    if (e == cudaSuccess) e = upload(&c->W32, W32);
+    if (e == cudaSuccess) e = upload(&c->det32, det32);
+    if (e == cudaSuccess) e = upload(&c->q32, q32);
+    if (e == cudaSuccess) e = upload(&c->mu32, mu32);
+    if (e == cudaSuccess) e = upload(&c->r32, zero32);
+  }
   if (e != cudaSuccess) {
     free_problem(c);
     fc3dgpu_set_error("fc2dgpu_ctx_set_problem: %s", cudaGetErrorString(e));
@@ -536,6 +627,9 @@ extern "C" int fc2dgpu_ctx_set_q_mu(fc2dgpu_ctx* c, const double* q, const doubl
   K2(cudaSetDevice(c->device));
   K2(cudaMemcpy(c->q, qp.data(), sizeof(double) * qp.size(), cudaMemcpyHostToDevice));
   K2(cudaMemcpy(c->mu, mup.data(), sizeof(double) * mup.size(), cudaMemcpyHostToDevice));
+  const std::vector<float> q32(qp.begin(), qp.end()), mu32(mup.begin(), mup.end());
+  K2(cudaMemcpy(c->q32, q32.data(), sizeof(float) * q32.size(), cudaMemcpyHostToDevice));
+  K2(cudaMemcpy(c->mu32, mu32.data(), sizeof(float) * mu32.size(), cudaMemcpyHostToDevice));
   c->norm_q = sqrt(s2);
   return 0;
 }
@@ -594,10 +688,10 @@ static bool cluster_fits(fc2dgpu_ctx* c, int cs, int nt, bool rep) {
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = config(c, cs, nt, smem, attr);
   int n = 0;
-  cudaError_t e = rep ? prepare(k_fc2d_nsgs<true>, cs, smem) : prepare(k_fc2d_nsgs<false>, cs, smem);
+  cudaError_t e = rep ? prepare(k_fc2d_nsgs<double, true>, cs, smem) : prepare(k_fc2d_nsgs<double, false>, cs, smem);
   if (e == cudaSuccess)
-    e = rep ? cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<true>, &cfg)
-            : cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<false>, &cfg);
+    e = rep ? cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<double, true>, &cfg)
+            : cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<double, false>, &cfg);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return false;
@@ -624,9 +718,8 @@ static void choose_shape(fc2dgpu_ctx* c) {
   c->rep = rep;
 }
 
-template <typename K>
-static cudaError_t launch(fc2dgpu_ctx* c, K kernel, const Args& a) {
-  const size_t smem = c->rep ? rep_bytes(c) : 0;
+template <typename K, typename A>
+static cudaError_t launch(fc2dgpu_ctx* c, K kernel, const A& a, size_t smem) {
   cudaError_t e = prepare(kernel, c->cs, smem);
   if (e != cudaSuccess) return e;
   cudaLaunchAttribute attr[1];
@@ -668,8 +761,8 @@ extern "C" int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx* c, int* cluster_blocks, int
   return 0;
 }
 
-static Args args_of(const fc2dgpu_ctx* c) {
-  Args a;
+static Args<double> args64(const fc2dgpu_ctx* c) {
+  Args<double> a;
   memset(&a, 0, sizeof(a));
   a.nc = c->nc;
   a.ncol = c->ncol;
@@ -682,11 +775,52 @@ static Args args_of(const fc2dgpu_ctx* c) {
   a.q = c->q;
   a.mu = c->mu;
   a.r = c->r;
+  a.rw = c->r;
   a.u = c->u;
   a.norm_q = c->norm_q;
   a.trace = c->trace;
   a.out = c->out;
   return a;
+}
+
+static Args<float> args32(const fc2dgpu_ctx* c) {
+  Args<float> a;
+  memset(&a, 0, sizeof(a));
+  a.nc = c->nc;
+  a.ncol = c->ncol;
+  a.cptr = c->cptr;
+  a.rp = c->rp;
+  a.col = c->col;
+  a.dpos = c->dpos;
+  a.W = c->W32;
+  a.det = c->det32;
+  a.q = c->q32;
+  a.mu = c->mu32;
+  a.r = c->r;
+  a.rw = c->r32;
+  a.u = c->u;
+  a.norm_q = c->norm_q;
+  a.trace = c->trace;
+  a.out = c->out + 4;
+  return a;
+}
+
+extern "C" int fc2dgpu_ctx_set_precision(fc2dgpu_ctx* c, int precision, double switch_tol, int stall_window) {
+  if (!c || precision < 0 || precision > 1 || !(switch_tol >= 0.0) || stall_window < 0) {
+    fc3dgpu_set_error("fc2dgpu_ctx_set_precision: precision 0 or 1, switch_tol >= 0, stall_window >= 0");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  c->precision = precision;
+  c->switch_tol = switch_tol;
+  c->stall = stall_window > 0 ? stall_window : 64;
+  return 0;
+}
+
+extern "C" int fc2dgpu_ctx_last_sweeps(fc2dgpu_ctx* c, int* sweeps32, int* sweeps64) {
+  if (!c) return NUMERICS_ERR_INVALID_ARGUMENT;
+  if (sweeps32) *sweeps32 = c->sweeps32;
+  if (sweeps64) *sweeps64 = c->sweeps64;
+  return 0;
 }
 
 extern "C" int fc2dgpu_ctx_compute_error(fc2dgpu_ctx* c, double norm_q, double* error) {
@@ -695,9 +829,9 @@ extern "C" int fc2dgpu_ctx_compute_error(fc2dgpu_ctx* c, double norm_q, double* 
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
   K2(cudaSetDevice(c->device));
-  Args a = args_of(c);
+  Args<double> a = args64(c);
   a.norm_q = norm_q;
-  K2(c->rep ? launch(c, k_fc2d_error<true>, a) : launch(c, k_fc2d_error<false>, a));
+  K2(c->rep ? launch(c, k_fc2d_error<true>, a, rep_bytes(c)) : launch(c, k_fc2d_error<false>, a, 0));
   K2(cudaMemcpyAsync(error, c->out + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   K2(cudaStreamSynchronize(c->stream));
   return 0;
@@ -723,16 +857,32 @@ extern "C" int fc2dgpu_ctx_solve(fc2dgpu_ctx* c, double tol, int max_iter, int e
     return 0;
   }
   K2(cudaSetDevice(c->device));
-  Args a = args_of(c);
+  Args<double> a = args64(c);
   a.tol = tol;
   a.max_iter = max_iter;
-  a.mode = error_evaluation == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL ? 0
-           : error_evaluation == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT                ? 1
-                                                                                               : 2;
+  a.mode = error_evaluation == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL ? FULL_FINAL
+           : error_evaluation == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT                ? LIGHT
+                                                                                               : NO_EVAL;
+  // mixed precision: FP32 sweeps first (for the two modes that stop on an
+  // error), then the FP64 sweeps of the reference's loop from their iterate,
+  // on the budget and trace position the FP32 phase leaves (read on the
+  // device: both launches go out back to back)
+  const bool mixed = c->precision == 0 && a.mode != NO_EVAL && max_iter > 0;
   K2(cudaEventRecord(c->ev[0], c->stream));
-  K2(c->rep ? launch(c, k_fc2d_nsgs<true>, a) : launch(c, k_fc2d_nsgs<false>, a));
+  if (mixed) {
+    Args<float> b = args32(c);
+    b.tol = tol;
+    b.max_iter = max_iter;
+    b.mode = FP32_PHASE;
+    b.switch_tol = c->switch_tol > 0.0 ? c->switch_tol : std::max(0.1 * tol, 1e-6);
+    b.stall = c->stall;
+    K2(c->rep ? launch(c, k_fc2d_nsgs<float, true>, b, sizeof(float2) * (size_t)c->nc)
+              : launch(c, k_fc2d_nsgs<float, false>, b, 0));
+    a.before = c->out + 4;
+  }
+  K2(c->rep ? launch(c, k_fc2d_nsgs<double, true>, a, rep_bytes(c)) : launch(c, k_fc2d_nsgs<double, false>, a, 0));
   K2(cudaEventRecord(c->ev[1], c->stream));
-  double out[4];
+  double out[8];
   K2(cudaMemcpyAsync(out, c->out, sizeof(out), cudaMemcpyDeviceToHost, c->stream));
   K2(cudaStreamSynchronize(c->stream));
   float t = 0.f;
@@ -741,6 +891,8 @@ extern "C" int fc2dgpu_ctx_solve(fc2dgpu_ctx* c, double tol, int max_iter, int e
   if (error) *error = out[1];
   if (info) *info = (int)out[2];
   if (ms) *ms = t;
+  c->sweeps32 = mixed ? (int)out[4] : 0;
+  c->sweeps64 = (int)out[0] - c->sweeps32;
   c->trace_len = std::min((int)out[0], TRACE_CAP);
   return 0;
 }

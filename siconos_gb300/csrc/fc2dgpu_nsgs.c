@@ -151,6 +151,15 @@ int fc2dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velo
   if (rc == 1) rc = fc2dgpu_ctx_set_q_mu(ctx, problem->q, problem->mu);
   if (!rc) rc = fc2dgpu_ctx_set_r(ctx, reaction);
   if (rc) return rc;
+  const int prec = options->iparam[FC3DGPU_IPARAM_PRECISION];
+  if (prec != 0 && prec != 1) {
+    fc3dgpu_set_error("iparam[FC3DGPU_IPARAM_PRECISION] must be 0 (FP32 + FP64 polish) or 1 (FP64)");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  const double sw = options->dparam[FC3DGPU_DPARAM_SWITCH_TOL];
+  const double stall = options->dparam[FC3DGPU_DPARAM_STALL];
+  rc = fc2dgpu_ctx_set_precision(ctx, prec, sw > 0 ? sw : 0.0, stall > 0 ? (int)stall : 0);
+  if (rc) return rc;
   const int eval = options->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION];
   int iters = 0, info = 1;
   double error = INFINITY, ms = 0.0;
@@ -164,6 +173,8 @@ int fc2dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velo
   options->iparam[SICONOS_IPARAM_ITER_DONE] = iters;
   options->dparam[SICONOS_DPARAM_RESIDU] = error;
   options->iparam[FC3DGPU_IPARAM_COLOURS] = fc2dgpu_ctx_colours(ctx, NULL);
+  fc2dgpu_ctx_last_sweeps(ctx, &options->iparam[FC3DGPU_IPARAM_SWEEPS_FP32],
+                          &options->iparam[FC3DGPU_IPARAM_SWEEPS_FP64]);
   options->dparam[FC3DGPU_DPARAM_MS_SOLVE] = ms;
   if (options->callback && options->callback->collectStatsIteration && iters > 0) {
     /* the sweeps run on the device: the per-iteration callback is replayed

@@ -240,6 +240,8 @@ ABI = {
     "fc2dgpu_ctx_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "fc2dgpu_ctx_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                            C.POINTER(C.c_int)]),
+    "fc2dgpu_ctx_set_precision": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
+    "fc2dgpu_ctx_last_sweeps": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "fc2dgpu_percolour_create": (C.c_void_p, [C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]),
     "fc2dgpu_percolour_destroy": (None, [C.c_void_p]),
     "fc2dgpu_percolour_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int), _DP,
@@ -599,6 +601,17 @@ class Fc2dContext:
         if n < 0:
             raise RuntimeError(last_error())
         return n, out
+
+    def set_precision(self, precision: int, switch_tol: float = 0.0, stall_window: int = 0):
+        """0: FP32 sweeps, then the FP64 sweeps of the reference's loop from
+        their iterate; 1: FP64 sweeps only (the default of a context)."""
+        _check(lib().fc2dgpu_ctx_set_precision(self.ctx, precision, switch_tol, stall_window))
+
+    def last_sweeps(self):
+        """(FP32 sweeps, FP64 sweeps) of the last solve."""
+        a, b = C.c_int(), C.c_int()
+        _check(lib().fc2dgpu_ctx_last_sweeps(self.ctx, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_launch(self, cluster_blocks: int = 0, threads: int = 0, reactions: int = 0):
         """Sweep launch shape (0 = automatic; reactions 1 in HBM, 2 replicated

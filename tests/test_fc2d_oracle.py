@@ -68,6 +68,19 @@ def test_port_order_permutes_sweep():
     assert not np.array_equal(a.r, c.r)
 
 
+def test_f32_sweeps_track_f64():
+    """The single-precision restatement follows the FP64 sweep to FP32
+    rounding (it is the checker of the GPU's FP32 phase)."""
+    import oracle as O
+    P, _ = load_fc2d("fc2d_FrictionContactProblem00071")
+    r32 = O.fc2d_sweeps_f32_port(P, np.zeros(2 * P.nc), 30)
+    ref = O.fc2d_nsgs_port(P, tol=0.0, maxiter=30)
+    assert np.abs(r32 - ref.r).max() <= 1e-5 * np.abs(ref.r).max()
+    assert not np.array_equal(r32, ref.r)
+    again = O.fc2d_sweeps_f32_port(P, r32, 0)
+    np.testing.assert_array_equal(again, r32)
+
+
 def test_port_singular_diagonal_block():
     import oracle as O
     rowptr = np.array([0, 1, 2], np.int64)
@@ -99,6 +112,7 @@ def test_options_defaults(built_lib):
     assert o.iparam[sn.SICONOS_IPARAM_MAX_ITER] == 1000
     assert o.dparam[sn.SICONOS_DPARAM_TOL] == 1e-4
     assert o.iparam[sn.SICONOS_IPARAM_NSGS_SHUFFLE] == 0
+    assert o.iparam[sn.FC3DGPU_IPARAM_PRECISION] == 0  # FP32 sweeps + FP64 polish
     assert o.iparam[sn.SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] == \
         sn.SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL
     o.iparam[sn.SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = sn.SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT

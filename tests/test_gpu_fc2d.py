@@ -256,3 +256,50 @@ def test_per_colour_design_solves_fixture(sn, case):
     assert short["iterations"] == 5
     np.testing.assert_allclose(r5, ref.r, rtol=0, atol=1e-9 * max(1.0, np.abs(ref.r).max()))
     pc.close()
+
+
+def test_fp32_phase_bit_exact(sn):
+    """The FP32 phase of the mixed mode is the single-precision sweep of the
+    oracle (oracle_fc2d_sweeps_f32) in colour order, bit for bit: 20 FP32
+    sweeps (switch never reached), no FP64 budget left, the FP64 error of
+    that iterate."""
+    import oracle as O
+    P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_02020_00213")
+    ctx = _ctx(sn, P)
+    _, colour = ctx.colours()
+    ctx.set_precision(0, 1e-30, 1 << 20)
+    res = ctx.solve(1e-5, 20)
+    assert ctx.last_sweeps() == (20, 0) and res["iterations"] == 20
+    r, u = ctx.get_r_u()
+    r32 = O.fc2d_sweeps_f32_port(P, np.zeros(2 * P.nc), 20, order=_order(colour))
+    np.testing.assert_array_equal(r, r32)
+    e, u_ref = O.fc2d_compute_error_port(P, r32)
+    np.testing.assert_array_equal(u, u_ref)
+    assert res["error"] == pytest.approx(e, rel=RTOL, abs=0)
+    ctx.close()
+
+
+@pytest.mark.parametrize("case", FC2D_CASES)
+def test_mixed_precision_solve(sn, case):
+    """FP32 sweeps then the reference's FP64 loop: the result is the oracle's
+    FP64 loop started from the oracle's FP32 iterate after the same number of
+    FP32 sweeps, bit for bit, and it meets the tolerance the reference
+    meets."""
+    import oracle as O
+    P, g = load_fc2d(case)
+    ctx = _ctx(sn, P)
+    _, colour = ctx.colours()
+    order = _order(colour)
+    ctx.set_precision(0)
+    res = ctx.solve(1e-5, 10000)
+    s32, s64 = ctx.last_sweeps()
+    assert s32 + s64 == res["iterations"] and s32 >= 1
+    r, u = ctx.get_r_u()
+    r32 = O.fc2d_sweeps_f32_port(P, np.zeros(2 * P.nc), s32, order=order)
+    ref = O.fc2d_nsgs_port(P, r0=r32, tol=1e-5, maxiter=10000 - s32, order=order)
+    assert (res["info"], s64) == (ref.info, ref.iterations)
+    np.testing.assert_array_equal(r, ref.r)
+    np.testing.assert_array_equal(u, ref.u)
+    assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
+    assert res["info"] == int(g["info"]) == 0 and res["error"] < 1e-5
+    ctx.close()
