@@ -83,7 +83,7 @@ int fc2dgpu_ctx_solve(fc2dgpu_ctx *ctx, double tol, int max_iter, int error_eval
                       int *info, double *ms);
 /* Precision of the sweeps.  1 (a new context's default): FP64 sweeps only,
  * the reference's iterates bit for bit.  0: FP32 sweeps until the FP32
- * light error is below switch_tol (0 = max(tol / 10, 1e-6)) or has not
+ * light error is below switch_tol (0 = max(tol, 1e-6)) or has not
  * reached a new low for stall_window sweeps (0 = 64), then the reference's
  * FP64 loop from that iterate on the remaining budget; FP64 is slow on this
  * GPU (about 64-cycle latency per operation, 550 for a division), FP32 an

@@ -98,6 +98,15 @@ struct Reactions {
   }
 };
 
+// Barrier between colours: the hardware cluster barrier (about 670 cycles on
+// this part), or the block barrier (about 290) when the cluster is one block.
+__device__ __forceinline__ void colour_sync(cg::cluster_group& cl) {
+  if (cl.num_blocks() == 1)
+    __syncthreads();
+  else
+    cl.sync();
+}
+
 template <typename T, typename V>
 __device__ __forceinline__ void mvp2x2(const T* a, const V v, T* y) {
   const V a01 = __ldg(reinterpret_cast<const V*>(a));
@@ -140,7 +149,7 @@ __device__ __forceinline__ void cluster_sum(T v[N], Reduce<T>& R, cg::cluster_gr
       R.part[slot][i] = s;
     }
   }
-  cl.sync();
+  colour_sync(cl);
   if (w == 0) {
     // lane k fetches block k's partials (the remote loads overlap), lane 0
     // adds them in rank order
@@ -325,7 +334,7 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
         v[1] += P[0] * P[0] + P[1] * P[1];
         rx.put(p, P[0], P[1], cl);
       }
-      if (c + 1 < a.ncol) cl.sync();
+      if (c + 1 < a.ncol) colour_sync(cl);
     }
     cluster_sum<2>(v, R, cl);
     err = sqrt(v[0]);
@@ -412,7 +421,7 @@ struct fc2dgpu_ctx {
   // FP32 copies for the first phase of a mixed-precision solve
   float *W32 = nullptr, *det32 = nullptr, *q32 = nullptr, *mu32 = nullptr, *r32 = nullptr;
   int precision = 1;          // 0 FP32 sweeps + FP64 polish, 1 FP64 sweeps only
-  double switch_tol = 0.0;    // FP32 phase stops below this light error (0: max(tol / 10, 1e-6))
+  double switch_tol = 0.0;    // FP32 phase stops below this light error (0: max(tol, 1e-6))
   int stall = 64;             // ... or after this many sweeps without a new lowest error
   int sweeps32 = 0, sweeps64 = 0;
   int trace_len = 0;
@@ -709,7 +718,9 @@ static void choose_shape(fc2dgpu_ctx* c) {
   cs = std::min(std::max(cs, 1), CS_MAX);
   if (nt <= 0) nt = std::min(NT_MAX, std::max(32, ((c->max_colour + cs - 1) / cs + 31) / 32 * 32));
   nt = std::min(std::max(nt / 32 * 32, 32), NT_MAX);
-  bool rep = c->rep_req == 2 || (c->rep_req == 0 && rep_bytes(c) <= REP_MAX_BYTES);
+  // a replicated copy costs one distributed shared-memory store per block of
+  // the cluster for each update: it pays for clusters of up to 4 blocks
+  bool rep = c->rep_req == 2 || (c->rep_req == 0 && rep_bytes(c) <= REP_MAX_BYTES && cs <= 4);
   if (rep && c->rep_req == 0 && !cluster_fits(c, cs, nt, true)) rep = false;
   if (c->cs_req <= 0)
     while (cs > 1 && !cluster_fits(c, cs, nt, rep)) cs /= 2;
@@ -874,7 +885,7 @@ extern "C" int fc2dgpu_ctx_solve(fc2dgpu_ctx* c, double tol, int max_iter, int e
     b.tol = tol;
     b.max_iter = max_iter;
     b.mode = FP32_PHASE;
-    b.switch_tol = c->switch_tol > 0.0 ? c->switch_tol : std::max(0.1 * tol, 1e-6);
+    b.switch_tol = c->switch_tol > 0.0 ? c->switch_tol : std::max(tol, 1e-6);
     b.stall = c->stall;
     K2(c->rep ? launch(c, k_fc2d_nsgs<float, true>, b, sizeof(float2) * (size_t)c->nc)
               : launch(c, k_fc2d_nsgs<float, false>, b, 0));
