@@ -244,6 +244,57 @@ def time_to_tolerance(d, s, tols=(1e-3, 1e-8), budget=(3000, 500)):
     return out
 
 
+def fc2d_granular(case="fc2d_fc2d_granularflowonwall_07002_00801", tol=1e-5, reps=3):
+    """The largest problem of the reference's 2D GPU test collection (7,002
+    contacts, 31,452 2x2 blocks; tol 1e-5 and 10,000 iterations as
+    test_fc2d_gpu.c), solved from zero: the cluster solver in FP64 (the
+    reference's iterates bit for bit, colour order) and in FP32 + FP64 polish,
+    the reference's per-colour GPU design (cuSPARSE SpMV + local-solve kernel
+    per colour, a graph per sweep, host convergence test), and the CPU
+    restatement of fc2d_nsgs (one core).  Device times from CUDA events, the
+    per-colour design's and the CPU's from the host clock."""
+    import oracle as O
+    import siconos_gb300.numerics as sn
+    z = np.load(ROOT / "tests" / "golden" / f"{case}.npz")
+    nc = int(z["nc"])
+    args = (nc, z["rowptr"], z["colidx"], z["blocks"], z["q"], z["mu"])
+    out = {"contacts": nc, "blocks": int(z["rowptr"][-1]), "tol": tol}
+    ctx = sn.Fc2dContext(*args)
+    try:
+        out["colours"] = ctx.colours()[0]
+        out["launch_shape"] = list(ctx.launch_shape())
+        for name, prec in (("gpu_fp64", 1), ("gpu_fp32_fp64_polish", 0)):
+            ctx.set_precision(prec)
+            ms = []
+            for _ in range(reps + 1):
+                ctx.set_r(np.zeros(2 * nc))
+                res = ctx.solve(tol, 10000)
+                ms.append(res["ms"])
+            out[name] = {"ms": statistics.median(ms[1:]), "sweeps": res["iterations"],
+                         "sweeps_fp32_fp64": list(ctx.last_sweeps()), "info": res["info"], "error": res["error"]}
+    finally:
+        ctx.close()
+    pc = sn.Fc2dPerColour(*args)
+    try:
+        ms = []
+        for _ in range(reps):
+            res = pc.solve(tol, 10000)
+            ms.append(res["ms"])
+        out["reference_design_gpu"] = {"ms": statistics.median(ms), "sweeps": res["iterations"], "info": res["info"],
+                                       "error": res["error"]}
+    finally:
+        pc.close()
+    P = O.Problem(*args, 2)
+    t = time.perf_counter()
+    ref = O.fc2d_nsgs_port(P, tol=tol, maxiter=10000)
+    out["cpu_reference_port_1core"] = {"ms": 1e3 * (time.perf_counter() - t), "sweeps": ref.iterations,
+                                       "info": ref.info, "error": ref.error}
+    cpu = out["cpu_reference_port_1core"]["ms"]
+    for k in ("gpu_fp64", "gpu_fp32_fp64_polish", "reference_design_gpu"):
+        out[k]["speedup_vs_cpu"] = cpu / out[k]["ms"]
+    return out
+
+
 def batched_c3(count=512, seed=7):
     """512 independent lattices (dims U[3..20]x[3..20]x[2..10], mu U(0.1, 0.9))
     in one persistent launch per phase: FP32 throughput over a fixed budget,
@@ -426,7 +477,8 @@ def run_ours(args):
             sup = {}
             for key, fn in (("time_to_tolerance_60x60x30", lambda: time_to_tolerance(d, s)),
                             ("batched_512_scenes", batched_c3),
-                            ("time_stepping_80x80x40", time_stepping_c5)):
+                            ("time_stepping_80x80x40", time_stepping_c5),
+                            ("fc2d_granular_7002", fc2d_granular)):
                 try:
                     sup[key] = fn()
                 except Exception as e:  # a failed extra must not lose the headline line
