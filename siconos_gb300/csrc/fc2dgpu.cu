@@ -322,10 +322,28 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
         const V old = rx.get(p);
         T ql[2] = {a.q[2 * p], a.q[2 * p + 1]};
         const int s0 = a.rp[p], s1 = a.rp[p + 1], sd = s0 + a.dpos[p];
-        // every block on the diagonal is left out (SBM_row_prod_no_diag_2x2)
-        for (int s = s0; s < s1; s++) {
-          const int j = a.col[s];
-          if (j != p) mvp2x2(a.W + 4 * (size_t)s, rx.get(j), ql);
+        // every block on the diagonal is left out (SBM_row_prod_no_diag_2x2);
+        // a row of up to NB blocks has all its neighbours' reactions fetched
+        // before the first product (one memory round trip, not one per
+        // block), then the products run in the row's order
+        constexpr int NB = sizeof(T) == sizeof(float) ? 16 : 8;
+        if (s1 - s0 <= NB) {
+          int cj[NB];
+          V rj[NB];
+#pragma unroll
+          for (int k = 0; k < NB; k++)
+            if (k < s1 - s0) cj[k] = a.col[s0 + k];
+#pragma unroll
+          for (int k = 0; k < NB; k++)
+            if (k < s1 - s0 && cj[k] != p) rj[k] = rx.get(cj[k]);
+#pragma unroll
+          for (int k = 0; k < NB; k++)
+            if (k < s1 - s0 && cj[k] != p) mvp2x2(a.W + 4 * (size_t)(s0 + k), rj[k], ql);
+        } else {
+          for (int s = s0; s < s1; s++) {
+            const int j = a.col[s];
+            if (j != p) mvp2x2(a.W + 4 * (size_t)s, rx.get(j), ql);
+          }
         }
         T P[2] = {old.x, old.y};
         local_solve<T>(a.W + 4 * (size_t)sd, a.det[p], ql, a.mu[p], P);
