@@ -74,6 +74,15 @@ def port():
         lib.oracle_fc2d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
                                          C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
                                          C.POINTER(C.c_int)]
+        lib.oracle_rfc3d_nsgs.restype = C.c_int
+        lib.oracle_rfc3d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, _F64, C.c_double,
+                                          C.c_int, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                          C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+        lib.oracle_rfc3d_compute_error.restype = C.c_double
+        lib.oracle_rfc3d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, _F64,
+                                                   C.c_double]
+        lib.oracle_rfc3d_max_eig.restype = C.c_double
+        lib.oracle_rfc3d_max_eig.argtypes = [_F64]
         lib.oracle_fc2d_sweeps_f32.restype = C.c_int
         lib.oracle_fc2d_sweeps_f32.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, C.c_int, C.c_void_p]
         lib.oracle_fc2d_compute_error.restype = C.c_double
@@ -131,6 +140,20 @@ def ref():
         lib.ref_fc2d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64]
         lib.ref_dat_write.restype = C.c_int
         lib.ref_dat_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]
+        lib.ref_rfc3d_nsgs.restype = C.c_int
+        lib.ref_rfc3d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, _F64, C.c_double,
+                                       C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
+                                       C.POINTER(C.c_int)]
+        lib.ref_rfc3d_compute_error.restype = C.c_double
+        lib.ref_rfc3d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, _F64]
+        lib.ref_rfc3d_max_eig.restype = C.c_double
+        lib.ref_rfc3d_max_eig.argtypes = [_F64]
+        lib.ref_rfc3d_dat_open.restype = C.c_void_p
+        lib.ref_rfc3d_dat_open.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                                           C.POINTER(C.c_int)]
+        lib.ref_rfc3d_dat_get.restype = C.c_int
+        lib.ref_rfc3d_dat_get.argtypes = [C.c_void_p, _I64, _I64, _F64, _F64, _F64, _F64]
+        lib.ref_rfc3d_dat_close.argtypes = [C.c_void_p]
         lib.computeAlartCurnierSTD.restype = None
         lib.computeAlartCurnierSTD.argtypes = [_F64, _F64, C.c_double, _F64, _F64, C.c_void_p, C.c_void_p]
         lib.ref_solve_3x3_gepp.restype = C.c_int
@@ -289,4 +312,90 @@ def fc2d_compute_error_ref(P: Problem, r) -> tuple[float, np.ndarray]:
                                      np.ascontiguousarray(P.blocks, np.float64).reshape(-1),
                                      np.ascontiguousarray(P.q, np.float64), np.ascontiguousarray(P.mu, np.float64),
                                      np.ascontiguousarray(r, np.float64), u)
+    return e, u
+
+
+# ---- 3D rolling friction (5 components per contact) -------------------------
+@dataclass
+class RollingProblem:
+    """A rolling-friction problem: W as block-CSR of 5x5 column-major blocks,
+    q[5 nc], mu and mu_r per contact."""
+
+    nc: int
+    rowptr: np.ndarray
+    colidx: np.ndarray
+    blocks: np.ndarray
+    q: np.ndarray
+    mu: np.ndarray
+    mur: np.ndarray
+
+    @property
+    def nnzb(self) -> int:
+        return int(self.rowptr[-1])
+
+    def arrays(self):
+        return (self.nc, np.ascontiguousarray(self.rowptr, np.int64), np.ascontiguousarray(self.colidx, np.int64),
+                np.ascontiguousarray(self.blocks, np.float64).reshape(-1), np.ascontiguousarray(self.q, np.float64),
+                np.ascontiguousarray(self.mu, np.float64), np.ascontiguousarray(self.mur, np.float64))
+
+
+def read_rfc3d_dat(path: str | Path) -> RollingProblem:
+    """A rolling-friction ``.dat`` fixture read by the reference's own reader."""
+    lib = ref()
+    if lib is None:
+        raise RuntimeError("oracle/_ref is not built")
+    nc, nnzb, st = C.c_int(), C.c_int64(), C.c_int()
+    h = lib.ref_rfc3d_dat_open(str(path).encode(), C.byref(nc), C.byref(nnzb), C.byref(st))
+    if not h:
+        raise IOError(f"cannot read {path}")
+    n, nb = nc.value, nnzb.value
+    rp = np.zeros(n + 1, np.int64)
+    ci = np.zeros(max(nb, 1), np.int64)
+    bl = np.zeros(25 * max(nb, 1))
+    q, mu, mur = np.zeros(5 * n), np.zeros(n), np.zeros(n)
+    rc = lib.ref_rfc3d_dat_get(h, rp, ci, bl, q, mu, mur)
+    lib.ref_rfc3d_dat_close(h)
+    if rc != 0:
+        raise IOError(f"unsupported storage in {path}")
+    return RollingProblem(n, rp, ci[:nb].copy(), bl[: 25 * nb].reshape(nb, 25).copy(), q, mu, mur)
+
+
+def _rfc3d_solve(fn, P: RollingProblem, r0, tol, maxiter, order, trace_cap, is_port):
+    r = np.zeros(5 * P.nc) if r0 is None else np.ascontiguousarray(r0, dtype=np.float64).copy()
+    u = np.zeros(5 * P.nc)
+    it, err, tl = C.c_int(), C.c_double(), C.c_int()
+    tr = np.zeros(max(trace_cap, 1))
+    order_arr = None if order is None else np.ascontiguousarray(order, np.int32)
+    args = [*P.arrays(), r, u, tol, maxiter]
+    if is_port:
+        args.append(None if order_arr is None else order_arr.ctypes.data)
+    args += [C.byref(it), C.byref(err), tr.ctypes.data if trace_cap else None, trace_cap, C.byref(tl)]
+    info = fn(*args)
+    return Result(info, it.value, err.value, r, u, tr[: min(tl.value, trace_cap)].copy())
+
+
+def rfc3d_nsgs_port(P: RollingProblem, r0=None, tol=1e-8, maxiter=10000, order=None, trace_cap=0) -> Result:
+    """The restatement of rolling_friction_3d_nsgs (oracle/rfc3d_oracle.c)."""
+    return _rfc3d_solve(port().oracle_rfc3d_nsgs, P, r0, tol, maxiter, order, trace_cap, True)
+
+
+def rfc3d_nsgs_ref(P: RollingProblem, r0=None, tol=1e-8, maxiter=10000, trace_cap=0) -> Result:
+    """The reference's own rolling_friction_3d_nsgs through its driver."""
+    lib = ref()
+    if lib is None:
+        raise RuntimeError("oracle/_ref is not built")
+    return _rfc3d_solve(lib.ref_rfc3d_nsgs, P, r0, tol, maxiter, None, trace_cap, False)
+
+
+def rfc3d_compute_error_port(P: RollingProblem, r) -> tuple[float, np.ndarray]:
+    u = np.zeros(5 * P.nc)
+    a = P.arrays()
+    nq = float(np.sqrt(np.sum(a[4] * a[4])))
+    e = port().oracle_rfc3d_compute_error(*a, np.ascontiguousarray(r, np.float64), u, nq)
+    return e, u
+
+
+def rfc3d_compute_error_ref(P: RollingProblem, r) -> tuple[float, np.ndarray]:
+    u = np.zeros(5 * P.nc)
+    e = ref().ref_rfc3d_compute_error(*P.arrays(), np.ascontiguousarray(r, np.float64), u)
     return e, u

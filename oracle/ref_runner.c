@@ -21,6 +21,11 @@
 #include "fc3d_compute_error.h"
 #include "numerics_verbose.h"
 #include "op3x3.h"
+#include "op5x5.h"
+#include "RollingFrictionContactProblem.h"
+#include "RollingFrictionContact_options.h"
+#include "rolling_fc_Solvers.h"
+#include "rolling_friction_3d_compute_error.h"
 #include "projectionOnCone.h"
 
 /* Build a 3x3-block SBM that points into caller-owned arrays.  blocks holds
@@ -310,3 +315,171 @@ int ref_dat_write(const char *fname, int dim, int nc, const int64_t *rowptr, con
 int ref_solve_3x3_gepp(const double *a, double *b) { return solve_3x3_gepp(a, b); }
 unsigned ref_projection_on_cone(double *r, double mu) { return projectionOnCone(r, mu); }
 void ref_set_verbose(int v) { numerics_set_verbose(v); }
+
+/* ---- 3D rolling friction (dimension 5) ---------------------------------- */
+
+/* The reference's rolling-friction NSGS extracts diagonal blocks of dense
+ * or CSparse storage only (its sparse-block branch asserts,
+ * NumericsMatrix.c:1870), so W goes to it as a dense column-major matrix. */
+static NumericsMatrix *make_dense_d(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                                    int d) {
+  const size_t n = (size_t)d * (size_t)nc;
+  double *A = (double *)calloc(n * n, sizeof(double));
+  for (int i = 0; i < nc; i++)
+    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; k++)
+      for (int b = 0; b < d; b++)
+        for (int a = 0; a < d; a++)
+          A[((size_t)d * (size_t)colidx[k] + (size_t)b) * n + (size_t)d * (size_t)i + (size_t)a] =
+              blocks[(size_t)(d * d) * (size_t)k + (size_t)(d * b + a)];
+  return NM_create_from_data(NM_DENSE, (int)n, (int)n, A);
+}
+
+static void free_dense(NumericsMatrix *M) {
+  free(M->matrix0);
+  M->matrix0 = NULL;
+  NM_clear(M);
+  free(M);
+}
+
+/* The reference's rolling_friction_3d_driver with SICONOS_ROLLING_FRICTION_3D_NSGS
+ * default options, tolerance and iteration budget set, on a block-CSR W of
+ * 5x5 blocks (passed as a dense matrix).  r holds the warm start. */
+int ref_rfc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
+                   const double *mu, const double *mur, double *r, double *u, double tol, int maxiter, int *iters,
+                   double *err, double *trace, int trace_cap, int *trace_len) {
+  NumericsMatrix *M = make_dense_d(nc, rowptr, colidx, blocks, 5);
+  RollingFrictionContactProblem P;
+  memset(&P, 0, sizeof(P));
+  P.dimension = 5;
+  P.numberOfContacts = nc;
+  P.M = M;
+  P.q = (double *)q;
+  P.mu = (double *)mu;
+  P.mu_r = (double *)mur;
+  SolverOptions *opt = solver_options_create(SICONOS_ROLLING_FRICTION_3D_NSGS);
+  opt->iparam[SICONOS_IPARAM_MAX_ITER] = maxiter;
+  opt->dparam[SICONOS_DPARAM_TOL] = tol;
+  Trace t = {trace, trace_cap, 0};
+  Callback cb = {&t, trace_cb};
+  if (trace) opt->callback = &cb;
+  int info = rolling_friction_3d_driver(&P, r, u, opt);
+  if (iters) *iters = opt->iparam[SICONOS_IPARAM_ITER_DONE];
+  if (err) *err = opt->dparam[SICONOS_DPARAM_RESIDU];
+  if (trace_len) *trace_len = t.len;
+  opt->callback = NULL;
+  solver_options_delete(opt);
+  free_dense(M);
+  return info;
+}
+
+/* The reference's rolling_friction_3d_compute_error on r; u receives q + W r. */
+double ref_rfc3d_compute_error(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                               const double *q, const double *mu, const double *mur, const double *r, double *u) {
+  NumericsMatrix *M = make_dense_d(nc, rowptr, colidx, blocks, 5);
+  RollingFrictionContactProblem P;
+  memset(&P, 0, sizeof(P));
+  P.dimension = 5;
+  P.numberOfContacts = nc;
+  P.M = M;
+  P.q = (double *)q;
+  P.mu = (double *)mu;
+  P.mu_r = (double *)mur;
+  double norm_q = cblas_dnrm2(5 * nc, q, 1);
+  double e = 0.0;
+  rolling_friction_3d_compute_error(&P, (double *)r, u, 1e-300, NULL, norm_q, &e);
+  free_dense(M);
+  return e;
+}
+
+/* Largest eigenvalue by the reference's 5x5 symmetric eigenvalue routine. */
+double ref_rfc3d_max_eig(const double *a) {
+  double ev[5];
+  eigvals_sym5x5_for_loop(a, ev);
+  return ev[4];
+}
+
+/* A rolling-friction problem read by the reference's reader
+ * (rollingFrictionContact_new_from_filename), W given back as block-CSR of
+ * 5x5 blocks: sparse-block storage as stored, dense storage as every block
+ * holding a nonzero entry plus the diagonal. */
+typedef struct {
+  RollingFrictionContactProblem *P;
+} RDatHandle;
+
+void *ref_rfc3d_dat_open(const char *fname, int *nc, int64_t *nnzb, int *storage) {
+  RollingFrictionContactProblem *P = rollingFrictionContact_new_from_filename(fname);
+  if (!P) return NULL;
+  if (P->dimension != 5) {
+    rollingFrictionContactProblem_free(P);
+    return NULL;
+  }
+  RDatHandle *h = (RDatHandle *)malloc(sizeof(RDatHandle));
+  h->P = P;
+  *nc = P->numberOfContacts;
+  *storage = (int)P->M->storageType;
+  const int n = P->numberOfContacts, d = 5;
+  if (P->M->storageType == NM_SPARSE_BLOCK)
+    *nnzb = (int64_t)P->M->matrix1->nbblocks;
+  else if (P->M->storageType == NM_DENSE) {
+    int64_t cnt = 0;
+    for (int bi = 0; bi < n; bi++)
+      for (int bj = 0; bj < n; bj++) {
+        int nz = (bi == bj);
+        for (int a = 0; a < d && !nz; a++)
+          for (int b = 0; b < d && !nz; b++)
+            nz = P->M->matrix0[(size_t)(d * bj + b) * (size_t)(d * n) + (size_t)(d * bi + a)] != 0.0;
+        cnt += nz;
+      }
+    *nnzb = cnt;
+  } else
+    *nnzb = -1;
+  return h;
+}
+
+int ref_rfc3d_dat_get(void *hv, int64_t *rowptr, int64_t *colidx, double *blocks, double *q, double *mu,
+                      double *mur) {
+  RDatHandle *h = (RDatHandle *)hv;
+  RollingFrictionContactProblem *P = h->P;
+  const int n = P->numberOfContacts, d = 5;
+  memcpy(q, P->q, sizeof(double) * (size_t)d * (size_t)n);
+  memcpy(mu, P->mu, sizeof(double) * (size_t)n);
+  memcpy(mur, P->mu_r, sizeof(double) * (size_t)n);
+  if (P->M->storageType == NM_SPARSE_BLOCK) {
+    SparseBlockStructuredMatrix *m = P->M->matrix1;
+    for (int i = 0; i <= n; i++)
+      rowptr[i] = (int64_t)(i < (int)m->filled1 ? m->index1_data[i] : m->index1_data[m->filled1 - 1]);
+    for (size_t k = 0; k < m->nbblocks; k++) {
+      colidx[k] = (int64_t)m->index2_data[k];
+      memcpy(&blocks[(size_t)(d * d) * k], m->block[k], (size_t)(d * d) * sizeof(double));
+    }
+    return 0;
+  }
+  if (P->M->storageType == NM_DENSE) {
+    int64_t k = 0;
+    const double *A = P->M->matrix0;
+    for (int bi = 0; bi < n; bi++) {
+      rowptr[bi] = k;
+      for (int bj = 0; bj < n; bj++) {
+        int nz = (bi == bj);
+        for (int a = 0; a < d && !nz; a++)
+          for (int b = 0; b < d && !nz; b++) nz = A[(size_t)(d * bj + b) * (size_t)(d * n) + (size_t)(d * bi + a)] != 0.0;
+        if (!nz) continue;
+        colidx[k] = bj;
+        for (int b = 0; b < d; b++)
+          for (int a = 0; a < d; a++)
+            blocks[(size_t)(d * d) * (size_t)k + (size_t)(d * b + a)] =
+                A[(size_t)(d * bj + b) * (size_t)(d * n) + (size_t)(d * bi + a)];
+        k++;
+      }
+    }
+    rowptr[n] = k;
+    return 0;
+  }
+  return -1;
+}
+
+void ref_rfc3d_dat_close(void *hv) {
+  RDatHandle *h = (RDatHandle *)hv;
+  rollingFrictionContactProblem_free(h->P);
+  free(h);
+}

@@ -3,7 +3,7 @@
 Run in a checkout that has the reference sources (the library in
 ``oracle/_ref`` is built from them by ``oracle/build_ref.py``):
 
-    python tests/golden/make_golden.py /path/to/reference [--only=fc2d]
+    python tests/golden/make_golden.py /path/to/reference [--only=fc2d|rfc3d]
 
 For each SBM/dense friction-contact fixture of the reference's own test data
 (numerics/src/FrictionContact/test/data) and for the 5x5x6 lattice scene,
@@ -106,12 +106,47 @@ def make_fc2d(data: Path):
         print(f"{f}: nc={P.nc} nnzb={P.nnzb} {kind} info={full.info} it={full.iterations} err={full.error:.3e}")
 
 
+RFC3D_FIXTURES = [
+    # the reference's rolling-friction test data (RollingFrictionContact/test/
+    # data); the reference's rolling NSGS takes dense storage only, the
+    # CSparse-stored files are left out
+    "RFC3D_sphere_1.dat",
+    "RFC3D_sphere_2.dat",
+    "RFC3D_cube_1.dat",
+    "rfc3d_sphere_from_grfc3d_dense.dat",
+    "rockfall_14_25792.dat",
+    "rockfall_21_54029.dat",
+]
+
+
+def make_rfc3d(data: Path):
+    """Rolling-friction problems with the reference's rolling_friction_3d_nsgs
+    results (its defaults, tol 1e-8, 10000 iterations; and a 20-iteration
+    run), W as read by the reference (dense, every 5x5 block holding a
+    nonzero kept, in column order)."""
+    import oracle as O
+    for f in RFC3D_FIXTURES:
+        P = O.read_rfc3d_dat(data / f)
+        full = O.rfc3d_nsgs_ref(P, tol=1e-8, maxiter=10000, trace_cap=10000)
+        short = O.rfc3d_nsgs_ref(P, tol=1e-8, maxiter=20, trace_cap=20)
+        name = "rfc3d_" + f.replace(".dat", "").replace("-", "_")
+        d = dict(nc=P.nc, rowptr=P.rowptr, colidx=P.colidx, blocks=P.blocks, q=P.q, mu=P.mu, mur=P.mur,
+                 info=full.info, iterations=full.iterations, error=full.error, r=full.r, u=full.u, trace=full.trace,
+                 info20=short.info, iterations20=short.iterations, error20=short.error, r20=short.r, u20=short.u,
+                 trace20=short.trace, source=f)
+        np.savez_compressed(HERE / f"{name}.npz", **d)
+        print(f"{f}: nc={P.nc} nnzb={P.nnzb} info={full.info} it={full.iterations} err={full.error:.3e}")
+
+
 def main(ref_root: str, only: str | None = None):
     from oracle import build_ref
     import oracle as O
 
     build_ref.build(ref_root)
     data = Path(ref_root) / "numerics" / "src" / "FrictionContact" / "test" / "data"
+    if only == "rfc3d":
+        make_rfc3d(Path(ref_root) / "numerics" / "src" / "RollingFrictionContact" / "test" / "data")
+        return
     if only == "fc2d":
         from siconos_gb300 import build as B
         B.build()
