@@ -12,6 +12,7 @@
  *   NumericsMatrix               linalg/NumericsMatrix.h:73-89 (only the
  *                                members up to `version` are read)
  *   FrictionContactProblem       FrictionContact/FrictionContactProblem.h:33-46
+ *   RollingFrictionContactProblem RollingFrictionContact/RollingFrictionContactProblem.h:33-53
  *   Callback, SolverOptions      core/SolverOptions.h:36-91
  */
 #ifndef SICONOS_NUMERICS_ABI_H
@@ -70,6 +71,16 @@ typedef struct FrictionContactProblem {
   double *mu;
 } FrictionContactProblem;
 
+/* RollingFrictionContact/RollingFrictionContactProblem.h:33-53 */
+typedef struct RollingFrictionContactProblem {
+  int dimension;
+  int numberOfContacts;
+  NumericsMatrix *M;
+  double *q;
+  double *mu;
+  double *mu_r;
+} RollingFrictionContactProblem;
+
 typedef struct {
   void *env;
   void (*collectStatsIteration)(void *env, size_t size, double *reaction, double *velocity, double error,
@@ -100,6 +111,8 @@ typedef struct SolverOptions {
 /* solver ids (FrictionContact_options.h:83, :152) */
 #define SICONOS_FRICTION_2D_NSGS 400
 #define SICONOS_FRICTION_3D_NSGS 500
+#define SICONOS_ROLLING_FRICTION_3D_NSGS 3000
+#define SICONOS_ROLLING_FRICTION_3D_ONECONTACT_NSN 3003
 #define SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID 565
 
 /* generic indices (SolverOptions.h:94-121) */
@@ -141,7 +154,9 @@ typedef struct SolverOptions {
 #define SICONOS_FRICTION_3D_NSN_HYBRID_MAX_LOOP 15
 #define SICONOS_FRICTION_3D_NSN_HYBRID_MAX_ITER 16
 #define SICONOS_FRICTION_3D_NSN_RHO 3
+#define SICONOS_FRICTION_3D_NSN_FORMULATION_RHO_STRATEGY_SPECTRAL_NORM 1
 #define SICONOS_FRICTION_3D_NSN_FORMULATION_RHO_STRATEGY_SPLIT_SPECTRAL_NORM 3
+#define SICONOS_FRICTION_3D_NSN_FORMULATION_NATURALMAP 4
 #define SICONOS_FRICTION_3D_NSN_FORMULATION_ALARTCURNIER_STD 0
 #define SICONOS_FRICTION_3D_NSN_LINESEARCH_GOLDSTEINPRICE 0
 #define SICONOS_FRICTION_3D_NSN_HYBRID_STRATEGY_NSN_AND_PLI_NSN_LOOP 2

@@ -20,13 +20,15 @@ OUT = PKG / "_lib"
 LIB = OUT / "libfc3dgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c"]
+C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c", "rfc3dgpu_nsgs.c"]
 CU_SOURCES = {
     "fc3dgpu_ctx.cu": ["--fmad=false"],
     "fc3dgpu_sweep_f64.cu": ["--fmad=false"],
     "fc3dgpu_noalloc.cu": ["--fmad=false"],
     # host code computes determinants and norms the kernel reuses
     "fc2dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    # host code computes the rolling solver's rho (Jacobi eigenvalues)
+    "rfc3dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # the reference's per-colour design, kept for measurement beside fc2dgpu.cu
     "fc2dgpu_percolour.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # BF16 tensor-core MLP of the learned warm start

@@ -31,6 +31,9 @@ LIB_PATH = _PKG / "_lib" / "libfc3dgpu.so"
 SICONOS_FRICTION_2D_NSGS = 400
 SICONOS_FRICTION_2D_NSGS_GPU = 412
 SICONOS_FRICTION_3D_NSGS = 500
+SICONOS_ROLLING_FRICTION_3D_NSGS = 3000
+SICONOS_ROLLING_FRICTION_3D_ONECONTACT_NSN = 3003
+SICONOS_ROLLING_FRICTION_3D_NSGS_GPU = 3020
 SICONOS_FRICTION_3D_NSGS_GPU = 531
 SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID = 565
 SICONOS_IPARAM_MAX_ITER = 0
@@ -92,6 +95,11 @@ class NumericsMatrix(C.Structure):
 class _FCP(C.Structure):
     _fields_ = [("dimension", C.c_int), ("numberOfContacts", C.c_int), ("M", C.POINTER(NumericsMatrix)),
                 ("q", _DP), ("mu", _DP)]
+
+
+class _RFCP(C.Structure):
+    _fields_ = [("dimension", C.c_int), ("numberOfContacts", C.c_int), ("M", C.POINTER(NumericsMatrix)),
+                ("q", _DP), ("mu", _DP), ("mu_r", _DP)]
 
 
 CALLBACK_T = C.CFUNCTYPE(None, C.c_void_p, C.c_size_t, _DP, _DP, C.c_double, C.c_void_p)
@@ -242,6 +250,27 @@ ABI = {
                                            C.POINTER(C.c_int)]),
     "fc2dgpu_ctx_set_precision": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
     "fc2dgpu_ctx_last_sweeps": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "rfc3dgpu_nsgs": (C.c_int, [C.POINTER(_RFCP), _DP, _DP, C.POINTER(_SO)]),
+    "rfc3dgpu_nsgs_solve_wrap": (C.c_int, [C.c_void_p, _DP, _DP, C.POINTER(_SO)]),
+    "rfc3dgpu_nsgs_init_wrap": (C.c_int, [C.c_void_p, C.POINTER(_SO)]),
+    "rfc3dgpu_nsgs_free_wrap": (None, [C.c_void_p, C.POINTER(_SO)]),
+    "rfc3dgpu_nsgs_set_default": (None, [C.POINTER(_SO)]),
+    "rfc3dgpu_options_create": (C.POINTER(_SO), []),
+    "rfc3dgpu_options_delete": (None, [C.POINTER(_SO)]),
+    "rfc3dgpu_release": (None, [C.POINTER(_SO)]),
+    "rfc3dgpu_driver": (C.c_int, [C.POINTER(_RFCP), _DP, _DP, C.POINTER(_SO)]),
+    "rfc3dgpu_compute_error": (C.c_int, [C.POINTER(_RFCP), _DP, _DP, C.c_double, C.c_double, _DP]),
+    "rfc3dgpu_ctx_create": (C.c_void_p, [C.c_int]),
+    "rfc3dgpu_ctx_destroy": (None, [C.c_void_p]),
+    "rfc3dgpu_ctx_set_problem": (C.c_int, [C.c_void_p, C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, C.c_int]),
+    "rfc3dgpu_ctx_set_r": (C.c_int, [C.c_void_p, _F64]),
+    "rfc3dgpu_ctx_solve": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                     _DP, C.POINTER(C.c_int), _DP]),
+    "rfc3dgpu_ctx_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rfc3dgpu_ctx_compute_error": (C.c_int, [C.c_void_p, C.c_double, _DP]),
+    "rfc3dgpu_ctx_colours": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rfc3dgpu_ctx_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "rfc3dgpu_ctx_rho": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fc2dgpu_percolour_create": (C.c_void_p, [C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]),
     "fc2dgpu_percolour_destroy": (None, [C.c_void_p]),
     "fc2dgpu_percolour_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int), _DP,
@@ -286,8 +315,8 @@ class SparseBlockMatrix:
     def __init__(self, nc: int, rowptr, colidx, blocks, block_size: int = 3):
         self.nc = int(nc)
         self.bs = int(block_size)
-        if self.bs not in (2, 3):
-            raise ValueError("blocks are 2x2 or 3x3")
+        if self.bs not in (2, 3, 5):
+            raise ValueError("blocks are 2x2, 3x3 or 5x5")
         self.rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
         self.colidx = np.ascontiguousarray(colidx, dtype=np.int64)
         self.blocks = np.ascontiguousarray(np.asarray(blocks, dtype=np.float64).reshape(-1, self.bs * self.bs))
@@ -390,7 +419,8 @@ class SolverOptions:
     """``SolverOptions(solver_id)`` for ``SICONOS_FRICTION_3D_NSGS_GPU`` or
     ``SICONOS_FRICTION_2D_NSGS_GPU``."""
 
-    _KINDS = {SICONOS_FRICTION_3D_NSGS_GPU: "fc3dgpu", SICONOS_FRICTION_2D_NSGS_GPU: "fc2dgpu"}
+    _KINDS = {SICONOS_FRICTION_3D_NSGS_GPU: "fc3dgpu", SICONOS_FRICTION_2D_NSGS_GPU: "fc2dgpu",
+              SICONOS_ROLLING_FRICTION_3D_NSGS_GPU: "rfc3dgpu"}
 
     def __init__(self, solver_id: int = SICONOS_FRICTION_3D_NSGS_GPU):
         if solver_id not in self._KINDS:
@@ -632,6 +662,127 @@ class Fc2dContext:
     def close(self):
         if getattr(self, "ctx", None):
             lib().fc2dgpu_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RollingFrictionContactProblem:
+    """``RollingFrictionContactProblem(5, nc, M, q, mu, mu_r)`` sharing the
+    numpy buffers; M dense (Fortran order) or a 5x5 :class:`SparseBlockMatrix`."""
+
+    def __init__(self, dim: int, nc: int, M, q, mu, mu_r):
+        if dim != 5:
+            raise ValueError("dimension 5")
+        if isinstance(M, SparseBlockMatrix) and M.bs != 5:
+            raise ValueError("block size differs from the dimension")
+        as_f64 = (lambda x: x if (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous)
+                  else np.ascontiguousarray(x, dtype=np.float64))
+        self._q, self._mu, self._mu_r = as_f64(q), as_f64(mu), as_f64(mu_r)
+        self._M = M
+        nm = NumericsMatrix()
+        nm.size0 = nm.size1 = 5 * nc
+        if isinstance(M, SparseBlockMatrix):
+            nm.storageType = NM_SPARSE_BLOCK
+            nm.matrix1 = C.pointer(M.c)
+        else:
+            if not (isinstance(M, np.ndarray) and M.dtype == np.float64 and M.flags.f_contiguous):
+                raise TypeError("dense M must be a Fortran-ordered float64 numpy array")
+            nm.storageType = NM_DENSE
+            nm.matrix0 = M.ctypes.data_as(_DP)
+        nm.version.number = 1
+        self._nm = nm
+        p = _RFCP()
+        p.dimension = 5
+        p.numberOfContacts = nc
+        p.M = C.pointer(nm)
+        p.q = self._q.ctypes.data_as(_DP)
+        p.mu = self._mu.ctypes.data_as(_DP)
+        p.mu_r = self._mu_r.ctypes.data_as(_DP)
+        self.c = p
+
+    @property
+    def numberOfContacts(self) -> int:
+        return self.c.numberOfContacts
+
+
+def rolling_friction_3d_driver(problem: RollingFrictionContactProblem, reaction, velocity, options) -> int:
+    """rolling_friction_3d_driver for ``SICONOS_ROLLING_FRICTION_3D_NSGS_GPU``."""
+    n = 5 * problem.numberOfContacts
+    return lib().rfc3dgpu_driver(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), options.ptr)
+
+
+def rolling_friction_3d_compute_error(problem, reaction, velocity, tolerance: float, norm_q: float):
+    n = 5 * problem.numberOfContacts
+    err = C.c_double()
+    info = lib().rfc3dgpu_compute_error(C.byref(problem.c), _vec(reaction, n), _vec(velocity, n), tolerance, norm_q,
+                                        C.byref(err))
+    return info, err.value
+
+
+class RollingContext:
+    """Device-resident rolling-friction problem (``rfc3dgpu_ctx_*``)."""
+
+    def __init__(self, nc, rowptr, colidx, blocks, q, mu, mu_r, colouring: int = 0, device: int = 0):
+        L = lib()
+        self.ctx = L.rfc3dgpu_ctx_create(device)
+        if not self.ctx:
+            raise RuntimeError(last_error())
+        self.nc = int(nc)
+        rc = L.rfc3dgpu_ctx_set_problem(self.ctx, self.nc, np.ascontiguousarray(rowptr, np.int64),
+                                        np.ascontiguousarray(colidx, np.int64),
+                                        np.ascontiguousarray(blocks, np.float64).reshape(-1),
+                                        np.ascontiguousarray(q, np.float64), np.ascontiguousarray(mu, np.float64),
+                                        np.ascontiguousarray(mu_r, np.float64), colouring)
+        if rc != 0:
+            L.rfc3dgpu_ctx_destroy(self.ctx)
+            self.ctx = None
+            raise ValueError(last_error())
+
+    def set_r(self, r):
+        _check(lib().rfc3dgpu_ctx_set_r(self.ctx, np.ascontiguousarray(r, np.float64)))
+
+    def solve(self, tol: float, max_iter: int, local_tol: float = 1e-12, local_max_iter: int = 10) -> dict:
+        it, info = C.c_int(), C.c_int()
+        err, ms = C.c_double(), C.c_double()
+        _check(lib().rfc3dgpu_ctx_solve(self.ctx, tol, max_iter, local_tol, local_max_iter, C.byref(it),
+                                        C.byref(err), C.byref(info), C.byref(ms)))
+        return dict(iterations=it.value, error=err.value, info=info.value, ms=ms.value)
+
+    def get_r_u(self):
+        r, u = np.zeros(5 * self.nc), np.zeros(5 * self.nc)
+        _check(lib().rfc3dgpu_ctx_get_r_u(self.ctx, r.ctypes.data, u.ctypes.data))
+        return r, u
+
+    def compute_error(self, norm_q: float) -> float:
+        e = C.c_double()
+        _check(lib().rfc3dgpu_ctx_compute_error(self.ctx, norm_q, C.byref(e)))
+        return e.value
+
+    def colours(self):
+        out = np.zeros(self.nc, np.int32)
+        n = lib().rfc3dgpu_ctx_colours(self.ctx, out.ctypes.data)
+        if n < 0:
+            raise RuntimeError(last_error())
+        return n, out
+
+    def rho(self) -> np.ndarray:
+        out = np.zeros(self.nc)
+        _check(lib().rfc3dgpu_ctx_rho(self.ctx, out.ctypes.data))
+        return out
+
+    def trace(self, cap: int) -> np.ndarray:
+        out = np.zeros(max(cap, 1))
+        n = lib().rfc3dgpu_ctx_trace(self.ctx, out.ctypes.data, cap)
+        return out[:max(n, 0)].copy()
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            lib().rfc3dgpu_ctx_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):

@@ -15,7 +15,7 @@ def declared_functions():
     names = set()
     for h in (ROOT / "include").glob("*.h"):
         text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
-        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b(fc[23]dgpu_\w+)\s*\(", text, flags=re.M):
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:fc[23]|rfc3)dgpu_\w+)\s*\(", text, flags=re.M):
             names.add(m.group(1))
     return sorted(names)
 
@@ -24,7 +24,8 @@ def test_headers_declare_entry_points():
     names = declared_functions()
     for must in ["fc3dgpu_nsgs", "fc3dgpu_nsgs_set_default", "fc3dgpu_nsgs_batch", "fc3dgpu_compute_error",
                  "fc3dgpu_driver", "fc3dgpu_colour", "fc3dgpu_ctx_solve", "fc3dgpu_lattice_create",
-                 "fc2dgpu_nsgs", "fc2dgpu_driver", "fc2dgpu_ctx_solve", "fc2dgpu_percolour_solve"]:
+                 "fc2dgpu_nsgs", "fc2dgpu_driver", "fc2dgpu_ctx_solve", "fc2dgpu_percolour_solve",
+                 "rfc3dgpu_nsgs", "rfc3dgpu_driver", "rfc3dgpu_ctx_solve"]:
         assert must in names
 
 
