@@ -295,6 +295,52 @@ def fc2d_granular(case="fc2d_fc2d_granularflowonwall_07002_00801", tol=1e-5, rep
     return out
 
 
+def rfc3d_tiled(copies=1000, sample_copies=100, tol=1e-8):
+    """Rolling friction: `copies` independent copies of the reference's
+    21-contact rockfall problem along W's diagonal (q of each copy scaled by
+    a seeded factor in [0.9, 1.1]), solved from zero to tol 1e-8 within
+    10,000 sweeps by the GPU solver (FP64, the reference's iterates in colour
+    order), against the CPU restatement of rolling_friction_3d_nsgs (one core)
+    on `sample_copies` copies for 200 sweeps; both as contact-sweeps/s."""
+    import oracle as O
+    import siconos_gb300.numerics as sn
+    z = np.load(ROOT / "tests" / "golden" / "rfc3d_rockfall_21_54029.npz")
+    P0 = O.RollingProblem(int(z["nc"]), z["rowptr"], z["colidx"], z["blocks"], z["q"], z["mu"], z["mur"])
+
+    def tile(k, seed):
+        g = np.random.default_rng(seed)
+        nc, nb = P0.nc, P0.nnzb
+        rp = [0]
+        for c in range(k):
+            rp.extend((P0.rowptr[1:] + c * nb).tolist())
+        return O.RollingProblem(k * nc, np.asarray(rp, np.int64),
+                                np.concatenate([P0.colidx + c * nc for c in range(k)]).astype(np.int64),
+                                np.tile(P0.blocks, (k, 1)), np.tile(P0.q, k) * np.repeat(g.uniform(0.9, 1.1, k), 5 * nc),
+                                np.tile(P0.mu, k), np.tile(P0.mur, k))
+    P = tile(copies, 7)
+    ctx = sn.RollingContext(P.nc, P.rowptr, P.colidx, P.blocks, P.q, P.mu, P.mur)
+    try:
+        ncol = ctx.colours()[0]
+        ctx.set_r(np.zeros(5 * P.nc))
+        ctx.solve(tol, 20)
+        ctx.set_r(np.zeros(5 * P.nc))
+        res = ctx.solve(tol, 10000)
+    finally:
+        ctx.close()
+    S = tile(sample_copies, 7)
+    t = time.perf_counter()
+    ref = O.rfc3d_nsgs_port(S, tol=0.0, maxiter=200)
+    cpu_s = time.perf_counter() - t
+    gpu = P.nc * res["iterations"] / (res["ms"] / 1e3)
+    cpu = S.nc * ref.iterations / cpu_s
+    return {"contacts": P.nc, "blocks": P.nnzb, "colours": ncol, "tol": tol,
+            "gpu_fp64": {"ms": res["ms"], "sweeps": res["iterations"], "info": res["info"], "error": res["error"],
+                         "contact_sweeps_per_s": gpu},
+            "cpu_reference_port_1core": {"contacts": S.nc, "sweeps": ref.iterations, "s": cpu_s,
+                                         "contact_sweeps_per_s": cpu},
+            "speedup_vs_cpu": gpu / cpu}
+
+
 def batched_c3(count=512, seed=7):
     """512 independent lattices (dims U[3..20]x[3..20]x[2..10], mu U(0.1, 0.9))
     in one persistent launch per phase: FP32 throughput over a fixed budget,
@@ -478,7 +524,8 @@ def run_ours(args):
             for key, fn in (("time_to_tolerance_60x60x30", lambda: time_to_tolerance(d, s)),
                             ("batched_512_scenes", batched_c3),
                             ("time_stepping_80x80x40", time_stepping_c5),
-                            ("fc2d_granular_7002", fc2d_granular)):
+                            ("fc2d_granular_7002", fc2d_granular),
+                            ("rfc3d_rockfall_x1000", rfc3d_tiled)):
                 try:
                     sup[key] = fn()
                 except Exception as e:  # a failed extra must not lose the headline line
