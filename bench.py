@@ -539,6 +539,15 @@ def run_ours(args):
     return 0
 
 
+# measurements beside the headline line (also runnable alone: --supplementary)
+SUPPLEMENTARY = {
+    "fc2d_granular_7002": lambda: fc2d_granular(),
+    "rfc3d_rockfall_x1000": lambda: rfc3d_tiled(),
+    "batched_512_scenes": lambda: batched_c3(),
+    "time_stepping_80x80x40": lambda: time_stepping_c5(),
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -549,7 +558,12 @@ def main():
     ap.add_argument("--cpu-sweeps", type=int, default=30)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the time-to-tolerance, batched and time-stepping measurements")
+    ap.add_argument("--supplementary", choices=sorted(SUPPLEMENTARY), default=None,
+                    help="run only this supplementary measurement and print its JSON")
     args = ap.parse_args()
+    if args.supplementary:
+        print(json.dumps({"supplementary": args.supplementary, **SUPPLEMENTARY[args.supplementary]()}), flush=True)
+        return 0
     if args.impl == "reference":
         args.cpu_sweeps = max(1, min(args.cpu_sweeps, 10))
         return run_reference(args)
