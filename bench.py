@@ -329,7 +329,7 @@ def rfc3d_tiled(copies=1000, sample_copies=100, tol=1e-8):
         ctx.close()
     S = tile(sample_copies, 7)
     t = time.perf_counter()
-    ref = O.rfc3d_nsgs_port(S, tol=0.0, maxiter=200)
+    ref = O.rfc3d_nsgs_port(S, tol=tol, maxiter=10000)
     cpu_s = time.perf_counter() - t
     gpu = P.nc * res["iterations"] / (res["ms"] / 1e3)
     cpu = S.nc * ref.iterations / cpu_s

@@ -367,7 +367,7 @@ __device__ void grid_sum(double v[N], const Args& a, Reduce& R, cg::grid_group& 
   if (threadIdx.x == 0) {
     for (int i = 0; i < N; i++) {
       double s = 0.0;
-      for (int k = 0; k < NT / 32; k++) s += R.warp[k][i];
+      for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += R.warp[k][i];
       __stcg(&slot[4 * blockIdx.x + i], s);
     }
   }
@@ -568,7 +568,7 @@ struct rfc3dgpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
-  int nc = 0, ncol = 0, max_colour = 0, blocks = 1;
+  int nc = 0, ncol = 0, max_colour = 0, blocks = 1, threads = NT;
   double norm_q = 0.0;
   std::vector<int> perm, iperm, colour;
   std::vector<double> rho_host;
@@ -757,12 +757,18 @@ extern "C" int rfc3dgpu_ctx_set_problem(rfc3dgpu_ctx* c, int nc, const int64_t* 
   c->ncol = ncol;
   c->max_colour = 0;
   for (int k = 0; k < ncol; k++) c->max_colour = std::max(c->max_colour, cptr[k + 1] - cptr[k]);
-  // grid: enough blocks for the largest colour, all resident (cooperative)
-  int per_sm = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rfc3d_nsgs, NT, 0);
+  // grid: the largest colour spread over as many SMs as it fills (the local
+  // Newton is bound by the FP64 pipe of each SM), smaller blocks when it
+  // fills fewer SMs than the device has; all blocks resident (cooperative)
+  int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  int threads = NT;
+  while (threads > 32 && (c->max_colour + threads - 1) / threads < sms) threads /= 2;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rfc3d_nsgs, threads, 0);
   const int resident = std::max(1, std::min(per_sm * sms, MAX_BLOCKS));
-  c->blocks = std::max(1, std::min((c->max_colour + NT - 1) / NT, resident));
+  c->threads = threads;
+  c->blocks = std::max(1, std::min((c->max_colour + threads - 1) / threads, resident));
   return 0;
 }
 
@@ -802,7 +808,7 @@ static Args args_of(const rfc3dgpu_ctx* c) {
 template <typename K>
 static cudaError_t launch(rfc3dgpu_ctx* c, K kernel, Args& a) {
   void* params[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)kernel, dim3(c->blocks), dim3(NT), params, 0, c->stream);
+  return cudaLaunchCooperativeKernel((const void*)kernel, dim3(c->blocks), dim3(c->threads), params, 0, c->stream);
 }
 
 extern "C" int rfc3dgpu_ctx_solve(rfc3dgpu_ctx* c, double tol, int max_iter, double local_tol, int local_max_iter,
