@@ -14,10 +14,10 @@ contact-sweeps/s = contacts x sweeps / seconds.
   the device), per-step CUDA events on the solver's own stream, L2 flushed
   (256 MB write) between steps outside the timed events.
 * ``e2e``: the same solve through the reference-facing C-ABI
-  (fc3d_driver -> fc3dgpu_nsgs) with host buffers: each step marks W as
-  changed, so it uploads W (the colouring and layout are kept once the
-  unchanged structure is recognised on the device), q, mu, r from host memory
-  and copies r, u back (wall clock).
+  (fc3d_driver -> fc3dgpu_nsgs) with the caller's buffers in pinned host
+  memory: each step marks W as changed, so it uploads W (the colouring and
+  layout are kept once the unchanged structure is recognised on the device),
+  q, mu, r from host memory and copies r, u back (wall clock).
 * ``cpu_baseline``: the CPU restatement of the reference's fc3d_nsgs
   (bit-exact with it) on a bounded sample of the same scene, one core.
 * ``--impl reference``: the reference's own CPU fc3d_nsgs (oracle/_ref when it
@@ -460,15 +460,26 @@ def run_ours(args):
     # e2e through the reference-facing C-ABI with host buffers
     e2e_value, h2d, d2h = None, 0, 0
     if rank == 0 or ws > 1:
-        W = sn.SparseBlockMatrix(s.nc, s.rowptr, s.colidx, s.blocks)
-        P = sn.FrictionContactProblem(3, s.nc, W, s.q, s.mu)
+        # the caller's buffers in pinned host memory (what a time-stepping
+        # code that feeds a GPU allocates), handed over through the C-ABI
+        import torch
+        keep = []
+
+        def pinned(a):
+            t = torch.empty(a.shape, dtype=torch.from_numpy(np.ascontiguousarray(a)).dtype, pin_memory=True)
+            v = t.numpy()
+            v[...] = a
+            keep.append(t)
+            return v
+        W = sn.SparseBlockMatrix(s.nc, pinned(s.rowptr), pinned(s.colidx), pinned(s.blocks))
+        P = sn.FrictionContactProblem(3, s.nc, W, pinned(s.q), pinned(s.mu))
         o = sn.SolverOptions()
         o.iparam[sn.SICONOS_IPARAM_MAX_ITER] = S
         o.dparam[sn.SICONOS_DPARAM_TOL] = 1e-8
         o.dparam[sn.FC3DGPU_DPARAM_SWITCH_TOL] = 1e-300
         o.dparam[sn.FC3DGPU_DPARAM_STALL] = 1e9
-        r = np.zeros(3 * s.nc)
-        u = np.zeros(3 * s.nc)
+        r = pinned(np.zeros(3 * s.nc))
+        u = pinned(np.zeros(3 * s.nc))
 
         def e2e_step():
             W.bump_version()  # a new W each step: full upload

@@ -323,8 +323,16 @@ class SparseBlockMatrix:
         nnzb = int(self.rowptr[-1])
         if self.blocks.shape[0] != nnzb or self.colidx.shape[0] != nnzb:
             raise ValueError("block-CSR arrays disagree on the number of blocks")
-        self._i1 = self.rowptr.astype(np.uintp)
-        self._i2 = self.colidx.astype(np.uintp)
+        # size_t views of the caller's index arrays (non-negative int64 and
+        # size_t share a representation on the LP64 targets this builds for):
+        # no copy, so buffers the caller allocated (pinned, say) are used as is
+        if np.dtype(np.uintp).itemsize == 8 and (self.rowptr.size == 0 or self.rowptr.min() >= 0) and \
+                (self.colidx.size == 0 or self.colidx.min() >= 0):
+            self._i1 = self.rowptr.view(np.uintp)
+            self._i2 = self.colidx.view(np.uintp)
+        else:
+            self._i1 = self.rowptr.astype(np.uintp)
+            self._i2 = self.colidx.astype(np.uintp)
         self._bs = (self.bs * np.arange(1, self.nc + 1)).astype(np.uintp)
         base = self.blocks.ctypes.data
         self._ptrs = self._ptr_array(base, max(nnzb, 1), 8 * self.bs * self.bs)
