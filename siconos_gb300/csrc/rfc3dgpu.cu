@@ -78,9 +78,13 @@ __device__ void gepp5(const double* a, double* b) {
   for (int i = 0; i < 25; i++) A[i] = a[i];
 #pragma unroll
   for (int i = 0; i < 5; i++) x[i] = b[i];
+  // fully unrolled: the row multipliers of one pivot step are independent
+  // divisions, issued together
+#pragma unroll
   for (int i = 0; i < 5; i++) {
     int p = i;
     double best = fabs(E(A, i, i));
+#pragma unroll
     for (int k = i + 1; k < 5; k++)
       if (fabs(E(A, k, i)) > best) {
         best = fabs(E(A, k, i));
@@ -88,23 +92,35 @@ __device__ void gepp5(const double* a, double* b) {
       }
     if (best < 1e-16) return;
     if (p != i) {
-      for (int j = 0; j < 5; j++) {
-        const double t = E(A, i, j);
-        E(A, i, j) = E(A, p, j);
-        E(A, p, j) = t;
-      }
-      const double t = x[i];
-      x[i] = x[p];
-      x[p] = t;
+      // swap rows i and p (p > i), with register-resident indexing
+#pragma unroll
+      for (int k = i + 1; k < 5; k++)
+        if (k == p) {
+#pragma unroll
+          for (int j = 0; j < 5; j++) {
+            const double t = E(A, i, j);
+            E(A, i, j) = E(A, k, j);
+            E(A, k, j) = t;
+          }
+          const double t = x[i];
+          x[i] = x[k];
+          x[k] = t;
+        }
     }
+    double f[5];
+#pragma unroll
+    for (int k = i + 1; k < 5; k++) f[k] = E(A, k, i) / E(A, i, i);
+#pragma unroll
     for (int k = i + 1; k < 5; k++) {
-      const double f = E(A, k, i) / E(A, i, i);
-      for (int j = i; j < 5; j++) E(A, k, j) -= f * E(A, i, j);
-      x[k] -= f * x[i];
+#pragma unroll
+      for (int j = i; j < 5; j++) E(A, k, j) -= f[k] * E(A, i, j);
+      x[k] -= f[k] * x[i];
     }
   }
+#pragma unroll
   for (int i = 4; i >= 0; i--) {
     double s = 0;
+#pragma unroll
     for (int j = i + 1; j < 5; j++) s += E(A, i, j) * x[j];
     x[i] = (x[i] - s) / E(A, i, i);
   }
