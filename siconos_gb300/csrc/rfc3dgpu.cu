@@ -72,7 +72,7 @@ __device__ __forceinline__ void mm5(const double* a, const double* b, double* c)
 }
 
 // solve_5x5_gepp_for_loop (op5x5.h:642-700): b unchanged on a tiny pivot
-__device__ void gepp5(const double* a, double* b) {
+__device__ __forceinline__ void gepp5(const double* a, double* b) {
   double A[25], x[5];
 #pragma unroll
   for (int i = 0; i < 25; i++) A[i] = a[i];
@@ -132,10 +132,11 @@ __device__ void gepp5(const double* a, double* b) {
 
 enum { RC_DUAL = 0, RC_INSIDE, RC_FRICTION, RC_ROLLING, RC_FRICTION_ROLLING };
 
-__device__ int proj_rcone(double* r, double mu, double mur) {
+__device__ __forceinline__ int proj_rcone(double* r, double mu, double mur) {
   const double nT = sqrt(r[1] * r[1] + r[2] * r[2]);
   const double nM = sqrt(r[3] * r[3] + r[4] * r[4]);
   if (mu * nT + mur * nM <= -r[0]) {
+#pragma unroll
     for (int i = 0; i < 5; i++) r[i] = 0.0;
     return RC_DUAL;
   }
@@ -169,12 +170,14 @@ __device__ int proj_rcone(double* r, double mu, double mur) {
 
 // subdifferentialProjectionOnRollingCone (projectionOnRollingCone.c),
 // zero where the reference leaves the matrix unset
-__device__ void subdiff_rcone(double* H, const double* r, double mu, double mur) {
+__device__ __forceinline__ void subdiff_rcone(double* H, const double* r, double mu, double mur) {
+#pragma unroll
   for (int i = 0; i < 25; i++) H[i] = 0.0;
   const double nT = sqrt(r[1] * r[1] + r[2] * r[2]);
   const double nM = sqrt(r[3] * r[3] + r[4] * r[4]);
   if (mu * nT + mur * nM <= -r[0]) return;
   if ((nT <= mu * r[0]) && (nM <= mur * r[0])) {
+#pragma unroll
     for (int i = 0; i < 5; i++) E(H, i, i) = 1.;
     return;
   }
@@ -258,7 +261,7 @@ __device__ void subdiff_rcone(double* H, const double* r, double mu, double mur)
 }
 
 // rolling_friction_3D_computeNaturalMap (rolling_naturalmap_functions.c:31-165)
-__device__ void natural_map(const double* R, const double* v, double mu, double mur, double rho, double* F,
+__device__ __forceinline__ void natural_map(const double* R, const double* v, double mu, double mur, double rho, double* F,
                             double* A, double* B) {
   const double nVT = sqrt(v[1] * v[1] + v[2] * v[2]);
   const double nOT = sqrt(v[3] * v[3] + v[4] * v[4]);
@@ -268,13 +271,18 @@ __device__ void natural_map(const double* R, const double* v, double mu, double 
   RV[2] = R[2] - rho * v[2];
   RV[3] = R[3] - rho * v[3];
   RV[4] = R[4] - rho * v[4];
+#pragma unroll
   for (int i = 0; i < 5; i++) F[i] = RV[i];
   const int where = proj_rcone(F, mu, mur);
+#pragma unroll
   for (int i = 0; i < 5; i++) F[i] = R[i] - F[i];
   if (!A) return;
   if (where == RC_DUAL) {
+#pragma unroll
     for (int i = 0; i < 25; i++) A[i] = 0.;
+#pragma unroll
     for (int i = 0; i < 25; i++) B[i] = 0.;
+#pragma unroll
     for (int i = 0; i < 5; i++) E(B, i, i) = 1.;
     return;
   }
@@ -294,6 +302,7 @@ __device__ void natural_map(const double* R, const double* v, double mu, double 
     s4 = v[4] / nOT;
   }
   double D[25];
+#pragma unroll
   for (int i = 0; i < 25; i++) D[i] = 0.;
   E(D, 0, 0) = rho;
   E(D, 0, 1) = rho * mu * s1;
@@ -305,26 +314,32 @@ __device__ void natural_map(const double* R, const double* v, double mu, double 
   E(D, 3, 3) = rho;
   E(D, 4, 4) = rho;
   if (where == RC_INSIDE) {
+#pragma unroll
     for (int i = 0; i < 25; i++) A[i] = D[i];
+#pragma unroll
     for (int i = 0; i < 25; i++) B[i] = 0.;
     return;
   }
   double H[25];
   subdiff_rcone(H, RV, mu, mur);
   mm5(H, D, A);
+#pragma unroll
   for (int i = 0; i < 25; i++) B[i] = 0.;
+#pragma unroll
   for (int i = 0; i < 5; i++) E(B, i, i) = 1.;
+#pragma unroll
   for (int i = 0; i < 25; i++) B[i] -= H[i];
 }
 
 // rolling_friction_3d_onecone_nonsmooth_Newton_solvers_solve_direct
 // (rolling_friction_3d_onecone_nonsmooth_Newton_solvers.c:344-505)
-__device__ void local_nsn(const double* M, const double* q, double mu, double mur, double rho, double* r, double tol,
+__device__ __forceinline__ void local_nsn(const double* M, const double* q, double mu, double mur, double rho, double* r, double tol,
                           int itermax) {
   const double nq = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] + q[4] * q[4]);
   double rel = 1.0;
   if (nq > DBL_EPSILON) rel /= nq;
   double v[5], F[5], A[25], B[25], AWB[25], dR[5];
+#pragma unroll
   for (int i = 0; i < 5; i++) v[i] = q[i];
   mvp5(M, r, v);
   natural_map(r, v, mu, mur, rho, F, nullptr, nullptr);
@@ -333,11 +348,16 @@ __device__ void local_nsn(const double* M, const double* q, double mu, double mu
   for (int it = 1; it < itermax; it++) {
     natural_map(r, v, mu, mur, rho, F, A, B);
     mm5(A, M, AWB);
+#pragma unroll
     for (int i = 0; i < 25; i++) AWB[i] += B[i];
+#pragma unroll
     for (int i = 0; i < 25; i++) AWB[i] *= -1.;
+#pragma unroll
     for (int i = 0; i < 5; i++) dR[i] = F[i];
     gepp5(AWB, dR);
+#pragma unroll
     for (int i = 0; i < 5; i++) r[i] += dR[i];
+#pragma unroll
     for (int i = 0; i < 5; i++) v[i] = q[i];
     mvp5(M, r, v);
     natural_map(r, v, mu, mur, rho, F, nullptr, nullptr);
