@@ -1155,10 +1155,16 @@ extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const doubl
   k_set_q_mu<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->qo, c->muo, c->q64, c->mu64, c->q32, c->mu32);
   CK(cudaGetLastError());
   c->launches++;
-  // |q| as the reference computes it (a plain sum of squares in index order)
-  double s2 = 0.0;
-  for (long long i = 0; i < 3LL * nc; i++) s2 += q[i] * q[i];
-  c->norm_q = sqrt(s2);
+  // |q|: four interleaved partial sums of squares combined in a fixed order
+  // (deterministic; it overlaps the copies just queued, and a plain
+  // index-order sum would be a 3nc-long dependent chain on the host)
+  double s4[4] = {0.0, 0.0, 0.0, 0.0};
+  const long long n3 = 3LL * nc;
+  long long i = 0;
+  for (; i + 4 <= n3; i += 4)
+    for (int k = 0; k < 4; k++) s4[k] += q[i + k] * q[i + k];
+  for (; i < n3; i++) s4[0] += q[i] * q[i];
+  c->norm_q = sqrt((s4[0] + s4[1]) + (s4[2] + s4[3]));
   if (c->nscenes > 0) {
     c->scene_normq_h.assign(c->nscenes, 0.0);
     for (int g = 0; g < c->nscenes; g++) {
