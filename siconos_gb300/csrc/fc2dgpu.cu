@@ -29,6 +29,7 @@ constexpr int CS_MAX = 16;   // blocks per cluster at most (non-portable size)
 constexpr int MAXC = 128;
 constexpr int TRACE_CAP = 1 << 16;
 constexpr size_t REP_MAX_BYTES = 208 * 1024;  // shared-memory copy of the reactions at most
+constexpr int GRID_MAX = 1024;                 // blocks of a cooperative grid at most
 
 template <typename T>
 struct Vec2;
@@ -65,8 +66,45 @@ struct Args {
   double switch_tol;      // FP32 phase: stop below this light error
   int stall;              // FP32 phase: stop after this many sweeps without a new lowest error
   const double* before;   // out[] of the phase run before this one (or null)
+  double* part;           // grid team: 2 x GRID_MAX x 4 block partial sums
   double* trace;
   double* out;  // [0] sweeps, [1] final error, [2] info, [3] last light error
+};
+
+// The blocks that share a solve.  A thread-block cluster (up to 16 SMs):
+// hardware cluster barrier, partial sums exchanged through distributed
+// shared memory.  A cooperative grid (every SM, for colours too large for a
+// cluster): grid barrier, partial sums through a ring in global memory.
+struct ClusterTeam {
+  static constexpr bool grid = false;
+  cg::cluster_group cl;
+  __device__ ClusterTeam() : cl(cg::this_cluster()) {}
+  __device__ __forceinline__ int rank() const { return (int)cl.block_rank(); }
+  __device__ __forceinline__ int size() const { return (int)cl.num_blocks(); }
+  // barrier between colours: the hardware cluster barrier (about 670 cycles
+  // on this part), or the block barrier (about 290) for a one-block cluster
+  __device__ __forceinline__ void sync() {
+    if (size() == 1)
+      __syncthreads();
+    else
+      cl.sync();
+  }
+  __device__ __forceinline__ void sync_all() { cl.sync(); }
+};
+
+struct GridTeam {
+  static constexpr bool grid = true;
+  cg::grid_group g;
+  __device__ GridTeam() : g(cg::this_grid()) {}
+  __device__ __forceinline__ int rank() const { return (int)blockIdx.x; }
+  __device__ __forceinline__ int size() const { return (int)gridDim.x; }
+  __device__ __forceinline__ void sync() {
+    if (gridDim.x == 1)
+      __syncthreads();
+    else
+      g.sync();
+  }
+  __device__ __forceinline__ void sync_all() { sync(); }
 };
 
 // Where the sweep keeps the reactions.  HBM: read past L1 (ld.global.cg)
@@ -85,27 +123,19 @@ struct Reactions {
     if (REP) return rs[j];
     return __ldcg(reinterpret_cast<const V*>(rw) + j);
   }
-  __device__ __forceinline__ void put(int j, T x0, T x1, cg::cluster_group& cl) const {
+  template <typename Team>
+  __device__ __forceinline__ void put(int j, T x0, T x1, Team& t) const {
     V v;
     v.x = x0;
     v.y = x1;
-    if (REP) {
-      const int cs = (int)cl.num_blocks();
-      for (int k = 0; k < cs; k++) cl.map_shared_rank(rs, k)[j] = v;
+    if constexpr (REP && !Team::grid) {
+      const int cs = t.size();
+      for (int k = 0; k < cs; k++) t.cl.map_shared_rank(rs, k)[j] = v;
     } else {
       __stcg(reinterpret_cast<V*>(rw) + j, v);
     }
   }
 };
-
-// Barrier between colours: the hardware cluster barrier (about 670 cycles on
-// this part), or the block barrier (about 290) when the cluster is one block.
-__device__ __forceinline__ void colour_sync(cg::cluster_group& cl) {
-  if (cl.num_blocks() == 1)
-    __syncthreads();
-  else
-    cl.sync();
-}
 
 template <typename T, typename V>
 __device__ __forceinline__ void mvp2x2(const T* a, const V v, T* y) {
@@ -117,12 +147,13 @@ __device__ __forceinline__ void mvp2x2(const T* a, const V v, T* y) {
   y[1] += a23.y * v.y;
 }
 
-// Cluster-wide sum of N values per thread, in a fixed order (xor-shuffle tree
+// Team-wide sum of N values per thread, in a fixed order (xor-shuffle tree
 // in each warp, the warps in order, then the blocks in rank order), so every
-// block of the cluster gets the same bits.  The cluster barrier inside also
-// orders every reaction update made before the call.  `part` is a two-slot
-// ring: a block writes slot k & 1 only after the barrier of call k - 1, which
-// every block passes after reading call k - 2's slot.
+// block gets the same bits.  The barrier inside also orders every reaction
+// update made before the call.  The block partials go through a two-slot
+// ring (shared memory of each cluster block, or global memory for a grid): a
+// block writes slot k & 1 only after the barrier of call k - 1, which every
+// block passes after reading call k - 2's slot.
 template <typename T>
 struct Reduce {
   T part[2][4];
@@ -131,8 +162,8 @@ struct Reduce {
   int calls;
 };
 
-template <int N, typename T>
-__device__ __forceinline__ void cluster_sum(T v[N], Reduce<T>& R, cg::cluster_group& cl) {
+template <int N, typename T, typename Team>
+__device__ __forceinline__ void team_sum(T v[N], Reduce<T>& R, Team& team, double* gpart) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < N; i++) {
@@ -142,21 +173,35 @@ __device__ __forceinline__ void cluster_sum(T v[N], Reduce<T>& R, cg::cluster_gr
   }
   __syncthreads();
   const int slot = R.calls & 1;
+  double* gslot = gpart + (size_t)slot * GRID_MAX * 4;
   if (threadIdx.x == 0) {
     for (int i = 0; i < N; i++) {
       T s = 0;
       for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += R.warp[k][i];
-      R.part[slot][i] = s;
+      if constexpr (Team::grid)
+        __stcg(&gslot[4 * blockIdx.x + i], (double)s);
+      else
+        R.part[slot][i] = s;
     }
   }
-  colour_sync(cl);
-  if (w == 0) {
+  team.sync();
+  if constexpr (Team::grid) {
+    // thread 0 adds the blocks' partials in order
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < N; i++) {
+        T s = 0;
+        for (int b = 0; b < (int)gridDim.x; b++) s += (T)__ldcg(&gslot[4 * b + i]);
+        R.bcast[i] = s;
+      }
+      R.calls++;
+    }
+  } else if (w == 0) {
     // lane k fetches block k's partials (the remote loads overlap), lane 0
     // adds them in rank order
-    const int cs = (int)cl.num_blocks();
+    const int cs = team.size();
     T mine[N];
 #pragma unroll
-    for (int i = 0; i < N; i++) mine[i] = lane < cs ? cl.map_shared_rank(&R.part[slot][0], lane)[i] : T(0);
+    for (int i = 0; i < N; i++) mine[i] = lane < cs ? team.cl.map_shared_rank(&R.part[slot][0], lane)[i] : T(0);
 #pragma unroll
     for (int i = 0; i < N; i++) {
       T s = 0;
@@ -174,11 +219,11 @@ __device__ __forceinline__ void cluster_sum(T v[N], Reduce<T>& R, cg::cluster_gr
 // fc2d_compute_error (fc2d_compute_error.c:40-140): u = q + W r block by
 // block (per block w_i = 1.0 w_i + 1.0 (a_i0 r0 + a_i1 r1), the reference's
 // 2x2 gemv), natural-map error, relative to max(|r|, |u|, |q|).  FP64 only.
-template <bool REP>
+template <bool REP, typename Team>
 __device__ double full_error(const Args<double>& a, const Reactions<double, REP>& rx, Reduce<double>& R,
-                             cg::cluster_group& cl) {
+                             Team& team) {
   double v[3] = {0.0, 0.0, 0.0};
-  const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
+  const int g0 = team.rank() * blockDim.x + threadIdx.x, G = team.size() * blockDim.x;
   for (int p = g0; p < a.nc; p += G) {
     double w[2] = {a.q[2 * p], a.q[2 * p + 1]};
     for (int s = a.rp[p]; s < a.rp[p + 1]; s++) {
@@ -210,7 +255,7 @@ __device__ double full_error(const Args<double>& a, const Reactions<double, REP>
     v[1] += r0 * r0 + r1 * r1;
     v[2] += w[0] * w[0] + w[1] * w[1];
   }
-  cluster_sum<3>(v, R, cl);
+  team_sum<3>(v, R, team, a.part);
   double e = sqrt(v[0]);
   const double scal = fmax(sqrt(v[1]), fmax(sqrt(v[2]), a.norm_q));
   if (fabs(scal) > DBL_EPSILON) e /= scal;
@@ -243,9 +288,9 @@ __device__ __forceinline__ void local_solve(const T* W, T D, const T* q, T mu, T
 // Bring the FP64 reactions into the sweep's copy (replica or FP32 copy in
 // HBM); the cluster barrier keeps other blocks from writing into a copy
 // before it is filled.
-template <typename T, bool REP>
+template <typename T, bool REP, typename Team>
 __device__ __forceinline__ Reactions<T, REP> open_reactions(const Args<T>& a, typename Vec2<T>::type* smem,
-                                                            cg::cluster_group& cl) {
+                                                            Team& team) {
   using V = typename Vec2<T>::type;
   Reactions<T, REP> rx{smem, a.rw};
   const double2* r = reinterpret_cast<const double2*>(a.r);
@@ -257,9 +302,9 @@ __device__ __forceinline__ Reactions<T, REP> open_reactions(const Args<T>& a, ty
       v.y = (T)x.y;
       smem[j] = v;
     }
-    cl.sync();
+    team.sync_all();
   } else if (sizeof(T) != sizeof(double)) {
-    const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
+    const int g0 = team.rank() * blockDim.x + threadIdx.x, G = team.size() * blockDim.x;
     for (int j = g0; j < a.nc; j += G) {
       const double2 x = __ldcg(r + j);
       V v;
@@ -267,7 +312,7 @@ __device__ __forceinline__ Reactions<T, REP> open_reactions(const Args<T>& a, ty
       v.y = (T)x.y;
       __stcg(reinterpret_cast<V*>(a.rw) + j, v);
     }
-    cl.sync();
+    team.sync_all();
   }
   return rx;
 }
@@ -275,16 +320,16 @@ __device__ __forceinline__ Reactions<T, REP> open_reactions(const Args<T>& a, ty
 // Write the sweep's copy back to the FP64 reactions (each block its own
 // contacts), then hold every block until no other may still read its
 // shared memory.
-template <typename T, bool REP>
-__device__ __forceinline__ void close_reactions(const Args<T>& a, const Reactions<T, REP>& rx, cg::cluster_group& cl) {
+template <typename T, bool REP, typename Team>
+__device__ __forceinline__ void close_reactions(const Args<T>& a, const Reactions<T, REP>& rx, Team& team) {
   if (REP || sizeof(T) != sizeof(double)) {
-    const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
+    const int g0 = team.rank() * blockDim.x + threadIdx.x, G = team.size() * blockDim.x;
     for (int p = g0; p < a.nc; p += G) {
       const typename Vec2<T>::type x = rx.get(p);
       __stcg(reinterpret_cast<double2*>(a.r) + p, make_double2((double)x.x, (double)x.y));
     }
   }
-  cl.sync();
+  team.sync_all();
 }
 
 // All sweeps of one problem (or of one precision phase of it) in one launch
@@ -298,18 +343,18 @@ __device__ __forceinline__ void close_reactions(const Args<T>& a, const Reaction
 // (each contact is updated once per sweep, so it is |r|^2 after the sweep).
 // A phase that follows another starts its sweep count, budget and trace
 // where the previous one stopped (read from the device, no host round trip).
-template <typename T, bool REP>
+template <typename T, bool REP, typename Team>
 __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
   using V = typename Vec2<T>::type;
   extern __shared__ __align__(16) unsigned char dsm[];
   V* rsm = reinterpret_cast<V*>(dsm);
   __shared__ Reduce<T> R;
-  cg::cluster_group cl = cg::this_cluster();
+  Team team;
   if (threadIdx.x == 0) R.calls = 0;
   __syncthreads();
-  const Reactions<T, REP> rx = open_reactions<T, REP>(a, rsm, cl);
-  const int g0 = (int)cl.block_rank() * blockDim.x + threadIdx.x, G = (int)cl.num_blocks() * blockDim.x;
-  const bool lead = cl.block_rank() == 0 && threadIdx.x == 0;
+  const Reactions<T, REP> rx = open_reactions<T, REP>(a, rsm, team);
+  const int g0 = team.rank() * blockDim.x + threadIdx.x, G = team.size() * blockDim.x;
+  const bool lead = team.rank() == 0 && threadIdx.x == 0;
   const int done = a.before ? (int)a.before[0] : 0;
   const int budget = a.max_iter - done;
   T tolerance = (T)a.tol, err = (T)INFINITY, best = (T)INFINITY;
@@ -350,11 +395,11 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
         const T x0 = old.x - P[0], x1 = old.y - P[1];
         v[0] += x0 * x0 + x1 * x1;
         v[1] += P[0] * P[0] + P[1] * P[1];
-        rx.put(p, P[0], P[1], cl);
+        rx.put(p, P[0], P[1], team);
       }
-      if (c + 1 < a.ncol) colour_sync(cl);
+      if (c + 1 < a.ncol) team.sync();
     }
-    cluster_sum<2>(v, R, cl);
+    team_sum<2>(v, R, team, a.part);
     err = sqrt(v[0]);
     const T nr = sqrt(v[1]);
     if (fabs(nr) > (T)DBL_EPSILON) err /= nr;
@@ -373,7 +418,7 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
       // determine_convergence_with_full_final (fc2d_nsgs.c:187-228)
       not_conv = 0;
       if constexpr (sizeof(T) == sizeof(double)) {
-        const double full = full_error<REP>(a, rx, R, cl);
+        const double full = full_error<REP>(a, rx, R, team);
         if (full > a.tol) {
           tolerance = err / full * a.tol;
           not_conv = 1;
@@ -384,7 +429,7 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
   double final_err = (double)err;
   if constexpr (sizeof(T) == sizeof(double)) {
     if (a.mode == FULL_FINAL) {
-      final_err = full_error<REP>(a, rx, R, cl);
+      final_err = full_error<REP>(a, rx, R, team);
       not_conv = !(final_err < a.tol);
     } else if (a.mode == NO_EVAL) {
       final_err = INFINITY;  // no branch of the sweep loop evaluates an error (fc2d_nsgs.c:438-448)
@@ -397,20 +442,20 @@ __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_nsgs(const Args<T> a) {
     a.out[2] = not_conv;
     a.out[3] = (double)err;
   }
-  close_reactions<T, REP>(a, rx, cl);
+  close_reactions<T, REP>(a, rx, team);
 }
 
-template <bool REP>
+template <bool REP, typename Team>
 __global__ void __launch_bounds__(NT_MAX, 1) k_fc2d_error(const Args<double> a) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ Reduce<double> R;
-  cg::cluster_group cl = cg::this_cluster();
+  Team team;
   if (threadIdx.x == 0) R.calls = 0;
   __syncthreads();
-  const Reactions<double, REP> rx = open_reactions<double, REP>(a, reinterpret_cast<double2*>(dsm), cl);
-  const double e = full_error<REP>(a, rx, R, cl);
-  if (cl.block_rank() == 0 && threadIdx.x == 0) a.out[1] = e;
-  close_reactions<double, REP>(a, rx, cl);
+  const Reactions<double, REP> rx = open_reactions<double, REP>(a, reinterpret_cast<double2*>(dsm), team);
+  const double e = full_error<REP>(a, rx, R, team);
+  if (team.rank() == 0 && threadIdx.x == 0) a.out[1] = e;
+  close_reactions<double, REP>(a, rx, team);
 }
 
 }  // namespace fc2dgpu
@@ -426,6 +471,8 @@ struct fc2dgpu_ctx {
   int rep_req = 0;             // reactions: 0 automatic, 1 in HBM, 2 replicated in shared memory
   int cs = 1, nt = 128;        // launch shape of the current problem
   bool rep = false;
+  bool grid = false;           // a cooperative grid of `blocks` blocks instead of a cluster
+  int blocks = 1;
   int max_colour = 0;          // contacts in the largest colour
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -435,7 +482,7 @@ struct fc2dgpu_ctx {
   std::vector<int> perm, iperm, colour;
   int *cptr = nullptr, *rp = nullptr, *col = nullptr, *dpos = nullptr;
   double *W = nullptr, *det = nullptr, *q = nullptr, *mu = nullptr, *r = nullptr, *u = nullptr, *trace = nullptr,
-         *out = nullptr;
+         *out = nullptr, *part = nullptr;
   // FP32 copies for the first phase of a mixed-precision solve
   float *W32 = nullptr, *det32 = nullptr, *q32 = nullptr, *mu32 = nullptr, *r32 = nullptr;
   int precision = 1;          // 0 FP32 sweeps + FP64 polish, 1 FP64 sweeps only
@@ -473,6 +520,7 @@ extern "C" void fc2dgpu_ctx_destroy(fc2dgpu_ctx* c) {
   free_problem(c);
   if (c->trace) cudaFree(c->trace);
   if (c->out) cudaFree(c->out);
+  if (c->part) cudaFree(c->part);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -495,7 +543,8 @@ extern "C" fc2dgpu_ctx* fc2dgpu_ctx_create(int device) {
   bool ok = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreate(&c->ev[0]) == cudaSuccess && cudaEventCreate(&c->ev[1]) == cudaSuccess &&
             cudaMalloc(&c->trace, sizeof(double) * TRACE_CAP) == cudaSuccess &&
-            cudaMalloc(&c->out, sizeof(double) * 8) == cudaSuccess;
+            cudaMalloc(&c->out, sizeof(double) * 8) == cudaSuccess &&
+            cudaMalloc(&c->part, sizeof(double) * 2 * GRID_MAX * 4) == cudaSuccess;
   if (!ok) {
     fc3dgpu_set_error("fc2dgpu_ctx_create: set-up failed (%s)", cudaGetErrorString(cudaGetLastError()));
     fc2dgpu_ctx_destroy(c);
@@ -715,10 +764,10 @@ static bool cluster_fits(fc2dgpu_ctx* c, int cs, int nt, bool rep) {
   cudaLaunchAttribute attr[1];
   cudaLaunchConfig_t cfg = config(c, cs, nt, smem, attr);
   int n = 0;
-  cudaError_t e = rep ? prepare(k_fc2d_nsgs<double, true>, cs, smem) : prepare(k_fc2d_nsgs<double, false>, cs, smem);
+  cudaError_t e = rep ? prepare(k_fc2d_nsgs<double, true, ClusterTeam>, cs, smem) : prepare(k_fc2d_nsgs<double, false, ClusterTeam>, cs, smem);
   if (e == cudaSuccess)
-    e = rep ? cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<double, true>, &cfg)
-            : cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<double, false>, &cfg);
+    e = rep ? cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<double, true, ClusterTeam>, &cfg)
+            : cudaOccupancyMaxActiveClusters(&n, k_fc2d_nsgs<double, false, ClusterTeam>, &cfg);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return false;
@@ -726,7 +775,31 @@ static bool cluster_fits(fc2dgpu_ctx* c, int cs, int nt, bool rep) {
   return n > 0;
 }
 
+// A colour with more contacts than a full cluster has threads (16 x 512)
+// goes to a cooperative grid over every SM instead (grid barrier, about
+// 1-2 us, instead of the cluster's 0.3 us; the FP64 pipes of all SMs).
+constexpr int GRID_FROM = CS_MAX * NT_MAX;
+
+static void choose_grid(fc2dgpu_ctx* c) {
+  int nt = c->nt_req > 0 ? c->nt_req : 256;
+  nt = std::min(std::max(nt / 32 * 32, 32), NT_MAX);
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fc2d_nsgs<double, false, GridTeam>, nt, 0);
+  const int resident = std::max(1, std::min(per_sm * sms, GRID_MAX));
+  c->grid = true;
+  c->rep = false;
+  c->nt = nt;
+  c->cs = 1;
+  c->blocks = std::max(1, std::min((c->max_colour + nt - 1) / nt, resident));
+}
+
 static void choose_shape(fc2dgpu_ctx* c) {
+  if (c->cs_req < 0 || (c->cs_req == 0 && c->rep_req != 2 && c->max_colour > GRID_FROM)) {
+    choose_grid(c);
+    return;
+  }
+  c->grid = false;
   int cs = c->cs_req, nt = c->nt_req;
   if (cs <= 0) {
     const int want = (c->max_colour + 63) / 64;  // about 64 contacts per SM and colour
@@ -748,6 +821,12 @@ static void choose_shape(fc2dgpu_ctx* c) {
 }
 
 template <typename K, typename A>
+static cudaError_t launch_grid(fc2dgpu_ctx* c, K kernel, const A& a) {
+  void* params[] = {(void*)&a};
+  return cudaLaunchCooperativeKernel((const void*)kernel, dim3(c->blocks), dim3(c->nt), params, 0, c->stream);
+}
+
+template <typename K, typename A>
 static cudaError_t launch(fc2dgpu_ctx* c, K kernel, const A& a, size_t smem) {
   cudaError_t e = prepare(kernel, c->cs, smem);
   if (e != cudaSuccess) return e;
@@ -757,10 +836,10 @@ static cudaError_t launch(fc2dgpu_ctx* c, K kernel, const A& a, size_t smem) {
 }
 
 extern "C" int fc2dgpu_ctx_set_launch(fc2dgpu_ctx* c, int cluster_blocks, int threads, int reactions) {
-  if (!c || cluster_blocks < 0 || cluster_blocks > CS_MAX || threads < 0 || threads > NT_MAX ||
-      (threads && threads % 32) || reactions < 0 || reactions > 2) {
-    fc3dgpu_set_error("fc2dgpu_ctx_set_launch: cluster of 0..%d blocks, 0 or 32..%d threads (multiple of 32), "
-                      "reactions 0, 1 or 2", CS_MAX, NT_MAX);
+  if (!c || cluster_blocks < -1 || cluster_blocks > CS_MAX || threads < 0 || threads > NT_MAX ||
+      (threads && threads % 32) || reactions < 0 || reactions > 2 || (cluster_blocks < 0 && reactions == 2)) {
+    fc3dgpu_set_error("fc2dgpu_ctx_set_launch: cluster of 0..%d blocks (-1: cooperative grid, reactions in HBM), 0 or "
+                      "32..%d threads (multiple of 32), reactions 0, 1 or 2", CS_MAX, NT_MAX);
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
   if (reactions == 2 && (c->nc == 0 || rep_bytes(c) > REP_MAX_BYTES)) {
@@ -784,7 +863,7 @@ extern "C" int fc2dgpu_ctx_set_launch(fc2dgpu_ctx* c, int cluster_blocks, int th
 
 extern "C" int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx* c, int* cluster_blocks, int* threads, int* reactions) {
   if (!c) return NUMERICS_ERR_INVALID_ARGUMENT;
-  if (cluster_blocks) *cluster_blocks = c->cs;
+  if (cluster_blocks) *cluster_blocks = c->grid ? -c->blocks : c->cs;
   if (threads) *threads = c->nt;
   if (reactions) *reactions = c->rep ? 2 : 1;
   return 0;
@@ -809,6 +888,7 @@ static Args<double> args64(const fc2dgpu_ctx* c) {
   a.norm_q = c->norm_q;
   a.trace = c->trace;
   a.out = c->out;
+  a.part = c->part;
   return a;
 }
 
@@ -831,6 +911,7 @@ static Args<float> args32(const fc2dgpu_ctx* c) {
   a.norm_q = c->norm_q;
   a.trace = c->trace;
   a.out = c->out + 4;
+  a.part = c->part;
   return a;
 }
 
@@ -860,7 +941,9 @@ extern "C" int fc2dgpu_ctx_compute_error(fc2dgpu_ctx* c, double norm_q, double* 
   K2(cudaSetDevice(c->device));
   Args<double> a = args64(c);
   a.norm_q = norm_q;
-  K2(c->rep ? launch(c, k_fc2d_error<true>, a, rep_bytes(c)) : launch(c, k_fc2d_error<false>, a, 0));
+  K2(c->grid ? launch_grid(c, k_fc2d_error<false, GridTeam>, a)
+     : c->rep ? launch(c, k_fc2d_error<true, ClusterTeam>, a, rep_bytes(c))
+              : launch(c, k_fc2d_error<false, ClusterTeam>, a, 0));
   K2(cudaMemcpyAsync(error, c->out + 1, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   K2(cudaStreamSynchronize(c->stream));
   return 0;
@@ -905,11 +988,14 @@ extern "C" int fc2dgpu_ctx_solve(fc2dgpu_ctx* c, double tol, int max_iter, int e
     b.mode = FP32_PHASE;
     b.switch_tol = c->switch_tol > 0.0 ? c->switch_tol : std::max(tol, 1e-6);
     b.stall = c->stall;
-    K2(c->rep ? launch(c, k_fc2d_nsgs<float, true>, b, sizeof(float2) * (size_t)c->nc)
-              : launch(c, k_fc2d_nsgs<float, false>, b, 0));
+    K2(c->grid  ? launch_grid(c, k_fc2d_nsgs<float, false, GridTeam>, b)
+       : c->rep ? launch(c, k_fc2d_nsgs<float, true, ClusterTeam>, b, sizeof(float2) * (size_t)c->nc)
+                : launch(c, k_fc2d_nsgs<float, false, ClusterTeam>, b, 0));
     a.before = c->out + 4;
   }
-  K2(c->rep ? launch(c, k_fc2d_nsgs<double, true>, a, rep_bytes(c)) : launch(c, k_fc2d_nsgs<double, false>, a, 0));
+  K2(c->grid  ? launch_grid(c, k_fc2d_nsgs<double, false, GridTeam>, a)
+     : c->rep ? launch(c, k_fc2d_nsgs<double, true, ClusterTeam>, a, rep_bytes(c))
+              : launch(c, k_fc2d_nsgs<double, false, ClusterTeam>, a, 0));
   K2(cudaEventRecord(c->ev[1], c->stream));
   double out[8];
   K2(cudaMemcpyAsync(out, c->out, sizeof(out), cudaMemcpyDeviceToHost, c->stream));

@@ -146,3 +146,28 @@ def test_driver_argument_checks(built_lib):
     # contact freezing is not implemented by the coloured sweep
     o.iparam[sn.SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] = 5
     assert sn.fc2d_nsgs_gpu(P, r, u, o) == sn.NUMERICS_ERR_NOT_IMPLEMENTED
+
+
+def tiled2d(P, copies: int, seed: int):
+    """`copies` independent copies of a 2D problem along W's diagonal, q of
+    each copy scaled by a seeded factor in [0.9, 1.1]."""
+    import oracle as O
+    g = np.random.default_rng(seed)
+    nc, nb = P.nc, P.nnzb
+    rp = [0]
+    for c in range(copies):
+        rp.extend((P.rowptr[1:] + c * nb).tolist())
+    return O.Problem(copies * nc, np.asarray(rp, np.int64),
+                     np.concatenate([P.colidx + c * nc for c in range(copies)]).astype(np.int64),
+                     np.tile(np.asarray(P.blocks).reshape(nb, 4), (copies, 1)),
+                     np.tile(P.q, copies) * np.repeat(g.uniform(0.9, 1.1, copies), 2 * nc), np.tile(P.mu, copies), 2)
+
+
+def test_tiled2d_copies_are_independent():
+    import oracle as O
+    P, _ = load_fc2d("fc2d_FrictionContactProblem00071")
+    T = tiled2d(P, 3, 2)
+    res = O.fc2d_nsgs_port(T, tol=0.0, maxiter=6)
+    for c in range(3):
+        Pc = O.Problem(P.nc, P.rowptr, P.colidx, P.blocks, T.q[2 * c * P.nc:2 * (c + 1) * P.nc], P.mu, 2)
+        np.testing.assert_array_equal(res.r[2 * c * P.nc:2 * (c + 1) * P.nc], O.fc2d_nsgs_port(Pc, tol=0.0, maxiter=6).r)

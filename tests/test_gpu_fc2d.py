@@ -102,10 +102,11 @@ def test_driver_solves_fixture(sn, case):
 
 
 @pytest.mark.parametrize("shape", [(1, 32, 1), (1, 512, 2), (2, 64, 1), (8, 128, 2), (16, 32, 1), (16, 32, 2),
-                                   (16, 512, 1), (16, 128, 2)])
+                                   (16, 512, 1), (16, 128, 2), (-1, 256, 1), (-1, 32, 1)])
 def test_launch_shape_does_not_change_iterates(sn, shape):
-    """Any cluster size, block size and place of the reactions gives the same
-    reaction bits; the errors differ only by the order of their sums."""
+    """Any cluster size (or a cooperative grid, -1), block size and place of
+    the reactions gives the same reaction bits; the errors differ only by the
+    order of their sums."""
     import oracle as O
     P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_02020_00213")
     ctx = _ctx(sn, P)
@@ -115,7 +116,10 @@ def test_launch_shape_does_not_change_iterates(sn, shape):
     except RuntimeError as e:
         assert "does not fit" in str(e)
         pytest.skip(f"cluster shape {shape} cannot be resident on this device")
-    assert got == shape
+    if shape[0] < 0:
+        assert got[0] < 0 and got[1:] == shape[1:]  # a grid of -got[0] blocks
+    else:
+        assert got == shape
     res = ctx.solve(0.0, 25)
     r, u = ctx.get_r_u()
     ref = O.fc2d_nsgs_port(P, tol=0.0, maxiter=25, order=_order(colour))
@@ -302,4 +306,30 @@ def test_mixed_precision_solve(sn, case):
     np.testing.assert_array_equal(u, ref.u)
     assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
     assert res["info"] == int(g["info"]) == 0 and res["error"] < 1e-5
+    ctx.close()
+
+
+def test_large_problem_runs_on_a_grid(sn):
+    """8 copies of the 7,002-contact granular problem (56,016 contacts): the
+    largest colour exceeds a full cluster, so the solve runs on a cooperative
+    grid over every SM; same bits as the oracle in colour order."""
+    import oracle as O
+    from test_fc2d_oracle import tiled2d
+    P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_07002_00801")
+    T = tiled2d(P, 8, 5)
+    ctx = _ctx(sn, T)
+    cs, nt, rx = ctx.launch_shape()
+    assert cs < 0 and rx == 1
+    _, colour = ctx.colours()
+    res = ctx.solve(0.0, 12)
+    r, u = ctx.get_r_u()
+    ref = O.fc2d_nsgs_port(T, tol=0.0, maxiter=12, order=_order(colour))
+    np.testing.assert_array_equal(r, ref.r)
+    np.testing.assert_array_equal(u, ref.u)
+    assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
+    ctx.set_precision(0, 1e-30, 1 << 20)
+    ctx.set_r(np.zeros(2 * T.nc))
+    ctx.solve(1e-5, 12)
+    r32, _ = ctx.get_r_u()
+    np.testing.assert_array_equal(r32, O.fc2d_sweeps_f32_port(T, np.zeros(2 * T.nc), 12, order=_order(colour)))
     ctx.close()
