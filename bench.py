@@ -292,6 +292,43 @@ def fc2d_granular(case="fc2d_fc2d_granularflowonwall_07002_00801", tol=1e-5, rep
     cpu = out["cpu_reference_port_1core"]["ms"]
     for k in ("gpu_fp64", "gpu_fp32_fp64_polish", "reference_design_gpu"):
         out[k]["speedup_vs_cpu"] = cpu / out[k]["ms"]
+    # 40 independent copies along W's diagonal (280,080 contacts; q of each
+    # copy scaled by a seeded factor in [0.9, 1.1]): colours too large for a
+    # cluster, so the solve runs on a cooperative grid over every SM; the CPU
+    # side measured on 4 copies; both as contact-sweeps/s
+    def tile(k, seed):
+        g = np.random.default_rng(seed)
+        nb = int(z["rowptr"][-1])
+        rp = [0]
+        for c in range(k):
+            rp.extend((z["rowptr"][1:] + c * nb).tolist())
+        return (k * nc, np.asarray(rp, np.int64),
+                np.concatenate([z["colidx"] + c * nc for c in range(k)]).astype(np.int64),
+                np.tile(np.asarray(z["blocks"]).reshape(nb, 4), (k, 1)),
+                np.tile(z["q"], k) * np.repeat(g.uniform(0.9, 1.1, k), 2 * nc), np.tile(z["mu"], k))
+    big = tile(40, 5)
+    ctx = sn.Fc2dContext(*big)
+    try:
+        row = {"contacts": big[0], "launch_shape": list(ctx.launch_shape())}
+        for name, prec in (("gpu_fp64", 1), ("gpu_fp32_fp64_polish", 0)):
+            ctx.set_precision(prec)
+            ctx.set_r(np.zeros(2 * big[0]))
+            ctx.solve(tol, 20)
+            ctx.set_r(np.zeros(2 * big[0]))
+            res = ctx.solve(tol, 10000)
+            row[name] = {"ms": res["ms"], "sweeps": res["iterations"], "info": res["info"], "error": res["error"],
+                         "contact_sweeps_per_s": big[0] * res["iterations"] / (res["ms"] / 1e3)}
+    finally:
+        ctx.close()
+    small = tile(4, 5)
+    t = time.perf_counter()
+    ref = O.fc2d_nsgs_port(O.Problem(*small, 2), tol=tol, maxiter=10000)
+    cpu_s = time.perf_counter() - t
+    row["cpu_reference_port_1core"] = {"contacts": small[0], "sweeps": ref.iterations, "s": cpu_s,
+                                       "contact_sweeps_per_s": small[0] * ref.iterations / cpu_s}
+    for k in ("gpu_fp64", "gpu_fp32_fp64_polish"):
+        row[k]["speedup_vs_cpu"] = row[k]["contact_sweeps_per_s"] / row["cpu_reference_port_1core"]["contact_sweeps_per_s"]
+    out["tiled_x40"] = row
     return out
 
 
