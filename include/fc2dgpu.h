@@ -9,9 +9,10 @@
  * the reference returns it.  Contacts are visited in colour order (contacts
  * of one colour share no W block), so the FP64 iterates are those of the
  * reference's sequential sweep run in that order, bit for bit.  One
- * thread-block cluster (up to 16 SMs) runs all sweeps of a problem in one
- * launch, with the hardware cluster barrier between colours and the
- * convergence logic on the device: no host round trip per sweep.
+ * thread-block cluster (up to 16 SMs; a cooperative grid over every SM when
+ * a colour is larger than a cluster) runs all sweeps of a problem in one
+ * launch, with a hardware barrier between colours and the convergence logic
+ * on the device: no host round trip per sweep.
  *
  * Buffers of the solver-level calls are HOST memory owned by the caller. */
 #ifndef FC2DGPU_H
@@ -101,11 +102,13 @@ int fc2dgpu_ctx_compute_error(fc2dgpu_ctx *ctx, double norm_q, double *error);
 /* Colour of each contact and the number of colours (return value). */
 int fc2dgpu_ctx_colours(fc2dgpu_ctx *ctx, int32_t *colour);
 /* Launch shape of the sweep kernel: a thread-block cluster of
- * cluster_blocks blocks (1..16) of `threads` threads (32..512, a multiple
- * of 32), the reactions kept in HBM (reactions = 1) or replicated in every
- * block's shared memory (2, up to 13,312 contacts); 0 picks each from the
- * problem (the default).  The iterates do not depend on the shape; the
- * reduction order of the errors does. */
+ * cluster_blocks blocks (1..16; -1: a cooperative grid over every SM) of
+ * `threads` threads (32..512, a multiple of 32), the reactions kept in HBM
+ * (reactions = 1) or replicated in every cluster block's shared memory (2,
+ * up to 13,312 contacts); 0 picks each from the problem (the default).
+ * fc2dgpu_ctx_launch_shape reports a grid as minus its block count.  The
+ * iterates do not depend on the shape; the reduction order of the errors
+ * does. */
 int fc2dgpu_ctx_set_launch(fc2dgpu_ctx *ctx, int cluster_blocks, int threads, int reactions);
 int fc2dgpu_ctx_launch_shape(fc2dgpu_ctx *ctx, int *cluster_blocks, int *threads, int *reactions);
 /* Per-sweep light error of the last solve (cap entries); returns how many. */

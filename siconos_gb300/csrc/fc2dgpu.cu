@@ -3,7 +3,8 @@
 // Layout: contacts permuted by colour (stable in contact order); per permuted
 // row its blocks in the caller's order (diagonal included, at dpos), each a
 // 2x2 column-major block, with the permuted column index; q, mu, r, u in
-// permuted order.  One thread-block cluster per problem (see k_fc2d_nsgs).
+// permuted order.  One thread-block cluster per problem, or a cooperative
+// grid over every SM when a colour is larger than a cluster (k_fc2d_nsgs).
 // FP64 without FMA contraction, in the reference's operation order.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -333,7 +334,7 @@ __device__ __forceinline__ void close_reactions(const Args<T>& a, const Reaction
 }
 
 // All sweeps of one problem (or of one precision phase of it) in one launch
-// of one thread-block cluster.  A colour's contacts are spread over the
+// of one thread-block cluster or one cooperative grid (the Team).  A colour's contacts are spread over the
 // cluster's threads (contact lo + g, lo + g + G, ... for global thread g of
 // G: a contact always lands on the same block, so its W row stays in that
 // SM's L1); the hardware cluster barrier (release / acquire) separates
