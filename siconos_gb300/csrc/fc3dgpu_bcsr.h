@@ -18,10 +18,17 @@ typedef struct {
   int64_t *rowptr;
   int64_t *colidx;
   double *blocks;
-  int borrowed; /* arrays point into the caller's SBM, not owned */
+  const double *const *block; /* or one pointer per block (then blocks is NULL) */
+  int borrowed;               /* arrays point into the caller's SBM, not owned */
 } Bcsr;
 
+/* Flat blocks: SBM storage whose blocks already sit back to back is viewed,
+ * other SBM storage and dense storage are repacked. */
 int fc3dgpu_bcsr_from_problem(const FrictionContactProblem *P, int d, Bcsr *out);
+/* As fc3dgpu_bcsr_from_problem, but SBM storage with every block row filled
+ * is viewed as is, blocks through its block pointer array (no pass over the
+ * blocks; for fc3dgpu_ctx_update_W_ptrs). */
+int fc3dgpu_bcsr_view(const FrictionContactProblem *P, int d, Bcsr *out);
 void fc3dgpu_bcsr_free(Bcsr *b);
 /* SolverOptions with iparam/dparam of the reference's size, max_iter and tol
  * set, as solver_options_create does. */

@@ -723,6 +723,8 @@ struct fc3dgpu_ctx {
   int colour_kind = -1;  // colouring of the current layout
   BUF(long long, wtmp);  // new structure for a comparison with the current one
   BUF(int, wdiff);
+  double* stage = nullptr;  // pinned staging for blocks gathered from scattered pointers
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
   // device assembly of W and q from rigid-body contacts
   int nb = 0;
   double step_h = 0.0;
@@ -838,6 +840,9 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
   if (c->nbrmask) cudaFree(c->nbrmask);
   for (int i = 0; i < 4; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  for (int i = 0; i < 2; i++)
+    if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
+  if (c->stage) cudaFreeHost(c->stage);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -926,10 +931,85 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, const
 
 static int build_layout(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, int nscenes, const int* scene_nc);
 
-static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx, const double* blocks,
+// The values of W: one array of nnzb column-major 3x3 blocks (flat), or one
+// pointer per block (ptrs[k] -> 9 doubles), the layout of the block array of
+// a SparseBlockStructuredMatrix (SparseBlockMatrix.h, block[k]).
+struct BlockSource {
+  const double* flat;
+  const double* const* ptrs;
+};
+
+// Blocks scanned per step of upload_blocks, and the longest run of adjacent
+// blocks sent as one copy.
+static const long long STAGE_BLOCKS = 1 << 16;
+static const long long RUN_BLOCKS = 1 << 19;
+
+// Copy nnzb blocks from src into c->blocks (stream-ordered).  From a block
+// pointer array, runs of blocks that lie back to back in memory are copied
+// straight from there, each run sent while the pointers after it are still
+// being checked; other blocks are gathered into two pinned staging buffers
+// used in turn.
+static int upload_blocks(fc3dgpu_ctx* c, long long nnzb, BlockSource src) {
+  cudaStream_t s = c->stream;
+  if (src.flat) {
+    CK(cudaMemcpyAsync(c->blocks, src.flat, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+  const double* const* p = src.ptrs;
+  long long run0 = 0, runn = 0;  // pending run of adjacent blocks: first index, length
+  int slot = 0;
+  for (long long k0 = 0; k0 < nnzb; k0 += STAGE_BLOCKS) {
+    const long long k1 = k0 + STAGE_BLOCKS < nnzb ? k0 + STAGE_BLOCKS : nnzb;
+    const double* base = p[k0];
+    if (!base) {
+      fc3dgpu_set_error("block %lld of W is a null pointer", k0);
+      return NUMERICS_ERR_NULL_POINTER;
+    }
+    const uintptr_t b0 = (uintptr_t)base, bsz = sizeof(double) * 9;
+    uintptr_t off = 0;  // zero when p[k0..k1) are adjacent 9-double blocks
+    for (long long k = k0; k < k1; k++) off |= (uintptr_t)p[k] ^ (b0 + bsz * (uintptr_t)(k - k0));
+    if (off == 0 && runn > 0 && b0 == (uintptr_t)p[run0] + bsz * (uintptr_t)(k0 - run0) &&
+        runn + (k1 - k0) <= RUN_BLOCKS) {
+      runn += k1 - k0;
+      continue;
+    }
+    if (runn > 0)
+      CK(cudaMemcpyAsync(c->blocks + 9 * run0, p[run0], sizeof(double) * 9 * runn, cudaMemcpyHostToDevice, s));
+    runn = 0;
+    if (off == 0) {
+      run0 = k0;
+      runn = k1 - k0;
+      continue;
+    }
+    // scattered blocks: gather through a staging buffer once its last copy is done
+    if (!c->stage) {
+      CK(cudaHostAlloc((void**)&c->stage, sizeof(double) * 9 * 2 * STAGE_BLOCKS, cudaHostAllocDefault));
+      for (int b = 0; b < 2; b++) CK(cudaEventCreateWithFlags(&c->stage_ev[b], cudaEventDisableTiming));
+    } else {
+      CK(cudaEventSynchronize(c->stage_ev[slot]));
+    }
+    double* buf = c->stage + 9 * STAGE_BLOCKS * slot;
+    for (long long k = k0; k < k1; k++) {
+      if (!p[k]) {
+        fc3dgpu_set_error("block %lld of W is a null pointer", k);
+        CK(cudaStreamSynchronize(s));
+        return NUMERICS_ERR_NULL_POINTER;
+      }
+      memcpy(buf + 9 * (k - k0), p[k], sizeof(double) * 9);
+    }
+    CK(cudaMemcpyAsync(c->blocks + 9 * k0, buf, sizeof(double) * 9 * (k1 - k0), cudaMemcpyHostToDevice, s));
+    CK(cudaEventRecord(c->stage_ev[slot], s));
+    slot ^= 1;
+  }
+  if (runn > 0)
+    CK(cudaMemcpyAsync(c->blocks + 9 * run0, p[run0], sizeof(double) * 9 * runn, cudaMemcpyHostToDevice, s));
+  return 0;
+}
+
+static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx, BlockSource blocks,
                       int kind, int nscenes, const int* scene_nc) {
   using namespace fc3dgpu;
-  if (!c || nc <= 0 || !rowptr || !colidx || !blocks) {
+  if (!c || nc <= 0 || !rowptr || !colidx || (!blocks.flat && !blocks.ptrs)) {
     fc3dgpu_set_error("fc3dgpu_ctx_set_W: invalid argument");
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
@@ -951,7 +1031,10 @@ static int set_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64
   CK(ensure(&c->blocks, &c->blocks_cap, (size_t)nnzb * 9));
   CK(cudaMemcpyAsync(c->rowptr, rowptr, sizeof(long long) * (nc + 1), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->colidx, colidx, sizeof(long long) * nnzb, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(c->blocks, blocks, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+  {
+    int rc = upload_blocks(c, nnzb, blocks);
+    if (rc) return rc;
+  }
   return build_layout(c, nc, nnzb, kind, nscenes, scene_nc);
 }
 
@@ -1098,7 +1181,7 @@ extern "C" int fc3dgpu_ctx_set_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, 
     cudaGraphExecDestroy(c->batch_graph);
     c->batch_graph = nullptr;
   }
-  return set_W_impl(c, nc, rowptr, colidx, blocks, kind, 0, nullptr);
+  return set_W_impl(c, nc, rowptr, colidx, BlockSource{blocks, nullptr}, kind, 0, nullptr);
 }
 
 // Many independent problems as one block-diagonal W: the union block-CSR
@@ -1137,7 +1220,11 @@ extern "C" int fc3dgpu_ctx_set_W_batch(fc3dgpu_ctx* c, int nscenes, const int* s
     cudaGraphExecDestroy(c->batch_graph);
     c->batch_graph = nullptr;
   }
-  return set_W_impl(c, (int)nc, rowptr, colidx, blocks, kind, nscenes, scene_nc);
+  if (!blocks) {
+    fc3dgpu_set_error("fc3dgpu_ctx_set_W_batch: invalid argument");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  return set_W_impl(c, (int)nc, rowptr, colidx, BlockSource{blocks, nullptr}, kind, nscenes, scene_nc);
 }
 
 extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const double* mu) {
@@ -2285,16 +2372,21 @@ __global__ void k_differs(long long n, const long long* __restrict__ a, const lo
 }
 }  // namespace fc3dgpu
 
-extern "C" int fc3dgpu_ctx_update_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx,
-                                    const double* blocks, int kind) {
+static int update_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx, BlockSource blocks,
+                         int kind) {
   using namespace fc3dgpu;
-  if (!c || nc <= 0 || !rowptr || !colidx || !blocks) {
+  if (!c || nc <= 0 || !rowptr || !colidx || (!blocks.flat && !blocks.ptrs)) {
     fc3dgpu_set_error("fc3dgpu_ctx_update_W: invalid argument");
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
   if (!c->have_W || c->nscenes > 0 || c->have_contacts || nc != c->nc || rowptr[nc] != c->nnzb ||
-      kind != c->colour_kind)
-    return fc3dgpu_ctx_set_W(c, nc, rowptr, colidx, blocks, kind);
+      kind != c->colour_kind) {
+    if (c->batch_graph) {
+      cudaGraphExecDestroy(c->batch_graph);
+      c->batch_graph = nullptr;
+    }
+    return set_W_impl(c, nc, rowptr, colidx, blocks, kind, 0, nullptr);
+  }
   CK(cudaSetDevice(c->device));
   cudaStream_t s = c->stream;
   const long long nnzb = c->nnzb;
@@ -2313,9 +2405,19 @@ extern "C" int fc3dgpu_ctx_update_W(fc3dgpu_ctx* c, int nc, const int64_t* rowpt
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
   c->launches += 2;
-  if (diff) return fc3dgpu_ctx_set_W(c, nc, rowptr, colidx, blocks, kind);
+  if (diff) {
+    if (c->batch_graph) {
+      cudaGraphExecDestroy(c->batch_graph);
+      c->batch_graph = nullptr;
+    }
+    return set_W_impl(c, nc, rowptr, colidx, blocks, kind, 0, nullptr);
+  }
   // same structure: new values into the existing layout
-  CK(cudaMemcpyAsync(c->blocks, blocks, sizeof(double) * 9 * nnzb, cudaMemcpyHostToDevice, s));
+  c->have_W = false;
+  {
+    int rc = upload_blocks(c, nnzb, blocks);
+    if (rc) return rc;
+  }
   const long long nw = c->nslots * 9 * FC3D_SLAB;
   k_fill_blocks<<<grid1d(nc, 128), 128, 0, s>>>(nc, c->rowptr, c->colidx, c->blocks, c->iperm, c->slab_off, c->W64,
                                                 c->col, c->D64, c->rho64);
@@ -2325,5 +2427,16 @@ extern "C" int fc3dgpu_ctx_update_W(fc3dgpu_ctx* c, int nc, const int64_t* rowpt
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s));
   c->launches += 4;
+  c->have_W = true;
   return 0;
+}
+
+extern "C" int fc3dgpu_ctx_update_W(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx,
+                                    const double* blocks, int kind) {
+  return update_W_impl(c, nc, rowptr, colidx, BlockSource{blocks, nullptr}, kind);
+}
+
+extern "C" int fc3dgpu_ctx_update_W_ptrs(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const int64_t* colidx,
+                                         const double* const* block, int kind) {
+  return update_W_impl(c, nc, rowptr, colidx, BlockSource{nullptr, block}, kind);
 }

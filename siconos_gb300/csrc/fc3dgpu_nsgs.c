@@ -157,7 +157,7 @@ void fc3dgpu_bcsr_free(Bcsr *b) {
   memset(b, 0, sizeof(*b));
 }
 
-int fc3dgpu_bcsr_from_problem(const FrictionContactProblem *P, int d, Bcsr *out) {
+static int bcsr_impl(const FrictionContactProblem *P, int d, Bcsr *out, int block_ptrs) {
   memset(out, 0, sizeof(*out));
   const int nc = P->numberOfContacts;
   const NumericsMatrix *M = P->M;
@@ -186,6 +186,13 @@ int fc3dgpu_bcsr_from_problem(const FrictionContactProblem *P, int d, Bcsr *out)
     /* Zero-copy view when every block row is filled and the blocks sit
      * back to back in one allocation (size_t and int64_t share a layout on
      * the LP64 targets this library builds for). */
+    if (sizeof(size_t) == sizeof(int64_t) && nrows_filled == (size_t)nc && nnzb > 0 && block_ptrs) {
+      out->rowptr = (int64_t *)S->index1_data;
+      out->colidx = (int64_t *)S->index2_data;
+      out->block = (const double *const *)S->block;
+      out->borrowed = 1;
+      return 0;
+    }
     if (sizeof(size_t) == sizeof(int64_t) && nrows_filled == (size_t)nc && nnzb > 0) {
       int contiguous = 1;
       for (long long k = 1; k < nnzb && contiguous; k++) contiguous = (S->block[k] == S->block[0] + dd * k);
@@ -257,6 +264,23 @@ int fc3dgpu_bcsr_from_problem(const FrictionContactProblem *P, int d, Bcsr *out)
   }
   fc3dgpu_set_error("storage type %d is not supported (SBM or dense only)", (int)M->storageType);
   return NUMERICS_ERR_NOT_IMPLEMENTED;
+}
+
+int fc3dgpu_bcsr_from_problem(const FrictionContactProblem *P, int d, Bcsr *out) { return bcsr_impl(P, d, out, 0); }
+
+int fc3dgpu_bcsr_view(const FrictionContactProblem *P, int d, Bcsr *out) { return bcsr_impl(P, d, out, 1); }
+
+/* W of the problem onto the device: new values keep the layout when the
+ * structure is unchanged (fc3dgpu_ctx_update_W[_ptrs]). */
+static int upload_W(fc3dgpu_ctx *ctx, const FrictionContactProblem *P, int kind, long long *nnzb) {
+  Bcsr b;
+  int rc = fc3dgpu_bcsr_view(P, 3, &b);
+  if (rc) return rc;
+  rc = b.block ? fc3dgpu_ctx_update_W_ptrs(ctx, b.nc, b.rowptr, b.colidx, b.block, kind)
+               : fc3dgpu_ctx_update_W(ctx, b.nc, b.rowptr, b.colidx, b.blocks, kind);
+  if (nnzb) *nnzb = b.nnzb;
+  fc3dgpu_bcsr_free(&b);
+  return rc;
 }
 
 static int check_problem(const FrictionContactProblem *P, const double *r, const double *u) {
@@ -362,14 +386,9 @@ static int cached_ctx(FrictionContactProblem *P, SolverOptions *o, fc3dgpu_ctx *
     c->ctx = fc3dgpu_ctx_create(0);
     if (!c->ctx) return NUMERICS_ERR_NOT_IMPLEMENTED;
   }
-  Bcsr b;
-  int rc = fc3dgpu_bcsr_from_problem(P, 3, &b);
-  if (rc) return rc;
   /* a W that changed since the cached one is most often new values on the
    * same structure (time stepping with fixed contacts): keep the layout then */
-  rc = fc3dgpu_ctx_update_W(c->ctx, b.nc, b.rowptr, b.colidx, b.blocks, kind);
-  c->nnzb = b.nnzb;
-  fc3dgpu_bcsr_free(&b);
+  int rc = upload_W(c->ctx, P, kind, &c->nnzb);
   if (rc) {
     c->M = NULL;
     return rc;
@@ -495,12 +514,7 @@ int fc3dgpu_compute_error(FrictionContactProblem *problem, double *reaction, dou
   if (!error) return NUMERICS_ERR_NULL_POINTER;
   fc3dgpu_ctx *ctx = fc3dgpu_ctx_create(0);
   if (!ctx) return NUMERICS_ERR_NOT_IMPLEMENTED;
-  Bcsr b;
-  rc = fc3dgpu_bcsr_from_problem(problem, 3, &b);
-  if (!rc) {
-    rc = fc3dgpu_ctx_set_W(ctx, b.nc, b.rowptr, b.colidx, b.blocks, 0);
-    fc3dgpu_bcsr_free(&b);
-  }
+  rc = upload_W(ctx, problem, 0, NULL);
   if (!rc) rc = fc3dgpu_ctx_set_q_mu(ctx, problem->q, problem->mu);
   if (!rc) rc = fc3dgpu_ctx_set_r(ctx, reaction);
   if (!rc) rc = fc3dgpu_ctx_set_norm_q(ctx, norm_q);

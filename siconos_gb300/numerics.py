@@ -166,6 +166,7 @@ ABI = {
     "fc3dgpu_ctx_set_W": (C.c_int, [C.c_void_p, C.c_int, _I64, _I64, _F64, C.c_int]),
     "fc3dgpu_ctx_set_q_mu": (C.c_int, [C.c_void_p, _F64, _F64]),
     "fc3dgpu_ctx_update_W": (C.c_int, [C.c_void_p, C.c_int, _I64, _I64, _F64, C.c_int]),
+    "fc3dgpu_ctx_update_W_ptrs": (C.c_int, [C.c_void_p, C.c_int, _I64, _I64, C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_set_W_batch": (C.c_int, [C.c_void_p, C.c_int, _I32, _I64, _I64, _F64, C.c_int]),
     "fc3dgpu_ctx_solve_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),

@@ -9,6 +9,8 @@
   reactions and velocities close to the reference's;
 * at the 60x60x30 scale, size-independent properties hold.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -235,3 +237,125 @@ def test_update_W_values_equals_fresh_upload(gpu):
     rc = L.fc3dgpu_ctx_update_W(gpu.ctx, t.nc, t.rowptr, t.colidx, np.ascontiguousarray(t.blocks).reshape(-1),
                                 sn.FC3DGPU_COLOURING_DEFAULT)
     assert rc == 0 and gpu.sizes()[0] == t.nc
+
+
+def _block_ptrs(blocks, layout, seed=0):
+    """A store holding the blocks and one pointer per block into it, laid out
+    as SBM storage may be: adjacent ("contiguous"), permuted inside a few
+    windows that cross the upload's 65,536-block steps ("windows"), in two
+    separate arrays split at a step boundary ("two_arrays") or all permuted
+    ("reversed")."""
+    nnzb = blocks.shape[0]
+    pos = np.arange(nnzb)
+    stores = []
+    if layout == "windows":
+        g = np.random.default_rng(seed)
+        for a, b in ((70000, 70100), (131072, 200000), (300000, nnzb)):
+            pos[a:b] = a + g.permutation(b - a)
+    elif layout == "reversed":
+        pos = pos[::-1].copy()
+    if layout == "two_arrays":
+        cut = 3 * 65536
+        a, b = np.ascontiguousarray(blocks[:cut]), np.ascontiguousarray(blocks[cut:])
+        ptrs = np.concatenate([a.ctypes.data + 72 * np.arange(cut, dtype=np.uint64),
+                               b.ctypes.data + 72 * np.arange(nnzb - cut, dtype=np.uint64)]).astype(np.uintp)
+        stores = [a, b]
+    else:
+        st = np.empty_like(blocks)
+        st[pos] = blocks
+        ptrs = (st.ctypes.data + 72 * pos.astype(np.uint64)).astype(np.uintp)
+        stores = [st]
+    return ptrs, stores
+
+
+@pytest.mark.parametrize("layout", ["contiguous", "windows", "two_arrays", "reversed"])
+def test_update_W_from_block_pointers(gpu, layout):
+    """fc3dgpu_ctx_update_W_ptrs (values through one pointer per block, the
+    SBM block array) loads the same W as the flat upload, whatever the
+    blocks' placement: the same blocks on the device and the same 15 FP64
+    sweeps bit for bit; on a context without W it is the full upload."""
+    import siconos_gb300.numerics as sn
+    from siconos_gb300 import scene
+    from siconos_gb300.device import DeviceSolver
+    s = scene.lattice(30, 30, 15, seed=5)
+    assert s.nnzb > 400000
+    blocks2 = np.ascontiguousarray(s.blocks.reshape(-1, 9) * 1.25)
+    L = gpu.L
+    gpu.load(s)
+    rc = L.fc3dgpu_ctx_update_W(gpu.ctx, s.nc, s.rowptr, s.colidx, blocks2.reshape(-1), sn.FC3DGPU_COLOURING_DEFAULT)
+    assert rc == 0, sn.last_error()
+    gpu.set_q_mu(s.q, s.mu)
+    gpu.zero_r()
+    st1 = gpu.solve(tol=1e-300, max_iter=15, precision=1)
+    r1, _ = gpu.get()
+    gpu.load(s)
+    ptrs, keep = _block_ptrs(blocks2, layout)
+    rc = L.fc3dgpu_ctx_update_W_ptrs(gpu.ctx, s.nc, s.rowptr, s.colidx, ptrs.ctypes.data, sn.FC3DGPU_COLOURING_DEFAULT)
+    assert rc == 0, sn.last_error()
+    assert np.array_equal(gpu.get_W()[2], blocks2)
+    gpu.set_q_mu(s.q, s.mu)
+    gpu.zero_r()
+    st2 = gpu.solve(tol=1e-300, max_iter=15, precision=1)
+    r2, _ = gpu.get()
+    assert (r1 == r2).all() and st1["error"] == st2["error"]
+    fresh = DeviceSolver(0)
+    try:
+        rc = L.fc3dgpu_ctx_update_W_ptrs(fresh.ctx, s.nc, s.rowptr, s.colidx, ptrs.ctypes.data,
+                                         sn.FC3DGPU_COLOURING_DEFAULT)
+        assert rc == 0, sn.last_error()
+        fresh.nc = s.nc
+        assert np.array_equal(fresh.get_W()[2], blocks2)
+        fresh.set_q_mu(s.q, s.mu)
+        fresh.zero_r()
+        st3 = fresh.solve(tol=1e-300, max_iter=15, precision=1)
+        assert (fresh.get()[0] == r1).all() and st3["error"] == st1["error"]
+    finally:
+        fresh.close()
+    del keep
+
+
+def test_update_W_null_block_pointer_is_an_error(gpu):
+    import siconos_gb300.numerics as sn
+    from siconos_gb300 import scene
+    s = scene.lattice(16, 16, 8, seed=5)
+    gpu.load(s)
+    blocks = np.ascontiguousarray(s.blocks.reshape(-1, 9))
+    for k in (0, 5, 70000 % s.nnzb):
+        ptrs, keep = _block_ptrs(blocks, "reversed")
+        ptrs[k] = 0
+        rc = gpu.L.fc3dgpu_ctx_update_W_ptrs(gpu.ctx, s.nc, s.rowptr, s.colidx, ptrs.ctypes.data,
+                                             sn.FC3DGPU_COLOURING_DEFAULT)
+        assert rc == sn.NUMERICS_ERR_NULL_POINTER and "null pointer" in sn.last_error()
+    # the context takes the next upload
+    ptrs, keep = _block_ptrs(blocks, "contiguous")
+    assert gpu.L.fc3dgpu_ctx_update_W_ptrs(gpu.ctx, s.nc, s.rowptr, s.colidx, ptrs.ctypes.data,
+                                           sn.FC3DGPU_COLOURING_DEFAULT) == 0
+    gpu.set_q_mu(s.q, s.mu)
+    gpu.zero_r()
+    assert gpu.solve(tol=1e-8, max_iter=1000)["status"] == 0
+
+
+def test_driver_with_scattered_sbm_blocks(gpu):
+    """fc3d_driver on SBM storage whose blocks are not adjacent in memory (as
+    separately allocated blocks are) solves exactly as with adjacent ones."""
+    P, _ = load_case("fixture_KaplasTower_i1061_4")
+    info1, r1, u1, _ = _driver(P)
+    import siconos_gb300.numerics as sn
+    W = sn.SparseBlockMatrix(P.nc, P.rowptr, P.colidx, P.blocks)
+    ptrs, keep = _block_ptrs(np.ascontiguousarray(P.blocks.reshape(-1, 9)), "reversed")
+    W.c.block = C.cast(ptrs.ctypes.data, type(W.c.block))
+    prob = sn.FrictionContactProblem(3, P.nc, W, P.q.copy(), P.mu.copy())
+    o = sn.SolverOptions()
+    o.iparam[sn.SICONOS_IPARAM_MAX_ITER] = 10000
+    o.dparam[sn.SICONOS_DPARAM_TOL] = 1e-8
+    r, u = np.zeros(3 * P.nc), np.zeros(3 * P.nc)
+    info = sn.fc3d_driver(prob, r, u, o)
+    assert info == info1 and (r == r1).all() and (u == u1).all()
+    # new values behind the same pointers: the cached layout takes them
+    for k in range(len(keep)):
+        keep[k] *= 1.0
+    W.bump_version()
+    r[:] = 0
+    assert sn.fc3d_driver(prob, r, u, o) == info1 and (r == r1).all()
+    o.release()
+    del keep
