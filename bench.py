@@ -60,7 +60,7 @@ def _peaks():
 
 def _traffic_per_sweep():
     """DRAM bytes per FP32 sweep from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "nsgs_kernel_f32_lattice_60x60x30.md"
+    p = ROOT / "profiles" / "nsgs_flow_kernel_lattice_60x60x30.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -488,7 +488,7 @@ def run_ours(args):
     achieved = bytes_launch / (sum(fp32_ms) / len(fp32_ms) / 1e3) / 1e9
     peak, peak_kind = _peaks()
     tps = _traffic_per_sweep()
-    roof = {"kernel": "nsgs_kernel<float,1> (persistent coloured FP32 sweeps, one launch per step)",
+    roof = {"kernel": "nsgs_flow_kernel<12> (slab-dataflow FP32 sweeps, one persistent launch per step)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": achieved / peak,
             "traffic": (tps * sum(fp32_sweeps) / len(fp32_sweeps)) if tps else None,

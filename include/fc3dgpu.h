@@ -45,9 +45,12 @@ extern "C" {
 /* Colouring kind: low byte 0 = hash priority, 1 = largest degree first;
  * FC3DGPU_COLOUR_PASSES(n) adds n iterated-greedy recolouring passes (the
  * classes revisited in reverse order), which shrink the small last colours:
- * on the 60x60x30 lattice 10 colours become 8. */
+ * on the 60x60x30 lattice 10 colours become 8; FC3DGPU_COLOUR_KEMPE then
+ * empties classes by Kempe-chain exchanges (fc3dgpu_colour_reduce, each
+ * problem of a batch on its own): 8 become 6. */
 #define FC3DGPU_COLOUR_PASSES(n) ((n) << 8)
-#define FC3DGPU_COLOURING_DEFAULT FC3DGPU_COLOUR_PASSES(4)
+#define FC3DGPU_COLOUR_KEMPE (1 << 16)
+#define FC3DGPU_COLOURING_DEFAULT (FC3DGPU_COLOUR_PASSES(4) | FC3DGPU_COLOUR_KEMPE)
 #define FC3DGPU_IPARAM_SWEEPS_FP64 28 /* out: FP64 sweeps done */
 #define FC3DGPU_IPARAM_COLOURS 29     /* out: number of colours */
 #define FC3DGPU_DPARAM_SWITCH_TOL 23  /* in: FP32 -> FP64 switch on the incremental error (default 1e-6) */
@@ -105,6 +108,15 @@ int fc3dgpu_nsgs_batch(int nproblems, FrictionContactProblem **problems, double 
  * decreasing priority, computed in Jones-Plassmann rounds on the GPU.
  * Returns the number of colours, <0 on failure. */
 int fc3dgpu_colour(int nc, const int64_t *rowptr, const int64_t *colidx, int kind, int32_t *colour);
+/* Host Kempe-chain reduction of a proper colouring: empties the highest
+ * colour classes while each of their contacts can take a lower colour,
+ * directly or after exchanging two colours on Kempe components (on a cubic
+ * sphere lattice: the greedy 8 colours become 6).  gptr/adj: the conflict
+ * graph as symmetric CSR; work_cap bounds one Kempe search (<= 0: nc).
+ * Returns the new number of colours (<0: out of memory, colour still
+ * proper).  Colouring kinds with FC3DGPU_COLOUR_KEMPE apply it after the
+ * device colouring. */
+int fc3dgpu_colour_reduce(int nc, const int *gptr, const int *adj, int *colour, int ncol, int work_cap);
 
 /* Device facts: SM count, L2 bytes, whether kernels can read pageable host
  * memory (and through the host page tables), cooperative launch support,
@@ -204,7 +216,10 @@ int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out8)
  * row-product pass, its number of local solves, and (staged sweeps) after the
  * staging wait and after the first slab round (entries 6, 7 spare); copies
  * the last record into out (cap entries) and returns how many were copied.
- * sweep 0 stops. */
+ * sweep 0 stops.  With the dataflow sweep (fc3dgpu_ctx_flow) the record is
+ * per slab: out[slab*8 + {0..5}] = globaltimer before the wait for its
+ * column slabs, after it, after its data landed in shared memory, after the
+ * row products, after the local solves, and its number of local solves. */
 int fc3dgpu_ctx_timeline(fc3dgpu_ctx *ctx, int sweep, unsigned long long *out, int cap);
 /* Bulk-copy (TMA) staging of each block's slab range into shared memory
  * in the FP32 sweeps: 1 on (default), 0 off.  Returns the previous value. */
@@ -214,6 +229,13 @@ int fc3dgpu_ctx_staging(fc3dgpu_ctx *ctx, int on);
  * with its own, 0 a grid-wide barrier after every colour.  Both give the same
  * iterates.  Returns the previous setting. */
 int fc3dgpu_ctx_sync(fc3dgpu_ctx *ctx, int neighbourhood);
+/* FP32 sweeps as a slab dataflow (1, default): each warp updates whole
+ * 32-row slabs once the slabs holding their columns reached the state the
+ * sequential sweep in colour order reads (per-slab completion counters, no
+ * barrier between colours); 0 the coloured kernel above.  The same sweep
+ * either way.  Applies with one lane per contact when no slab has more
+ * than 16 off-diagonal slots.  Returns the previous setting. */
+int fc3dgpu_ctx_flow(fc3dgpu_ctx *ctx, int on);
 /* r = 0 on the device (PLI steps reset), without a host copy. */
 int fc3dgpu_ctx_zero_r(fc3dgpu_ctx *ctx);
 /* The CUDA stream (cudaStream_t) every kernel of this context runs on, for

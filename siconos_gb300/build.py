@@ -20,7 +20,7 @@ OUT = PKG / "_lib"
 LIB = OUT / "libfc3dgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c", "rfc3dgpu_nsgs.c"]
+C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c", "rfc3dgpu_nsgs.c", "fc3d_colour.c"]
 CU_SOURCES = {
     "fc3dgpu_ctx.cu": ["--fmad=false"],
     "fc3dgpu_sweep_f64.cu": ["--fmad=false"],

@@ -692,6 +692,15 @@ struct fc3dgpu_ctx {
   int ccount[FC3D_MAX_COLOURS];
   std::vector<int> slab_nslot_h;
   int staging = 1;  // bulk-copy staging of slab ranges for the FP32 sweeps
+  // slab-dataflow FP32 sweep: on/off, and its per-layout column lists
+  // (state 0: not built for this layout, 1: built, -1: does not apply)
+  int flow_on = 1;
+  int flow_state = 0;
+  int flow_nw = 0, flow_maxslot = 0;
+  BUF(int, flow_dptr);
+  BUF(int, flow_dep);
+  BUF(unsigned, flow_done);
+  BUF(int, flow_sptr);
   // batched problems (0 = a single problem)
   int nscenes = 0;
   std::vector<int> scene_off_h;  // nscenes + 1 contact offsets
@@ -829,7 +838,8 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->counters, c->timeline, c->scene_off, c->grp, c->scounts, c->snslab, c->sncol, c->sbase,
                   c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64, c->feat,
                   c->prop, c->rbak, c->gapo, c->cbA, c->cbB, c->cframe, c->cpoint, c->bpos, c->bmass,
-                  c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum, c->wtmp, c->wdiff};
+                  c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum, c->wtmp, c->wdiff,
+                  c->flow_dptr, c->flow_dep, c->flow_done, c->flow_sptr};
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -896,6 +906,7 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, const
   CK(cudaMemcpyAsync(c->cursor, c->gptr, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s));
   k_adjacency<<<grid1d(nc), 256, 0, s>>>(nc, c->rowptr, c->colidx, c->cursor, c->adj);
   const int passes = (kind >> 8) & 0xff;
+  const bool kempe = (kind & FC3DGPU_COLOUR_KEMPE) != 0;
   kind &= 0xff;
   k_priority<<<grid1d(nc), 256, 0, s>>>(nc, c->gptr, c->adj, kind, c->key, c->colour, grp, group_off);
   int ncol = 0;
@@ -925,6 +936,38 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, const
     CK(cudaMemcpyAsync(&mx, c->scratch + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     ncol = mx + 1;
+  }
+  if (kempe && ncol > 1) {
+    // Kempe-chain reduction on the host (deterministic: it does not depend
+    // on the order of the adjacency lists the device wrote)
+    std::vector<int> gptr((size_t)nc + 1), adj((size_t)(nadj ? nadj : 1)), col((size_t)nc);
+    CK(cudaMemcpyAsync(gptr.data(), c->gptr, sizeof(int) * (nc + 1), cudaMemcpyDeviceToHost, s));
+    if (nadj) CK(cudaMemcpyAsync(adj.data(), c->adj, sizeof(int) * nadj, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(col.data(), c->colour, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (!grp) {
+      const int n = fc3dgpu_colour_reduce(nc, gptr.data(), adj.data(), col.data(), ncol, 0);
+      if (n > 0) ncol = n;
+    } else {
+      // each problem on its own (its rows only meet its own rows), so it
+      // gets the colouring it would get alone
+      std::vector<int> lg, la;
+      int mx = 0;
+      for (size_t g = 0; g + 1 < c->scene_off_h.size(); g++) {
+        const int o0 = c->scene_off_h[g], n = c->scene_off_h[g + 1] - o0;
+        lg.assign((size_t)n + 1, 0);
+        for (int k = 0; k <= n; k++) lg[k] = gptr[o0 + k] - gptr[o0];
+        la.assign((size_t)std::max(lg[n], 1), 0);
+        for (int k = 0; k < lg[n]; k++) la[k] = adj[gptr[o0] + k] - o0;
+        int ng = 0;
+        for (int k = 0; k < n; k++) ng = std::max(ng, col[o0 + k] + 1);
+        const int r = fc3dgpu_colour_reduce(n, lg.data(), la.data(), col.data() + o0, ng, 0);
+        mx = std::max(mx, r > 0 ? r : ng);
+      }
+      ncol = mx;
+    }
+    CK(cudaMemcpyAsync(c->colour, col.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
   }
   return ncol;
 }
@@ -1172,6 +1215,7 @@ static int build_layout(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, int ns
   c->have_W = true;
   c->colour_kind = kind;
   for (auto& n : c->nbrc) n.grid = 0;  // the rows' owners changed
+  c->flow_state = 0;
   return 0;
 }
 
@@ -1317,6 +1361,15 @@ extern "C" int fc3dgpu_ctx_staging(fc3dgpu_ctx* c, int on) {
   if (!c) return -1;
   const int old = c->staging;
   c->staging = on ? 1 : 0;
+  return old;
+}
+
+// Slab-dataflow FP32 sweep (no barriers between colours): on (1, default)
+// or off (0, the coloured persistent kernel).  Returns the previous setting.
+extern "C" int fc3dgpu_ctx_flow(fc3dgpu_ctx* c, int on) {
+  if (!c) return -1;
+  const int old = c->flow_on;
+  c->flow_on = on ? 1 : 0;
   return old;
 }
 
@@ -1505,6 +1558,44 @@ static size_t staging_sizes(fc3dgpu_ctx* c, int grid, unsigned* wb, unsigned* cb
   return tot;
 }
 
+// Column-slab lists of the dataflow sweep for the current layout; leaves
+// c->flow_state 1 when the sweep applies, -1 when not (slabs longer than
+// FC3D_FLOW_MAXSLOT or than the per-warp buffers allow).
+static int prepare_flow(fc3dgpu_ctx* c) {
+  using namespace fc3dgpu;
+  if (c->flow_state != 0) return 0;
+  c->flow_state = -1;
+  if (c->nscenes > 0 || c->ncol < 2 || c->nslab <= 0) return 0;
+  int maxslot = 0;
+  for (int s = 0; s < c->nslab; s++) maxslot = std::max(maxslot, c->slab_nslot_h[s]);
+  if (maxslot > FC3D_FLOW_MAXSLOT) return 0;
+  const int nw = flow_warps(maxslot);
+  if (nw == 0) return 0;
+  cudaStream_t s = c->stream;
+  const int nslab = c->nslab;
+  CK(ensure(&c->flow_dptr, &c->flow_dptr_cap, (size_t)nslab + 1));
+  CK(ensure(&c->flow_done, &c->flow_done_cap, (size_t)nslab));
+  CK(ensure(&c->flow_sptr, &c->flow_sptr_cap, FC3D_MAX_COLOURS + 1));
+  CK(cudaMemcpyAsync(c->flow_sptr, c->sptr, sizeof(int) * (FC3D_MAX_COLOURS + 1), cudaMemcpyHostToDevice, s));
+  // counts, their prefix sum on the host, then the lists
+  CK(build_flow_deps(nslab, c->npad, c->ncol, c->flow_sptr, c->perm, c->slab_nslot, c->slab_off, c->col, nullptr,
+                     c->flow_dptr, nullptr, s));
+  std::vector<int> ptr((size_t)nslab + 1, 0);
+  CK(cudaMemcpyAsync(ptr.data() + 1, c->flow_dptr, sizeof(int) * nslab, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int k = 0; k < nslab; k++) ptr[k + 1] += ptr[k];
+  CK(ensure(&c->flow_dep, &c->flow_dep_cap, (size_t)std::max(ptr[nslab], 1)));
+  CK(cudaMemcpyAsync(c->flow_dptr, ptr.data(), sizeof(int) * (nslab + 1), cudaMemcpyHostToDevice, s));
+  CK(build_flow_deps(nslab, c->npad, c->ncol, c->flow_sptr, c->perm, c->slab_nslot, c->slab_off, c->col,
+                     c->flow_dptr, nullptr, c->flow_dep, s));
+  CK(cudaStreamSynchronize(s));
+  c->launches += 2;
+  c->flow_nw = nw;
+  c->flow_maxslot = maxslot;
+  c->flow_state = 1;
+  return 0;
+}
+
 static int autotune_lanes(fc3dgpu_ctx* c) {
   // Measured on GB300 (60x60x30 lattice, 10 colours): one lane per contact
   // is fastest while a colour phase holds at least one 32-contact slab per
@@ -1564,10 +1655,28 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     k_r64_to_r32<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r64, c->r32);
     CK(cudaGetLastError());
     c->launches++;
-    if (lanes == 1)
+    bool flow = lanes == 1 && c->flow_on && !a.counters;
+    if (flow) {
+      if (int rc = prepare_flow(c)) return rc;
+      flow = c->flow_state == 1;
+    }
+    if (lanes == 1 && !flow)
       if (int rc = attach_nbr<float>(c, a, sweep_grid_f32(1))) return rc;
     CK(cudaMemsetAsync(c->barrier, 0, FC3D_BARRIER_WORDS * sizeof(unsigned), s));
-    CK(launch_sweep_f32(a, lanes, 0, smem, s, &grid));
+    if (flow) {
+      // the per-slab timeline fits the buffer up to this many slabs
+      if (c->nslab > FC3D_MAX_COLOURS * 1024) a.timeline = nullptr;
+      FlowArgs f;
+      f.dptr = c->flow_dptr;
+      f.dep = c->flow_dep;
+      f.done = c->flow_done;
+      f.maxslot = c->flow_maxslot;
+      f.buf_bytes = flow_buf_bytes(c->flow_maxslot);
+      CK(cudaMemsetAsync(c->flow_done, 0, sizeof(unsigned) * c->nslab, s));
+      CK(launch_flow_f32(a, f, c->flow_nw, s, &grid));
+    } else {
+      CK(launch_sweep_f32(a, lanes, 0, smem, s, &grid));
+    }
     c->launches++;
     CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(c->ev[1], s));

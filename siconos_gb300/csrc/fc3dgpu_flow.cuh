@@ -1,0 +1,365 @@
+// Slab-dataflow FP32 sweep: the coloured Gauss-Seidel sweep without
+// barriers between colours.
+//
+// The persistent sweep kernel (fc3dgpu_sweep.cuh) separates the colours of
+// a sweep by block-level barriers, so every colour costs the slowest
+// neighbour block's whole phase.  Here each warp owns whole 32-row slabs
+// (slab s goes to warp s mod warps, so a warp meets its slabs in colour
+// order) and each slab carries a completion counter: done[s] = the number
+// of sweeps in which its rows were updated.  Before updating slab s in
+// sweep k a warp waits, for every slab d holding a column of one of its
+// rows, until
+//
+//   done[d] >= k      when d has an earlier colour (its new reactions),
+//   done[d] >= k - 1  when d has a later colour (its previous reactions,
+//                     read before d may overwrite them: d waits for s),
+//
+// which is exactly the order of the sequential sweep in colour order
+// (fc3d_nsgs.c:711-875 visiting the contacts colour by colour): every row
+// reads the reactions a sequential sweep would read.  The (sweep, colour)
+// order of the waits is acyclic and every warp is resident (cooperative
+// launch), so the earliest unfinished slab can always proceed.  The light
+// error of a sweep (fc3d_nsgs.c:80-96) and the stop rules still need one
+// grid barrier per sweep.
+//
+// While a warp waits for a slab's columns, the bulk-copy engine brings that
+// slab's W, column indices, q, diagonal block, mu and rho into the warp's
+// shared-memory buffer; the next slab's copy is issued as soon as the
+// current one's inputs are in registers.
+#pragma once
+#include "fc3dgpu_sweep.cuh"
+
+namespace fc3dgpu {
+
+__device__ __forceinline__ void flow_issue(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned char* buf,
+                                           unsigned long long* bar) {
+  const long long o0 = a.slab_off[s];
+  const int ns = a.slab_nslot[s];
+  const unsigned wb = (unsigned)ns * 9 * FC3D_SLAB * 4, cb = (unsigned)ns * FC3D_SLAB * 4;
+  unsigned char* sc = buf + (size_t)f.maxslot * 9 * FC3D_SLAB * 4;
+  unsigned char* sq = sc + (size_t)f.maxslot * FC3D_SLAB * 4;
+  unsigned char* sd = sq + 3 * FC3D_SLAB * 4;
+  unsigned char* sm = sd + 9 * FC3D_SLAB * 4;
+  unsigned char* sr = sm + FC3D_SLAB * 4;
+  mbar_arrive_expect_tx(bar, wb + cb + (3 + 9 + 1 + 2) * FC3D_SLAB * 4);
+  if (wb) bulk_g2s(buf, a.W + (size_t)o0 * 9 * FC3D_SLAB, wb, bar);
+  if (cb) bulk_g2s(sc, a.col + (size_t)o0 * FC3D_SLAB, cb, bar);
+  bulk_g2s(sq, a.q + (size_t)s * 3 * FC3D_SLAB, 3 * FC3D_SLAB * 4, bar);
+  bulk_g2s(sd, a.D + (size_t)s * 9 * FC3D_SLAB, 9 * FC3D_SLAB * 4, bar);
+  bulk_g2s(sm, a.mu + (size_t)s * FC3D_SLAB, FC3D_SLAB * 4, bar);
+  bulk_g2s(sr, a.rho + (size_t)s * 2 * FC3D_SLAB, 2 * FC3D_SLAB * 4, bar);
+}
+
+// Sum of N values over the block (fixed order), written to out_partials.
+template <int N, int NW>
+__device__ __forceinline__ void flow_block_sum(double v[N], double* out_partials) {
+  __shared__ double sh[NW][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    double x = v[i];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[w][i] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < N) {
+    double s = 0.0;
+    for (int k = 0; k < NW; k++) s += sh[k][threadIdx.x];
+    out_partials[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+template <int NW>
+__device__ __forceinline__ bool flow_full_error(const SweepArgs<float>& a, unsigned& epoch, double& full) {
+  double v[3];
+  full_error_rows(a, v);
+  flow_block_sum<3, NW>(v, a.partials + blockIdx.x * 8 + 2);
+  if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) return false;
+  double s[3];
+  grid_sum<3>(a.partials, 2, s);
+  double e = sqrt(s[0]);
+  const double scal = fmax(a.norm_q, fmax(sqrt(s[2]), sqrt(s[1])));
+  if (fabs(scal) > DBL_EPSILON) e /= scal;
+  full = e;
+  return true;
+}
+
+// Wait until every slab slab s takes columns from has reached the state
+// sweep k needs (see the header).  Relaxed polls, then an acquire fence; the
+// caller's __syncwarp orders the other lanes' reads after it.
+__device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned k,
+                                               int lane) {
+  const int d0 = __ldg(&f.dptr[s]), d1 = __ldg(&f.dptr[s + 1]);
+  unsigned long long n = 0;
+  bool ok = true;
+  for (;;) {
+    bool mine = true;
+    for (int i = d0 + lane; i < d1; i += 32) {
+      const int d = __ldg(&f.dep[i]);
+      mine &= ld_relaxed_u32(&f.done[d & 0x7fffffff]) >= (d < 0 ? k - 1 : k);
+    }
+    if (__all_sync(0xffffffffu, mine)) break;
+    if (++n > a.spin_limit) {
+      ok = false;
+      if (lane == 0) atomicOr(a.status, 1);
+      break;
+    }
+    if (n > 1024) __nanosleep(64);
+  }
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  return ok;
+}
+
+// Row product, take-off test and local solve of the 32 rows of slab s from
+// the warp's buffer; issues the copy of slab `next` (or none when next < 0)
+// once the buffer is read.
+// Inputs of slab s the columns' state does not affect: the row's presence,
+// the slab's slot count and the row's own reaction (only this warp writes
+// it), loaded before the wait for the column slabs.
+struct FlowRow {
+  bool row;
+  int ns;
+  float ro[3];
+};
+
+__device__ __forceinline__ FlowRow flow_row(const SweepArgs<float>& a, int s, int lane) {
+  FlowRow x;
+  const int p = s * FC3D_SLAB + lane;
+  x.row = __ldg(&a.perm[p]) >= 0;
+  x.ns = __ldg(&a.slab_nslot[s]);
+  x.ro[0] = x.ro[1] = x.ro[2] = 0.f;
+  if (x.row) load_r3<float>(a.r, p, x.ro);
+  return x;
+}
+
+__device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowArgs& f, int s, int next,
+                                          unsigned char* buf, unsigned long long* bar, int lane, float ltol,
+                                          double& dr2, double& rr2, unsigned long long* tl, const FlowRow& x) {
+  const float* Ws = reinterpret_cast<const float*>(buf);
+  const int* Cs = reinterpret_cast<const int*>(buf + (size_t)f.maxslot * 9 * FC3D_SLAB * 4);
+  const float* Qs = reinterpret_cast<const float*>(Cs + (size_t)f.maxslot * FC3D_SLAB);
+  const float* Ds = Qs + 3 * FC3D_SLAB;
+  const float* Ms = Ds + 9 * FC3D_SLAB;
+  const float* Rs = Ms + FC3D_SLAB;
+  const int p = s * FC3D_SLAB + lane;
+  const int ns = x.ns;
+  const float ro[3] = {x.ro[0], x.ro[1], x.ro[2]};
+  float acc[3] = {0.f, 0.f, 0.f};
+  bool work = false;
+  LocalProblem<float> L;
+  if (x.row) {
+    acc[0] = Qs[lane];
+    acc[1] = Qs[FC3D_SLAB + lane];
+    acc[2] = Qs[2 * FC3D_SLAB + lane];
+    constexpr int CH = 16;
+    for (int t0 = 0; t0 < ns; t0 += CH) {
+      float rv[CH][3];
+#pragma unroll
+      for (int k = 0; k < CH; k++) {
+        const int pj = t0 + k < ns ? Cs[(t0 + k) * FC3D_SLAB + lane] : a.npad;
+        load_r3<float>(a.r, pj, rv[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < CH; k++) {
+        if (t0 + k < ns) {
+          const float* wp = Ws + (size_t)(t0 + k) * 9 * FC3D_SLAB + lane;
+          float wv[9];
+#pragma unroll
+          for (int e = 0; e < 9; e++) wv[e] = wp[e * FC3D_SLAB];
+          mvp3x3(wv, rv[k], acc);
+        }
+      }
+    }
+    if (acc[0] > -Eps<float>::v()) {
+      float* rp = a.r + (size_t)p * FC3D_RSTRIDE;
+      rp[0] = 0;
+      rp[1] = 0;
+      rp[2] = 0;
+      dr2 += (double)ro[0] * ro[0] + (double)ro[1] * ro[1] + (double)ro[2] * ro[2];
+    } else {
+      work = true;
+#pragma unroll
+      for (int e = 0; e < 9; e++) L.M[e] = Ds[e * FC3D_SLAB + lane];
+      L.mu = Ms[lane];
+      L.rhoN = Rs[lane];
+      L.rhoT = Rs[FC3D_SLAB + lane];
+      L.q[0] = acc[0];
+      L.q[1] = acc[1];
+      L.q[2] = acc[2];
+    }
+  }
+  const unsigned wmask = __ballot_sync(0xffffffffu, work);
+  if (tl) {
+    tl[3] = globaltimer_ns();
+    tl[5] = (unsigned long long)__popc(wmask);
+  }
+  if (next >= 0 && lane == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    flow_issue(a, f, next, buf, bar);
+  }
+  if (work) solve_row_s(a, L, p, ro, ltol, dr2, rr2);
+}
+
+template <int NW>
+__global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<float> a, const FlowArgs f) {
+  extern __shared__ __align__(128) unsigned char flow_smem[];
+  __shared__ __align__(8) unsigned long long bars[NW];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned char* buf = flow_smem + (size_t)w * f.buf_bytes;
+  unsigned long long* bar = &bars[w];
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  const int gw = blockIdx.x * NW + w, tw = gridDim.x * NW;
+  unsigned parity = 0;
+  bool pending = false, failed = false;
+  if (gw < a.nslab) {
+    if (lane == 0) flow_issue(a, f, gw, buf, bar);
+    pending = true;
+  }
+  unsigned epoch = 0;
+  double working = fmax(a.user_tol, a.switch_tol);
+  double incr = INFINITY, full = INFINITY, best = INFINITY;
+  int sweep = 0, best_sweep = 0;
+  bool converged = false;
+  while (sweep < a.max_sweeps) {
+    sweep++;
+    double acc[2] = {0.0, 0.0};
+    const bool record = a.timeline && sweep == a.timeline_sweep && lane == 0;
+    for (int s = gw; s < a.nslab && !failed; s += tw) {
+      unsigned long long* tl = record ? a.timeline + (size_t)s * FC3D_TL_STRIDE : nullptr;
+      if (tl) tl[0] = globaltimer_ns();
+      const FlowRow x = flow_row(a, s, lane);
+      if (!flow_wait_deps(a, f, s, (unsigned)sweep, lane)) {
+        failed = true;
+        break;
+      }
+      __syncwarp();
+      if (tl) tl[1] = globaltimer_ns();
+      if (pending) {
+        if (!mbar_wait_bounded(bar, parity, a.spin_limit, a.status)) {
+          failed = true;  // the copy stays pending: awaited again at exit
+          break;
+        }
+        parity ^= 1u;
+        pending = false;
+      }
+      if (tl) tl[2] = globaltimer_ns();
+      // the next slab of this warp: later in this sweep, else the first one
+      // of the next sweep (fetched even when no sweep follows; awaited at exit)
+      const int next = s + tw < a.nslab ? s + tw : gw;
+      flow_slab(a, f, s, next, buf, bar, lane, (float)a.local_tol, acc[0], acc[1], tl, x);
+      pending = true;
+      __syncwarp();
+      if (tl) tl[4] = globaltimer_ns();
+      if (lane == 0) st_release_u32(&f.done[s], (unsigned)sweep);
+    }
+    flow_block_sum<2, NW>(acc, a.partials + blockIdx.x * 8);
+    if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) break;
+    if (*(volatile int*)a.status & 1) break;
+    double sm[2];
+    grid_sum<2>(a.partials, 0, sm);
+    incr = sqrt(sm[0]);
+    const double nr = sqrt(sm[1]);
+    if (fabs(nr) > DBL_EPSILON) incr /= nr;
+    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0 && a.trace_base + sweep - 1 < a.trace_cap)
+      a.trace[a.trace_base + sweep - 1] = incr;
+    // the FP32 accelerator's stop rules, as the coloured kernel applies them
+    bool stop = false;
+    if (!(incr == incr)) {
+      if (threadIdx.x == 0) atomicOr(a.status, 2);
+      stop = true;
+    }
+    if (incr < a.switch_tol) stop = true;
+    if (incr < 0.99 * best) {
+      best = incr;
+      best_sweep = sweep;
+    } else if (a.stall_window > 0 && sweep - best_sweep >= a.stall_window) {
+      stop = true;
+    }
+    if (!stop && incr < working) {
+      if (!flow_full_error<NW>(a, epoch, full)) break;
+      const double target = fmax(a.user_tol, a.switch_tol);
+      if (full <= target) {
+        converged = true;
+        stop = true;
+      } else if (full > 0.0 && incr > 0.0) {
+        double nt = (incr / full) * target;
+        const double mint = fmax(target * 1e-6, DBL_EPSILON * 1e-6);
+        if (nt < mint) nt = mint;
+        if (nt < working) working = nt;
+      }
+    }
+    if (stop) break;
+  }
+  // a copy still in flight lands before the block leaves
+  if (pending) mbar_wait_bounded(bar, parity, a.spin_limit, a.status);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.out[0] = sweep;
+    a.out[1] = incr;
+    a.out[2] = full;
+    a.out[3] = converged ? 0 : 1;
+    a.out[4] = working;
+    a.out[5] = a.local_tol;
+  }
+}
+
+// Column slabs of every slab: the distinct slabs holding a column of one of
+// its rows.  One thread per slab; with dptr null it writes their number to
+// count[s], else the ascending list to dep[dptr[s] ..), bit 31 set for a
+// later colour.  Slabs have at most FC3D_FLOW_MAXSLOT slots.
+__global__ void k_flow_deps(int nslab, int npad, int ncol, const int* __restrict__ sptr_d,
+                            const int* __restrict__ perm, const int* __restrict__ slab_nslot,
+                            const long long* __restrict__ slab_off, const int* __restrict__ col,
+                            const int* __restrict__ dptr, int* __restrict__ count, int* __restrict__ dep) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslab) return;
+  auto colour_of = [&](int sl) {
+    int lo = 0, hi = ncol - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sptr_d[mid] <= sl)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    return lo;
+  };
+  int list[FC3D_SLAB * FC3D_FLOW_MAXSLOT];
+  int n = 0;
+  const int ns = min(slab_nslot[s], FC3D_FLOW_MAXSLOT);
+  const long long base = slab_off[s];
+  for (int k = 0; k < FC3D_SLAB; k++) {
+    if (perm[(size_t)s * FC3D_SLAB + k] < 0) continue;
+    for (int t = 0; t < ns; t++) {
+      const int j = col[(size_t)(base + t) * FC3D_SLAB + k];
+      if (j < 0 || j >= npad) continue;
+      const int d = j / FC3D_SLAB;
+      bool seen = d == s;
+      for (int i = 0; i < n && !seen; i++) seen = list[i] == d;
+      if (!seen) list[n++] = d;
+    }
+  }
+  if (!dptr) {
+    count[s] = n;
+    return;
+  }
+  for (int i = 1; i < n; i++) {
+    const int v = list[i];
+    int j = i - 1;
+    while (j >= 0 && list[j] > v) {
+      list[j + 1] = list[j];
+      j--;
+    }
+    list[j + 1] = v;
+  }
+  const int cs = colour_of(s);
+  int* out = dep + dptr[s];
+  for (int i = 0; i < n; i++) out[i] = colour_of(list[i]) > cs ? (int)(list[i] | 0x80000000u) : list[i];
+}
+
+}  // namespace fc3dgpu

@@ -114,4 +114,22 @@ struct WorkListS {
   int count[FC3D_PASS_SLABS];
 };
 
+// Slab-dataflow FP32 sweep (fc3dgpu_flow.cuh): longest slab (in slots) it
+// takes, and the kernel's arguments besides SweepArgs.
+#define FC3D_FLOW_MAXSLOT 16
+
+struct FlowArgs {
+  const int* dptr;     // per slab: its column slabs are dep[dptr[s] .. dptr[s + 1])
+  const int* dep;      // slab ids, ascending; bit 31 set: a later colour
+  unsigned* done;      // per slab: sweeps completed; zero at launch
+  unsigned buf_bytes;  // shared-memory buffer of one warp
+  int maxslot;         // slots of one slab the buffer holds
+};
+
+// Per-warp buffer: W (maxslot * 9 * 32), col (maxslot * 32), q (3 * 32),
+// D (9 * 32), mu (32), rho (2 * 32) in FP32, all 128-byte multiples.
+__host__ __device__ __forceinline__ unsigned flow_buf_bytes(int maxslot) {
+  return (unsigned)maxslot * FC3D_SLAB * (9 * 4 + 4) + FC3D_SLAB * (3 + 9 + 1 + 2) * 4;
+}
+
 }  // namespace fc3dgpu

@@ -528,19 +528,11 @@ __device__ __forceinline__ void stage_issue(const SweepArgs<Real>& a, int lo, in
 // process_colour_compact with W, col and q read from the staged shared
 // memory copy of the block's range (which must fit one pass), and the next
 // colour's range staged as soon as this one's row products are done.
+// Local solve of row pp from L's diagonal block, q, mu and rho (set by the
+// caller) and the reaction o before it; writes the new reaction.
 template <typename Real>
-__device__ __forceinline__ void solve_item_s(const SweepArgs<Real>& a, WorkListS<Real>& wk, int t, Real ltol,
-                                             double& dr2, double& rr2) {
-  const int pp = wk.p[t];
-  LocalProblem<Real> L;
-#pragma unroll
-  for (int e = 0; e < 9; e++) L.M[e] = wk.m[e][t];
-  L.q[0] = wk.q[0][t];
-  L.q[1] = wk.q[1][t];
-  L.q[2] = wk.q[2][t];
-  L.mu = wk.m[9][t];
-  L.rhoN = wk.m[10][t];
-  L.rhoT = wk.m[11][t];
+__device__ __forceinline__ void solve_row_s(const SweepArgs<Real>& a, LocalProblem<Real>& L, int pp, const Real o[3],
+                                            Real ltol, double& dr2, double& rr2) {
   L.rho_pli = __ldcg(&a.rpli[pp]);
   L.tol = ltol;
   L.newton_max = a.newton_max;
@@ -549,7 +541,6 @@ __device__ __forceinline__ void solve_item_s(const SweepArgs<Real>& a, WorkListS
   L.n_newton = 0;
   L.n_pli = 0;
   L.n_ls = 0;
-  Real o[3] = {wk.ro[0][t], wk.ro[1][t], wk.ro[2][t]};
   Real rn[3] = {o[0], o[1], o[2]};
   local_solve(L, rn);
   Real* rp = a.r + (size_t)pp * FC3D_RSTRIDE;
@@ -567,6 +558,22 @@ __device__ __forceinline__ void solve_item_s(const SweepArgs<Real>& a, WorkListS
     atomicAdd(&a.counters[3], 1ULL);
     atomicMax(&a.counters[4], (unsigned long long)L.n_newton);
   }
+}
+
+template <typename Real>
+__device__ __forceinline__ void solve_item_s(const SweepArgs<Real>& a, WorkListS<Real>& wk, int t, Real ltol,
+                                             double& dr2, double& rr2) {
+  LocalProblem<Real> L;
+#pragma unroll
+  for (int e = 0; e < 9; e++) L.M[e] = wk.m[e][t];
+  L.q[0] = wk.q[0][t];
+  L.q[1] = wk.q[1][t];
+  L.q[2] = wk.q[2][t];
+  L.mu = wk.m[9][t];
+  L.rhoN = wk.m[10][t];
+  L.rhoT = wk.m[11][t];
+  const Real o[3] = {wk.ro[0][t], wk.ro[1][t], wk.ro[2][t]};
+  solve_row_s(a, L, wk.p[t], o, ltol, dr2, rr2);
 }
 
 // process_colour_compact with every per-slab input (W, col, q, D, mu, rho)
@@ -677,6 +684,38 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
         if (lane == 0) wk.count[i] = __popc(msk[j]);
       }
       if (j == 0 && tl && threadIdx.x == 0) tl[3] = globaltimer_ns();
+    }
+    if (np <= NWB) {
+      // one slab per warp: every lane solves its own row where it sits, with
+      // no compaction through the work list (a block has at most one row
+      // per thread either way)
+      const bool work = w < np && ((msk[0] >> lane) & 1u);
+      LocalProblem<Real> L;
+      if (work) {
+#pragma unroll
+        for (int e = 0; e < 9; e++) L.M[e] = Ds[(w * 9 + e) * FC3D_SLAB + lane];
+        L.mu = Ms[w * FC3D_SLAB + lane];
+        L.rhoN = Rs[(w * 2) * FC3D_SLAB + lane];
+        L.rhoT = Rs[(w * 2 + 1) * FC3D_SLAB + lane];
+        L.q[0] = acc[0][0];
+        L.q[1] = acc[0][1];
+        L.q[2] = acc[0][2];
+      }
+      __syncthreads();
+      // every input of this range read: stage the next colour's range
+      if (issuer && nhi > nlo) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        stage_issue(a, nlo, nhi, stage, bar, n_o0, n_slots);
+      }
+      if (nhi > nlo) pending = true;
+      if (tl && threadIdx.x == 0) {
+        int total = 0;
+        for (int k = 0; k < np; k++) total += wk.count[k];
+        tl[0] = globaltimer_ns();
+        tl[1] = (unsigned long long)total;
+      }
+      if (work) solve_row_s(a, L, (lo + w) * FC3D_SLAB + lane, ro[0], ltol, dr2, rr2);
+      return true;
     }
     __syncthreads();
     int total = 0;

@@ -1,5 +1,6 @@
 // float instantiations of the persistent coloured NSGS kernel.
 #include "fc3dgpu_batch.cuh"
+#include "fc3dgpu_flow.cuh"
 #include "fc3dgpu_sweep.cuh"
 #include "fc3dgpu_sweep_launch.h"
 
@@ -61,6 +62,8 @@ void warm_sweep_kernels() {
   cudaFuncGetAttributes(&fa, nsgs_kernel<float, 2>);
   cudaFuncGetAttributes(&fa, nsgs_kernel<float, 4>);
   cudaFuncGetAttributes(&fa, nsgs_kernel<float, 8>);
+  cudaFuncGetAttributes(&fa, nsgs_flow_kernel<12>);
+  cudaFuncGetAttributes(&fa, nsgs_flow_kernel<8>);
   warm_sweep_kernels_f64();
 }
 
@@ -72,6 +75,57 @@ int sweep_grid_f32(int lanes) {
     case 8: return grid_t<8>();
     default: return 0;
   }
+}
+
+// Warps per block of the dataflow sweep: 12 (384 threads, the register
+// budget of the local solver) when twelve per-warp buffers fit the shared
+// memory of an SM, else 8, else none.
+int flow_warps(int maxslot) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t room = optin > 4096 ? (size_t)optin - 4096 : 0;  // static shared memory of the kernel
+  const size_t buf = flow_buf_bytes(maxslot);
+  if (12 * buf <= room) return 12;
+  if (8 * buf <= room) return 8;
+  return 0;
+}
+
+template <int NW>
+static cudaError_t launch_flow_t(const SweepArgs<float>& a, const FlowArgs& f, cudaStream_t s, int* grid) {
+  auto kern = nsgs_flow_kernel<NW>;
+  const size_t smem = (size_t)NW * f.buf_bytes;
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NW * 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int g = nsm;  // one block per SM: each holds NW per-warp buffers
+  if (g > 1024) g = 1024;
+  *grid = g;
+  void* args[] = {(void*)&a, (void*)&f};
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(g), dim3(NW * 32), args, smem, s);
+}
+
+cudaError_t launch_flow_f32(const SweepArgs<float>& a, const FlowArgs& f, int nw, cudaStream_t s, int* grid) {
+  switch (nw) {
+    case 12: return launch_flow_t<12>(a, f, s, grid);
+    case 8: return launch_flow_t<8>(a, f, s, grid);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t build_flow_deps(int nslab, int npad, int ncol, const int* sptr_d, const int* perm, const int* slab_nslot,
+                            const long long* slab_off, const int* col, const int* dptr, int* count, int* dep,
+                            cudaStream_t s) {
+  k_flow_deps<<<(nslab + 127) / 128, 128, 0, s>>>(nslab, npad, ncol, sptr_d, perm, slab_nslot, slab_off, col, dptr,
+                                                  count, dep);
+  return cudaGetLastError();
 }
 
 static int batch_cached_dev_f32 = -1, batch_cached_g_f32 = 0;

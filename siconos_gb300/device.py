@@ -70,6 +70,11 @@ class DeviceSolver:
     def staging(self, on: bool) -> bool:
         return bool(self.L.fc3dgpu_ctx_staging(self.ctx, int(on)))
 
+    def flow(self, on: bool) -> bool:
+        """Slab-dataflow FP32 sweeps (True) or the coloured kernel (False);
+        returns the previous setting."""
+        return bool(self.L.fc3dgpu_ctx_flow(self.ctx, int(on)))
+
     # ---- batched problems -------------------------------------------------
     def set_contacts(self, geo: dict, colouring: int = sn.FC3DGPU_COLOURING_DEFAULT):
         """Assemble W on the device from contact geometry (see

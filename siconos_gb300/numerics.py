@@ -49,7 +49,8 @@ SICONOS_DPARAM_RESIDU = 1
 FC3DGPU_IPARAM_PRECISION = 23
 FC3DGPU_IPARAM_LANES = 24
 FC3DGPU_IPARAM_WARMSTART = 25
-FC3DGPU_COLOURING_DEFAULT = 4 << 8  # hash priority + 4 recolouring passes
+FC3DGPU_COLOUR_KEMPE = 1 << 16
+FC3DGPU_COLOURING_DEFAULT = (4 << 8) | FC3DGPU_COLOUR_KEMPE  # hash priority, 4 recolouring passes, Kempe reduction
 FC3DGPU_IPARAM_COLOURING = 26
 FC3DGPU_IPARAM_SWEEPS_FP32 = 27
 FC3DGPU_IPARAM_SWEEPS_FP64 = 28
@@ -158,6 +159,7 @@ ABI = {
     "fc3dgpu_nsgs_batch": (C.c_int, [C.c_int, C.POINTER(C.POINTER(_FCP)), C.POINTER(_DP), C.POINTER(_DP),
                                      C.POINTER(_SO), C.POINTER(C.c_int)]),
     "fc3dgpu_colour": (C.c_int, [C.c_int, _I64, _I64, C.c_int, _I32]),
+    "fc3dgpu_colour_reduce": (C.c_int, [C.c_int, _I32, _I32, _I32, C.c_int, C.c_int]),
     "fc3dgpu_last_error": (C.c_char_p, []),
     "fc3dgpu_device_info": (C.c_int, [C.c_int, C.c_void_p]),
     "fc3dgpu_params_default": (None, [C.POINTER(FC3DGPUParams)]),
@@ -214,6 +216,7 @@ ABI = {
     "fc3dgpu_ctx_zero_r": (C.c_int, [C.c_void_p]),
     "fc3dgpu_ctx_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_sync": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_ctx_flow": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_timeline": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "fc3dgpu_ctx_launches": (C.c_ulonglong, [C.c_void_p]),
