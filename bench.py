@@ -554,7 +554,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": {"workload": f"{DIMS[0]}x{DIMS[1]}x{DIMS[2]} sphere lattice, {s.nc} contacts, {s.nnzb} "
                                    f"blocks, mu {MU}, seed {SEED}; one fc3d solve per step from r=0, tol 1e-8, "
-                                   f"budget {S} sweeps (coloured FP32 sweeps + FP64 fc3d_compute_error)",
+                                   f"budget {S} sweeps (FP32 sweeps in colour order + FP64 fc3d_compute_error)",
                        "colours": stats[0]["colours"], "lanes_per_contact": stats[0]["lanes"],
                        "grid": stats[0]["grid"], "l2": "flushed between steps (256 MB write outside the events)",
                        "parallelism": "replicas" if ws > 1 else "1 GPU"},

@@ -17,12 +17,14 @@
  * exchanging a and b on those components keeps the colouring proper and
  * frees a for v (the alternating-path step of the edge-colouring proof,
  * which always succeeds on bipartite body graphs while the classes left
- * are at least the largest number of contacts of one body).  A class that
- * cannot be emptied stays; the result is a proper colouring in any case.
+ * are at least the largest number of contacts of one body).  The first
+ * contact of a class that cannot move ends the reduction (that class
+ * stays); the result is a proper colouring in any case.
  *
  * The outcome depends only on the graph and the input colouring, not on the
  * order of the adjacency lists: candidates are taken in index order, colour
- * pairs in a fixed order, and a Kempe component is exchanged whole. */
+ * pairs in an order set by the colours around the candidate and its
+ * lowest-index neighbour, and a Kempe component is exchanged whole. */
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -30,6 +32,35 @@
 #define COLOUR_MAX 128
 
 static int has_colour(const uint64_t m[2], int c) { return (int)((m[c >> 6] >> (c & 63)) & 1u); }
+
+/* Exchange colours a and b on the (a, b)-Kempe components through v's
+ * a-coloured neighbours, unless one holds a b-coloured neighbour of v
+ * (nbr[w] == ngen marks v's neighbours) or a search passes work_cap
+ * vertices; returns 1 when exchanged (a is then free for v). */
+static int kempe_exchange(int v, int a, int b, const int *gptr, const int *adj, int *colour, int *seen, int gen,
+                          const int *nbr, int ngen, int *queue, int work_cap) {
+  int qn = 0;
+  for (int k = gptr[v]; k < gptr[v + 1]; k++) {
+    const int w = adj[k];
+    if (w != v && colour[w] == a && seen[w] != gen) {
+      seen[w] = gen;
+      queue[qn++] = w;
+    }
+  }
+  for (int h = 0; h < qn; h++) {
+    const int u = queue[h];
+    for (int k = gptr[u]; k < gptr[u + 1]; k++) {
+      const int w = adj[k];
+      if (seen[w] == gen || (colour[w] != a && colour[w] != b)) continue;
+      if (colour[w] == b && nbr[w] == ngen) return 0; /* a b-neighbour of v would turn a */
+      if (qn >= work_cap) return 0;
+      seen[w] = gen;
+      queue[qn++] = w;
+    }
+  }
+  for (int h = 0; h < qn; h++) colour[queue[h]] = colour[queue[h]] == a ? b : a;
+  return 1;
+}
 
 /* gptr/adj: the conflict graph, symmetric CSR (duplicates allowed), nc
  * vertices; colour[nc] a proper colouring with ncol colours.  work_cap
@@ -43,11 +74,13 @@ int fc3dgpu_colour_reduce(int nc, const int *gptr, const int *adj, int *colour, 
   int *nbr = (int *)calloc((size_t)nc, sizeof(int));
   int *queue = (int *)malloc(sizeof(int) * (size_t)nc);
   int *cls = (int *)malloc(sizeof(int) * (size_t)nc);
-  if (!seen || !nbr || !queue || !cls) {
+  int *side = (int *)calloc((size_t)nc, sizeof(int));
+  if (!seen || !nbr || !queue || !cls || !side) {
     free(seen);
     free(nbr);
     free(queue);
     free(cls);
+    free(side);
     return -1;
   }
   int gen = 0, ngen = 0;
@@ -60,55 +93,53 @@ int fc3dgpu_colour_reduce(int nc, const int *gptr, const int *adj, int *colour, 
     for (int t = 0; t < n; t++) {
       const int v = cls[t];
       uint64_t used[2] = {0, 0};
+      int cnt[COLOUR_MAX];
+      for (int x = 0; x < top; x++) cnt[x] = 0;
       ngen++;
       for (int k = gptr[v]; k < gptr[v + 1]; k++) {
         const int w = adj[k];
-        if (w == v) continue;
+        if (w == v || nbr[w] == ngen) continue;
         used[colour[w] >> 6] |= 1ull << (colour[w] & 63);
         nbr[w] = ngen;
+        if (colour[w] < top) cnt[colour[w]]++;
       }
       int c = -1;
       for (int x = 0; x < top && c < 0; x++)
         if (!has_colour(used, x)) c = x;
-      for (int a = 0; a < top && c < 0; a++) {
-        for (int b = 0; b < top && c < 0; b++) {
-          if (b == a || !has_colour(used, b)) continue;
-          /* the (a, b) components through v's a-neighbours */
-          gen++;
-          int qn = 0, ok = 1;
-          for (int k = gptr[v]; k < gptr[v + 1]; k++) {
-            const int w = adj[k];
-            if (w != v && colour[w] == a && seen[w] != gen) {
-              seen[w] = gen;
-              queue[qn++] = w;
-            }
-          }
-          for (int h = 0; h < qn && ok; h++) {
-            const int u = queue[h];
-            for (int k = gptr[u]; k < gptr[u + 1]; k++) {
-              const int w = adj[k];
-              if (seen[w] == gen || (colour[w] != a && colour[w] != b)) continue;
-              if (colour[w] == b && nbr[w] == ngen) {
-                ok = 0;  /* a b-neighbour of v would turn a */
-                break;
-              }
-              if (qn >= work_cap) {
-                ok = 0;
-                break;
-              }
-              seen[w] = gen;
-              queue[qn++] = w;
-            }
-          }
-          if (!ok) continue;
-          for (int h = 0; h < qn; h++) colour[queue[h]] = colour[queue[h]] == a ? b : a;
-          c = a;
+      /* Colour pairs to try.  On a line graph v joins two bodies: the
+       * neighbours through the body of its lowest-index neighbour w0 are w0
+       * and w0's neighbours (one clique), the others go through the second
+       * body.  A colour a held only on the second side and a colour b held
+       * only on the first is the pair of the edge-colouring proof; those
+       * pairs come first, then every pair of held colours. */
+      int w0 = -1;
+      if (c < 0)
+        for (int k = gptr[v]; k < gptr[v + 1]; k++)
+          if (adj[k] != v && (w0 < 0 || adj[k] < w0)) w0 = adj[k];
+      uint64_t s0[2] = {0, 0}, s1[2] = {0, 0};
+      if (w0 >= 0) {
+        for (int k = gptr[w0]; k < gptr[w0 + 1]; k++) side[adj[k]] = ngen;
+        side[w0] = ngen;
+        for (int k = gptr[v]; k < gptr[v + 1]; k++) {
+          const int w = adj[k];
+          if (w == v) continue;
+          uint64_t *m = (side[w] == ngen) ? s0 : s1;
+          m[colour[w] >> 6] |= 1ull << (colour[w] & 63);
         }
       }
-      if (c >= 0)
-        colour[v] = c;
-      else
-        left++;
+      for (int phase = 0; phase < 2 && c < 0; phase++)
+        for (int a = 0; a < top && c < 0; a++)
+          for (int b = 0; b < top && c < 0; b++) {
+            if (a == b || cnt[a] == 0 || cnt[b] == 0) continue;
+            const int pref = has_colour(s1, a) && !has_colour(s0, a) && has_colour(s0, b) && !has_colour(s1, b);
+            if (pref != (phase == 0)) continue;
+            if (kempe_exchange(v, a, b, gptr, adj, colour, seen, ++gen, nbr, ngen, queue, work_cap)) c = a;
+          }
+      if (c < 0) {
+        left = 1;  /* the class stays: stop at its first contact that cannot move */
+        break;
+      }
+      colour[v] = c;
     }
     if (left) break;
     ncol = top;
@@ -117,5 +148,6 @@ int fc3dgpu_colour_reduce(int nc, const int *gptr, const int *adj, int *colour, 
   free(nbr);
   free(queue);
   free(cls);
+  free(side);
   return ncol;
 }

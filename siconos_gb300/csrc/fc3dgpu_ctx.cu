@@ -1819,6 +1819,7 @@ extern "C" int fc3dgpu_ctx_timeline(fc3dgpu_ctx* c, int sweep, unsigned long lon
     CK(cudaMemcpyAsync(out, c->timeline, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
+  if (sweep > 0) CK(cudaMemsetAsync(c->timeline, 0, sizeof(unsigned long long) * need, c->stream));
   c->timeline_sweep = sweep;
   return n;
 }

@@ -165,6 +165,46 @@ def test_c2_scale_properties(gpu):
     assert st["sweeps32"] + st["sweeps64"] == 60 and st["status"] == 0
 
 
+@pytest.mark.parametrize("dims", [(30, 30, 15), (12, 12, 6)])
+def test_flow_equals_coloured(gpu, dims):
+    """The slab-dataflow FP32 sweep reads what the sequential sweep in colour
+    order reads, as the coloured kernel does: the same iterates bit for bit
+    after a fixed number of sweeps, and the same light-error trace up to the
+    order of its sums."""
+    from siconos_gb300 import scene
+    s = scene.lattice(*dims, seed=6)
+    gpu.load(s)
+    out = []
+    for on in (True, False):
+        prev = gpu.flow(on)
+        gpu.zero_r()
+        st = gpu.solve(tol=1e-300, max_iter=25, lanes=1, fp32_only=1, switch_tol=0.0, stall_window=0)
+        out.append((gpu.get()[0], st, gpu.trace(25)))
+        gpu.flow(prev)
+    (r1, s1, t1), (r2, s2, t2) = out
+    assert s1["status"] == 0 and s2["status"] == 0 and s1["sweeps32"] == s2["sweeps32"] == 25
+    assert np.array_equal(r1, r2)
+    np.testing.assert_allclose(t1, t2, rtol=1e-12, atol=0)
+
+
+def test_flow_timeline_per_slab(gpu):
+    """With the dataflow sweep the timeline holds one record per slab:
+    increasing timestamps and at most 32 local solves."""
+    from siconos_gb300 import scene
+    s = scene.lattice(30, 30, 15, seed=6)
+    gpu.load(s)
+    gpu.timeline(3)
+    gpu.zero_r()
+    gpu.solve(tol=1e-300, max_iter=5, lanes=1, fp32_only=1, switch_tol=0.0, stall_window=0)
+    tl = gpu.timeline(0).reshape(-1, 8).astype(np.int64)
+    nslab = (gpu.sizes()[0] + 31) // 32
+    rec = tl[tl[:, 0] > 0]
+    assert nslab <= len(rec) <= nslab + gpu.sizes()[2]
+    assert np.all(np.diff(rec[:, :5], axis=1) >= 0)
+    assert np.all((rec[:, 5] >= 0) & (rec[:, 5] <= 32))
+    gpu.timeline(0)
+
+
 def test_fp32_staged_equals_unstaged(gpu):
     """The bulk-copy staged FP32 sweep computes what the direct-load sweep
     computes (same slot order; only the data path differs)."""
