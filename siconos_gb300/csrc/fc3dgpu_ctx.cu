@@ -701,6 +701,7 @@ struct fc3dgpu_ctx {
   BUF(int, flow_dep);
   BUF(unsigned, flow_done);
   BUF(int, flow_sptr);
+  BUF(double, flow_part);
   // batched problems (0 = a single problem)
   int nscenes = 0;
   std::vector<int> scene_off_h;  // nscenes + 1 contact offsets
@@ -839,7 +840,7 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64, c->feat,
                   c->prop, c->rbak, c->gapo, c->cbA, c->cbB, c->cframe, c->cpoint, c->bpos, c->bmass,
                   c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum, c->wtmp, c->wdiff,
-                  c->flow_dptr, c->flow_dep, c->flow_done, c->flow_sptr};
+                  c->flow_dptr, c->flow_dep, c->flow_done, c->flow_sptr, c->flow_part};
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1576,6 +1577,7 @@ static int prepare_flow(fc3dgpu_ctx* c) {
   CK(ensure(&c->flow_dptr, &c->flow_dptr_cap, (size_t)nslab + 1));
   CK(ensure(&c->flow_done, &c->flow_done_cap, (size_t)nslab));
   CK(ensure(&c->flow_sptr, &c->flow_sptr_cap, FC3D_MAX_COLOURS + 1));
+  CK(ensure(&c->flow_part, &c->flow_part_cap, 1024 * 8));
   CK(cudaMemcpyAsync(c->flow_sptr, c->sptr, sizeof(int) * (FC3D_MAX_COLOURS + 1), cudaMemcpyHostToDevice, s));
   // counts, their prefix sum on the host, then the lists
   CK(build_flow_deps(nslab, c->npad, c->ncol, c->flow_sptr, c->perm, c->slab_nslot, c->slab_off, c->col, nullptr,
@@ -1670,6 +1672,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
       f.dptr = c->flow_dptr;
       f.dep = c->flow_dep;
       f.done = c->flow_done;
+      f.part = c->flow_part;
       f.maxslot = c->flow_maxslot;
       f.buf_bytes = flow_buf_bytes(c->flow_maxslot);
       CK(cudaMemsetAsync(c->flow_done, 0, sizeof(unsigned) * c->nslab, s));

@@ -86,6 +86,33 @@ __device__ __forceinline__ bool flow_full_error(const SweepArgs<float>& a, unsig
   return true;
 }
 
+// Wait until every block's flag shows epoch e (bounded; warp 0 polls, then
+// an acquire fence and a block barrier).
+__device__ __forceinline__ bool grid_wait(const unsigned* flags, unsigned e, unsigned long long limit, int* status) {
+  __shared__ int s_ok;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    unsigned long long n = 0;
+    int ok = 1;
+    for (;;) {
+      bool mine = true;
+      for (int b = lane; b < (int)gridDim.x; b += 32)
+        mine &= (ld_relaxed_u32(&flags[b * FC3D_FLAG_STRIDE]) >= e);
+      if (__all_sync(0xffffffffu, mine)) break;
+      if (++n > limit) {
+        ok = 0;
+        if (lane == 0) atomicOr(status, 1);
+        break;
+      }
+      if (n > 256) __nanosleep(32);
+    }
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    if (lane == 0) s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // Wait until every slab slab s takes columns from has reached the state
 // sweep k needs (see the header).  Relaxed polls, then an acquire fence; the
 // caller's __syncwarp orders the other lanes' reads after it.
@@ -221,11 +248,46 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
     if (lane == 0) flow_issue(a, f, gw, buf, bar);
     pending = true;
   }
-  unsigned epoch = 0;
+  // Light errors run one sweep behind: at the end of sweep j a block
+  // publishes its partial sums of sweep j (slot j mod 4 of f.part) and its
+  // arrival, then waits only for every block's arrival at the end of sweep
+  // j - 1 (long past, as a rule) and decides on sweep j - 1's light error:
+  // no grid barrier between sweeps.  A stop so decided takes effect after
+  // sweep j.  Four slots: when a block writes slot j mod 4, every block has
+  // read it (at the end of sweep j - 3; the block saw all arrivals of the
+  // end of sweep j - 2).  The full error needs one iterate everywhere, so it
+  // waits for every block's end of sweep j.
+  unsigned epoch = 0, e_last = 0, e_prev = 0;
   double working = fmax(a.user_tol, a.switch_tol);
   double incr = INFINITY, full = INFINITY, best = INFINITY;
   int sweep = 0, best_sweep = 0;
-  bool converged = false;
+  bool converged = false, aborted = false, stopped = false;
+  const double target = fmax(a.user_tol, a.switch_tol);
+  auto light_error = [&](int j) {
+    double sm[2];
+    grid_sum<2>(f.part, (j & 3) * 2, sm);
+    double e = sqrt(sm[0]);
+    const double nr = sqrt(sm[1]);
+    if (fabs(nr) > DBL_EPSILON) e /= nr;
+    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0 && a.trace_base + j - 1 < a.trace_cap)
+      a.trace[a.trace_base + j - 1] = e;
+    return e;
+  };
+  // the full error of the current iterate once every block ended sweep j
+  // (epoch e_end); adapts the working tolerance as the coloured kernel does
+  auto full_check = [&](double incr_j, unsigned e_end) {
+    if (!grid_wait(a.barrier, e_end, a.spin_limit, a.status)) return false;
+    if (!flow_full_error<NW>(a, epoch, full)) return false;
+    if (full <= target) {
+      converged = true;
+    } else if (full > 0.0 && incr_j > 0.0) {
+      double nt = (incr_j / full) * target;
+      const double mint = fmax(target * 1e-6, DBL_EPSILON * 1e-6);
+      if (nt < mint) nt = mint;
+      if (nt < working) working = nt;
+    }
+    return true;
+  };
   while (sweep < a.max_sweeps) {
     sweep++;
     double acc[2] = {0.0, 0.0};
@@ -258,43 +320,59 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
       if (tl) tl[4] = globaltimer_ns();
       if (lane == 0) st_release_u32(&f.done[s], (unsigned)sweep);
     }
-    flow_block_sum<2, NW>(acc, a.partials + blockIdx.x * 8);
-    if (!grid_barrier(a.barrier, epoch, a.spin_limit, a.status)) break;
-    if (*(volatile int*)a.status & 1) break;
-    double sm[2];
-    grid_sum<2>(a.partials, 0, sm);
-    incr = sqrt(sm[0]);
-    const double nr = sqrt(sm[1]);
-    if (fabs(nr) > DBL_EPSILON) incr /= nr;
-    if (a.trace && blockIdx.x == 0 && threadIdx.x == 0 && a.trace_base + sweep - 1 < a.trace_cap)
-      a.trace[a.trace_base + sweep - 1] = incr;
-    // the FP32 accelerator's stop rules, as the coloured kernel applies them
+    flow_block_sum<2, NW>(acc, f.part + blockIdx.x * 8 + (sweep & 3) * 2);
+    e_prev = e_last;
+    e_last = ++epoch;
+    if (threadIdx.x == 0) st_release_u32(&a.barrier[blockIdx.x * FC3D_FLAG_STRIDE], e_last);
+    if (sweep < 2) continue;
+    if (!grid_wait(a.barrier, e_prev, a.spin_limit, a.status) || (*(volatile int*)a.status & 1)) {
+      aborted = true;
+      break;
+    }
+    // the FP32 accelerator's stop rules on sweep - 1, as the coloured
+    // kernel applies them to each sweep
+    const double e1 = light_error(sweep - 1);
     bool stop = false;
-    if (!(incr == incr)) {
+    if (!(e1 == e1)) {
       if (threadIdx.x == 0) atomicOr(a.status, 2);
       stop = true;
     }
-    if (incr < a.switch_tol) stop = true;
-    if (incr < 0.99 * best) {
-      best = incr;
-      best_sweep = sweep;
-    } else if (a.stall_window > 0 && sweep - best_sweep >= a.stall_window) {
+    if (e1 < a.switch_tol) stop = true;
+    if (e1 < 0.99 * best) {
+      best = e1;
+      best_sweep = sweep - 1;
+    } else if (a.stall_window > 0 && sweep - 1 - best_sweep >= a.stall_window) {
       stop = true;
     }
-    if (!stop && incr < working) {
-      if (!flow_full_error<NW>(a, epoch, full)) break;
-      const double target = fmax(a.user_tol, a.switch_tol);
-      if (full <= target) {
-        converged = true;
-        stop = true;
-      } else if (full > 0.0 && incr > 0.0) {
-        double nt = (incr / full) * target;
-        const double mint = fmax(target * 1e-6, DBL_EPSILON * 1e-6);
-        if (nt < mint) nt = mint;
-        if (nt < working) working = nt;
+    if (!stop && e1 < working) {
+      if (!full_check(e1, e_last)) {
+        aborted = true;
+        break;
+      }
+      stop = converged;
+    }
+    if (stop) {
+      stopped = true;
+      break;
+    }
+  }
+  if (sweep > 0 && !aborted) {
+    // the light error of the last sweep; after a budget end, the stop rules
+    // on it as on every other sweep
+    if (!grid_wait(a.barrier, e_last, a.spin_limit, a.status) || (*(volatile int*)a.status & 1)) {
+      aborted = true;
+    } else {
+      incr = light_error(sweep);
+      if (!stopped) {
+        bool stop = false;
+        if (!(incr == incr)) {
+          if (threadIdx.x == 0) atomicOr(a.status, 2);
+          stop = true;
+        }
+        if (incr < a.switch_tol) stop = true;
+        if (!stop && incr < working) aborted = !full_check(incr, e_last);
       }
     }
-    if (stop) break;
   }
   // a copy still in flight lands before the block leaves
   if (pending) mbar_wait_bounded(bar, parity, a.spin_limit, a.status);

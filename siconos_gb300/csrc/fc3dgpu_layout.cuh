@@ -122,6 +122,7 @@ struct FlowArgs {
   const int* dptr;     // per slab: its column slabs are dep[dptr[s] .. dptr[s + 1])
   const int* dep;      // slab ids, ascending; bit 31 set: a later colour
   unsigned* done;      // per slab: sweeps completed; zero at launch
+  double* part;        // per block: 4 slots of (sum |dr|^2, sum |r|^2)
   unsigned buf_bytes;  // shared-memory buffer of one warp
   int maxslot;         // slots of one slab the buffer holds
 };
