@@ -31,6 +31,11 @@
 
 namespace fc3dgpu {
 
+// Polls of a slab's column counters before a warp starts to back off, and
+// the back-off (ns) between later polls.
+#define FC3D_FLOW_SPIN 1024
+#define FC3D_FLOW_SLEEP_NS 64
+
 __device__ __forceinline__ void flow_issue(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned char* buf,
                                            unsigned long long* bar) {
   const long long o0 = a.slab_off[s];
@@ -114,8 +119,9 @@ __device__ __forceinline__ bool grid_wait(const unsigned* flags, unsigned e, uns
 }
 
 // Wait until every slab slab s takes columns from has reached the state
-// sweep k needs (see the header).  Relaxed polls, then an acquire fence; the
-// caller's __syncwarp orders the other lanes' reads after it.
+// sweep k needs (see the header).  Acquire loads of the counters (the
+// writers release them after their reactions), no fence: the caller's
+// __syncwarp orders the other lanes' reads after them.
 __device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned k,
                                                int lane) {
   const int d0 = __ldg(&f.dptr[s]), d1 = __ldg(&f.dptr[s + 1]);
@@ -125,7 +131,7 @@ __device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const 
     bool mine = true;
     for (int i = d0 + lane; i < d1; i += 32) {
       const int d = __ldg(&f.dep[i]);
-      mine &= ld_relaxed_u32(&f.done[d & 0x7fffffff]) >= (d < 0 ? k - 1 : k);
+      mine &= ld_acquire_u32(&f.done[d & 0x7fffffff]) >= (d < 0 ? k - 1 : k);
     }
     if (__all_sync(0xffffffffu, mine)) break;
     if (++n > a.spin_limit) {
@@ -133,9 +139,8 @@ __device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const 
       if (lane == 0) atomicOr(a.status, 1);
       break;
     }
-    if (n > 1024) __nanosleep(64);
+    if (n > FC3D_FLOW_SPIN) __nanosleep(FC3D_FLOW_SLEEP_NS);
   }
-  asm volatile("fence.acq_rel.gpu;" ::: "memory");
   return ok;
 }
 
@@ -161,9 +166,11 @@ __device__ __forceinline__ FlowRow flow_row(const SweepArgs<float>& a, int s, in
   return x;
 }
 
+// The new reaction of the lane's row goes to rn (zero on take-off); the
+// light-error sums are left to the caller, after the slab's release.
 __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowArgs& f, int s, int next,
                                           unsigned char* buf, unsigned long long* bar, int lane, float ltol,
-                                          double& dr2, double& rr2, unsigned long long* tl, const FlowRow& x) {
+                                          float rn[3], unsigned long long* tl, const FlowRow& x) {
   const float* Ws = reinterpret_cast<const float*>(buf);
   const int* Cs = reinterpret_cast<const int*>(buf + (size_t)f.maxslot * 9 * FC3D_SLAB * 4);
   const float* Qs = reinterpret_cast<const float*>(Cs + (size_t)f.maxslot * FC3D_SLAB);
@@ -204,7 +211,6 @@ __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowA
       rp[0] = 0;
       rp[1] = 0;
       rp[2] = 0;
-      dr2 += (double)ro[0] * ro[0] + (double)ro[1] * ro[1] + (double)ro[2] * ro[2];
     } else {
       work = true;
 #pragma unroll
@@ -226,7 +232,24 @@ __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowA
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     flow_issue(a, f, next, buf, bar);
   }
-  if (work) solve_row_s(a, L, p, ro, ltol, dr2, rr2);
+  rn[0] = rn[1] = rn[2] = 0.f;
+  if (work) {
+    L.rho_pli = __ldcg(&a.rpli[p]);
+    L.tol = ltol;
+    L.newton_max = a.newton_max;
+    L.pli_max = a.pli_max;
+    L.ls_max = a.ls_max;
+    L.n_newton = L.n_pli = L.n_ls = 0;
+    rn[0] = ro[0];
+    rn[1] = ro[1];
+    rn[2] = ro[2];
+    local_solve(L, rn);
+    float* rp = a.r + (size_t)p * FC3D_RSTRIDE;
+    rp[0] = rn[0];
+    rp[1] = rn[1];
+    rp[2] = rn[2];
+    a.rpli[p] = L.rho_pli;
+  }
 }
 
 template <int NW>
@@ -314,11 +337,19 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
       // the next slab of this warp: later in this sweep, else the first one
       // of the next sweep (fetched even when no sweep follows; awaited at exit)
       const int next = s + tw < a.nslab ? s + tw : gw;
-      flow_slab(a, f, s, next, buf, bar, lane, (float)a.local_tol, acc[0], acc[1], tl, x);
+      float rn[3];
+      flow_slab(a, f, s, next, buf, bar, lane, (float)a.local_tol, rn, tl, x);
       pending = true;
       __syncwarp();
       if (tl) tl[4] = globaltimer_ns();
       if (lane == 0) st_release_u32(&f.done[s], (unsigned)sweep);
+      if (x.row) {
+        // light-error sums (fc3d_nsgs.c:80-96), off the slab's critical path
+        const double d0 = (double)x.ro[0] - (double)rn[0], d1 = (double)x.ro[1] - (double)rn[1],
+                     d2 = (double)x.ro[2] - (double)rn[2];
+        acc[0] += d0 * d0 + d1 * d1 + d2 * d2;
+        acc[1] += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+      }
     }
     flow_block_sum<2, NW>(acc, f.part + blockIdx.x * 8 + (sweep & 3) * 2);
     e_prev = e_last;
