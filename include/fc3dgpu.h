@@ -184,9 +184,9 @@ int fc3dgpu_ctx_update_W(fc3dgpu_ctx *ctx, int nc, const int64_t *rowptr, const 
 /* fc3dgpu_ctx_update_W with the values given as one pointer per block
  * (block[k] -> the 9 doubles of block k, column-major): the block array of
  * a SparseBlockStructuredMatrix (SparseBlockMatrix.h), so SBM storage needs
- * no repacking.  Runs of blocks adjacent in memory are copied straight from
- * there, each run sent while the pointers after it are checked; scattered
- * blocks are gathered through pinned staging buffers. */
+ * no repacking.  The pointers are checked first (by up to four host
+ * threads); runs of blocks adjacent in memory are then copied straight from
+ * there, scattered blocks gathered through pinned staging buffers. */
 int fc3dgpu_ctx_update_W_ptrs(fc3dgpu_ctx *ctx, int nc, const int64_t *rowptr, const int64_t *colidx,
                               const double *const *block, int colour_kind);
 int fc3dgpu_ctx_set_W_batch(fc3dgpu_ctx *ctx, int nproblems, const int *problem_nc, const int64_t *rowptr,

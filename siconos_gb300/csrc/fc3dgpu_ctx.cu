@@ -578,6 +578,9 @@ __global__ void k_get_r_u(int nc, const int* __restrict__ iperm, const double* _
 #include <stdarg.h>
 
 #include <algorithm>
+#include <atomic>
+#include <memory>
+#include <thread>
 #include <vector>
 #include <stdio.h>
 #include <stdlib.h>
@@ -989,10 +992,10 @@ static const long long STAGE_BLOCKS = 1 << 16;
 static const long long RUN_BLOCKS = 1 << 19;
 
 // Copy nnzb blocks from src into c->blocks (stream-ordered).  From a block
-// pointer array, runs of blocks that lie back to back in memory are copied
-// straight from there, each run sent while the pointers after it are still
-// being checked; other blocks are gathered into two pinned staging buffers
-// used in turn.
+// pointer array (checked in steps of STAGE_BLOCKS by four host threads while
+// the steps already checked are copied), runs of blocks that lie back to back
+// in memory are copied straight from there; other blocks are gathered into
+// two pinned staging buffers used in turn.
 static int upload_blocks(fc3dgpu_ctx* c, long long nnzb, BlockSource src) {
   cudaStream_t s = c->stream;
   if (src.flat) {
@@ -1000,6 +1003,49 @@ static int upload_blocks(fc3dgpu_ctx* c, long long nnzb, BlockSource src) {
     return 0;
   }
   const double* const* p = src.ptrs;
+  const uintptr_t bsz = sizeof(double) * 9;
+  // which steps hold adjacent 9-double blocks, checked by four host threads
+  // taking the steps in turn (the pointer array is 8 bytes a block: 27.6 MB
+  // at 3.45 M blocks); the copies below start as soon as their steps are
+  // checked
+  const long long nstep = (nnzb + STAGE_BLOCKS - 1) / STAGE_BLOCKS;
+  std::unique_ptr<std::atomic<int>[]> adjacent(new std::atomic<int>[(size_t)nstep]);
+  for (long long st = 0; st < nstep; st++) adjacent[st].store(-1, std::memory_order_relaxed);
+  auto scan = [&](long long first, long long stride) {
+    for (long long st = first; st < nstep; st += stride) {
+      const long long k0 = st * STAGE_BLOCKS, k1 = k0 + STAGE_BLOCKS < nnzb ? k0 + STAGE_BLOCKS : nnzb;
+      const uintptr_t b0 = (uintptr_t)p[k0];
+      uintptr_t off = 0;
+      for (long long k = k0; k < k1; k++) off |= (uintptr_t)p[k] ^ (b0 + bsz * (uintptr_t)(k - k0));
+      adjacent[st].store(b0 != 0 && off == 0, std::memory_order_release);
+    }
+  };
+  struct Joiner {
+    std::vector<std::thread> th;
+    ~Joiner() {
+      for (auto& t : th) t.join();
+    }
+  } workers;
+  {
+    const int nth = nstep >= 16 ? 4 : 0;  // small arrays: checked here
+    int started = 0;
+    try {
+      for (int t = 0; t < nth; t++) {
+        workers.th.emplace_back(scan, (long long)t, (long long)nth);
+        started++;
+      }
+    } catch (...) {
+      // fewer threads to be had
+    }
+    // the steps of threads that could not be started are checked here
+    if (nth == 0) scan(0, 1);
+    for (int t = started; t < nth; t++) scan((long long)t, (long long)nth);
+  }
+  auto is_adjacent = [&](long long st) {
+    int v;
+    while ((v = adjacent[st].load(std::memory_order_acquire)) < 0) std::this_thread::yield();
+    return v == 1;
+  };
   long long run0 = 0, runn = 0;  // pending run of adjacent blocks: first index, length
   int slot = 0;
   for (long long k0 = 0; k0 < nnzb; k0 += STAGE_BLOCKS) {
@@ -1007,12 +1053,12 @@ static int upload_blocks(fc3dgpu_ctx* c, long long nnzb, BlockSource src) {
     const double* base = p[k0];
     if (!base) {
       fc3dgpu_set_error("block %lld of W is a null pointer", k0);
+      if (runn > 0 || slot) CK(cudaStreamSynchronize(s));
       return NUMERICS_ERR_NULL_POINTER;
     }
-    const uintptr_t b0 = (uintptr_t)base, bsz = sizeof(double) * 9;
-    uintptr_t off = 0;  // zero when p[k0..k1) are adjacent 9-double blocks
-    for (long long k = k0; k < k1; k++) off |= (uintptr_t)p[k] ^ (b0 + bsz * (uintptr_t)(k - k0));
-    if (off == 0 && runn > 0 && b0 == (uintptr_t)p[run0] + bsz * (uintptr_t)(k0 - run0) &&
+    const uintptr_t b0 = (uintptr_t)base;
+    const bool adj = is_adjacent(k0 / STAGE_BLOCKS);
+    if (adj && runn > 0 && b0 == (uintptr_t)p[run0] + bsz * (uintptr_t)(k0 - run0) &&
         runn + (k1 - k0) <= RUN_BLOCKS) {
       runn += k1 - k0;
       continue;
@@ -1020,7 +1066,7 @@ static int upload_blocks(fc3dgpu_ctx* c, long long nnzb, BlockSource src) {
     if (runn > 0)
       CK(cudaMemcpyAsync(c->blocks + 9 * run0, p[run0], sizeof(double) * 9 * runn, cudaMemcpyHostToDevice, s));
     runn = 0;
-    if (off == 0) {
+    if (adj) {
       run0 = k0;
       runn = k1 - k0;
       continue;
