@@ -736,8 +736,14 @@ struct fc3dgpu_ctx {
   int colour_kind = -1;  // colouring of the current layout
   BUF(long long, wtmp);  // new structure for a comparison with the current one
   BUF(int, wdiff);
-  double* stage = nullptr;  // pinned staging for blocks gathered from scattered pointers
-  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  // upload of W's values through block pointers: per host thread a stream,
+  // two pinned staging buffers for scattered blocks with their copy events,
+  // and an event closing the thread's copies
+  cudaStream_t up_stream[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* up_stage[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t up_ev[4][2] = {};
+  cudaEvent_t up_done[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t up_start = nullptr;
   // device assembly of W and q from rigid-body contacts
   int nb = 0;
   double step_h = 0.0;
@@ -854,9 +860,14 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
   if (c->nbrmask) cudaFree(c->nbrmask);
   for (int i = 0; i < 4; i++)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
-  for (int i = 0; i < 2; i++)
-    if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
-  if (c->stage) cudaFreeHost(c->stage);
+  for (int t = 0; t < 4; t++) {
+    for (int i = 0; i < 2; i++)
+      if (c->up_ev[t][i]) cudaEventDestroy(c->up_ev[t][i]);
+    if (c->up_done[t]) cudaEventDestroy(c->up_done[t]);
+    if (c->up_stage[t]) cudaFreeHost(c->up_stage[t]);
+    if (c->up_stream[t]) cudaStreamDestroy(c->up_stream[t]);
+  }
+  if (c->up_start) cudaEventDestroy(c->up_start);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -986,16 +997,16 @@ struct BlockSource {
   const double* const* ptrs;
 };
 
-// Blocks scanned per step of upload_blocks, and the longest run of adjacent
-// blocks sent as one copy.
+// Blocks per step of upload_blocks (one copy each), and the host threads
+// that take the steps in turn.
 static const long long STAGE_BLOCKS = 1 << 16;
-static const long long RUN_BLOCKS = 1 << 19;
+static const int UPLOAD_THREADS = 4;
 
-// Copy nnzb blocks from src into c->blocks (stream-ordered).  From a block
-// pointer array (checked in steps of STAGE_BLOCKS by four host threads while
-// the steps already checked are copied), runs of blocks that lie back to back
-// in memory are copied straight from there; other blocks are gathered into
-// two pinned staging buffers used in turn.
+// Copy nnzb blocks from src into c->blocks (stream-ordered on c->stream).
+// From a block pointer array, up to four host threads take the steps of
+// STAGE_BLOCKS blocks in turn, each on its own stream: a step whose blocks
+// lie back to back in memory is copied straight from there, another one is
+// gathered into one of the thread's two pinned staging buffers first.
 static int upload_blocks(fc3dgpu_ctx* c, long long nnzb, BlockSource src) {
   cudaStream_t s = c->stream;
   if (src.flat) {
@@ -1003,96 +1014,92 @@ static int upload_blocks(fc3dgpu_ctx* c, long long nnzb, BlockSource src) {
     return 0;
   }
   const double* const* p = src.ptrs;
-  const uintptr_t bsz = sizeof(double) * 9;
-  // which steps hold adjacent 9-double blocks, checked by four host threads
-  // taking the steps in turn (the pointer array is 8 bytes a block: 27.6 MB
-  // at 3.45 M blocks); the copies below start as soon as their steps are
-  // checked
   const long long nstep = (nnzb + STAGE_BLOCKS - 1) / STAGE_BLOCKS;
-  std::unique_ptr<std::atomic<int>[]> adjacent(new std::atomic<int>[(size_t)nstep]);
-  for (long long st = 0; st < nstep; st++) adjacent[st].store(-1, std::memory_order_relaxed);
-  auto scan = [&](long long first, long long stride) {
-    for (long long st = first; st < nstep; st += stride) {
+  const int nth = nstep >= 8 ? UPLOAD_THREADS : 1;
+  if (!c->up_start) CK(cudaEventCreateWithFlags(&c->up_start, cudaEventDisableTiming));
+  for (int t = 0; t < nth; t++) {
+    if (!c->up_stream[t]) CK(cudaStreamCreateWithFlags(&c->up_stream[t], cudaStreamNonBlocking));
+    if (!c->up_done[t]) CK(cudaEventCreateWithFlags(&c->up_done[t], cudaEventDisableTiming));
+    for (int i = 0; i < 2; i++)
+      if (!c->up_ev[t][i]) CK(cudaEventCreateWithFlags(&c->up_ev[t][i], cudaEventDisableTiming));
+  }
+  // the copies follow whatever the context's stream already holds
+  CK(cudaEventRecord(c->up_start, s));
+  std::atomic<int> failed{0};           // 1: a null block pointer, 2: a CUDA call failed
+  std::atomic<long long> null_at{-1};
+  std::atomic<int> cuda_err{0};
+  auto worker = [&](int t) {
+    auto ok = [&](cudaError_t e) {
+      if (e == cudaSuccess) return true;
+      cuda_err.store((int)e);
+      failed.store(2);
+      return false;
+    };
+    if (!ok(cudaSetDevice(c->device)) || !ok(cudaStreamWaitEvent(c->up_stream[t], c->up_start, 0))) return;
+    const uintptr_t bsz = sizeof(double) * 9;
+    int slot = 0;
+    for (long long st = t; st < nstep && !failed.load(std::memory_order_relaxed); st += nth) {
       const long long k0 = st * STAGE_BLOCKS, k1 = k0 + STAGE_BLOCKS < nnzb ? k0 + STAGE_BLOCKS : nnzb;
       const uintptr_t b0 = (uintptr_t)p[k0];
       uintptr_t off = 0;
       for (long long k = k0; k < k1; k++) off |= (uintptr_t)p[k] ^ (b0 + bsz * (uintptr_t)(k - k0));
-      adjacent[st].store(b0 != 0 && off == 0, std::memory_order_release);
+      if (b0 != 0 && off == 0) {
+        if (!ok(cudaMemcpyAsync(c->blocks + 9 * k0, p[k0], sizeof(double) * 9 * (k1 - k0), cudaMemcpyHostToDevice,
+                                c->up_stream[t])))
+          return;
+        continue;
+      }
+      // scattered blocks: into a staging buffer once its last copy is done
+      if (!c->up_stage[t] &&
+          !ok(cudaHostAlloc((void**)&c->up_stage[t], sizeof(double) * 9 * 2 * STAGE_BLOCKS, cudaHostAllocDefault)))
+        return;
+      if (!ok(cudaEventSynchronize(c->up_ev[t][slot]))) return;
+      double* buf = c->up_stage[t] + 9 * STAGE_BLOCKS * slot;
+      for (long long k = k0; k < k1; k++) {
+        if (!p[k]) {
+          null_at.store(k);
+          failed.store(1);
+          return;
+        }
+        memcpy(buf + 9 * (k - k0), p[k], sizeof(double) * 9);
+      }
+      if (!ok(cudaMemcpyAsync(c->blocks + 9 * k0, buf, sizeof(double) * 9 * (k1 - k0), cudaMemcpyHostToDevice,
+                              c->up_stream[t])) ||
+          !ok(cudaEventRecord(c->up_ev[t][slot], c->up_stream[t])))
+        return;
+      slot ^= 1;
     }
   };
-  struct Joiner {
-    std::vector<std::thread> th;
-    ~Joiner() {
-      for (auto& t : th) t.join();
-    }
-  } workers;
   {
-    const int nth = nstep >= 16 ? 4 : 0;  // small arrays: checked here
-    int started = 0;
+    std::vector<std::thread> th;
+    int started = 1;
     try {
-      for (int t = 0; t < nth; t++) {
-        workers.th.emplace_back(scan, (long long)t, (long long)nth);
+      for (int t = 1; t < nth; t++) {
+        th.emplace_back(worker, t);
         started++;
       }
     } catch (...) {
-      // fewer threads to be had
+      // fewer threads to be had: the rest run here
     }
-    // the steps of threads that could not be started are checked here
-    if (nth == 0) scan(0, 1);
-    for (int t = started; t < nth; t++) scan((long long)t, (long long)nth);
+    worker(0);
+    for (int t = started; t < nth; t++) worker(t);
+    for (auto& x : th) x.join();
   }
-  auto is_adjacent = [&](long long st) {
-    int v;
-    while ((v = adjacent[st].load(std::memory_order_acquire)) < 0) std::this_thread::yield();
-    return v == 1;
-  };
-  long long run0 = 0, runn = 0;  // pending run of adjacent blocks: first index, length
-  int slot = 0;
-  for (long long k0 = 0; k0 < nnzb; k0 += STAGE_BLOCKS) {
-    const long long k1 = k0 + STAGE_BLOCKS < nnzb ? k0 + STAGE_BLOCKS : nnzb;
-    const double* base = p[k0];
-    if (!base) {
-      fc3dgpu_set_error("block %lld of W is a null pointer", k0);
-      if (runn > 0 || slot) CK(cudaStreamSynchronize(s));
-      return NUMERICS_ERR_NULL_POINTER;
-    }
-    const uintptr_t b0 = (uintptr_t)base;
-    const bool adj = is_adjacent(k0 / STAGE_BLOCKS);
-    if (adj && runn > 0 && b0 == (uintptr_t)p[run0] + bsz * (uintptr_t)(k0 - run0) &&
-        runn + (k1 - k0) <= RUN_BLOCKS) {
-      runn += k1 - k0;
-      continue;
-    }
-    if (runn > 0)
-      CK(cudaMemcpyAsync(c->blocks + 9 * run0, p[run0], sizeof(double) * 9 * runn, cudaMemcpyHostToDevice, s));
-    runn = 0;
-    if (adj) {
-      run0 = k0;
-      runn = k1 - k0;
-      continue;
-    }
-    // scattered blocks: gather through a staging buffer once its last copy is done
-    if (!c->stage) {
-      CK(cudaHostAlloc((void**)&c->stage, sizeof(double) * 9 * 2 * STAGE_BLOCKS, cudaHostAllocDefault));
-      for (int b = 0; b < 2; b++) CK(cudaEventCreateWithFlags(&c->stage_ev[b], cudaEventDisableTiming));
-    } else {
-      CK(cudaEventSynchronize(c->stage_ev[slot]));
-    }
-    double* buf = c->stage + 9 * STAGE_BLOCKS * slot;
-    for (long long k = k0; k < k1; k++) {
-      if (!p[k]) {
-        fc3dgpu_set_error("block %lld of W is a null pointer", k);
-        CK(cudaStreamSynchronize(s));
-        return NUMERICS_ERR_NULL_POINTER;
-      }
-      memcpy(buf + 9 * (k - k0), p[k], sizeof(double) * 9);
-    }
-    CK(cudaMemcpyAsync(c->blocks + 9 * k0, buf, sizeof(double) * 9 * (k1 - k0), cudaMemcpyHostToDevice, s));
-    CK(cudaEventRecord(c->stage_ev[slot], s));
-    slot ^= 1;
+  // the context's stream waits for every thread's copies
+  for (int t = 0; t < nth; t++) {
+    CK(cudaEventRecord(c->up_done[t], c->up_stream[t]));
+    CK(cudaStreamWaitEvent(s, c->up_done[t], 0));
   }
-  if (runn > 0)
-    CK(cudaMemcpyAsync(c->blocks + 9 * run0, p[run0], sizeof(double) * 9 * runn, cudaMemcpyHostToDevice, s));
+  if (failed.load()) {
+    CK(cudaStreamSynchronize(s));
+    if (failed.load() == 2) {
+      fc3dgpu_set_error("CUDA error %d (%s) in the upload of W", cuda_err.load(),
+                        cudaGetErrorString((cudaError_t)cuda_err.load()));
+      return NUMERICS_ERR_UNKNOWN;
+    }
+    fc3dgpu_set_error("block %lld of W is a null pointer", null_at.load());
+    return NUMERICS_ERR_NULL_POINTER;
+  }
   return 0;
 }
 
