@@ -337,8 +337,9 @@ def rfc3d_tiled(copies=1000, sample_copies=100, tol=1e-8):
     21-contact rockfall problem along W's diagonal (q of each copy scaled by
     a seeded factor in [0.9, 1.1]), solved from zero to tol 1e-8 within
     10,000 sweeps by the GPU solver (FP64, the reference's iterates in colour
-    order), against the CPU restatement of rolling_friction_3d_nsgs (one core)
-    on `sample_copies` copies for 200 sweeps; both as contact-sweeps/s."""
+    order; and FP32 sweeps followed by the reference's FP64 loop), against the
+    CPU restatement of rolling_friction_3d_nsgs (one core) on `sample_copies`
+    copies; all as contact-sweeps/s."""
     import oracle as O
     import siconos_gb300.numerics as sn
     z = np.load(ROOT / "tests" / "golden" / "rfc3d_rockfall_21_54029.npz")
@@ -362,6 +363,13 @@ def rfc3d_tiled(copies=1000, sample_copies=100, tol=1e-8):
         ctx.solve(tol, 20)
         ctx.set_r(np.zeros(5 * P.nc))
         res = ctx.solve(tol, 10000)
+        # mixed precision: FP32 sweeps, then the reference's FP64 loop
+        ctx.set_precision(0)
+        ctx.set_r(np.zeros(5 * P.nc))
+        ctx.solve(tol, 20)
+        ctx.set_r(np.zeros(5 * P.nc))
+        mixed = ctx.solve(tol, 10000)
+        mixed["sweeps_fp32_fp64"] = list(ctx.last_sweeps())
     finally:
         ctx.close()
     S = tile(sample_copies, 7)
@@ -373,6 +381,10 @@ def rfc3d_tiled(copies=1000, sample_copies=100, tol=1e-8):
     return {"contacts": P.nc, "blocks": P.nnzb, "colours": ncol, "tol": tol,
             "gpu_fp64": {"ms": res["ms"], "sweeps": res["iterations"], "info": res["info"], "error": res["error"],
                          "contact_sweeps_per_s": gpu},
+            "gpu_fp32_fp64": {"ms": mixed["ms"], "sweeps": mixed["iterations"],
+                              "sweeps_fp32_fp64": mixed["sweeps_fp32_fp64"], "info": mixed["info"],
+                              "error": mixed["error"], "contact_sweeps_per_s": P.nc * mixed["iterations"] /
+                              (mixed["ms"] / 1e3), "time_vs_fp64": res["ms"] / mixed["ms"]},
             "cpu_reference_port_1core": {"contacts": S.nc, "sweeps": ref.iterations, "s": cpu_s,
                                          "contact_sweeps_per_s": cpu},
             "speedup_vs_cpu": gpu / cpu}

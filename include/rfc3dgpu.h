@@ -14,7 +14,12 @@
  * the FP64 iterates are those of the reference's sequential sweep in that
  * order, bit for bit.  All sweeps of a solve run in one cooperative launch
  * with a grid barrier between colours and the convergence logic on the
- * device.
+ * device.  Mixed precision (the solver-level default, iparam[23] = 0): FP32
+ * sweeps of the same loop first (one-contact tolerance 1e-6), until the
+ * light error drops below dparam[23] (0: max(tol, 1e-6)) or stalls for
+ * dparam[25] sweeps (0: 64), then the reference's FP64 loop from their
+ * iterate; iparam[23] = 1 runs the FP64 loop only.  iparam[27] / [28] report
+ * the FP32 and FP64 sweeps. 
  *
  * Buffers of the solver-level calls are HOST memory owned by the caller. */
 #ifndef RFC3DGPU_H
@@ -83,6 +88,12 @@ int rfc3dgpu_ctx_colours(rfc3dgpu_ctx *ctx, int32_t *colour);
 int rfc3dgpu_ctx_trace(rfc3dgpu_ctx *ctx, double *out, int cap);
 /* rho of each contact (contact order), as the solve uses it. */
 int rfc3dgpu_ctx_rho(rfc3dgpu_ctx *ctx, double *rho);
+/* 1: FP64 sweeps only (the context's default); 0: FP32 sweeps until the
+ * light error drops below switch_tol (0: max(tol, 1e-6)) or makes no 1 %
+ * progress for stall_window sweeps (0: 64), then the FP64 loop. */
+int rfc3dgpu_ctx_set_precision(rfc3dgpu_ctx *ctx, int precision, double switch_tol, int stall_window);
+/* FP32 and FP64 sweeps of the last solve. */
+int rfc3dgpu_ctx_last_sweeps(rfc3dgpu_ctx *ctx, int *sweeps32, int *sweeps64);
 
 #ifdef __cplusplus
 }

@@ -6,7 +6,9 @@
 // One cooperative launch runs every sweep: a colour's contacts are spread
 // over all threads of the grid, a grid barrier separates colours, and the
 // convergence logic runs on the device with the same bits in every block.
-// FP64 without FMA contraction, in the reference's operation order.
+// FP64 without FMA contraction, in the reference's operation order; in mixed
+// precision FP32 sweeps of the same loop run first and the FP64 loop starts
+// from their iterate.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <float.h>
@@ -31,38 +33,59 @@ constexpr int MAXC = 128;
 constexpr int TRACE_CAP = 1 << 16;
 constexpr int MAX_BLOCKS = 1024;
 
-struct Args {
+// Kernel arguments; Real = double for the reference's loop, float for the
+// FP32 sweeps that precede it in mixed precision.
+template <typename Real>
+struct ArgsT {
   int nc, ncol;
   const int* cptr;  // ncol + 1 permuted-row bounds of the colours
   const int* rp;    // nc + 1 slot pointer per permuted row
   const int* col;   // permuted column of each slot (slots in ascending original column)
   const int* dpos;  // offset in the row of its first diagonal block
-  const double* W;  // 25 per slot
-  const double* q;
-  const double* mu;
-  const double* mur;
-  const double* rho;
-  double* r;
+  const Real* W;    // 25 per slot
+  const Real* q;
+  const Real* mu;
+  const Real* mur;
+  const Real* rho;
+  Real* r;
   double* u;
   double norm_q, tol, local_tol;
   int local_max, max_iter;
   double* part;   // 2 slots x MAX_BLOCKS x 4 block partial sums
-  double* trace;
+  double* trace;  // per-sweep light error, from trace[0]
   double* out;    // [0] sweeps, [1] final error, [2] info, [3] last light error
+  int trace_cap;  // entries of trace this launch may write
+  // FP32 sweeps only: their stop rules on the light error
+  double switch_tol;
+  int stall_window;
 };
+using Args = ArgsT<double>;
 
 #define E(M, i, j) (M)[(i) + 5 * (j)]
 
+template <typename Real>
+struct Eps;
+template <>
+struct Eps<double> {
+  static __device__ __forceinline__ double v() { return DBL_EPSILON; }
+};
+template <>
+struct Eps<float> {
+  static __device__ __forceinline__ float v() { return FLT_EPSILON; }
+};
+
 // ---- 5x5 algebra in the reference's operation order (op5x5.h) -------------
 
-__device__ __forceinline__ void mvp5(const double* a, const double* v, double* r) {
+template <typename Real>
+__device__ __forceinline__ void mvp5(const Real* a, const Real* v, Real* r) {
 #pragma unroll
   for (int j = 0; j < 5; j++)
 #pragma unroll
     for (int i = 0; i < 5; i++) r[i] += a[i + 5 * j] * v[j];
 }
 
-__device__ __forceinline__ void mm5(const double* a, const double* b, double* c) {
+template <typename Real>
+__device__ __forceinline__ void mm5(const Real* a, const Real* b, Real* c) {
 #pragma unroll
   for (int j = 0; j < 5; j++)
 #pragma unroll
@@ -72,8 +95,9 @@ __device__ __forceinline__ void mm5(const double* a, const double* b, double* c)
 }
 
 // solve_5x5_gepp_for_loop (op5x5.h:642-700): b unchanged on a tiny pivot
-__device__ __forceinline__ void gepp5(const double* a, double* b) {
-  double A[25], x[5];
+template <typename Real>
+__device__ __forceinline__ void gepp5(const Real* a, Real* b) {
+  Real A[25], x[5];
 #pragma unroll
   for (int i = 0; i < 25; i++) A[i] = a[i];
 #pragma unroll
@@ -83,14 +107,14 @@ __device__ __forceinline__ void gepp5(const double* a, double* b) {
 #pragma unroll
   for (int i = 0; i < 5; i++) {
     int p = i;
-    double best = fabs(E(A, i, i));
+    Real best = fabs(E(A, i, i));
 #pragma unroll
     for (int k = i + 1; k < 5; k++)
       if (fabs(E(A, k, i)) > best) {
         best = fabs(E(A, k, i));
         p = k;
       }
-    if (best < 1e-16) return;
+    if (best < Real(1e-16)) return;
     if (p != i) {
       // swap rows i and p (p > i), with register-resident indexing
 #pragma unroll
@@ -98,16 +122,16 @@ __device__ __forceinline__ void gepp5(const double* a, double* b) {
         if (k == p) {
 #pragma unroll
           for (int j = 0; j < 5; j++) {
-            const double t = E(A, i, j);
+            const Real t = E(A, i, j);
             E(A, i, j) = E(A, k, j);
             E(A, k, j) = t;
           }
-          const double t = x[i];
+          const Real t = x[i];
           x[i] = x[k];
           x[k] = t;
         }
     }
-    double f[5];
+    Real f[5];
 #pragma unroll
     for (int k = i + 1; k < 5; k++) f[k] = E(A, k, i) / E(A, i, i);
 #pragma unroll
@@ -119,7 +143,7 @@ __device__ __forceinline__ void gepp5(const double* a, double* b) {
   }
 #pragma unroll
   for (int i = 4; i >= 0; i--) {
-    double s = 0;
+    Real s = 0;
 #pragma unroll
     for (int j = i + 1; j < 5; j++) s += E(A, i, j) * x[j];
     x[i] = (x[i] - s) / E(A, i, i);
@@ -132,17 +156,18 @@ __device__ __forceinline__ void gepp5(const double* a, double* b) {
 
 enum { RC_DUAL = 0, RC_INSIDE, RC_FRICTION, RC_ROLLING, RC_FRICTION_ROLLING };
 
-__device__ __forceinline__ int proj_rcone(double* r, double mu, double mur) {
-  const double nT = sqrt(r[1] * r[1] + r[2] * r[2]);
-  const double nM = sqrt(r[3] * r[3] + r[4] * r[4]);
+template <typename Real>
+__device__ __forceinline__ int proj_rcone(Real* r, Real mu, Real mur) {
+  const Real nT = sqrt(r[1] * r[1] + r[2] * r[2]);
+  const Real nM = sqrt(r[3] * r[3] + r[4] * r[4]);
   if (mu * nT + mur * nM <= -r[0]) {
 #pragma unroll
-    for (int i = 0; i < 5; i++) r[i] = 0.0;
+    for (int i = 0; i < 5; i++) r[i] = Real(0.0);
     return RC_DUAL;
   }
   if ((nT <= mu * r[0]) && (nM <= mur * r[0])) return RC_INSIDE;
-  const double mu2 = mu * mu, mur2 = mur * mur;
-  double t = (mu * nT + mur * nM + r[0]) / (mur2 + mu2 + 1.0);
+  const Real mu2 = mu * mu, mur2 = mur * mur;
+  Real t = (mu * nT + mur * nM + r[0]) / (mur2 + mu2 + Real(1.0));
   if ((nT > mu * t) && (nM > mur * t)) {
     r[0] = t;
     r[1] = mu * r[0] * r[1] / nT;
@@ -151,14 +176,14 @@ __device__ __forceinline__ int proj_rcone(double* r, double mu, double mur) {
     r[4] = mur * r[0] * r[4] / nM;
     return RC_FRICTION_ROLLING;
   }
-  t = (mu * nT + r[0]) / (mu2 + 1.0);
+  t = (mu * nT + r[0]) / (mu2 + Real(1.0));
   if ((nT > mu * t) && (nM <= mur * t)) {
     r[0] = t;
     r[1] = mu * r[0] * r[1] / nT;
     r[2] = mu * r[0] * r[2] / nT;
     return RC_FRICTION;
   }
-  t = (mur * nM + r[0]) / (mur2 + 1.0);
+  t = (mur * nM + r[0]) / (mur2 + Real(1.0));
   if ((nT <= mu * t) && (nM > mur * t)) {
     r[0] = t;
     r[3] = mur * r[0] * r[3] / nM;
@@ -170,36 +195,37 @@ __device__ __forceinline__ int proj_rcone(double* r, double mu, double mur) {
 
 // subdifferentialProjectionOnRollingCone (projectionOnRollingCone.c),
 // zero where the reference leaves the matrix unset
-__device__ __forceinline__ void subdiff_rcone(double* H, const double* r, double mu, double mur) {
+template <typename Real>
+__device__ __forceinline__ void subdiff_rcone(Real* H, const Real* r, Real mu, Real mur) {
 #pragma unroll
-  for (int i = 0; i < 25; i++) H[i] = 0.0;
-  const double nT = sqrt(r[1] * r[1] + r[2] * r[2]);
-  const double nM = sqrt(r[3] * r[3] + r[4] * r[4]);
+  for (int i = 0; i < 25; i++) H[i] = Real(0.0);
+  const Real nT = sqrt(r[1] * r[1] + r[2] * r[2]);
+  const Real nM = sqrt(r[3] * r[3] + r[4] * r[4]);
   if (mu * nT + mur * nM <= -r[0]) return;
   if ((nT <= mu * r[0]) && (nM <= mur * r[0])) {
 #pragma unroll
-    for (int i = 0; i < 5; i++) E(H, i, i) = 1.;
+    for (int i = 0; i < 5; i++) E(H, i, i) = Real(1.);
     return;
   }
-  const double mu2 = mu * mu, mur2 = mur * mur;
-  const double a1 = mu * nT + mur * nM + r[0];
-  double k = 1. / (1. + mu2 + mur2);
-  double t = a1 * k;
+  const Real mu2 = mu * mu, mur2 = mur * mur;
+  const Real a1 = mu * nT + mur * nM + r[0];
+  Real k = Real(1.) / (Real(1.) + mu2 + mur2);
+  Real t = a1 * k;
   if ((nT > mu * t) && (nM > mur * t)) {
-    E(H, 0, 0) = 1. * k;
-    const double s1 = r[1] / nT, s2 = r[2] / nT;
-    const double mk = mu * k;
+    E(H, 0, 0) = Real(1.) * k;
+    const Real s1 = r[1] / nT, s2 = r[2] / nT;
+    const Real mk = mu * k;
     E(H, 0, 1) = mk * s1;
     E(H, 0, 2) = mk * s2;
-    const double s3 = r[3] / nM, s4 = r[4] / nM;
-    const double rk = mur * k;
+    const Real s3 = r[3] / nM, s4 = r[4] / nM;
+    const Real rk = mur * k;
     E(H, 0, 3) = rk * s3;
     E(H, 0, 4) = rk * s4;
     E(H, 1, 0) = E(H, 0, 1);
     E(H, 2, 0) = E(H, 0, 2);
     E(H, 3, 0) = E(H, 0, 3);
     E(H, 4, 0) = E(H, 0, 4);
-    const double mkT = mk / nT, a2 = r[0] + mur * nM;
+    const Real mkT = mk / nT, a2 = r[0] + mur * nM;
     E(H, 1, 1) = mkT * (-a2 * s1 * s1 + a1);
     E(H, 1, 2) = mkT * (-a2 * s1 * s2);
     E(H, 1, 3) = mk * s1 * mur * s3;
@@ -208,7 +234,7 @@ __device__ __forceinline__ void subdiff_rcone(double* H, const double* r, double
     E(H, 2, 2) = mkT * (-a2 * s2 * s2 + a1);
     E(H, 2, 3) = mk * s2 * mur * s3;
     E(H, 2, 4) = mk * s2 * mur * s4;
-    const double rkM = rk / nM, a3 = r[0] + mu * nT;
+    const Real rkM = rk / nM, a3 = r[0] + mu * nT;
     E(H, 3, 3) = rkM * (-a3 * s3 * s3 + a1);
     E(H, 3, 4) = rkM * (-a3 * s3 * s4);
     E(H, 3, 1) = E(H, 1, 3);
@@ -219,53 +245,54 @@ __device__ __forceinline__ void subdiff_rcone(double* H, const double* r, double
     E(H, 4, 2) = E(H, 2, 4);
     return;
   }
-  const double b1 = r[0] + mu * nT;
-  k = 1. / (1. + mu2);
+  const Real b1 = r[0] + mu * nT;
+  k = Real(1.) / (Real(1.) + mu2);
   t = b1 * k;
   if ((nT > mu * t) && (nM <= mur * t)) {
-    E(H, 0, 0) = 1. * k;
-    const double s1 = r[1] / nT, s2 = r[2] / nT;
-    const double mk = mu * k;
+    E(H, 0, 0) = Real(1.) * k;
+    const Real s1 = r[1] / nT, s2 = r[2] / nT;
+    const Real mk = mu * k;
     E(H, 1, 0) = mk * s1;
     E(H, 2, 0) = mk * s2;
     E(H, 0, 1) = E(H, 1, 0);
     E(H, 0, 2) = E(H, 2, 0);
-    const double mkT = mk / nT;
+    const Real mkT = mk / nT;
     E(H, 1, 1) = mkT * (-r[0] * s1 * s1 + b1);
     E(H, 1, 2) = mkT * (-r[0] * s1 * s2);
     E(H, 2, 1) = mkT * (-r[0] * s1 * s2);
     E(H, 2, 2) = mkT * (-r[0] * s2 * s2 + b1);
-    E(H, 3, 3) = 1.;
-    E(H, 4, 4) = 1.;
+    E(H, 3, 3) = Real(1.);
+    E(H, 4, 4) = Real(1.);
     return;
   }
-  const double c1 = mur * nM + r[0];
-  const double kr = 1. / (1. + mur2);
+  const Real c1 = mur * nM + r[0];
+  const Real kr = Real(1.) / (Real(1.) + mur2);
   t = c1 * kr;
   if ((nT <= mu * t) && (nM > mur * t)) {
-    E(H, 0, 0) = 1. * kr;
-    const double s3 = r[3] / nM, s4 = r[4] / nM;
-    const double rk = mur * kr;
+    E(H, 0, 0) = Real(1.) * kr;
+    const Real s3 = r[3] / nM, s4 = r[4] / nM;
+    const Real rk = mur * kr;
     E(H, 3, 0) = rk * s3;
     E(H, 4, 0) = rk * s4;
     E(H, 0, 3) = E(H, 3, 0);
     E(H, 0, 4) = E(H, 4, 0);
-    const double rkM = rk / nM;
+    const Real rkM = rk / nM;
     E(H, 3, 3) = rkM * (-r[0] * s3 * s3 + c1);
     E(H, 3, 4) = rkM * (-r[0] * s3 * s4);
     E(H, 4, 3) = rkM * (-r[0] * s3 * s4);
     E(H, 4, 4) = rkM * (-r[0] * s4 * s4 + c1);
-    E(H, 1, 1) = 1.;
-    E(H, 2, 2) = 1.;
+    E(H, 1, 1) = Real(1.);
+    E(H, 2, 2) = Real(1.);
   }
 }
 
 // rolling_friction_3D_computeNaturalMap (rolling_naturalmap_functions.c:31-165)
-__device__ __forceinline__ void natural_map(const double* R, const double* v, double mu, double mur, double rho, double* F,
-                            double* A, double* B) {
-  const double nVT = sqrt(v[1] * v[1] + v[2] * v[2]);
-  const double nOT = sqrt(v[3] * v[3] + v[4] * v[4]);
-  double RV[5];
+template <typename Real>
+__device__ __forceinline__ void natural_map(const Real* R, const Real* v, Real mu, Real mur, Real rho, Real* F,
+                            Real* A, Real* B) {
+  const Real nVT = sqrt(v[1] * v[1] + v[2] * v[2]);
+  const Real nOT = sqrt(v[3] * v[3] + v[4] * v[4]);
+  Real RV[5];
   RV[0] = R[0] - rho * (v[0] + mu * nVT + mur * nOT);
   RV[1] = R[1] - rho * v[1];
   RV[2] = R[2] - rho * v[2];
@@ -273,37 +300,37 @@ __device__ __forceinline__ void natural_map(const double* R, const double* v, do
   RV[4] = R[4] - rho * v[4];
 #pragma unroll
   for (int i = 0; i < 5; i++) F[i] = RV[i];
-  const int where = proj_rcone(F, mu, mur);
+  const int where = proj_rcone<Real>(F, mu, mur);
 #pragma unroll
   for (int i = 0; i < 5; i++) F[i] = R[i] - F[i];
   if (!A) return;
   if (where == RC_DUAL) {
 #pragma unroll
-    for (int i = 0; i < 25; i++) A[i] = 0.;
+    for (int i = 0; i < 25; i++) A[i] = Real(0.);
 #pragma unroll
-    for (int i = 0; i < 25; i++) B[i] = 0.;
+    for (int i = 0; i < 25; i++) B[i] = Real(0.);
 #pragma unroll
-    for (int i = 0; i < 5; i++) E(B, i, i) = 1.;
+    for (int i = 0; i < 5; i++) E(B, i, i) = Real(1.);
     return;
   }
-  double s1, s2, s3, s4;
-  if (nVT <= 0.0) {
-    s1 = 1.;
-    s2 = 0.;
+  Real s1, s2, s3, s4;
+  if (nVT <= Real(0.0)) {
+    s1 = Real(1.);
+    s2 = Real(0.);
   } else {
     s1 = v[1] / nVT;
     s2 = v[2] / nVT;
   }
-  if (nOT <= 0.0) {
-    s3 = 1.;
-    s4 = 0.;
+  if (nOT <= Real(0.0)) {
+    s3 = Real(1.);
+    s4 = Real(0.);
   } else {
     s3 = v[3] / nOT;
     s4 = v[4] / nOT;
   }
-  double D[25];
+  Real D[25];
 #pragma unroll
-  for (int i = 0; i < 25; i++) D[i] = 0.;
+  for (int i = 0; i < 25; i++) D[i] = Real(0.);
   E(D, 0, 0) = rho;
   E(D, 0, 1) = rho * mu * s1;
   E(D, 0, 2) = rho * mu * s2;
@@ -317,55 +344,56 @@ __device__ __forceinline__ void natural_map(const double* R, const double* v, do
 #pragma unroll
     for (int i = 0; i < 25; i++) A[i] = D[i];
 #pragma unroll
-    for (int i = 0; i < 25; i++) B[i] = 0.;
+    for (int i = 0; i < 25; i++) B[i] = Real(0.);
     return;
   }
-  double H[25];
-  subdiff_rcone(H, RV, mu, mur);
-  mm5(H, D, A);
+  Real H[25];
+  subdiff_rcone<Real>(H, RV, mu, mur);
+  mm5<Real>(H, D, A);
 #pragma unroll
-  for (int i = 0; i < 25; i++) B[i] = 0.;
+  for (int i = 0; i < 25; i++) B[i] = Real(0.);
 #pragma unroll
-  for (int i = 0; i < 5; i++) E(B, i, i) = 1.;
+  for (int i = 0; i < 5; i++) E(B, i, i) = Real(1.);
 #pragma unroll
   for (int i = 0; i < 25; i++) B[i] -= H[i];
 }
 
 // rolling_friction_3d_onecone_nonsmooth_Newton_solvers_solve_direct
 // (rolling_friction_3d_onecone_nonsmooth_Newton_solvers.c:344-505)
-__device__ __forceinline__ void local_nsn(const double* M, const double* q, double mu, double mur, double rho, double* r, double tol,
+template <typename Real>
+__device__ __forceinline__ void local_nsn(const Real* M, const Real* q, Real mu, Real mur, Real rho, Real* r, Real tol,
                           int itermax) {
-  const double nq = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] + q[4] * q[4]);
-  double rel = 1.0;
-  if (nq > DBL_EPSILON) rel /= nq;
-  double v[5], F[5], A[25], B[25], AWB[25], dR[5];
+  const Real nq = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3] + q[4] * q[4]);
+  Real rel = Real(1.0);
+  if (nq > Eps<Real>::v()) rel /= nq;
+  Real v[5], F[5], A[25], B[25], AWB[25], dR[5];
 #pragma unroll
   for (int i = 0; i < 5; i++) v[i] = q[i];
-  mvp5(M, r, v);
-  natural_map(r, v, mu, mur, rho, F, nullptr, nullptr);
-  double res = sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3] + F[4] * F[4]) * rel;
+  mvp5<Real>(M, r, v);
+  natural_map<Real>(r, v, mu, mur, rho, F, nullptr, nullptr);
+  Real res = sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3] + F[4] * F[4]) * rel;
   if (res < tol) return;
   for (int it = 1; it < itermax; it++) {
-    natural_map(r, v, mu, mur, rho, F, A, B);
-    mm5(A, M, AWB);
+    natural_map<Real>(r, v, mu, mur, rho, F, A, B);
+    mm5<Real>(A, M, AWB);
 #pragma unroll
     for (int i = 0; i < 25; i++) AWB[i] += B[i];
 #pragma unroll
-    for (int i = 0; i < 25; i++) AWB[i] *= -1.;
+    for (int i = 0; i < 25; i++) AWB[i] *= -Real(1.);
 #pragma unroll
     for (int i = 0; i < 5; i++) dR[i] = F[i];
-    gepp5(AWB, dR);
+    gepp5<Real>(AWB, dR);
 #pragma unroll
     for (int i = 0; i < 5; i++) r[i] += dR[i];
 #pragma unroll
     for (int i = 0; i < 5; i++) v[i] = q[i];
-    mvp5(M, r, v);
-    natural_map(r, v, mu, mur, rho, F, nullptr, nullptr);
-    const double e2 = (F[0] * F[0] + F[1] * F[1] + F[2] * F[2] * F[2] + F[3] * F[3] + F[4] * F[4]) * rel;
-    const double old = res;
-    res = sqrt(fmax(0.0, e2));
+    mvp5<Real>(M, r, v);
+    natural_map<Real>(r, v, mu, mur, rho, F, nullptr, nullptr);
+    const Real e2 = (F[0] * F[0] + F[1] * F[1] + F[2] * F[2] * F[2] + F[3] * F[3] + F[4] * F[4]) * rel;
+    const Real old = res;
+    res = sqrt(fmax(Real(0.0), e2));
     if (res < tol) return;
-    if (fabs(res - old) < DBL_EPSILON) return;
+    if (fabs(res - old) < Eps<Real>::v()) return;
   }
 }
 
@@ -389,8 +417,8 @@ struct Reduce {
 // through a two-slot ring in global memory: a block writes slot k & 1 only
 // after the barrier of call k - 1, which every block passes after reading
 // call k - 2's slot.  The barrier also orders all reaction updates before it.
-template <int N>
-__device__ void grid_sum(double v[N], const Args& a, Reduce& R, cg::grid_group& g) {
+template <int N, typename A>
+__device__ void grid_sum(double v[N], const A& a, Reduce& R, cg::grid_group& g) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < N; i++) {
@@ -461,6 +489,54 @@ __device__ double full_error(const Args& a, Reduce& R, cg::grid_group& g) {
   return e;
 }
 
+// One sweep over the colours (rolling_friction_3d_nsgs.c:520-590 in colour
+// order): per contact q_loc = q_p + the row sums over the other contacts'
+// columns (in column order), the take-off shortcut or the one-contact
+// Newton, the new reaction; v gets this thread's sum |r_old - r_new|^2 and
+// sum |r_new|^2 (in the precision of the sweep, summed in FP64).
+template <typename Real>
+__device__ __forceinline__ void sweep_colours(const ArgsT<Real>& a, Real local_tol, double v[2],
+                                              cg::grid_group& g) {
+  const int g0 = blockIdx.x * blockDim.x + threadIdx.x, G = gridDim.x * blockDim.x;
+  for (int c = 0; c < a.ncol; c++) {
+    for (int p = a.cptr[c] + g0; p < a.cptr[c + 1]; p += G) {
+      Real s[5] = {Real(0.0), Real(0.0), Real(0.0), Real(0.0), Real(0.0)};
+      const int s0 = a.rp[p], s1 = a.rp[p + 1];
+      for (int sl = s0; sl < s1; sl++) {
+        const int j = a.col[sl];
+        if (j == p) continue;
+        const Real* blk = a.W + 25 * (size_t)sl;
+        Real x[5];
+        for (int k = 0; k < 5; k++) x[k] = __ldcg(&a.r[5 * (size_t)j + k]);
+        for (int k = 0; k < 5; k++)
+          for (int i = 0; i < 5; i++) s[i] += __ldg(&blk[i + 5 * k]) * x[k];
+      }
+      Real ql[5], rl[5], old[5];
+      for (int i = 0; i < 5; i++) {
+        ql[i] = a.q[5 * (size_t)p + i] + s[i];
+        old[i] = __ldcg(&a.r[5 * (size_t)p + i]);
+        rl[i] = old[i];
+      }
+      if (ql[0] > -Eps<Real>::v()) {
+        for (int i = 0; i < 5; i++) rl[i] = Real(0.0);
+      } else {
+        Real M[25];
+        const Real* d = a.W + 25 * (size_t)(s0 + a.dpos[p]);
+        for (int i = 0; i < 25; i++) M[i] = __ldg(&d[i]);
+        local_nsn<Real>(M, ql, a.mu[p], a.mur[p], a.rho[p], rl, local_tol, a.local_max);
+      }
+      const Real d0 = old[0] - rl[0], d1 = old[1] - rl[1], d2 = old[2] - rl[2], d3 = old[3] - rl[3],
+                 d4 = old[4] - rl[4];
+      v[0] += (double)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4);
+      for (int i = 0; i < 5; i++) {
+        v[1] += (double)(rl[i] * rl[i]);
+        __stcg(&a.r[5 * (size_t)p + i], rl[i]);
+      }
+    }
+    if (c + 1 < a.ncol) grid_sync(g);
+  }
+}
+
 __global__ void __launch_bounds__(NT) k_rfc3d_nsgs(const Args a) {
   __shared__ Reduce R;
   cg::grid_group g = cg::this_grid();
@@ -473,49 +549,12 @@ __global__ void __launch_bounds__(NT) k_rfc3d_nsgs(const Args a) {
   while (iter < a.max_iter && not_conv) {
     ++iter;
     double v[2] = {0.0, 0.0};
-    for (int c = 0; c < a.ncol; c++) {
-      for (int p = a.cptr[c] + g0; p < a.cptr[c + 1]; p += G) {
-        // q_loc = q_p + (row sums over the other contacts' columns, in order)
-        double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-        const int s0 = a.rp[p], s1 = a.rp[p + 1];
-        for (int sl = s0; sl < s1; sl++) {
-          const int j = a.col[sl];
-          if (j == p) continue;
-          const double* blk = a.W + 25 * (size_t)sl;
-          double x[5];
-          for (int k = 0; k < 5; k++) x[k] = __ldcg(&a.r[5 * (size_t)j + k]);
-          for (int k = 0; k < 5; k++)
-            for (int i = 0; i < 5; i++) s[i] += __ldg(&blk[i + 5 * k]) * x[k];
-        }
-        double ql[5], rl[5], old[5];
-        for (int i = 0; i < 5; i++) {
-          ql[i] = a.q[5 * (size_t)p + i] + s[i];
-          old[i] = __ldcg(&a.r[5 * (size_t)p + i]);
-          rl[i] = old[i];
-        }
-        if (ql[0] > -DBL_EPSILON) {
-          for (int i = 0; i < 5; i++) rl[i] = 0.0;
-        } else {
-          double M[25];
-          const double* d = a.W + 25 * (size_t)(s0 + a.dpos[p]);
-          for (int i = 0; i < 25; i++) M[i] = __ldg(&d[i]);
-          local_nsn(M, ql, a.mu[p], a.mur[p], a.rho[p], rl, local_tol, a.local_max);
-        }
-        const double d0 = old[0] - rl[0], d1 = old[1] - rl[1], d2 = old[2] - rl[2], d3 = old[3] - rl[3],
-                     d4 = old[4] - rl[4];
-        v[0] += (d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4);
-        for (int i = 0; i < 5; i++) {
-          v[1] += rl[i] * rl[i];
-          __stcg(&a.r[5 * (size_t)p + i], rl[i]);
-        }
-      }
-      if (c + 1 < a.ncol) grid_sync(g);
-    }
+    sweep_colours<double>(a, local_tol, v, g);
     grid_sum<2>(v, a, R, g);
     err = sqrt(v[0]);
     const double nr = sqrt(v[1]);
     if (fabs(nr) > DBL_EPSILON) err /= nr;
-    if (a.trace && lead && iter <= TRACE_CAP) a.trace[iter - 1] = err;
+    if (a.trace && lead && iter <= a.trace_cap) a.trace[iter - 1] = err;
     // determine_convergence_with_full_final (rolling_friction_3d_nsgs.c:243-285)
     not_conv = 1;
     if (err < tolerance) {
@@ -539,6 +578,56 @@ __global__ void __launch_bounds__(NT) k_rfc3d_nsgs(const Args a) {
     a.out[2] = not_conv;
     a.out[3] = light;
   }
+}
+
+// The FP32 sweeps of mixed precision: the reference's loop in FP32 (FP64
+// sums of the light error) without its full-error test, ending when the
+// light error drops below switch_tol, makes no 1 % progress for
+// stall_window sweeps, turns non-finite (out[2] = 1) or the budget ends.
+// The FP64 loop then starts from their iterate.
+__global__ void __launch_bounds__(NT) k_rfc3d_sweeps32(const ArgsT<float> a) {
+  __shared__ Reduce R;
+  cg::grid_group g = cg::this_grid();
+  if (threadIdx.x == 0) R.calls = 0;
+  __syncthreads();
+  const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+  double err = INFINITY, best = INFINITY;
+  int iter = 0, best_iter = 0;
+  bool finite = true;
+  while (iter < a.max_iter) {
+    ++iter;
+    double v[2] = {0.0, 0.0};
+    sweep_colours<float>(a, (float)a.local_tol, v, g);
+    grid_sum<2>(v, a, R, g);
+    err = sqrt(v[0]);
+    const double nr = sqrt(v[1]);
+    if (fabs(nr) > DBL_EPSILON) err /= nr;
+    if (a.trace && lead && iter <= a.trace_cap) a.trace[iter - 1] = err;
+    if (!(err == err) || isinf(err)) {
+      finite = false;
+      break;
+    }
+    if (err < a.switch_tol) break;
+    if (err < 0.99 * best) {
+      best = err;
+      best_iter = iter;
+    } else if (a.stall_window > 0 && iter - best_iter >= a.stall_window) {
+      break;
+    }
+  }
+  if (lead) {
+    a.out[0] = iter;
+    a.out[2] = finite ? 0 : 1;
+    a.out[3] = err;
+  }
+}
+
+__global__ void k_rfc3d_to_f32(int n, const double* __restrict__ x, float* __restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = (float)x[i];
+}
+
+__global__ void k_rfc3d_to_f64(int n, const float* __restrict__ x, double* __restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = (double)x[i];
 }
 
 __global__ void __launch_bounds__(NT) k_rfc3d_error(const Args a) {
@@ -611,8 +700,19 @@ struct rfc3dgpu_ctx {
   int *cptr = nullptr, *rp = nullptr, *col = nullptr, *dpos = nullptr;
   double *W = nullptr, *q = nullptr, *mu = nullptr, *mur = nullptr, *rho = nullptr, *r = nullptr, *u = nullptr,
          *part = nullptr, *trace = nullptr, *out = nullptr;
+  // FP32 copies for the FP32 sweeps of mixed precision
+  float *W32 = nullptr, *q32 = nullptr, *mu32 = nullptr, *mur32 = nullptr, *rho32 = nullptr, *r32 = nullptr;
   int trace_len = 0;
+  // 1: FP64 sweeps only (default); 0: FP32 sweeps, then the FP64 loop
+  int precision = 1;
+  double switch_tol = 0.0;  // FP32 sweeps end below this light error (0: max(tol, 1e-6))
+  int stall = 64;
+  int sweeps32 = 0, sweeps64 = 0;
 };
+
+// local tolerance of the FP32 one-contact Newton (the reference's 1e-12 is
+// below FP32 resolution)
+static const double LOCAL_TOL32 = 1e-6;
 
 #define KR(x)                                                                             \
   do {                                                                                    \
@@ -624,11 +724,13 @@ struct rfc3dgpu_ctx {
   } while (0)
 
 static void free_problem(rfc3dgpu_ctx* c) {
-  void* ptrs[] = {c->cptr, c->rp, c->col, c->dpos, c->W, c->q, c->mu, c->mur, c->rho, c->r, c->u};
+  void* ptrs[] = {c->cptr, c->rp,  c->col, c->dpos, c->W,   c->q,    c->mu,    c->mur,   c->rho,
+                  c->r,    c->u,   c->W32, c->q32,  c->mu32, c->mur32, c->rho32, c->r32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   c->cptr = c->rp = c->col = c->dpos = nullptr;
   c->W = c->q = c->mu = c->mur = c->rho = c->r = c->u = nullptr;
+  c->W32 = c->q32 = c->mu32 = c->mur32 = c->rho32 = c->r32 = nullptr;
   c->nc = 0;
 }
 
@@ -784,6 +886,15 @@ extern "C" int rfc3dgpu_ctx_set_problem(rfc3dgpu_ctx* c, int nc, const int64_t* 
   if (e == cudaSuccess) e = upload(&c->rho, rhop);
   if (e == cudaSuccess) e = upload(&c->r, zero);
   if (e == cudaSuccess) e = upload(&c->u, zero);
+  {
+    auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+    if (e == cudaSuccess) e = upload(&c->W32, f32(W));
+    if (e == cudaSuccess) e = upload(&c->q32, f32(qp));
+    if (e == cudaSuccess) e = upload(&c->mu32, f32(mup));
+    if (e == cudaSuccess) e = upload(&c->mur32, f32(murp));
+    if (e == cudaSuccess) e = upload(&c->rho32, f32(rhop));
+    if (e == cudaSuccess) e = upload(&c->r32, f32(zero));
+  }
   if (e != cudaSuccess) {
     free_problem(c);
     fc3dgpu_set_error("rfc3dgpu_ctx_set_problem: %s", cudaGetErrorString(e));
@@ -800,9 +911,10 @@ extern "C" int rfc3dgpu_ctx_set_problem(rfc3dgpu_ctx* c, int nc, const int64_t* 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
   int threads = NT;
   while (threads > 32 && (c->max_colour + threads - 1) / threads < sms) threads /= 2;
-  int per_sm = 0;
+  int per_sm = 0, per_sm32 = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rfc3d_nsgs, threads, 0);
-  const int resident = std::max(1, std::min(per_sm * sms, MAX_BLOCKS));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm32, k_rfc3d_sweeps32, threads, 0);
+  const int resident = std::max(1, std::min(std::min(per_sm, per_sm32) * sms, MAX_BLOCKS));
   c->threads = threads;
   c->blocks = std::max(1, std::min((c->max_colour + threads - 1) / threads, resident));
   return 0;
@@ -837,12 +949,37 @@ static Args args_of(const rfc3dgpu_ctx* c) {
   a.norm_q = c->norm_q;
   a.part = c->part;
   a.trace = c->trace;
+  a.trace_cap = TRACE_CAP;
   a.out = c->out;
   return a;
 }
 
-template <typename K>
-static cudaError_t launch(rfc3dgpu_ctx* c, K kernel, Args& a) {
+static ArgsT<float> args32_of(const rfc3dgpu_ctx* c) {
+  ArgsT<float> a;
+  memset(&a, 0, sizeof(a));
+  a.nc = c->nc;
+  a.ncol = c->ncol;
+  a.cptr = c->cptr;
+  a.rp = c->rp;
+  a.col = c->col;
+  a.dpos = c->dpos;
+  a.W = c->W32;
+  a.q = c->q32;
+  a.mu = c->mu32;
+  a.mur = c->mur32;
+  a.rho = c->rho32;
+  a.r = c->r32;
+  a.u = c->u;
+  a.norm_q = c->norm_q;
+  a.part = c->part;
+  a.trace = c->trace;
+  a.trace_cap = TRACE_CAP;
+  a.out = c->out;
+  return a;
+}
+
+template <typename K, typename A>
+static cudaError_t launch(rfc3dgpu_ctx* c, K kernel, A& a) {
   void* params[] = {&a};
   return cudaLaunchCooperativeKernel((const void*)kernel, dim3(c->blocks), dim3(c->threads), params, 0, c->stream);
 }
@@ -854,24 +991,69 @@ extern "C" int rfc3dgpu_ctx_solve(rfc3dgpu_ctx* c, double tol, int max_iter, dou
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
   KR(cudaSetDevice(c->device));
+  const int n5 = 5 * c->nc;
+  KR(cudaEventRecord(c->ev[0], c->stream));
+  double out[4];
+  int sweeps32 = 0;
+  if (c->precision == 0 && max_iter > 0) {
+    // FP32 sweeps from the current reaction, then the FP64 loop from theirs
+    ArgsT<float> a = args32_of(c);
+    a.max_iter = max_iter;
+    a.local_tol = std::max(local_tol, LOCAL_TOL32);
+    a.local_max = local_max_iter;
+    a.switch_tol = c->switch_tol > 0.0 ? c->switch_tol : std::max(tol, 1e-6);
+    a.stall_window = c->stall;
+    k_rfc3d_to_f32<<<(n5 + 255) / 256, 256, 0, c->stream>>>(n5, c->r, c->r32);
+    KR(cudaGetLastError());
+    KR(launch(c, k_rfc3d_sweeps32, a));
+    KR(cudaMemcpyAsync(out, c->out, sizeof(out), cudaMemcpyDeviceToHost, c->stream));
+    KR(cudaStreamSynchronize(c->stream));
+    sweeps32 = (int)out[0];
+    // a non-finite FP32 iterate is dropped: the FP64 loop starts where the
+    // FP32 sweeps did
+    if (out[2] == 0.0) {
+      k_rfc3d_to_f64<<<(n5 + 255) / 256, 256, 0, c->stream>>>(n5, c->r32, c->r);
+      KR(cudaGetLastError());
+    }
+  }
   Args a = args_of(c);
   a.tol = tol;
-  a.max_iter = max_iter;
+  a.max_iter = max_iter - sweeps32;
   a.local_tol = local_tol;
   a.local_max = local_max_iter;
-  KR(cudaEventRecord(c->ev[0], c->stream));
+  a.trace = c->trace + std::min(sweeps32, TRACE_CAP);
+  a.trace_cap = TRACE_CAP - std::min(sweeps32, TRACE_CAP);
   KR(launch(c, k_rfc3d_nsgs, a));
   KR(cudaEventRecord(c->ev[1], c->stream));
-  double out[4];
   KR(cudaMemcpyAsync(out, c->out, sizeof(out), cudaMemcpyDeviceToHost, c->stream));
   KR(cudaStreamSynchronize(c->stream));
   float t = 0.f;
   cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
-  if (iters) *iters = (int)out[0];
+  c->sweeps32 = sweeps32;
+  c->sweeps64 = (int)out[0];
+  if (iters) *iters = sweeps32 + (int)out[0];
   if (error) *error = out[1];
   if (info) *info = (int)out[2];
   if (ms) *ms = t;
-  c->trace_len = std::min((int)out[0], TRACE_CAP);
+  c->trace_len = std::min(sweeps32 + (int)out[0], TRACE_CAP);
+  return 0;
+}
+
+extern "C" int rfc3dgpu_ctx_set_precision(rfc3dgpu_ctx* c, int precision, double switch_tol, int stall_window) {
+  if (!c || precision < 0 || precision > 1 || !(switch_tol >= 0.0) || stall_window < 0) {
+    fc3dgpu_set_error("rfc3dgpu_ctx_set_precision: precision 0 or 1, switch_tol >= 0, stall_window >= 0");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  c->precision = precision;
+  c->switch_tol = switch_tol;
+  c->stall = stall_window > 0 ? stall_window : 64;
+  return 0;
+}
+
+extern "C" int rfc3dgpu_ctx_last_sweeps(rfc3dgpu_ctx* c, int* sweeps32, int* sweeps64) {
+  if (!c) return NUMERICS_ERR_INVALID_ARGUMENT;
+  if (sweeps32) *sweeps32 = c->sweeps32;
+  if (sweeps64) *sweeps64 = c->sweeps64;
   return 0;
 }
 

@@ -115,6 +115,9 @@ void rfc3dgpu_nsgs_set_default(SolverOptions *options) {
   ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY] = 0;
   dp[SICONOS_DPARAM_TOL] = 1e-4;
   dp[SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO] = 10.0;
+  ip[FC3DGPU_IPARAM_PRECISION] = 0;  /* FP32 sweeps, then the reference's FP64 loop */
+  dp[FC3DGPU_DPARAM_SWITCH_TOL] = 0.0;
+  dp[FC3DGPU_DPARAM_STALL] = 0.0;
   if (options->numberOfInternalSolvers == 0 || !options->internalSolvers) {
     options->numberOfInternalSolvers = 1;
     options->internalSolvers = (SolverOptions **)calloc(1, sizeof(SolverOptions *));
@@ -200,6 +203,15 @@ int rfc3dgpu_nsgs(RollingFrictionContactProblem *problem, double *reaction, doub
   rc = cached_ctx(problem, options, &ctx);
   if (!rc) rc = rfc3dgpu_ctx_set_r(ctx, reaction);
   if (rc) return rc;
+  const int prec = options->iparam[FC3DGPU_IPARAM_PRECISION];
+  if (prec != 0 && prec != 1) {
+    fc3dgpu_set_error("iparam[FC3DGPU_IPARAM_PRECISION] must be 0 (FP32 + FP64 loop) or 1 (FP64)");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  const double sw = options->dparam[FC3DGPU_DPARAM_SWITCH_TOL];
+  const double stall = options->dparam[FC3DGPU_DPARAM_STALL];
+  rc = rfc3dgpu_ctx_set_precision(ctx, prec, sw > 0 ? sw : 0.0, stall > 0 ? (int)stall : 0);
+  if (rc) return rc;
   const SolverOptions *lo = options->internalSolvers[0];
   int iters = 0, info = 1;
   double error = INFINITY, ms = 0.0;
@@ -212,6 +224,8 @@ int rfc3dgpu_nsgs(RollingFrictionContactProblem *problem, double *reaction, doub
   options->dparam[SICONOS_DPARAM_RESIDU] = error;
   options->iparam[FC3DGPU_IPARAM_COLOURS] = rfc3dgpu_ctx_colours(ctx, NULL);
   options->dparam[FC3DGPU_DPARAM_MS_SOLVE] = ms;
+  rfc3dgpu_ctx_last_sweeps(ctx, &options->iparam[FC3DGPU_IPARAM_SWEEPS_FP32],
+                           &options->iparam[FC3DGPU_IPARAM_SWEEPS_FP64]);
   if (options->callback && options->callback->collectStatsIteration && iters > 0) {
     double *tr = (double *)malloc(sizeof(double) * (size_t)iters);
     if (tr) {

@@ -275,6 +275,8 @@ ABI = {
     "rfc3dgpu_ctx_colours": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rfc3dgpu_ctx_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "rfc3dgpu_ctx_rho": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rfc3dgpu_ctx_set_precision": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
+    "rfc3dgpu_ctx_last_sweeps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc2dgpu_percolour_create": (C.c_void_p, [C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]),
     "fc2dgpu_percolour_destroy": (None, [C.c_void_p]),
     "fc2dgpu_percolour_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int), _DP,
@@ -791,6 +793,17 @@ class RollingContext:
         out = np.zeros(max(cap, 1))
         n = lib().rfc3dgpu_ctx_trace(self.ctx, out.ctypes.data, cap)
         return out[:max(n, 0)].copy()
+
+    def set_precision(self, precision: int, switch_tol: float = 0.0, stall_window: int = 0):
+        """0: FP32 sweeps, then the reference's FP64 loop from their iterate;
+        1: FP64 sweeps only (the default of a context)."""
+        _check(lib().rfc3dgpu_ctx_set_precision(self.ctx, precision, switch_tol, stall_window))
+
+    def last_sweeps(self):
+        """(FP32 sweeps, FP64 sweeps) of the last solve."""
+        a, b = C.c_int(), C.c_int()
+        _check(lib().rfc3dgpu_ctx_last_sweeps(self.ctx, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def close(self):
         if getattr(self, "ctx", None):

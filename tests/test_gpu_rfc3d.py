@@ -122,3 +122,59 @@ def test_bad_structure_is_rejected(sn):
                           [0.1, 0.1])
     with pytest.raises(ValueError, match="friction"):
         sn.RollingContext(1, [0, 1], [0], np.eye(5).reshape(-1), -np.ones(5), [-0.5], [0.1])
+
+
+@pytest.mark.parametrize("case", ["rfc3d_rockfall_14_25792", "rfc3d_rockfall_21_54029", "rfc3d_RFC3D_cube_1"])
+def test_mixed_precision_reaches_tolerance(sn, case):
+    """FP32 sweeps, then the reference's FP64 loop from their iterate: the
+    same tolerance as the FP64 solver, the error the oracle computes for the
+    final reaction, the sweeps split between the precisions."""
+    import oracle as O
+    P, g = load_rfc3d(case)
+    ctx = _ctx(sn, P)
+    ctx.set_precision(0)
+    res = ctx.solve(1e-8, 10000)
+    s32, s64 = ctx.last_sweeps()
+    r, u = ctx.get_r_u()
+    ctx.close()
+    assert res["info"] == 0 and res["error"] < 1e-8
+    assert s32 + s64 == res["iterations"] and s32 >= 1
+    e, u_chk = O.rfc3d_compute_error_port(P, r)
+    np.testing.assert_array_equal(u, u_chk)
+    assert e == pytest.approx(res["error"], rel=RTOL, abs=0)
+
+
+def test_mixed_precision_on_tiled_problem(sn):
+    """Mixed precision on 200 copies of the rockfall problem: it meets the
+    tolerance, and its FP64 part is the reference's loop from the FP32
+    iterate, bit for bit the oracle's sweeps in colour order from it."""
+    import oracle as O
+    P, _ = load_rfc3d("rfc3d_rockfall_21_54029")
+    T = tiled(P, 200, 3)
+    ctx = _ctx(sn, T)
+    _, colour = ctx.colours()
+    ctx.set_precision(0, switch_tol=1e-5)
+    res = ctx.solve(1e-8, 10000)
+    s32, s64 = ctx.last_sweeps()
+    r_mixed, _ = ctx.get_r_u()
+    assert res["info"] == 0 and res["error"] < 1e-8 and s32 > 0 and s64 > 0
+    # the FP32 iterate alone: the same FP32 sweeps within a budget of s32
+    ctx.set_r(np.zeros(5 * T.nc))
+    ctx.solve(1e-8, s32)
+    assert ctx.last_sweeps() == (s32, 0)
+    r32, _ = ctx.get_r_u()
+    ctx.close()
+    ref = O.rfc3d_nsgs_port(T, r0=r32, tol=1e-8, maxiter=10000 - s32, order=_order(colour))
+    assert ref.iterations == s64
+    np.testing.assert_array_equal(r_mixed, ref.r)
+    assert res["error"] == pytest.approx(ref.error, rel=RTOL, abs=0)
+
+
+def test_precision_arguments_are_checked(sn):
+    P, _ = load_rfc3d("rfc3d_RFC3D_cube_1")
+    ctx = _ctx(sn, P)
+    with pytest.raises(RuntimeError):
+        ctx.set_precision(2)
+    with pytest.raises(RuntimeError):
+        ctx.set_precision(0, switch_tol=-1.0)
+    ctx.close()
