@@ -236,6 +236,12 @@ int fc3dgpu_ctx_sync(fc3dgpu_ctx *ctx, int neighbourhood);
  * either way.  Applies with one lane per contact when no slab has more
  * than 16 off-diagonal slots.  Returns the previous setting. */
 int fc3dgpu_ctx_flow(fc3dgpu_ctx *ctx, int on);
+/* Polls before a barrier, slab-counter or bulk-copy wait of the sweep
+ * kernels gives up (0: the default 2^22, seconds); the kernel then records
+ * FC3DGPU_STATUS_BARRIER_TIMEOUT, every block leaves (each after its own
+ * bulk copies in flight have landed) and the solve returns an error; the
+ * context stays usable.  Returns the previous setting. */
+unsigned long long fc3dgpu_ctx_spin_limit(fc3dgpu_ctx *ctx, unsigned long long polls);
 /* r = 0 on the device (PLI steps reset), without a host copy. */
 int fc3dgpu_ctx_zero_r(fc3dgpu_ctx *ctx);
 /* The CUDA stream (cudaStream_t) every kernel of this context runs on, for

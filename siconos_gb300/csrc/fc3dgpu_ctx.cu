@@ -695,6 +695,7 @@ struct fc3dgpu_ctx {
   int ccount[FC3D_MAX_COLOURS];
   std::vector<int> slab_nslot_h;
   int staging = 1;  // bulk-copy staging of slab ranges for the FP32 sweeps
+  unsigned long long spin_limit = 0;  // polls before a device wait gives up (0: 2^22)
   // slab-dataflow FP32 sweep: on/off, and its per-layout column lists
   // (state 0: not built for this layout, 1: built, -1: does not apply)
   int flow_on = 1;
@@ -1427,6 +1428,17 @@ extern "C" int fc3dgpu_ctx_flow(fc3dgpu_ctx* c, int on) {
   return old;
 }
 
+// Polls before a barrier, slab-counter or bulk-copy wait of the sweep
+// kernels gives up (0: the default 2^22); a wait that gives up sets
+// FC3DGPU_STATUS_BARRIER_TIMEOUT and the solve returns an error.  Returns
+// the previous setting.
+extern "C" unsigned long long fc3dgpu_ctx_spin_limit(fc3dgpu_ctx* c, unsigned long long polls) {
+  if (!c) return 0;
+  const unsigned long long old = c->spin_limit;
+  c->spin_limit = polls;
+  return old;
+}
+
 extern "C" int fc3dgpu_ctx_zero_r(fc3dgpu_ctx* c) {
   if (!c || !c->have_W) {
     fc3dgpu_set_error("fc3dgpu_ctx_zero_r: no problem");
@@ -1512,7 +1524,7 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.trace_cap = (int)c->trace_cap;
   a.trace_base = 0;
   a.norm_q = c->norm_q;
-  a.spin_limit = 1ULL << 22;
+  a.spin_limit = c->spin_limit ? c->spin_limit : 1ULL << 22;
   a.counters = c->counters_on ? c->counters : nullptr;
   a.timeline = c->timeline_sweep > 0 ? c->timeline : nullptr;
   a.timeline_sweep = c->timeline_sweep;
@@ -1815,7 +1827,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
   if (st) *st = S;
   if (status) {
     fc3dgpu_set_error("device status %d (%s)", status,
-                      (status & FC3DGPU_STATUS_BARRIER_TIMEOUT) ? "grid barrier timed out" : "non-finite iterate");
+                      (status & FC3DGPU_STATUS_BARRIER_TIMEOUT) ? "a device wait timed out" : "non-finite iterate");
     return NUMERICS_ERR_UNKNOWN;
   }
   return 0;

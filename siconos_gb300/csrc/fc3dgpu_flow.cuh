@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
     }
   }
   // a copy still in flight lands before the block leaves
-  if (pending) mbar_wait_bounded(bar, parity, a.spin_limit, a.status);
+  if (pending) mbar_wait_bounded(bar, parity, exit_wait_limit(a.spin_limit), a.status);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.out[0] = sweep;
     a.out[1] = incr;

@@ -327,6 +327,15 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
                : "memory");
 }
 
+// Polls granted to the wait for a block's own bulk copies in flight before
+// it leaves the kernel (however small the spin limit of the other waits:
+// no block exits with a copy into its shared memory still running).
+#define FC3D_EXIT_WAIT (1ULL << 24)
+
+__device__ __forceinline__ unsigned long long exit_wait_limit(unsigned long long spin_limit) {
+  return spin_limit > FC3D_EXIT_WAIT ? spin_limit : FC3D_EXIT_WAIT;
+}
+
 // Bounded wait for the staging barrier: on expiry records the timeout bit.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity, unsigned long long limit,
                                                   int* status) {
@@ -879,8 +888,11 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
             stage + ((a.stage_w_bytes + a.stage_c_bytes + a.stage_q_bytes + a.stage_d_bytes / 9 * 12 + 15) & ~15u));
         if (!process_colour_staged<Real>(a, c, (Real)local_tol, acc[0], acc[1], wks, stage, &stage_bar, parity,
                                          pending,
-                                         tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * FC3D_TL_STRIDE + 2 : nullptr))
+                                         tl ? a.timeline + ((size_t)c * gridDim.x + blockIdx.x) * FC3D_TL_STRIDE + 2 : nullptr)) {
+          // the staged copy the wait gave up on lands before the block leaves
+          if (pending) mbar_wait_bounded(&stage_bar, parity, exit_wait_limit(a.spin_limit), a.status);
           return;
+        }
       } else if (T == 1) {
         int lo, hi;
         block_range(s0, a.sptr[c + 1], lo, hi);
@@ -908,7 +920,7 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
                                         a.nbr_ptr[blockIdx.x + 1] - a.nbr_ptr[blockIdx.x], a.spin_limit, a.status)
                           : grid_barrier(a.barrier, epoch, a.spin_limit, a.status);
       if (!ok) {
-        if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+        if (pending) mbar_wait_bounded(&stage_bar, parity, exit_wait_limit(a.spin_limit), a.status);
         return;
       }
     }
@@ -924,7 +936,7 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
       // check_convergence_with_adaptation (fc3d_nsgs.c:496-534)
       if (incr < working) {
         if (!full_error_phase(a, 2, epoch, full)) {
-          if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+          if (pending) mbar_wait_bounded(&stage_bar, parity, exit_wait_limit(a.spin_limit), a.status);
           return;
         }
         if (full <= a.user_tol) {
@@ -958,7 +970,7 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
       // as their full error (FP32 arithmetic, FP64 sums) reaches it
       if (!stop && incr < working) {
         if (!full_error_phase(a, 2, epoch, full)) {
-          if (pending) mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+          if (pending) mbar_wait_bounded(&stage_bar, parity, exit_wait_limit(a.spin_limit), a.status);
           return;
         }
         const double target = fmax(a.user_tol, a.switch_tol);
@@ -977,7 +989,7 @@ __global__ void __launch_bounds__(BlockDim<Real>::value, 1) nsgs_kernel(const Sw
   }
   if (pending) {
     // a staged copy of the colour after the last one is still in flight
-    mbar_wait_bounded(&stage_bar, parity, a.spin_limit, a.status);
+    mbar_wait_bounded(&stage_bar, parity, exit_wait_limit(a.spin_limit), a.status);
     pending = false;
   }
   int info = 1;

@@ -70,6 +70,11 @@ class DeviceSolver:
     def staging(self, on: bool) -> bool:
         return bool(self.L.fc3dgpu_ctx_staging(self.ctx, int(on)))
 
+    def spin_limit(self, polls: int) -> int:
+        """Polls before a device wait gives up (0 = default); returns the
+        previous setting."""
+        return int(self.L.fc3dgpu_ctx_spin_limit(self.ctx, polls))
+
     def flow(self, on: bool) -> bool:
         """Slab-dataflow FP32 sweeps (True) or the coloured kernel (False);
         returns the previous setting."""

@@ -217,6 +217,7 @@ ABI = {
     "fc3dgpu_ctx_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_sync": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_flow": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_ctx_spin_limit": (C.c_ulonglong, [C.c_void_p, C.c_ulonglong]),
     "fc3dgpu_ctx_timeline": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "fc3dgpu_ctx_launches": (C.c_ulonglong, [C.c_void_p]),

@@ -399,3 +399,32 @@ def test_driver_with_scattered_sbm_blocks(gpu):
     assert sn.fc3d_driver(prob, r, u, o) == info1 and (r == r1).all()
     o.release()
     del keep
+
+
+@pytest.mark.parametrize("flow", [True, False])
+def test_wait_timeout_is_an_error_and_the_context_recovers(gpu, flow):
+    """With a spin limit of one poll the sweep kernels' waits give up: every
+    block leaves (after its own bulk copies), the solve reports the timeout,
+    and the next solve with the default limit gives the same iterates as
+    before."""
+    from siconos_gb300 import scene
+    s = scene.lattice(30, 30, 15, seed=2)
+    gpu.load(s)
+    prev = gpu.flow(flow)
+    kw = dict(tol=1e-300, max_iter=20, lanes=1, fp32_only=1, switch_tol=0.0, stall_window=0)
+    try:
+        gpu.zero_r()
+        gpu.solve(**kw)
+        r_ref, _ = gpu.get()
+        old = gpu.spin_limit(1)
+        gpu.zero_r()
+        with pytest.raises(RuntimeError, match="timed out"):
+            gpu.solve(**kw)
+        gpu.spin_limit(old)
+        gpu.zero_r()
+        st = gpu.solve(**kw)
+        r, _ = gpu.get()
+        assert st["status"] == 0 and np.array_equal(r, r_ref)
+    finally:
+        gpu.flow(prev)
+        gpu.spin_limit(0)
