@@ -34,6 +34,10 @@ void fc3dgpu_bcsr_free(Bcsr *b);
  * set, as solver_options_create does. */
 SolverOptions *fc3dgpu_options_alloc(int id, int max_iter, double tol);
 void fc3dgpu_set_error(const char *fmt, ...);
+/* |q| as fc3dgpu_ctx_set_q_mu computes it, and fc3dgpu_ctx_set_q_mu with
+ * that value given (so the host can compute it while W uploads). */
+double fc3dgpu_norm_q_host(const double *q, long long n);
+int fc3dgpu_ctx_set_q_mu_norm(fc3dgpu_ctx *ctx, const double *q, const double *mu, double norm_q);
 
 #ifdef __cplusplus
 }

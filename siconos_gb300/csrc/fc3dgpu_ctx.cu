@@ -1326,7 +1326,30 @@ extern "C" int fc3dgpu_ctx_set_W_batch(fc3dgpu_ctx* c, int nscenes, const int* s
   return set_W_impl(c, (int)nc, rowptr, colidx, BlockSource{blocks, nullptr}, kind, nscenes, scene_nc);
 }
 
+// |q| of 3nc doubles: four interleaved partial sums of squares combined in a
+// fixed order (deterministic; a plain index-order sum would be a 3nc-long
+// dependent chain).
+extern "C" double fc3dgpu_norm_q_host(const double* q, long long n) {
+  double s4[4] = {0.0, 0.0, 0.0, 0.0};
+  long long i = 0;
+  for (; i + 4 <= n; i += 4)
+    for (int k = 0; k < 4; k++) s4[k] += q[i + k] * q[i + k];
+  for (; i < n; i++) s4[0] += q[i] * q[i];
+  return sqrt((s4[0] + s4[1]) + (s4[2] + s4[3]));
+}
+
+static int set_q_mu_impl(fc3dgpu_ctx* c, const double* q, const double* mu, double norm_q);
+
 extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const double* mu) {
+  return set_q_mu_impl(c, q, mu, -1.0);
+}
+
+// fc3dgpu_ctx_set_q_mu with |q| computed by the caller (fc3dgpu_norm_q_host)
+extern "C" int fc3dgpu_ctx_set_q_mu_norm(fc3dgpu_ctx* c, const double* q, const double* mu, double norm_q) {
+  return set_q_mu_impl(c, q, mu, norm_q);
+}
+
+static int set_q_mu_impl(fc3dgpu_ctx* c, const double* q, const double* mu, double norm_q) {
   using namespace fc3dgpu;
   if (!c || !c->have_W || !q || !mu) {
     fc3dgpu_set_error("fc3dgpu_ctx_set_q_mu: W not set or null input");
@@ -1341,16 +1364,8 @@ extern "C" int fc3dgpu_ctx_set_q_mu(fc3dgpu_ctx* c, const double* q, const doubl
   k_set_q_mu<<<grid1d(nc), 256, 0, c->stream>>>(nc, c->iperm, c->qo, c->muo, c->q64, c->mu64, c->q32, c->mu32);
   CK(cudaGetLastError());
   c->launches++;
-  // |q|: four interleaved partial sums of squares combined in a fixed order
-  // (deterministic; it overlaps the copies just queued, and a plain
-  // index-order sum would be a 3nc-long dependent chain on the host)
-  double s4[4] = {0.0, 0.0, 0.0, 0.0};
-  const long long n3 = 3LL * nc;
-  long long i = 0;
-  for (; i + 4 <= n3; i += 4)
-    for (int k = 0; k < 4; k++) s4[k] += q[i + k] * q[i + k];
-  for (; i < n3; i++) s4[0] += q[i] * q[i];
-  c->norm_q = sqrt((s4[0] + s4[1]) + (s4[2] + s4[3]));
+  // |q| on the host (it overlaps the copies just queued), unless given
+  c->norm_q = norm_q >= 0.0 ? norm_q : fc3dgpu_norm_q_host(q, 3LL * nc);
   if (c->nscenes > 0) {
     c->scene_normq_h.assign(c->nscenes, 0.0);
     for (int g = 0; g < c->nscenes; g++) {

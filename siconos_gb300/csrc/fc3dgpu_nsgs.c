@@ -12,6 +12,7 @@
  *   per-iteration callback                    fc3d_nsgs.c:103-110 */
 #include <float.h>
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -402,6 +403,19 @@ static int cached_ctx(FrictionContactProblem *P, SolverOptions *o, fc3dgpu_ctx *
   return 0;
 }
 
+/* |q| computed on a host thread while W uploads */
+typedef struct {
+  const double *q;
+  long long n;
+  double norm;
+} NormJob;
+
+static void *norm_job(void *p) {
+  NormJob *j = (NormJob *)p;
+  j->norm = fc3dgpu_norm_q_host(j->q, j->n);
+  return NULL;
+}
+
 int fc3dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velocity, SolverOptions *options) {
   int rc = check_problem(problem, reaction, velocity);
   if (rc) return rc;
@@ -409,9 +423,14 @@ int fc3dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velo
   if (rc) return rc;
   const double t0 = now_s();
   fc3dgpu_ctx *ctx = NULL;
+  NormJob nj = {problem->q, 3LL * problem->numberOfContacts, 0.0};
+  pthread_t th;
+  const int threaded = pthread_create(&th, NULL, norm_job, &nj) == 0;
+  if (!threaded) norm_job(&nj);
   rc = cached_ctx(problem, options, &ctx);
+  if (threaded) pthread_join(th, NULL);
   if (rc) return rc;
-  rc = fc3dgpu_ctx_set_q_mu(ctx, problem->q, problem->mu);
+  rc = fc3dgpu_ctx_set_q_mu_norm(ctx, problem->q, problem->mu, nj.norm);
   if (!rc) rc = fc3dgpu_ctx_set_r(ctx, reaction);
   if (rc) return rc;
   fc3dgpu_params p;
