@@ -54,7 +54,7 @@ extern "C" {
 #define FC3DGPU_IPARAM_SWEEPS_FP64 28 /* out: FP64 sweeps done */
 #define FC3DGPU_IPARAM_COLOURS 29     /* out: number of colours */
 #define FC3DGPU_DPARAM_SWITCH_TOL 23  /* in: FP32 -> FP64 switch on the incremental error (default 1e-6) */
-#define FC3DGPU_DPARAM_LOCAL_TOL32 24 /* in: FP32 local Newton tolerance (default 1e-6) */
+#define FC3DGPU_DPARAM_LOCAL_TOL32 24 /* in: FP32 local Newton tolerance (default 1e-5) */
 #define FC3DGPU_DPARAM_STALL 25       /* in: FP32 stall window in sweeps (default 64) */
 #define FC3DGPU_DPARAM_MS_SWEEP32 26  /* out: mean device time of one FP32 sweep (ms) */
 #define FC3DGPU_DPARAM_MS_SWEEP64 27  /* out: mean device time of one FP64 sweep (ms) */

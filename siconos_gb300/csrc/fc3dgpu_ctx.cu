@@ -784,7 +784,12 @@ extern "C" void fc3dgpu_params_default(fc3dgpu_params* p) {
   p->switch_tol = 1e-6;
   p->stall_window = 64;
   p->local_tol = 1e-14;
-  p->local_tol32 = 1e-6;
+  // FP32 local tolerance: 1e-6 sits a few FP32 ulps above the resolution of
+  // the relative local error, so Newton often cannot certify it and falls to
+  // PLI; 1e-5 gives the same progress per sweep (60x60x30 lattice: the same
+  // light error after 100 sweeps to 4 digits, the same 550 sweeps to 1e-3)
+  // for 3 % less time per sweep
+  p->local_tol32 = 1e-5;
   p->newton_max = 100;
   p->pli_max = 100;
   p->ls_max = 10;

@@ -113,7 +113,7 @@ void fc3dgpu_nsgs_set_default(SolverOptions *options) {
   ip[FC3DGPU_IPARAM_WARMSTART] = 0;
   ip[FC3DGPU_IPARAM_COLOURING] = FC3DGPU_COLOURING_DEFAULT;
   dp[FC3DGPU_DPARAM_SWITCH_TOL] = 1e-6;
-  dp[FC3DGPU_DPARAM_LOCAL_TOL32] = 1e-6;
+  dp[FC3DGPU_DPARAM_LOCAL_TOL32] = 1e-5;
   dp[FC3DGPU_DPARAM_STALL] = 64;
   if (options->numberOfInternalSolvers == 0 || !options->internalSolvers) {
     options->numberOfInternalSolvers = 1;
