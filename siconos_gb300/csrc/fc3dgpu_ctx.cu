@@ -281,12 +281,16 @@ __global__ void k_fill_col_pad(long long nslots, int npad, int* __restrict__ col
 }
 
 // scatter the blocks of each row into the slab layout (FP64 master copy)
-__global__ void k_fill_blocks(int nc, const long long* __restrict__ rowptr, const long long* __restrict__ colidx,
-                              const double* __restrict__ blocks, const int* __restrict__ iperm,
-                              const long long* __restrict__ slab_off, double* __restrict__ W, int* __restrict__ col,
-                              double* __restrict__ D, double* __restrict__ rho) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
-    const int p = iperm[i];
+// One thread per padded row, in slab order: the 32 rows of a slab write
+// each slot's element e as one coalesced line.
+__global__ void k_fill_blocks(int npad, const int* __restrict__ perm, const long long* __restrict__ rowptr,
+                              const long long* __restrict__ colidx, const double* __restrict__ blocks,
+                              const int* __restrict__ iperm, const long long* __restrict__ slab_off,
+                              double* __restrict__ W, int* __restrict__ col, double* __restrict__ D,
+                              double* __restrict__ rho) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x) {
+    const int i = perm[p];
+    if (i < 0) continue;
     const int slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
     const long long base = slab_off[slab];
     int s = 0;
@@ -1263,8 +1267,8 @@ static int build_layout(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, int ns
   CK(cudaMemsetAsync(c->r32, 0, sizeof(float) * (npad + 1) * 4, s));
   CK(cudaMemsetAsync(c->u64, 0, sizeof(double) * npad * 3, s));
   k_fill_col_pad<<<grid1d((long long)nslots * FC3D_SLAB), 256, 0, s>>>(nslots, npad, c->col);
-  k_fill_blocks<<<grid1d(nc, 128), 128, 0, s>>>(nc, c->rowptr, c->colidx, c->blocks, c->iperm, c->slab_off, c->W64,
-                                                c->col, c->D64, c->rho64);
+  k_fill_blocks<<<grid1d(npad, 128), 128, 0, s>>>(npad, c->perm, c->rowptr, c->colidx, c->blocks, c->iperm,
+                                                  c->slab_off, c->W64, c->col, c->D64, c->rho64);
   k_to_f32<<<grid1d((long long)nw), 256, 0, s>>>((long long)nw, c->W64, c->W32);
   k_to_f32<<<grid1d((long long)nslab * 9 * 32), 256, 0, s>>>((long long)nslab * 9 * 32, c->D64, c->D32);
   k_to_f32<<<grid1d((long long)nslab * 2 * 32), 256, 0, s>>>((long long)nslab * 2 * 32, c->rho64, c->rho32);
@@ -2626,8 +2630,8 @@ static int update_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const in
     if (rc) return rc;
   }
   const long long nw = c->nslots * 9 * FC3D_SLAB;
-  k_fill_blocks<<<grid1d(nc, 128), 128, 0, s>>>(nc, c->rowptr, c->colidx, c->blocks, c->iperm, c->slab_off, c->W64,
-                                                c->col, c->D64, c->rho64);
+  k_fill_blocks<<<grid1d(c->npad, 128), 128, 0, s>>>(c->npad, c->perm, c->rowptr, c->colidx, c->blocks, c->iperm,
+                                                     c->slab_off, c->W64, c->col, c->D64, c->rho64);
   k_to_f32<<<grid1d(nw), 256, 0, s>>>(nw, c->W64, c->W32);
   k_to_f32<<<grid1d((long long)c->nslab * 9 * 32), 256, 0, s>>>((long long)c->nslab * 9 * 32, c->D64, c->D32);
   k_to_f32<<<grid1d((long long)c->nslab * 2 * 32), 256, 0, s>>>((long long)c->nslab * 2 * 32, c->rho64, c->rho32);
