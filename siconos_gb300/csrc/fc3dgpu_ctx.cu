@@ -749,6 +749,7 @@ struct fc3dgpu_ctx {
   cudaEvent_t up_ev[4][2] = {};
   cudaEvent_t up_done[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t up_start = nullptr;
+  int* diff_h = nullptr;  // pinned: the structure comparison's result
   // device assembly of W and q from rigid-body contacts
   int nb = 0;
   double step_h = 0.0;
@@ -878,6 +879,7 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
     if (c->up_stream[t]) cudaStreamDestroy(c->up_stream[t]);
   }
   if (c->up_start) cudaEventDestroy(c->up_start);
+  if (c->diff_h) cudaFreeHost(c->diff_h);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -2611,24 +2613,31 @@ static int update_W_impl(fc3dgpu_ctx* c, int nc, const int64_t* rowptr, const in
   CK(cudaMemsetAsync(c->wdiff, 0, sizeof(int), s));
   k_differs<<<grid1d(nc + 1), 256, 0, s>>>(nc + 1, c->wtmp, c->rowptr, c->wdiff);
   k_differs<<<grid1d(nnzb), 256, 0, s>>>(nnzb, c->wtmp + nc + 1, c->colidx, c->wdiff);
-  int diff = 1;
-  CK(cudaMemcpyAsync(&diff, c->wdiff, sizeof(int), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
+  if (!c->diff_h) CK(cudaHostAlloc((void**)&c->diff_h, sizeof(int), cudaHostAllocDefault));
+  *c->diff_h = 1;
+  CK(cudaMemcpyAsync(c->diff_h, c->wdiff, sizeof(int), cudaMemcpyDeviceToHost, s));
   CK(cudaGetLastError());
   c->launches += 2;
-  if (diff) {
+  // the new values go to c->blocks while the comparison runs (the host
+  // checks and gathers the blocks meanwhile; the copies queue behind it)
+  c->have_W = false;
+  {
+    int rc = upload_blocks(c, nnzb, blocks);
+    if (rc) {
+      cudaStreamSynchronize(s);
+      return rc;
+    }
+  }
+  CK(cudaStreamSynchronize(s));
+  if (*c->diff_h) {
+    // another structure: the full upload (the values again with it)
     if (c->batch_graph) {
       cudaGraphExecDestroy(c->batch_graph);
       c->batch_graph = nullptr;
     }
     return set_W_impl(c, nc, rowptr, colidx, blocks, kind, 0, nullptr);
   }
-  // same structure: new values into the existing layout
-  c->have_W = false;
-  {
-    int rc = upload_blocks(c, nnzb, blocks);
-    if (rc) return rc;
-  }
+  // same structure: the new values into the existing layout
   const long long nw = c->nslots * 9 * FC3D_SLAB;
   k_fill_blocks<<<grid1d(c->npad, 128), 128, 0, s>>>(c->npad, c->perm, c->rowptr, c->colidx, c->blocks, c->iperm,
                                                      c->slab_off, c->W64, c->col, c->D64, c->rho64);
