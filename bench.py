@@ -500,7 +500,7 @@ def run_ours(args):
     achieved = bytes_launch / (sum(fp32_ms) / len(fp32_ms) / 1e3) / 1e9
     peak, peak_kind = _peaks()
     tps = _traffic_per_sweep()
-    roof = {"kernel": "nsgs_flow_kernel<12> (slab-dataflow FP32 sweeps, one persistent launch per step)",
+    roof = {"kernel": "nsgs_flow_kernel<10> (slab-dataflow FP32 sweeps, one persistent launch per step)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": achieved / peak,
             "traffic": (tps * sum(fp32_sweeps) / len(fp32_sweeps)) if tps else None,
