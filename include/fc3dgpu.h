@@ -32,8 +32,11 @@ extern "C" {
 #endif
 
 /* New solver id in the free FC3D range (FrictionContact_options.h:83-131
- * uses 500-530; the driver accepts 500-599, fc3d_driver.c:212). */
+ * uses 500-530; the driver accepts 500-599, fc3d_driver.c:212).  A Siconos
+ * build that lists it in that enum defines FC3DGPU_ID_IN_SICONOS_ENUM. */
+#ifndef FC3DGPU_ID_IN_SICONOS_ENUM
 #define SICONOS_FRICTION_3D_NSGS_GPU 531
+#endif
 
 /* GPU knobs live in option slots the NSGS solver does not use.  dparam
  * 20-22 keep the reference's timing meaning (SolverOptions.h:118-120). */

@@ -125,12 +125,18 @@ typedef struct SolverOptions {
 #define SICONOS_DPARAM_TIME_IN_LOOP 21
 #define SICONOS_DPARAM_TIME_AFTER_LOOP 22
 
-/* fc3d / NSGS indices (FrictionContact_options.h:220-273,
- * NonSmoothGaussSeidel_options.h:50-230) */
+/* fc3d / NSGS indices (FrictionContact_options.h:220-236,
+ * NonSmoothGaussSeidel_options.h:50-100).  The error-evaluation indices are
+ * the ones the reference's compiled solvers use: NonSmoothGaussSeidel_options.h:275-276
+ * and :284 re-map SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION(_FREQUENCY) and
+ * SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO onto the generic NSGS
+ * slots 13, 14 and 11 after FrictionContact_options.h declares them as 7, 8
+ * and 2, so fc3d_nsgs.c, fc2d_nsgs.c and rolling_friction_3d_nsgs.c read
+ * slots 13, 14 (iparam) and 11 (dparam). */
 #define SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY 2
 #define SICONOS_FRICTION_3D_CURRENT_CONTACT_NUMBER 5
-#define SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION 7
-#define SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY 8
+#define SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION 13
+#define SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY 14
 #define SICONOS_FRICTION_3D_NSGS_RELAXATION 10
 #define SICONOS_FRICTION_3D_NSGS_SHUFFLE 11
 #define SICONOS_FRICTION_3D_NSGS_SHUFFLE_SEED 12
@@ -138,7 +144,7 @@ typedef struct SolverOptions {
 #define SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION 16
 #define SICONOS_FRICTION_3D_NSGS_PRINTING_LIKE_IPM 17
 #define SICONOS_FRICTION_3D_NSGS_RELAXATION_VALUE 10
-#define SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO 2
+#define SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO 11
 #define SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL 0
 #define SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT 1
 #define SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL 2

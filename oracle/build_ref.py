@@ -35,6 +35,24 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
 LIB = OUT / "libsiconos_numerics_ref.so"
+# the reference checkout the library was built from (one line), for the
+# tests that compile against its headers
+SOURCE = OUT / "SOURCE"
+ENV = "SICONOS_REFERENCE"
+
+
+def source_dir() -> Path | None:
+    """The reference checkout: ``$SICONOS_REFERENCE``, else the one
+    ``oracle/_ref`` was built from; None when neither names a checkout."""
+    for cand in (os.environ.get(ENV), SOURCE.read_text().strip() if SOURCE.exists() else None):
+        if cand and (Path(cand) / "numerics" / "src").is_dir():
+            return Path(cand)
+    return None
+
+
+def include_flags(ref: Path) -> list[str]:
+    """The include path the reference's sources compile with here."""
+    return _includes(Path(ref))
 
 EXCLUDE_PARTS = ("/test/", "/test-utils/", "/linalg/optional/", "/FrictionContact/parallel/",
                  "/Unstable_or_deprecated/", "/tools/parallel/")
@@ -68,7 +86,7 @@ def _compile(args):
     return src, r.returncode == 0, r.stderr[-400:]
 
 
-def build(ref: str | os.PathLike = "/root/reference", verbose: bool = False) -> Path:
+def build(ref: str | os.PathLike, verbose: bool = False) -> Path:
     ref = Path(ref)
     if not (ref / "numerics" / "src").is_dir():
         raise FileNotFoundError(f"reference numerics sources not found under {ref}")
@@ -109,10 +127,14 @@ def build(ref: str | os.PathLike = "/root/reference", verbose: bool = False) -> 
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle/_ref link failed:\n" + r.stderr[-3000:])
+    SOURCE.write_text(str(ref.resolve()) + "\n")
     if verbose:
         print(f"[oracle/_ref] {len(objs)} objects, {len(failed)} skipped, {len(missing)} stubs -> {LIB}")
     return LIB
 
 
 if __name__ == "__main__":
-    build(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", verbose=True)
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(ENV)
+    if not src:
+        sys.exit(f"usage: python oracle/build_ref.py <reference checkout>  (or set {ENV})")
+    build(src, verbose=True)

@@ -40,7 +40,7 @@ SICONOS_IPARAM_MAX_ITER = 0
 SICONOS_IPARAM_ITER_DONE = 1
 SICONOS_IPARAM_NSGS_SHUFFLE = 5
 SICONOS_DPARAM_TOL = 0
-SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION = 7
+SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION = 13  # the reference's compiled slot (NonSmoothGaussSeidel_options.h:275)
 SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT = 15
 SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL = 0
 SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT = 1

@@ -18,6 +18,7 @@ generator reproduces them bit for bit.
 from __future__ import annotations
 
 import hashlib
+import os
 import sys
 from pathlib import Path
 
@@ -203,4 +204,8 @@ def main(ref_root: str, only: str | None = None):
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     only = next((a[7:] for a in sys.argv[1:] if a.startswith("--only=")), None)
-    main(args[0] if args else "/root/reference", only)
+    src = args[0] if args else os.environ.get("SICONOS_REFERENCE")
+    if not src:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout> [--only=NAME]"
+                 "  (or set SICONOS_REFERENCE)")
+    main(src, only)

@@ -40,8 +40,10 @@ def test_options_mirror_reference_defaults(built_lib):
     ip, dp = o.iparam, o.dparam
     # fc3d_nsgs_set_default (fc3d_nsgs.c:919-950) with registry defaults
     assert ip[0] == 1000 and dp[0] == 1e-4
-    assert ip[7] == 2 and ip[2] == 1 and ip[11] == 0 and ip[15] == 0 and ip[16] == 0 and ip[10] == 0
-    assert dp[2] == 10.0 and ip[17] == 1
+    # error evaluation in slot 13 and the internal error ratio in dparam 11:
+    # the slots the reference's compiled fc3d_nsgs reads (NonSmoothGaussSeidel_options.h:275-284)
+    assert ip[13] == 2 and ip[2] == 1 and ip[11] == 0 and ip[15] == 0 and ip[16] == 0 and ip[10] == 0
+    assert dp[11] == 10.0 and ip[17] == 1 and ip[14] == 0
     loc = o.internalSolvers[0]
     # fc3d_onecontact_nsn_gp_set_default (onecontact.c:1037-1056), registry 100 / 1e-14
     assert loc.solverId == 565

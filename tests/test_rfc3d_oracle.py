@@ -113,7 +113,7 @@ def test_options_defaults(built_lib):
     o = sn.SolverOptions(sn.SICONOS_ROLLING_FRICTION_3D_NSGS_GPU)
     assert o.solverId == 3020
     assert o.iparam[0] == 1000 and o.dparam[0] == 1e-4
-    assert o.iparam[7] == 2 and o.iparam[2] == 1 and o.dparam[2] == 10.0
+    assert o.iparam[13] == 2 and o.iparam[2] == 1 and o.dparam[11] == 10.0
     loc = o.internalSolvers[0]
     assert loc.solverId == sn.SICONOS_ROLLING_FRICTION_3D_ONECONTACT_NSN
     assert loc.iparam[0] == 10 and loc.dparam[0] == 1e-12
