@@ -308,9 +308,15 @@ int fc3dgpu_ctx_get_velocities(fc3dgpu_ctx *ctx, double *vel);
  *
  * Scratch is a fixed device array of FC3DGPU_NOALLOC_SCRATCH_BYTES inside the
  * library; no call allocates or frees memory.  The first call on a device
- * looks the array up (once per device): make it before any stream capture
- * starts.  Calls share the array, so two calls in flight at once on the same
- * device (other streams or host threads) race: order them on one stream.
+ * looks the array up (once per device and CUDA context, normally the
+ * device's primary context; a new context, e.g. after cudaDeviceReset, is
+ * looked up again at its first call): make that call before any stream
+ * capture starts.  Calls share the array, so two calls in flight at once on
+ * the same device (other streams or host threads) race: order them on one
+ * stream.  Every pointer must be memory the current device can use as given
+ * (its own device memory, managed memory, or mapped pinned host memory);
+ * others, including another device's memory, are refused with
+ * NUMERICS_ERR_INVALID_ARGUMENT before any device work.
  * More than FC3DGPU_NOALLOC_MAX_CONTACTS contacts is rejected with
  * NUMERICS_ERR_INVALID_ARGUMENT before any device work. */
 #define FC3DGPU_NOALLOC_MAX_CONTACTS 4194304

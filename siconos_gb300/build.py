@@ -18,6 +18,11 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libfc3dgpu.so"
+# measurement-only comparator (the reference's per-colour 2D GPU design with
+# cuSPARSE): its own library, so the solver library links no cuSPARSE
+COMPARATOR = OUT / "libfc2dpercolour.so"
+COMPARATOR_SOURCE = "fc2dgpu_percolour.cu"
+COMPARATOR_FLAGS = ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c", "rfc3dgpu_nsgs.c", "fc3d_colour.c"]
@@ -29,8 +34,6 @@ CU_SOURCES = {
     "fc2dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # host code computes the rolling solver's rho (Jacobi eigenvalues)
     "rfc3dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
-    # the reference's per-colour design, kept for measurement beside fc2dgpu.cu
-    "fc2dgpu_percolour.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # BF16 tensor-core MLP of the learned warm start
     "fc3dgpu_mlp.cu": [],
     # the FP32 sweeps are the accelerator whose result the FP64 polish
@@ -73,6 +76,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if force or _deps_newer(obj, src):
             jobs.append(["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", *inc, "-c", str(src),
                          "-o", str(obj)])
+    cmp_src, cmp_obj = CSRC / COMPARATOR_SOURCE, OUT / (COMPARATOR_SOURCE + ".o")
+    if force or _deps_newer(cmp_obj, cmp_src):
+        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *COMPARATOR_FLAGS, *inc,
+                     "-c", str(cmp_src), "-o", str(cmp_obj)])
     for s, extra in CU_SOURCES.items():
         src, obj = CSRC / s, OUT / (s + ".o")
         objs.append(obj)
@@ -85,8 +92,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             logs.append(out)
     if jobs or force or not LIB.exists():
         tmp = OUT / (LIB.name + ".tmp")
-        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs], "-lcusparse"])
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o in objs]])
         os.replace(tmp, LIB)
+    if jobs or force or not COMPARATOR.exists():
+        tmp = OUT / (COMPARATOR.name + ".tmp")
+        _run([nvcc, *ARCH, "-shared", "-o", str(tmp), str(cmp_obj), f"-L{OUT}", "-lfc3dgpu", "-lcusparse",
+              "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"])
+        os.replace(tmp, COMPARATOR)
     if verbose:
         for l in logs:
             print(l)

@@ -48,7 +48,7 @@ struct fc3dgpu_dat {
   double *blocks, *q, *mu;
 };
 
-static char g_dat_err[256];
+static _Thread_local char g_dat_err[256];
 const char *fc3dgpu_dat_last_error(void) { return g_dat_err; }
 
 typedef struct {

@@ -729,6 +729,7 @@ struct fc3dgpu_ctx {
   BUF(double, sout64);
   cudaGraphExec_t batch_graph = nullptr;
   fc3dgpu_params batch_graph_params;
+  int batch_grid32 = 0, batch_grid64 = 0;  // resident blocks of the batched kernels, set before capture
   // neighbourhood synchronisation: block neighbour lists per grid size
   struct Nbr {
     int grid = 0;
@@ -2017,7 +2018,7 @@ static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
     b.queue = c->squeue;
     b.scene_out = c->sout32;
     b.scene_out_prev = nullptr;
-    CK(launch_batch_f32(b, s, &g));
+    CK(launch_batch_f32(b, c->batch_grid32, s, &g));
     k_r32_to_r64<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r32, c->rpli32, c->r64, c->rpli64);
   }
   k_batch_budget<<<grid1d(ns), 256, 0, s>>>(ns, c->sout32, p->fp32_only ? 0 : p->max_iter, c->sbudget);
@@ -2044,7 +2045,7 @@ static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
     b.queue = c->squeue + 1;
     b.scene_out = c->sout64;
     b.scene_out_prev = p->precision == 0 ? c->sout32 : nullptr;
-    CK(launch_batch_f64(b, s, &g));
+    CK(launch_batch_f64(b, c->batch_grid64, s, &g));
   }
   return 0;
 }
@@ -2068,8 +2069,8 @@ extern "C" int fc3dgpu_ctx_solve_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p, 
     c->batch_graph = nullptr;
   }
   if (!c->batch_graph) {
-    CK(prepare_batch_f32());
-    CK(prepare_batch_f64());
+    CK(batch_grid_f32(&c->batch_grid32));
+    CK(batch_grid_f64(&c->batch_grid64));
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     int rc = record_batch(c, p);

@@ -140,18 +140,48 @@ __global__ void __launch_bounds__(CHUNK) k_error_noalloc(int nc, long long nnz, 
   }
 }
 
-// per-device address of g_scratch and SM count, looked up once
+// Address of g_scratch and SM count per device, looked up at the first call
+// with that device current.  The address belongs to the CUDA context that was
+// current then (the device's primary context, unless the caller made another
+// driver context current): the entry is keyed by that context and looked up
+// again when another context is current, e.g. after cudaDeviceReset.
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mutex;
-double* g_addr[MAX_DEVICES];
-int g_sms[MAX_DEVICES];
+struct Entry {
+  void* ctx;
+  double* addr;
+  int sms;
+};
+Entry g_entry[MAX_DEVICES];
+typedef int (*CtxGetCurrent)(void**);  // cuCtxGetCurrent, through the runtime
+CtxGetCurrent g_ctx_current = nullptr;
+
+static void* current_context() {
+  void* ctx = nullptr;
+  if (g_ctx_current && g_ctx_current(&ctx) != 0) ctx = nullptr;
+  return ctx;
+}
 
 int setup(int dev, double** addr, int* sms) {
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_addr[dev]) {
+  if (!g_ctx_current) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      cudaGetLastError();
+      fc3dgpu_set_error("fc3dgpu_compute_error_device: cuCtxGetCurrent is not available");
+      return NUMERICS_ERR_NOT_IMPLEMENTED;
+    }
+    g_ctx_current = reinterpret_cast<CtxGetCurrent>(fn);
+  }
+  Entry& en = g_entry[dev];
+  void* ctx = current_context();
+  if (!en.addr || !ctx || ctx != en.ctx) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
     if (e != cudaSuccess || !p) {
+      cudaGetLastError();
       fc3dgpu_set_error("fc3dgpu_compute_error_device: cudaGetSymbolAddress on device %d: %s", dev,
                         cudaGetErrorString(e));
       return NUMERICS_ERR_UNKNOWN;
@@ -159,25 +189,35 @@ int setup(int dev, double** addr, int* sms) {
     int n = 0;
     e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess || n <= 0) {
+      cudaGetLastError();
       fc3dgpu_set_error("fc3dgpu_compute_error_device: SM count of device %d: %s", dev, cudaGetErrorString(e));
       return NUMERICS_ERR_UNKNOWN;
     }
-    g_sms[dev] = n;
-    g_addr[dev] = static_cast<double*>(p);
+    en.ctx = current_context();  // the look-up made the primary context current if none was
+    en.sms = n;
+    en.addr = static_cast<double*>(p);
   }
-  *addr = g_addr[dev];
-  *sms = g_sms[dev];
+  *addr = en.addr;
+  *sms = en.sms;
   return 0;
 }
 
-bool device_accessible(const void* p) {
+// Memory a kernel on device dev may read or write through p as given: device
+// memory of that device (memory of another device is refused, since peer
+// access may be off), managed memory, or mapped pinned host memory whose
+// device address is p itself.
+bool device_accessible(const void* p, int dev) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged ||
-         (at.type == cudaMemoryTypeHost && at.devicePointer != nullptr);
+  switch (at.type) {
+    case cudaMemoryTypeDevice: return at.device == dev;
+    case cudaMemoryTypeManaged: return true;
+    case cudaMemoryTypeHost: return at.devicePointer == p;
+    default: return false;
+  }
 }
 
 }  // namespace noalloc
@@ -216,8 +256,8 @@ extern "C" int fc3dgpu_compute_error_device(int nc, int64_t nnz, const int64_t* 
   }
   const void* ptrs[] = {rowptr, colidx, blocks, q, mu, reaction, velocity, error};
   for (const void* p : ptrs)
-    if (p && !device_accessible(p)) {
-      fc3dgpu_set_error("fc3dgpu_compute_error_device: %p is not memory the device can access", p);
+    if (p && !device_accessible(p, dev)) {
+      fc3dgpu_set_error("fc3dgpu_compute_error_device: %p is not memory device %d can access", p, dev);
       return NUMERICS_ERR_INVALID_ARGUMENT;
     }
   double* scratch = nullptr;

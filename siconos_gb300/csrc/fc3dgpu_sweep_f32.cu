@@ -7,28 +7,23 @@
 namespace fc3dgpu {
 void warm_sweep_kernels_f64();
 
+// The grid is queried at every launch (a few microseconds of host work
+// against a solve of milliseconds): no launch state is kept between calls, so
+// contexts on different host threads and devices never share any.
 template <int T>
 static cudaError_t launch_t(const SweepArgs<float>& a, int max_grid, size_t smem, cudaStream_t s, int* grid) {
   auto kern = nsgs_kernel<float, T>;
-  static int cached_dev = -1, cached_g = 0;
-  static size_t cached_smem = 0;
-  int dev = 0;
+  int dev = 0, nsm = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (cached_dev != dev || cached_smem != smem) {
-    int nsm = 0, per_sm = 0;
-    e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<float>::value, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    cached_g = nsm * per_sm;
-    cached_dev = dev;
-    cached_smem = smem;
-  }
-  int g = cached_g;
+  e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<float>::value, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int g = nsm * per_sm;
   if (max_grid > 0 && g > max_grid) g = max_grid;
   if (g > 1024) g = 1024;
   *grid = g;
@@ -130,45 +125,28 @@ cudaError_t build_flow_deps(int nslab, int npad, int ncol, const int* sptr_d, co
   return cudaGetLastError();
 }
 
-static int batch_cached_dev_f32 = -1, batch_cached_g_f32 = 0;
-
-// Occupancy of the batched kernel, queried outside any stream capture.
-cudaError_t prepare_batch_f32() {
+// Resident blocks of the batched kernel on the current device, queried
+// outside any stream capture; the caller keeps the figure with its context.
+cudaError_t batch_grid_f32(int* grid) {
   auto kern = nsgs_batch_kernel<float>;
   int dev = 0, nsm = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (batch_cached_dev_f32 == dev) return cudaSuccess;
   e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<float>::value, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  batch_cached_g_f32 = nsm * per_sm;
-  batch_cached_dev_f32 = dev;
+  *grid = nsm * per_sm;
   return cudaSuccess;
 }
 
-cudaError_t launch_batch_f32(const BatchArgs<float>& b, cudaStream_t s, int* grid) {
-  auto kern = nsgs_batch_kernel<float>;
-  int& cached_dev = batch_cached_dev_f32;
-  int& cached_g = batch_cached_g_f32;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (cached_dev != dev) {
-    int nsm = 0, per_sm = 0;
-    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<float>::value, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    cached_g = nsm * per_sm;
-    cached_dev = dev;
-  }
-  int g = cached_g < b.nscenes ? cached_g : b.nscenes;
+// One block per problem, at most max_grid (batch_grid_f32) resident blocks.
+cudaError_t launch_batch_f32(const BatchArgs<float>& b, int max_grid, cudaStream_t s, int* grid) {
+  if (max_grid < 1) return cudaErrorInvalidConfiguration;
+  const int g = max_grid < b.nscenes ? max_grid : b.nscenes;
   *grid = g;
-  kern<<<g, BlockDim<float>::value, 0, s>>>(b);
+  nsgs_batch_kernel<float><<<g, BlockDim<float>::value, 0, s>>>(b);
   return cudaGetLastError();
 }
 

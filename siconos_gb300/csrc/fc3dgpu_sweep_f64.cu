@@ -5,28 +5,23 @@
 
 namespace fc3dgpu {
 
+// The grid is queried at every launch (a few microseconds of host work
+// against a solve of milliseconds): no launch state is kept between calls, so
+// contexts on different host threads and devices never share any.
 template <int T>
 static cudaError_t launch_t(const SweepArgs<double>& a, int max_grid, size_t smem, cudaStream_t s, int* grid) {
   auto kern = nsgs_kernel<double, T>;
-  static int cached_dev = -1, cached_g = 0;
-  static size_t cached_smem = 0;
-  int dev = 0;
+  int dev = 0, nsm = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (cached_dev != dev || cached_smem != smem) {
-    int nsm = 0, per_sm = 0;
-    e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<double>::value, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    cached_g = nsm * per_sm;
-    cached_dev = dev;
-    cached_smem = smem;
-  }
-  int g = cached_g;
+  e = cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<double>::value, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int g = nsm * per_sm;
   if (max_grid > 0 && g > max_grid) g = max_grid;
   if (g > 1024) g = 1024;
   *grid = g;
@@ -72,45 +67,28 @@ int sweep_grid_f64(int lanes) {
   }
 }
 
-static int batch_cached_dev_f64 = -1, batch_cached_g_f64 = 0;
-
-// Occupancy of the batched kernel, queried outside any stream capture.
-cudaError_t prepare_batch_f64() {
+// Resident blocks of the batched kernel on the current device, queried
+// outside any stream capture; the caller keeps the figure with its context.
+cudaError_t batch_grid_f64(int* grid) {
   auto kern = nsgs_batch_kernel<double>;
   int dev = 0, nsm = 0, per_sm = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (batch_cached_dev_f64 == dev) return cudaSuccess;
   e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<double>::value, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  batch_cached_g_f64 = nsm * per_sm;
-  batch_cached_dev_f64 = dev;
+  *grid = nsm * per_sm;
   return cudaSuccess;
 }
 
-cudaError_t launch_batch_f64(const BatchArgs<double>& b, cudaStream_t s, int* grid) {
-  auto kern = nsgs_batch_kernel<double>;
-  int& cached_dev = batch_cached_dev_f64;
-  int& cached_g = batch_cached_g_f64;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (cached_dev != dev) {
-    int nsm = 0, per_sm = 0;
-    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BlockDim<double>::value, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    cached_g = nsm * per_sm;
-    cached_dev = dev;
-  }
-  int g = cached_g < b.nscenes ? cached_g : b.nscenes;
+// One block per problem, at most max_grid (batch_grid_f64) resident blocks.
+cudaError_t launch_batch_f64(const BatchArgs<double>& b, int max_grid, cudaStream_t s, int* grid) {
+  if (max_grid < 1) return cudaErrorInvalidConfiguration;
+  const int g = max_grid < b.nscenes ? max_grid : b.nscenes;
   *grid = g;
-  kern<<<g, BlockDim<double>::value, 0, s>>>(b);
+  nsgs_batch_kernel<double><<<g, BlockDim<double>::value, 0, s>>>(b);
   return cudaGetLastError();
 }
 

@@ -19,11 +19,13 @@ int sweep_grid_f32(int lanes);
 void warm_sweep_kernels();
 template <typename Real>
 struct BatchArgs;
-cudaError_t launch_batch_f32(const BatchArgs<float>& b, cudaStream_t s, int* grid);
-cudaError_t launch_batch_f64(const BatchArgs<double>& b, cudaStream_t s, int* grid);
+// Batched kernel: resident blocks on the current device (query outside any
+// stream capture), and the launch of min(max_grid, problems) blocks.
+cudaError_t batch_grid_f32(int* grid);
+cudaError_t batch_grid_f64(int* grid);
+cudaError_t launch_batch_f32(const BatchArgs<float>& b, int max_grid, cudaStream_t s, int* grid);
+cudaError_t launch_batch_f64(const BatchArgs<double>& b, int max_grid, cudaStream_t s, int* grid);
 void warm_batch_kernel_f32();
-cudaError_t prepare_batch_f32();
-cudaError_t prepare_batch_f64();
 void warm_batch_kernel_f64();
 int sweep_grid_f64(int lanes);
 // Slab-dataflow FP32 sweep: warps per block for slabs of up to maxslot

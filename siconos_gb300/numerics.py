@@ -278,12 +278,36 @@ ABI = {
     "rfc3dgpu_ctx_rho": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rfc3dgpu_ctx_set_precision": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
     "rfc3dgpu_ctx_last_sweeps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+# the per-colour comparator (include/fc2dgpu_percolour.h): a separate,
+# measurement-only library; the solver library does not link cuSPARSE
+COMPARATOR_ABI = {
     "fc2dgpu_percolour_create": (C.c_void_p, [C.c_int, C.c_int, _I64, _I64, _F64, _F64, _F64, C.c_int]),
     "fc2dgpu_percolour_destroy": (None, [C.c_void_p]),
     "fc2dgpu_percolour_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int), _DP,
                                           C.POINTER(C.c_int), _DP]),
     "fc2dgpu_percolour_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
 }
+_comparator = None
+
+
+def comparator_lib():
+    """The loaded ``libfc2dpercolour.so`` (the reference's per-colour 2D GPU
+    design, for measurement beside the solver)."""
+    global _comparator
+    if _comparator is None:
+        lib()  # resolves its dependency on libfc3dgpu.so
+        path = LIB_PATH.parent / "libfc2dpercolour.so"
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing: build it with siconos_gb300.build.build()")
+        L = C.CDLL(str(path))
+        for name, (res, args) in COMPARATOR_ABI.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _comparator = L
+    return _comparator
 
 
 def lib():
@@ -825,7 +849,7 @@ class Fc2dPerColour:
 
     def __init__(self, nc, rowptr, colidx, blocks, q, mu, colouring: int = 0, device: int = 0):
         self.nc = int(nc)
-        self.h = lib().fc2dgpu_percolour_create(device, self.nc, np.ascontiguousarray(rowptr, np.int64),
+        self.h = comparator_lib().fc2dgpu_percolour_create(device, self.nc, np.ascontiguousarray(rowptr, np.int64),
                                                 np.ascontiguousarray(colidx, np.int64),
                                                 np.ascontiguousarray(blocks, np.float64).reshape(-1),
                                                 np.ascontiguousarray(q, np.float64),
@@ -837,18 +861,18 @@ class Fc2dPerColour:
         it, info = C.c_int(), C.c_int()
         err, ms = C.c_double(), C.c_double()
         r0p = None if r0 is None else np.ascontiguousarray(r0, np.float64)
-        _check(lib().fc2dgpu_percolour_solve(self.h, None if r0p is None else r0p.ctypes.data, tol, max_iter,
+        _check(comparator_lib().fc2dgpu_percolour_solve(self.h, None if r0p is None else r0p.ctypes.data, tol, max_iter,
                                              C.byref(it), C.byref(err), C.byref(info), C.byref(ms)))
         return dict(iterations=it.value, error=err.value, info=info.value, ms=ms.value)
 
     def get_r_u(self):
         r, u = np.zeros(2 * self.nc), np.zeros(2 * self.nc)
-        _check(lib().fc2dgpu_percolour_get_r_u(self.h, r.ctypes.data, u.ctypes.data))
+        _check(comparator_lib().fc2dgpu_percolour_get_r_u(self.h, r.ctypes.data, u.ctypes.data))
         return r, u
 
     def close(self):
         if getattr(self, "h", None):
-            lib().fc2dgpu_percolour_destroy(self.h)
+            comparator_lib().fc2dgpu_percolour_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -11,9 +11,13 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def declared_functions():
+def declared_functions(comparator=False):
+    """Functions include/*.h declares: the solver library's, or (comparator)
+    those of the measurement-only per-colour library."""
     names = set()
     for h in (ROOT / "include").glob("*.h"):
+        if (h.name == "fc2dgpu_percolour.h") != comparator:
+            continue
         text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
         for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:fc[23]|rfc3)dgpu_\w+)\s*\(", text, flags=re.M):
             names.add(m.group(1))
@@ -24,14 +28,31 @@ def test_headers_declare_entry_points():
     names = declared_functions()
     for must in ["fc3dgpu_nsgs", "fc3dgpu_nsgs_set_default", "fc3dgpu_nsgs_batch", "fc3dgpu_compute_error",
                  "fc3dgpu_driver", "fc3dgpu_colour", "fc3dgpu_ctx_solve", "fc3dgpu_lattice_create",
-                 "fc2dgpu_nsgs", "fc2dgpu_driver", "fc2dgpu_ctx_solve", "fc2dgpu_percolour_solve",
+                 "fc2dgpu_nsgs", "fc2dgpu_driver", "fc2dgpu_ctx_solve",
                  "rfc3dgpu_nsgs", "rfc3dgpu_driver", "rfc3dgpu_ctx_solve"]:
         assert must in names
+    assert "fc2dgpu_percolour_solve" in declared_functions(comparator=True)
 
 
 @pytest.mark.parametrize("name", declared_functions())
 def test_library_exports(built_lib, name):
     assert hasattr(built_lib, name), name
+
+
+@pytest.mark.parametrize("name", declared_functions(comparator=True))
+def test_comparator_library_exports(built_lib, name):
+    import siconos_gb300.numerics as sn
+    assert hasattr(sn.comparator_lib(), name), name
+
+
+def test_solver_library_links_no_cusparse(built_lib):
+    """The solver library has no library GEMM/SpMV backend: cuSPARSE is
+    linked only into the measurement-only comparator."""
+    import subprocess
+    from siconos_gb300 import build as B
+    dyn = subprocess.run(["readelf", "-d", str(B.LIB)], capture_output=True, text=True).stdout
+    assert "cusparse" not in dyn
+    assert "cusparse" in subprocess.run(["readelf", "-d", str(B.COMPARATOR)], capture_output=True, text=True).stdout
 
 
 def test_options_mirror_reference_defaults(built_lib):
