@@ -97,6 +97,13 @@ def port():
         lib.oracle_projection_on_cone.argtypes = [_F64, C.c_double]
         lib.oracle_local_solve.restype = C.c_double
         lib.oracle_local_solve.argtypes = [_F64, _F64, C.c_double, _F64, _F64, C.c_double]
+        lib.fc3dgpu_lattice_create.restype = C.c_void_p
+        lib.fc3dgpu_lattice_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_double, C.c_double]
+        lib.fc3dgpu_lattice_free.argtypes = [C.c_void_p]
+        lib.fc3dgpu_lattice_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                              C.POINTER(C.c_int64)]
+        lib.fc3dgpu_lattice_fill_W.argtypes = [C.c_void_p, _I64, _I64, _F64]
+        lib.fc3dgpu_lattice_fill_q.argtypes = [C.c_void_p, C.c_double, _F64]
         if hasattr(lib, "oracle_colour_greedy"):
             lib.oracle_colour_greedy.restype = C.c_int
             lib.oracle_colour_greedy.argtypes = [C.c_int, _I64, _I64, C.c_int, _I32]
@@ -106,6 +113,31 @@ def port():
             lib.oracle_colour_priority.argtypes = [C.c_uint32, C.c_int, C.c_uint32]
         _port = lib
     return _port
+
+
+def lattice(nx: int, ny: int, nz: int, seed: int = 1, mu: float = 0.5, jitter_std: float = 1e-3,
+            v0_std: float = 0.1, h: float = 1e-3) -> Problem:
+    """The seeded sphere-lattice scene as a Problem, from the generator
+    compiled into the oracle library (the same source and results as
+    ``siconos_gb300.scene.lattice``), for CPU-only measurements that must not
+    load the solver library."""
+    L = port()
+    hdl = L.fc3dgpu_lattice_create(nx, ny, nz, seed, jitter_std, v0_std)
+    if not hdl:
+        raise ValueError("bad lattice size")
+    try:
+        nb, nc, nnzb = C.c_int(), C.c_int(), C.c_int64()
+        L.fc3dgpu_lattice_sizes(hdl, C.byref(nb), C.byref(nc), C.byref(nnzb))
+        n, k = nc.value, nnzb.value
+        rp = np.zeros(n + 1, np.int64)
+        ci = np.zeros(k, np.int64)
+        bl = np.zeros(9 * k)
+        q = np.zeros(3 * n)
+        L.fc3dgpu_lattice_fill_W(hdl, rp, ci, bl)
+        L.fc3dgpu_lattice_fill_q(hdl, h, q)
+    finally:
+        L.fc3dgpu_lattice_free(hdl)
+    return Problem(n, rp, ci, bl.reshape(k, 9), q, np.full(n, float(mu)))
 
 
 def ref_available() -> bool:

@@ -10,7 +10,7 @@ Recipe (nothing is copied out of the reference tree):
 
 1. compile every ``numerics/src/**/*.c`` except tests, optional linear-algebra
    back-ends, the OpenMP/PETSc/CUDA ``FrictionContact/parallel`` solvers and
-   ``Unstable_or_deprecated`` with ``gcc -std=gnu11 -O2 -DCS_LONG -DNCOMPLEX``,
+   ``Unstable_or_deprecated`` with ``gcc -std=gnu11 -O3 -DCS_LONG -DNCOMPLEX``,
    against the reference's own headers plus the self-written stand-ins in
    ``oracle/include`` (cs.h, cblas.h, openblas_config.h, lapacke.h);
 2. compile ``oracle/ref_shim.c`` (naive CBLAS loops) and
@@ -56,7 +56,7 @@ def include_flags(ref: Path) -> list[str]:
 
 EXCLUDE_PARTS = ("/test/", "/test-utils/", "/linalg/optional/", "/FrictionContact/parallel/",
                  "/Unstable_or_deprecated/", "/tools/parallel/")
-CFLAGS = ["-std=gnu11", "-O2", "-fPIC", "-DCS_LONG", "-DNCOMPLEX", "-ffp-contract=off", "-w"]
+CFLAGS = ["-std=gnu11", "-O3", "-fPIC", "-DCS_LONG", "-DNCOMPLEX", "-ffp-contract=off", "-w"]
 
 
 def _sources(ref: Path) -> list[Path]:

@@ -3,7 +3,7 @@
 Run in a checkout that has the reference sources (the library in
 ``oracle/_ref`` is built from them by ``oracle/build_ref.py``):
 
-    python tests/golden/make_golden.py /path/to/reference [--only=fc2d|rfc3d]
+    python tests/golden/make_golden.py /path/to/reference [--only=fc2d|rfc3d|to_tolerance]
 
 For each SBM/dense friction-contact fixture of the reference's own test data
 (numerics/src/FrictionContact/test/data) and for the 5x5x6 lattice scene,
@@ -139,6 +139,26 @@ def make_rfc3d(data: Path):
         print(f"{f}: nc={P.nc} nnzb={P.nnzb} info={full.info} it={full.iterations} err={full.error:.3e}")
 
 
+def make_to_tolerance():
+    """The reference's own fc3d_nsgs (oracle/_ref) on the 60x60x30 lattice
+    (seed 1, mu 0.5) from r = 0 to 1e-3 and to 1e-4 (defaults, budget
+    10000): info, sweeps, final error and the whole error trace.  Too slow
+    for a test to recompute (about a minute per tolerance on one core); the
+    benchmark reads the sweep counts as the reference's side of the time to
+    tolerance."""
+    import json
+
+    import oracle as O
+    P = O.lattice(60, 60, 30, seed=1, mu=0.5)
+    out = {"scene": "lattice 60x60x30, seed 1, mu 0.5", "nc": P.nc, "nnzb": P.nnzb, "source": "oracle/_ref"}
+    for tol in (1e-3, 1e-4):
+        res = O.nsgs_ref(P, tol=tol, maxiter=10000, trace_cap=10000)
+        out[f"{tol:g}"] = {"info": res.info, "iterations": res.iterations, "error": res.error,
+                           "trace": [float(x) for x in res.trace[:res.iterations]]}
+        print(f"to {tol:g}: info={res.info} it={res.iterations} err={res.error:.3e}")
+    (HERE / "lattice_60x60x30_s1_to_tolerance.json").write_text(json.dumps(out) + "\n")
+
+
 def main(ref_root: str, only: str | None = None):
     from oracle import build_ref
     import oracle as O
@@ -147,6 +167,9 @@ def main(ref_root: str, only: str | None = None):
     data = Path(ref_root) / "numerics" / "src" / "FrictionContact" / "test" / "data"
     if only == "rfc3d":
         make_rfc3d(Path(ref_root) / "numerics" / "src" / "RollingFrictionContact" / "test" / "data")
+        return
+    if only == "to_tolerance":
+        make_to_tolerance()
         return
     if only == "fc2d":
         from siconos_gb300 import build as B

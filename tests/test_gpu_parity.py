@@ -428,3 +428,49 @@ def test_wait_timeout_is_an_error_and_the_context_recovers(gpu, flow):
     finally:
         gpu.flow(prev)
         gpu.spin_limit(0)
+
+
+def test_c2_fp64_sweeps_bit_exact_vs_coloured_oracle(gpu):
+    """At the benchmark's scale (60x60x30, 320,400 contacts): 20 FP64 sweeps
+    on the GPU reproduce the oracle's sequential sweep run in the same colour
+    order bit for bit (r), with the same light-error trace up to the order of
+    its sums and the same final fc3d_compute_error."""
+    P = O.lattice(60, 60, 30, seed=1, mu=0.5)
+    gpu.set_W(P.nc, P.rowptr, P.colidx, P.blocks)
+    gpu.set_q_mu(P.q, P.mu)
+    gpu.set_r(np.zeros(3 * P.nc))
+    st = gpu.solve(tol=1e-300, max_iter=20, precision=1, lanes=1)
+    r, u = gpu.get()
+    tr = gpu.trace(20)
+    ref = O.nsgs_port(P, tol=1e-300, maxiter=20, order=_colour_order(gpu.colours()), trace_cap=20)
+    assert st["sweeps64"] == 20 and ref.iterations == 20
+    assert np.array_equal(r, ref.r), np.abs(r - ref.r).max()
+    np.testing.assert_allclose(tr, ref.trace[:20], rtol=1e-12, atol=0)
+    assert abs(st["error"] - ref.error) <= 1e-12 * ref.error
+    assert np.allclose(u, ref.u, rtol=0, atol=1e-13 * (1 + np.abs(ref.u).max()))
+
+
+@pytest.mark.parametrize("case", CONVERGING + ["fixture_RockPile_tob1"])
+def test_fp64_tolerance_manager_matches_coloured_oracle(gpu, case):
+    """A whole FP64 solve at tol 1e-8 against the oracle in colour order:
+    the device-side tolerance manager (fc3d_nsgs.c:496-558: full error when
+    the light error falls below the working tolerance, the working tolerance
+    adapted from incr/full, the final full error, the strict `<`) takes the
+    oracle's decisions: same info, same sweep count, the same light-error
+    trace (up to the order of its sums), the same reaction bit for bit and
+    the same final error.  RockPile does not converge: 2000 sweeps, info -20."""
+    P, _ = load_case(case)
+    maxiter = 2000 if case == "fixture_RockPile_tob1" else 10000
+    gpu.set_W(P.nc, P.rowptr, P.colidx, P.blocks)
+    gpu.set_q_mu(P.q, P.mu)
+    gpu.set_r(np.zeros(3 * P.nc))
+    st = gpu.solve(tol=1e-8, max_iter=maxiter, precision=1, lanes=1)
+    r, _ = gpu.get()
+    ref = O.nsgs_port(P, tol=1e-8, maxiter=maxiter, order=_colour_order(gpu.colours()), trace_cap=maxiter)
+    assert st["info"] == ref.info, (st, ref.info, ref.iterations)
+    assert st["sweeps64"] == ref.iterations and st["sweeps32"] == 0
+    tr = gpu.trace(maxiter)
+    assert len(tr) == ref.iterations
+    np.testing.assert_allclose(tr, ref.trace[:ref.iterations], rtol=1e-12, atol=0)
+    assert np.array_equal(r, ref.r), np.abs(r - ref.r).max()
+    assert abs(st["error"] - ref.error) <= 1e-12 * max(ref.error, 1e-300)
