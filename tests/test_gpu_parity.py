@@ -474,3 +474,38 @@ def test_fp64_tolerance_manager_matches_coloured_oracle(gpu, case):
     np.testing.assert_allclose(tr, ref.trace[:ref.iterations], rtol=1e-12, atol=0)
     assert np.array_equal(r, ref.r), np.abs(r - ref.r).max()
     assert abs(st["error"] - ref.error) <= 1e-12 * max(ref.error, 1e-300)
+
+
+# Bounds for the FP32 dataflow sweep against the FP64 oracle after the same k
+# sweeps in the same colour order.  The FP32 sweep stops each one-contact
+# Newton at a relative local error of 1e-5 (FP64: 1e-14) and rounds to FP32
+# (6e-8), so every sweep moves each reaction by up to about 1e-5 relative
+# from the FP64 sweep's; Gauss-Seidel does not amplify such perturbations
+# (measured on GB300: at most 2.3e-5 relative in r and 1.2e-4 in the error
+# over 100 sweeps on the lattices below).  The bounds leave 4x-8x margin.
+FP32_R_BOUND = 1e-4
+FP32_ERR_BOUND = 1e-3
+
+
+@pytest.mark.parametrize("dims", [(5, 5, 6), (60, 60, 30)])
+def test_fp32_flow_tracks_fp64_oracle(gpu, dims):
+    """The benchmarked kernel (slab-dataflow FP32 sweeps) after k = 10, 50,
+    100 sweeps from r = 0, against the colour-ordered FP64 oracle after k
+    sweeps: the reactions within FP32_R_BOUND (relative 2-norm) and the FP64
+    fc3d_compute_error of the FP32 iterate within FP32_ERR_BOUND of the
+    oracle's (relative)."""
+    P = O.lattice(*dims, seed=1, mu=0.5)
+    gpu.set_W(P.nc, P.rowptr, P.colidx, P.blocks)
+    gpu.set_q_mu(P.q, P.mu)
+    gpu.set_r(np.zeros(3 * P.nc))
+    gpu.flow(True)  # the benchmarked kernel (the default)
+    order = _colour_order(gpu.colours())
+    for k in (10, 50, 100):
+        gpu.zero_r()
+        st = gpu.solve(tol=1e-300, max_iter=k, fp32_only=1, switch_tol=0.0, stall_window=0)
+        assert st["status"] == 0 and st["sweeps32"] == k and st["lanes"] == 1
+        r32, _ = gpu.get()
+        ref = O.nsgs_port(P, tol=1e-300, maxiter=k, order=order)
+        e32, _ = O.compute_error_port(P, r32)
+        assert np.linalg.norm(r32 - ref.r) <= FP32_R_BOUND * np.linalg.norm(ref.r), k
+        assert abs(e32 - ref.error) <= FP32_ERR_BOUND * ref.error, (k, e32, ref.error)
