@@ -141,7 +141,12 @@ typedef struct fc3dgpu_ctx fc3dgpu_ctx;
 typedef struct {
   double tol;          /* user tolerance on fc3d_compute_error */
   int max_iter;        /* total sweep budget */
-  int precision;       /* 0 mixed (FP32 sweeps + FP64 polish), 1 FP64 only */
+  int precision;       /* 0 mixed (FP32 sweeps + FP64 polish), 1 FP64 only,
+                          2 mixed with the fast FP64 polish, 3 fast FP64 only
+                          (fast: the one-contact solver's FP64 divisions and
+                          square roots refined from FP32 seeds, about 1e-14
+                          relative; the error that decides convergence stays
+                          exact FP64) */
   int lanes;           /* lanes per contact (1,2,4,8); 0 = autotune */
   double switch_tol;   /* FP32 phase ends when incr error < switch_tol ... */
   int stall_window;    /* ... or has not improved for this many sweeps */
@@ -151,6 +156,8 @@ typedef struct {
   int pli_max;         /* 100 */
   int ls_max;          /* 10 */
   int fp32_only;       /* 1: run FP32 sweeps only, for throughput runs */
+  int local_mode32;    /* FP32 one-contact solver: 0 the reference's hybrid
+                          (default), 1 damped Newton alone */
 } fc3dgpu_params;
 
 typedef struct {
@@ -242,6 +249,26 @@ int fc3dgpu_ctx_sync(fc3dgpu_ctx *ctx, int neighbourhood);
  * either way.  Applies with one lane per contact when no slab has more
  * than 16 off-diagonal slots.  Returns the previous setting. */
 int fc3dgpu_ctx_flow(fc3dgpu_ctx *ctx, int on);
+/* Warps per block of the dataflow sweep: 8, 10 or 12 (0: the default, 10,
+ * or the autotuner's choice); fewer when the per-warp buffers of the current
+ * layout do not fit.  Returns the previous request. */
+int fc3dgpu_ctx_flow_warps(fc3dgpu_ctx *ctx, int nw);
+/* Measuring autotuner of the sweep variant, run at the first solve of a new
+ * structure with automatic lanes (fc3dgpu_params.lanes = 0): it times a few
+ * sweeps of each candidate from the current reaction (restored afterwards)
+ * and keeps the fastest for the structure.  mode 1 (default): only variants
+ * with the same iterates bit for bit (the dataflow sweep with 8, 10 or 12
+ * warps a block, the coloured kernel with one lane per contact; FP64 sweeps
+ * keep one lane per contact, the oracle's iterates); mode 2: also 2, 4 and
+ * 8 lanes per contact in both precisions (other summation orders); mode 0:
+ * off.  Returns the previous mode. */
+int fc3dgpu_ctx_autotune(fc3dgpu_ctx *ctx, int mode);
+/* The autotuner's choice for the current structure: choice4 = {dataflow
+ * sweep (0/1), its warps a block, FP32 lanes, FP64 lanes}; ms11 = device time
+ * of one sweep of each candidate (FP32: dataflow 8, 10, 12 warps, coloured
+ * 1, 2, 4, 8 lanes; FP64: 1, 2, 4, 8 lanes; infinity when not run).  Returns
+ * 1 when the structure is not tuned yet, 0 otherwise. */
+int fc3dgpu_ctx_tuning(fc3dgpu_ctx *ctx, int *choice4, float *ms11);
 /* Polls before a barrier, slab-counter or bulk-copy wait of the sweep
  * kernels gives up (0: the default 2^22, seconds); the kernel then records
  * FC3DGPU_STATUS_BARRIER_TIMEOUT, every block leaves (each after its own

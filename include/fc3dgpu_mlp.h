@@ -62,6 +62,13 @@ int fc3dgpu_mlp_infer(fc3dgpu_mlp *m, size_t n, const float *X, float *Y, int on
 /* Device arrays, on `stream` (cudaStream_t) instead of the model's stream. */
 int fc3dgpu_mlp_infer_stream(fc3dgpu_mlp *m, size_t n, const float *X, float *Y, void *stream);
 
+/* Matrix products on the Blackwell tensor cores (tcgen05.mma with TMEM
+ * accumulators, 128 samples per block; tcgen05 != 0, the default) or on the
+ * warp-level mma.sync path (64 samples per block), the checked reference.
+ * Same network, same BF16 operands and FP32 accumulation; the two differ
+ * in the order of the FP32 sums only.  Returns the previous setting. */
+int fc3dgpu_mlp_set_tensor_path(fc3dgpu_mlp *m, int tcgen05);
+
 /* Learned warm start of a device context.  The reaction currently in the
  * context (the previous step's, or what fc3dgpu_ctx_set_r gave) is the
  * fallback.  Features are formed on the device (gap: host array of nc

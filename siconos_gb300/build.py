@@ -29,6 +29,8 @@ C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c",
 CU_SOURCES = {
     "fc3dgpu_ctx.cu": ["--fmad=false"],
     "fc3dgpu_sweep_f64.cu": ["--fmad=false"],
+    # the same FP64 kernels with the fast one-contact arithmetic (opt-in)
+    "fc3dgpu_sweep_f64fast.cu": ["--fmad=false"],
     "fc3dgpu_noalloc.cu": ["--fmad=false"],
     # host code computes determinants and norms the kernel reuses
     "fc2dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],

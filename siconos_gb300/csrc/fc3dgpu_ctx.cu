@@ -16,6 +16,7 @@
 
 #include "fc3dgpu_batch_args.cuh"
 #include "fc3dgpu_sweep_launch.h"
+#include "fc3dgpu_fast64.h"
 #include "fc3dgpu_layout.cuh"
 #include "fc3dgpu_local.cuh"
 #include "fc3dgpu_mlp.h"
@@ -705,6 +706,16 @@ struct fc3dgpu_ctx {
   int flow_on = 1;
   int flow_state = 0;
   int flow_nw = 0, flow_maxslot = 0;
+  int flow_want = 0;  // warps per block of the dataflow sweep asked for (0: default)
+  // measuring autotuner (per layout): chosen FP32 variant and FP64 lanes,
+  // and the measured device time of one sweep of every candidate
+  int tuned = 0;          // 0: not yet for this layout
+  int tune_mode = 1;      // 0 off, 1 result-preserving variants only, 2 every variant
+  int tune_flow = 0, tune_nw = 0, tune_lanes32 = 1, tune_lanes64 = 1;
+  float tune_ms32[7] = {0}, tune_ms64[4] = {0};
+  BUF(double, tune_r64);
+  BUF(double, tune_rpli64);
+  BUF(float, tune_rpli32);
   BUF(int, flow_dptr);
   BUF(int, flow_dep);
   BUF(unsigned, flow_done);
@@ -729,7 +740,8 @@ struct fc3dgpu_ctx {
   BUF(double, sout64);
   cudaGraphExec_t batch_graph = nullptr;
   fc3dgpu_params batch_graph_params;
-  int batch_grid32 = 0, batch_grid64 = 0;  // resident blocks of the batched kernels, set before capture
+  // resident blocks of the batched kernels (FP32, FP64, fast FP64), set before capture
+  int batch_grid32 = 0, batch_grid64 = 0, batch_grid64f = 0;
   // neighbourhood synchronisation: block neighbour lists per grid size
   struct Nbr {
     int grid = 0;
@@ -799,6 +811,7 @@ extern "C" void fc3dgpu_params_default(fc3dgpu_params* p) {
   p->newton_max = 100;
   p->pli_max = 100;
   p->ls_max = 10;
+  p->local_mode32 = 0;
   p->fp32_only = 0;
 }
 
@@ -1283,6 +1296,7 @@ static int build_layout(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, int ns
   c->colour_kind = kind;
   for (auto& n : c->nbrc) n.grid = 0;  // the rows' owners changed
   c->flow_state = 0;
+  c->tuned = 0;
   return 0;
 }
 
@@ -1455,6 +1469,22 @@ extern "C" int fc3dgpu_ctx_flow(fc3dgpu_ctx* c, int on) {
   return old;
 }
 
+extern "C" int fc3dgpu_ctx_flow_warps(fc3dgpu_ctx* c, int nw) {
+  if (!c) return -1;
+  if (nw != 0 && nw != 8 && nw != 10 && nw != 12) {
+    fc3dgpu_set_error("fc3dgpu_ctx_flow_warps: 8, 10 or 12 warps per block (0: default)");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  const int old = c->flow_want;
+  c->flow_want = nw;
+  if (c->flow_state == 1) {
+    if (cudaSetDevice(c->device) != cudaSuccess) return NUMERICS_ERR_UNKNOWN;
+    const int got = fc3dgpu::flow_warps(c->flow_maxslot, nw);
+    if (got > 0) c->flow_nw = got;
+  }
+  return old;
+}
+
 // Polls before a barrier, slab-counter or bulk-copy wait of the sweep
 // kernels gives up (0: the default 2^22); a wait that gives up sets
 // FC3DGPU_STATUS_BARRIER_TIMEOUT and the solve returns an error.  Returns
@@ -1561,6 +1591,7 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.nbr_ptr = nullptr;
   a.nbr = nullptr;
   a.nbr_grid = 0;
+  a.local_mode = 0;
 }
 
 // Neighbour lists of every block for a sweep over `grid` blocks (one lane
@@ -1662,7 +1693,7 @@ static int prepare_flow(fc3dgpu_ctx* c) {
   int maxslot = 0;
   for (int s = 0; s < c->nslab; s++) maxslot = std::max(maxslot, c->slab_nslot_h[s]);
   if (maxslot > FC3D_FLOW_MAXSLOT) return 0;
-  const int nw = flow_warps(maxslot);
+  const int nw = flow_warps(maxslot, c->flow_want);
   if (nw == 0) return 0;
   cudaStream_t s = c->stream;
   const int nslab = c->nslab;
@@ -1690,19 +1721,170 @@ static int prepare_flow(fc3dgpu_ctx* c) {
   return 0;
 }
 
-static int autotune_lanes(fc3dgpu_ctx* c) {
-  // Measured on GB300 (60x60x30 lattice, 10 colours): one lane per contact
-  // is fastest while a colour phase holds at least one 32-contact slab per
-  // resident warp; splitting a contact over more lanes only pays when the
-  // phases are too small to give every warp a slab.
-  const long long per_phase = (long long)c->nc / (c->ncol > 0 ? c->ncol : 1);
-  const long long warps = (long long)c->nsm * 16;
-  if (per_phase >= 32 * warps / 4) return 1;
-  if (per_phase >= 32 * warps / 16) return 2;
-  return 4;
+// Measuring autotuner.  At the first solve of a layout with automatic lanes
+// it times FP32 sweeps of the candidate variants, each as one warm-up solve
+// and one measured solve (device time from CUDA events) from the current
+// reaction, which is restored afterwards, and keeps the fastest for the
+// layout (a new structure tunes again).  Mode 1 (the default) weighs only
+// variants that give the same iterates bit for bit: the dataflow sweep with
+// 8, 10 or 12 warps a block (each warp stages its own slab, so this is the
+// staging depth of an SM) and the coloured kernel with one lane per contact
+// (bulk-copy staged); FP64 sweeps keep one lane per contact (the oracle's
+// iterates).  Mode 2 adds the coloured kernel with 2, 4 and 8 lanes per
+// contact in both precisions (a row's product split over lanes: other sums,
+// so the choice shows in the last bits); mode 0 uses the defaults unmeasured.
+// On the 60x60x30 lattice mode 1 costs about 3 ms once per structure.
+static int solve_impl(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgpu_stats* st);
+
+static float tune_one(fc3dgpu_ctx* c, const fc3dgpu_params& base, int precision, int lanes, int sweeps) {
+  fc3dgpu_params q = base;
+  q.precision = precision;
+  q.lanes = lanes;
+  q.tol = 1e-300;
+  q.switch_tol = 0.0;
+  q.stall_window = 0;
+  q.fp32_only = precision == 0 ? 1 : 0;
+  fc3dgpu_stats S;
+  q.max_iter = 2;
+  if (solve_impl(c, &q, &S) != 0) return INFINITY;
+  q.max_iter = sweeps;
+  if (solve_impl(c, &q, &S) != 0) return INFINITY;
+  const double ms = precision == 0 ? S.ms_fp32 : S.ms_fp64;
+  const int n = precision == 0 ? S.sweeps32 : S.sweeps64;
+  return n > 0 ? (float)(ms / n) : INFINITY;
+}
+
+static int autotune(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
+  using namespace fc3dgpu;
+  if (c->tuned) return 0;
+  cudaStream_t s = c->stream;
+  const size_t nr = ((size_t)c->npad + 1) * 4;
+  CK(ensure(&c->tune_r64, &c->tune_r64_cap, nr));
+  CK(ensure(&c->tune_rpli64, &c->tune_rpli64_cap, (size_t)c->npad));
+  CK(ensure(&c->tune_rpli32, &c->tune_rpli32_cap, (size_t)c->npad));
+  CK(cudaMemcpyAsync(c->tune_r64, c->r64, sizeof(double) * nr, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(c->tune_rpli64, c->rpli64, sizeof(double) * c->npad, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(c->tune_rpli32, c->rpli32, sizeof(float) * c->npad, cudaMemcpyDeviceToDevice, s));
+  const int flow_on = c->flow_on, want = c->flow_want;
+  unsigned long long* tl = c->timeline;
+  const int tls = c->timeline_sweep, cnt = c->counters_on;
+  c->timeline_sweep = 0;
+  c->counters_on = 0;
+  const int sw32 = 6, sw64 = 3;
+  const bool all = c->tune_mode >= 2;
+  float best32 = INFINITY, best64 = INFINITY;
+  int k = 0;
+  c->tune_flow = 0;
+  c->tune_nw = 0;
+  c->tune_lanes32 = 1;
+  c->tune_lanes64 = 1;
+  // the dataflow sweep at 8, 10, 12 warps a block
+  c->flow_on = 1;
+  if (int rc = prepare_flow(c)) return rc;
+  const bool flow_ok = c->flow_state == 1;
+  const int nws[3] = {8, 10, 12};
+  for (int i = 0; i < 3; i++, k++) {
+    c->tune_ms32[k] = INFINITY;
+    if (!flow_ok) continue;
+    const int got = flow_warps(c->flow_maxslot, nws[i]);
+    if (got != nws[i]) continue;
+    c->flow_nw = got;
+    const float ms = tune_one(c, *p, 0, 1, sw32);
+    c->tune_ms32[k] = ms;
+    if (ms < best32) {
+      best32 = ms;
+      c->tune_flow = 1;
+      c->tune_nw = got;
+      c->tune_lanes32 = 1;
+    }
+  }
+  // the coloured kernel at 1 (and, in mode 2, 2, 4, 8) lanes per contact
+  c->flow_on = 0;
+  const int ls[4] = {1, 2, 4, 8};
+  for (int i = 0; i < 4; i++, k++) {
+    c->tune_ms32[k] = INFINITY;
+    if (i > 0 && !all) continue;
+    const float ms = tune_one(c, *p, 0, ls[i], sw32);
+    c->tune_ms32[k] = ms;
+    if (ms < best32) {
+      best32 = ms;
+      c->tune_flow = 0;
+      c->tune_lanes32 = ls[i];
+    }
+  }
+  for (int i = 0; i < 4; i++) {
+    c->tune_ms64[i] = INFINITY;
+    if (!all) continue;
+    const float ms = tune_one(c, *p, 1, ls[i], sw64);
+    c->tune_ms64[i] = ms;
+    if (ms < best64) {
+      best64 = ms;
+      c->tune_lanes64 = ls[i];
+    }
+  }
+  if (!all) best64 = 0.f;  // one lane per contact, unmeasured
+  c->flow_on = flow_on;
+  c->flow_want = want;
+  if (c->flow_state == 1) c->flow_nw = c->tune_flow ? c->tune_nw : flow_warps(c->flow_maxslot, want);
+  c->timeline = tl;
+  c->timeline_sweep = tls;
+  c->counters_on = cnt;
+  CK(cudaMemcpyAsync(c->r64, c->tune_r64, sizeof(double) * nr, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(c->rpli64, c->tune_rpli64, sizeof(double) * c->npad, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(c->rpli32, c->tune_rpli32, sizeof(float) * c->npad, cudaMemcpyDeviceToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  if (!(best32 < INFINITY) || !(best64 < INFINITY)) {
+    fc3dgpu_set_error("autotuner: no sweep variant ran");
+    return NUMERICS_ERR_UNKNOWN;
+  }
+  c->tuned = 1;
+  return 0;
+}
+
+extern "C" int fc3dgpu_ctx_autotune(fc3dgpu_ctx* c, int mode) {
+  if (!c) return -1;
+  if (mode < 0 || mode > 2) {
+    fc3dgpu_set_error("fc3dgpu_ctx_autotune: mode 0, 1 or 2");
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  const int old = c->tune_mode;
+  if (mode != old) c->tuned = 0;
+  c->tune_mode = mode;
+  return old;
+}
+
+extern "C" int fc3dgpu_ctx_tuning(fc3dgpu_ctx* c, int* choice4, float* ms11) {
+  if (!c) return NUMERICS_ERR_NULL_POINTER;
+  if (!c->tuned) return 1;
+  if (choice4) {
+    choice4[0] = c->tune_flow;
+    choice4[1] = c->tune_flow ? c->tune_nw : 0;
+    choice4[2] = c->tune_lanes32;
+    choice4[3] = c->tune_lanes64;
+  }
+  if (ms11) {
+    for (int i = 0; i < 7; i++) ms11[i] = c->tune_ms32[i];
+    for (int i = 0; i < 4; i++) ms11[7 + i] = c->tune_ms64[i];
+  }
+  return 0;
 }
 
 extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgpu_stats* st) {
+  if (!c || !p || !c->have_W || !c->have_q || !c->have_r) {
+    fc3dgpu_set_error("fc3dgpu_ctx_solve: problem, q/mu or r not set");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (p->lanes <= 0 && !c->tuned && c->tune_mode > 0 && c->nscenes == 0) {
+    if (cudaSetDevice(c->device) != cudaSuccess) {
+      fc3dgpu_set_error("fc3dgpu_ctx_solve: cudaSetDevice(%d) failed", c->device);
+      return NUMERICS_ERR_UNKNOWN;
+    }
+    if (int rc = autotune(c, p)) return rc;
+  }
+  return solve_impl(c, p, st);
+}
+
+static int solve_impl(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgpu_stats* st) {
   using namespace fc3dgpu;
   if (!c || !p || !c->have_W || !c->have_q || !c->have_r) {
     fc3dgpu_set_error("fc3dgpu_ctx_solve: problem, q/mu or r not set");
@@ -1712,15 +1894,20 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
   cudaStream_t s = c->stream;
   fc3dgpu_stats S;
   memset(&S, 0, sizeof(S));
-  // automatic lanes: one per contact whenever the FP32 dataflow sweep
-  // applies (it beats the coloured kernel at every lane count, measured on
-  // GB300 from 1,056 to 320,400 contacts), else the coloured kernel's tuning
-  // (the FP64 sweeps keep the coloured kernel's tuning)
-  const int lanes64 = p->lanes > 0 ? p->lanes : autotune_lanes(c);
-  int lanes = lanes64;
-  if (p->lanes <= 0 && c->flow_on && p->precision == 0 && !c->counters_on) {
-    if (int rc = prepare_flow(c)) return rc;
-    if (c->flow_state == 1) lanes = 1;
+  // automatic lanes: the autotuner's choices for this layout (without it,
+  // one lane per contact and the dataflow sweep where it applies)
+  const bool tuned = p->lanes <= 0 && c->tuned;
+  const int lanes64 = p->lanes > 0 ? p->lanes : (tuned ? c->tune_lanes64 : 1);
+  const int lanes = p->lanes > 0 ? p->lanes : (tuned ? c->tune_lanes32 : 1);
+  const bool use_flow = c->flow_on && (!tuned || c->tune_flow);
+  const bool mixed = p->precision == 0 || p->precision == 2, fast64 = p->precision >= 2;
+  if (p->precision < 0 || p->precision > 3) {
+    fc3dgpu_set_error("precision must be 0, 1, 2 or 3 (got %d)", p->precision);
+    return NUMERICS_ERR_INVALID_OPTION;
+  }
+  if (p->local_mode32 != 0 && p->local_mode32 != 1) {
+    fc3dgpu_set_error("local_mode32 must be 0 or 1 (got %d)", p->local_mode32);
+    return NUMERICS_ERR_INVALID_OPTION;
   }
   if (lanes64 != 1 && lanes64 != 2 && lanes64 != 4 && lanes64 != 8) {
     fc3dgpu_set_error("lanes per contact must be 1, 2, 4 or 8 (got %d)", lanes64);
@@ -1736,7 +1923,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
   int sweeps32 = 0, grid = 0;
   bool converged32 = false;
   double out[8];
-  if (p->precision == 0 && p->max_iter > 0) {
+  if (mixed && p->max_iter > 0) {
     SweepArgs<float> a;
     fill_args<float>(c, a, c->W32, c->D32, c->q32, c->mu32, c->rho32, c->r32, c->rpli32);
     a.max_sweeps = p->max_iter;
@@ -1748,6 +1935,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     a.newton_max = p->newton_max;
     a.pli_max = p->pli_max;
     a.ls_max = p->ls_max;
+    a.local_mode = p->local_mode32;
     size_t smem = 0;
     if (lanes == 1) {
       const int g1 = sweep_grid_f32(1);
@@ -1758,7 +1946,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     k_r64_to_r32<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->r64, c->r32);
     CK(cudaGetLastError());
     c->launches++;
-    bool flow = lanes == 1 && c->flow_on && !a.counters;
+    bool flow = lanes == 1 && use_flow && !a.counters;
     if (flow) {
       if (int rc = prepare_flow(c)) return rc;
       flow = c->flow_state == 1;
@@ -1812,12 +2000,18 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     int g64 = 0;
     if (lanes64 == 1)
       if (int rc = attach_nbr<double>(c, a, sweep_grid_f64(1))) return rc;
+    // the exact FP64 kernels, or those with the fast one-contact arithmetic
+    // (same grid: same occupancy)
+    auto launch64 = [&](const SweepArgs<double>& x) {
+      return fast64 ? fc3dgpu_launch_sweep_f64_fast(&x, lanes64, 0, s, &g64)
+                    : launch_sweep_f64(x, lanes64, 0, 0, s, &g64);
+    };
     if (converged32 && budget > 0) {
       // the FP32 iterate met the tolerance in FP32 arithmetic: check it in
       // FP64 before any FP64 sweep
       a.max_sweeps = 0;
       CK(cudaMemsetAsync(c->barrier, 0, FC3D_BARRIER_WORDS * sizeof(unsigned), s));
-      CK(launch_sweep_f64(a, lanes64, 0, 0, s, &g64));
+      CK(launch64(a));
       c->launches++;
       CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
@@ -1825,7 +2019,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
     }
     if (!(converged32 && a.max_sweeps == 0)) {
       CK(cudaMemsetAsync(c->barrier, 0, FC3D_BARRIER_WORDS * sizeof(unsigned), s));
-      CK(launch_sweep_f64(a, lanes64, 0, 0, s, &g64));
+      CK(launch64(a));
       c->launches++;
       CK(cudaMemcpyAsync(out, c->out, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
     }
@@ -1840,7 +2034,7 @@ extern "C" int fc3dgpu_ctx_solve(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgp
   cudaEventElapsedTime(&ms2, c->ev[1], c->ev[2]);
   S.sweeps32 = sweeps32;
   S.sweeps64 = (int)out[0];
-  if (S.sweeps64 > 0 || p->precision == 1) S.incr_error = out[1];
+  if (S.sweeps64 > 0 || !mixed) S.incr_error = out[1];
   S.error = out[2];
   S.info = (int)out[3];
   if (p->fp32_only && sweeps32 >= p->max_iter && S.info > 0) S.info = NUMERICS_ERR_MAX_ITER;
@@ -1995,7 +2189,8 @@ static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
   int g = 0;
   CK(cudaMemsetAsync(c->squeue, 0, 2 * sizeof(int), s));
   CK(cudaMemsetAsync(c->sout32, 0, sizeof(double) * 8 * ns, s));
-  if (p->precision == 0 && p->max_iter > 0) {
+  const bool mixed = p->precision == 0 || p->precision == 2;
+  if (mixed && p->max_iter > 0) {
     BatchArgs<float> b;
     fill_args<float>(c, b.base, c->W32, c->D32, c->q32, c->mu32, c->rho32, c->r32, c->rpli32);
     b.base.max_sweeps = p->max_iter;
@@ -2007,6 +2202,7 @@ static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
     b.base.newton_max = p->newton_max;
     b.base.pli_max = p->pli_max;
     b.base.ls_max = p->ls_max;
+    b.base.local_mode = p->local_mode32;
     b.base.trace = nullptr;
     b.base.timeline = nullptr;
     b.nscenes = ns;
@@ -2044,8 +2240,11 @@ static int record_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p) {
     b.scene_budget = c->sbudget;
     b.queue = c->squeue + 1;
     b.scene_out = c->sout64;
-    b.scene_out_prev = p->precision == 0 ? c->sout32 : nullptr;
-    CK(launch_batch_f64(b, c->batch_grid64, s, &g));
+    b.scene_out_prev = mixed ? c->sout32 : nullptr;
+    if (p->precision >= 2)
+      CK(fc3dgpu_launch_batch_f64_fast(&b, c->batch_grid64f, s, &g));
+    else
+      CK(launch_batch_f64(b, c->batch_grid64, s, &g));
   }
   return 0;
 }
@@ -2069,8 +2268,13 @@ extern "C" int fc3dgpu_ctx_solve_batch(fc3dgpu_ctx* c, const fc3dgpu_params* p, 
     c->batch_graph = nullptr;
   }
   if (!c->batch_graph) {
+    if (p->precision < 0 || p->precision > 3 || (p->local_mode32 != 0 && p->local_mode32 != 1)) {
+      fc3dgpu_set_error("fc3dgpu_ctx_solve_batch: precision must be 0-3 and local_mode32 0 or 1");
+      return NUMERICS_ERR_INVALID_OPTION;
+    }
     CK(batch_grid_f32(&c->batch_grid32));
     CK(batch_grid_f64(&c->batch_grid64));
+    CK(fc3dgpu_batch_grid_f64_fast(&c->batch_grid64f));
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     int rc = record_batch(c, p);

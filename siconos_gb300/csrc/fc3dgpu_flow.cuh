@@ -239,6 +239,7 @@ __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowA
     L.newton_max = a.newton_max;
     L.pli_max = a.pli_max;
     L.ls_max = a.ls_max;
+    L.mode = a.local_mode;
     L.n_newton = L.n_pli = L.n_ls = 0;
     rn[0] = ro[0];
     rn[1] = ro[1];
@@ -340,16 +341,17 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
       float rn[3];
       flow_slab(a, f, s, next, buf, bar, lane, (float)a.local_tol, rn, tl, x);
       pending = true;
+      if (x.row) {
+        // light-error sums (fc3d_nsgs.c:80-96), while the reaction stores
+        // drain: squares in FP32, sums in FP64 (the FP64 pipe is a small
+        // share of the SM's)
+        const float d0 = x.ro[0] - rn[0], d1 = x.ro[1] - rn[1], d2 = x.ro[2] - rn[2];
+        acc[0] += (double)(d0 * d0 + d1 * d1 + d2 * d2);
+        acc[1] += (double)(rn[0] * rn[0] + rn[1] * rn[1] + rn[2] * rn[2]);
+      }
       __syncwarp();
       if (tl) tl[4] = globaltimer_ns();
       if (lane == 0) st_release_u32(&f.done[s], (unsigned)sweep);
-      if (x.row) {
-        // light-error sums (fc3d_nsgs.c:80-96), off the slab's critical path
-        const double d0 = (double)x.ro[0] - (double)rn[0], d1 = (double)x.ro[1] - (double)rn[1],
-                     d2 = (double)x.ro[2] - (double)rn[2];
-        acc[0] += d0 * d0 + d1 * d1 + d2 * d2;
-        acc[1] += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
-      }
     }
     flow_block_sum<2, NW>(acc, f.part + blockIdx.x * 8 + (sweep & 3) * 2);
     e_prev = e_last;

@@ -30,10 +30,55 @@ struct Eps<float> {
   static __device__ __forceinline__ float v() { return FLT_EPSILON; }
 };
 
+// Square root and division of the one-contact solver (Newton, line search,
+// 3x3 elimination, PLI).  They are the plain operations, except in the
+// kernels built with FC3D_FAST_F64 (the opt-in fast FP64 polish), where the
+// FP64 ones are refined from FP32 seeds (see below).  The natural-map error
+// (projection on the cone) and rho always use the plain operations: they
+// decide convergence and are stored with the layout.
+template <typename Real>
+__device__ __forceinline__ Real esqrt(Real x) {
+  return sqrt(x);
+}
 template <typename Real>
 __device__ __forceinline__ Real dsqrt(Real x) {
   return sqrt(x);
 }
+template <typename Real>
+__device__ __forceinline__ Real ldiv(Real a, Real b) {
+  return a / b;
+}
+#ifdef FC3D_FAST_F64
+// One Newton-Raphson step for the reciprocal, y1 = y0 (2 - b y0) written as
+// y1 = y0 + y0 (1 - b y0), from the correctly rounded FP32 reciprocal of b
+// rounded to FP32: the seed's relative error e0 is below 1.2e-7, the step's
+// about e0^2 < 1.5e-14, so a / b comes out within about 1.5e-14 relative
+// (the exact division takes about twice as many dependent FP64 operations).
+// Arguments outside the FP32 range (and zero, infinities, NaN) take the
+// exact division.
+template <>
+__device__ __forceinline__ double ldiv<double>(double a, double b) {
+  const float bf = __double2float_rn(b);
+  if (!(fabsf(bf) > 1e-30f && fabsf(bf) < 1e30f)) return a / b;
+  double y = (double)__frcp_rn(bf);
+  const double e = fma(-b, y, 1.0);
+  y = fma(y, e, y);
+  return a * y;
+}
+// sqrt(x) from an FP32 reciprocal square root y0 by one Newton-Raphson step
+// on h = x y0 (the coupled iteration sqrt(x) ~ h (1 + r / 2) with
+// r = 1 - h y0): relative error about (3 e0 / 2)^2, below 1e-13 for the
+// FP32 seed.  Non-positive, tiny and huge arguments take the exact root.
+template <>
+__device__ __forceinline__ double dsqrt<double>(double x) {
+  const float xf = __double2float_rn(x);
+  if (!(xf > 1e-30f && xf < 1e30f)) return sqrt(x);
+  const double y = (double)rsqrtf(xf);
+  const double h = x * y;
+  const double r = fma(-h, y, 1.0);
+  return fma(h, 0.5 * r, h);
+}
+#endif
 
 // r += a v (column-major a), column by column (op3x3.h:342)
 template <typename Real>
@@ -59,15 +104,15 @@ __device__ __forceinline__ int solve3x3(const Real a[9], Real b[3]) {
   Real aa0 = fabs(a0), aa1 = fabs(a1), aa2 = fabs(a2);
   int p1 = aa0 >= aa1 ? (aa0 >= aa2 ? 0 : 2) : (aa1 >= aa2 ? 1 : 2);
   if (p1 == 0) {
-    f1 = a1 / a0; f2 = a2 / a0; lp0 = a0; alp0 = fabs(a0); lp1 = a[3]; lp2 = a[6];
+    f1 = ldiv(a1, a0); f2 = ldiv(a2, a0); lp0 = a0; alp0 = fabs(a0); lp1 = a[3]; lp2 = a[6];
     lm1 = a[4] - f1 * lp1; lm2 = a[7] - f1 * lp2; ln1 = a[5] - f2 * lp1; ln2 = a[8] - f2 * lp2;
     bl = b[0]; bm = b[1] - f1 * bl; bn = b[2] - f2 * bl;
   } else if (p1 == 1) {
-    f1 = a0 / a1; f2 = a2 / a1; lp0 = a1; alp0 = fabs(a1); lp1 = a[4]; lp2 = a[7];
+    f1 = ldiv(a0, a1); f2 = ldiv(a2, a1); lp0 = a1; alp0 = fabs(a1); lp1 = a[4]; lp2 = a[7];
     lm1 = a[3] - f1 * lp1; lm2 = a[6] - f1 * lp2; ln1 = a[5] - f2 * lp1; ln2 = a[8] - f2 * lp2;
     bl = b[1]; bm = b[0] - f1 * bl; bn = b[2] - f2 * bl;
   } else {
-    f1 = a0 / a2; f2 = a1 / a2; lp0 = a2; alp0 = fabs(a2); lp1 = a[5]; lp2 = a[8];
+    f1 = ldiv(a0, a2); f2 = ldiv(a1, a2); lp0 = a2; alp0 = fabs(a2); lp1 = a[5]; lp2 = a[8];
     lm1 = a[3] - f1 * lp1; lm2 = a[6] - f1 * lp2; ln1 = a[4] - f2 * lp1; ln2 = a[7] - f2 * lp2;
     bl = b[2]; bm = b[0] - f1 * bl; bn = b[1] - f2 * bl;
   }
@@ -75,16 +120,16 @@ __device__ __forceinline__ int solve3x3(const Real a[9], Real b[3]) {
   Real alm1 = fabs(lm1), aln1 = fabs(ln1);
   if (alm1 >= aln1) {
     if (alm1 < E) return 1;
-    f1 = ln1 / lm1;
-    s2 = (bn - f1 * bm) / (ln2 - f1 * lm2);
-    s1 = (bm - lm2 * s2) / lm1;
+    f1 = ldiv(ln1, lm1);
+    s2 = ldiv(bn - f1 * bm, ln2 - f1 * lm2);
+    s1 = ldiv(bm - lm2 * s2, lm1);
   } else {
     if (aln1 < E) return 1;
-    f1 = lm1 / ln1;
-    s2 = (bm - f1 * bn) / (lm2 - f1 * ln2);
-    s1 = (bn - ln2 * s2) / ln1;
+    f1 = ldiv(lm1, ln1);
+    s2 = ldiv(bm - f1 * bn, lm2 - f1 * ln2);
+    s1 = ldiv(bn - ln2 * s2, ln1);
   }
-  b[0] = (bl - s1 * lp1 - s2 * lp2) / lp0;
+  b[0] = ldiv(bl - s1 * lp1 - s2 * lp2, lp0);
   b[1] = s1;
   b[2] = s2;
   return 0;
@@ -93,7 +138,7 @@ __device__ __forceinline__ int solve3x3(const Real a[9], Real b[3]) {
 // projection on the Coulomb cone of coefficient mu (projectionOnCone.c:32-49)
 template <typename Real>
 __device__ __forceinline__ void project_cone(Real r[3], Real mu) {
-  Real normT = dsqrt(r[1] * r[1] + r[2] * r[2]);
+  Real normT = esqrt(r[1] * r[1] + r[2] * r[2]);
   if (mu * normT <= -r[0]) {
     r[0] = 0;
     r[1] = 0;
@@ -111,7 +156,7 @@ __device__ __forceinline__ void project_cone(Real r[3], Real mu) {
 template <typename Real>
 __device__ __forceinline__ Real unitary_error2(const Real r[3], const Real u[3], Real mu) {
   Real w[3];
-  w[0] = r[0] - u[0] - mu * dsqrt(u[1] * u[1] + u[2] * u[2]);
+  w[0] = r[0] - u[0] - mu * esqrt(u[1] * u[1] + u[2] * u[2]);
   w[1] = r[1] - u[1];
   w[2] = r[2] - u[2];
   project_cone(w, mu);
@@ -152,7 +197,7 @@ __device__ __forceinline__ void ac_std(const Real R[3], const Real v[3], Real mu
     }
   } else if (RV > Radius) {
     if (Radius > Real(0)) {
-      Real RV1 = Real(1) / RV;
+      Real RV1 = ldiv(Real(1), RV);
       F[1] = R[1] - Radius * RVT * RV1;
       F[2] = R[2] - Radius * RVS * RV1;
       if (GRAD) {
@@ -193,6 +238,7 @@ struct LocalProblem {
   Real rho_pli;  // PLI step, persists across sweeps
   Real tol;
   int newton_max, pli_max, ls_max;
+  int mode;       // 0: the reference's hybrid; 1: damped Newton only
   Real residual;  // SOLVER_RESIDUAL of the local options
   int n_newton, n_pli, n_ls;  // work counters
 };
@@ -204,7 +250,7 @@ __device__ __forceinline__ Real local_error(const LocalProblem<Real>& L, const R
   mvp3x3(L.M, r, v);
   Real e = Real(0) + unitary_error2(r, v, L.mu);
   e = dsqrt(e);
-  if (fabs(nq) > Eps<Real>::v()) e /= nq;
+  if (fabs(nq) > Eps<Real>::v()) e = ldiv(e, nq);
   return e;
 }
 
@@ -243,7 +289,7 @@ __device__ __forceinline__ Real line_search_gp(LocalProblem<Real>& L, const Real
     for (int i = 0; i < 3; i++) v[i] = M[i] * tmp[0] + L.q[i] + M[i + 3] * tmp[1] + M[i + 6] * tmp[2];
     ac_std<Real, false>(tmp, v, L.mu, L.rhoN, L.rhoT, F, nullptr, nullptr);
     Real qv = Real(0.5) * (((Real(0) + F[0] * F[0]) + F[1] * F[1]) + F[2] * F[2]);
-    Real slope = (qv - q0) / alpha;
+    Real slope = ldiv(qv - q0, alpha);
     bool C1 = (slope >= m2 * dqdt0), C2 = (slope <= m1 * dqdt0);
     if (C1 && C2) return alpha;
     if (!C1)
@@ -263,7 +309,7 @@ __device__ __forceinline__ void newton_damped(LocalProblem<Real>& L, Real r[3]) 
   const Real E = Eps<Real>::v();
   Real nq = dsqrt(L.q[0] * L.q[0] + L.q[1] * L.q[1] + L.q[2] * L.q[2]);
   Real nrel = 1;
-  if (nq > E) nrel /= nq;
+  if (nq > E) nrel = ldiv(nrel, nq);
   Real dR[3], F[3] = {0, 0, 0}, A[9], B[9], AWB[9];
 #pragma unroll
   for (int e = 0; e < 9; e++) { A[e] = 0; B[e] = 0; }
@@ -328,7 +374,7 @@ __device__ __forceinline__ void pli_solve(LocalProblem<Real>& L, Real r[3]) {
     for (int i = 0; i < 3; i++) vel_k[i] = M[i] * r[0] + L.q[i] + M[i + 3] * r[1] + M[i + 6] * r[2];
     int ls = 0;
     bool success = false;
-    rho_k = rho / tau;
+    rho_k = ldiv(rho, tau);
     Real normUT = dsqrt(vel_k[1] * vel_k[1] + vel_k[2] * vel_k[2]);
     while (!success && (ls < 10)) {
       rho_k = rho_k * tau;
@@ -382,6 +428,20 @@ __device__ __forceinline__ void local_solve(LocalProblem<Real>& L, Real r[3]) {
     L.residual = 0;
     return;
   }
+  if (L.mode == 1) {
+    // accelerator mode of the FP32 sweeps: the damped Newton alone, from
+    // the contact's current reaction, with no natural-map error evaluations,
+    // no keep-or-discard and no PLI loop; a non-finite result keeps the
+    // incoming reaction.  The FP64 polish runs the reference's hybrid.
+    const Real r0[3] = {r[0], r[1], r[2]};
+    newton_damped(L, r);
+    if (!(isfinite(r[0]) && isfinite(r[1]) && isfinite(r[2]))) {
+      r[0] = r0[0];
+      r[1] = r0[1];
+      r[2] = r0[2];
+    }
+    return;
+  }
   Real rb[3] = {r[0], r[1], r[2]};
   Real cur = local_error(L, r);
   newton_damped(L, r);
@@ -408,7 +468,7 @@ __device__ __forceinline__ void ac_rho(const Real M[9], Real& rhoN, Real& rhoT) 
   Real sw = M[1 + 1 * 3] + M[2 + 2 * 3];
   Real dw = sw * sw - Real(4.0) * (sw - M[2 + 1 * 3] + M[1 + 2 * 3]);
   if (dw > Real(0))
-    dw = dsqrt(dw);
+    dw = esqrt(dw);
   else
     dw = 0;
   rhoN = Real(1.0) / M[0];

@@ -256,6 +256,7 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   L.newton_max = a.newton_max;
   L.pli_max = a.pli_max;
   L.ls_max = a.ls_max;
+  L.mode = a.local_mode;
   L.n_newton = 0;
   L.n_pli = 0;
   L.n_ls = 0;
@@ -368,6 +369,7 @@ __device__ __forceinline__ void solve_item(const SweepArgs<Real>& a, WorkList<Re
   L.newton_max = a.newton_max;
   L.pli_max = a.pli_max;
   L.ls_max = a.ls_max;
+  L.mode = a.local_mode;
   L.n_newton = 0;
   L.n_pli = 0;
   L.n_ls = 0;
@@ -547,6 +549,7 @@ __device__ __forceinline__ void solve_row_s(const SweepArgs<Real>& a, LocalProbl
   L.newton_max = a.newton_max;
   L.pli_max = a.pli_max;
   L.ls_max = a.ls_max;
+  L.mode = a.local_mode;
   L.n_newton = 0;
   L.n_pli = 0;
   L.n_ls = 0;

@@ -57,6 +57,7 @@ void warm_sweep_kernels() {
   cudaFuncGetAttributes(&fa, nsgs_kernel<float, 2>);
   cudaFuncGetAttributes(&fa, nsgs_kernel<float, 4>);
   cudaFuncGetAttributes(&fa, nsgs_kernel<float, 8>);
+  cudaFuncGetAttributes(&fa, nsgs_flow_kernel<12>);
   cudaFuncGetAttributes(&fa, nsgs_flow_kernel<10>);
   cudaFuncGetAttributes(&fa, nsgs_flow_kernel<8>);
   warm_sweep_kernels_f64();
@@ -72,19 +73,21 @@ int sweep_grid_f32(int lanes) {
   }
 }
 
-// Warps per block of the dataflow sweep: 10 (320 threads) when ten per-warp
-// buffers fit the shared memory of an SM, else 8, else none.  On the
-// 60x60x30 lattice 10 warps sweep 1.3 % faster than 12 and 10 % faster than
-// 8 or 14 (fewer warps polling the same slab counters, against fewer slabs
-// in flight).
-int flow_warps(int maxslot) {
+// Warps per block of the dataflow sweep that fit the shared memory of an SM
+// with per-warp buffers for slabs of up to maxslot slots: the largest of
+// `want` (8, 10 or 12; 0 = 10, the default) and the smaller counts that fit,
+// else 0.  On the 60x60x30 lattice 10 warps were measured the fastest with
+// round-trip polls of the slab counters; the autotuner measures 8, 10 and 12.
+int flow_warps(int maxslot, int want) {
   int dev = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t room = optin > 4096 ? (size_t)optin - 4096 : 0;  // static shared memory of the kernel
   const size_t buf = flow_buf_bytes(maxslot);
-  if (10 * buf <= room) return 10;
-  if (8 * buf <= room) return 8;
+  if (want <= 0) want = 10;
+  const int cand[3] = {12, 10, 8};
+  for (int nw : cand)
+    if (nw <= want && (size_t)nw * buf <= room) return nw;
   return 0;
 }
 
@@ -111,6 +114,7 @@ static cudaError_t launch_flow_t(const SweepArgs<float>& a, const FlowArgs& f, c
 
 cudaError_t launch_flow_f32(const SweepArgs<float>& a, const FlowArgs& f, int nw, cudaStream_t s, int* grid) {
   switch (nw) {
+    case 12: return launch_flow_t<12>(a, f, s, grid);
     case 10: return launch_flow_t<10>(a, f, s, grid);
     case 8: return launch_flow_t<8>(a, f, s, grid);
     default: return cudaErrorInvalidValue;

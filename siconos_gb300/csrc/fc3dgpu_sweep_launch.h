@@ -29,9 +29,10 @@ void warm_batch_kernel_f32();
 void warm_batch_kernel_f64();
 int sweep_grid_f64(int lanes);
 // Slab-dataflow FP32 sweep: warps per block for slabs of up to maxslot
-// slots (0: the per-warp buffers do not fit), its cooperative launch (one
-// block per SM), and the build of its per-slab column lists (k_flow_deps).
-int flow_warps(int maxslot);
+// slots, at most `want` (0: the default; 0 returned: the per-warp buffers do
+// not fit), its cooperative launch (one block per SM), and the build of its
+// per-slab column lists (k_flow_deps).
+int flow_warps(int maxslot, int want);
 cudaError_t launch_flow_f32(const SweepArgs<float>& a, const FlowArgs& f, int nw, cudaStream_t s, int* grid);
 cudaError_t build_flow_deps(int nslab, int npad, int ncol, const int* sptr_d, const int* perm, const int* slab_nslot,
                             const long long* slab_off, const int* col, const int* dptr, int* count, int* dep,

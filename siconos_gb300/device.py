@@ -80,6 +80,35 @@ class DeviceSolver:
         returns the previous setting."""
         return bool(self.L.fc3dgpu_ctx_flow(self.ctx, int(on)))
 
+    def flow_warps(self, nw: int) -> int:
+        """Warps per block of the dataflow sweep (8, 10, 12; 0 = default);
+        returns the previous request."""
+        rc = int(self.L.fc3dgpu_ctx_flow_warps(self.ctx, nw))
+        if rc < 0:
+            raise RuntimeError(sn.last_error())
+        return rc
+
+    def autotune(self, mode: int) -> int:
+        """Autotuner mode (0 off, 1 result-preserving variants, 2 all);
+        returns the previous mode."""
+        rc = int(self.L.fc3dgpu_ctx_autotune(self.ctx, mode))
+        if rc < 0:
+            raise RuntimeError(sn.last_error())
+        return rc
+
+    def tuning(self):
+        """The autotuner's choice for the current structure, or None."""
+        ch = np.zeros(4, np.int32)
+        ms = np.zeros(11, np.float32)
+        if self.L.fc3dgpu_ctx_tuning(self.ctx, ch.ctypes.data, ms.ctypes.data) != 0:
+            return None
+        return {"flow": bool(ch[0]), "flow_warps": int(ch[1]), "lanes32": int(ch[2]), "lanes64": int(ch[3]),
+                "ms_sweep32": {"flow8": float(ms[0]), "flow10": float(ms[1]), "flow12": float(ms[2]),
+                               "lanes1": float(ms[3]), "lanes2": float(ms[4]), "lanes4": float(ms[5]),
+                               "lanes8": float(ms[6])},
+                "ms_sweep64": {"lanes1": float(ms[7]), "lanes2": float(ms[8]), "lanes4": float(ms[9]),
+                               "lanes8": float(ms[10])}}
+
     # ---- batched problems -------------------------------------------------
     def set_contacts(self, geo: dict, colouring: int = sn.FC3DGPU_COLOURING_DEFAULT):
         """Assemble W on the device from contact geometry (see

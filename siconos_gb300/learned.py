@@ -92,6 +92,11 @@ class WarmStartMLP:
         if rc != 0:
             raise RuntimeError(f"{what} failed ({rc}): {sn.last_error()}")
 
+    def tensor_path(self, tcgen05: bool) -> bool:
+        """Products on tcgen05 (True) or on the mma.sync reference path
+        (False); returns the previous setting."""
+        return bool(self.L.fc3dgpu_mlp_set_tensor_path(self.h, int(tcgen05)))
+
     def set_params(self, params, stats):
         params = np.ascontiguousarray(params, np.float32)
         stats = np.ascontiguousarray(stats, np.float32)

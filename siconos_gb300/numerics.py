@@ -125,7 +125,7 @@ class FC3DGPUParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precision", C.c_int), ("lanes", C.c_int),
                 ("switch_tol", C.c_double), ("stall_window", C.c_int), ("local_tol", C.c_double),
                 ("local_tol32", C.c_double), ("newton_max", C.c_int), ("pli_max", C.c_int), ("ls_max", C.c_int),
-                ("fp32_only", C.c_int)]
+                ("fp32_only", C.c_int), ("local_mode32", C.c_int)]
 
 
 class FC3DGPUStats(C.Structure):
@@ -191,6 +191,7 @@ ABI = {
     "fc3dgpu_mlp_train_step_device": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_float]),
     "fc3dgpu_mlp_infer": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_int]),
     "fc3dgpu_mlp_infer_stream": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc3dgpu_mlp_set_tensor_path": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_warm_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_ctx_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_ctx_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -217,6 +218,9 @@ ABI = {
     "fc3dgpu_ctx_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_sync": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_flow": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_ctx_flow_warps": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_ctx_autotune": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_ctx_tuning": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_ctx_spin_limit": (C.c_ulonglong, [C.c_void_p, C.c_ulonglong]),
     "fc3dgpu_ctx_timeline": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     "fc3dgpu_ctx_stream": (C.c_void_p, [C.c_void_p]),

@@ -82,13 +82,18 @@ def lattice(nx: int, ny: int, nz: int, seed: int = 1, mu: float = 0.5, jitter_st
     return LatticeScene((nx, ny, nz), seed, n, nb.value, rp, ci, bl.reshape(k, 9), q, np.full(n, float(mu)), gap, hdl)
 
 
-def batch_scenes(count: int = 512, seed: int = 7, lo=(3, 3, 2), hi=(20, 20, 10), mu_range=(0.1, 0.9)):
-    """Independent scenes with dims drawn uniformly in [lo, hi] per axis and
-    mu ~ U(mu_range) per scene."""
+def batch_specs(count: int = 512, seed: int = 7, lo=(3, 3, 2), hi=(20, 20, 10), mu_range=(0.1, 0.9)):
+    """(dims, seed, mu) of each scene of the batch: dims drawn uniformly in
+    [lo, hi] per axis, mu ~ U(mu_range) per scene."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
-        d = [int(rng.integers(lo[a], hi[a] + 1)) for a in range(3)]
+        d = tuple(int(rng.integers(lo[a], hi[a] + 1)) for a in range(3))
         m = float(rng.uniform(*mu_range))
-        out.append(lattice(*d, seed=seed * 100003 + k, mu=m))
+        out.append((d, seed * 100003 + k, m))
     return out
+
+
+def batch_scenes(count: int = 512, seed: int = 7, lo=(3, 3, 2), hi=(20, 20, 10), mu_range=(0.1, 0.9)):
+    """Independent scenes of batch_specs."""
+    return [lattice(*d, seed=sd, mu=m) for d, sd, m in batch_specs(count, seed, lo, hi, mu_range)]

@@ -40,13 +40,20 @@ def _layers_close(g, ref, tol):
             assert num <= tol * max(den, 1e-12), (a, b, num, den)
 
 
+@pytest.mark.parametrize("tc", [False, True], ids=["mma_sync", "tcgen05"])
 @pytest.mark.parametrize("n", [64, 300, 1000])
-def test_gradient_matches_oracle(mlp, n):
+def test_gradient_matches_oracle(mlp, n, tc):
+    """Both tensor-core paths (tcgen05 with TMEM accumulators, and the
+    mma.sync reference) against the CPU oracle's gradient."""
     p, st, X, T = _problem(n, n)
     mlp.set_params(p, st)
     mlp.set_data(X, T)
     idx = np.random.default_rng(5).permutation(n).astype(np.int32)
-    g, loss = mlp.grad(idx)
+    prev = mlp.tensor_path(tc)
+    try:
+        g, loss = mlp.grad(idx)
+    finally:
+        mlp.tensor_path(prev)
     loss_o, g_o = M.loss_and_grad(p, st, X[idx], T[idx])
     assert abs(loss - loss_o) <= 1e-3 * loss_o
     # same rounding points, FP32 sums in another order: 1e-2 per layer
@@ -57,10 +64,15 @@ def test_gradient_matches_oracle(mlp, n):
     assert cos > 0.999
 
 
-def test_inference_matches_oracle(mlp):
+@pytest.mark.parametrize("tc", [False, True], ids=["mma_sync", "tcgen05"])
+def test_inference_matches_oracle(mlp, tc):
     p, st, X, T = _problem(7, 777)
     mlp.set_params(p, st)
-    Y = mlp.infer(X)
+    prev = mlp.tensor_path(tc)
+    try:
+        Y = mlp.infer(X)
+    finally:
+        mlp.tensor_path(prev)
     y, _ = M.forward(p, st, X)
     Yo = y * st[2 * M.NF + M.NO:] + st[2 * M.NF:2 * M.NF + M.NO]
     scale = np.abs(Yo).max(axis=0)
@@ -162,3 +174,27 @@ def test_warm_start_keeps_a_better_fallback(mlp):
         assert st["sweeps64"] == 1
     finally:
         d.close()
+
+
+def test_tensor_paths_agree(mlp):
+    """tcgen05 and mma.sync compute the same products (same BF16 operands,
+    FP32 sums in another order): proposals within 1e-3 of the output scale,
+    gradients within 1e-2 per layer, on a batch that spans several tiles of
+    either path (2,000 samples)."""
+    p, st, X, T = _problem(11, 2000)
+    mlp.set_params(p, st)
+    mlp.set_data(X, T)
+    idx = np.random.default_rng(3).permutation(2000).astype(np.int32)
+    out = {}
+    prev = mlp.tensor_path(False)
+    try:
+        for tc in (False, True):
+            mlp.tensor_path(tc)
+            out[tc] = (mlp.infer(X), *mlp.grad(idx))
+    finally:
+        mlp.tensor_path(prev)
+    (y0, g0, l0), (y1, g1, l1) = out[False], out[True]
+    scale = np.abs(y0).max(axis=0)
+    assert (np.abs(y1 - y0).max(axis=0) <= 1e-3 * scale).all()
+    assert abs(l1 - l0) <= 1e-4 * l0
+    _layers_close(g1, g0, 1e-2)
