@@ -706,6 +706,53 @@ def run_ours(args):
     return 0
 
 
+def profile_case(name):
+    """Small cases for ncu captures, each launching the kernel named twice
+    (the first launch a warm-up: capture with -s 1 -c 1):
+    flow     nsgs_flow_kernel, 5 FP32 sweeps of the 60x60x30 lattice;
+    fp64     nsgs_kernel<double,1>, 3 FP64 sweeps of the same lattice;
+    mlp      k_train_tile_tc, one training step on 16,384 samples;
+    infer    k_infer_tc on 320,400 samples."""
+    from siconos_gb300 import build as B
+    B.build()
+    if name in ("flow", "fp64"):
+        from siconos_gb300.device import DeviceSolver
+        import oracle as O
+        P = O.lattice(*DIMS, seed=SEED, mu=MU)
+        d = DeviceSolver(0)
+        try:
+            d.set_W(P.nc, P.rowptr, P.colidx, P.blocks)
+            d.set_q_mu(P.q, P.mu)
+            for _ in range(2):
+                d.zero_r()
+                if name == "flow":
+                    st = d.solve(tol=1e-300, max_iter=5, lanes=1, fp32_only=1, switch_tol=0.0, stall_window=0)
+                else:
+                    st = d.solve(tol=1e-300, max_iter=3, lanes=1, precision=1)
+            return {"profile": name, "ms_fp32": st["ms_fp32"], "ms_fp64": st["ms_fp64"], "status": st["status"]}
+        finally:
+            d.close()
+    from siconos_gb300.learned import WarmStartMLP, init_params, make_stats
+    g = np.random.default_rng(0)
+    n = 16384 if name == "mlp" else 320400
+    X = g.standard_normal((n, 17)).astype(np.float32)
+    T = g.standard_normal((n, 3)).astype(np.float32)
+    m = WarmStartMLP(0)
+    try:
+        m.set_params(init_params(0), make_stats(X, T))
+        if name == "mlp":
+            m.set_data(X, T)
+            idx = np.arange(n, dtype=np.int32)
+            for _ in range(2):
+                _, loss = m.grad(idx)
+            return {"profile": name, "loss": float(loss)}
+        for _ in range(2):
+            Y = m.infer(X)
+        return {"profile": name, "mean": float(np.abs(Y).mean())}
+    finally:
+        m.close()
+
+
 # measurements beside the headline line (also runnable alone: --supplementary)
 SUPPLEMENTARY = {
     "fc2d_granular_7002": lambda: fc2d_granular(),
@@ -727,7 +774,12 @@ def main():
                     help="skip the time-to-tolerance, batched and time-stepping measurements")
     ap.add_argument("--supplementary", choices=sorted(SUPPLEMENTARY), default=None,
                     help="run only this supplementary measurement and print its JSON")
+    ap.add_argument("--profile", choices=["flow", "fp64", "mlp", "infer"], default=None,
+                    help="run a small case for an ncu capture and print its JSON")
     args = ap.parse_args()
+    if args.profile:
+        print(json.dumps(profile_case(args.profile)), flush=True)
+        return 0
     if args.supplementary:
         print(json.dumps({"supplementary": args.supplementary, **SUPPLEMENTARY[args.supplementary]()}), flush=True)
         return 0
