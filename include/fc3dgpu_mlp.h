@@ -69,14 +69,23 @@ int fc3dgpu_mlp_infer_stream(fc3dgpu_mlp *m, size_t n, const float *X, float *Y,
  * in the order of the FP32 sums only.  Returns the previous setting. */
 int fc3dgpu_mlp_set_tensor_path(fc3dgpu_mlp *m, int tcgen05);
 
+/* What the network's three outputs mean: 0 (default) the reaction itself,
+ * 1 the change from the previous-step reaction (features 13-15).  Returns the
+ * previous setting; fc3dgpu_mlp_residual reads it. */
+int fc3dgpu_mlp_set_residual(fc3dgpu_mlp *m, int residual);
+int fc3dgpu_mlp_residual(const fc3dgpu_mlp *m);
+
 /* Learned warm start of a device context.  The reaction currently in the
  * context (the previous step's, or what fc3dgpu_ctx_set_r gave) is the
  * fallback.  Features are formed on the device (gap: host array of nc
- * values in the caller's contact order, or NULL for 0), the proposal is
- * projected on each friction cone, and it replaces the reaction only when
- * its fc3d_compute_error is below the fallback's.  out3 (NULL or 3 doubles):
- * error of the fallback, error of the proposal, 1 when the proposal was
- * taken.  The norm of q is the context's. */
+ * values in the caller's contact order, or NULL for 0) and the network
+ * proposes a target (its output, or the fallback plus its output for a
+ * residual network).  The candidates fallback + alpha (target - fallback),
+ * alpha = 1, 1/2, 1/4, each projected on every friction cone, are evaluated
+ * with fc3d_compute_error; the best replaces the reaction only when its error
+ * is below the fallback's.  out3 (NULL or 3 doubles): error of the fallback,
+ * error of the best candidate, 1 when it was taken.  The norm of q is the
+ * context's. */
 int fc3dgpu_ctx_warm_start(fc3dgpu_ctx *ctx, fc3dgpu_mlp *m, const double *gap, double *out3);
 /* The 17 features of every contact, as the warm start forms them, in the
  * caller's contact order (X: host array of nc*17 floats). */

@@ -487,15 +487,24 @@ __global__ void k_gather_features(int nc, const int* __restrict__ iperm, const f
   }
 }
 
-// Keep the current reaction in rbak and put the proposal, projected on the
-// row's friction cone, in its place.
+// The candidate prev + alpha (target - prev), projected on each row's
+// friction cone, in place of the current reaction; prev is the reaction
+// before the warm start, saved in rbak on the first candidate (save != 0).
+// target is the network's output Y, or prev + Y for a network that predicts
+// the change of the reaction (residual != 0).
 __global__ void k_take_proposal(int npad, const int* __restrict__ perm, const float* __restrict__ Y,
                                 const double* __restrict__ mu64, double* __restrict__ r64, float* __restrict__ r32,
-                                double* __restrict__ rbak) {
+                                double* __restrict__ rbak, double alpha, int residual, int save) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npad; p += gridDim.x * blockDim.x) {
-    for (int a = 0; a < 3; a++) rbak[4 * (size_t)p + a] = r64[4 * (size_t)p + a];
+    if (save)
+      for (int a = 0; a < 3; a++) rbak[4 * (size_t)p + a] = r64[4 * (size_t)p + a];
     if (perm[p] < 0) continue;
-    double r[3] = {(double)Y[3 * (size_t)p], (double)Y[3 * (size_t)p + 1], (double)Y[3 * (size_t)p + 2]};
+    double r[3];
+    for (int a = 0; a < 3; a++) {
+      const double prev = rbak[4 * (size_t)p + a], y = (double)Y[3 * (size_t)p + a];
+      const double target = residual ? prev + y : y;
+      r[a] = prev + alpha * (target - prev);
+    }
     const int slab = p / FC3D_SLAB, k = p % FC3D_SLAB;
     project_cone<double>(r, mu64[(size_t)slab * FC3D_SLAB + k]);
     for (int a = 0; a < 3; a++) {
@@ -2380,16 +2389,36 @@ extern "C" int fc3dgpu_ctx_warm_start(fc3dgpu_ctx* c, fc3dgpu_mlp* m, const doub
     fc3dgpu_set_error("warm start: allocation failed");
     return NUMERICS_ERR_MEMORY;
   }
-  double e0 = 0.0, e1 = 0.0;
+  double e0 = 0.0, e1 = INFINITY;
   if (int rc = fc3dgpu_ctx_compute_error(c, &e0)) return rc;
   if (int rc = features_impl(c, gap)) return rc;
   if (int rc = fc3dgpu_mlp_infer_stream(m, (size_t)c->npad, c->feat, c->prop, s)) return rc;
   c->launches++;
-  k_take_proposal<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->perm, c->prop, c->mu64, c->r64, c->r32, c->rbak);
-  CK(cudaGetLastError());
-  c->launches++;
-  if (int rc = fc3dgpu_ctx_compute_error(c, &e1)) return rc;
-  const bool take = e1 < e0;  // false for a NaN proposal
+  // the full step, then half and a quarter of it from the current reaction:
+  // the candidate with the smallest fc3d_compute_error, when below e0
+  const int residual = fc3dgpu_mlp_residual(m);
+  const double alphas[3] = {1.0, 0.5, 0.25};
+  double best_alpha = 0.0;
+  for (int i = 0; i < 3; i++) {
+    k_take_proposal<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->perm, c->prop, c->mu64, c->r64, c->r32, c->rbak,
+                                                     alphas[i], residual, i == 0);
+    CK(cudaGetLastError());
+    c->launches++;
+    double e = 0.0;
+    if (int rc = fc3dgpu_ctx_compute_error(c, &e)) return rc;
+    if (e < e1) {  // false for a NaN candidate
+      e1 = e;
+      best_alpha = alphas[i];
+    }
+  }
+  const bool take = e1 < e0;
+  if (take && best_alpha != alphas[2]) {
+    k_take_proposal<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->perm, c->prop, c->mu64, c->r64, c->r32, c->rbak,
+                                                     best_alpha, residual, 0);
+    CK(cudaGetLastError());
+    c->launches++;
+    CK(cudaStreamSynchronize(s));
+  }
   if (!take) {
     k_restore_r<<<grid1d(c->npad), 256, 0, s>>>(c->npad, c->rbak, c->r64, c->r32);
     CK(cudaGetLastError());

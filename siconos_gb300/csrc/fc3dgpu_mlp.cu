@@ -737,6 +737,7 @@ struct fc3dgpu_mlp {
   int step = 0;
   bool have_params = false;
   int tc = 1;              // products on tcgen05 (1, default) or mma.sync (0, the checked reference)
+  int residual = 0;        // the network predicts the change of the reaction
   int* status = nullptr;   // nonzero: a tensor-core product did not complete
 };
 
@@ -1009,6 +1010,15 @@ extern "C" int fc3dgpu_mlp_infer(fc3dgpu_mlp* m, size_t n, const float* X, float
   MCK(e);
   return check_status(m);
 }
+
+extern "C" int fc3dgpu_mlp_set_residual(fc3dgpu_mlp* m, int residual) {
+  if (!m) return NUMERICS_ERR_NULL_POINTER;
+  const int prev = m->residual;
+  m->residual = residual ? 1 : 0;
+  return prev;
+}
+
+extern "C" int fc3dgpu_mlp_residual(const fc3dgpu_mlp* m) { return m ? m->residual : 0; }
 
 extern "C" int fc3dgpu_mlp_set_tensor_path(fc3dgpu_mlp* m, int tcgen05) {
   if (!m) return NUMERICS_ERR_NULL_POINTER;

@@ -176,14 +176,20 @@ class WarmStartMLP:
             n += len(part)
         return tot / max(1, n)
 
+    def residual(self, on: bool) -> bool:
+        """Outputs are the change of the reaction (True) or the reaction
+        (False); returns the previous setting."""
+        return bool(self.L.fc3dgpu_mlp_set_residual(self.h, int(on)))
+
     def save(self, path, **meta):
         p, s = self.get_params()
-        np.savez(path, params=p, stats=s, **meta)
+        np.savez(path, params=p, stats=s, residual=np.int32(self.L.fc3dgpu_mlp_residual(self.h)), **meta)
 
     def load(self, path=DEFAULT_WEIGHTS):
         z = np.load(path)
         self.set_params(z["params"], z["stats"])
-        return {k: z[k] for k in z.files if k not in ("params", "stats")}
+        self.residual(bool(int(z["residual"])) if "residual" in z.files else False)
+        return {k: z[k] for k in z.files if k not in ("params", "stats", "residual")}
 
     def close(self):
         if getattr(self, "h", None):

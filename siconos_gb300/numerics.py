@@ -192,6 +192,8 @@ ABI = {
     "fc3dgpu_mlp_infer": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_int]),
     "fc3dgpu_mlp_infer_stream": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_mlp_set_tensor_path": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_mlp_set_residual": (C.c_int, [C.c_void_p, C.c_int]),
+    "fc3dgpu_mlp_residual": (C.c_int, [C.c_void_p]),
     "fc3dgpu_ctx_warm_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_ctx_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc3dgpu_ctx_sizes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

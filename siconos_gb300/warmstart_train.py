@@ -9,11 +9,15 @@ scene gives two solves, both run as one batch per chunk of scenes:
   step 1  after a velocity random-walk step (v0 += N(0, 0.01^2) per degree
           of freedom, contacts kept), warm-started from step 0's reaction
           (which becomes the previous-reaction features).
-Solves use the FP32 sweeps + FP64 polish to tol 1e-8 within the sweep
-budget.  Up to `per_scene` contacts per scene and step are kept, so large
-scenes do not dominate.  The network is then trained with Adam on the GPU
-(minibatches of 4096, cosine learning-rate decay) and saved with its
-statistics and training record.
+Solves use the FP32 sweeps + FP64 polish to the tolerance `tol` (default
+1e-3, the tolerance the time-stepping and benchmark solves work to) within
+10,000 sweeps, and only scenes whose FP64 fc3d_compute_error reached it give
+pairs.  With --residual the targets are the change of the reaction from the
+previous-step reaction (features 13-15; zero on a first step), and the warm
+start adds the output to that reaction.  Up to `per_scene` contacts per scene
+and step are kept, so large scenes do not dominate.  The network is then
+trained with Adam on the GPU (minibatches of 4096, cosine learning-rate
+decay) and saved with its statistics and training record.
 """
 from __future__ import annotations
 
@@ -30,12 +34,14 @@ from .scene import lattice
 
 
 def generate(n_scenes: int, seed: int = 1000, lo=(5, 5, 5), hi=(30, 30, 30), per_scene: int = 2048,
-             chunk: int = 128, max_iter: int = 300, walk_std: float = 0.01, device: int = 0, log=None):
+             chunk: int = 128, max_iter: int = 10000, walk_std: float = 0.01, device: int = 0, log=None,
+             tol: float = 1e-3, residual: bool = False):
     rng = np.random.default_rng(seed)
     Xs, Ts = [], []
-    summary = {"scenes": 0, "contacts": 0, "solves": 0, "sweeps": 0, "errors_step0": [], "errors_step1": []}
+    summary = {"scenes": 0, "contacts": 0, "solves": 0, "sweeps": 0, "errors_step0": [], "errors_step1": [],
+               "kept_step0": 0, "kept_step1": 0}
     d = DeviceSolver(device)
-    kw = dict(tol=1e-8, max_iter=max_iter)
+    kw = dict(tol=tol, max_iter=max_iter)
     try:
         for c0 in range(0, n_scenes, chunk):
             k = min(chunk, n_scenes - c0)
@@ -46,22 +52,29 @@ def generate(n_scenes: int, seed: int = 1000, lo=(5, 5, 5), hi=(30, 30, 30), per
             d.load_batch(scenes)
             o1 = d.solve_batch(**kw)
             r1, _ = d.get_batch()
-            for sc, r in zip(scenes, r1):
+            for j, (sc, r) in enumerate(zip(scenes, r1)):
+                if o1["info"][j] != 0:
+                    continue  # FP64 error above tol: no pairs from this solve
                 X = host_features(sc.nc, sc.rowptr, sc.colidx, sc.blocks, sc.q, sc.mu, None, sc.gap)
                 sel = rng.permutation(sc.nc)[:per_scene]
                 Xs.append(X[sel])
                 Ts.append(r.reshape(-1, 3)[sel].astype(np.float32))
+                summary["kept_step0"] += 1
             for j, sc in enumerate(scenes):
                 sc.perturb(seed * 7919 + c0 + j, walk_std)
             d.set_q_mu(np.concatenate([sc.q for sc in scenes]), np.concatenate([sc.mu for sc in scenes]))
             d.set_r(np.concatenate(r1))
             o2 = d.solve_batch(**kw)
             r2, _ = d.get_batch()
-            for sc, rp, r in zip(scenes, r1, r2):
+            for j, (sc, rp, r) in enumerate(zip(scenes, r1, r2)):
+                if o1["info"][j] != 0 or o2["info"][j] != 0:
+                    continue
                 X = host_features(sc.nc, sc.rowptr, sc.colidx, sc.blocks, sc.q, sc.mu, rp, sc.gap)
                 sel = rng.permutation(sc.nc)[:per_scene]
                 Xs.append(X[sel])
-                Ts.append(r.reshape(-1, 3)[sel].astype(np.float32))
+                t = r.reshape(-1, 3)[sel] - (rp.reshape(-1, 3)[sel] if residual else 0.0)
+                Ts.append(t.astype(np.float32))
+                summary["kept_step1"] += 1
             summary["scenes"] += k
             summary["contacts"] += int(sum(sc.nc for sc in scenes))
             summary["solves"] += 2 * k
@@ -85,10 +98,11 @@ def generate(n_scenes: int, seed: int = 1000, lo=(5, 5, 5), hi=(30, 30, 30), per
 
 
 def train(X, T, epochs: int = 20, batch: int = 4096, lr: float = 2e-3, wd: float = 1e-4, seed: int = 0,
-          device: int = 0, log=None):
+          device: int = 0, log=None, residual: bool = False):
     rng = np.random.default_rng(seed)
     val = rng.choice(len(X), max(1, len(X) // 50), replace=False)
     m = WarmStartMLP(device)
+    m.residual(residual)
     m.set_params(init_params(seed), make_stats(X, T))
     m.set_data(X, T)
     t = time.perf_counter()
@@ -104,7 +118,9 @@ def main(argv=None):
     ap.add_argument("--hi", type=int, default=30)
     ap.add_argument("--per-scene", type=int, default=2048)
     ap.add_argument("--chunk", type=int, default=128)
-    ap.add_argument("--max-iter", type=int, default=300)
+    ap.add_argument("--max-iter", type=int, default=10000)
+    ap.add_argument("--tol", type=float, default=1e-3)
+    ap.add_argument("--residual", action="store_true", help="targets: change of the reaction from the previous step")
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=2e-3)
@@ -115,9 +131,10 @@ def main(argv=None):
         print(json.dumps(row), flush=True)
 
     t0 = time.perf_counter()
-    X, T, summary = generate(a.scenes, a.seed, (a.lo,) * 3, (a.hi,) * 3, a.per_scene, a.chunk, a.max_iter, log=log)
+    X, T, summary = generate(a.scenes, a.seed, (a.lo,) * 3, (a.hi,) * 3, a.per_scene, a.chunk, a.max_iter, log=log,
+                             tol=a.tol, residual=a.residual)
     t_gen = time.perf_counter() - t0
-    m, hist, t_train = train(X, T, a.epochs, a.batch, a.lr, log=log)
+    m, hist, t_train = train(X, T, a.epochs, a.batch, a.lr, log=log, residual=a.residual)
     cfg = dict({k: v for k, v in vars(a).items() if k != "out"}, samples=len(X), generate_s=t_gen,
                train_s=t_train, **summary)
     log({"config": cfg, "final": hist[-1]})

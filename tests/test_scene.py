@@ -49,3 +49,26 @@ def test_golden_lattice_matches_generator(built_lib):
     z = np.load(GOLDEN / "lattice_5x5x6_s1.npz")
     s = scene.lattice(5, 5, 6, seed=1)
     assert np.array_equal(s.blocks, z["blocks"]) and np.array_equal(s.q, z["q"])
+
+
+@pytest.mark.parametrize("dims, seed, mu", [((5, 5, 6), 1, 0.5), ((7, 3, 4), 11, 0.3), ((3, 3, 2), 2, 0.9)])
+def test_oracle_generator_equals_package_generator(built_lib, dims, seed, mu):
+    """The generator compiled into the oracle library (what the benchmark's
+    reference arm uses, so that it loads no solver library) gives the arrays
+    of siconos_gb300.scene.lattice bit for bit."""
+    import oracle as O
+    from siconos_gb300 import scene as sc
+    P = O.lattice(*dims, seed=seed, mu=mu)
+    s = sc.lattice(*dims, seed=seed, mu=mu)
+    assert P.nc == s.nc
+    for a, b in ((P.rowptr, s.rowptr), (P.colidx, s.colidx), (P.blocks, s.blocks), (P.q, s.q), (P.mu, s.mu)):
+        assert np.array_equal(a, b)
+
+
+def test_batch_specs_match_batch_scenes(built_lib):
+    from siconos_gb300 import scene as sc
+    specs = sc.batch_specs(count=6, seed=3)
+    scenes = sc.batch_scenes(count=6, seed=3)
+    for (d, seed, mu), s in zip(specs, scenes):
+        t = sc.lattice(*d, seed=seed, mu=mu)
+        assert t.nc == s.nc and np.array_equal(t.q, s.q) and float(s.mu[0]) == mu
