@@ -616,10 +616,10 @@ def test_autotuner_mode2_chooses_among_all_lanes(gpu):
     try:
         gpu.load(s)
         gpu.zero_r()
-        st = gpu.solve(tol=1e-6, max_iter=5000)
+        st = gpu.solve(tol=1e-3, max_iter=5000)
         t = gpu.tuning()
         assert t is not None and t["lanes32"] in (1, 2, 4, 8) and t["lanes64"] in (1, 2, 4, 8)
         assert all(np.isfinite(v) for v in t["ms_sweep64"].values())
-        assert st["info"] == 0 and st["error"] <= 1e-6
+        assert st["info"] == 0 and st["error"] <= 1e-3
     finally:
         gpu.autotune(prev)
