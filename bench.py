@@ -623,7 +623,7 @@ def run_ours(args):
 
     cpu = None
     extra = {}
-    if rank == 0:
+    if rank == 0 and not args.no_extras:
         # the same solve with FP64 sweeps (the reference's arithmetic) and with
         # the learned warm start, to the same FP64-verified tolerance
         from siconos_gb300.learned import WarmStartMLP, warm_start
@@ -659,21 +659,22 @@ def run_ours(args):
             "reached": reached and st64["info"] == 0 and stl["info"] == 0,
             "final_error": max(st["error"] for st in stats),
         }
-        if args.cpu_sweeps > 0:
-            import oracle as O
-            P0 = O.Problem(s.nc, s.rowptr, s.colidx, s.blocks, s.q, s.mu)
-            dt, _ = cpu_sample(P0, args.cpu_sweeps, False)
-            cpu = {"value": s.nc * args.cpu_sweeps / dt, "unit": "contact-sweeps/s", "cores": 1, "kind": "port",
-                   "sample": f"the first {args.cpu_sweeps} sequential NSGS sweeps of the same {s.nc}-contact solve "
-                             f"(CPU restatement, bit-exact with the reference's fc3d_nsgs, -O3)"}
-            # the reference's own fc3d_nsgs needs ref_sweeps sweeps to the same
-            # tolerance on this scene (recorded from oracle/_ref by
-            # tests/golden/make_golden.py): its time to tolerance at the
-            # sampled per-sweep time
-            ref_sweeps = _reference_sweeps_to_tol()
-            if ref_sweeps:
-                extra["sweeps_to_tol"]["reference_cpu"] = ref_sweeps
-                extra["time_to_tol_ms"]["reference_cpu_1core_est"] = 1e3 * dt / args.cpu_sweeps * ref_sweeps
+    if rank == 0 and args.cpu_sweeps > 0:
+        import oracle as O
+        P0 = O.Problem(s.nc, s.rowptr, s.colidx, s.blocks, s.q, s.mu)
+        dt, _ = cpu_sample(P0, args.cpu_sweeps, False)
+        cpu = {"value": s.nc * args.cpu_sweeps / dt, "unit": "contact-sweeps/s", "cores": 1, "kind": "port",
+               "sample": f"the first {args.cpu_sweeps} sequential NSGS sweeps of the same {s.nc}-contact solve "
+                         f"(CPU restatement, bit-exact with the reference's fc3d_nsgs, -O3)"}
+        # the reference's own fc3d_nsgs needs ref_sweeps sweeps to the same
+        # tolerance on this scene (recorded from oracle/_ref by
+        # tests/golden/make_golden.py): its time to tolerance at the sampled
+        # per-sweep time
+        ref_sweeps = _reference_sweeps_to_tol()
+        if ref_sweeps:
+            extra.setdefault("sweeps_to_tol", {})["reference_cpu"] = ref_sweeps
+            extra.setdefault("time_to_tol_ms", {"tol": TOL})["reference_cpu_1core_est"] = \
+                1e3 * dt / args.cpu_sweeps * ref_sweeps
     if rank == 0:
         clocks = clk.summary()
         line = {
@@ -779,7 +780,7 @@ def main():
     ap.add_argument("--cpu-sweeps", type=int, default=100,
                     help="sweeps of the CPU sample (per step for --impl reference, capped at 10 there)")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the time-to-tolerance, batched and time-stepping measurements")
+                    help="skip the comparison solves (FP64, learned start) and the supplementary measurements")
     ap.add_argument("--supplementary", choices=sorted(SUPPLEMENTARY), default=None,
                     help="run only this supplementary measurement and print its JSON")
     ap.add_argument("--profile", choices=["flow", "fp64", "mlp", "infer"], default=None,
