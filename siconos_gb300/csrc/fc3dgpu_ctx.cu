@@ -593,6 +593,7 @@ __global__ void k_get_r_u(int nc, const int* __restrict__ iperm, const double* _
 
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <memory>
 #include <thread>
 #include <vector>
@@ -728,6 +729,7 @@ struct fc3dgpu_ctx {
   BUF(int, flow_dptr);
   BUF(int, flow_dep);
   BUF(unsigned, flow_done);
+  BUF(int2, flow_need);
   BUF(int, flow_sptr);
   BUF(double, flow_part);
   // batched problems (0 = a single problem)
@@ -883,7 +885,7 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64, c->feat,
                   c->prop, c->rbak, c->gapo, c->cbA, c->cbB, c->cframe, c->cpoint, c->bpos, c->bmass,
                   c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum, c->wtmp, c->wdiff,
-                  c->flow_dptr, c->flow_dep, c->flow_done, c->flow_sptr, c->flow_part};
+                  c->flow_dptr, c->flow_dep, c->flow_done, c->flow_need, c->flow_sptr, c->flow_part};
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1711,7 +1713,7 @@ static int prepare_flow(fc3dgpu_ctx* c) {
   CK(ensure(&c->flow_sptr, &c->flow_sptr_cap, FC3D_MAX_COLOURS + 1));
   CK(ensure(&c->flow_part, &c->flow_part_cap, 1024 * 8));
   CK(cudaMemcpyAsync(c->flow_sptr, c->sptr, sizeof(int) * (FC3D_MAX_COLOURS + 1), cudaMemcpyHostToDevice, s));
-  // counts, their prefix sum on the host, then the lists
+  // column-slab counts, their prefix sum on the host, then the lists
   CK(build_flow_deps(nslab, c->npad, c->ncol, c->flow_sptr, c->perm, c->slab_nslot, c->slab_off, c->col, nullptr,
                      c->flow_dptr, nullptr, s));
   std::vector<int> ptr((size_t)nslab + 1, 0);
@@ -1722,6 +1724,46 @@ static int prepare_flow(fc3dgpu_ctx* c) {
   CK(cudaMemcpyAsync(c->flow_dptr, ptr.data(), sizeof(int) * (nslab + 1), cudaMemcpyHostToDevice, s));
   CK(build_flow_deps(nslab, c->npad, c->ncol, c->flow_sptr, c->perm, c->slab_nslot, c->slab_off, c->col,
                      c->flow_dptr, nullptr, c->flow_dep, s));
+  std::vector<int> cols((size_t)std::max(ptr[nslab], 1));
+  CK(cudaMemcpyAsync(cols.data(), c->flow_dep, sizeof(int) * ptr[nslab], cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  // Symmetric lists: the slabs s takes columns from and the slabs that take
+  // columns from s (the same sets when W's block pattern is symmetric, as a
+  // Delassus operator's is).  A finished slab signals every slab of its
+  // list, and a slab of a later colour that s reads must wait for s even
+  // when it does not read s.
+  std::vector<int> rptr((size_t)nslab + 1, 0);
+  for (int k = 0; k < ptr[nslab]; k++) rptr[(cols[k] & 0x7fffffff) + 1]++;
+  for (int k = 0; k < nslab; k++) rptr[k + 1] += rptr[k];
+  std::vector<int> rev((size_t)std::max(rptr[nslab], 1)), fill(rptr.begin(), rptr.end() - 1);
+  for (int t = 0; t < nslab; t++)  // ascending t: each reverse list comes out sorted
+    for (int k = ptr[t]; k < ptr[t + 1]; k++) rev[fill[cols[k] & 0x7fffffff]++] = t;
+  auto colour_of = [&](int sl) { return (int)(std::upper_bound(c->sptr, c->sptr + c->ncol + 1, sl) - c->sptr) - 1; };
+  std::vector<int> sym, sptr_sym((size_t)nslab + 1, 0);
+  std::vector<int2> need((size_t)nslab);
+  sym.reserve((size_t)ptr[nslab] + 16);
+  for (int t = 0; t < nslab; t++) {
+    const int ct = colour_of(t);
+    int a = ptr[t], b = rptr[t], nhi = 0;
+    const size_t start = sym.size();
+    while (a < ptr[t + 1] || b < rptr[t + 1]) {
+      const int x = a < ptr[t + 1] ? (cols[a] & 0x7fffffff) : INT_MAX;
+      const int y = b < rptr[t + 1] ? rev[b] : INT_MAX;
+      const int d = std::min(x, y);
+      if (x == d) a++;
+      if (y == d) b++;
+      const bool hi = colour_of(d) > ct;
+      nhi += hi;
+      sym.push_back(hi ? (int)((unsigned)d | 0x80000000u) : d);
+    }
+    sptr_sym[t + 1] = (int)sym.size();
+    need[t] = make_int2((int)(sym.size() - start), nhi);
+  }
+  CK(ensure(&c->flow_dep, &c->flow_dep_cap, std::max(sym.size(), (size_t)1)));
+  CK(ensure(&c->flow_need, &c->flow_need_cap, (size_t)nslab));
+  CK(cudaMemcpyAsync(c->flow_dptr, sptr_sym.data(), sizeof(int) * (nslab + 1), cudaMemcpyHostToDevice, s));
+  if (!sym.empty()) CK(cudaMemcpyAsync(c->flow_dep, sym.data(), sizeof(int) * sym.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->flow_need, need.data(), sizeof(int2) * nslab, cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
   c->launches += 2;
   c->flow_nw = nw;
@@ -1970,6 +2012,7 @@ static int solve_impl(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgpu_stats* st
       f.dptr = c->flow_dptr;
       f.dep = c->flow_dep;
       f.done = c->flow_done;
+      f.need = c->flow_need;
       f.part = c->flow_part;
       f.maxslot = c->flow_maxslot;
       f.buf_bytes = flow_buf_bytes(c->flow_maxslot);

@@ -5,18 +5,27 @@
 // a sweep by block-level barriers, so every colour costs the slowest
 // neighbour block's whole phase.  Here each warp owns whole 32-row slabs
 // (slab s goes to warp s mod warps, so a warp meets its slabs in colour
-// order) and each slab carries a completion counter: done[s] = the number
-// of sweeps in which its rows were updated.  Before updating slab s in
-// sweep k a warp waits, for every slab d holding a column of one of its
-// rows, until
+// order).  Slab s must not start sweep k before, for every slab d holding
+// a column of one of its rows (and every slab holding a row that reads one
+// of s's columns: the neighbour lists are made symmetric),
 //
-//   done[d] >= k      when d has an earlier colour (its new reactions),
-//   done[d] >= k - 1  when d has a later colour (its previous reactions,
-//                     read before d may overwrite them: d waits for s),
+//   d has updated its rows in sweep k      when d has an earlier colour,
+//   d has updated its rows in sweep k - 1  when d has a later colour (its
+//                     previous reactions, read before d may overwrite
+//                     them: d waits for s),
 //
 // which is exactly the order of the sequential sweep in colour order
 // (fc3d_nsgs.c:711-875 visiting the contacts colour by colour): every row
-// reads the reactions a sequential sweep would read.  The (sweep, colour)
+// reads the reactions a sequential sweep would read.
+//
+// Each slab carries an arrival counter that every neighbour increments
+// after each of its updates.  A neighbour of an earlier colour cannot
+// update sweep k + 1 before s has updated sweep k, and one of a later colour
+// cannot update sweep k before s has, so while s waits for sweep k its
+// counter never exceeds  n * k - n_later  (n neighbours, n_later of them of
+// a later colour) and reaches it exactly when all of them are done: one
+// acquire load of the slab's own counter replaces a load per neighbour.
+// The (sweep, colour)
 // order of the waits is acyclic and every warp is resident (cooperative
 // launch), so the earliest unfinished slab can always proceed.  The light
 // error of a sweep (fc3d_nsgs.c:80-96) and the stop rules still need one
@@ -31,7 +40,7 @@
 
 namespace fc3dgpu {
 
-// Polls of a slab's column counters before a warp starts to back off, and
+// Polls of a slab's arrival counter before a warp starts to back off, and
 // the back-off (ns) between later polls.
 #define FC3D_FLOW_SPIN 1024
 #define FC3D_FLOW_SLEEP_NS 64
@@ -118,22 +127,14 @@ __device__ __forceinline__ bool grid_wait(const unsigned* flags, unsigned e, uns
   return s_ok != 0;
 }
 
-// Wait until every slab slab s takes columns from has reached the state
-// sweep k needs (see the header).  Acquire loads of the counters (the
-// writers release them after their reactions), no fence: the caller's
-// __syncwarp orders the other lanes' reads after them.
-__device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned k,
+// Wait until every neighbour slab of s has reached the state sweep k needs
+// (see the header): one acquire load of s's arrival counter by every lane
+// (one request for the warp) per poll.
+__device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned target,
                                                int lane) {
-  const int d0 = __ldg(&f.dptr[s]), d1 = __ldg(&f.dptr[s + 1]);
   unsigned long long n = 0;
   bool ok = true;
-  for (;;) {
-    bool mine = true;
-    for (int i = d0 + lane; i < d1; i += 32) {
-      const int d = __ldg(&f.dep[i]);
-      mine &= ld_acquire_u32(&f.done[d & 0x7fffffff]) >= (d < 0 ? k - 1 : k);
-    }
-    if (__all_sync(0xffffffffu, mine)) break;
+  while (ld_acquire_u32(&f.done[s]) < target) {
     if (++n > a.spin_limit) {
       ok = false;
       if (lane == 0) atomicOr(a.status, 1);
@@ -141,7 +142,18 @@ __device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const 
     }
     if (n > FC3D_FLOW_SPIN) __nanosleep(FC3D_FLOW_SLEEP_NS);
   }
-  return ok;
+  return __all_sync(0xffffffffu, ok);
+}
+
+// Signal slab s's update to its neighbours: a fence orders the warp's
+// reaction stores (made visible to this lane by the caller's __syncwarp)
+// before the increments, which the waiting warps acquire.
+__device__ __forceinline__ void flow_signal(const FlowArgs& f, int d0, int d1, int dep0, int lane) {
+  __threadfence();
+  for (int i = d0 + lane; i < d1; i += 32) {
+    const int d = i == d0 + lane ? dep0 : __ldg(&f.dep[i]);
+    atomicAdd(&f.done[d & 0x7fffffff], 1u);
+  }
 }
 
 // Row product, take-off test and local solve of the 32 rows of slab s from
@@ -154,6 +166,8 @@ struct FlowRow {
   bool row;
   int ns;
   float ro[3];
+  int d0, d1, dep0;  // the slab's neighbour list, and this lane's first entry
+  unsigned need_a, need_b;  // wait for sweep k: counter >= need_a * k - need_b
 };
 
 __device__ __forceinline__ FlowRow flow_row(const SweepArgs<float>& a, int s, int lane) {
@@ -164,6 +178,15 @@ __device__ __forceinline__ FlowRow flow_row(const SweepArgs<float>& a, int s, in
   x.ro[0] = x.ro[1] = x.ro[2] = 0.f;
   if (x.row) load_r3<float>(a.r, p, x.ro);
   return x;
+}
+
+__device__ __forceinline__ void flow_links(const FlowArgs& f, int s, int lane, FlowRow& x) {
+  x.d0 = __ldg(&f.dptr[s]);
+  x.d1 = __ldg(&f.dptr[s + 1]);
+  x.dep0 = x.d0 + lane < x.d1 ? __ldg(&f.dep[x.d0 + lane]) : 0;
+  const int2 nd = __ldg(&f.need[s]);
+  x.need_a = (unsigned)nd.x;
+  x.need_b = (unsigned)nd.y;
 }
 
 // The new reaction of the lane's row goes to rn (zero on take-off); the
@@ -319,8 +342,9 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
     for (int s = gw; s < a.nslab && !failed; s += tw) {
       unsigned long long* tl = record ? a.timeline + (size_t)s * FC3D_TL_STRIDE : nullptr;
       if (tl) tl[0] = globaltimer_ns();
-      const FlowRow x = flow_row(a, s, lane);
-      if (!flow_wait_deps(a, f, s, (unsigned)sweep, lane)) {
+      FlowRow x = flow_row(a, s, lane);
+      flow_links(f, s, lane, x);
+      if (!flow_wait_deps(a, f, s, x.need_a * (unsigned)sweep - x.need_b, lane)) {
         failed = true;
         break;
       }
@@ -351,7 +375,7 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
       }
       __syncwarp();
       if (tl) tl[4] = globaltimer_ns();
-      if (lane == 0) st_release_u32(&f.done[s], (unsigned)sweep);
+      flow_signal(f, x.d0, x.d1, x.dep0, lane);
     }
     flow_block_sum<2, NW>(acc, f.part + blockIdx.x * 8 + (sweep & 3) * 2);
     e_prev = e_last;

@@ -120,9 +120,10 @@ struct WorkListS {
 #define FC3D_FLOW_MAXSLOT 16
 
 struct FlowArgs {
-  const int* dptr;     // per slab: its column slabs are dep[dptr[s] .. dptr[s + 1])
+  const int* dptr;     // per slab: its neighbour slabs are dep[dptr[s] .. dptr[s + 1])
   const int* dep;      // slab ids, ascending; bit 31 set: a later colour
-  unsigned* done;      // per slab: sweeps completed; zero at launch
+  unsigned* done;      // per slab: neighbour-slab updates signalled to it; zero at launch
+  const int2* need;    // per slab: (neighbour slabs, those of a later colour)
   double* part;        // per block: 4 slots of (sum |dr|^2, sum |r|^2)
   unsigned buf_bytes;  // shared-memory buffer of one warp
   int maxslot;         // slots of one slab the buffer holds

@@ -189,6 +189,38 @@ def test_flow_equals_coloured(gpu, dims):
     np.testing.assert_allclose(t1, t2, rtol=1e-5, atol=0)
 
 
+def test_flow_nonsymmetric_pattern(gpu):
+    """A block pattern that is not symmetric (row i reads contact j, row j
+    does not read i): the dataflow sweep still waits for every slab whose
+    reactions a later-coloured row would overwrite, so it gives the coloured
+    kernel's iterates bit for bit, run after run."""
+    from types import SimpleNamespace
+    from siconos_gb300 import scene
+    s = scene.lattice(20, 20, 10, seed=6)
+    rng = np.random.default_rng(3)
+    keep = np.ones(len(s.colidx), bool)
+    rows = np.repeat(np.arange(s.nc), np.diff(s.rowptr))
+    upper = s.colidx > rows
+    keep[upper] = rng.random(int(upper.sum())) > 0.3
+    counts = np.bincount(rows[keep], minlength=s.nc)
+    rowptr = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    t = SimpleNamespace(nc=s.nc, rowptr=rowptr, colidx=s.colidx[keep].copy(),
+                        blocks=np.asarray(s.blocks).reshape(-1, 9)[keep].copy(), q=s.q, mu=s.mu)
+    gpu.load(t)
+    kw = dict(tol=1e-300, max_iter=25, lanes=1, fp32_only=1, switch_tol=0.0, stall_window=0)
+    out = []
+    for on in (False, True, True, True):
+        prev = gpu.flow(on)
+        gpu.zero_r()
+        st = gpu.solve(**kw)
+        out.append(gpu.get()[0])
+        gpu.flow(prev)
+        assert st["status"] == 0 and st["sweeps32"] == 25
+    assert np.all(np.isfinite(out[0]))
+    for r in out[1:]:
+        assert np.array_equal(r, out[0])
+
+
 def test_flow_timeline_per_slab(gpu):
     """With the dataflow sweep the timeline holds one record per slab:
     increasing timestamps and at most 32 local solves."""
