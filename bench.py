@@ -410,6 +410,51 @@ def rfc3d_tiled(copies=1000, sample_copies=100, tol=1e-8):
             "speedup_vs_cpu": gpu / cpu}
 
 
+def gfc3d_global(dims=(60, 60, 30), tol=1e-4, budget=10000, cpu_iters=10, reps=3):
+    """The global problem (GFC3D NSGS, gfc3d_nsgs.c:62-198) on the sphere
+    lattice in global form (6 dofs per body, bodies of mass 10, inertia 1:
+    the reference's unit-step iteration diverges at unit mass), from r = 0
+    to the reference's default tolerance 1e-4 within 10,000 iterations: the
+    GPU solver (one cooperative launch per solve; device-resident inputs
+    larger than L2) against the CPU restatement of gfc3d_nsgs (bit-exact
+    with the reference, one core) on its first `cpu_iters` iterations.  The
+    roofline: the unpadded bytes one iteration streams (H by rows and by
+    contacts, M, the vectors) over the measured time per iteration."""
+    import oracle as O
+    import siconos_gb300.numerics as sn
+    from siconos_gb300 import scene
+    P = scene.lattice_global(*dims, seed=SEED, mu=MU)
+    ctx = sn.Gfc3dContext.from_problem(P)
+    try:
+        info = ctx.info()
+        ctx.set_start()
+        ctx.solve(tol, 20)
+        runs = []
+        for _ in range(reps):
+            ctx.set_start()
+            runs.append(ctx.solve(tol, budget))
+        ctx.set_start()
+        fixed = ctx.solve(0.0, 200)
+    finally:
+        ctx.close()
+    res = sorted(runs, key=lambda x: x["ms"])[len(runs) // 2]
+    ms_it = fixed["ms"] / fixed["iterations"]
+    peak, peak_kind = _peaks()
+    achieved = info["bytes_per_iteration"] / (ms_it / 1e3) / 1e9
+    Q = O.lattice_global(*dims, seed=SEED, mu=MU)
+    t = time.perf_counter()
+    O.gfc3d_nsgs_port(Q, tol=0.0, maxiter=cpu_iters)
+    cpu_it_s = (time.perf_counter() - t) / cpu_iters
+    return {"dofs": P.n, "contacts": P.nc, "nnz_H": int(P.Hp[-1]), "tol": tol, "budget": budget,
+            "gpu": {"ms": res["ms"], "iterations": res["iterations"], "info": res["info"], "error": res["error"],
+                    "ms_per_iteration": ms_it, "contact_iterations_per_s": P.nc / (ms_it / 1e3)},
+            "roofline": {"bound": "hbm", "bytes_per_iteration": info["bytes_per_iteration"], "achieved": achieved,
+                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak},
+            "cpu_reference_port_1core": {"iterations_sampled": cpu_iters, "ms_per_iteration": 1e3 * cpu_it_s,
+                                         "time_to_tol_est_ms": 1e3 * cpu_it_s * res["iterations"]},
+            "speedup_vs_cpu": cpu_it_s * 1e3 / ms_it}
+
+
 def _cpu_scene(spec):
     """One scene of the batch on one host core: the reference's sequential
     NSGS (the restatement) for at most `sweeps` sweeps, tol 1e-8."""
@@ -699,6 +744,7 @@ def run_ours(args):
                             ("batched_512_scenes", batched_c3),
                             ("time_stepping_80x80x40", time_stepping_c5),
                             ("fc2d_granular_7002", fc2d_granular),
+                            ("gfc3d_global_60x60x30", gfc3d_global),
                             ("rfc3d_rockfall_x1000", rfc3d_tiled)):
                 try:
                     sup[key] = fn()
@@ -721,9 +767,22 @@ def profile_case(name):
     flow     nsgs_flow_kernel, 5 FP32 sweeps of the 60x60x30 lattice;
     fp64     nsgs_kernel<double,1>, 3 FP64 sweeps of the same lattice;
     mlp      k_train_tile_tc, one training step on 16,384 samples;
-    infer    k_infer_tc on 320,400 samples."""
+    infer    k_infer_tc on 320,400 samples;
+    gfc3d    k_gfc3d, 20 iterations of the 60x60x30 lattice in global form."""
     from siconos_gb300 import build as B
     B.build()
+    if name == "gfc3d":
+        import siconos_gb300.numerics as sn
+        from siconos_gb300 import scene
+        P = scene.lattice_global(*DIMS, seed=SEED, mu=MU)
+        ctx = sn.Gfc3dContext.from_problem(P)
+        try:
+            for _ in range(2):
+                ctx.set_start()
+                st = ctx.solve(0.0, 20)
+            return {"profile": name, "ms": st["ms"], "iterations": st["iterations"], **ctx.info()}
+        finally:
+            ctx.close()
     if name in ("flow", "fp64"):
         from siconos_gb300.device import DeviceSolver
         import oracle as O
@@ -768,6 +827,7 @@ SUPPLEMENTARY = {
     "rfc3d_rockfall_x1000": lambda: rfc3d_tiled(),
     "batched_512_scenes": lambda: batched_c3(),
     "time_stepping_80x80x40": lambda: time_stepping_c5(),
+    "gfc3d_global_60x60x30": lambda: gfc3d_global(),
 }
 
 
@@ -783,7 +843,7 @@ def main():
                     help="skip the comparison solves (FP64, learned start) and the supplementary measurements")
     ap.add_argument("--supplementary", choices=sorted(SUPPLEMENTARY), default=None,
                     help="run only this supplementary measurement and print its JSON")
-    ap.add_argument("--profile", choices=["flow", "fp64", "mlp", "infer"], default=None,
+    ap.add_argument("--profile", choices=["flow", "fp64", "mlp", "infer", "gfc3d"], default=None,
                     help="run a small case for an ncu capture and print its JSON")
     args = ap.parse_args()
     if args.profile:

@@ -53,6 +53,24 @@ int fc3dgpu_lattice_fill_geometry(const fc3dgpu_lattice *L, double *gap, int32_t
 int fc3dgpu_lattice_fill_contacts(const fc3dgpu_lattice *L, double *frame, double *point, double *body_pos,
                                   double *body_mass, double *body_inertia, double *vel);
 
+/* The same scene in the global form of the reference's
+ * GlobalFrictionContactProblem (M v = q + H r, u = H^T v + b): 6 degrees of
+ * freedom per body (linear then angular velocity), M = diag(m I3, I I3),
+ * H (6 nb x 3 nc) with, for contact c on body b (sign s = +1 for body B, -1
+ * for body A, arm d = contact point - centre, frame rows R_0..R_2),
+ * H[6b + a, 3c + k] = s R_k[a] and H[6b + 3 + a, 3c + k] = s (d x R_k)[a],
+ * so that H^T M^-1 H is the W of fc3dgpu_lattice_fill_W divided by
+ * mass_scale, the factor applied to every mass and inertia (the reference's
+ * global NSGS takes unit steps, r <- proj(r - u), and diverges once W has
+ * an eigenvalue above 2: about 19 at unit mass, so 10 is the scale of the
+ * global benchmark); q = M (v + h g), b = 0.  Sizes: n = 6 nb,
+ * nnz(M) = n, nnz(H) = 18 x (body-contact incidences). */
+int fc3dgpu_lattice_global_sizes(const fc3dgpu_lattice *L, int64_t *n, int64_t *nnzH);
+/* M and H as CSR (row pointers n + 1, ascending columns, values), q[n],
+ * b[3 nc]. */
+int fc3dgpu_lattice_fill_global(const fc3dgpu_lattice *L, double h, double mass_scale, int64_t *Mp, int64_t *Mi, double *Mx,
+                                int64_t *Hp, int64_t *Hi, double *Hx, double *q, double *b);
+
 /* Random walk of the body velocities: v += N(0, std^2) per degree of
  * freedom, from its own stream seeded by seed. */
 int fc3dgpu_lattice_perturb_velocities(fc3dgpu_lattice *L, uint64_t seed, double std);

@@ -13,6 +13,7 @@
  *                                members up to `version` are read)
  *   FrictionContactProblem       FrictionContact/FrictionContactProblem.h:33-46
  *   RollingFrictionContactProblem RollingFrictionContact/RollingFrictionContactProblem.h:33-53
+ *   GlobalFrictionContactProblem FrictionContact/GlobalFrictionContactProblem.h:34-66
  *   Callback, SolverOptions      core/SolverOptions.h:36-91
  */
 #ifndef SICONOS_NUMERICS_ABI_H
@@ -81,6 +82,22 @@ typedef struct RollingFrictionContactProblem {
   double *mu_r;
 } RollingFrictionContactProblem;
 
+/* FrictionContact/GlobalFrictionContactProblem.h:34-66 */
+typedef struct GlobalFrictionContactProblem {
+  int dimension;
+  int numberOfContacts;
+  NumericsMatrix *M;
+  NumericsMatrix *H;
+  double *q;
+  double norm_q;
+  double *b;
+  double norm_b;
+  double *mu;
+  NumericsMatrix *M_inverse;
+  char *name;
+  void *env;
+} GlobalFrictionContactProblem;
+
 typedef struct {
   void *env;
   void (*collectStatsIteration)(void *env, size_t size, double *reaction, double *velocity, double error,
@@ -114,6 +131,7 @@ typedef struct SolverOptions {
 #define SICONOS_ROLLING_FRICTION_3D_NSGS 3000
 #define SICONOS_ROLLING_FRICTION_3D_ONECONTACT_NSN 3003
 #define SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID 565
+#define SICONOS_GLOBAL_FRICTION_3D_NSGS 605
 
 /* generic indices (SolverOptions.h:94-121) */
 #define SICONOS_IPARAM_MAX_ITER 0

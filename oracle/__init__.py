@@ -431,3 +431,201 @@ def rfc3d_compute_error_ref(P: RollingProblem, r) -> tuple[float, np.ndarray]:
     u = np.zeros(5 * P.nc)
     e = ref().ref_rfc3d_compute_error(*P.arrays(), np.ascontiguousarray(r, np.float64), u)
     return e, u
+
+
+# ---- global 3D friction contact (M v = q + H r, u = H^T v + b) --------------
+@dataclass
+class GlobalProblem:
+    """A global friction-contact problem: M (n x n) and H (n x 3 nc) as CSR
+    (row pointers, ascending column indices, values), q[n], b[3 nc], mu[nc]."""
+
+    n: int
+    nc: int
+    Mp: np.ndarray
+    Mi: np.ndarray
+    Mx: np.ndarray
+    Hp: np.ndarray
+    Hi: np.ndarray
+    Hx: np.ndarray
+    q: np.ndarray
+    b: np.ndarray
+    mu: np.ndarray
+
+    @staticmethod
+    def from_dense(M, H, q, b, mu) -> "GlobalProblem":
+        M = np.asarray(M, np.float64)
+        H = np.asarray(H, np.float64)
+        n = M.shape[0]
+        nc = H.shape[1] // 3
+
+        def csr(A):
+            p = np.zeros(A.shape[0] + 1, np.int64)
+            rows, cols = np.nonzero(A)
+            np.add.at(p, rows + 1, 1)
+            return np.cumsum(p), cols.astype(np.int64), A[rows, cols].astype(np.float64)
+
+        return GlobalProblem(n, nc, *csr(M), *csr(H), np.ascontiguousarray(q, np.float64),
+                             np.ascontiguousarray(b, np.float64), np.ascontiguousarray(mu, np.float64))
+
+    def dense(self):
+        M = np.zeros((self.n, self.n))
+        H = np.zeros((self.n, 3 * self.nc))
+        for i in range(self.n):
+            M[i, self.Mi[self.Mp[i]:self.Mp[i + 1]]] = self.Mx[self.Mp[i]:self.Mp[i + 1]]
+            H[i, self.Hi[self.Hp[i]:self.Hp[i + 1]]] = self.Hx[self.Hp[i]:self.Hp[i + 1]]
+        return M, H
+
+    def arrays(self):
+        c = np.ascontiguousarray
+        return (self.n, self.nc, c(self.Mp, np.int64), c(self.Mi, np.int64), c(self.Mx, np.float64),
+                c(self.Hp, np.int64), c(self.Hi, np.int64), c(self.Hx, np.float64), c(self.q, np.float64),
+                c(self.b, np.float64), c(self.mu, np.float64))
+
+
+@dataclass
+class GlobalResult:
+    info: int
+    iterations: int  # -1 where the solver does not report it (the reference's)
+    error: float
+    r: np.ndarray
+    u: np.ndarray
+    v: np.ndarray
+    trace: np.ndarray
+
+
+def _gport():
+    lib = port()
+    if not getattr(lib, "_gfc3d_typed", False):
+        lib.oracle_gfc3d_nsgs.restype = C.c_int
+        lib.oracle_gfc3d_nsgs.argtypes = [C.c_int64, C.c_int, _I64, _I64, _F64, _I64, _I64, _F64, _F64, _F64, _F64,
+                                          _F64, _F64, _F64, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                          C.POINTER(C.c_double), C.c_void_p, C.c_int]
+        lib.oracle_gfc3d_compute_error.restype = C.c_double
+        lib.oracle_gfc3d_compute_error.argtypes = [C.c_int64, C.c_int, _I64, _I64, _F64, _I64, _I64, _F64, _F64,
+                                                   _F64, _F64, _F64, _F64, _F64]
+        lib.oracle_gfc3d_components.restype = C.c_int
+        lib.oracle_gfc3d_components.argtypes = [C.c_int64, _I64, _I64, _I64]
+        lib._gfc3d_typed = True
+    return lib
+
+
+def _gref():
+    lib = ref()
+    if lib is None:
+        raise RuntimeError("oracle/_ref is not built")
+    if not getattr(lib, "_gfc3d_typed", False):
+        lib.ref_gfc3d_dat_open.restype = C.c_void_p
+        lib.ref_gfc3d_dat_open.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int)]
+        lib.ref_gfc3d_dat_get.restype = C.c_int
+        lib.ref_gfc3d_dat_get.argtypes = [C.c_void_p, _F64, _F64, _F64, _F64, _F64]
+        lib.ref_gfc3d_dat_close.argtypes = [C.c_void_p]
+        lib.ref_gfc3d_nsgs.restype = C.c_int
+        lib.ref_gfc3d_nsgs.argtypes = [C.c_int, C.c_int, _F64, _F64, _F64, _F64, _F64, _F64, _F64, _F64, C.c_double,
+                                       C.c_int, C.c_int, C.POINTER(C.c_double)]
+        lib.ref_gfc3d_compute_error.restype = C.c_double
+        lib.ref_gfc3d_compute_error.argtypes = [C.c_int, C.c_int, _F64, _F64, _F64, _F64, _F64, _F64, _F64, _F64]
+        lib._gfc3d_typed = True
+    return lib
+
+
+def read_gfc3d_dat(path: str | Path) -> tuple[GlobalProblem, int, int]:
+    """A GFC3D ``.dat`` fixture read by the reference's own reader; returns
+    the problem and the storage types of M and H in the file."""
+    lib = _gref()
+    n, nc, ms, hs = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    h = lib.ref_gfc3d_dat_open(str(path).encode(), C.byref(n), C.byref(nc), C.byref(ms), C.byref(hs))
+    if not h:
+        raise IOError(f"cannot read {path}")
+    M = np.zeros(n.value * n.value)
+    H = np.zeros(max(n.value * 3 * nc.value, 1))
+    q, b, mu = np.zeros(n.value), np.zeros(max(3 * nc.value, 1)), np.zeros(max(nc.value, 1))
+    rc = lib.ref_gfc3d_dat_get(h, M, H, q, b, mu)
+    lib.ref_gfc3d_dat_close(h)
+    if rc != 0:
+        raise IOError(f"unsupported problem in {path}")
+    m = 3 * nc.value
+    P = GlobalProblem.from_dense(M.reshape(n.value, n.value, order="F"),
+                                 H[: n.value * m].reshape(n.value, m, order="F"), q, b[:m], mu[: nc.value])
+    return P, ms.value, hs.value
+
+
+def gfc3d_nsgs_port(P: GlobalProblem, r0=None, v0=None, tol=1e-8, maxiter=1000, freq=0,
+                    trace_cap=0) -> GlobalResult:
+    """The restatement of gfc3d_nsgs (oracle/gfc3d_oracle.c)."""
+    r = np.zeros(3 * P.nc) if r0 is None else np.ascontiguousarray(r0, np.float64).copy()
+    v = np.zeros(P.n) if v0 is None else np.ascontiguousarray(v0, np.float64).copy()
+    u = np.zeros(3 * P.nc)
+    it, err = C.c_int(), C.c_double()
+    tr = np.zeros(max(trace_cap, 1))
+    info = _gport().oracle_gfc3d_nsgs(*P.arrays(), r, u, v, tol, maxiter, freq, C.byref(it), C.byref(err),
+                                      tr.ctypes.data if trace_cap else None, trace_cap)
+    return GlobalResult(info, it.value, err.value, r, u, v, tr[: min(it.value, trace_cap)].copy())
+
+
+def gfc3d_nsgs_ref(P: GlobalProblem, r0=None, v0=None, tol=1e-8, maxiter=1000, freq=0) -> GlobalResult:
+    """The reference's own gfc3d_nsgs through gfc3d_driver, on dense M and H."""
+    lib = _gref()
+    M, H = P.dense()
+    r = np.zeros(3 * P.nc) if r0 is None else np.ascontiguousarray(r0, np.float64).copy()
+    v = np.zeros(P.n) if v0 is None else np.ascontiguousarray(v0, np.float64).copy()
+    u = np.zeros(max(3 * P.nc, 1))
+    err = C.c_double()
+    info = lib.ref_gfc3d_nsgs(P.n, P.nc, np.asfortranarray(M).reshape(-1, order="F"),
+                              np.ascontiguousarray(np.asfortranarray(H).reshape(-1, order="F")), P.q,
+                              np.ascontiguousarray(P.b) if P.nc else np.zeros(1), P.mu if P.nc else np.zeros(1),
+                              r if P.nc else np.zeros(1), u, v, tol, maxiter, freq, C.byref(err))
+    return GlobalResult(info, -1, err.value, r, u[: 3 * P.nc], v, np.zeros(0))
+
+
+def gfc3d_compute_error_port(P: GlobalProblem, r, v) -> tuple[float, np.ndarray]:
+    u = np.zeros(3 * P.nc)
+    e = _gport().oracle_gfc3d_compute_error(*P.arrays(), np.ascontiguousarray(r, np.float64),
+                                            np.ascontiguousarray(v, np.float64), u)
+    return e, u
+
+
+def gfc3d_compute_error_ref(P: GlobalProblem, r, v) -> tuple[float, np.ndarray]:
+    M, H = P.dense()
+    u = np.zeros(3 * P.nc)
+    e = _gref().ref_gfc3d_compute_error(P.n, P.nc, np.asfortranarray(M).reshape(-1, order="F"),
+                                        np.ascontiguousarray(np.asfortranarray(H).reshape(-1, order="F")), P.q, P.b,
+                                        P.mu, np.ascontiguousarray(r, np.float64),
+                                        np.ascontiguousarray(v, np.float64), u)
+    return e, u
+
+
+def gfc3d_components(P: GlobalProblem) -> tuple[int, np.ndarray]:
+    """Connected components of M's pattern (the blocks M is factorised by)."""
+    comp = np.zeros(P.n, np.int64)
+    k = _gport().oracle_gfc3d_components(P.n, np.ascontiguousarray(P.Mp, np.int64),
+                                         np.ascontiguousarray(P.Mi, np.int64), comp)
+    return k, comp
+
+
+def lattice_global(nx: int, ny: int, nz: int, seed: int = 1, mu: float = 0.5, jitter_std: float = 1e-3,
+                   v0_std: float = 0.1, h: float = 1e-3, mass_scale: float = 10.0) -> GlobalProblem:
+    """The seeded sphere lattice in the global form (M v = q + H r,
+    u = H^T v + b; 6 dofs per body), from the generator compiled into the
+    oracle library (the same source as ``siconos_gb300.scene.lattice_global``)."""
+    L = port()
+    if not getattr(L, "_global_typed", False):
+        L.fc3dgpu_lattice_global_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.fc3dgpu_lattice_fill_global.argtypes = [C.c_void_p, C.c_double, C.c_double, _I64, _I64, _F64, _I64, _I64, _F64, _F64,
+                                                  _F64]
+        L._global_typed = True
+    hdl = L.fc3dgpu_lattice_create(nx, ny, nz, seed, jitter_std, v0_std)
+    if not hdl:
+        raise ValueError("bad lattice size")
+    try:
+        nb, nc, nnzb = C.c_int(), C.c_int(), C.c_int64()
+        L.fc3dgpu_lattice_sizes(hdl, C.byref(nb), C.byref(nc), C.byref(nnzb))
+        n, nh = C.c_int64(), C.c_int64()
+        L.fc3dgpu_lattice_global_sizes(hdl, C.byref(n), C.byref(nh))
+        Mp, Mi, Mx = np.zeros(n.value + 1, np.int64), np.zeros(n.value, np.int64), np.zeros(n.value)
+        Hp, Hi, Hx = np.zeros(n.value + 1, np.int64), np.zeros(nh.value, np.int64), np.zeros(nh.value)
+        q, b = np.zeros(n.value), np.zeros(3 * nc.value)
+        L.fc3dgpu_lattice_fill_global(hdl, h, mass_scale, Mp, Mi, Mx, Hp, Hi, Hx, q, b)
+    finally:
+        L.fc3dgpu_lattice_free(hdl)
+    return GlobalProblem(n.value, nc.value, Mp, Mi, Mx, Hp, Hi, Hx, q, b, np.full(nc.value, float(mu)))

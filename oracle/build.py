@@ -20,7 +20,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build"
 LIB = OUT / "liboracle.so"
-SOURCES = ["fc3d_oracle.c", "colour_oracle.c", "fc2d_oracle.c", "rfc3d_oracle.c"]
+SOURCES = ["fc3d_oracle.c", "colour_oracle.c", "fc2d_oracle.c", "rfc3d_oracle.c", "gfc3d_oracle.c"]
 ROOT = HERE.parent
 GENERATOR = ROOT / "siconos_gb300" / "csrc" / "fc3d_lattice.c"
 

@@ -4,7 +4,9 @@
  * run the unmodified reference fc3d_driver (SICONOS_FRICTION_3D_NSGS,
  * fc3d_nsgs.c:560) and fc3d_compute_error (fc3d_compute_error.c:70) on
  * problems given as block-CSR arrays, and read the reference's .dat
- * fixtures with its own reader (FrictionContactProblem.c:103). */
+ * fixtures with its own reader (FrictionContactProblem.c:103).  The global
+ * problem (gfc3d_driver, SICONOS_GLOBAL_FRICTION_3D_NSGS, gfc3d_nsgs.c:62)
+ * runs on dense M and H. */
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -27,6 +29,9 @@
 #include "rolling_fc_Solvers.h"
 #include "rolling_friction_3d_compute_error.h"
 #include "projectionOnCone.h"
+#include "GlobalFrictionContactProblem.h"
+#include "gfc3d_compute_error.h"
+#include "SiconosBlas.h"
 
 /* Build a 3x3-block SBM that points into caller-owned arrays.  blocks holds
  * nnzb column-major 3x3 blocks in row order, rowptr/colidx the block-CSR
@@ -482,4 +487,102 @@ void ref_rfc3d_dat_close(void *hv) {
   RDatHandle *h = (RDatHandle *)hv;
   rollingFrictionContactProblem_free(h->P);
   free(h);
+}
+
+
+/* ---------------- global FC3D (M v = q + H r, u = H^T v + b) ---------------- */
+
+typedef struct {
+  GlobalFrictionContactProblem *P;
+} GDatHandle;
+
+/* A GFC3D .dat fixture through the reference's reader
+ * (GlobalFrictionContactProblem.c:118); M and H are then read entry by entry
+ * (NM_get_value), whatever their storage. */
+void *ref_gfc3d_dat_open(const char *fname, int *n, int *nc, int *mstorage, int *hstorage) {
+  GlobalFrictionContactProblem *P = globalFrictionContact_new_from_filename(fname);
+  if (!P) return NULL;
+  GDatHandle *h = (GDatHandle *)malloc(sizeof(GDatHandle));
+  h->P = P;
+  *n = P->M->size0;
+  *nc = P->numberOfContacts;
+  *mstorage = (int)P->M->storageType;
+  *hstorage = (int)P->H->storageType;
+  return h;
+}
+
+/* M (n x n) and H (n x 3nc) column-major, q, b, mu. */
+int ref_gfc3d_dat_get(void *hv, double *M, double *H, double *q, double *b, double *mu) {
+  GlobalFrictionContactProblem *P = ((GDatHandle *)hv)->P;
+  const int n = P->M->size0, m = 3 * P->numberOfContacts;
+  if (P->dimension != 3 || P->H->size0 != n || P->H->size1 != m) return -1;
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) M[(size_t)j * n + i] = NM_get_value(P->M, i, j);
+  for (int j = 0; j < m; j++)
+    for (int i = 0; i < n; i++) H[(size_t)j * n + i] = NM_get_value(P->H, i, j);
+  memcpy(q, P->q, sizeof(double) * (size_t)n);
+  memcpy(b, P->b, sizeof(double) * (size_t)m);
+  memcpy(mu, P->mu, sizeof(double) * (size_t)P->numberOfContacts);
+  return 0;
+}
+
+void ref_gfc3d_dat_close(void *hv) {
+  GDatHandle *h = (GDatHandle *)hv;
+  globalFrictionContact_free(h->P);
+  free(h);
+}
+
+static GlobalFrictionContactProblem *make_gfc3d(int n, int nc, const double *M, const double *H, const double *q,
+                                                const double *b, const double *mu) {
+  GlobalFrictionContactProblem *P = globalFrictionContactProblem_new();
+  const int m = 3 * nc;
+  P->dimension = 3;
+  P->numberOfContacts = nc;
+  P->M = NM_create(NM_DENSE, n, n);
+  memcpy(P->M->matrix0, M, sizeof(double) * (size_t)n * (size_t)n);
+  /* the dense LU factors go to a copy of M, not into M itself (by default
+     NM_LU_factorize factorises in place, NumericsMatrix.c:89, :3547, and
+     gfc3d_compute_error would then multiply by the packed factors) */
+  NM_preserve(P->M);
+  P->H = NM_create(NM_DENSE, n, m);
+  memcpy(P->H->matrix0, H, sizeof(double) * (size_t)n * (size_t)(m > 0 ? m : 0));
+  P->q = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  P->b = (double *)malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+  P->mu = (double *)malloc(sizeof(double) * (size_t)(nc > 0 ? nc : 1));
+  memcpy(P->q, q, sizeof(double) * (size_t)n);
+  memcpy(P->b, b, sizeof(double) * (size_t)m);
+  memcpy(P->mu, mu, sizeof(double) * (size_t)nc);
+  return P;
+}
+
+/* gfc3d_driver with SICONOS_GLOBAL_FRICTION_3D_NSGS (defaults of
+ * solver_options_create, then max_iter, tol and the error-evaluation
+ * frequency); r, u, v in/out.  Returns info; *error = dparam[1]. */
+int ref_gfc3d_nsgs(int n, int nc, const double *M, const double *H, const double *q, const double *b,
+                   const double *mu, double *r, double *u, double *v, double tol, int maxiter, int freq,
+                   double *error) {
+  GlobalFrictionContactProblem *P = make_gfc3d(n, nc, M, H, q, b, mu);
+  SolverOptions *o = solver_options_create(SICONOS_GLOBAL_FRICTION_3D_NSGS);
+  o->iparam[SICONOS_IPARAM_MAX_ITER] = maxiter;
+  o->dparam[SICONOS_DPARAM_TOL] = tol;
+  o->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY] = freq;
+  int info = gfc3d_driver(P, r, u, v, o);
+  *error = o->dparam[SICONOS_DPARAM_RESIDU];
+  solver_options_delete(o);
+  globalFrictionContact_free(P);
+  return info;
+}
+
+/* gfc3d_compute_error (gfc3d_compute_error.c:38) of (r, v); writes u. */
+double ref_gfc3d_compute_error(int n, int nc, const double *M, const double *H, const double *q, const double *b,
+                               const double *mu, const double *r, const double *v, double *u) {
+  GlobalFrictionContactProblem *P = make_gfc3d(n, nc, M, H, q, b, mu);
+  SolverOptions *o = solver_options_create(SICONOS_GLOBAL_FRICTION_3D_NSGS);
+  double e = 0.0;
+  const int m = 3 * nc;
+  gfc3d_compute_error(P, (double *)r, u, (double *)v, 1e-300, o, cblas_dnrm2(n, P->q, 1), cblas_dnrm2(m, P->b, 1),
+                      &e);
+  solver_options_delete(o);
+  globalFrictionContact_free(P);
+  return e;
 }

@@ -7,6 +7,7 @@
 #include <math.h>
 #include <stddef.h>
 #include "cblas.h"
+#include "lapacke.h"
 
 double cblas_dnrm2(const blasint n, const double *x, const blasint incx) {
   double s = 0.0;
@@ -104,4 +105,70 @@ void cblas_dtrsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const
     if (Diag == CblasNonUnit) v /= (TransA == CblasNoTrans ? at(order, A, lda, i, i) : at(order, A, lda, i, i));
     X[(size_t)i * incX] = v;
   }
+}
+
+/* Dense LU for the reference's NM_LU_factorize / NM_LU_solve on NM_DENSE
+ * matrices (NumericsMatrix.c:3543-3590, :3699-3735), column-major only:
+ * unblocked right-looking elimination, first largest pivot, multipliers by
+ * division; on an exactly zero pivot the column is skipped and info records
+ * it.  dgetrs applies the row swaps in order, then the unit-lower forward
+ * substitution (ascending columns) and the upper back substitution
+ * (descending columns, then the division by the pivot).  The CPU restatement
+ * in gfc3d_oracle.c factorises and solves in the same order. */
+lapack_int LAPACKE_dgetrf(int layout, lapack_int m, lapack_int n, double *a, lapack_int lda, lapack_int *ipiv) {
+  lapack_int info = 0;
+  if (layout != LAPACK_COL_MAJOR) return -1;
+  lapack_int mn = m < n ? m : n;
+  for (lapack_int j = 0; j < mn; j++) {
+    lapack_int p = j;
+    double best = -1.0;
+    for (lapack_int i = j; i < m; i++)
+      if (fabs(a[(size_t)j * lda + i]) > best) {
+        best = fabs(a[(size_t)j * lda + i]);
+        p = i;
+      }
+    ipiv[j] = p + 1;
+    if (a[(size_t)j * lda + p] == 0.0) {
+      if (!info) info = j + 1;
+      continue;
+    }
+    if (p != j)
+      for (lapack_int k = 0; k < n; k++) {
+        double t = a[(size_t)k * lda + j];
+        a[(size_t)k * lda + j] = a[(size_t)k * lda + p];
+        a[(size_t)k * lda + p] = t;
+      }
+    for (lapack_int i = j + 1; i < m; i++) a[(size_t)j * lda + i] = a[(size_t)j * lda + i] / a[(size_t)j * lda + j];
+    for (lapack_int k = j + 1; k < n; k++)
+      for (lapack_int i = j + 1; i < m; i++)
+        a[(size_t)k * lda + i] = a[(size_t)k * lda + i] - a[(size_t)j * lda + i] * a[(size_t)k * lda + j];
+  }
+  return info;
+}
+
+lapack_int LAPACKE_dgetrs(int layout, char trans, lapack_int n, lapack_int nrhs, const double *a, lapack_int lda,
+                          const lapack_int *ipiv, double *b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR || (trans != 'N' && trans != 'n')) return -1;
+  for (lapack_int c = 0; c < nrhs; c++) {
+    double *x = b + (size_t)c * ldb;
+    for (lapack_int i = 0; i < n; i++) {
+      lapack_int p = ipiv[i] - 1;
+      if (p != i) {
+        double t = x[i];
+        x[i] = x[p];
+        x[p] = t;
+      }
+    }
+    for (lapack_int i = 0; i < n; i++) {
+      double v = x[i];
+      for (lapack_int k = 0; k < i; k++) v = v - a[(size_t)k * lda + i] * x[k];
+      x[i] = v;
+    }
+    for (lapack_int i = n - 1; i >= 0; i--) {
+      double v = x[i];
+      for (lapack_int k = n - 1; k > i; k--) v = v - a[(size_t)k * lda + i] * x[k];
+      x[i] = v / a[(size_t)i * lda + i];
+    }
+  }
+  return 0;
 }

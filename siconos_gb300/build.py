@@ -25,7 +25,8 @@ COMPARATOR_SOURCE = "fc2dgpu_percolour.cu"
 COMPARATOR_FLAGS = ["--fmad=false", "-Xcompiler", "-ffp-contract=off"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c", "rfc3dgpu_nsgs.c", "fc3d_colour.c"]
+C_SOURCES = ["fc3d_lattice.c", "fc3dgpu_nsgs.c", "fc3d_dat.c", "fc2dgpu_nsgs.c", "rfc3dgpu_nsgs.c", "fc3d_colour.c",
+             "gfc3dgpu_nsgs.c"]
 CU_SOURCES = {
     "fc3dgpu_ctx.cu": ["--fmad=false"],
     "fc3dgpu_sweep_f64.cu": ["--fmad=false"],
@@ -36,6 +37,9 @@ CU_SOURCES = {
     "fc2dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # host code computes the rolling solver's rho (Jacobi eigenvalues)
     "rfc3dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    # the global problem: the reference's iterates bit for bit; host code
+    # computes |q|
+    "gfc3dgpu.cu": ["--fmad=false", "-Xcompiler", "-ffp-contract=off"],
     # BF16 tensor-core MLP of the learned warm start
     "fc3dgpu_mlp.cu": [],
     # the FP32 sweeps are the accelerator whose result the FP64 polish

@@ -324,6 +324,55 @@ int fc3dgpu_lattice_fill_q(const fc3dgpu_lattice *L, double h, double *q) {
   return 0;
 }
 
+int fc3dgpu_lattice_global_sizes(const fc3dgpu_lattice *L, int64_t *n, int64_t *nnzH) {
+  if (!L) return -1;
+  if (n) *n = 6 * (int64_t)L->nb;
+  if (nnzH) *nnzH = 18 * (int64_t)L->bptr[L->nb];
+  return 0;
+}
+
+int fc3dgpu_lattice_fill_global(const fc3dgpu_lattice *L, double h, double mass_scale, int64_t *Mp, int64_t *Mi, double *Mx,
+                                int64_t *Hp, int64_t *Hi, double *Hx, double *q, double *b) {
+  if (!L) return -1;
+  int64_t k = 0;
+  for (int bd = 0; bd < L->nb; bd++) {
+    const double *v = &L->vel[6 * bd];
+    for (int a = 0; a < 6; a++) {
+      const int64_t i = 6 * (int64_t)bd + a;
+      const double mass = mass_scale * (a < 3 ? MASS : INERTIA);
+      Mp[i] = i;
+      Mi[i] = i;
+      Mx[i] = mass;
+      q[i] = mass * (a == 2 ? v[2] - 9.81 * h : v[a]);
+      Hp[i] = k;
+      /* incident contacts in ascending order (blist is in contact order) */
+      for (int32_t p = L->bptr[bd]; p < L->bptr[bd + 1]; p++) {
+        const int c = L->blist[p];
+        double s, d[3];
+        contact_arm(L, c, bd, &s, d);
+        const double *R = &L->frame[9 * c];
+        for (int r = 0; r < 3; r++) {
+          double x;
+          if (a < 3) {
+            x = R[3 * r + a];
+          } else {
+            double dxr[3];
+            cross(d, &R[3 * r], dxr);
+            x = dxr[a - 3];
+          }
+          Hi[k] = 3 * (int64_t)c + r;
+          Hx[k] = s * x;
+          k++;
+        }
+      }
+    }
+  }
+  Mp[6 * (int64_t)L->nb] = 6 * (int64_t)L->nb;
+  Hp[6 * (int64_t)L->nb] = k;
+  for (int64_t j = 0; j < 3 * (int64_t)L->nc; j++) b[j] = 0.0;
+  return 0;
+}
+
 int fc3dgpu_lattice_fill_geometry(const fc3dgpu_lattice *L, double *gap, int32_t *bodyA, int32_t *bodyB) {
   if (!L) return -1;
   if (gap) memcpy(gap, L->gap, sizeof(double) * (size_t)L->nc);

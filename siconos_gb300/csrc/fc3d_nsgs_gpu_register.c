@@ -11,14 +11,27 @@
  * (utils/solver_registry.c:48).  The default budget and tolerance are the
  * stock NSGS solver's (1000 iterations, 1e-4).
  *
- * fc3dgpu.h defines the id as a macro; a build that adds it to the
+ * The global solver SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU (619) registers the
+ * same way as gfc3d_nsgs.c:232-237 registers GFC3D_NSGS
+ * (REGISTER_SOLVER_3VAR, solve3 = gfc3dgpu_nsgs_solve_wrap); the reference's
+ * gfc3d_driver dispatches by a switch on the id (gfc3d_driver.c:120-293),
+ * so a build that adds it also adds one case there that calls the
+ * registry's solve3 for this id (see the integration notes).
+ *
+ * fc3dgpu.h defines the ids as macros; a build that adds them to the
  * enum of FrictionContact_options.h instead compiles this file with
  * -DFC3DGPU_ID_IN_SICONOS_ENUM.
  */
 #define FC3DGPU_USE_SICONOS_HEADERS
 #include "fc3dgpu.h"
+#include "gfc3dgpu.h"
 #include "solver_registry.h"
 
 REGISTER_SOLVER(SICONOS_FRICTION_3D_NSGS_GPU, "FC3D_NSGS_GPU",
                 "Coloured non-smooth Gauss-Seidel for 3D friction contact on GB300", fc3dgpu_nsgs_init_wrap,
                 fc3dgpu_nsgs_solve_wrap, fc3dgpu_nsgs_free_wrap, NULL, fc3dgpu_nsgs_set_default, 1000, 1e-4, 0)
+
+REGISTER_SOLVER_3VAR(SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU, "GFC3D_NSGS_GPU",
+                     "Global 3D friction contact NSGS (projected iteration) on GB300", gfc3dgpu_nsgs_init_wrap,
+                     gfc3dgpu_nsgs_solve_wrap, gfc3dgpu_nsgs_free_wrap, NULL, gfc3dgpu_nsgs_set_default, 1000,
+                     1e-4, 0)

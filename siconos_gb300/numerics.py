@@ -36,11 +36,14 @@ SICONOS_ROLLING_FRICTION_3D_ONECONTACT_NSN = 3003
 SICONOS_ROLLING_FRICTION_3D_NSGS_GPU = 3020
 SICONOS_FRICTION_3D_NSGS_GPU = 531
 SICONOS_FRICTION_3D_ONECONTACT_NSN_GP_HYBRID = 565
+SICONOS_GLOBAL_FRICTION_3D_NSGS = 605
+SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU = 619
 SICONOS_IPARAM_MAX_ITER = 0
 SICONOS_IPARAM_ITER_DONE = 1
 SICONOS_IPARAM_NSGS_SHUFFLE = 5
 SICONOS_DPARAM_TOL = 0
 SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION = 13  # the reference's compiled slot (NonSmoothGaussSeidel_options.h:275)
+SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY = 14
 SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT = 15
 SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL = 0
 SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT = 1
@@ -101,6 +104,13 @@ class _FCP(C.Structure):
 class _RFCP(C.Structure):
     _fields_ = [("dimension", C.c_int), ("numberOfContacts", C.c_int), ("M", C.POINTER(NumericsMatrix)),
                 ("q", _DP), ("mu", _DP), ("mu_r", _DP)]
+
+
+class _GFCP(C.Structure):
+    _fields_ = [("dimension", C.c_int), ("numberOfContacts", C.c_int), ("M", C.POINTER(NumericsMatrix)),
+                ("H", C.POINTER(NumericsMatrix)), ("q", _DP), ("norm_q", C.c_double), ("b", _DP),
+                ("norm_b", C.c_double), ("mu", _DP), ("M_inverse", C.POINTER(NumericsMatrix)), ("name", C.c_char_p),
+                ("env", C.c_void_p)]
 
 
 CALLBACK_T = C.CFUNCTYPE(None, C.c_void_p, C.c_size_t, _DP, _DP, C.c_double, C.c_void_p)
@@ -284,6 +294,33 @@ ABI = {
     "rfc3dgpu_ctx_rho": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rfc3dgpu_ctx_set_precision": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int]),
     "rfc3dgpu_ctx_last_sweeps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gfc3dgpu_nsgs": (C.c_int, [C.POINTER(_GFCP), _DP, _DP, _DP, C.POINTER(_SO)]),
+    "gfc3dgpu_nsgs_solve_wrap": (C.c_int, [C.c_void_p, _DP, _DP, _DP, C.POINTER(_SO)]),
+    "gfc3dgpu_nsgs_init_wrap": (C.c_int, [C.c_void_p, C.POINTER(_SO)]),
+    "gfc3dgpu_nsgs_free_wrap": (None, [C.c_void_p, C.POINTER(_SO)]),
+    "gfc3dgpu_nsgs_set_default": (None, [C.POINTER(_SO)]),
+    "gfc3dgpu_options_create": (C.POINTER(_SO), []),
+    "gfc3dgpu_options_delete": (None, [C.POINTER(_SO)]),
+    "gfc3dgpu_release": (None, [C.POINTER(_SO)]),
+    "gfc3dgpu_driver": (C.c_int, [C.POINTER(_GFCP), _DP, _DP, _DP, C.POINTER(_SO)]),
+    "gfc3dgpu_compute_error": (C.c_int, [C.POINTER(_GFCP), _DP, _DP, _DP, C.c_double, C.c_double, C.c_double,
+                                         _DP]),
+    "gfc3dgpu_ctx_create": (C.c_void_p, [C.c_int]),
+    "gfc3dgpu_ctx_destroy": (None, [C.c_void_p]),
+    "gfc3dgpu_ctx_set_problem": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, _I64, _I64, _F64, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, _F64, C.c_void_p, C.c_void_p]),
+    "gfc3dgpu_ctx_set_start": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gfc3dgpu_ctx_solve": (C.c_int, [C.c_void_p, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int), _DP,
+                                     C.POINTER(C.c_int), _DP]),
+    "gfc3dgpu_ctx_get": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gfc3dgpu_ctx_compute_error": (C.c_int, [C.c_void_p, C.c_double, _DP]),
+    "gfc3dgpu_ctx_trace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "gfc3dgpu_ctx_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _DP,
+                                    C.POINTER(C.c_int)]),
+    "gfc3dgpu_ctx_spin_limit": (C.c_int, [C.c_void_p, C.c_ulonglong]),
+    "fc3dgpu_lattice_global_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "fc3dgpu_lattice_fill_global": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _I64, _I64, _F64, _I64, _I64, _F64, _F64,
+                                              _F64]),
 }
 
 # the per-colour comparator (include/fc2dgpu_percolour.h): a separate,
@@ -465,7 +502,7 @@ class SolverOptions:
     ``SICONOS_FRICTION_2D_NSGS_GPU``."""
 
     _KINDS = {SICONOS_FRICTION_3D_NSGS_GPU: "fc3dgpu", SICONOS_FRICTION_2D_NSGS_GPU: "fc2dgpu",
-              SICONOS_ROLLING_FRICTION_3D_NSGS_GPU: "rfc3dgpu"}
+              SICONOS_ROLLING_FRICTION_3D_NSGS_GPU: "rfc3dgpu", SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU: "gfc3dgpu"}
 
     def __init__(self, solver_id: int = SICONOS_FRICTION_3D_NSGS_GPU):
         if solver_id not in self._KINDS:
@@ -904,3 +941,212 @@ def colour(rowptr, colidx, kind: int = 0) -> tuple[int, np.ndarray]:
     if n < 0:
         raise RuntimeError(last_error())
     return n, out
+
+
+# ---- global 3D friction contact (M v = q + H r, u = H^T v + b) --------------
+class BlockMatrix:
+    """A sparse-block matrix with blocks of any sizes (the reference's
+    SparseBlockStructuredMatrix in general form): ``row_sizes`` and
+    ``col_sizes`` the block sizes, ``blocks`` a dict (block row, block
+    column) -> dense block.  Blocks are kept column-major in one array."""
+
+    def __init__(self, row_sizes, col_sizes, blocks: dict):
+        self.row_sizes = np.asarray(row_sizes, np.int64)
+        self.col_sizes = np.asarray(col_sizes, np.int64)
+        keys = sorted(blocks)
+        self.shape = (int(self.row_sizes.sum()), int(self.col_sizes.sum()))
+        self._cum0 = np.cumsum(self.row_sizes).astype(np.uintp)
+        self._cum1 = np.cumsum(self.col_sizes).astype(np.uintp)
+        nbr = len(self.row_sizes)
+        i1 = np.zeros(nbr + 1, np.uintp)
+        for bi, _ in keys:
+            i1[bi + 1] += 1
+        self._i1 = np.cumsum(i1).astype(np.uintp)
+        self._i2 = np.array([bj for _, bj in keys] or [0], np.uintp)
+        offs, vals = [], []
+        o = 0
+        for k in keys:
+            a = np.asarray(blocks[k], np.float64)
+            if a.shape != (self.row_sizes[k[0]], self.col_sizes[k[1]]):
+                raise ValueError(f"block {k} has shape {a.shape}")
+            offs.append(o)
+            vals.append(a.reshape(-1, order="F"))
+            o += a.size
+        self.data = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1))
+        base = self.data.ctypes.data
+        self._ptrs = (_DP * max(len(keys), 1))(*[C.cast(base + 8 * x, _DP) for x in offs])
+        s = SparseBlockStructuredMatrix()
+        s.nbblocks = len(keys)
+        s.block = C.cast(self._ptrs, C.POINTER(_DP))
+        s.blocknumber0 = nbr
+        s.blocknumber1 = len(self.col_sizes)
+        s.blocksize0 = self._cum0.ctypes.data_as(_SZP)
+        s.blocksize1 = self._cum1.ctypes.data_as(_SZP)
+        s.filled1 = nbr + 1
+        s.filled2 = len(keys)
+        s.index1_data = self._i1.ctypes.data_as(_SZP)
+        s.index2_data = self._i2.ctypes.data_as(_SZP)
+        s.diagonal_blocks = None
+        s.version.number = 1
+        self.c = s
+
+    @staticmethod
+    def from_dense(A, row_sizes, col_sizes) -> "BlockMatrix":
+        """Every block of A (cut by the sizes) with a nonzero entry."""
+        r0 = np.concatenate([[0], np.cumsum(row_sizes)])
+        c0 = np.concatenate([[0], np.cumsum(col_sizes)])
+        blocks = {}
+        for bi in range(len(row_sizes)):
+            for bj in range(len(col_sizes)):
+                blk = A[r0[bi]:r0[bi + 1], c0[bj]:c0[bj + 1]]
+                if np.any(blk != 0):
+                    blocks[(bi, bj)] = np.array(blk)
+        return BlockMatrix(row_sizes, col_sizes, blocks)
+
+
+def _nm_of(A, rows, cols):
+    nm = NumericsMatrix()
+    nm.size0, nm.size1 = rows, cols
+    if isinstance(A, BlockMatrix):
+        if A.shape != (rows, cols):
+            raise ValueError(f"block matrix is {A.shape}, expected {(rows, cols)}")
+        nm.storageType = NM_SPARSE_BLOCK
+        nm.matrix1 = C.pointer(A.c)
+    else:
+        if not (isinstance(A, np.ndarray) and A.dtype == np.float64 and A.flags.f_contiguous and
+                A.shape == (rows, cols)):
+            raise TypeError(f"dense matrices are Fortran-ordered float64 arrays of shape {(rows, cols)}")
+        nm.storageType = NM_DENSE
+        nm.matrix0 = A.ctypes.data_as(_DP)
+    nm.version.number = 1
+    return nm
+
+
+class GlobalFrictionContactProblem:
+    """``GlobalFrictionContactProblem(dim, nc, M, H, q, b, mu)``: M (n x n)
+    and H (n x 3 nc) dense (Fortran order) or :class:`BlockMatrix`; the numpy
+    buffers are shared."""
+
+    def __init__(self, dim: int, nc: int, M, H, q, b, mu):
+        if dim != 3:
+            raise ValueError("dimension 3")
+        as_f64 = (lambda x: x if (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous)
+                  else np.ascontiguousarray(x, dtype=np.float64))
+        self._q, self._b, self._mu = as_f64(q), as_f64(b), as_f64(mu)
+        n = self._q.size
+        self._M, self._H = M, H
+        self._nm = _nm_of(M, n, n)
+        self._nh = _nm_of(H, n, 3 * nc)
+        p = _GFCP()
+        p.dimension = 3
+        p.numberOfContacts = nc
+        p.M = C.pointer(self._nm)
+        p.H = C.pointer(self._nh)
+        p.q = self._q.ctypes.data_as(_DP)
+        p.b = self._b.ctypes.data_as(_DP)
+        p.mu = self._mu.ctypes.data_as(_DP)
+        self.c = p
+        self.n = n
+
+    @property
+    def numberOfContacts(self) -> int:
+        return self.c.numberOfContacts
+
+
+def gfc3d_driver(problem: GlobalFrictionContactProblem, reaction, velocity, globalVelocity, options) -> int:
+    """gfc3d_driver for ``SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU``: returns ``info``."""
+    m = 3 * problem.numberOfContacts
+    return lib().gfc3dgpu_driver(C.byref(problem.c), _vec(reaction, m) if m else None,
+                                 _vec(velocity, m) if m else None, _vec(globalVelocity, problem.n), options.ptr)
+
+
+def gfc3d_nsgs_gpu(problem, reaction, velocity, globalVelocity, options) -> int:
+    """The solver entry itself (what the registry binds), options as given."""
+    m = 3 * problem.numberOfContacts
+    return lib().gfc3dgpu_nsgs(C.byref(problem.c), _vec(reaction, m), _vec(velocity, m),
+                               _vec(globalVelocity, problem.n), options.ptr)
+
+
+def gfc3d_compute_error(problem, reaction, velocity, globalVelocity, tolerance: float, norm_q: float):
+    """(info, error) as the reference's gfc3d_compute_error; writes velocity."""
+    m = 3 * problem.numberOfContacts
+    err = C.c_double()
+    info = lib().gfc3dgpu_compute_error(C.byref(problem.c), _vec(reaction, m), _vec(velocity, m),
+                                        _vec(globalVelocity, problem.n), tolerance, norm_q, 0.0, C.byref(err))
+    return info, err.value
+
+
+class Gfc3dContext:
+    """Device-resident global problem (``gfc3dgpu_ctx_*``): M and H as CSR
+    arrays, uploaded once, solved many times."""
+
+    def __init__(self, n, nc, Mp, Mi, Mx, Hp, Hi, Hx, q, b, mu, device: int = 0):
+        L = lib()
+        self.ctx = L.gfc3dgpu_ctx_create(device)
+        if not self.ctx:
+            raise RuntimeError(last_error())
+        self.n, self.nc = int(n), int(nc)
+        c = np.ascontiguousarray
+        self._keep = [c(Hp, np.int64), c(Hi, np.int64), c(Hx, np.float64), c(b, np.float64), c(mu, np.float64)]
+        hp, hi, hx, bb, mm = self._keep
+        rc = L.gfc3dgpu_ctx_set_problem(self.ctx, self.n, self.nc, c(Mp, np.int64), c(Mi, np.int64),
+                                        c(Mx, np.float64), hp.ctypes.data, hi.ctypes.data, hx.ctypes.data,
+                                        c(q, np.float64), bb.ctypes.data, mm.ctypes.data)
+        if rc != 0:
+            L.gfc3dgpu_ctx_destroy(self.ctx)
+            self.ctx = None
+            raise ValueError(last_error())
+
+    @staticmethod
+    def from_problem(P, device: int = 0) -> "Gfc3dContext":
+        """From any object with the fields of ``oracle.GlobalProblem``."""
+        return Gfc3dContext(P.n, P.nc, P.Mp, P.Mi, P.Mx, P.Hp, P.Hi, P.Hx, P.q, P.b, P.mu, device)
+
+    def set_start(self, r=None, v=None):
+        rr = None if r is None else np.ascontiguousarray(r, np.float64)
+        vv = None if v is None else np.ascontiguousarray(v, np.float64)
+        _check(lib().gfc3dgpu_ctx_set_start(self.ctx, None if rr is None else rr.ctypes.data,
+                                            None if vv is None else vv.ctypes.data))
+
+    def solve(self, tol: float, max_iter: int, freq: int = 0) -> dict:
+        it, info = C.c_int(), C.c_int()
+        err, ms = C.c_double(), C.c_double()
+        _check(lib().gfc3dgpu_ctx_solve(self.ctx, tol, max_iter, freq, C.byref(it), C.byref(err), C.byref(info),
+                                        C.byref(ms)))
+        return dict(iterations=it.value, error=err.value, info=info.value, ms=ms.value)
+
+    def get(self):
+        r, u, v = np.zeros(3 * self.nc), np.zeros(3 * self.nc), np.zeros(self.n)
+        _check(lib().gfc3dgpu_ctx_get(self.ctx, r.ctypes.data, u.ctypes.data, v.ctypes.data))
+        return r, u, v
+
+    def compute_error(self, norm_q: float = -1.0) -> float:
+        e = C.c_double()
+        _check(lib().gfc3dgpu_ctx_compute_error(self.ctx, norm_q, C.byref(e)))
+        return e.value
+
+    def trace(self, cap: int) -> np.ndarray:
+        out = np.zeros(max(cap, 1))
+        k = lib().gfc3dgpu_ctx_trace(self.ctx, out.ctypes.data, cap)
+        return out[:max(k, 0)].copy()
+
+    def info(self) -> dict:
+        nc, mx, dg, gr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        by = C.c_double()
+        _check(lib().gfc3dgpu_ctx_info(self.ctx, C.byref(nc), C.byref(mx), C.byref(dg), C.byref(by), C.byref(gr)))
+        return dict(components=nc.value, max_component=mx.value, diagonal=bool(dg.value),
+                    bytes_per_iteration=by.value, grid=gr.value)
+
+    def spin_limit(self, polls: int):
+        _check(lib().gfc3dgpu_ctx_spin_limit(self.ctx, polls))
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            lib().gfc3dgpu_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

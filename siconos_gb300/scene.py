@@ -82,6 +82,32 @@ def lattice(nx: int, ny: int, nz: int, seed: int = 1, mu: float = 0.5, jitter_st
     return LatticeScene((nx, ny, nz), seed, n, nb.value, rp, ci, bl.reshape(k, 9), q, np.full(n, float(mu)), gap, hdl)
 
 
+def lattice_global(nx: int, ny: int, nz: int, seed: int = 1, mu: float = 0.5, jitter_std: float = 1e-3,
+                   v0_std: float = 0.1, h: float = 1e-3, mass_scale: float = 10.0):
+    """The scene in the global form of the reference's
+    GlobalFrictionContactProblem (M v = q + H r, u = H^T v + b, 6 dofs per
+    body): a namespace with n, nc and the CSR arrays Mp, Mi, Mx, Hp, Hi, Hx
+    and q, b, mu (see include/fc3dgpu_scene.h)."""
+    from types import SimpleNamespace
+    L = sn.lib()
+    hdl = L.fc3dgpu_lattice_create(nx, ny, nz, seed, jitter_std, v0_std)
+    if not hdl:
+        raise ValueError("bad lattice size")
+    try:
+        nb, nc, nnzb = C.c_int(), C.c_int(), C.c_int64()
+        L.fc3dgpu_lattice_sizes(hdl, C.byref(nb), C.byref(nc), C.byref(nnzb))
+        n, nh = C.c_int64(), C.c_int64()
+        L.fc3dgpu_lattice_global_sizes(hdl, C.byref(n), C.byref(nh))
+        Mp, Mi, Mx = np.zeros(n.value + 1, np.int64), np.zeros(n.value, np.int64), np.zeros(n.value)
+        Hp, Hi, Hx = np.zeros(n.value + 1, np.int64), np.zeros(nh.value, np.int64), np.zeros(nh.value)
+        q, b = np.zeros(n.value), np.zeros(3 * nc.value)
+        L.fc3dgpu_lattice_fill_global(hdl, h, mass_scale, Mp, Mi, Mx, Hp, Hi, Hx, q, b)
+    finally:
+        L.fc3dgpu_lattice_free(hdl)
+    return SimpleNamespace(dims=(nx, ny, nz), seed=seed, n=n.value, nc=nc.value, nbodies=nb.value, Mp=Mp, Mi=Mi,
+                           Mx=Mx, Hp=Hp, Hi=Hi, Hx=Hx, q=q, b=b, mu=np.full(nc.value, float(mu)))
+
+
 def batch_specs(count: int = 512, seed: int = 7, lo=(3, 3, 2), hi=(20, 20, 10), mu_range=(0.1, 0.9)):
     """(dims, seed, mu) of each scene of the batch: dims drawn uniformly in
     [lo, hi] per axis, mu ~ U(mu_range) per scene."""

@@ -3,7 +3,7 @@
 Run in a checkout that has the reference sources (the library in
 ``oracle/_ref`` is built from them by ``oracle/build_ref.py``):
 
-    python tests/golden/make_golden.py /path/to/reference [--only=fc2d|rfc3d|to_tolerance]
+    python tests/golden/make_golden.py /path/to/reference [--only=fc2d|rfc3d|gfc3d|to_tolerance]
 
 For each SBM/dense friction-contact fixture of the reference's own test data
 (numerics/src/FrictionContact/test/data) and for the 5x5x6 lattice scene,
@@ -139,6 +139,42 @@ def make_rfc3d(data: Path):
         print(f"{f}: nc={P.nc} nnzb={P.nnzb} info={full.info} it={full.iterations} err={full.error:.3e}")
 
 
+GFC3D_FIXTURES = [
+    # the reference's global-problem test data (data_collection_gfc3d); the
+    # reference built here reads M and H in dense and sparse-block storage
+    # (GFC3D_TwoRods1-condensed.dat stores H in CSparse form, which it
+    # cannot read)
+    "GFC3D_Example0.dat",
+    "GFC3D_Example00.dat",
+    "GFC3D_Example00_badly_scaled.dat",
+    "GFC3D_Example0_SBM.dat",
+    "GFC3D_Example1.dat",
+    "GFC3D_OneContact.dat",
+    "GFC3D_TwoRods1.dat",
+]
+
+
+def make_gfc3d(data: Path):
+    """Global problems with the reference's gfc3d_nsgs results through its
+    gfc3d_driver on dense copies of M and H (the settings of its gfc3d test
+    collection: tol 1e-8 with 1000 iterations, and the default tol 1e-4 with
+    10000), a 20-iteration run, and the 5x5x6 sphere lattice in global form
+    (bodies of mass 10, inertia 1)."""
+    import oracle as O
+    cases = [(f.replace(".dat", "").replace("-", "_"), O.read_gfc3d_dat(data / f)[0], f) for f in GFC3D_FIXTURES]
+    cases.append(("lattice_5x5x6_s1", O.lattice_global(5, 5, 6, seed=1), "lattice 5x5x6 seed 1, mass scale 10"))
+    for name, P, src in cases:
+        d = dict(n=P.n, nc=P.nc, Mp=P.Mp, Mi=P.Mi, Mx=P.Mx, Hp=P.Hp, Hi=P.Hi, Hx=P.Hx, q=P.q, b=P.b, mu=P.mu,
+                 source=src)
+        for tag, tol, it in (("", 1e-8, 1000), ("_default", 1e-4, 10000), ("20", 0.0, 20)):
+            res = O.gfc3d_nsgs_ref(P, tol=tol, maxiter=it)
+            d.update({f"info{tag}": res.info, f"error{tag}": res.error, f"r{tag}": res.r, f"u{tag}": res.u,
+                      f"v{tag}": res.v})
+        np.savez_compressed(HERE / f"gfc3d_{name}.npz", **d)
+        print(f"{src}: n={P.n} nc={P.nc} info={d['info']} err={d['error']:.3e} "
+              f"default: info={d['info_default']} err={d['error_default']:.3e}")
+
+
 def make_to_tolerance():
     """The reference's own fc3d_nsgs (oracle/_ref) on the 60x60x30 lattice
     (seed 1, mu 0.5) from r = 0 to 1e-3 and to 1e-4 (defaults, budget
@@ -167,6 +203,9 @@ def main(ref_root: str, only: str | None = None):
     data = Path(ref_root) / "numerics" / "src" / "FrictionContact" / "test" / "data"
     if only == "rfc3d":
         make_rfc3d(Path(ref_root) / "numerics" / "src" / "RollingFrictionContact" / "test" / "data")
+        return
+    if only == "gfc3d":
+        make_gfc3d(data)
         return
     if only == "to_tolerance":
         make_to_tolerance()

@@ -8,6 +8,12 @@
  *   name, solve_is_gpu, iparam/dparam defaults, info, iterations, residual,
  *   the reference's own fc3d_compute_error of the returned reaction (when
  *   the solve returned one) and the GPU library's last message.
+ *
+ * With a fifth argument (a GFC3D .dat file) it does the same for the global
+ * solver: the registry entry of SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU, the
+ * options the reference's solver_options_create gives it, and a solve
+ * through the entry's solve3 (what gfc3d_driver's case for the id calls),
+ * checked with the reference's own gfc3d_compute_error (keys prefixed g_).
  */
 #define FC3DGPU_USE_SICONOS_HEADERS
 #include <math.h>
@@ -20,6 +26,9 @@
 #include "SolverOptions.h"
 #include "fc3d_compute_error.h"
 #include "fc3dgpu.h"
+#include "gfc3dgpu.h"
+#include "GlobalFrictionContactProblem.h"
+#include "gfc3d_compute_error.h"
 #include "solver_registry.h"
 
 int main(int argc, char **argv) {
@@ -68,5 +77,42 @@ int main(int argc, char **argv) {
   frictionContactProblem_free(problem);
   free(r);
   free(u);
+  if (argc > 4) {
+    GlobalFrictionContactProblem *gp = globalFrictionContact_new_from_filename(argv[4]);
+    if (!gp) {
+      fprintf(stderr, "cannot read %s\n", argv[4]);
+      return 2;
+    }
+    const SolverEntry *g = solver_registry_lookup(SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU);
+    printf("g_registered %d\n", g != NULL);
+    if (!g) return 3;
+    printf("g_name %s\n", g->name);
+    printf("g_solve3_is_gpu %d\n", g->has_3var && g->solve3 == gfc3dgpu_nsgs_solve_wrap);
+    SolverOptions *go = solver_options_create(SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU);
+    printf("g_default_max_iter %d\n", go->iparam[SICONOS_IPARAM_MAX_ITER]);
+    printf("g_default_tol %.17g\n", go->dparam[SICONOS_DPARAM_TOL]);
+    go->dparam[SICONOS_DPARAM_TOL] = tol;
+    go->iparam[SICONOS_IPARAM_MAX_ITER] = max_iter;
+    const int m = 3 * gp->numberOfContacts, nd = gp->M->size0;
+    double *gr = calloc((size_t)m, sizeof(double)), *gu = calloc((size_t)m, sizeof(double));
+    double *gv = calloc((size_t)nd, sizeof(double));
+    const int ginfo = g->solve3(gp, gr, gu, gv, go);
+    printf("g_info %d\n", ginfo);
+    printf("g_residual %.17g\n", go->dparam[SICONOS_DPARAM_RESIDU]);
+    if (ginfo >= 0) {
+      double err = 0.0, nq = 0.0, nb = 0.0;
+      for (int i = 0; i < nd; i++) nq += gp->q[i] * gp->q[i];
+      for (int i = 0; i < m; i++) nb += gp->b[i] * gp->b[i];
+      gfc3d_compute_error(gp, gr, gu, gv, tol, go, sqrt(nq), sqrt(nb), &err);
+      printf("g_reference_error %.17g\n", err);
+    }
+    printf("g_message %s\n", fc3dgpu_last_error());
+    gfc3dgpu_release(go);
+    solver_options_delete(go);
+    globalFrictionContact_free(gp);
+    free(gr);
+    free(gu);
+    free(gv);
+  }
   return 0;
 }

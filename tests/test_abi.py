@@ -19,7 +19,7 @@ def declared_functions(comparator=False):
         if (h.name == "fc2dgpu_percolour.h") != comparator:
             continue
         text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
-        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:fc[23]|rfc3)dgpu_\w+)\s*\(", text, flags=re.M):
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:g?fc[23]|rfc3)dgpu_\w+)\s*\(", text, flags=re.M):
             names.add(m.group(1))
     return sorted(names)
 
@@ -29,7 +29,8 @@ def test_headers_declare_entry_points():
     for must in ["fc3dgpu_nsgs", "fc3dgpu_nsgs_set_default", "fc3dgpu_nsgs_batch", "fc3dgpu_compute_error",
                  "fc3dgpu_driver", "fc3dgpu_colour", "fc3dgpu_ctx_solve", "fc3dgpu_lattice_create",
                  "fc2dgpu_nsgs", "fc2dgpu_driver", "fc2dgpu_ctx_solve",
-                 "rfc3dgpu_nsgs", "rfc3dgpu_driver", "rfc3dgpu_ctx_solve"]:
+                 "rfc3dgpu_nsgs", "rfc3dgpu_driver", "rfc3dgpu_ctx_solve",
+                 "gfc3dgpu_nsgs", "gfc3dgpu_driver", "gfc3dgpu_ctx_solve"]:
         assert must in names
     assert "fc2dgpu_percolour_solve" in declared_functions(comparator=True)
 

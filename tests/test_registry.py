@@ -51,8 +51,9 @@ def registry_program(tmp_path_factory, built_lib):
     return out
 
 
-def _run(prog, dat, tol=1e-8, max_iter=10000):
-    r = subprocess.run([str(prog), str(dat), repr(tol), str(max_iter)], capture_output=True, text=True, timeout=600)
+def _run(prog, dat, tol=1e-8, max_iter=10000, gdat=None):
+    args = [str(prog), str(dat), repr(tol), str(max_iter)] + ([str(gdat)] if gdat else [])
+    r = subprocess.run(args, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     out = {}
     for line in r.stdout.splitlines():
@@ -106,7 +107,31 @@ def test_reference_driver_trivial_case_never_reaches_solver(registry_program, tm
     assert int(out["info"]) == 0 and int(out["iterations"]) == 0
 
 
-@pytest.mark.parametrize("ref_id, ours", [(500, 531), (400, 412), (3000, 3020)])
+def test_global_solver_registered_and_solves_through_solve3(registry_program, tmp_path):
+    """SICONOS_GLOBAL_FRICTION_3D_NSGS_GPU in the reference's registry: the
+    reference's solver_options_create(619) gives the registry defaults, and
+    the entry's solve3 (what the id's case in gfc3d_driver calls) solves the
+    reference's GFC3D_TwoRods1 problem as read by the reference's reader."""
+    build_ref, src = _reference()
+    P, g = load_case("fixture_FC3D_Example1_SBM")
+    dat = tmp_path / "fc3d.dat"
+    O.write_dat_ref(P, dat)
+    gdat = src / "numerics" / "src" / "FrictionContact" / "test" / "data" / "GFC3D_TwoRods1.dat"
+    out, err = _run(registry_program, dat, 1e-8, 1000, gdat)
+    assert out["g_registered"] == "1" and out["g_name"] == "GFC3D_NSGS_GPU" and out["g_solve3_is_gpu"] == "1"
+    assert out["g_default_max_iter"] == "1000" and float(out["g_default_tol"]) == 1e-4
+    info = int(out["g_info"])
+    if _gpu_present():
+        gold = np.load(ROOT / "tests" / "golden" / "gfc3d_GFC3D_TwoRods1.npz")
+        assert info == 0, out
+        assert float(out["g_reference_error"]) <= 1e-8
+        assert abs(float(out["g_residual"]) - float(gold["error"])) <= 1e-12 * float(gold["error"])
+    else:
+        assert info == NUMERICS_ERR_NOT_IMPLEMENTED, out
+        assert "CUDA" in out["g_message"] or "device" in out["g_message"], out["g_message"]
+
+
+@pytest.mark.parametrize("ref_id, ours", [(500, 531), (400, 412), (3000, 3020), (605, 619)])
 def test_option_slots_equal_reference_defaults(built_lib, ref_id, ours):
     """Every option slot the GPU solvers share with the reference's stock NSGS
     (fc3d, fc2d, rolling) holds the reference's default after the reference's
