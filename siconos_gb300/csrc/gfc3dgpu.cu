@@ -150,6 +150,12 @@ __device__ __forceinline__ void gsum(const double* part, int slot, double out[N]
   __syncthreads();
 }
 
+// Rank of the calling warp for the grid-stride slab loops: consecutive ranks
+// go to different blocks, so the slabs left over after equal shares fall
+// one to a block (blocks spread over the SMs) rather than all to the first
+// blocks' SMs.
+__device__ __forceinline__ int warp_rank() { return (int)((threadIdx.x >> 5) * gridDim.x + blockIdx.x); }
+
 __device__ __forceinline__ double* part_of(const Args& a, int parity) {
   return a.part + (size_t)parity * GRID_MAX * 8;
 }
@@ -161,7 +167,7 @@ __device__ __forceinline__ double* part_of(const Args& a, int parity) {
 __device__ __forceinline__ void phase_a(const Args& a, bool err, const double* vprev, double* vcur, bool store,
                                         bool no_h, double e[3]) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * NT + threadIdx.x) >> 5, tw = (gridDim.x * NT) >> 5;
+  const int gw = warp_rank(), tw = (gridDim.x * NT) >> 5;
   for (int s = gw; s < a.nslab_d; s += tw) {
     const long long i = (long long)s * 32 + lane;
     const bool row = i < a.n;
@@ -251,7 +257,7 @@ __device__ __forceinline__ void phase_b(const Args& a, double* v) {
     return;
   }
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * NT + threadIdx.x) >> 5, tw = (gridDim.x * NT) >> 5;
+  const int gw = warp_rank(), tw = (gridDim.x * NT) >> 5;
   for (int c = gw; c < a.ncomp; c += tw) {
     const int o = a.cptr[c], sz = a.cptr[c + 1] - o;
     const double* A = a.lu + a.luoff[c];
@@ -303,7 +309,7 @@ __device__ __forceinline__ double unitary_error(const double r[3], const double 
 // error terms e[0..2] (|u|^2, |r|^2, complementarity) of the result.
 __device__ __forceinline__ void phase_c(const Args& a, const double* v, bool update, double e[3]) {
   const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * NT + threadIdx.x) >> 5, tw = (gridDim.x * NT) >> 5;
+  const int gw = warp_rank(), tw = (gridDim.x * NT) >> 5;
   for (int s = gw; s < a.nslab_c; s += tw) {
     const int c = s * 32 + lane;
     const long long o = a.toff[s];
