@@ -114,6 +114,14 @@ int gfc3dgpu_ctx_trace(gfc3dgpu_ctx *ctx, double *out, int cap);
  * least (the unpadded arrays it streams, each once) and the grid size. */
 int gfc3dgpu_ctx_info(gfc3dgpu_ctx *ctx, int *ncomp, int *max_component, int *diagonal, double *bytes_per_iteration,
                       int *grid);
+/* Arithmetic of the row products: 0 (a new context's default) the
+ * reference's, a multiply and an add each rounded, so r, u and v equal the
+ * reference's bit for bit; 1 (opt-in) fused multiply-adds, which halve the
+ * FP64 operations of the products (the kernel is bound by the FP64 pipe) and
+ * give iterates equal to the reference's to rounding, not bit for bit.
+ * Through the solver options: iparam[FC3DGPU_IPARAM_PRECISION] = 2 selects
+ * the fused products, any other value the reference's. */
+int gfc3dgpu_ctx_set_arithmetic(gfc3dgpu_ctx *ctx, int fused);
 /* Poll limit of every grid-barrier wait (0: the default of 2^22 polls). */
 int gfc3dgpu_ctx_spin_limit(gfc3dgpu_ctx *ctx, unsigned long long polls);
 

@@ -150,6 +150,15 @@ __device__ __forceinline__ void gsum(const double* part, int slot, double out[N]
   __syncthreads();
 }
 
+// acc + a b: two roundings as the reference computes it, or (FAST, the
+// opt-in fused mode) one fused multiply-add.  The translation unit is
+// compiled without FMA contraction, so the first form stays unfused.
+template <bool FAST>
+__device__ __forceinline__ double madd(double acc, double a, double b) {
+  if (FAST) return fma(a, b, acc);
+  return acc + a * b;
+}
+
 // Rank of the calling warp for the grid-stride slab loops: consecutive ranks
 // go to different blocks, so the slabs left over after equal shares fall
 // one to a block (blocks spread over the SMs) rather than all to the first
@@ -164,6 +173,7 @@ __device__ __forceinline__ double* part_of(const Args& a, int parity) {
 // `err`, the error terms of (r, vprev) go to e[0..2] (|H r|^2, |M v|^2,
 // |q + H r - M v|^2); vcur receives t / M_ii for a diagonal M (when non
 // null), else t is stored.  no_h: t = q (no contact).
+template <bool FAST>
 __device__ __forceinline__ void phase_a(const Args& a, bool err, const double* vprev, double* vcur, bool store,
                                         bool no_h, double e[3]) {
   const int lane = threadIdx.x & 31;
@@ -185,11 +195,11 @@ __device__ __forceinline__ void phase_a(const Args& a, bool err, const double* v
           rv[j] = __ldcg(&a.r[__ldg(&a.hcol[p])]);
         }
 #pragma unroll
-        for (int j = 0; j < 4; j++) sh = sh + hv[j] * rv[j];
+        for (int j = 0; j < 4; j++) sh = madd<FAST>(sh, hv[j], rv[j]);
       }
       for (; k < ns; k++) {
         const size_t p = (size_t)(o + k) * 32 + lane;
-        sh = sh + __ldg(&a.hval[p]) * __ldcg(&a.r[__ldg(&a.hcol[p])]);
+        sh = madd<FAST>(sh, __ldg(&a.hval[p]), __ldcg(&a.r[__ldg(&a.hcol[p])]));
       }
     }
     if (!row) continue;
@@ -203,7 +213,7 @@ __device__ __forceinline__ void phase_a(const Args& a, bool err, const double* v
       double sm = 0.0;
       for (int k = 0; k < ns; k++) {
         const size_t p = (size_t)(o + k) * 32 + lane;
-        sm = sm + __ldg(&a.mval[p]) * __ldcg(&vprev[__ldg(&a.mcol[p])]);
+        sm = madd<FAST>(sm, __ldg(&a.mval[p]), __ldcg(&vprev[__ldg(&a.mcol[p])]));
       }
       const double hr = 0.0 + 1.0 * sh;    // NM_gemv(1.0, H, r, 0.0, tmp)
       const double mv = 0.0 + -1.0 * sm;   // NM_gemv(-1.0, M, v, 0.0, tmp)
@@ -307,6 +317,7 @@ __device__ __forceinline__ double unitary_error(const double r[3], const double 
 // Phase C over the contact slabs (one warp per slab): u = b + H^T v, the
 // projected update of r (gfc3d_nsgs.c:150-165) when `update`, and the
 // error terms e[0..2] (|u|^2, |r|^2, complementarity) of the result.
+template <bool FAST>
 __device__ __forceinline__ void phase_c(const Args& a, const double* v, bool update, double e[3]) {
   const int lane = threadIdx.x & 31;
   const int gw = warp_rank(), tw = (gridDim.x * NT) >> 5;
@@ -329,18 +340,18 @@ __device__ __forceinline__ void phase_c(const Args& a, const double* v, bool upd
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {
-        acc[0] = acc[0] + tv[j][0] * vv[j];
-        acc[1] = acc[1] + tv[j][1] * vv[j];
-        acc[2] = acc[2] + tv[j][2] * vv[j];
+        acc[0] = madd<FAST>(acc[0], tv[j][0], vv[j]);
+        acc[1] = madd<FAST>(acc[1], tv[j][1], vv[j]);
+        acc[2] = madd<FAST>(acc[2], tv[j][2], vv[j]);
       }
     }
     for (; k < ns; k++) {
       const size_t p = (size_t)(o + k) * 32 + lane;
       const double vj = __ldcg(&v[__ldg(&a.tcol[p])]);
       const size_t pv = (size_t)(o + k) * 96 + lane;
-      acc[0] = acc[0] + __ldg(&a.tval[pv]) * vj;
-      acc[1] = acc[1] + __ldg(&a.tval[pv + 32]) * vj;
-      acc[2] = acc[2] + __ldg(&a.tval[pv + 64]) * vj;
+      acc[0] = madd<FAST>(acc[0], __ldg(&a.tval[pv]), vj);
+      acc[1] = madd<FAST>(acc[1], __ldg(&a.tval[pv + 32]), vj);
+      acc[2] = madd<FAST>(acc[2], __ldg(&a.tval[pv + 64]), vj);
     }
     if (c >= a.nc) continue;
     double u[3], r[3];
@@ -383,6 +394,7 @@ __device__ __forceinline__ double error_of(const Args& a, const double sa[3], co
   return err + ec;
 }
 
+template <bool FAST>
 __global__ void __launch_bounds__(NT) k_gfc3d(Args a) {
   unsigned epoch = 0;
   const bool diag = a.mdiag != nullptr;
@@ -390,7 +402,7 @@ __global__ void __launch_bounds__(NT) k_gfc3d(Args a) {
   if (a.mode == 2) {
     // v = M^-1 q (gfc3d_driver's no-contact case)
     double e[3] = {0, 0, 0};
-    phase_a(a, false, nullptr, diag ? a.v0 : nullptr, true, true, e);
+    phase_a<FAST>(a, false, nullptr, diag ? a.v0 : nullptr, true, true, e);
     if (!diag) {
       if (!grid_barrier(a.flags, epoch, a.spin_limit, a.status)) return;
       phase_b(a, a.v0);
@@ -407,9 +419,9 @@ __global__ void __launch_bounds__(NT) k_gfc3d(Args a) {
     // the error of (r, v0) with u = b + H^T v0 (max_iter 0, or an error
     // evaluation alone)
     double ec[3] = {0, 0, 0}, ea[3] = {0, 0, 0};
-    phase_c(a, a.v0, false, ec);
+    phase_c<FAST>(a, a.v0, false, ec);
     bsum<3>(ec, part_of(a, 0) + blockIdx.x * 8 + 3);
-    phase_a(a, true, a.v0, nullptr, false, false, ea);
+    phase_a<FAST>(a, true, a.v0, nullptr, false, false, ea);
     bsum<3>(ea, part_of(a, 0) + blockIdx.x * 8);
     if (!grid_barrier(a.flags, epoch, a.spin_limit, a.status)) return;
     double sa[3], sc[3];
@@ -431,7 +443,7 @@ __global__ void __launch_bounds__(NT) k_gfc3d(Args a) {
     // phase A of iteration k, with the error terms of iteration k - 1
     double ea[3] = {0, 0, 0};
     const bool final_only = k > a.max_iter;  // the error of the last iterate alone
-    phase_a(a, k >= 2, vb[prev], diag ? vb[cur] : nullptr, !final_only, false, ea);
+    phase_a<FAST>(a, k >= 2, vb[prev], diag ? vb[cur] : nullptr, !final_only, false, ea);
     bsum<3>(ea, part_of(a, cur) + blockIdx.x * 8);
     if (!grid_barrier(a.flags, epoch, a.spin_limit, a.status)) return;
     if (k >= 2) {
@@ -459,7 +471,7 @@ __global__ void __launch_bounds__(NT) k_gfc3d(Args a) {
       if (!grid_barrier(a.flags, epoch, a.spin_limit, a.status)) return;
     }
     double ec[3] = {0, 0, 0};
-    phase_c(a, vb[cur], true, ec);
+    phase_c<FAST>(a, vb[cur], true, ec);
     bsum<3>(ec, part_of(a, cur) + blockIdx.x * 8 + 3);
     if (!grid_barrier(a.flags, epoch, a.spin_limit, a.status)) return;
   }
@@ -544,6 +556,7 @@ struct gfc3dgpu_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   unsigned long long spin = DEFAULT_SPIN;
+  int fast = 0;  // 1: fused multiply-adds in the products (opt-in)
   long long n = 0;
   int nc = 0;
   bool ready = false;
@@ -631,12 +644,15 @@ extern "C" gfc3dgpu_ctx* gfc3dgpu_ctx_create(int device) {
     return nullptr;
   }
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gfc3d, NT, 0) != cudaSuccess || per_sm < 1) {
+  int per_sm_fast = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gfc3d<false>, NT, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_fast, k_gfc3d<true>, NT, 0) != cudaSuccess ||
+      std::min(per_sm, per_sm_fast) < 1) {
     fc3dgpu_set_error("gfc3dgpu_ctx_create: the solve kernel does not fit an SM");
     gfc3dgpu_ctx_destroy(c);
     return nullptr;
   }
-  c->grid = std::min(GRID_MAX, c->sms * std::min(per_sm, 2));
+  c->grid = std::min(GRID_MAX, c->sms * std::min(std::min(per_sm, per_sm_fast), 2));
   return c;
 }
 
@@ -999,7 +1015,8 @@ static int launch(gfc3dgpu_ctx* c, Args& a, double out[4], float* ms) {
   G2(cudaMemsetAsync(c->status, 0, sizeof(int), c->stream));
   G2(cudaEventRecord(c->ev[0], c->stream));
   void* params[] = {&a};
-  G2(cudaLaunchCooperativeKernel((const void*)k_gfc3d, dim3(c->grid), dim3(NT), params, 0, c->stream));
+  const void* kern = c->fast ? (const void*)k_gfc3d<true> : (const void*)k_gfc3d<false>;
+  G2(cudaLaunchCooperativeKernel(kern, dim3(c->grid), dim3(NT), params, 0, c->stream));
   G2(cudaEventRecord(c->ev[1], c->stream));
   int status = 0;
   G2(cudaMemcpyAsync(out, c->out, sizeof(double) * 4, cudaMemcpyDeviceToHost, c->stream));
@@ -1092,6 +1109,15 @@ extern "C" int gfc3dgpu_ctx_info(gfc3dgpu_ctx* c, int* ncomp, int* max_component
   if (diagonal) *diagonal = c->diag ? 1 : 0;
   if (bytes_per_iteration) *bytes_per_iteration = c->bytes_iter;
   if (grid) *grid = c->grid;
+  return 0;
+}
+
+extern "C" int gfc3dgpu_ctx_set_arithmetic(gfc3dgpu_ctx* c, int fused) {
+  if (!c || (fused != 0 && fused != 1)) {
+    fc3dgpu_set_error("gfc3dgpu_ctx_set_arithmetic: 0 (the reference's) or 1 (fused multiply-adds)");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  c->fast = fused;
   return 0;
 }
 

@@ -276,6 +276,7 @@ int gfc3dgpu_nsgs(GlobalFrictionContactProblem *problem, double *reaction, doubl
   gfc3dgpu_ctx *ctx = cached_ctx(options, &rc);
   if (!ctx) return rc;
   rc = upload(ctx, problem);
+  if (!rc) rc = gfc3dgpu_ctx_set_arithmetic(ctx, options->iparam[FC3DGPU_IPARAM_PRECISION] == 2);
   if (!rc) rc = gfc3dgpu_ctx_set_start(ctx, reaction, globalVelocity);
   if (rc) return rc;
   const double tol = options->dparam[SICONOS_DPARAM_TOL];

@@ -318,6 +318,7 @@ ABI = {
     "gfc3dgpu_ctx_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _DP,
                                     C.POINTER(C.c_int)]),
     "gfc3dgpu_ctx_spin_limit": (C.c_int, [C.c_void_p, C.c_ulonglong]),
+    "gfc3dgpu_ctx_set_arithmetic": (C.c_int, [C.c_void_p, C.c_int]),
     "fc3dgpu_lattice_global_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "fc3dgpu_lattice_fill_global": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _I64, _I64, _F64, _I64, _I64, _F64, _F64,
                                               _F64]),
@@ -1139,6 +1140,11 @@ class Gfc3dContext:
 
     def spin_limit(self, polls: int):
         _check(lib().gfc3dgpu_ctx_spin_limit(self.ctx, polls))
+
+    def set_arithmetic(self, fused: bool):
+        """False: the reference's products (bit-exact iterates, the default);
+        True: fused multiply-adds (opt-in, equal to rounding)."""
+        _check(lib().gfc3dgpu_ctx_set_arithmetic(self.ctx, int(bool(fused))))
 
     def close(self):
         if getattr(self, "ctx", None):

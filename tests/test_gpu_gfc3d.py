@@ -230,3 +230,35 @@ def test_wait_timeout_is_an_error_and_the_context_recovers(gpu):
         c.close()
     assert res["iterations"] == 20
     assert np.array_equal(r, g["r20"]) and np.array_equal(v, g["v20"])
+
+
+def test_fused_products_opt_in(gpu):
+    """The opt-in fused multiply-adds: iterates equal to the reference's to
+    rounding (200 iterations), the same tolerance reached in about as many
+    iterations, the result's error re-evaluated by the oracle below it; the
+    default arithmetic stays bit-exact on the same context."""
+    import oracle as O
+    P = O.lattice_global(20, 20, 10, seed=3, mu=0.3)
+    ref200 = O.gfc3d_nsgs_port(P, tol=0.0, maxiter=200)
+    ref = O.gfc3d_nsgs_port(P, tol=1e-4, maxiter=10000)
+    c = _ctx(P)
+    try:
+        c.set_arithmetic(True)
+        c.solve(0.0, 200)
+        r, u, v = c.get()
+        assert not np.array_equal(r, ref200.r)
+        assert np.linalg.norm(r - ref200.r) <= 1e-10 * np.linalg.norm(ref200.r)
+        assert np.linalg.norm(v - ref200.v) <= 1e-10 * np.linalg.norm(ref200.v)
+        c.set_start()
+        res = c.solve(1e-4, 10000)
+        r, u, v = c.get()
+        assert res["info"] == 0 and abs(res["iterations"] - ref.iterations) <= 0.02 * ref.iterations
+        e, _ = O.gfc3d_compute_error_port(P, r, v)
+        assert e < 1e-4 * (1 + 1e-9)
+        c.set_arithmetic(False)
+        c.set_start()
+        c.solve(0.0, 200)
+        r, u, v = c.get()
+        assert np.array_equal(r, ref200.r) and np.array_equal(v, ref200.v)
+    finally:
+        c.close()
