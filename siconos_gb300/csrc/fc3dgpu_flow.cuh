@@ -101,7 +101,9 @@ __device__ __forceinline__ bool flow_full_error(const SweepArgs<float>& a, unsig
 }
 
 // Wait until every block's flag shows epoch e (bounded; warp 0 polls, then
-// an acquire fence and a block barrier).
+// an acquire fence and a block barrier).  False when the wait gave up or a
+// timeout anywhere is on record: one value for the whole block (read once,
+// shared), so every warp leaves the sweep loop at the same barrier.
 __device__ __forceinline__ bool grid_wait(const unsigned* flags, unsigned e, unsigned long long limit, int* status) {
   __shared__ int s_ok;
   if (threadIdx.x < 32) {
@@ -121,7 +123,7 @@ __device__ __forceinline__ bool grid_wait(const unsigned* flags, unsigned e, uns
       if (n > 256) __nanosleep(32);
     }
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
-    if (lane == 0) s_ok = ok;
+    if (lane == 0) s_ok = ok && !(*(volatile int*)status & 1);
   }
   __syncthreads();
   return s_ok != 0;
@@ -382,7 +384,7 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
     e_last = ++epoch;
     if (threadIdx.x == 0) st_release_u32(&a.barrier[blockIdx.x * FC3D_FLAG_STRIDE], e_last);
     if (sweep < 2) continue;
-    if (!grid_wait(a.barrier, e_prev, a.spin_limit, a.status) || (*(volatile int*)a.status & 1)) {
+    if (!grid_wait(a.barrier, e_prev, a.spin_limit, a.status)) {
       aborted = true;
       break;
     }
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
   if (sweep > 0 && !aborted) {
     // the light error of the last sweep; after a budget end, the stop rules
     // on it as on every other sweep
-    if (!grid_wait(a.barrier, e_last, a.spin_limit, a.status) || (*(volatile int*)a.status & 1)) {
+    if (!grid_wait(a.barrier, e_last, a.spin_limit, a.status)) {
       aborted = true;
     } else {
       incr = light_error(sweep);
