@@ -104,7 +104,8 @@ static int csr_of(const NumericsMatrix *A, const char *name, Csr *out) {
     fc3dgpu_set_error("%s: sparse-block storage without data", name);
     return NUMERICS_ERR_NULL_POINTER;
   }
-  if ((int64_t)S->blocksize0[S->blocknumber0 - 1] != rows || (int64_t)S->blocksize1[S->blocknumber1 - 1] != cols) {
+  if (S->blocknumber0 < 1 || S->blocknumber1 < 1 || (int64_t)S->blocksize0[S->blocknumber0 - 1] != rows ||
+      (int64_t)S->blocksize1[S->blocknumber1 - 1] != cols) {
     fc3dgpu_set_error("%s: block sizes do not add up to %lld x %lld", name, (long long)rows, (long long)cols);
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }

@@ -3,7 +3,7 @@
 Run in a checkout that has the reference sources (the library in
 ``oracle/_ref`` is built from them by ``oracle/build_ref.py``):
 
-    python tests/golden/make_golden.py /path/to/reference [--only=fc2d|rfc3d|gfc3d|to_tolerance]
+    python tests/golden/make_golden.py /path/to/reference [--only=fixtures|fc2d|rfc3d|gfc3d|to_tolerance]
 
 For each SBM/dense friction-contact fixture of the reference's own test data
 (numerics/src/FrictionContact/test/data) and for the 5x5x6 lattice scene,
@@ -41,6 +41,28 @@ FIXTURES = [
     "FC3D_Example1.dat",
     "Rover4396.dat",
     "NESpheres_10_1.dat",
+    # the rest of the reference's fc3d test collection (data_collection_1.c)
+    # and OneObject from data_collection_3.c
+    "FrictionContact3D_RR_1c.dat",
+    "Capsules-i100-1090.dat",
+    "Capsules-i100-889.dat",
+    "Capsules-i101-404.dat",
+    "Capsules-i103-990.dat",
+    "Rover1039.dat",
+    "Rover1040.dat",
+    "Rover1041.dat",
+    "Rover11035.dat",
+    "Rover11211.dat",
+    "Rover3865.dat",
+    "Rover4144.dat",
+    "Rover4493.dat",
+    "Rover4516.dat",
+    "Rover4609.dat",
+    "Rover4613.dat",
+    "Rover4622.dat",
+    "Rover9770.dat",
+    "NESpheres_30_1.dat",
+    "OneObject-i100000-499.hdf5.dat",
 ]
 
 
@@ -216,12 +238,16 @@ def main(ref_root: str, only: str | None = None):
         make_fc2d(data)
         return
     for f in FIXTURES:
+        name = "fixture_" + f.replace(".hdf5", "").replace(".dat", "").replace("-", "_")
+        if only == "fixtures" and (HERE / f"{name}.npz").exists():
+            continue  # --only=fixtures: the fixtures not yet generated
         P = O.read_dat(data / f)
         full = O.nsgs_ref(P, tol=1e-8, maxiter=10000, trace_cap=20000)
         short = O.nsgs_ref(P, tol=1e-8, maxiter=20, trace_cap=20)
-        name = "fixture_" + f.replace(".hdf5", "").replace(".dat", "").replace("-", "_")
         save_case(name, P, full, short, {"source": f})
         print(f"{f}: nc={P.nc} nnzb={P.nnzb} info={full.info} it={full.iterations} err={full.error:.3e}")
+    if only == "fixtures":
+        return
 
     # lattice scenes (generator in the product library)
     from siconos_gb300 import build as B
