@@ -230,9 +230,11 @@ int fc3dgpu_ctx_counters(fc3dgpu_ctx *ctx, int enable, unsigned long long *out8)
  * staging wait and after the first slab round (entries 6, 7 spare); copies
  * the last record into out (cap entries) and returns how many were copied.
  * sweep 0 stops.  With the dataflow sweep (fc3dgpu_ctx_flow) the record is
- * per slab: out[slab*8 + {0..5}] = globaltimer before the wait for its
+ * per slab: out[slab*8 + {0..7}] = globaltimer before the wait for its
  * column slabs, after it, after its data landed in shared memory, after the
- * row products, after the local solves, and its number of local solves. */
+ * row products, after the light-error sums that follow the local solves, its
+ * number of local solves, after the next slab's bulk copies were issued (just
+ * before the local solves), and after the local solves with their stores. */
 int fc3dgpu_ctx_timeline(fc3dgpu_ctx *ctx, int sweep, unsigned long long *out, int cap);
 /* Bulk-copy (TMA) staging of each block's slab range into shared memory
  * in the FP32 sweeps: 1 on (default), 0 off.  Returns the previous value. */

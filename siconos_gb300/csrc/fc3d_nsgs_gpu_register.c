@@ -15,8 +15,8 @@
  * same way as gfc3d_nsgs.c:232-237 registers GFC3D_NSGS
  * (REGISTER_SOLVER_3VAR, solve3 = gfc3dgpu_nsgs_solve_wrap); the reference's
  * gfc3d_driver dispatches by a switch on the id (gfc3d_driver.c:120-293),
- * so a build that adds it also adds one case there that calls the
- * registry's solve3 for this id (see the integration notes).
+ * so a build that adds it also adds one case there that looks the id up in
+ * the registry and calls the entry's solve3.
  *
  * fc3dgpu.h defines the ids as macros; a build that adds them to the
  * enum of FrictionContact_options.h instead compiles this file with

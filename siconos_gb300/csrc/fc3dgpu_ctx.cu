@@ -732,6 +732,8 @@ struct fc3dgpu_ctx {
   BUF(int2, flow_need);
   BUF(int, flow_sptr);
   BUF(double, flow_part);
+  BUF(long long, flow_rec_off);
+  BUF(float, flow_rec);
   // batched problems (0 = a single problem)
   int nscenes = 0;
   std::vector<int> scene_off_h;  // nscenes + 1 contact offsets
@@ -885,7 +887,8 @@ extern "C" void fc3dgpu_ctx_destroy(fc3dgpu_ctx* c) {
                   c->ssptr, c->sorder, c->snormq, c->sbudget, c->squeue, c->sout32, c->sout64, c->feat,
                   c->prop, c->rbak, c->gapo, c->cbA, c->cbB, c->cframe, c->cpoint, c->bpos, c->bmass,
                   c->binert, c->bvel, c->bdeg, c->bptr, c->blist, c->crowlen, c->qsum, c->wtmp, c->wdiff,
-                  c->flow_dptr, c->flow_dep, c->flow_done, c->flow_need, c->flow_sptr, c->flow_part};
+                  c->flow_dptr, c->flow_dep, c->flow_done, c->flow_need, c->flow_sptr, c->flow_part,
+                  c->flow_rec_off, c->flow_rec};
   if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1764,6 +1767,12 @@ static int prepare_flow(fc3dgpu_ctx* c) {
   CK(cudaMemcpyAsync(c->flow_dptr, sptr_sym.data(), sizeof(int) * (nslab + 1), cudaMemcpyHostToDevice, s));
   if (!sym.empty()) CK(cudaMemcpyAsync(c->flow_dep, sym.data(), sizeof(int) * sym.size(), cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->flow_need, need.data(), sizeof(int2) * nslab, cudaMemcpyHostToDevice, s));
+  // offsets of the per-slab records (filled before each solve's FP32 sweeps)
+  std::vector<long long> roff((size_t)nslab + 1, 0);
+  for (int t = 0; t < nslab; t++) roff[t + 1] = roff[t] + flow_rec_floats(c->slab_nslot_h[t]);
+  CK(ensure(&c->flow_rec_off, &c->flow_rec_off_cap, (size_t)nslab + 1));
+  CK(ensure(&c->flow_rec, &c->flow_rec_cap, (size_t)std::max(roff[nslab], 1LL)));
+  CK(cudaMemcpyAsync(c->flow_rec_off, roff.data(), sizeof(long long) * (nslab + 1), cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
   c->launches += 2;
   c->flow_nw = nw;
@@ -2016,7 +2025,12 @@ static int solve_impl(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgpu_stats* st
       f.part = c->flow_part;
       f.maxslot = c->flow_maxslot;
       f.buf_bytes = flow_buf_bytes(c->flow_maxslot);
+      f.rec = c->flow_rec;
+      f.rec_off = c->flow_rec_off;
       CK(cudaMemsetAsync(c->flow_done, 0, sizeof(unsigned) * c->nslab, s));
+      CK(pack_flow_records(c->nslab, c->slab_off, c->slab_nslot, c->W32, c->col, c->q32, c->D32, c->mu32, c->rho32,
+                           c->flow_rec_off, c->flow_rec, s));
+      c->launches++;
       CK(launch_flow_f32(a, f, c->flow_nw, s, &grid));
     } else {
       CK(launch_sweep_f32(a, lanes, 0, smem, s, &grid));

@@ -32,9 +32,10 @@
 // grid barrier per sweep.
 //
 // While a warp waits for a slab's columns, the bulk-copy engine brings that
-// slab's W, column indices, q, diagonal block, mu and rho into the warp's
-// shared-memory buffer; the next slab's copy is issued as soon as the
-// current one's inputs are in registers.
+// slab's W, column indices, q, diagonal block, mu and rho (one record per
+// slab, packed before the sweeps) into the warp's shared-memory buffer; the
+// next slab's copy is issued as soon as the current one's inputs are in
+// registers.
 #pragma once
 #include "fc3dgpu_sweep.cuh"
 
@@ -45,23 +46,41 @@ namespace fc3dgpu {
 #define FC3D_FLOW_SPIN 1024
 #define FC3D_FLOW_SLEEP_NS 64
 
+// Stage slab s's record into the warp's buffer: one bulk copy completing
+// on the warp's mbarrier (six copies from the separate arrays cost about
+// 0.6 us of issue on the warp's chain of slabs).
 __device__ __forceinline__ void flow_issue(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned char* buf,
                                            unsigned long long* bar) {
-  const long long o0 = a.slab_off[s];
-  const int ns = a.slab_nslot[s];
-  const unsigned wb = (unsigned)ns * 9 * FC3D_SLAB * 4, cb = (unsigned)ns * FC3D_SLAB * 4;
-  unsigned char* sc = buf + (size_t)f.maxslot * 9 * FC3D_SLAB * 4;
-  unsigned char* sq = sc + (size_t)f.maxslot * FC3D_SLAB * 4;
-  unsigned char* sd = sq + 3 * FC3D_SLAB * 4;
-  unsigned char* sm = sd + 9 * FC3D_SLAB * 4;
-  unsigned char* sr = sm + FC3D_SLAB * 4;
-  mbar_arrive_expect_tx(bar, wb + cb + (3 + 9 + 1 + 2) * FC3D_SLAB * 4);
-  if (wb) bulk_g2s(buf, a.W + (size_t)o0 * 9 * FC3D_SLAB, wb, bar);
-  if (cb) bulk_g2s(sc, a.col + (size_t)o0 * FC3D_SLAB, cb, bar);
-  bulk_g2s(sq, a.q + (size_t)s * 3 * FC3D_SLAB, 3 * FC3D_SLAB * 4, bar);
-  bulk_g2s(sd, a.D + (size_t)s * 9 * FC3D_SLAB, 9 * FC3D_SLAB * 4, bar);
-  bulk_g2s(sm, a.mu + (size_t)s * FC3D_SLAB, FC3D_SLAB * 4, bar);
-  bulk_g2s(sr, a.rho + (size_t)s * 2 * FC3D_SLAB, 2 * FC3D_SLAB * 4, bar);
+  const unsigned bytes = flow_rec_floats(a.slab_nslot[s]) * 4;
+  mbar_arrive_expect_tx(bar, bytes);
+  bulk_g2s(buf, f.rec + f.rec_off[s], bytes, bar);
+}
+
+// The per-slab records (flow_rec_floats) from the slab-major arrays of the
+// layout; one block per slab at a time.  Run before a solve's FP32 sweeps
+// (the arrays change with W, q and mu).
+__global__ void k_flow_pack(int nslab, const long long* __restrict__ slab_off, const int* __restrict__ slab_nslot,
+                            const float* __restrict__ W, const int* __restrict__ col, const float* __restrict__ q,
+                            const float* __restrict__ D, const float* __restrict__ mu,
+                            const float* __restrict__ rho, const long long* __restrict__ rec_off,
+                            float* __restrict__ rec) {
+  for (int s = blockIdx.x; s < nslab; s += gridDim.x) {
+    const int ns = slab_nslot[s];
+    const size_t o0 = (size_t)slab_off[s];
+    float* R = rec + rec_off[s];
+    const int nw = ns * 9 * FC3D_SLAB, ncl = ns * FC3D_SLAB;
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) R[i] = W[o0 * 9 * FC3D_SLAB + i];
+    int* RC = reinterpret_cast<int*>(R + nw);
+    for (int i = threadIdx.x; i < ncl; i += blockDim.x) RC[i] = col[o0 * FC3D_SLAB + i];
+    float* RQ = R + nw + ncl;
+    for (int i = threadIdx.x; i < 3 * FC3D_SLAB; i += blockDim.x) RQ[i] = q[(size_t)s * 3 * FC3D_SLAB + i];
+    float* RD = RQ + 3 * FC3D_SLAB;
+    for (int i = threadIdx.x; i < 9 * FC3D_SLAB; i += blockDim.x) RD[i] = D[(size_t)s * 9 * FC3D_SLAB + i];
+    float* RM = RD + 9 * FC3D_SLAB;
+    for (int i = threadIdx.x; i < FC3D_SLAB; i += blockDim.x) RM[i] = mu[(size_t)s * FC3D_SLAB + i];
+    float* RR = RM + FC3D_SLAB;
+    for (int i = threadIdx.x; i < 2 * FC3D_SLAB; i += blockDim.x) RR[i] = rho[(size_t)s * 2 * FC3D_SLAB + i];
+  }
 }
 
 // Sum of N values over the block (fixed order), written to out_partials.
@@ -196,14 +215,14 @@ __device__ __forceinline__ void flow_links(const FlowArgs& f, int s, int lane, F
 __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowArgs& f, int s, int next,
                                           unsigned char* buf, unsigned long long* bar, int lane, float ltol,
                                           float rn[3], unsigned long long* tl, const FlowRow& x) {
+  const int ns = x.ns;
   const float* Ws = reinterpret_cast<const float*>(buf);
-  const int* Cs = reinterpret_cast<const int*>(buf + (size_t)f.maxslot * 9 * FC3D_SLAB * 4);
-  const float* Qs = reinterpret_cast<const float*>(Cs + (size_t)f.maxslot * FC3D_SLAB);
+  const int* Cs = reinterpret_cast<const int*>(buf + (size_t)ns * 9 * FC3D_SLAB * 4);
+  const float* Qs = reinterpret_cast<const float*>(Cs + (size_t)ns * FC3D_SLAB);
   const float* Ds = Qs + 3 * FC3D_SLAB;
   const float* Ms = Ds + 9 * FC3D_SLAB;
   const float* Rs = Ms + FC3D_SLAB;
   const int p = s * FC3D_SLAB + lane;
-  const int ns = x.ns;
   const float ro[3] = {x.ro[0], x.ro[1], x.ro[2]};
   float acc[3] = {0.f, 0.f, 0.f};
   bool work = false;
@@ -257,6 +276,7 @@ __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowA
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     flow_issue(a, f, next, buf, bar);
   }
+  if (tl) tl[6] = globaltimer_ns();
   rn[0] = rn[1] = rn[2] = 0.f;
   if (work) {
     L.rho_pli = __ldcg(&a.rpli[p]);
@@ -276,6 +296,8 @@ __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowA
     rp[2] = rn[2];
     a.rpli[p] = L.rho_pli;
   }
+  __syncwarp();
+  if (tl) tl[7] = globaltimer_ns();
 }
 
 template <int NW>

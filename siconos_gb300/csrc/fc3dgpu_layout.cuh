@@ -127,12 +127,17 @@ struct FlowArgs {
   double* part;        // per block: 4 slots of (sum |dr|^2, sum |r|^2)
   unsigned buf_bytes;  // shared-memory buffer of one warp
   int maxslot;         // slots of one slab the buffer holds
+  const float* rec;          // per slab one record of its sweep inputs (flow_rec_floats)
+  const long long* rec_off;  // float offset of slab s's record in rec
 };
 
-// Per-warp buffer: W (maxslot * 9 * 32), col (maxslot * 32), q (3 * 32),
-// D (9 * 32), mu (32), rho (2 * 32) in FP32, all 128-byte multiples.
-__host__ __device__ __forceinline__ unsigned flow_buf_bytes(int maxslot) {
-  return (unsigned)maxslot * FC3D_SLAB * (9 * 4 + 4) + FC3D_SLAB * (3 + 9 + 1 + 2) * 4;
+// Per-slab record of the FP32 inputs of a slab with ns slots, back to back:
+// W (ns * 9 * 32), col (ns * 32, int), q (3 * 32), D (9 * 32), mu (32),
+// rho (2 * 32); every part a 128-byte multiple, so one bulk copy stages a
+// slab.  The per-warp buffer holds the record of the longest slab.
+__host__ __device__ __forceinline__ unsigned flow_rec_floats(int ns) {
+  return (unsigned)ns * FC3D_SLAB * (9 + 1) + FC3D_SLAB * (3 + 9 + 1 + 2);
 }
+__host__ __device__ __forceinline__ unsigned flow_buf_bytes(int maxslot) { return flow_rec_floats(maxslot) * 4; }
 
 }  // namespace fc3dgpu

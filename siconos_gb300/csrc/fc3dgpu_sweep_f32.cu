@@ -121,6 +121,15 @@ cudaError_t launch_flow_f32(const SweepArgs<float>& a, const FlowArgs& f, int nw
   }
 }
 
+cudaError_t pack_flow_records(int nslab, const long long* slab_off, const int* slab_nslot, const float* W,
+                              const int* col, const float* q, const float* D, const float* mu, const float* rho,
+                              const long long* rec_off, float* rec, cudaStream_t s) {
+  if (nslab <= 0) return cudaSuccess;
+  const int grid = nslab < 4096 ? nslab : 4096;
+  k_flow_pack<<<grid, 256, 0, s>>>(nslab, slab_off, slab_nslot, W, col, q, D, mu, rho, rec_off, rec);
+  return cudaGetLastError();
+}
+
 cudaError_t build_flow_deps(int nslab, int npad, int ncol, const int* sptr_d, const int* perm, const int* slab_nslot,
                             const long long* slab_off, const int* col, const int* dptr, int* count, int* dep,
                             cudaStream_t s) {

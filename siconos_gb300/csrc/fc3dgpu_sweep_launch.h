@@ -34,6 +34,10 @@ int sweep_grid_f64(int lanes);
 // per-slab column lists (k_flow_deps).
 int flow_warps(int maxslot, int want);
 cudaError_t launch_flow_f32(const SweepArgs<float>& a, const FlowArgs& f, int nw, cudaStream_t s, int* grid);
+// The dataflow sweep's per-slab records from the layout's FP32 arrays.
+cudaError_t pack_flow_records(int nslab, const long long* slab_off, const int* slab_nslot, const float* W,
+                              const int* col, const float* q, const float* D, const float* mu, const float* rho,
+                              const long long* rec_off, float* rec, cudaStream_t s);
 cudaError_t build_flow_deps(int nslab, int npad, int ncol, const int* sptr_d, const int* perm, const int* slab_nslot,
                             const long long* slab_off, const int* col, const int* dptr, int* count, int* dep,
                             cudaStream_t s);
