@@ -304,14 +304,32 @@ def fc2d_granular(case="fc2d_fc2d_granularflowonwall_07002_00801", tol=1e-5, rep
                                        "error": res["error"]}
     finally:
         pc.close()
+    # the same sweep with the reference's own local-solve kernel, compiled
+    # from its source into a CUDA image beside the reference library
+    img = ROOT / "oracle" / "_ref" / "fc2d_nsgs_graph_permut_cuda.fatbin"
+    if img.exists():
+        pc = sn.Fc2dPerColour(*args)
+        try:
+            pc.use_kernel_file(img)
+            ms = []
+            for _ in range(reps):
+                res = pc.solve(tol, 10000)
+                ms.append(res["ms"])
+            out["reference_kernel_gpu"] = {"ms": statistics.median(ms), "sweeps": res["iterations"],
+                                           "info": res["info"], "error": res["error"],
+                                           "kernel": "fc2d_nsgs_local_solve_kernel_range_reduce from the reference's "
+                                                     "source (nvcc -O3, sm_103a)"}
+        finally:
+            pc.close()
     P = O.Problem(*args, 2)
     t = time.perf_counter()
     ref = O.fc2d_nsgs_port(P, tol=tol, maxiter=10000)
     out["cpu_reference_port_1core"] = {"ms": 1e3 * (time.perf_counter() - t), "sweeps": ref.iterations,
                                        "info": ref.info, "error": ref.error}
     cpu = out["cpu_reference_port_1core"]["ms"]
-    for k in ("gpu_fp64", "gpu_fp32_fp64_polish", "reference_design_gpu"):
-        out[k]["speedup_vs_cpu"] = cpu / out[k]["ms"]
+    for k in ("gpu_fp64", "gpu_fp32_fp64_polish", "reference_design_gpu", "reference_kernel_gpu"):
+        if k in out:
+            out[k]["speedup_vs_cpu"] = cpu / out[k]["ms"]
     # 40 independent copies along W's diagonal (280,080 contacts; q of each
     # copy scaled by a seeded factor in [0.9, 1.1]): colours too large for a
     # cluster, so the solve runs on a cooperative grid over every SM; the CPU
@@ -594,7 +612,7 @@ def run_ours(args):
     d.set_q_mu(s.q, s.mu)
     stream = torch.cuda.ExternalStream(d.stream(), device=f"cuda:{dev}")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
-    kw = dict(tol=TOL, max_iter=BUDGET)
+    kw = dict(tol=TOL, max_iter=BUDGET, lanes=args.lanes)
 
     def step():
         d.zero_r()
@@ -655,6 +673,7 @@ def run_ours(args):
         o = sn.SolverOptions()
         o.iparam[sn.SICONOS_IPARAM_MAX_ITER] = BUDGET
         o.dparam[sn.SICONOS_DPARAM_TOL] = TOL
+        o.iparam[sn.FC3DGPU_IPARAM_LANES] = args.lanes
         r = pinned(np.zeros(3 * s.nc))
         u = pinned(np.zeros(3 * s.nc))
 
@@ -855,6 +874,9 @@ def main():
                     help="sweeps of the CPU sample (per step for --impl reference, capped at 10 there)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the comparison solves (FP64, learned start) and the supplementary measurements")
+    ap.add_argument("--lanes", type=int, default=0, choices=[0, 1, 2, 4, 8],
+                    help="lanes per contact of the headline solves; 0 (default) lets the measuring autotuner "
+                         "pick the sweep variant, 1 fixes the dataflow sweep without tuning launches")
     ap.add_argument("--supplementary", choices=sorted(SUPPLEMENTARY), default=None,
                     help="run only this supplementary measurement and print its JSON")
     ap.add_argument("--profile", choices=["flow", "fp64", "mlp", "infer", "gfc3d"], default=None,

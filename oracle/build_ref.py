@@ -20,6 +20,15 @@ Recipe (nothing is copied out of the reference tree):
    MUMPS ... none reached on the SBM NSGS path), generate an aborting stub for
    each, and link ``oracle/_ref/libsiconos_numerics_ref.so``.
 
+4. compile the device code of the reference's 2D GPU solver
+   (``FrictionContact/parallel/gpu/fc2d_nsgs_graph_permut_cuda.cu``, its
+   local-solve kernel) with ``nvcc -fatbin`` for sm_103a into
+   ``oracle/_ref/fc2d_nsgs_graph_permut_cuda.fatbin``, with the reference's
+   Release flags (``-O3 -DNDEBUG -DSICONOS_CUDA``, default contraction): an
+   image the measurement-only per-colour comparator loads to run the
+   reference's own kernel (its host code needs PETSc's colouring and does not
+   build here).
+
 ``-ffp-contract=off`` keeps x86-64 and aarch64 builds bit-identical (gcc
 contracts a*b+c into FMA by default on aarch64).
 """
@@ -53,6 +62,9 @@ def source_dir() -> Path | None:
 def include_flags(ref: Path) -> list[str]:
     """The include path the reference's sources compile with here."""
     return _includes(Path(ref))
+
+FC2D_CUDA_SOURCE = Path("numerics/src/FrictionContact/parallel/gpu/fc2d_nsgs_graph_permut_cuda.cu")
+FC2D_CUDA_IMAGE = OUT / "fc2d_nsgs_graph_permut_cuda.fatbin"
 
 EXCLUDE_PARTS = ("/test/", "/test-utils/", "/linalg/optional/", "/FrictionContact/parallel/",
                  "/Unstable_or_deprecated/", "/tools/parallel/")
@@ -130,7 +142,36 @@ def build(ref: str | os.PathLike, verbose: bool = False) -> Path:
     SOURCE.write_text(str(ref.resolve()) + "\n")
     if verbose:
         print(f"[oracle/_ref] {len(objs)} objects, {len(failed)} skipped, {len(missing)} stubs -> {LIB}")
+    build_cuda(ref, verbose)
     return LIB
+
+
+def build_cuda(ref: str | os.PathLike, verbose: bool = False) -> Path | None:
+    """Step 4: the reference's fc2d CUDA file as an sm_103a fatbin (device
+    code only; nvcc parses the host code against the reference's headers).
+    Returns None, keeping any earlier image, when nvcc is missing or fails."""
+    ref = Path(ref)
+    src = ref / FC2D_CUDA_SOURCE
+    if not src.is_file():
+        return None
+    if FC2D_CUDA_IMAGE.exists() and FC2D_CUDA_IMAGE.stat().st_mtime > src.stat().st_mtime:
+        return FC2D_CUDA_IMAGE
+    OUT.mkdir(parents=True, exist_ok=True)
+    tmp = FC2D_CUDA_IMAGE.with_suffix(".tmp")
+    cmd = ["nvcc", "-fatbin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-DNDEBUG", "-DSICONOS_CUDA",
+           "-DCS_LONG", "-DNCOMPLEX", "-w", *_includes(ref), str(src), "-o", str(tmp)]
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+    except FileNotFoundError:
+        return None
+    if r.returncode != 0:
+        if verbose:
+            print(f"[oracle/_ref] fc2d CUDA image not built: {r.stderr[-400:]}", file=sys.stderr)
+        return None
+    os.replace(tmp, FC2D_CUDA_IMAGE)
+    if verbose:
+        print(f"[oracle/_ref] -> {FC2D_CUDA_IMAGE}")
+    return FC2D_CUDA_IMAGE
 
 
 if __name__ == "__main__":

@@ -29,7 +29,7 @@ __global__ void k_local_solve_colour(const double* __restrict__ Wd, const double
   const int i = k1 + blockIdx.x * blockDim.x + threadIdx.x;
   double p2 = 0.0, e2 = 0.0;
   if (i < k2) {
-    const double q0 = y[2 * (i - k1)] + qc[2 * i], q1 = y[2 * (i - k1) + 1] + qc[2 * i + 1];
+    const double q0 = y[2 * i] + qc[2 * i], q1 = y[2 * i + 1] + qc[2 * i + 1];
     const double* w = Wd + 4 * (size_t)i;
     const double Wnn = w[0], Wtn = w[1], Wnt = w[2], Wtt = w[3], D = det[i], m = mu[i];
     const double o0 = z[2 * i], o1 = z[2 * i + 1];
@@ -90,8 +90,12 @@ struct fc2dgpu_percolour {
   int64_t *d_ci = nullptr;
   double *d_val = nullptr, *d_Wd = nullptr, *d_det = nullptr, *d_q = nullptr, *d_mu = nullptr, *d_z = nullptr,
          *d_y = nullptr, *d_sum = nullptr;
+  std::vector<void*> work;  // SpMV work buffers per colour (owned by bufs)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // the local-solve kernel loaded from a CUDA library image, when set
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kref = nullptr;
 };
 
 #define KP(x)                                                                             \
@@ -128,6 +132,7 @@ extern "C" void fc2dgpu_percolour_destroy(fc2dgpu_percolour* h) {
     if (p) cudaFree(p);
   if (h->sp) cusparseDestroy(h->sp);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->lib) cudaLibraryUnload(h->lib);
   delete h;
 }
 
@@ -136,6 +141,48 @@ static cudaError_t put(T** d, const std::vector<T>& v) {
   cudaError_t e = cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(v.size(), 1));
   if (e == cudaSuccess && !v.empty()) e = cudaMemcpy(*d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
   return e;
+}
+
+// One sweep as a CUDA graph: a memset of the two sums, then per colour the
+// SpMV of its rows and the local-solve kernel (this file's, or the loaded
+// one with the same arguments: 256 threads, 2 x 256 doubles of dynamic
+// shared memory as fc2d_nsgs_graph_permut_cuda.cu:574-587 launches it).
+static int capture(fc2dgpu_percolour* h) {
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  h->exec = nullptr;
+  h->graph = nullptr;
+  const double one = 1.0, zero = 0.0;
+  KP(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(h->d_sum, 0, sizeof(double) * 2, h->stream);
+  cudaError_t le = cudaSuccess;
+  for (int c = 0; c < h->ncol; c++) {
+    if (!h->mats[c]) continue;
+    int lo = h->cptr[c], hi = h->cptr[c + 1];
+    const int blocks = (hi - lo + TPB - 1) / TPB;
+    cusparseSpMV(h->sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, h->mats[c], h->zvec, &zero, h->ys[c], CUDA_R_64F,
+                 CUSPARSE_SPMV_ALG_DEFAULT, h->work[c]);
+    if (h->kref) {
+      const double *Wd = h->d_Wd, *det = h->d_det, *y = h->d_y, *qc = h->d_q, *mu = h->d_mu;
+      double *z = h->d_z, *s0 = h->d_sum, *s1 = h->d_sum + 1;
+      void* args[] = {&Wd, &det, &y, &qc, &mu, &z, &s0, &s1, &lo, &hi};
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(blocks);
+      cfg.blockDim = dim3(TPB);
+      cfg.dynamicSmemBytes = 2 * TPB * sizeof(double);
+      cfg.stream = h->stream;
+      const cudaError_t e = cudaLaunchKernelExC(&cfg, (const void*)h->kref, args);
+      if (le == cudaSuccess) le = e;
+    } else {
+      k_local_solve_colour<<<blocks, TPB, 0, h->stream>>>(h->d_Wd, h->d_det, h->d_y, h->d_q, h->d_mu, h->d_z,
+                                                          h->d_sum, h->d_sum + 1, lo, hi);
+    }
+  }
+  const cudaError_t ec = cudaStreamEndCapture(h->stream, &h->graph);
+  KP(le);
+  KP(ec);
+  KP(cudaGraphInstantiate(&h->exec, h->graph, 0));
+  return 0;
 }
 
 static int setup(fc2dgpu_percolour* h, int colour_kind) {
@@ -209,7 +256,8 @@ static int setup(fc2dgpu_percolour* h, int colour_kind) {
   const double one = 1.0, zero = 0.0;
   h->mats.assign(ncol, nullptr);
   h->ys.assign(ncol, nullptr);
-  std::vector<void*> work(ncol, nullptr);
+  std::vector<void*>& work = h->work;
+  work.assign(ncol, nullptr);
   for (int c = 0; c < ncol; c++) {
     const int lo = h->cptr[c], n = h->cptr[c + 1] - lo;
     if (n == 0) continue;
@@ -223,27 +271,15 @@ static int setup(fc2dgpu_percolour* h, int colour_kind) {
     SP(cusparseCreateCsr(&h->mats[c], 2 * (int64_t)n, 2 * (int64_t)nc, last - first, d_rpc, h->d_ci + first,
                          h->d_val + first, CUSPARSE_INDEX_64I, CUSPARSE_INDEX_64I, CUSPARSE_INDEX_BASE_ZERO,
                          CUDA_R_64F));
-    SP(cusparseCreateDnVec(&h->ys[c], 2 * (int64_t)n, h->d_y, CUDA_R_64F));
+    // the colour's products land at its own rows of y (global row index)
+    SP(cusparseCreateDnVec(&h->ys[c], 2 * (int64_t)n, h->d_y + 2 * (size_t)lo, CUDA_R_64F));
     size_t sz = 0;
     SP(cusparseSpMV_bufferSize(h->sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, h->mats[c], h->zvec, &zero, h->ys[c],
                                CUDA_R_64F, CUSPARSE_SPMV_ALG_DEFAULT, &sz));
     KP(cudaMalloc(&work[c], std::max<size_t>(sz, 16)));
     h->bufs.push_back(work[c]);
   }
-  // capture one sweep
-  KP(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  cudaMemsetAsync(h->d_sum, 0, sizeof(double) * 2, h->stream);
-  for (int c = 0; c < ncol; c++) {
-    if (!h->mats[c]) continue;
-    const int lo = h->cptr[c], n = h->cptr[c + 1] - lo;
-    cusparseSpMV(h->sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, h->mats[c], h->zvec, &zero, h->ys[c], CUDA_R_64F,
-                 CUSPARSE_SPMV_ALG_DEFAULT, work[c]);
-    k_local_solve_colour<<<(n + TPB - 1) / TPB, TPB, 0, h->stream>>>(h->d_Wd, h->d_det, h->d_y, h->d_q, h->d_mu,
-                                                                     h->d_z, h->d_sum, h->d_sum + 1, lo, lo + n);
-  }
-  KP(cudaStreamEndCapture(h->stream, &h->graph));
-  KP(cudaGraphInstantiate(&h->exec, h->graph, 0));
-  return 0;
+  return capture(h);
 }
 
 extern "C" fc2dgpu_percolour* fc2dgpu_percolour_create(int device, int nc, const int64_t* rowptr,
@@ -384,6 +420,32 @@ extern "C" int fc2dgpu_percolour_solve(fc2dgpu_percolour* h, const double* r0, d
   if (info) *info = err < tol ? 0 : 1;
   if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   return 0;
+}
+
+// The reference kernel's C++ name in the image (fc2d_nsgs_graph_permut_cuda.cu:213-223:
+// five const double*, three double*, two const int).
+static const char* const REF_KERNEL = "_Z41fc2d_nsgs_local_solve_kernel_range_reducePKdS0_S0_S0_S0_PdS1_S1_ii";
+
+extern "C" int fc2dgpu_percolour_use_kernel_file(fc2dgpu_percolour* h, const char* path) {
+  if (!h || !path) return NUMERICS_ERR_INVALID_ARGUMENT;
+  KP(cudaSetDevice(h->device));
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t k = nullptr;
+  cudaError_t e = cudaLibraryLoadFromFile(&lib, path, nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) {
+    fc3dgpu_set_error("fc2dgpu_percolour_use_kernel_file: cannot load %s: %s", path, cudaGetErrorString(e));
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  e = cudaLibraryGetKernel(&k, lib, REF_KERNEL);
+  if (e != cudaSuccess) {
+    cudaLibraryUnload(lib);
+    fc3dgpu_set_error("fc2dgpu_percolour_use_kernel_file: no %s in %s: %s", REF_KERNEL, path, cudaGetErrorString(e));
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (h->lib) cudaLibraryUnload(h->lib);
+  h->lib = lib;
+  h->kref = k;
+  return capture(h);
 }
 
 extern "C" int fc2dgpu_percolour_get_r_u(fc2dgpu_percolour* h, double* r, double* u) {

@@ -332,6 +332,7 @@ COMPARATOR_ABI = {
     "fc2dgpu_percolour_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.POINTER(C.c_int), _DP,
                                           C.POINTER(C.c_int), _DP]),
     "fc2dgpu_percolour_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fc2dgpu_percolour_use_kernel_file": (C.c_int, [C.c_void_p, C.c_char_p]),
 }
 _comparator = None
 
@@ -913,6 +914,12 @@ class Fc2dPerColour:
         r, u = np.zeros(2 * self.nc), np.zeros(2 * self.nc)
         _check(comparator_lib().fc2dgpu_percolour_get_r_u(self.h, r.ctypes.data, u.ctypes.data))
         return r, u
+
+    def use_kernel_file(self, path) -> None:
+        """Run the local-solve kernel of a CUDA library image (the
+        reference's fc2d_nsgs_local_solve_kernel_range_reduce, compiled from
+        its own source) in the sweep instead of the comparator's."""
+        _check(comparator_lib().fc2dgpu_percolour_use_kernel_file(self.h, str(path).encode()))
 
     def close(self):
         if getattr(self, "h", None):

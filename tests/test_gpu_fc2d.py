@@ -262,6 +262,44 @@ def test_per_colour_design_solves_fixture(sn, case):
     pc.close()
 
 
+def test_reference_kernel_image(sn):
+    """The reference's own local-solve kernel (fc2d_nsgs_graph_permut_cuda.cu:213-300,
+    compiled from its source into oracle/_ref by oracle/build_ref.py) in the
+    comparator's sweep: after 5 sweeps its iterate equals the comparator
+    kernel's to rounding (the reference build contracts products into FMAs,
+    the comparator does not), and from zero it reaches tol 1e-5 in the
+    comparator's sweep count to within 2 %, with fc2d_compute_error of its
+    reaction below the tolerance."""
+    from pathlib import Path
+    import oracle as O
+    img = Path(O.__file__).resolve().parent / "_ref" / "fc2d_nsgs_graph_permut_cuda.fatbin"
+    if not img.exists():
+        pytest.skip("the reference's fc2d CUDA image was not built (no reference checkout)")
+    P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_02020_00213")
+    pc = sn.Fc2dPerColour(P.nc, P.rowptr, P.colidx, P.blocks, P.q, P.mu)
+    rk = sn.Fc2dPerColour(P.nc, P.rowptr, P.colidx, P.blocks, P.q, P.mu)
+    try:
+        rk.use_kernel_file(img)
+        a = pc.solve(0.0, 5)
+        b = rk.solve(0.0, 5)
+        assert a["iterations"] == b["iterations"] == 5
+        ra, _ = pc.get_r_u()
+        rb, _ = rk.get_r_u()
+        np.testing.assert_allclose(rb, ra, rtol=0, atol=1e-10 * max(1.0, np.abs(ra).max()))
+        a = pc.solve(1e-5, 10000)
+        b = rk.solve(1e-5, 10000)
+        assert a["info"] == 0 and b["info"] == 0
+        assert abs(b["iterations"] - a["iterations"]) <= max(2, 0.02 * a["iterations"])
+        rb, _ = rk.get_r_u()
+        e, _ = O.fc2d_compute_error_port(P, rb)
+        assert e < 1e-5 and e == pytest.approx(b["error"], rel=1e-14, abs=0)
+        with pytest.raises(RuntimeError):
+            rk.use_kernel_file(img.with_name("no_such_image.fatbin"))
+    finally:
+        pc.close()
+        rk.close()
+
+
 def test_fp32_phase_bit_exact(sn):
     """The FP32 phase of the mixed mode is the single-precision sweep of the
     oracle (oracle_fc2d_sweeps_f32) in colour order, bit for bit: 20 FP32
