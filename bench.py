@@ -306,19 +306,24 @@ def fc2d_granular(case="fc2d_fc2d_granularflowonwall_07002_00801", tol=1e-5, rep
         pc.close()
     # the same sweep with the reference's own local-solve kernel, compiled
     # from its source into a CUDA image beside the reference library
-    img = ROOT / "oracle" / "_ref" / "fc2d_nsgs_graph_permut_cuda.fatbin"
-    if img.exists():
+    # (scalar-CSR SpMVs in a graph; the BLOCKLEGACY file's BSR matvecs
+    # without a graph)
+    for key, name, bsr in (("reference_kernel_gpu", "fc2d_nsgs_graph_permut_cuda", False),
+                           ("reference_blocklegacy_kernel_gpu", "fc2d_nsgs_graph_permut_cuda_blocklegacy", True)):
+        img = ROOT / "oracle" / "_ref" / f"{name}.fatbin"
+        if not img.exists():
+            continue
         pc = sn.Fc2dPerColour(*args)
         try:
             pc.use_kernel_file(img)
+            pc.use_bsr(bsr)
             ms = []
             for _ in range(reps):
                 res = pc.solve(tol, 10000)
                 ms.append(res["ms"])
-            out["reference_kernel_gpu"] = {"ms": statistics.median(ms), "sweeps": res["iterations"],
-                                           "info": res["info"], "error": res["error"],
-                                           "kernel": "fc2d_nsgs_local_solve_kernel_range_reduce from the reference's "
-                                                     "source (nvcc -O3, sm_103a)"}
+            out[key] = {"ms": statistics.median(ms), "sweeps": res["iterations"], "info": res["info"],
+                        "error": res["error"], "kernel": f"the local-solve kernel of the reference's {name}.cu, "
+                                                         "compiled from its source (nvcc -O3, sm_103a)"}
         finally:
             pc.close()
     P = O.Problem(*args, 2)
@@ -327,7 +332,8 @@ def fc2d_granular(case="fc2d_fc2d_granularflowonwall_07002_00801", tol=1e-5, rep
     out["cpu_reference_port_1core"] = {"ms": 1e3 * (time.perf_counter() - t), "sweeps": ref.iterations,
                                        "info": ref.info, "error": ref.error}
     cpu = out["cpu_reference_port_1core"]["ms"]
-    for k in ("gpu_fp64", "gpu_fp32_fp64_polish", "reference_design_gpu", "reference_kernel_gpu"):
+    for k in ("gpu_fp64", "gpu_fp32_fp64_polish", "reference_design_gpu", "reference_kernel_gpu",
+              "reference_blocklegacy_kernel_gpu"):
         if k in out:
             out[k]["speedup_vs_cpu"] = cpu / out[k]["ms"]
     # 40 independent copies along W's diagonal (280,080 contacts; q of each

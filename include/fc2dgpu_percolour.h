@@ -41,15 +41,25 @@ void fc2dgpu_percolour_destroy(fc2dgpu_percolour *h);
  * iteration loop (graph replays and the per-sweep copies included). */
 int fc2dgpu_percolour_solve(fc2dgpu_percolour *h, const double *r0, double tol, int max_iter, int *iters,
                             double *error, int *info, double *ms);
-/* Run the reference's own local-solve kernel in the captured sweep instead of
- * this library's: `path` names a CUDA library image (cubin or fatbin for this
+/* Run the reference's own local-solve kernel in the sweep instead of this
+ * library's: `path` names a CUDA library image (cubin or fatbin for this
  * device) holding fc2d_nsgs_local_solve_kernel_range_reduce compiled from
- * fc2d_nsgs_graph_permut_cuda.cu:213-300 (C++ linkage; arguments as that
+ * fc2d_nsgs_graph_permut_cuda.cu:213-300, or ..._range_reduce_2 from
+ * fc2d_nsgs_graph_permut_cuda_blocklegacy.cu:215-300 (C++ linkage; arguments as that
  * file launches it at :583-586: colour range [k1, k2) in the permuted
  * numbering, SpMV output indexed by the global row).  The sweep graph is
  * recaptured; 0 on success, NUMERICS_ERR_INVALID_ARGUMENT when the image
  * does not load or lacks the kernel (message in fc3dgpu_last_error). */
 int fc2dgpu_percolour_use_kernel_file(fc2dgpu_percolour *h, const char *path);
+/* on = 1: sweep as the reference's BLOCKLEGACY variant
+ * (SICONOS_FRICTION_2D_NSGS_GRAPH_PERMUT_CUDA_BLOCKLEGACY,
+ * fc2d_nsgs_graph_permut_cuda_blocklegacy.cu:380-567): per colour
+ * cusparseDbsrmv of its block rows (2x2 blocks, column-major, int32 indices,
+ * diagonal blocks kept with zero values) and the local-solve kernel, issued
+ * every sweep without a graph; 0: back to the graph of scalar-CSR SpMVs.
+ * The kernel is this library's or the image's (..._range_reduce_2 in an
+ * image of the BLOCKLEGACY file). */
+int fc2dgpu_percolour_use_bsr(fc2dgpu_percolour *h, int on);
 /* Reaction and velocity of the last solve in contact order. */
 int fc2dgpu_percolour_get_r_u(fc2dgpu_percolour *h, double *r, double *u);
 

@@ -20,10 +20,10 @@ Recipe (nothing is copied out of the reference tree):
    MUMPS ... none reached on the SBM NSGS path), generate an aborting stub for
    each, and link ``oracle/_ref/libsiconos_numerics_ref.so``.
 
-4. compile the device code of the reference's 2D GPU solver
-   (``FrictionContact/parallel/gpu/fc2d_nsgs_graph_permut_cuda.cu``, its
-   local-solve kernel) with ``nvcc -fatbin`` for sm_103a into
-   ``oracle/_ref/fc2d_nsgs_graph_permut_cuda.fatbin``, with the reference's
+4. compile the device code of the reference's 2D GPU solvers
+   (``FrictionContact/parallel/gpu/fc2d_nsgs_graph_permut_cuda.cu`` and
+   ``..._blocklegacy.cu``, their local-solve kernels) with ``nvcc -fatbin``
+   for sm_103a into ``oracle/_ref/<file>.fatbin``, with the reference's
    Release flags (``-O3 -DNDEBUG -DSICONOS_CUDA``, default contraction): an
    image the measurement-only per-colour comparator loads to run the
    reference's own kernel (its host code needs PETSc's colouring and does not
@@ -63,8 +63,10 @@ def include_flags(ref: Path) -> list[str]:
     """The include path the reference's sources compile with here."""
     return _includes(Path(ref))
 
-FC2D_CUDA_SOURCE = Path("numerics/src/FrictionContact/parallel/gpu/fc2d_nsgs_graph_permut_cuda.cu")
+FC2D_CUDA_SOURCES = (Path("numerics/src/FrictionContact/parallel/gpu/fc2d_nsgs_graph_permut_cuda.cu"),
+                     Path("numerics/src/FrictionContact/parallel/gpu/fc2d_nsgs_graph_permut_cuda_blocklegacy.cu"))
 FC2D_CUDA_IMAGE = OUT / "fc2d_nsgs_graph_permut_cuda.fatbin"
+FC2D_CUDA_IMAGE_BLOCKLEGACY = OUT / "fc2d_nsgs_graph_permut_cuda_blocklegacy.fatbin"
 
 EXCLUDE_PARTS = ("/test/", "/test-utils/", "/linalg/optional/", "/FrictionContact/parallel/",
                  "/Unstable_or_deprecated/", "/tools/parallel/")
@@ -146,36 +148,34 @@ def build(ref: str | os.PathLike, verbose: bool = False) -> Path:
     return LIB
 
 
-def build_cuda(ref: str | os.PathLike, verbose: bool = False) -> Path | None:
-    """Step 4: the reference's fc2d CUDA file as an sm_103a fatbin (device
+def build_cuda(ref: str | os.PathLike, verbose: bool = False) -> list[Path]:
+    """Step 4: the reference's two fc2d CUDA files as sm_103a fatbins (device
     code only; nvcc parses the host code against the reference's headers).
-    Returns None, keeping any earlier image, when nvcc is missing or fails."""
+    Returns the images present; an image whose compile fails (or with no nvcc)
+    is left out, keeping any earlier one."""
     ref = Path(ref)
-    src = ref / FC2D_CUDA_SOURCE
-    if not src.is_file():
-        return None
-    if FC2D_CUDA_IMAGE.exists() and FC2D_CUDA_IMAGE.stat().st_mtime > src.stat().st_mtime:
-        return FC2D_CUDA_IMAGE
-    OUT.mkdir(parents=True, exist_ok=True)
-    tmp = FC2D_CUDA_IMAGE.with_suffix(".tmp")
-    cmd = ["nvcc", "-fatbin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-DNDEBUG", "-DSICONOS_CUDA",
-           "-DCS_LONG", "-DNCOMPLEX", "-w", *_includes(ref), str(src), "-o", str(tmp)]
-    try:
-        r = subprocess.run(cmd, capture_output=True, text=True)
-    except FileNotFoundError:
-        return None
-    if r.returncode != 0:
+    out = []
+    for rel, img in zip(FC2D_CUDA_SOURCES, (FC2D_CUDA_IMAGE, FC2D_CUDA_IMAGE_BLOCKLEGACY)):
+        src = ref / rel
+        if not src.is_file():
+            continue
+        if img.exists() and img.stat().st_mtime > src.stat().st_mtime:
+            out.append(img)
+            continue
+        OUT.mkdir(parents=True, exist_ok=True)
+        tmp = img.with_suffix(".tmp")
+        cmd = ["nvcc", "-fatbin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-DNDEBUG", "-DSICONOS_CUDA",
+               "-DCS_LONG", "-DNCOMPLEX", "-w", *_includes(ref), str(src), "-o", str(tmp)]
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True)
+        except FileNotFoundError:
+            return out
+        if r.returncode != 0:
+            if verbose:
+                print(f"[oracle/_ref] {img.name} not built: {r.stderr[-400:]}", file=sys.stderr)
+            continue
+        os.replace(tmp, img)
         if verbose:
-            print(f"[oracle/_ref] fc2d CUDA image not built: {r.stderr[-400:]}", file=sys.stderr)
-        return None
-    os.replace(tmp, FC2D_CUDA_IMAGE)
-    if verbose:
-        print(f"[oracle/_ref] -> {FC2D_CUDA_IMAGE}")
-    return FC2D_CUDA_IMAGE
-
-
-if __name__ == "__main__":
-    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(ENV)
-    if not src:
-        sys.exit(f"usage: python oracle/build_ref.py <reference checkout>  (or set {ENV})")
-    build(src, verbose=True)
+            print(f"[oracle/_ref] -> {img}")
+        out.append(img)
+    return out

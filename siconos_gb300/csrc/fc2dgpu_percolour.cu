@@ -96,6 +96,14 @@ struct fc2dgpu_percolour {
   // the local-solve kernel loaded from a CUDA library image, when set
   cudaLibrary_t lib = nullptr;
   cudaKernel_t kref = nullptr;
+  // block-sparse sweep (the reference's BLOCKLEGACY variant): per colour a
+  // BSR matvec of 2x2 blocks (diagonal blocks kept with zero values), int32
+  // indices, launched each sweep without a graph
+  bool bsr = false;
+  cusparseMatDescr_t descr = nullptr;
+  std::vector<int> bsr_cnnz;  // first block of each colour, and the end
+  int *d_brp = nullptr, *d_bci = nullptr;
+  double* d_bval = nullptr;
 };
 
 #define KP(x)                                                                             \
@@ -133,6 +141,10 @@ extern "C" void fc2dgpu_percolour_destroy(fc2dgpu_percolour* h) {
   if (h->sp) cusparseDestroy(h->sp);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->lib) cudaLibraryUnload(h->lib);
+  if (h->descr) cusparseDestroyMatDescr(h->descr);
+  void* bptrs[] = {h->d_brp, h->d_bci, h->d_bval};
+  for (void* p : bptrs)
+    if (p) cudaFree(p);
   delete h;
 }
 
@@ -141,6 +153,26 @@ static cudaError_t put(T** d, const std::vector<T>& v) {
   cudaError_t e = cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(v.size(), 1));
   if (e == cudaSuccess && !v.empty()) e = cudaMemcpy(*d, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
   return e;
+}
+
+// The local-solve kernel of colour range [lo, hi): this file's, or the loaded
+// one with the same arguments.
+static cudaError_t launch_local(fc2dgpu_percolour* h, int lo, int hi) {
+  const int blocks = (hi - lo + TPB - 1) / TPB;
+  if (h->kref) {
+    const double *Wd = h->d_Wd, *det = h->d_det, *y = h->d_y, *qc = h->d_q, *mu = h->d_mu;
+    double *z = h->d_z, *s0 = h->d_sum, *s1 = h->d_sum + 1;
+    void* args[] = {&Wd, &det, &y, &qc, &mu, &z, &s0, &s1, &lo, &hi};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(TPB);
+    cfg.dynamicSmemBytes = 2 * TPB * sizeof(double);
+    cfg.stream = h->stream;
+    return cudaLaunchKernelExC(&cfg, (const void*)h->kref, args);
+  }
+  k_local_solve_colour<<<blocks, TPB, 0, h->stream>>>(h->d_Wd, h->d_det, h->d_y, h->d_q, h->d_mu, h->d_z, h->d_sum,
+                                                      h->d_sum + 1, lo, hi);
+  return cudaGetLastError();
 }
 
 // One sweep as a CUDA graph: a memset of the two sums, then per colour the
@@ -158,25 +190,10 @@ static int capture(fc2dgpu_percolour* h) {
   cudaError_t le = cudaSuccess;
   for (int c = 0; c < h->ncol; c++) {
     if (!h->mats[c]) continue;
-    int lo = h->cptr[c], hi = h->cptr[c + 1];
-    const int blocks = (hi - lo + TPB - 1) / TPB;
     cusparseSpMV(h->sp, CUSPARSE_OPERATION_NON_TRANSPOSE, &one, h->mats[c], h->zvec, &zero, h->ys[c], CUDA_R_64F,
                  CUSPARSE_SPMV_ALG_DEFAULT, h->work[c]);
-    if (h->kref) {
-      const double *Wd = h->d_Wd, *det = h->d_det, *y = h->d_y, *qc = h->d_q, *mu = h->d_mu;
-      double *z = h->d_z, *s0 = h->d_sum, *s1 = h->d_sum + 1;
-      void* args[] = {&Wd, &det, &y, &qc, &mu, &z, &s0, &s1, &lo, &hi};
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(blocks);
-      cfg.blockDim = dim3(TPB);
-      cfg.dynamicSmemBytes = 2 * TPB * sizeof(double);
-      cfg.stream = h->stream;
-      const cudaError_t e = cudaLaunchKernelExC(&cfg, (const void*)h->kref, args);
-      if (le == cudaSuccess) le = e;
-    } else {
-      k_local_solve_colour<<<blocks, TPB, 0, h->stream>>>(h->d_Wd, h->d_det, h->d_y, h->d_q, h->d_mu, h->d_z,
-                                                          h->d_sum, h->d_sum + 1, lo, hi);
-    }
+    const cudaError_t e = launch_local(h, h->cptr[c], h->cptr[c + 1]);
+    if (le == cudaSuccess) le = e;
   }
   const cudaError_t ec = cudaStreamEndCapture(h->stream, &h->graph);
   KP(le);
@@ -377,6 +394,64 @@ static int pull_z(fc2dgpu_percolour* h) {
   return 0;
 }
 
+// One sweep of the block-sparse variant (fc2d_nsgs_graph_permut_cuda_blocklegacy.cu:533-567):
+// the sums cleared, then per colour cusparseDbsrmv of its block rows (column-
+// major 2x2 blocks) into y at its rows, and the local-solve kernel.
+static int bsr_sweep(fc2dgpu_percolour* h) {
+  const double one = 1.0, zero = 0.0;
+  KP(cudaMemsetAsync(h->d_sum, 0, sizeof(double) * 2, h->stream));
+  for (int c = 0; c < h->ncol; c++) {
+    const int lo = h->cptr[c], hi = h->cptr[c + 1];
+    if (hi == lo) continue;
+    const int first = h->bsr_cnnz[c], nnz = h->bsr_cnnz[c + 1] - first;
+    SP(cusparseDbsrmv(h->sp, CUSPARSE_DIRECTION_COLUMN, CUSPARSE_OPERATION_NON_TRANSPOSE, hi - lo, h->nc, nnz, &one,
+                      h->descr, h->d_bval + 4 * (size_t)first, h->d_brp + lo + c, h->d_bci + first, 2, h->d_z, &zero,
+                      h->d_y + 2 * (size_t)lo));
+    KP(launch_local(h, lo, hi));
+  }
+  return 0;
+}
+
+extern "C" int fc2dgpu_percolour_use_bsr(fc2dgpu_percolour* h, int on) {
+  if (!h) return NUMERICS_ERR_INVALID_ARGUMENT;
+  KP(cudaSetDevice(h->device));
+  if (on && !h->d_brp) {
+    const int nc = h->nc;
+    // permuted block rows in colour order, columns in the permuted numbering
+    // (sorted), the diagonal block kept with zero values; per colour a row
+    // pointer of its own (nc + colours entries)
+    std::vector<int> rp, ci;
+    std::vector<double> val;
+    std::vector<std::pair<int, int64_t>> row;
+    h->bsr_cnnz.assign(h->ncol + 1, 0);
+    for (int c = 0; c < h->ncol; c++) {
+      const int base = (int)ci.size();
+      h->bsr_cnnz[c] = base;
+      for (int p = h->cptr[c]; p < h->cptr[c + 1]; p++) {
+        rp.push_back((int)ci.size() - base);
+        const int i = h->perm[p];
+        row.clear();
+        for (int64_t k = h->rowptr[i]; k < h->rowptr[i + 1]; k++) row.push_back({h->iperm[h->colidx[k]], k});
+        std::sort(row.begin(), row.end());
+        for (auto& e : row) {
+          ci.push_back(e.first);
+          for (int t = 0; t < 4; t++) val.push_back(e.first == p ? 0.0 : h->blocks[4 * e.second + t]);
+        }
+      }
+      rp.push_back((int)ci.size() - base);
+    }
+    h->bsr_cnnz[h->ncol] = (int)ci.size();
+    KP(put(&h->d_brp, rp));
+    KP(put(&h->d_bci, ci));
+    KP(put(&h->d_bval, val));
+    SP(cusparseCreateMatDescr(&h->descr));
+    SP(cusparseSetMatIndexBase(h->descr, CUSPARSE_INDEX_BASE_ZERO));
+    SP(cusparseSetMatType(h->descr, CUSPARSE_MATRIX_TYPE_GENERAL));
+  }
+  h->bsr = on != 0;
+  return 0;
+}
+
 extern "C" int fc2dgpu_percolour_solve(fc2dgpu_percolour* h, const double* r0, double tol, int max_iter, int* iters,
                                        double* error, int* info, double* ms) {
   if (!h || max_iter < 0) return NUMERICS_ERR_INVALID_ARGUMENT;
@@ -392,7 +467,11 @@ extern "C" int fc2dgpu_percolour_solve(fc2dgpu_percolour* h, const double* r0, d
   double tolerance = tol, err = INFINITY;
   int iter = 0, not_conv = 1;
   while (iter < max_iter && not_conv) {
-    KP(cudaGraphLaunch(h->exec, h->stream));
+    if (h->bsr) {
+      if (int rc = bsr_sweep(h)) return rc;
+    } else {
+      KP(cudaGraphLaunch(h->exec, h->stream));
+    }
     double e2 = 0.0, p2 = 0.0;
     KP(cudaMemcpyAsync(&e2, h->d_sum + 1, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     KP(cudaStreamSynchronize(h->stream));
@@ -422,9 +501,12 @@ extern "C" int fc2dgpu_percolour_solve(fc2dgpu_percolour* h, const double* r0, d
   return 0;
 }
 
-// The reference kernel's C++ name in the image (fc2d_nsgs_graph_permut_cuda.cu:213-223:
-// five const double*, three double*, two const int).
-static const char* const REF_KERNEL = "_Z41fc2d_nsgs_local_solve_kernel_range_reducePKdS0_S0_S0_S0_PdS1_S1_ii";
+// The reference kernels' C++ names (five const double*, three double*, two
+// const int): fc2d_nsgs_graph_permut_cuda.cu:213-223 and
+// fc2d_nsgs_graph_permut_cuda_blocklegacy.cu:215-224.
+static const char* const REF_KERNELS[] = {
+    "_Z41fc2d_nsgs_local_solve_kernel_range_reducePKdS0_S0_S0_S0_PdS1_S1_ii",
+    "_Z43fc2d_nsgs_local_solve_kernel_range_reduce_2PKdS0_S0_S0_S0_PdS1_S1_ii"};
 
 extern "C" int fc2dgpu_percolour_use_kernel_file(fc2dgpu_percolour* h, const char* path) {
   if (!h || !path) return NUMERICS_ERR_INVALID_ARGUMENT;
@@ -433,13 +515,18 @@ extern "C" int fc2dgpu_percolour_use_kernel_file(fc2dgpu_percolour* h, const cha
   cudaKernel_t k = nullptr;
   cudaError_t e = cudaLibraryLoadFromFile(&lib, path, nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e != cudaSuccess) {
+    cudaGetLastError();  // the failed load is reported here, not by a later launch check
     fc3dgpu_set_error("fc2dgpu_percolour_use_kernel_file: cannot load %s: %s", path, cudaGetErrorString(e));
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
-  e = cudaLibraryGetKernel(&k, lib, REF_KERNEL);
+  for (const char* name : REF_KERNELS) {
+    e = cudaLibraryGetKernel(&k, lib, name);
+    if (e == cudaSuccess) break;
+  }
   if (e != cudaSuccess) {
     cudaLibraryUnload(lib);
-    fc3dgpu_set_error("fc2dgpu_percolour_use_kernel_file: no %s in %s: %s", REF_KERNEL, path, cudaGetErrorString(e));
+    cudaGetLastError();
+    fc3dgpu_set_error("fc2dgpu_percolour_use_kernel_file: no reference local-solve kernel in %s", path);
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
   if (h->lib) cudaLibraryUnload(h->lib);

@@ -333,6 +333,7 @@ COMPARATOR_ABI = {
                                           C.POINTER(C.c_int), _DP]),
     "fc2dgpu_percolour_get_r_u": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fc2dgpu_percolour_use_kernel_file": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "fc2dgpu_percolour_use_bsr": (C.c_int, [C.c_void_p, C.c_int]),
 }
 _comparator = None
 
@@ -920,6 +921,11 @@ class Fc2dPerColour:
         reference's fc2d_nsgs_local_solve_kernel_range_reduce, compiled from
         its own source) in the sweep instead of the comparator's."""
         _check(comparator_lib().fc2dgpu_percolour_use_kernel_file(self.h, str(path).encode()))
+
+    def use_bsr(self, on: bool = True) -> None:
+        """Sweep as the reference's BLOCKLEGACY variant: per colour a
+        cuSPARSE BSR matvec of 2x2 blocks and the local solve, no graph."""
+        _check(comparator_lib().fc2dgpu_percolour_use_bsr(self.h, int(on)))
 
     def close(self):
         if getattr(self, "h", None):

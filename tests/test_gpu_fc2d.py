@@ -262,17 +262,21 @@ def test_per_colour_design_solves_fixture(sn, case):
     pc.close()
 
 
-def test_reference_kernel_image(sn):
-    """The reference's own local-solve kernel (fc2d_nsgs_graph_permut_cuda.cu:213-300,
-    compiled from its source into oracle/_ref by oracle/build_ref.py) in the
-    comparator's sweep: after 5 sweeps its iterate equals the comparator
+@pytest.mark.parametrize("variant", ["graph", "blocklegacy"])
+def test_reference_kernel_image(sn, variant):
+    """The reference's own local-solve kernels, compiled from their sources
+    into oracle/_ref by oracle/build_ref.py, in the comparator's sweep:
+    fc2d_nsgs_graph_permut_cuda.cu:213-300 after scalar-CSR SpMVs in a graph,
+    and fc2d_nsgs_graph_permut_cuda_blocklegacy.cu:215-300 after a BSR matvec
+    per colour (:533-567).  After 5 sweeps the iterate equals the comparator
     kernel's to rounding (the reference build contracts products into FMAs,
-    the comparator does not), and from zero it reaches tol 1e-5 in the
-    comparator's sweep count to within 2 %, with fc2d_compute_error of its
-    reaction below the tolerance."""
+    the comparator does not; the BSR matvec sums in another order), and from
+    zero the solve reaches tol 1e-5 in the comparator's sweep count to within
+    2 %, with fc2d_compute_error of its reaction below the tolerance."""
     from pathlib import Path
     import oracle as O
-    img = Path(O.__file__).resolve().parent / "_ref" / "fc2d_nsgs_graph_permut_cuda.fatbin"
+    name = "fc2d_nsgs_graph_permut_cuda" + ("_blocklegacy" if variant == "blocklegacy" else "")
+    img = Path(O.__file__).resolve().parent / "_ref" / f"{name}.fatbin"
     if not img.exists():
         pytest.skip("the reference's fc2d CUDA image was not built (no reference checkout)")
     P, _ = load_fc2d("fc2d_fc2d_granularflowonwall_02020_00213")
@@ -280,6 +284,8 @@ def test_reference_kernel_image(sn):
     rk = sn.Fc2dPerColour(P.nc, P.rowptr, P.colidx, P.blocks, P.q, P.mu)
     try:
         rk.use_kernel_file(img)
+        if variant == "blocklegacy":
+            rk.use_bsr(True)
         a = pc.solve(0.0, 5)
         b = rk.solve(0.0, 5)
         assert a["iterations"] == b["iterations"] == 5
@@ -298,6 +304,28 @@ def test_reference_kernel_image(sn):
     finally:
         pc.close()
         rk.close()
+
+
+def test_per_colour_bsr_matches_csr(sn):
+    """The comparator's block-sparse sweep (BSR matvec per colour, diagonal
+    blocks kept with zero values) and its scalar-CSR sweep give the same
+    iterates to rounding, and switching back restores the graph sweep."""
+    P, _ = load_fc2d("fc2d_FrictionContactProblem00727")
+    pc = sn.Fc2dPerColour(P.nc, P.rowptr, P.colidx, P.blocks, P.q, P.mu)
+    try:
+        a = pc.solve(0.0, 10)
+        ra, _ = pc.get_r_u()
+        pc.use_bsr(True)
+        b = pc.solve(0.0, 10)
+        rb, _ = pc.get_r_u()
+        assert a["iterations"] == b["iterations"] == 10
+        np.testing.assert_allclose(rb, ra, rtol=0, atol=1e-10 * max(1.0, np.abs(ra).max()))
+        pc.use_bsr(False)
+        c = pc.solve(0.0, 10)
+        rc, _ = pc.get_r_u()
+        np.testing.assert_array_equal(rc, ra)
+    finally:
+        pc.close()
 
 
 def test_fp32_phase_bit_exact(sn):
