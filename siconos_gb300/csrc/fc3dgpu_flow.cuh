@@ -49,11 +49,24 @@ namespace fc3dgpu {
 // Stage slab s's record into the warp's buffer: one bulk copy completing
 // on the warp's mbarrier (six copies from the separate arrays cost about
 // 0.6 us of issue on the warp's chain of slabs).
-__device__ __forceinline__ void flow_issue(const SweepArgs<float>& a, const FlowArgs& f, int s, unsigned char* buf,
+// The record's place and size are loaded ahead (flow_next), so the issue
+// does not wait for them on the warp's chain.
+struct FlowNext {
+  long long off;
+  unsigned bytes;
+};
+
+__device__ __forceinline__ FlowNext flow_next(const SweepArgs<float>& a, const FlowArgs& f, int s) {
+  FlowNext n;
+  n.off = __ldg(&f.rec_off[s]);
+  n.bytes = flow_rec_floats(__ldg(&a.slab_nslot[s])) * 4;
+  return n;
+}
+
+__device__ __forceinline__ void flow_issue(const FlowArgs& f, const FlowNext& n, unsigned char* buf,
                                            unsigned long long* bar) {
-  const unsigned bytes = flow_rec_floats(a.slab_nslot[s]) * 4;
-  mbar_arrive_expect_tx(bar, bytes);
-  bulk_g2s(buf, f.rec + f.rec_off[s], bytes, bar);
+  mbar_arrive_expect_tx(bar, n.bytes);
+  bulk_g2s(buf, f.rec + n.off, n.bytes, bar);
 }
 
 // The per-slab records (flow_rec_floats) from the slab-major arrays of the
@@ -212,7 +225,7 @@ __device__ __forceinline__ void flow_links(const FlowArgs& f, int s, int lane, F
 
 // The new reaction of the lane's row goes to rn (zero on take-off); the
 // light-error sums are left to the caller, after the slab's release.
-__device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowArgs& f, int s, int next,
+__device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowArgs& f, int s, const FlowNext& next,
                                           unsigned char* buf, unsigned long long* bar, int lane, float ltol,
                                           float rn[3], unsigned long long* tl, const FlowRow& x) {
   const int ns = x.ns;
@@ -272,9 +285,9 @@ __device__ __forceinline__ void flow_slab(const SweepArgs<float>& a, const FlowA
     tl[3] = globaltimer_ns();
     tl[5] = (unsigned long long)__popc(wmask);
   }
-  if (next >= 0 && lane == 0) {
+  if (lane == 0) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    flow_issue(a, f, next, buf, bar);
+    flow_issue(f, next, buf, bar);
   }
   if (tl) tl[6] = globaltimer_ns();
   rn[0] = rn[1] = rn[2] = 0.f;
@@ -316,7 +329,7 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
   unsigned parity = 0;
   bool pending = false, failed = false;
   if (gw < a.nslab) {
-    if (lane == 0) flow_issue(a, f, gw, buf, bar);
+    if (lane == 0) flow_issue(f, flow_next(a, f, gw), buf, bar);
     pending = true;
   }
   // Light errors run one sweep behind: at the end of sweep j a block
@@ -366,6 +379,9 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
     for (int s = gw; s < a.nslab && !failed; s += tw) {
       unsigned long long* tl = record ? a.timeline + (size_t)s * FC3D_TL_STRIDE : nullptr;
       if (tl) tl[0] = globaltimer_ns();
+      // the next slab of this warp: later in this sweep, else the first one
+      // of the next sweep (fetched even when no sweep follows; awaited at exit)
+      const FlowNext next = flow_next(a, f, s + tw < a.nslab ? s + tw : gw);
       FlowRow x = flow_row(a, s, lane);
       flow_links(f, s, lane, x);
       if (!flow_wait_deps(a, f, s, x.need_a * (unsigned)sweep - x.need_b, lane)) {
@@ -383,9 +399,6 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
         pending = false;
       }
       if (tl) tl[2] = globaltimer_ns();
-      // the next slab of this warp: later in this sweep, else the first one
-      // of the next sweep (fetched even when no sweep follows; awaited at exit)
-      const int next = s + tw < a.nslab ? s + tw : gw;
       float rn[3];
       flow_slab(a, f, s, next, buf, bar, lane, (float)a.local_tol, rn, tl, x);
       pending = true;
