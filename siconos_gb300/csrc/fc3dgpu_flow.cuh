@@ -182,45 +182,50 @@ __device__ __forceinline__ bool flow_wait_deps(const SweepArgs<float>& a, const 
 // Signal slab s's update to its neighbours: a fence orders the warp's
 // reaction stores (made visible to this lane by the caller's __syncwarp)
 // before the increments, which the waiting warps acquire.
-__device__ __forceinline__ void flow_signal(const FlowArgs& f, int d0, int d1, int dep0, int lane) {
+// The lane's first two entries of the neighbour list come loaded (dep0,
+// dep1), so no load waits between the fence and the increments for up to 64
+// neighbours.
+__device__ __forceinline__ void flow_signal(const FlowArgs& f, int d0, int d1, int dep0, int dep1, int lane) {
   __threadfence();
-  for (int i = d0 + lane; i < d1; i += 32) {
-    const int d = i == d0 + lane ? dep0 : __ldg(&f.dep[i]);
-    atomicAdd(&f.done[d & 0x7fffffff], 1u);
-  }
+  const int i0 = d0 + lane;
+  if (i0 < d1) atomicAdd(&f.done[dep0 & 0x7fffffff], 1u);
+  if (i0 + 32 < d1) atomicAdd(&f.done[dep1 & 0x7fffffff], 1u);
+  for (int i = i0 + 64; i < d1; i += 32) atomicAdd(&f.done[__ldg(&f.dep[i]) & 0x7fffffff], 1u);
 }
 
 // Row product, take-off test and local solve of the 32 rows of slab s from
 // the warp's buffer; issues the copy of slab `next` (or none when next < 0)
 // once the buffer is read.
 // Inputs of slab s the columns' state does not affect: the row's presence,
-// the slab's slot count and the row's own reaction (only this warp writes
-// it), loaded before the wait for the column slabs.
+// the slab's slot count, its neighbour list and wait rule (static, loaded a
+// slab ahead by flow_static, so they are in registers when the slab starts)
+// and the row's own reaction (only this warp writes it; loaded at the slab's
+// start, with the wait for the column slabs).
 struct FlowRow {
   bool row;
   int ns;
   float ro[3];
-  int d0, d1, dep0;  // the slab's neighbour list, and this lane's first entry
+  int d0, d1, dep0, dep1;  // the slab's neighbour list, and this lane's first two entries
   unsigned need_a, need_b;  // wait for sweep k: counter >= need_a * k - need_b
 };
 
-__device__ __forceinline__ FlowRow flow_row(const SweepArgs<float>& a, int s, int lane) {
+__device__ __forceinline__ FlowRow flow_static(const SweepArgs<float>& a, const FlowArgs& f, int s, int lane) {
   FlowRow x;
-  const int p = s * FC3D_SLAB + lane;
-  x.row = __ldg(&a.perm[p]) >= 0;
+  x.row = __ldg(&a.perm[s * FC3D_SLAB + lane]) >= 0;
   x.ns = __ldg(&a.slab_nslot[s]);
-  x.ro[0] = x.ro[1] = x.ro[2] = 0.f;
-  if (x.row) load_r3<float>(a.r, p, x.ro);
-  return x;
-}
-
-__device__ __forceinline__ void flow_links(const FlowArgs& f, int s, int lane, FlowRow& x) {
   x.d0 = __ldg(&f.dptr[s]);
   x.d1 = __ldg(&f.dptr[s + 1]);
   x.dep0 = x.d0 + lane < x.d1 ? __ldg(&f.dep[x.d0 + lane]) : 0;
+  x.dep1 = x.d0 + lane + 32 < x.d1 ? __ldg(&f.dep[x.d0 + lane + 32]) : 0;
   const int2 nd = __ldg(&f.need[s]);
   x.need_a = (unsigned)nd.x;
   x.need_b = (unsigned)nd.y;
+  x.ro[0] = x.ro[1] = x.ro[2] = 0.f;
+  return x;
+}
+
+__device__ __forceinline__ void flow_own_r(const SweepArgs<float>& a, int s, int lane, FlowRow& x) {
+  if (x.row) load_r3<float>(a.r, s * FC3D_SLAB + lane, x.ro);
 }
 
 // The new reaction of the lane's row goes to rn (zero on take-off); the
@@ -328,9 +333,11 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
   const int gw = blockIdx.x * NW + w, tw = gridDim.x * NW;
   unsigned parity = 0;
   bool pending = false, failed = false;
+  FlowRow xs;  // the static inputs of the warp's next slab
   if (gw < a.nslab) {
     if (lane == 0) flow_issue(f, flow_next(a, f, gw), buf, bar);
     pending = true;
+    xs = flow_static(a, f, gw, lane);
   }
   // Light errors run one sweep behind: at the end of sweep j a block
   // publishes its partial sums of sweep j (slot j mod 4 of f.part) and its
@@ -381,9 +388,11 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
       if (tl) tl[0] = globaltimer_ns();
       // the next slab of this warp: later in this sweep, else the first one
       // of the next sweep (fetched even when no sweep follows; awaited at exit)
-      const FlowNext next = flow_next(a, f, s + tw < a.nslab ? s + tw : gw);
-      FlowRow x = flow_row(a, s, lane);
-      flow_links(f, s, lane, x);
+      const int sn = s + tw < a.nslab ? s + tw : gw;
+      const FlowNext next = flow_next(a, f, sn);
+      FlowRow x = xs;
+      xs = flow_static(a, f, sn, lane);
+      flow_own_r(a, s, lane, x);
       if (!flow_wait_deps(a, f, s, x.need_a * (unsigned)sweep - x.need_b, lane)) {
         failed = true;
         break;
@@ -412,7 +421,7 @@ __global__ void __launch_bounds__(NW * 32, 1) nsgs_flow_kernel(const SweepArgs<f
       }
       __syncwarp();
       if (tl) tl[4] = globaltimer_ns();
-      flow_signal(f, x.d0, x.d1, x.dep0, lane);
+      flow_signal(f, x.d0, x.d1, x.dep0, x.dep1, lane);
     }
     flow_block_sum<2, NW>(acc, f.part + blockIdx.x * 8 + (sweep & 3) * 2);
     e_prev = e_last;
