@@ -24,12 +24,26 @@
  * The outcome depends only on the graph and the input colouring, not on the
  * order of the adjacency lists: candidates are taken in index order, colour
  * pairs in an order set by the colours around the candidate and its
- * lowest-index neighbour, and a Kempe component is exchanged whole. */
+ * lowest-index neighbour, and a Kempe component is exchanged whole.
+ *
+ * Most of the time goes to the Kempe searches, and their components grow with
+ * the lattice (on 60x60x30 a tenth of the exchanges move more than 64
+ * contacts, a few more than 1,000).  Trying every pair with a small search
+ * cap before any pair with a larger one prefers short components: 1.35x less
+ * time than taking the first pair that works on the 60x60x30 lattice, 1.57x
+ * on 80x80x40, with as good a colouring (548 against 550 colour-order sweeps
+ * to an error of 1e-3 on 60x60x30). */
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
 #define COLOUR_MAX 128
+/* Kempe searches by iterative deepening: the components a search may visit
+ * start at SEARCH_CAP0 vertices and grow by SEARCH_CAP_GROWTH.  A search that
+ * reaches the cap fails whatever the order it visits the component in, so
+ * the outcome still does not depend on the adjacency lists' order. */
+#define SEARCH_CAP0 32
+#define SEARCH_CAP_GROWTH 4
 
 static int has_colour(const uint64_t m[2], int c) { return (int)((m[c >> 6] >> (c & 63)) & 1u); }
 
@@ -127,14 +141,21 @@ int fc3dgpu_colour_reduce(int nc, const int *gptr, const int *adj, int *colour, 
           m[colour[w] >> 6] |= 1ull << (colour[w] & 63);
         }
       }
-      for (int phase = 0; phase < 2 && c < 0; phase++)
-        for (int a = 0; a < top && c < 0; a++)
-          for (int b = 0; b < top && c < 0; b++) {
-            if (a == b || cnt[a] == 0 || cnt[b] == 0) continue;
-            const int pref = has_colour(s1, a) && !has_colour(s0, a) && has_colour(s0, b) && !has_colour(s1, b);
-            if (pref != (phase == 0)) continue;
-            if (kempe_exchange(v, a, b, gptr, adj, colour, seen, ++gen, nbr, ngen, queue, work_cap)) c = a;
-          }
+      /* Every pair first with its search capped at SEARCH_CAP0 vertices,
+       * then with the cap times SEARCH_CAP_GROWTH, up to work_cap: a pair
+       * with short Kempe components goes before the first pair that works. */
+      for (int cap = SEARCH_CAP0; c < 0; cap *= SEARCH_CAP_GROWTH) {
+        const int lim = cap < work_cap ? cap : work_cap;
+        for (int phase = 0; phase < 2 && c < 0; phase++)
+          for (int a = 0; a < top && c < 0; a++)
+            for (int b = 0; b < top && c < 0; b++) {
+              if (a == b || cnt[a] == 0 || cnt[b] == 0) continue;
+              const int pref = has_colour(s1, a) && !has_colour(s0, a) && has_colour(s0, b) && !has_colour(s1, b);
+              if (pref != (phase == 0)) continue;
+              if (kempe_exchange(v, a, b, gptr, adj, colour, seen, ++gen, nbr, ngen, queue, lim)) c = a;
+            }
+        if (lim >= work_cap) break;
+      }
       if (c < 0) {
         left = 1;  /* the class stays: stop at its first contact that cannot move */
         break;
