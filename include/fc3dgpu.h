@@ -50,7 +50,7 @@ extern "C" {
  * classes revisited in reverse order), which shrink the small last colours:
  * on the 60x60x30 lattice 10 colours become 8; FC3DGPU_COLOUR_KEMPE then
  * empties classes by Kempe-chain exchanges (fc3dgpu_colour_reduce, each
- * problem of a batch on its own): 8 become 6, for about 130 ms of host work
+ * problem of a batch on its own): 8 become 6, for about 70 ms of host work
  * per new structure at 320,400 contacts (worth it when a structure is solved
  * more than a few times; leave it out when the contact set changes at every
  * call). */
