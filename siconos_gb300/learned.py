@@ -8,7 +8,7 @@ CUDA kernels; this module holds the host side: parameter initialisation,
 statistics, the training loop, training-set generation with the GPU solver
 on the lattice generator, and the evaluation of what the proposal saves.
 
-Plain NSGS stays the fallback and the judge: the context keeps its current
+Plain NSGS stays the fallback and the arbiter: the context keeps its current
 reaction (zero or the previous step's) whenever the proposal's
 fc3d_compute_error is not smaller.
 """
