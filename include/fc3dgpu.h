@@ -123,6 +123,13 @@ int fc3dgpu_colour(int nc, const int64_t *rowptr, const int64_t *colidx, int kin
  * proper).  Colouring kinds with FC3DGPU_COLOUR_KEMPE apply it after the
  * device colouring. */
 int fc3dgpu_colour_reduce(int nc, const int *gptr, const int *adj, int *colour, int ncol, int work_cap);
+/* The same for a batch: each group (rows group_off[g] .. group_off[g+1]-1,
+ * conflicting only within the group; gptr/adj over all rows) reduced on its
+ * own, exactly as fc3dgpu_colour_reduce reduces it alone, by up to nthreads
+ * host threads.  Returns the largest number of colours over the groups (<0:
+ * out of memory, colour still proper). */
+int fc3dgpu_colour_reduce_groups(int ngroups, const int *group_off, const int *gptr, const int *adj, int *colour,
+                                 int nthreads);
 
 /* Device facts: SM count, L2 bytes, whether kernels can read pageable host
  * memory (and through the host page tables), cooperative launch support,

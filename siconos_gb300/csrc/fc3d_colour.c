@@ -33,6 +33,7 @@
  * time than taking the first pair that works on the 60x60x30 lattice, 1.57x
  * on 80x80x40, with as good a colouring (548 against 550 colour-order sweeps
  * to an error of 1e-3 on 60x60x30). */
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -171,4 +172,79 @@ int fc3dgpu_colour_reduce(int nc, const int *gptr, const int *adj, int *colour, 
   free(cls);
   free(side);
   return ncol;
+}
+
+/* Batches: every group (one problem of a batch: rows group_off[g] ..
+ * group_off[g + 1] - 1, whose conflicts stay inside the group) is reduced on
+ * its own, as fc3dgpu_colour_reduce reduces it alone, by up to nthreads host
+ * threads taking groups in turn; the groups are independent, so the result
+ * does not depend on the threads. */
+typedef struct {
+  int ngroups;
+  const int *group_off, *gptr, *adj;
+  int *colour, *out;
+  int next; /* next group to take (atomic) */
+} reduce_groups_job;
+
+static void *reduce_groups_worker(void *arg) {
+  reduce_groups_job *J = (reduce_groups_job *)arg;
+  int *lg = NULL, *la = NULL;
+  size_t lg_cap = 0, la_cap = 0;
+  for (;;) {
+    const int g = __atomic_fetch_add(&J->next, 1, __ATOMIC_RELAXED);
+    if (g >= J->ngroups) break;
+    const int o0 = J->group_off[g], n = J->group_off[g + 1] - o0;
+    if (n <= 0) {
+      J->out[g] = 0;
+      continue;
+    }
+    const int a0 = J->gptr[o0], na = J->gptr[o0 + n] - a0;
+    if ((size_t)n + 1 > lg_cap || (size_t)(na > 0 ? na : 1) > la_cap) {
+      free(lg);
+      free(la);
+      lg_cap = (size_t)n + 1 > lg_cap ? (size_t)n + 1 : lg_cap;
+      la_cap = (size_t)(na > 0 ? na : 1) > la_cap ? (size_t)(na > 0 ? na : 1) : la_cap;
+      lg = (int *)malloc(sizeof(int) * lg_cap);
+      la = (int *)malloc(sizeof(int) * la_cap);
+      if (!lg || !la) {
+        J->out[g] = -1;
+        lg_cap = la_cap = 0;
+        continue;
+      }
+    }
+    for (int k = 0; k <= n; k++) lg[k] = J->gptr[o0 + k] - a0;
+    for (int k = 0; k < na; k++) la[k] = J->adj[a0 + k] - o0;
+    int ng = 0;
+    for (int k = 0; k < n; k++)
+      if (J->colour[o0 + k] + 1 > ng) ng = J->colour[o0 + k] + 1;
+    const int r = fc3dgpu_colour_reduce(n, lg, la, J->colour + o0, ng, 0);
+    J->out[g] = r > 0 ? r : (r < 0 ? r : ng);
+  }
+  free(lg);
+  free(la);
+  return NULL;
+}
+
+int fc3dgpu_colour_reduce_groups(int ngroups, const int *group_off, const int *gptr, const int *adj, int *colour,
+                                 int nthreads) {
+  if (ngroups <= 0) return 0;
+  int *out = (int *)calloc((size_t)ngroups, sizeof(int));
+  if (!out) return -1;
+  reduce_groups_job J = {ngroups, group_off, gptr, adj, colour, out, 0};
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > ngroups) nthreads = ngroups;
+  if (nthreads > 64) nthreads = 64;
+  pthread_t th[64];
+  int started = 0;
+  for (int t = 1; t < nthreads; t++)
+    if (pthread_create(&th[started], NULL, reduce_groups_worker, &J) == 0) started++;
+  reduce_groups_worker(&J);
+  for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+  int mx = 0, bad = 0;
+  for (int g = 0; g < ngroups; g++) {
+    if (out[g] < 0) bad = 1;
+    if (out[g] > mx) mx = out[g];
+  }
+  free(out);
+  return bad ? -1 : mx;
 }

@@ -1005,21 +1005,12 @@ static int colour_device(fc3dgpu_ctx* c, int nc, long long nnzb, int kind, const
       if (n > 0) ncol = n;
     } else {
       // each problem on its own (its rows only meet its own rows), so it
-      // gets the colouring it would get alone
-      std::vector<int> lg, la;
-      int mx = 0;
-      for (size_t g = 0; g + 1 < c->scene_off_h.size(); g++) {
-        const int o0 = c->scene_off_h[g], n = c->scene_off_h[g + 1] - o0;
-        lg.assign((size_t)n + 1, 0);
-        for (int k = 0; k <= n; k++) lg[k] = gptr[o0 + k] - gptr[o0];
-        la.assign((size_t)std::max(lg[n], 1), 0);
-        for (int k = 0; k < lg[n]; k++) la[k] = adj[gptr[o0] + k] - o0;
-        int ng = 0;
-        for (int k = 0; k < n; k++) ng = std::max(ng, col[o0 + k] + 1);
-        const int r = fc3dgpu_colour_reduce(n, lg.data(), la.data(), col.data() + o0, ng, 0);
-        mx = std::max(mx, r > 0 ? r : ng);
-      }
-      ncol = mx;
+      // gets the colouring it would get alone; the problems on the host's
+      // threads
+      const int ng = (int)c->scene_off_h.size() - 1;
+      const int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), 16u);
+      const int r = fc3dgpu_colour_reduce_groups(ng, c->scene_off_h.data(), gptr.data(), adj.data(), col.data(), nth);
+      if (r > 0) ncol = r;
     }
     CK(cudaMemcpyAsync(c->colour, col.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));

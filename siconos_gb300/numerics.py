@@ -170,6 +170,7 @@ ABI = {
                                      C.POINTER(_SO), C.POINTER(C.c_int)]),
     "fc3dgpu_colour": (C.c_int, [C.c_int, _I64, _I64, C.c_int, _I32]),
     "fc3dgpu_colour_reduce": (C.c_int, [C.c_int, _I32, _I32, _I32, C.c_int, C.c_int]),
+    "fc3dgpu_colour_reduce_groups": (C.c_int, [C.c_int, _I32, _I32, _I32, _I32, C.c_int]),
     "fc3dgpu_last_error": (C.c_char_p, []),
     "fc3dgpu_device_info": (C.c_int, [C.c_int, C.c_void_p]),
     "fc3dgpu_params_default": (None, [C.POINTER(FC3DGPUParams)]),

@@ -78,3 +78,34 @@ def test_search_cap_keeps_the_colouring_proper(built_lib):
     n1, out = reduce(P, col, n0, cap=1)
     assert 6 <= n1 <= n0
     assert O.port().oracle_colour_check(P.nc, P.rowptr, P.colidx, out) == 0
+
+
+@pytest.mark.parametrize("threads", [1, 3, 16])
+def test_batch_groups_reduce_as_alone(built_lib, threads):
+    """fc3dgpu_colour_reduce_groups on a batch of independent lattices (their
+    conflict graphs side by side): each group gets exactly the colouring
+    fc3dgpu_colour_reduce gives it alone, whatever the number of threads, and
+    the return value is the largest number of colours."""
+    import oracle as O
+    import siconos_gb300.numerics as sn
+    from siconos_gb300 import scene
+    dims = [(3, 3, 2), (7, 5, 3), (12, 12, 6), (4, 9, 2), (5, 5, 6), (2, 2, 2), (9, 3, 4)]
+    gp_all, adj_all, col_all, off, alone, counts = [0], [], [], [0], [], []
+    for k, d in enumerate(dims):
+        s = scene.lattice(*d, seed=k + 1)
+        P = O.Problem(s.nc, s.rowptr, s.colidx, s.blocks, s.q, s.mu)
+        n0, col = greedy(P)
+        gptr, adj = conflict_graph(P)
+        gp_all.extend((gptr[1:] + gp_all[-1]).tolist())
+        adj_all.append(adj + off[-1])
+        col_all.append(col)
+        n1, out = reduce(P, col, n0)
+        alone.append(out)
+        counts.append(n1)
+        off.append(off[-1] + P.nc)
+    gp = np.asarray(gp_all, np.int32)
+    adj = np.concatenate(adj_all).astype(np.int32)
+    col = np.concatenate(col_all).astype(np.int32)
+    r = sn.lib().fc3dgpu_colour_reduce_groups(len(dims), np.asarray(off, np.int32), gp, adj, col, threads)
+    assert r == max(counts)
+    np.testing.assert_array_equal(col, np.concatenate(alone))
