@@ -529,10 +529,14 @@ extern "C" int fc2dgpu_percolour_use_kernel_file(fc2dgpu_percolour* h, const cha
     fc3dgpu_set_error("fc2dgpu_percolour_use_kernel_file: no reference local-solve kernel in %s", path);
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
-  if (h->lib) cudaLibraryUnload(h->lib);
+  // the new sweep graph first: the old one (destroyed by capture) may
+  // launch the old library's kernel
+  cudaLibrary_t old = h->lib;
   h->lib = lib;
   h->kref = k;
-  return capture(h);
+  const int rc = capture(h);
+  if (old) cudaLibraryUnload(old);
+  return rc;
 }
 
 extern "C" int fc2dgpu_percolour_get_r_u(fc2dgpu_percolour* h, double* r, double* u) {
