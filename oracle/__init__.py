@@ -70,6 +70,11 @@ def port():
         lib.oracle_fc3d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
                                          C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
                                          C.POINTER(C.c_int)]
+        lib.oracle_fc3d_nsgs_opts.restype = C.c_int
+        lib.oracle_fc3d_nsgs_opts.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double,
+                                              C.c_int, C.c_void_p, _I32, C.c_double, C.POINTER(C.c_int),
+                                              C.POINTER(C.c_double), C.c_void_p, C.c_int, C.POINTER(C.c_int),
+                                              C.POINTER(C.c_int)]
         lib.oracle_fc2d_nsgs.restype = C.c_int
         lib.oracle_fc2d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
                                          C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
@@ -157,6 +162,10 @@ def ref():
         lib.ref_fc3d_nsgs.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
                                       C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p, C.c_int,
                                       C.POINTER(C.c_int)]
+        lib.ref_fc3d_nsgs_opts.restype = C.c_int
+        lib.ref_fc3d_nsgs_opts.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
+                                           _I32, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p,
+                                           C.c_int, C.POINTER(C.c_int)]
         lib.ref_fc3d_compute_error.restype = C.c_double
         lib.ref_fc3d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64]
         lib.ref_dat_open.restype = C.c_void_p
@@ -247,15 +256,55 @@ def _solve(fn, P: Problem, r0, tol, maxiter, order, trace_cap, is_port):
     return Result(info, it.value, err.value, r, u, tr[: min(tl.value, trace_cap)].copy())
 
 
-def nsgs_port(P: Problem, r0=None, tol=1e-8, maxiter=10000, order=None, trace_cap=0) -> Result:
-    return _solve(port().oracle_fc3d_nsgs, P, r0, tol, maxiter, order, trace_cap, True)
+# NSGS options beyond the defaults (fc3d_nsgs.c:711-900): error evaluation
+# (0 FULL, 1 LIGHT, 2 LIGHT_WITH_FULL_FINAL, 3 ADAPTIVE), the full-error
+# frequency of FULL, the local tolerance strategy (0 ADAPTIVE, 1 GIVEN_VALUE,
+# 2 ADAPTIVE_N_CONTACT) and its ratio.
+DEFAULT_NSGS_OPTIONS = {"err_mode": 2, "freq": 0, "strategy": 1, "ratio": 10.0}
 
 
-def nsgs_ref(P: Problem, r0=None, tol=1e-8, maxiter=10000, trace_cap=0) -> Result:
+def _opts4(options):
+    o = dict(DEFAULT_NSGS_OPTIONS, **(options or {}))
+    return np.array([o["err_mode"], o["freq"], o["strategy"], 0], np.int32), float(o["ratio"])
+
+
+def nsgs_port(P: Problem, r0=None, tol=1e-8, maxiter=10000, order=None, trace_cap=0, options=None,
+              u0=None) -> Result:
+    """The restatement of fc3d_nsgs.  With `options` (keys of
+    DEFAULT_NSGS_OPTIONS) the general loop with those options; `u0` is the
+    velocity on entry, which the LIGHT and ADAPTIVE evaluations leave as it
+    is (the result's `u_written` tells)."""
+    if options is None:
+        return _solve(port().oracle_fc3d_nsgs, P, r0, tol, maxiter, order, trace_cap, True)
+    return _solve_opts(port().oracle_fc3d_nsgs_opts, P, r0, tol, maxiter, order, trace_cap, options, u0, True)
+
+
+def nsgs_ref(P: Problem, r0=None, tol=1e-8, maxiter=10000, trace_cap=0, options=None, u0=None) -> Result:
     lib = ref()
     if lib is None:
         raise RuntimeError("oracle/_ref is not built")
-    return _solve(lib.ref_fc3d_nsgs, P, r0, tol, maxiter, None, trace_cap, False)
+    if options is None:
+        return _solve(lib.ref_fc3d_nsgs, P, r0, tol, maxiter, None, trace_cap, False)
+    return _solve_opts(lib.ref_fc3d_nsgs_opts, P, r0, tol, maxiter, None, trace_cap, options, u0, False)
+
+
+def _solve_opts(fn, P: Problem, r0, tol, maxiter, order, trace_cap, options, u0, is_port):
+    r = np.zeros(3 * P.nc) if r0 is None else np.ascontiguousarray(r0, dtype=np.float64).copy()
+    u = np.zeros(3 * P.nc) if u0 is None else np.ascontiguousarray(u0, dtype=np.float64).copy()
+    it, err, tl, uw = C.c_int(), C.c_double(), C.c_int(), C.c_int()
+    tr = np.zeros(max(trace_cap, 1))
+    blocks = np.ascontiguousarray(P.blocks, dtype=np.float64).reshape(-1)
+    o4, ratio = _opts4(options)
+    args = [P.nc, P.rowptr, P.colidx, blocks, P.q, P.mu, r, u, tol, maxiter]
+    if is_port:
+        args.append(None if order is None else np.ascontiguousarray(order, np.int32).ctypes.data)
+    args += [o4, ratio, C.byref(it), C.byref(err), tr.ctypes.data if trace_cap else None, trace_cap, C.byref(tl)]
+    if is_port:
+        args.append(C.byref(uw))
+    info = fn(*args)
+    res = Result(info, it.value, err.value, r, u, tr[: min(tl.value, trace_cap)].copy())
+    res.u_written = bool(uw.value) if is_port else None
+    return res
 
 
 def compute_error_port(P: Problem, r) -> tuple[float, np.ndarray]:

@@ -6,9 +6,14 @@
  * SICONOS_FRICTION_3D_NSGS solve on a 3x3 block-sparse W:
  *
  *   fc3d_driver trivial case        fc3d_driver.c:51-71
- *   NSGS outer loop, default branch fc3d_nsgs.c:711-900 (LIGHT_WITH_FULL_FINAL,
- *                                   GIVEN_VALUE local tolerance, no shuffle,
- *                                   freezing, relaxation or filter)
+ *   NSGS outer loop, general branch fc3d_nsgs.c:711-900 (error evaluation
+ *                                   FULL with its frequency, LIGHT,
+ *                                   LIGHT_WITH_FULL_FINAL or ADAPTIVE; local
+ *                                   tolerance GIVEN_VALUE, ADAPTIVE or
+ *                                   ADAPTIVE_N_CONTACT,
+ *                                   fc3d_set_internalsolver_tolerance.c:31-63;
+ *                                   no shuffle, freezing, relaxation or
+ *                                   filter)
  *   light error                     fc3d_nsgs.c:80-96
  *   tolerance manager               tolerance_manager.h:63-241
  *   local q                         fc3d_local_problem_tools.c:48-63,
@@ -440,15 +445,33 @@ typedef struct {
   double user_tol, working_tol, min_tol, local_tol;
 } TolMgr;
 
+/* The NSGS options beyond the defaults that the loop below follows
+ * (fc3d_nsgs.c:711-900, the general branch): the error evaluation
+ * (SICONOS_NSGS_ERROR_EVALUATION_FULL 0, LIGHT 1, LIGHT_WITH_FULL_FINAL 2,
+ * ADAPTIVE 3, NonSmoothGaussSeidel_options.h:125-143), the full-error
+ * frequency of FULL (calculateFullErrorAdaptiveInterval, fc3d_nsgs.c:392-412),
+ * and the local tolerance strategy applied at the start of each iteration
+ * (fc3d_set_internalsolver_tolerance.c:31-63: ADAPTIVE 0, GIVEN_VALUE 1,
+ * ADAPTIVE_N_CONTACT 2) with its ratio (dparam INTERNAL_ERROR_RATIO). */
+typedef struct {
+  int err_mode, freq, strategy;
+  double ratio;
+} NsgsOpts;
+
 /* Returns info: 0 converged, 1 not converged, -20 max iterations (and the
- * driver's trivial-case 0).  r is the warm start on entry. */
-int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
+ * driver's trivial-case 0).  r is the warm start on entry.  *u_written
+ * (optional) tells whether u was written: the reference computes u only
+ * with the full error, so the LIGHT and ADAPTIVE evaluations leave it as
+ * given, FULL with a frequency leaves the u of the last evaluated iterate. */
+static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
                      const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *order,
-                     int *iters, double *err, double *trace, int trace_cap, int *trace_len) {
+                     const NsgsOpts *op, int *iters, double *err, double *trace, int trace_cap, int *trace_len,
+                     int *u_written) {
   int n = 3 * nc;
   if (iters) *iters = 0;
   if (err) *err = 0.0;
   if (trace_len) *trace_len = 0;
+  if (u_written) *u_written = 0;
   /* driver trivial case */
   int trivial = 1;
   for (int i = 0; i < nc; i++)
@@ -459,6 +482,7 @@ int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const
   if (trivial) {
     memcpy(u, q, sizeof(double) * (size_t)n);
     memset(r, 0, sizeof(double) * (size_t)n);
+    if (u_written) *u_written = 1;
     return 0;
   }
   double norm_q = nrm2(n, q);
@@ -489,6 +513,12 @@ int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const
   while (iter < maxiter && hasNotConverged > 0) {
     ++iter;
     double light = 0.0;
+    /* fc3d_set_internalsolver_tolerance: the local solver's tolerance from
+     * the previous iteration's error */
+    if (op->strategy == 0)
+      tm.local_tol = fmax(incr_error / op->ratio, tol / nc);
+    else if (op->strategy == 2)
+      tm.local_tol = incr_error / (op->ratio * nc);
     for (int ii = 0; ii < nc; ii++) {
       int c = order ? order[ii] : ii;
       L.M = &blocks[9 * diag[c]];
@@ -509,39 +539,61 @@ int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const
       r[3 * c + 1] = lr[1];
       r[3 * c + 2] = lr[2];
     }
-    /* light error */
-    incr_error = sqrt(light);
-    double nr = nrm2(n, r);
-    if (fabs(nr) > DBL_EPSILON) incr_error /= nr;
-    /* check_convergence_with_adaptation */
-    if (incr_error >= tolerance) {
-      hasNotConverged = 1;
-    } else {
-      full_error = oracle_fc3d_compute_error(nc, rowptr, colidx, blocks, q, mu, r, u, norm_q);
-      if (full_error <= tm.user_tol) {
-        hasNotConverged = 0;
-      } else if (incr_error < 1e-15 || incr_error < DBL_EPSILON * 100.0) {
-        double nt = fmax(tm.local_tol / 100.0, tm.min_tol);
-        tm.local_tol = nt;
+    if (op->err_mode == 1) {
+      /* LIGHT: the light error against the working tolerance */
+      incr_error = sqrt(light);
+      double nr = nrm2(n, r);
+      if (fabs(nr) > DBL_EPSILON) incr_error /= nr;
+      hasNotConverged = incr_error < tolerance ? 0 : 1;
+    } else if (op->err_mode == 2) {
+      /* LIGHT_WITH_FULL_FINAL: light error, then check_convergence_with_adaptation */
+      incr_error = sqrt(light);
+      double nr = nrm2(n, r);
+      if (fabs(nr) > DBL_EPSILON) incr_error /= nr;
+      if (incr_error >= tolerance) {
         hasNotConverged = 1;
       } else {
-        if (full_error > 0.0 && incr_error > 0.0) {
-          double ratio = incr_error / full_error;
-          double nt = ratio * tm.user_tol;
-          double user_min = tm.user_tol * 1e-6;
-          double mint = user_min > tm.min_tol ? user_min : tm.min_tol;
-          if (nt < mint) nt = mint;
-          if (nt > 0.0 && nt < tolerance) tolerance = nt;
+        full_error = oracle_fc3d_compute_error(nc, rowptr, colidx, blocks, q, mu, r, u, norm_q);
+        if (u_written) *u_written = 1;
+        if (full_error <= tm.user_tol) {
+          hasNotConverged = 0;
+        } else if (incr_error < 1e-15 || incr_error < DBL_EPSILON * 100.0) {
+          double nt = fmax(tm.local_tol / 100.0, tm.min_tol);
+          tm.local_tol = nt;
+          hasNotConverged = 1;
+        } else {
+          if (full_error > 0.0 && incr_error > 0.0) {
+            double ratio = incr_error / full_error;
+            double nt = ratio * tm.user_tol;
+            double user_min = tm.user_tol * 1e-6;
+            double mint = user_min > tm.min_tol ? user_min : tm.min_tol;
+            if (nt < mint) nt = mint;
+            if (nt > 0.0 && nt < tolerance) tolerance = nt;
+          }
+          hasNotConverged = 1;
         }
-        hasNotConverged = 1;
+        if (!(tolerance > 0.0)) break;
       }
-      if (!(tolerance > 0.0)) break;
+    } else if (op->err_mode == 0) {
+      /* FULL: the full error every iteration, or every freq iterations
+       * (1e24 between evaluations) */
+      full_error = 1e24;
+      if (op->freq <= 0 || iter % op->freq == 0) {
+        full_error = oracle_fc3d_compute_error(nc, rowptr, colidx, blocks, q, mu, r, u, norm_q);
+        if (u_written) *u_written = 1;
+      }
+      incr_error = full_error;
+      hasNotConverged = full_error < tolerance ? 0 : 1;
     }
+    /* ADAPTIVE (3): the loop has no branch for it; it runs to the budget */
     if (trace && tlen < trace_cap) trace[tlen] = incr_error;
     tlen++;
   }
-  full_error = oracle_fc3d_compute_error(nc, rowptr, colidx, blocks, q, mu, r, u, norm_q);
-  hasNotConverged = full_error < tol ? 0 : 1;
+  if (op->err_mode == 2) {
+    full_error = oracle_fc3d_compute_error(nc, rowptr, colidx, blocks, q, mu, r, u, norm_q);
+    if (u_written) *u_written = 1;
+    hasNotConverged = full_error < tol ? 0 : 1;
+  }
   int info = hasNotConverged;
   if (iter == maxiter && hasNotConverged > 0) info = -20;
   if (iters) *iters = iter;
@@ -551,6 +603,26 @@ int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const
   free(rho);
   free(rho_pli);
   return info;
+}
+
+/* The reference's default options: LIGHT_WITH_FULL_FINAL, GIVEN_VALUE. */
+int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
+                     const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *order,
+                     int *iters, double *err, double *trace, int trace_cap, int *trace_len) {
+  const NsgsOpts op = {2, 0, 1, 10.0};
+  return nsgs_impl(nc, rowptr, colidx, blocks, q, mu, r, u, tol, maxiter, order, &op, iters, err, trace, trace_cap,
+                   trace_len, NULL);
+}
+
+/* Any error evaluation (0-3), frequency and local tolerance strategy (0-2);
+ * opts4 = {err_mode, freq, strategy, 0}, ratio the INTERNAL_ERROR_RATIO. */
+int oracle_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
+                          const double *q, const double *mu, double *r, double *u, double tol, int maxiter,
+                          const int32_t *order, const int32_t *opts4, double ratio, int *iters, double *err,
+                          double *trace, int trace_cap, int *trace_len, int *u_written) {
+  const NsgsOpts op = {opts4[0], opts4[1], opts4[2], ratio};
+  return nsgs_impl(nc, rowptr, colidx, blocks, q, mu, r, u, tol, maxiter, order, &op, iters, err, trace, trace_cap,
+                   trace_len, u_written);
 }
 
 /* One contact's local solve from the reference's default local options, for

@@ -128,6 +128,40 @@ int ref_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const do
   return info;
 }
 
+/* ref_fc3d_nsgs with NSGS options beyond the defaults: opts4 = {error
+ * evaluation (iparam 13), its frequency (iparam 14), local tolerance
+ * strategy (iparam 2), 0}, ratio the INTERNAL_ERROR_RATIO (dparam 11). */
+int ref_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
+                       const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *opts4,
+                       double ratio, int *iters, double *err, double *trace, int trace_cap, int *trace_len) {
+  NumericsMatrix *M = make_sbm(nc, rowptr, colidx, blocks);
+  FrictionContactProblem P;
+  memset(&P, 0, sizeof(P));
+  P.dimension = 3;
+  P.numberOfContacts = nc;
+  P.M = M;
+  P.q = (double *)q;
+  P.mu = (double *)mu;
+  SolverOptions *opt = solver_options_create(SICONOS_FRICTION_3D_NSGS);
+  opt->iparam[SICONOS_IPARAM_MAX_ITER] = maxiter;
+  opt->dparam[SICONOS_DPARAM_TOL] = tol;
+  opt->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = opts4[0];
+  opt->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY] = opts4[1];
+  opt->iparam[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = opts4[2];
+  opt->dparam[SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO] = ratio;
+  Trace t = {trace, trace_cap, 0};
+  Callback cb = {&t, trace_cb};
+  if (trace) opt->callback = &cb;
+  int info = fc3d_driver(&P, r, u, opt);
+  if (iters) *iters = opt->iparam[SICONOS_IPARAM_ITER_DONE];
+  if (err) *err = opt->dparam[SICONOS_DPARAM_RESIDU];
+  if (trace_len) *trace_len = t.len;
+  opt->callback = NULL;
+  solver_options_delete(opt);
+  free_sbm(M);
+  return info;
+}
+
 /* The reference's 2D NSGS (fc2d_driver with SICONOS_FRICTION_2D_NSGS and its
  * defaults, tolerance and iteration budget set) on a block-CSR W of 2x2
  * blocks. */
