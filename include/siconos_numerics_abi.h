@@ -167,7 +167,10 @@ typedef struct SolverOptions {
 #define SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT 1
 #define SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL 2
 #define SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_ADAPTIVE 3
+/* local tolerance strategies (NonSmoothGaussSeidel_options.h:222-228) */
+#define SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE 0
 #define SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_GIVEN_VALUE 1
+#define SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE_N_CONTACT 2
 
 /* one-contact local solver indices (FrictionContact_options.h:294-365) */
 #define SICONOS_FRICTION_3D_NSN_RHO_STRATEGY 9

@@ -315,17 +315,19 @@ static int check_options(const SolverOptions *o) {
     return NUMERICS_ERR_INVALID_OPTION;
   }
   const int *ip = o->iparam;
-  if (ip[SICONOS_FRICTION_3D_NSGS_SHUFFLE] != 0 || ip[SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] > 0 ||
-      ip[SICONOS_FRICTION_3D_NSGS_RELAXATION] != 0 || ip[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] != 0) {
+  /* value checks as fc3d_nsgs.c:630-665 makes them */
+  const int shuffle = ip[SICONOS_FRICTION_3D_NSGS_SHUFFLE], em = ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION];
+  if (shuffle < 0 || shuffle > 2) {
+    fc3dgpu_set_error("iparam[SICONOS_FRICTION_3D_NSGS_SHUFFLE] must be 0, 1 or 2");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (em < SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL || em > SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_ADAPTIVE) {
+    fc3dgpu_set_error("iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] must be 0, 1, 2 or 3");
+    return NUMERICS_ERR_INVALID_ARGUMENT;
+  }
+  if (shuffle != 0 || ip[SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] > 0 || ip[SICONOS_FRICTION_3D_NSGS_RELAXATION] != 0 ||
+      ip[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] != 0) {
     fc3dgpu_set_error("GPU NSGS sweeps in colour order: shuffle, freezing, relaxation and filter are not supported");
-    return NUMERICS_ERR_NOT_IMPLEMENTED;
-  }
-  if (ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] != SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL) {
-    fc3dgpu_set_error("GPU NSGS supports ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL only");
-    return NUMERICS_ERR_NOT_IMPLEMENTED;
-  }
-  if (ip[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] != SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_GIVEN_VALUE) {
-    fc3dgpu_set_error("GPU NSGS supports INTERNAL_ERROR_STRATEGY_GIVEN_VALUE only");
     return NUMERICS_ERR_NOT_IMPLEMENTED;
   }
   if (o->numberOfInternalSolvers < 1 || !o->internalSolvers || !o->internalSolvers[0]) {
@@ -416,6 +418,130 @@ static void *norm_job(void *p) {
   return NULL;
 }
 
+/* The options whose loop runs on the host (fc3d_nsgs.c:711-900, the
+ * general branch): an error evaluation other than LIGHT_WITH_FULL_FINAL, or
+ * a local tolerance set from the error at each iteration
+ * (fc3d_set_internalsolver_tolerance.c:31-63). */
+static int host_loop_options(const SolverOptions *o) {
+  const int em = o->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION];
+  const int st = o->iparam[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY];
+  return em != SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL ||
+         st == SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE ||
+         st == SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE_N_CONTACT;
+}
+
+/* That loop: one FP64 sweep in colour order a device call
+ * (fc3dgpu_ctx_solve with a budget of one sweep and a zero tolerance, which
+ * reports the sweep's light error and the full error of its iterate, u on
+ * the device), the decisions on the host as the reference takes them:
+ *   local tolerance at the start of each iteration: ADAPTIVE
+ *     max(error / ratio, tol / nc), ADAPTIVE_N_CONTACT error / (ratio nc),
+ *     from the previous iteration's error (infinite before the first);
+ *   FULL: the full error every iteration, or every `freq` iterations
+ *     (1e24 between evaluations, fc3d_nsgs.c:392-412), against the tolerance;
+ *   LIGHT: the light error against the tolerance, no full error, u as given;
+ *   LIGHT_WITH_FULL_FINAL: the tolerance manager (tolerance_manager.h) and
+ *     the final full error, as the device loop of the default options;
+ *   ADAPTIVE: the reference's loop has no branch for it: the budget runs
+ *     out, info -20, residual infinite, u as given.
+ * The per-iteration error is kept for the callback, replayed after the loop
+ * as for the device loop.  Returns info; the outputs as the reference's. */
+static int nsgs_host_loop(fc3dgpu_ctx *ctx, FrictionContactProblem *P, double *reaction, double *velocity,
+                          SolverOptions *o, const fc3dgpu_params *p0, double *trace, int trace_cap, int *tlen,
+                          int *iters, double *residual, double *incr_out, double *ms) {
+  const int nc = P->numberOfContacts;
+  const int *ip = o->iparam;
+  const int em = ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION];
+  const int freq = ip[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY];
+  const int strategy = ip[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY];
+  const double ratio = o->dparam[SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO];
+  const double user_tol = p0->tol, min_tol = DBL_EPSILON * 1e-6;
+  fc3dgpu_params p = *p0;
+  p.max_iter = 1;
+  p.tol = 0.0;
+  p.precision = (p0->precision == 2 || p0->precision == 3) ? 3 : 1;
+  double tolerance = user_tol, local_tol = p0->local_tol;
+  double incr = INFINITY, full = INFINITY, last_full = INFINITY;
+  int not_conv = 1, iter = 0, nt_trace = 0;
+  double *scratch = (double *)malloc(sizeof(double) * 3 * (size_t)nc);
+  if (!scratch) {
+    fc3dgpu_set_error("host allocation failed");
+    return NUMERICS_ERR_MEMORY;
+  }
+  *ms = 0.0;
+  while (iter < p0->max_iter && not_conv > 0) {
+    ++iter;
+    if (strategy == SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE)
+      local_tol = fmax(incr / ratio, user_tol / nc);
+    else if (strategy == SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE_N_CONTACT)
+      local_tol = incr / (ratio * nc);
+    p.local_tol = local_tol;
+    fc3dgpu_stats st;
+    int rc = fc3dgpu_ctx_solve(ctx, &p, &st);
+    if (rc) {
+      free(scratch);
+      return rc;
+    }
+    *ms += st.ms_total;
+    last_full = st.error;
+    if (em == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT) {
+      incr = st.incr_error;
+      not_conv = incr < tolerance ? 0 : 1;
+    } else if (em == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL) {
+      incr = st.incr_error;
+      if (incr < tolerance) {
+        full = st.error;
+        if (full <= user_tol) {
+          not_conv = 0;
+        } else if (incr < 1e-15 || incr < DBL_EPSILON * 100.0) {
+          local_tol = fmax(local_tol / 100.0, min_tol);
+        } else if (full > 0.0 && incr > 0.0) {
+          double nt = incr / full * user_tol;
+          const double umin = user_tol * 1e-6, mint = umin > min_tol ? umin : min_tol;
+          if (nt < mint) nt = mint;
+          if (nt > 0.0 && nt < tolerance) tolerance = nt;
+        }
+        if (!(tolerance > 0.0)) break; /* before the iteration's callback, as fc3d_nsgs.c:841-846 */
+      }
+    } else if (em == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL) {
+      full = 1e24;
+      if (freq <= 0 || iter % freq == 0) {
+        full = st.error;
+        /* u of this iterate, as the reference's fc3d_compute_error leaves it */
+        rc = fc3dgpu_ctx_get_r_u(ctx, scratch, velocity);
+        if (rc) {
+          free(scratch);
+          return rc;
+        }
+      }
+      incr = full;
+      not_conv = full < tolerance ? 0 : 1;
+    }
+    if (trace && nt_trace < trace_cap) trace[nt_trace] = incr;
+    nt_trace++;
+  }
+  int rc = 0;
+  if (em == SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL) {
+    /* the final full error: the last call's (that of the final iterate,
+     * u left on the device), or one evaluation when no sweep ran */
+    full = last_full;
+    if (iter == 0) rc = fc3dgpu_ctx_compute_error(ctx, &full);
+    if (!rc) rc = fc3dgpu_ctx_get_r_u(ctx, reaction, velocity);
+    not_conv = full < user_tol ? 0 : 1;
+  } else {
+    rc = fc3dgpu_ctx_get_r_u(ctx, reaction, scratch);
+  }
+  free(scratch);
+  if (rc) return rc;
+  *iters = iter;
+  *tlen = nt_trace;
+  *residual = full;
+  *incr_out = incr;
+  int info = not_conv;
+  if (iter == p0->max_iter && not_conv > 0) info = NUMERICS_ERR_MAX_ITER;
+  return info;
+}
+
 int fc3dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velocity, SolverOptions *options) {
   int rc = check_problem(problem, reaction, velocity);
   if (rc) return rc;
@@ -435,6 +561,39 @@ int fc3dgpu_nsgs(FrictionContactProblem *problem, double *reaction, double *velo
   if (rc) return rc;
   fc3dgpu_params p;
   params_from_options(options, &p);
+  if (host_loop_options(options)) {
+    const double t1 = now_s();
+    const int cap = p.max_iter > 0 ? p.max_iter : 1;
+    double *tr = (double *)malloc(sizeof(double) * (size_t)cap);
+    int iters = 0, tlen = 0;
+    double residual = INFINITY, incr = INFINITY, ms = 0.0;
+    const int info = nsgs_host_loop(ctx, problem, reaction, velocity, options, &p, tr, cap, &tlen, &iters,
+                                    &residual, &incr, &ms);
+    const double t2 = now_s();
+    if (info < 0 && info != NUMERICS_ERR_MAX_ITER) {
+      free(tr);
+      return info;
+    }
+    int *ip = options->iparam;
+    double *dp = options->dparam;
+    ip[SICONOS_IPARAM_ITER_DONE] = iters;
+    dp[SICONOS_DPARAM_RESIDU] = residual;
+    ip[FC3DGPU_IPARAM_SWEEPS_FP32] = 0;
+    ip[FC3DGPU_IPARAM_SWEEPS_FP64] = iters;
+    dp[SICONOS_DPARAM_TIME_BEFORE_LOOP] = t1 - t0;
+    dp[SICONOS_DPARAM_TIME_IN_LOOP] = t2 - t1;
+    dp[SICONOS_DPARAM_TIME_AFTER_LOOP] = 0.0;
+    dp[FC3DGPU_DPARAM_MS_SWEEP32] = 0.0;
+    dp[FC3DGPU_DPARAM_MS_SWEEP64] = iters ? ms / iters : 0.0;
+    dp[FC3DGPU_DPARAM_MS_SOLVE] = ms;
+    dp[FC3DGPU_DPARAM_INCR_ERROR] = incr;
+    if (tr && options->callback && options->callback->collectStatsIteration)
+      for (int k = 0; k < tlen && k < cap; k++)
+        options->callback->collectStatsIteration(options->callback->env, (size_t)(3 * problem->numberOfContacts),
+                                                 reaction, velocity, tr[k], NULL);
+    free(tr);
+    return info;
+  }
   fc3dgpu_stats st;
   const double t1 = now_s();
   rc = fc3dgpu_ctx_solve(ctx, &p, &st);

@@ -48,6 +48,12 @@ SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT = 15
 SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_FULL = 0
 SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT = 1
 SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_LIGHT_WITH_FULL_FINAL = 2
+SICONOS_FRICTION_3D_NSGS_ERROR_EVALUATION_ADAPTIVE = 3
+SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY = 2
+SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE = 0
+SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_GIVEN_VALUE = 1
+SICONOS_FRICTION_3D_INTERNAL_ERROR_STRATEGY_ADAPTIVE_N_CONTACT = 2
+SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO = 11
 SICONOS_DPARAM_RESIDU = 1
 FC3DGPU_IPARAM_PRECISION = 23
 FC3DGPU_IPARAM_LANES = 24

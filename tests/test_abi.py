@@ -107,6 +107,33 @@ def test_invalid_inputs_rejected(built_lib):
     o.iparam[11] = 1  # shuffle
     assert sn.fc3d_driver(P, r, u, o) == sn.NUMERICS_ERR_NOT_IMPLEMENTED
     assert "shuffle" in sn.last_error()
+    # values the reference refuses (fc3d_nsgs.c:630-665): invalid argument
+    o.iparam[11] = 5
+    assert sn.fc3d_driver(P, r, u, o) == sn.NUMERICS_ERR_INVALID_ARGUMENT
+    o.iparam[11] = 0
+    o.iparam[sn.SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = 7
+    assert sn.fc3d_driver(P, r, u, o) == sn.NUMERICS_ERR_INVALID_ARGUMENT
+    assert "ERROR_EVALUATION" in sn.last_error()
+
+
+@pytest.mark.parametrize("em,strategy", [(0, 1), (1, 1), (3, 1), (2, 0), (2, 2)])
+def test_other_nsgs_options_pass_the_checks(built_lib, em, strategy):
+    """The reference's other error evaluations and local tolerance
+    strategies are accepted (they run as a host loop of single sweeps); on a
+    machine without a GPU the solve then stops at the device, not at the
+    option checks."""
+    import siconos_gb300.numerics as sn
+    ctx = sn.lib().fc3dgpu_ctx_create(0)
+    if ctx:
+        sn.lib().fc3dgpu_ctx_destroy(ctx)
+        pytest.skip("a GPU is present")
+    o = sn.SolverOptions()
+    o.iparam[sn.SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = em
+    o.iparam[sn.SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = strategy
+    P = _tiny_problem([-1.0, 0.0, 0.0])
+    r, u = np.zeros(3), np.zeros(3)
+    assert sn.fc3d_driver(P, r, u, o) == sn.NUMERICS_ERR_NOT_IMPLEMENTED
+    assert "only" not in sn.last_error() and "not supported" not in sn.last_error()
 
 
 def test_solve_fails_loudly_without_gpu(built_lib):
