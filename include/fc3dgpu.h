@@ -87,7 +87,11 @@ int fc3dgpu_driver(FrictionContactProblem *problem, double *reaction, double *ve
  * (onecontact.c:1037-1056: 100 Newton iterations, tol 1e-14, GP line search
  * of 10, NSN_AND_PLI_NSN_LOOP, one loop, 100 PLI iterations) -- plus the GPU
  * knobs above.  Internal solver options are allocated with calloc, like
- * solver_options_create, when options has none. */
+ * solver_options_create, when options has none.  fc3dgpu_nsgs also honours
+ * the other error evaluations (FULL with its frequency, LIGHT, ADAPTIVE) and
+ * the ADAPTIVE / ADAPTIVE_N_CONTACT local tolerances as fc3d_nsgs.c:711-900
+ * does, with FP64 sweeps, one device call a sweep; shuffle, freezing,
+ * relaxation and filter give NUMERICS_ERR_NOT_IMPLEMENTED. */
 void fc3dgpu_nsgs_set_default(SolverOptions *options);
 
 /* Stand-alone options (what solver_options_create(SICONOS_FRICTION_3D_NSGS_GPU)
