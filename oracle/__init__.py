@@ -72,7 +72,7 @@ def port():
                                          C.POINTER(C.c_int)]
         lib.oracle_fc3d_nsgs_opts.restype = C.c_int
         lib.oracle_fc3d_nsgs_opts.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double,
-                                              C.c_int, C.c_void_p, _I32, C.c_double, C.POINTER(C.c_int),
+                                              C.c_int, C.c_void_p, _I32, _F64, C.POINTER(C.c_int),
                                               C.POINTER(C.c_double), C.c_void_p, C.c_int, C.POINTER(C.c_int),
                                               C.POINTER(C.c_int)]
         lib.oracle_fc2d_nsgs.restype = C.c_int
@@ -164,7 +164,7 @@ def ref():
                                       C.POINTER(C.c_int)]
         lib.ref_fc3d_nsgs_opts.restype = C.c_int
         lib.ref_fc3d_nsgs_opts.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64, C.c_double, C.c_int,
-                                           _I32, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p,
+                                           _I32, _F64, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_void_p,
                                            C.c_int, C.POINTER(C.c_int)]
         lib.ref_fc3d_compute_error.restype = C.c_double
         lib.ref_fc3d_compute_error.argtypes = [C.c_int, _I64, _I64, _F64, _F64, _F64, _F64, _F64]
@@ -259,13 +259,16 @@ def _solve(fn, P: Problem, r0, tol, maxiter, order, trace_cap, is_port):
 # NSGS options beyond the defaults (fc3d_nsgs.c:711-900): error evaluation
 # (0 FULL, 1 LIGHT, 2 LIGHT_WITH_FULL_FINAL, 3 ADAPTIVE), the full-error
 # frequency of FULL, the local tolerance strategy (0 ADAPTIVE, 1 GIVEN_VALUE,
-# 2 ADAPTIVE_N_CONTACT) and its ratio.
-DEFAULT_NSGS_OPTIONS = {"err_mode": 2, "freq": 0, "strategy": 1, "ratio": 10.0}
+# 2 ADAPTIVE_N_CONTACT) and its ratio, relaxation (1 = on) with omega, and
+# the filter of local solutions (1 = on).
+DEFAULT_NSGS_OPTIONS = {"err_mode": 2, "freq": 0, "strategy": 1, "ratio": 10.0, "relax": 0, "omega": 1.0,
+                        "filter": 0}
 
 
-def _opts4(options):
+def _opts6(options):
     o = dict(DEFAULT_NSGS_OPTIONS, **(options or {}))
-    return np.array([o["err_mode"], o["freq"], o["strategy"], 0], np.int32), float(o["ratio"])
+    return (np.array([o["err_mode"], o["freq"], o["strategy"], o["relax"], o["filter"], 0], np.int32),
+            np.array([o["ratio"], o["omega"]], np.float64))
 
 
 def nsgs_port(P: Problem, r0=None, tol=1e-8, maxiter=10000, order=None, trace_cap=0, options=None,
@@ -294,11 +297,11 @@ def _solve_opts(fn, P: Problem, r0, tol, maxiter, order, trace_cap, options, u0,
     it, err, tl, uw = C.c_int(), C.c_double(), C.c_int(), C.c_int()
     tr = np.zeros(max(trace_cap, 1))
     blocks = np.ascontiguousarray(P.blocks, dtype=np.float64).reshape(-1)
-    o4, ratio = _opts4(options)
+    o6, d2 = _opts6(options)
     args = [P.nc, P.rowptr, P.colidx, blocks, P.q, P.mu, r, u, tol, maxiter]
     if is_port:
         args.append(None if order is None else np.ascontiguousarray(order, np.int32).ctypes.data)
-    args += [o4, ratio, C.byref(it), C.byref(err), tr.ctypes.data if trace_cap else None, trace_cap, C.byref(tl)]
+    args += [o6, d2, C.byref(it), C.byref(err), tr.ctypes.data if trace_cap else None, trace_cap, C.byref(tl)]
     if is_port:
         args.append(C.byref(uw))
     info = fn(*args)

@@ -452,10 +452,16 @@ typedef struct {
  * frequency of FULL (calculateFullErrorAdaptiveInterval, fc3d_nsgs.c:392-412),
  * and the local tolerance strategy applied at the start of each iteration
  * (fc3d_set_internalsolver_tolerance.c:31-63: ADAPTIVE 0, GIVEN_VALUE 1,
- * ADAPTIVE_N_CONTACT 2) with its ratio (dparam INTERNAL_ERROR_RATIO). */
+ * ADAPTIVE_N_CONTACT 2) with its ratio (dparam INTERNAL_ERROR_RATIO); and
+ * per contact the relaxation of the new reaction (performRelaxation_3,
+ * fc3d_nsgs.c:73-78, before its light-error term) and the filter that keeps
+ * the old reaction when the local solver's residual is not finite or above
+ * 1 (acceptLocalReactionFiltered, fc3d_nsgs.c:338-389). */
 typedef struct {
   int err_mode, freq, strategy;
   double ratio;
+  int relax, filter; /* RELAXATION == TRUE, FILTER_LOCAL_SOLUTION == TRUE */
+  double omega;      /* RELAXATION_VALUE */
 } NsgsOpts;
 
 /* Returns info: 0 converged, 1 not converged, -20 max iterations (and the
@@ -533,8 +539,14 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
       L.tol = tm.local_tol;
       double lr[3] = {r[3 * c], r[3 * c + 1], r[3 * c + 2]};
       local_solve(&L, lr);
+      if (op->relax) {
+        lr[0] = op->omega * lr[0] + (1.0 - op->omega) * r[3 * c];
+        lr[1] = op->omega * lr[1] + (1.0 - op->omega) * r[3 * c + 1];
+        lr[2] = op->omega * lr[2] + (1.0 - op->omega) * r[3 * c + 2];
+      }
       double d0 = r[3 * c] - lr[0], d1 = r[3 * c + 1] - lr[1], d2 = r[3 * c + 2] - lr[2];
       light += d0 * d0 + d1 * d1 + d2 * d2;
+      if (op->filter && (isnan(L.residual) || isinf(L.residual) || L.residual > 1.0)) continue;
       r[3 * c] = lr[0];
       r[3 * c + 1] = lr[1];
       r[3 * c + 2] = lr[2];
@@ -609,18 +621,19 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
 int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
                      const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *order,
                      int *iters, double *err, double *trace, int trace_cap, int *trace_len) {
-  const NsgsOpts op = {2, 0, 1, 10.0};
+  const NsgsOpts op = {2, 0, 1, 10.0, 0, 0, 1.0};
   return nsgs_impl(nc, rowptr, colidx, blocks, q, mu, r, u, tol, maxiter, order, &op, iters, err, trace, trace_cap,
                    trace_len, NULL);
 }
 
-/* Any error evaluation (0-3), frequency and local tolerance strategy (0-2);
- * opts4 = {err_mode, freq, strategy, 0}, ratio the INTERNAL_ERROR_RATIO. */
+/* Any error evaluation (0-3), frequency, local tolerance strategy (0-2),
+ * relaxation and filter: opts6 = {err_mode, freq, strategy, relax, filter,
+ * 0}, dopts2 = {INTERNAL_ERROR_RATIO, RELAXATION_VALUE}. */
 int oracle_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
                           const double *q, const double *mu, double *r, double *u, double tol, int maxiter,
-                          const int32_t *order, const int32_t *opts4, double ratio, int *iters, double *err,
+                          const int32_t *order, const int32_t *opts6, const double *dopts2, int *iters, double *err,
                           double *trace, int trace_cap, int *trace_len, int *u_written) {
-  const NsgsOpts op = {opts4[0], opts4[1], opts4[2], ratio};
+  const NsgsOpts op = {opts6[0], opts6[1], opts6[2], dopts2[0], opts6[3] == 1, opts6[4] == 1, dopts2[1]};
   return nsgs_impl(nc, rowptr, colidx, blocks, q, mu, r, u, tol, maxiter, order, &op, iters, err, trace, trace_cap,
                    trace_len, u_written);
 }

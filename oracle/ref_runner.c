@@ -128,12 +128,14 @@ int ref_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const do
   return info;
 }
 
-/* ref_fc3d_nsgs with NSGS options beyond the defaults: opts4 = {error
+/* ref_fc3d_nsgs with NSGS options beyond the defaults: opts6 = {error
  * evaluation (iparam 13), its frequency (iparam 14), local tolerance
- * strategy (iparam 2), 0}, ratio the INTERNAL_ERROR_RATIO (dparam 11). */
+ * strategy (iparam 2), relaxation (iparam 10), filter (iparam 16), 0},
+ * dopts2 = {INTERNAL_ERROR_RATIO (dparam 11), RELAXATION_VALUE (dparam 10)}. */
 int ref_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
-                       const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *opts4,
-                       double ratio, int *iters, double *err, double *trace, int trace_cap, int *trace_len) {
+                       const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *opts6,
+                       const double *dopts2, int *iters, double *err, double *trace, int trace_cap,
+                       int *trace_len) {
   NumericsMatrix *M = make_sbm(nc, rowptr, colidx, blocks);
   FrictionContactProblem P;
   memset(&P, 0, sizeof(P));
@@ -145,10 +147,13 @@ int ref_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, con
   SolverOptions *opt = solver_options_create(SICONOS_FRICTION_3D_NSGS);
   opt->iparam[SICONOS_IPARAM_MAX_ITER] = maxiter;
   opt->dparam[SICONOS_DPARAM_TOL] = tol;
-  opt->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = opts4[0];
-  opt->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY] = opts4[1];
-  opt->iparam[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = opts4[2];
-  opt->dparam[SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO] = ratio;
+  opt->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = opts6[0];
+  opt->iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY] = opts6[1];
+  opt->iparam[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = opts6[2];
+  opt->iparam[SICONOS_FRICTION_3D_NSGS_RELAXATION] = opts6[3];
+  opt->iparam[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] = opts6[4];
+  opt->dparam[SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO] = dopts2[0];
+  opt->dparam[SICONOS_FRICTION_3D_NSGS_RELAXATION_VALUE] = dopts2[1];
   Trace t = {trace, trace_cap, 0};
   Callback cb = {&t, trace_cb};
   if (trace) opt->callback = &cb;

@@ -1,9 +1,10 @@
 """The oracle's NSGS loop under the reference's other options, pinned to
 the reference itself (oracle/_ref): the error evaluations FULL (every
 iteration, or every `freq` iterations), LIGHT and ADAPTIVE (which the
-reference's loop has no branch for, so it runs to the budget), and the
-local tolerance strategies ADAPTIVE and ADAPTIVE_N_CONTACT
-(fc3d_nsgs.c:711-900, fc3d_set_internalsolver_tolerance.c:31-63).  Equal bit
+reference's loop has no branch for, so it runs to the budget), the local
+tolerance strategies ADAPTIVE and ADAPTIVE_N_CONTACT, the relaxation of each
+new reaction and the filter of local solutions (fc3d_nsgs.c:711-900,
+fc3d_set_internalsolver_tolerance.c:31-63).  Equal bit
 for bit: info, iterations, final error (infinite where the reference leaves
 it so), the per-iteration error its callback reports, r, and u (left as
 given where the reference never computes it)."""
@@ -21,6 +22,11 @@ COMBOS = {
     "lwff_adaptive_n_contact": dict(err_mode=2, strategy=2),
     "light_adaptive_tol": dict(err_mode=1, strategy=0),
     "full_adaptive_n_contact_ratio3": dict(err_mode=0, strategy=2, ratio=3.0),
+    "relax_0.8": dict(err_mode=2, relax=1, omega=0.8),
+    "relax_1.2_full": dict(err_mode=0, relax=1, omega=1.2),
+    "filter": dict(err_mode=2, filter=1),
+    "filter_light": dict(err_mode=1, filter=1),
+    "relax_filter_adaptive_tol": dict(err_mode=2, relax=1, omega=0.9, filter=1, strategy=0),
 }
 CASES = [c for c in FIXTURE_CASES if "Rover" not in c] + ["fixture_Rover4144"] + LATTICE_CASES
 
