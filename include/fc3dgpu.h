@@ -169,6 +169,13 @@ typedef struct {
   int fp32_only;       /* 1: run FP32 sweeps only, for throughput runs */
   int local_mode32;    /* FP32 one-contact solver: 0 the reference's hybrid
                           (default), 1 damped Newton alone */
+  int relax;           /* FP64 sweeps: each new reaction relaxed,
+                          omega r_new + (1 - omega) r_old (0 = off) */
+  double omega;
+  int filter;          /* FP64 sweeps: keep the old reaction when the local
+                          residual is not finite or above 1 (0 = off); the
+                          FP32 sweeps do neither, so a solve with either
+                          runs FP64 sweeps only */
 } fc3dgpu_params;
 
 typedef struct {

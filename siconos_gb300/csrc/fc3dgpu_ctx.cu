@@ -826,6 +826,9 @@ extern "C" void fc3dgpu_params_default(fc3dgpu_params* p) {
   p->ls_max = 10;
   p->local_mode32 = 0;
   p->fp32_only = 0;
+  p->relax = 0;
+  p->omega = 1.0;
+  p->filter = 0;
 }
 
 extern "C" fc3dgpu_ctx* fc3dgpu_ctx_create(int device) {
@@ -1597,6 +1600,9 @@ static void fill_args(fc3dgpu_ctx* c, fc3dgpu::SweepArgs<Real>& a, const Real* W
   a.nbr = nullptr;
   a.nbr_grid = 0;
   a.local_mode = 0;
+  a.relax = 0;
+  a.filter = 0;
+  a.omega = 1.0;
 }
 
 // Neighbour lists of every block for a sweep over `grid` blocks (one lane
@@ -2051,6 +2057,9 @@ static int solve_impl(fc3dgpu_ctx* c, const fc3dgpu_params* p, fc3dgpu_stats* st
     a.switch_tol = 0.0;
     a.stall_window = 0;
     a.trace_base = sweeps32;
+    a.relax = p->relax;
+    a.omega = p->omega;
+    a.filter = p->filter;
     a.newton_max = p->newton_max;
     a.pli_max = p->pli_max;
     a.ls_max = p->ls_max;

@@ -64,6 +64,10 @@ struct SweepArgs {
   double norm_q;
   int newton_max, pli_max, ls_max;
   int local_mode;  // one-contact solver: 0 the reference's hybrid, 1 damped Newton only (FP32 sweeps)
+  // the reference's optional per-contact steps (FP64 sweeps): relaxation of
+  // each new reaction with omega, and the filter of local solutions
+  int relax, filter;
+  double omega;
   unsigned long long spin_limit;
   unsigned long long* counters;  // optional work counters: Newton its, PLI its, line-search evals, solves, max Newton
   unsigned long long* timeline;  // optional: globaltimer at each colour phase's start and work end, per block

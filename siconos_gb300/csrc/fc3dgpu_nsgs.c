@@ -325,9 +325,8 @@ static int check_options(const SolverOptions *o) {
     fc3dgpu_set_error("iparam[SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] must be 0, 1, 2 or 3");
     return NUMERICS_ERR_INVALID_ARGUMENT;
   }
-  if (shuffle != 0 || ip[SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] > 0 || ip[SICONOS_FRICTION_3D_NSGS_RELAXATION] != 0 ||
-      ip[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] != 0) {
-    fc3dgpu_set_error("GPU NSGS sweeps in colour order: shuffle, freezing, relaxation and filter are not supported");
+  if (shuffle != 0 || ip[SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] > 0) {
+    fc3dgpu_set_error("GPU NSGS sweeps in colour order: shuffle and freezing are not supported");
     return NUMERICS_ERR_NOT_IMPLEMENTED;
   }
   if (o->numberOfInternalSolvers < 1 || !o->internalSolvers || !o->internalSolvers[0]) {
@@ -354,6 +353,12 @@ static void params_from_options(const SolverOptions *o, fc3dgpu_params *p) {
   if (dp[FC3DGPU_DPARAM_LOCAL_TOL32] > 0) p->local_tol32 = dp[FC3DGPU_DPARAM_LOCAL_TOL32];
   if (dp[FC3DGPU_DPARAM_STALL] > 0) p->stall_window = (int)dp[FC3DGPU_DPARAM_STALL];
   p->local_tol = lo->dparam[SICONOS_DPARAM_TOL];
+  /* relaxation and the filter of local solutions (fc3d_nsgs.c:760-830) are
+   * steps of the FP64 sweeps: with either, FP64 sweeps only */
+  p->relax = ip[SICONOS_FRICTION_3D_NSGS_RELAXATION] == 1;
+  p->omega = dp[SICONOS_FRICTION_3D_NSGS_RELAXATION_VALUE];
+  p->filter = ip[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] == 1;
+  if (p->relax || p->filter) p->precision = (p->precision == 2 || p->precision == 3) ? 3 : 1;
   p->newton_max = lo->iparam[SICONOS_IPARAM_MAX_ITER];
   if (lo->iparam[SICONOS_FRICTION_3D_NSN_HYBRID_MAX_ITER] > 0) p->pli_max = lo->iparam[SICONOS_FRICTION_3D_NSN_HYBRID_MAX_ITER];
   if (lo->iparam[SICONOS_FRICTION_3D_NSN_LINESEARCH_MAX_ITER] > 0) p->ls_max = lo->iparam[SICONOS_FRICTION_3D_NSN_LINESEARCH_MAX_ITER];

@@ -185,6 +185,27 @@ __device__ __forceinline__ void load_r3<double>(const double* r, int p, double o
   out[2] = b.x;
 }
 
+// The reference's optional steps after a contact's local solve
+// (fc3d_nsgs.c:760-830): the new reaction relaxed towards the old one,
+// omega rn + (1 - omega) o (performRelaxation_3, :73-78; the light-error
+// term then uses the relaxed reaction), and the filter that keeps the old
+// reaction when the local solver's residual is not finite or above 1
+// (acceptLocalReactionFiltered, :338-389).  keep: the reaction to store.
+template <typename Real>
+__device__ __forceinline__ void nsgs_accept(const SweepArgs<Real>& a, const LocalProblem<Real>& L, const Real o[3],
+                                            Real rn[3], Real keep[3]) {
+  if (a.relax) {
+    const Real w = (Real)a.omega;
+    rn[0] = w * rn[0] + (Real(1.0) - w) * o[0];
+    rn[1] = w * rn[1] + (Real(1.0) - w) * o[1];
+    rn[2] = w * rn[2] + (Real(1.0) - w) * o[2];
+  }
+  const bool discard = a.filter && (isnan(L.residual) || isinf(L.residual) || L.residual > Real(1.0));
+  keep[0] = discard ? o[0] : rn[0];
+  keep[1] = discard ? o[1] : rn[1];
+  keep[2] = discard ? o[2] : rn[2];
+}
+
 template <typename Real, int T>
 __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab, int round, int lane, Real ltol,
                                              double& dr2, double& rr2) {
@@ -266,6 +287,8 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   rn[1] = ro[1];
   rn[2] = ro[2];
   local_solve(L, rn);
+  Real keep[3];
+  nsgs_accept(a, L, ro, rn, keep);
   if (a.counters) {
     // warp-aggregated: one atomic per counter per warp and unit
     unsigned long long c0 = j == 0 ? L.n_newton : 0, c1 = j == 0 ? L.n_pli : 0, c2 = j == 0 ? L.n_ls : 0;
@@ -287,14 +310,14 @@ __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab,
   }
   if (j == 0) {
     Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
-    rp[0] = rn[0];
-    rp[1] = rn[1];
-    rp[2] = rn[2];
+    rp[0] = keep[0];
+    rp[1] = keep[1];
+    rp[2] = keep[2];
     a.rpli[p] = L.rho_pli;
     const double d0 = (double)ro[0] - (double)rn[0], d1 = (double)ro[1] - (double)rn[1],
                  d2 = (double)ro[2] - (double)rn[2];
     dr2 += d0 * d0 + d1 * d1 + d2 * d2;
-    rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+    rr2 += (double)keep[0] * keep[0] + (double)keep[1] * keep[1] + (double)keep[2] * keep[2];
   }
 }
 
@@ -376,14 +399,16 @@ __device__ __forceinline__ void solve_item(const SweepArgs<Real>& a, WorkList<Re
   Real o[3] = {wk.ro[t][0], wk.ro[t][1], wk.ro[t][2]};
   Real rn[3] = {o[0], o[1], o[2]};
   local_solve(L, rn);
+  Real keep[3];
+  nsgs_accept(a, L, o, rn, keep);
   Real* rp = a.r + (size_t)pp * FC3D_RSTRIDE;
-  rp[0] = rn[0];
-  rp[1] = rn[1];
-  rp[2] = rn[2];
+  rp[0] = keep[0];
+  rp[1] = keep[1];
+  rp[2] = keep[2];
   a.rpli[pp] = L.rho_pli;
   const double d0 = (double)o[0] - (double)rn[0], d1 = (double)o[1] - (double)rn[1], d2 = (double)o[2] - (double)rn[2];
   dr2 += d0 * d0 + d1 * d1 + d2 * d2;
-  rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+  rr2 += (double)keep[0] * keep[0] + (double)keep[1] * keep[1] + (double)keep[2] * keep[2];
   if (a.counters) {
     atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
     atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);
@@ -555,14 +580,16 @@ __device__ __forceinline__ void solve_row_s(const SweepArgs<Real>& a, LocalProbl
   L.n_ls = 0;
   Real rn[3] = {o[0], o[1], o[2]};
   local_solve(L, rn);
+  Real keep[3];
+  nsgs_accept(a, L, o, rn, keep);
   Real* rp = a.r + (size_t)pp * FC3D_RSTRIDE;
-  rp[0] = rn[0];
-  rp[1] = rn[1];
-  rp[2] = rn[2];
+  rp[0] = keep[0];
+  rp[1] = keep[1];
+  rp[2] = keep[2];
   a.rpli[pp] = L.rho_pli;
   const double d0 = (double)o[0] - (double)rn[0], d1 = (double)o[1] - (double)rn[1], d2 = (double)o[2] - (double)rn[2];
   dr2 += d0 * d0 + d1 * d1 + d2 * d2;
-  rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+  rr2 += (double)keep[0] * keep[0] + (double)keep[1] * keep[1] + (double)keep[2] * keep[2];
   if (a.counters) {
     atomicAdd(&a.counters[0], (unsigned long long)L.n_newton);
     atomicAdd(&a.counters[1], (unsigned long long)L.n_pli);

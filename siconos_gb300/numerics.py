@@ -141,7 +141,8 @@ class FC3DGPUParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("precision", C.c_int), ("lanes", C.c_int),
                 ("switch_tol", C.c_double), ("stall_window", C.c_int), ("local_tol", C.c_double),
                 ("local_tol32", C.c_double), ("newton_max", C.c_int), ("pli_max", C.c_int), ("ls_max", C.c_int),
-                ("fp32_only", C.c_int), ("local_mode32", C.c_int)]
+                ("fp32_only", C.c_int), ("local_mode32", C.c_int), ("relax", C.c_int), ("omega", C.c_double),
+                ("filter", C.c_int)]
 
 
 class FC3DGPUStats(C.Structure):

@@ -116,12 +116,12 @@ def test_invalid_inputs_rejected(built_lib):
     assert "ERROR_EVALUATION" in sn.last_error()
 
 
-@pytest.mark.parametrize("em,strategy", [(0, 1), (1, 1), (3, 1), (2, 0), (2, 2)])
-def test_other_nsgs_options_pass_the_checks(built_lib, em, strategy):
-    """The reference's other error evaluations and local tolerance
-    strategies are accepted (they run as a host loop of single sweeps); on a
-    machine without a GPU the solve then stops at the device, not at the
-    option checks."""
+@pytest.mark.parametrize("em,strategy,relax,filt", [(0, 1, 0, 0), (1, 1, 0, 0), (3, 1, 0, 0), (2, 0, 0, 0),
+                                                   (2, 2, 0, 0), (2, 1, 1, 0), (2, 1, 0, 1), (0, 0, 1, 1)])
+def test_other_nsgs_options_pass_the_checks(built_lib, em, strategy, relax, filt):
+    """The reference's other error evaluations, local tolerance strategies,
+    relaxation and filter are accepted; on a machine without a GPU the solve
+    then stops at the device, not at the option checks."""
     import siconos_gb300.numerics as sn
     ctx = sn.lib().fc3dgpu_ctx_create(0)
     if ctx:
@@ -130,6 +130,8 @@ def test_other_nsgs_options_pass_the_checks(built_lib, em, strategy):
     o = sn.SolverOptions()
     o.iparam[sn.SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION] = em
     o.iparam[sn.SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = strategy
+    o.iparam[10] = relax  # SICONOS_FRICTION_3D_NSGS_RELAXATION
+    o.iparam[16] = filt  # SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION
     P = _tiny_problem([-1.0, 0.0, 0.0])
     r, u = np.zeros(3), np.zeros(3)
     assert sn.fc3d_driver(P, r, u, o) == sn.NUMERICS_ERR_NOT_IMPLEMENTED

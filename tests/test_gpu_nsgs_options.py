@@ -1,8 +1,10 @@
 """The reference's other NSGS options through the GPU solver: error
-evaluations FULL (every iteration, or every `freq`), LIGHT and ADAPTIVE, and
-the local tolerance strategies ADAPTIVE and ADAPTIVE_N_CONTACT
-(fc3d_nsgs.c:711-900, fc3d_set_internalsolver_tolerance.c:31-63).  They run
-as a host loop of single FP64 sweeps in colour order; against the oracle's
+evaluations FULL (every iteration, or every `freq`), LIGHT and ADAPTIVE, the
+local tolerance strategies ADAPTIVE and ADAPTIVE_N_CONTACT, relaxation and
+the filter of local solutions (fc3d_nsgs.c:711-900,
+fc3d_set_internalsolver_tolerance.c:31-63).  The first two run as a host
+loop of single FP64 sweeps in colour order, relaxation and filter in the
+FP64 sweep kernels; against the oracle's
 loop with the same options in the same order (the oracle itself pinned to
 the reference under these options by test_nsgs_options_oracle.py): the same
 info and iteration count, the reaction bit for bit, the residual (infinite
@@ -24,6 +26,10 @@ COMBOS = {
     "lwff_adaptive_n_contact": dict(err_mode=2, strategy=2),
     "light_adaptive_tol": dict(err_mode=1, strategy=0),
     "full_adaptive_n_contact_ratio3": dict(err_mode=0, strategy=2, ratio=3.0),
+    "relax_0.8": dict(err_mode=2, relax=1, omega=0.8),
+    "relax_1.2_full": dict(err_mode=0, relax=1, omega=1.2),
+    "filter": dict(err_mode=2, filter=1),
+    "relax_filter_adaptive_tol": dict(err_mode=2, relax=1, omega=0.9, filter=1, strategy=0),
 }
 CASES = ["fixture_KaplasTower_i1061_4", "fixture_Confeti_ex13_Fc3D_SBM", "lattice_5x5x6_s1",
          "fixture_BoxesStack1_i100000_32"]
@@ -46,6 +52,9 @@ def test_options_match_coloured_oracle(built_lib, case, combo):
     so.iparam[sn.SICONOS_FRICTION_3D_IPARAM_ERROR_EVALUATION_FREQUENCY] = o["freq"]
     so.iparam[sn.SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = o["strategy"]
     so.dparam[sn.SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO] = o["ratio"]
+    so.iparam[10] = o["relax"]  # SICONOS_FRICTION_3D_NSGS_RELAXATION
+    so.dparam[10] = o["omega"]  # SICONOS_FRICTION_3D_NSGS_RELAXATION_VALUE
+    so.iparam[16] = o["filter"]  # SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION
     r = np.zeros(3 * P.nc)
     u = np.full(3 * P.nc, 7.25)
     info = sn.fc3d_nsgs_gpu(prob, r, u, so)
