@@ -206,6 +206,25 @@ __device__ __forceinline__ void nsgs_accept(const SweepArgs<Real>& a, const Loca
   keep[2] = discard ? o[2] : rn[2];
 }
 
+// A take-off contact (local reaction 0, residual 0) under relaxation: the
+// zero relaxed towards the old reaction as nsgs_accept relaxes any local
+// solution, stored, with its light-error and norm terms.
+template <typename Real>
+__device__ __forceinline__ void takeoff_relaxed(const SweepArgs<Real>& a, const Real o[3], Real* rp, double& dr2,
+                                                double& rr2) {
+  const Real w = (Real)a.omega;
+  Real rn[3];
+  rn[0] = w * Real(0.0) + (Real(1.0) - w) * o[0];
+  rn[1] = w * Real(0.0) + (Real(1.0) - w) * o[1];
+  rn[2] = w * Real(0.0) + (Real(1.0) - w) * o[2];
+  rp[0] = rn[0];
+  rp[1] = rn[1];
+  rp[2] = rn[2];
+  const double d0 = (double)o[0] - (double)rn[0], d1 = (double)o[1] - (double)rn[1], d2 = (double)o[2] - (double)rn[2];
+  dr2 += d0 * d0 + d1 * d1 + d2 * d2;
+  rr2 += (double)rn[0] * rn[0] + (double)rn[1] * rn[1] + (double)rn[2] * rn[2];
+}
+
 template <typename Real, int T>
 __device__ __forceinline__ void process_unit(const SweepArgs<Real>& a, int slab, int round, int lane, Real ltol,
                                              double& dr2, double& rr2) {
@@ -486,10 +505,14 @@ __device__ __forceinline__ void process_range_compact(const SweepArgs<Real>& a, 
           load_r3<Real>(a.r, p, ro[j]);
           if (acc[j][0] > -Eps<Real>::v()) {
             Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
-            rp[0] = 0;
-            rp[1] = 0;
-            rp[2] = 0;
-            dr2 += (double)ro[j][0] * ro[j][0] + (double)ro[j][1] * ro[j][1] + (double)ro[j][2] * ro[j][2];
+            if (a.relax) {
+              takeoff_relaxed(a, ro[j], rp, dr2, rr2);
+            } else {
+              rp[0] = 0;
+              rp[1] = 0;
+              rp[2] = 0;
+              dr2 += (double)ro[j][0] * ro[j][0] + (double)ro[j][1] * ro[j][1] + (double)ro[j][2] * ro[j][2];
+            }
           } else {
             work = true;
           }
@@ -711,10 +734,14 @@ __device__ __forceinline__ bool process_colour_staged(const SweepArgs<Real>& a, 
           }
           if (acc[j][0] > -Eps<Real>::v()) {
             Real* rp = a.r + (size_t)p * FC3D_RSTRIDE;
-            rp[0] = 0;
-            rp[1] = 0;
-            rp[2] = 0;
-            dr2 += (double)ro[j][0] * ro[j][0] + (double)ro[j][1] * ro[j][1] + (double)ro[j][2] * ro[j][2];
+            if (a.relax) {
+              takeoff_relaxed(a, ro[j], rp, dr2, rr2);
+            } else {
+              rp[0] = 0;
+              rp[1] = 0;
+              rp[2] = 0;
+              dr2 += (double)ro[j][0] * ro[j][0] + (double)ro[j][1] * ro[j][1] + (double)ro[j][2] * ro[j][2];
+            }
           } else {
             work = true;
           }
