@@ -90,8 +90,9 @@ int fc3dgpu_driver(FrictionContactProblem *problem, double *reaction, double *ve
  * solver_options_create, when options has none.  fc3dgpu_nsgs also honours
  * the other error evaluations (FULL with its frequency, LIGHT, ADAPTIVE) and
  * the ADAPTIVE / ADAPTIVE_N_CONTACT local tolerances as fc3d_nsgs.c:711-900
- * does, with FP64 sweeps, one device call a sweep; shuffle, freezing,
- * relaxation and filter give NUMERICS_ERR_NOT_IMPLEMENTED. */
+ * does, with FP64 sweeps, one device call a sweep; relaxation and the filter
+ * of local solutions in the FP64 sweeps; shuffle and freezing give
+ * NUMERICS_ERR_NOT_IMPLEMENTED. */
 void fc3dgpu_nsgs_set_default(SolverOptions *options);
 
 /* Stand-alone options (what solver_options_create(SICONOS_FRICTION_3D_NSGS_GPU)
