@@ -259,15 +259,15 @@ def _solve(fn, P: Problem, r0, tol, maxiter, order, trace_cap, is_port):
 # NSGS options beyond the defaults (fc3d_nsgs.c:711-900): error evaluation
 # (0 FULL, 1 LIGHT, 2 LIGHT_WITH_FULL_FINAL, 3 ADAPTIVE), the full-error
 # frequency of FULL, the local tolerance strategy (0 ADAPTIVE, 1 GIVEN_VALUE,
-# 2 ADAPTIVE_N_CONTACT) and its ratio, relaxation (1 = on) with omega, and
-# the filter of local solutions (1 = on).
+# 2 ADAPTIVE_N_CONTACT) and its ratio, relaxation (1 = on) with omega, the
+# filter of local solutions (1 = on) and contact freezing (sweeps skipped).
 DEFAULT_NSGS_OPTIONS = {"err_mode": 2, "freq": 0, "strategy": 1, "ratio": 10.0, "relax": 0, "omega": 1.0,
-                        "filter": 0}
+                        "filter": 0, "freeze": 0}
 
 
 def _opts6(options):
     o = dict(DEFAULT_NSGS_OPTIONS, **(options or {}))
-    return (np.array([o["err_mode"], o["freq"], o["strategy"], o["relax"], o["filter"], 0], np.int32),
+    return (np.array([o["err_mode"], o["freq"], o["strategy"], o["relax"], o["filter"], o["freeze"]], np.int32),
             np.array([o["ratio"], o["omega"]], np.float64))
 
 

@@ -12,8 +12,8 @@
  *                                   tolerance GIVEN_VALUE, ADAPTIVE or
  *                                   ADAPTIVE_N_CONTACT,
  *                                   fc3d_set_internalsolver_tolerance.c:31-63;
- *                                   no shuffle, freezing, relaxation or
- *                                   filter)
+ *                                   relaxation, filter and freezing; no
+ *                                   shuffle)
  *   light error                     fc3d_nsgs.c:80-96
  *   tolerance manager               tolerance_manager.h:63-241
  *   local q                         fc3d_local_problem_tools.c:48-63,
@@ -456,12 +456,17 @@ typedef struct {
  * per contact the relaxation of the new reaction (performRelaxation_3,
  * fc3d_nsgs.c:73-78, before its light-error term) and the filter that keeps
  * the old reaction when the local solver's residual is not finite or above
- * 1 (acceptLocalReactionFiltered, fc3d_nsgs.c:338-389). */
+ * 1 (acceptLocalReactionFiltered, fc3d_nsgs.c:338-389); and contact freezing
+ * (fc3d_nsgs.c:719-810): from the 10th iteration a contact whose light-error
+ * term is small against its reaction, or whose reaction is small against the
+ * last light error's |r|, is skipped for `freeze` sweeps, its stored term
+ * still summed; all counters reset when nc - 1 contacts are frozen. */
 typedef struct {
   int err_mode, freq, strategy;
   double ratio;
   int relax, filter; /* RELAXATION == TRUE, FILTER_LOCAL_SOLUTION == TRUE */
   double omega;      /* RELAXATION_VALUE */
+  int freeze;        /* FREEZING_CONTACT: sweeps a converged contact is skipped */
 } NsgsOpts;
 
 /* Returns info: 0 converged, 1 not converged, -20 max iterations (and the
@@ -516,9 +521,26 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
   L.newton_max = 100;
   L.pli_max = 100;
   L.ls_max = 10;
+  /* freezing state: counters, each contact's last light-error term, and |r|
+   * of the last light error (1e24 before any) */
+  unsigned *frozen = NULL;
+  double *le2 = NULL, norm_r = 1e24;
+  if (op->freeze > 0) {
+    frozen = (unsigned *)calloc((size_t)nc, sizeof(unsigned));
+    le2 = (double *)calloc((size_t)nc, sizeof(double));
+  }
   while (iter < maxiter && hasNotConverged > 0) {
     ++iter;
     double light = 0.0;
+    const double tmp = (double)nc * (double)nc / 1000.;
+    const double crit1 = tolerance * tolerance / tmp, crit2 = norm_r * norm_r / tmp;
+    if (frozen) {
+      unsigned nfrozen = 0;
+      for (int i = 0; i < nc; i++)
+        if (frozen[i] > 0) nfrozen++;
+      if ((size_t)nfrozen >= (size_t)nc - 1)
+        for (int i = 0; i < nc; i++) frozen[i] = 0;
+    }
     /* fc3d_set_internalsolver_tolerance: the local solver's tolerance from
      * the previous iteration's error */
     if (op->strategy == 0)
@@ -527,6 +549,11 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
       tm.local_tol = incr_error / (op->ratio * nc);
     for (int ii = 0; ii < nc; ii++) {
       int c = order ? order[ii] : ii;
+      if (frozen && frozen[c] > 0) {
+        frozen[c] -= 1;
+        light += le2[c];
+        continue;
+      }
       L.M = &blocks[9 * diag[c]];
       L.q[0] = q[3 * c];
       L.q[1] = q[3 * c + 1];
@@ -545,7 +572,13 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
         lr[2] = op->omega * lr[2] + (1.0 - op->omega) * r[3 * c + 2];
       }
       double d0 = r[3 * c] - lr[0], d1 = r[3 * c + 1] - lr[1], d2 = r[3 * c + 2] - lr[2];
-      light += d0 * d0 + d1 * d1 + d2 * d2;
+      const double e2 = d0 * d0 + d1 * d1 + d2 * d2;
+      light += e2;
+      if (frozen) {
+        le2[c] = e2;
+        const double sq = lr[0] * lr[0] + lr[1] * lr[1] + lr[2] * lr[2];
+        if ((e2 <= crit1 * sq || sq <= crit2) && iter >= 10) frozen[c] = (unsigned)op->freeze;
+      }
       if (op->filter && (isnan(L.residual) || isinf(L.residual) || L.residual > 1.0)) continue;
       r[3 * c] = lr[0];
       r[3 * c + 1] = lr[1];
@@ -555,12 +588,14 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
       /* LIGHT: the light error against the working tolerance */
       incr_error = sqrt(light);
       double nr = nrm2(n, r);
+      norm_r = nr;
       if (fabs(nr) > DBL_EPSILON) incr_error /= nr;
       hasNotConverged = incr_error < tolerance ? 0 : 1;
     } else if (op->err_mode == 2) {
       /* LIGHT_WITH_FULL_FINAL: light error, then check_convergence_with_adaptation */
       incr_error = sqrt(light);
       double nr = nrm2(n, r);
+      norm_r = nr;
       if (fabs(nr) > DBL_EPSILON) incr_error /= nr;
       if (incr_error >= tolerance) {
         hasNotConverged = 1;
@@ -614,6 +649,8 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
   free(diag);
   free(rho);
   free(rho_pli);
+  free(frozen);
+  free(le2);
   return info;
 }
 
@@ -621,19 +658,19 @@ static int nsgs_impl(int nc, const int64_t *rowptr, const int64_t *colidx, const
 int oracle_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
                      const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *order,
                      int *iters, double *err, double *trace, int trace_cap, int *trace_len) {
-  const NsgsOpts op = {2, 0, 1, 10.0, 0, 0, 1.0};
+  const NsgsOpts op = {2, 0, 1, 10.0, 0, 0, 1.0, 0};
   return nsgs_impl(nc, rowptr, colidx, blocks, q, mu, r, u, tol, maxiter, order, &op, iters, err, trace, trace_cap,
                    trace_len, NULL);
 }
 
 /* Any error evaluation (0-3), frequency, local tolerance strategy (0-2),
- * relaxation and filter: opts6 = {err_mode, freq, strategy, relax, filter,
- * 0}, dopts2 = {INTERNAL_ERROR_RATIO, RELAXATION_VALUE}. */
+ * relaxation, filter and freezing: opts6 = {err_mode, freq, strategy, relax,
+ * filter, freeze}, dopts2 = {INTERNAL_ERROR_RATIO, RELAXATION_VALUE}. */
 int oracle_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks,
                           const double *q, const double *mu, double *r, double *u, double tol, int maxiter,
                           const int32_t *order, const int32_t *opts6, const double *dopts2, int *iters, double *err,
                           double *trace, int trace_cap, int *trace_len, int *u_written) {
-  const NsgsOpts op = {opts6[0], opts6[1], opts6[2], dopts2[0], opts6[3] == 1, opts6[4] == 1, dopts2[1]};
+  const NsgsOpts op = {opts6[0], opts6[1], opts6[2], dopts2[0], opts6[3] == 1, opts6[4] == 1, dopts2[1], opts6[5]};
   return nsgs_impl(nc, rowptr, colidx, blocks, q, mu, r, u, tol, maxiter, order, &op, iters, err, trace, trace_cap,
                    trace_len, u_written);
 }

@@ -130,7 +130,8 @@ int ref_fc3d_nsgs(int nc, const int64_t *rowptr, const int64_t *colidx, const do
 
 /* ref_fc3d_nsgs with NSGS options beyond the defaults: opts6 = {error
  * evaluation (iparam 13), its frequency (iparam 14), local tolerance
- * strategy (iparam 2), relaxation (iparam 10), filter (iparam 16), 0},
+ * strategy (iparam 2), relaxation (iparam 10), filter (iparam 16), freezing
+ * (iparam 15)},
  * dopts2 = {INTERNAL_ERROR_RATIO (dparam 11), RELAXATION_VALUE (dparam 10)}. */
 int ref_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, const double *blocks, const double *q,
                        const double *mu, double *r, double *u, double tol, int maxiter, const int32_t *opts6,
@@ -152,6 +153,7 @@ int ref_fc3d_nsgs_opts(int nc, const int64_t *rowptr, const int64_t *colidx, con
   opt->iparam[SICONOS_FRICTION_3D_IPARAM_INTERNAL_ERROR_STRATEGY] = opts6[2];
   opt->iparam[SICONOS_FRICTION_3D_NSGS_RELAXATION] = opts6[3];
   opt->iparam[SICONOS_FRICTION_3D_NSGS_FILTER_LOCAL_SOLUTION] = opts6[4];
+  opt->iparam[SICONOS_FRICTION_3D_NSGS_FREEZING_CONTACT] = opts6[5];
   opt->dparam[SICONOS_FRICTION_3D_DPARAM_INTERNAL_ERROR_RATIO] = dopts2[0];
   opt->dparam[SICONOS_FRICTION_3D_NSGS_RELAXATION_VALUE] = dopts2[1];
   Trace t = {trace, trace_cap, 0};

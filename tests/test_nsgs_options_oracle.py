@@ -3,8 +3,8 @@ the reference itself (oracle/_ref): the error evaluations FULL (every
 iteration, or every `freq` iterations), LIGHT and ADAPTIVE (which the
 reference's loop has no branch for, so it runs to the budget), the local
 tolerance strategies ADAPTIVE and ADAPTIVE_N_CONTACT, the relaxation of each
-new reaction and the filter of local solutions (fc3d_nsgs.c:711-900,
-fc3d_set_internalsolver_tolerance.c:31-63).  Equal bit
+new reaction, the filter of local solutions and contact freezing
+(fc3d_nsgs.c:711-900, fc3d_set_internalsolver_tolerance.c:31-63).  Equal bit
 for bit: info, iterations, final error (infinite where the reference leaves
 it so), the per-iteration error its callback reports, r, and u (left as
 given where the reference never computes it)."""
@@ -27,6 +27,10 @@ COMBOS = {
     "filter": dict(err_mode=2, filter=1),
     "filter_light": dict(err_mode=1, filter=1),
     "relax_filter_adaptive_tol": dict(err_mode=2, relax=1, omega=0.9, filter=1, strategy=0),
+    "freeze5": dict(freeze=5),
+    "freeze3_light": dict(freeze=3, err_mode=1),
+    "freeze2_full": dict(freeze=2, err_mode=0),
+    "freeze7_relax": dict(freeze=7, relax=1, omega=0.9),
 }
 CASES = [c for c in FIXTURE_CASES if "Rover" not in c] + ["fixture_Rover4144"] + LATTICE_CASES
 
@@ -43,7 +47,7 @@ def test_options_oracle_equals_reference(case, combo):
     if not _ref_available():
         pytest.skip("oracle/_ref is not built")
     P, _ = load_case(case)
-    o = COMBOS[combo]
+    o = dict(O.DEFAULT_NSGS_OPTIONS, **COMBOS[combo])
     mi = 40 if o["err_mode"] == 3 else 2000
     u0 = np.full(3 * P.nc, 7.25)
     a = O.nsgs_ref(P, tol=1e-8, maxiter=mi, trace_cap=mi, options=o, u0=u0)
